@@ -1,0 +1,465 @@
+/*
+ * pic_oracle.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of the OSIRIS particle-in-cell time step (push, charge-conserving current
+ * deposition, periodic guard fold/replace, Yee field advance, periodic particle wrap, cell
+ * sort, seeded particle load, energy and charge diagnostics).  It is the parity checker for
+ * the CUDA implementation in osiris_gb300/: only tests/, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py load it.  The product never links or calls it.
+ *
+ * The push/deposit part (oracle_push_tmpl.h) is pinned bit for bit against the reference's own
+ * AVX2 kernels compiled from source (oracle/Makefile target `ref`, fixtures in tests/golden/).
+ * The grid phases (oracle_fields_tmpl.h) restate Fortran code that cannot be compiled here (no
+ * Fortran compiler); they are pinned by known-answer tests (periodic plane wave, fold identity,
+ * charge conservation) in tests/test_oracle_*.py.
+ *
+ * Build: see oracle/Makefile (gcc -O2 -ffp-contract=off -fopenmp, portable C99).
+ */
+
+#define _POSIX_C_SOURCE 200809L
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "pic_oracle.h"
+
+/* double-precision B-spline weights (order 1..4) used by the charge deposit diagnostic */
+void ora_spline_weights_f64(int order, double x, double *w)
+{
+    double a = 0.5 - x, b = 0.5 + x;
+    switch (order) {
+    case 1:
+        w[0] = a; w[1] = b;
+        break;
+    case 2:
+        w[0] = 0.5 * a * a; w[1] = fma(a, b, 0.5); w[2] = 0.5 * b * b;
+        break;
+    case 3:
+        w[0] = a * a * a / 6.0;
+        w[1] = fma(0.5, b * b * b, 2.0 / 3.0 - b * b);
+        w[2] = fma(0.5, a * a * a, 2.0 / 3.0 - a * a);
+        w[3] = b * b * b / 6.0;
+        break;
+    default: {
+        double ab = a * b;
+        w[0] = a * a * a * a / 24.0;
+        w[1] = fma(a, fma(a, 1.5 + ab, 1.0), 0.25) / 6.0;
+        w[2] = fma(ab, fma(0.25, ab, 0.5), 11.0 / 24.0);
+        w[3] = fma(b, fma(b, 1.5 + ab, 1.0), 0.25) / 6.0;
+        w[4] = b * b * b * b / 24.0;
+    } break;
+    }
+}
+
+/* ---------------------------------------------------------------- single precision ------ */
+#define R float
+#define SFX f32
+#define VW 8
+#define K(v) ((float)(v))
+#define FMA fmaf
+#define SQRT sqrtf
+
+#define ORD 1
+#define OFS 1
+#include "oracle_push_tmpl.h"
+#undef ORD
+#undef OFS
+#define ORD 2
+#define OFS 2
+#include "oracle_push_tmpl.h"
+#undef ORD
+#undef OFS
+#define ORD 3
+#define OFS 2
+#include "oracle_push_tmpl.h"
+#undef ORD
+#undef OFS
+#define ORD 4
+#define OFS 3
+#include "oracle_push_tmpl.h"
+#undef ORD
+#undef OFS
+#include "oracle_fields_tmpl.h"
+
+#undef R
+#undef SFX
+#undef VW
+#undef K
+#undef FMA
+#undef SQRT
+
+/* ---------------------------------------------------------------- double precision ------ */
+#define R double
+#define SFX f64
+#define VW 4
+#define K(v) ((double)(v))
+#define FMA fma
+#define SQRT sqrt
+
+#define ORD 1
+#define OFS 1
+#include "oracle_push_tmpl.h"
+#undef ORD
+#undef OFS
+#define ORD 2
+#define OFS 2
+#include "oracle_push_tmpl.h"
+#undef ORD
+#undef OFS
+#define ORD 3
+#define OFS 2
+#include "oracle_push_tmpl.h"
+#undef ORD
+#undef OFS
+#define ORD 4
+#define OFS 3
+#include "oracle_push_tmpl.h"
+#undef ORD
+#undef OFS
+#include "oracle_fields_tmpl.h"
+
+#undef R
+#undef SFX
+#undef VW
+#undef K
+#undef FMA
+#undef SQRT
+
+/* ---------------------------------------------------------------- dispatch -------------- */
+
+typedef void (*push_f32_t)(int *, float *, float *, float *, int *, int *, float *, float *,
+                           float *, int *, int *, float *, int *, int *, double *, double *,
+                           double *);
+typedef void (*push_f64_t)(int *, double *, double *, double *, int *, int *, double *,
+                           double *, double *, int *, int *, double *, int *, int *, double *,
+                           double *, double *);
+
+static push_f32_t push_table_f32(int dim, int order)
+{
+    static const push_f32_t t[3][4] = {
+        {ora_vadvance_deposit_1d_s1_f32, ora_vadvance_deposit_1d_s2_f32,
+         ora_vadvance_deposit_1d_s3_f32, ora_vadvance_deposit_1d_s4_f32},
+        {ora_vadvance_deposit_2d_s1_f32, ora_vadvance_deposit_2d_s2_f32,
+         ora_vadvance_deposit_2d_s3_f32, ora_vadvance_deposit_2d_s4_f32},
+        {ora_vadvance_deposit_3d_s1_f32, ora_vadvance_deposit_3d_s2_f32,
+         ora_vadvance_deposit_3d_s3_f32, ora_vadvance_deposit_3d_s4_f32}};
+    if (dim < 1 || dim > 3 || order < 1 || order > 4) return 0;
+    return t[dim - 1][order - 1];
+}
+
+static push_f64_t push_table_f64(int dim, int order)
+{
+    static const push_f64_t t[3][4] = {
+        {ora_vadvance_deposit_1d_s1_f64, ora_vadvance_deposit_1d_s2_f64,
+         ora_vadvance_deposit_1d_s3_f64, ora_vadvance_deposit_1d_s4_f64},
+        {ora_vadvance_deposit_2d_s1_f64, ora_vadvance_deposit_2d_s2_f64,
+         ora_vadvance_deposit_2d_s3_f64, ora_vadvance_deposit_2d_s4_f64},
+        {ora_vadvance_deposit_3d_s1_f64, ora_vadvance_deposit_3d_s2_f64,
+         ora_vadvance_deposit_3d_s3_f64, ora_vadvance_deposit_3d_s4_f64}};
+    if (dim < 1 || dim > 3 || order < 1 || order > 4) return 0;
+    return t[dim - 1][order - 1];
+}
+
+int ora_push_f32(int dim, int order, int *ix, float *x, float *u, float *q, int i0, int i1,
+                 float rqm, float *e, float *b, int *emf_size, int *emf_off, float *j,
+                 int *j_size, int *j_off, double *dx, double dt, double *ene)
+{
+    push_f32_t f = push_table_f32(dim, order);
+    if (!f) return -1;
+    f(ix, x, u, q, &i0, &i1, &rqm, e, b, emf_size, emf_off, j, j_size, j_off, dx, &dt, ene);
+    return 0;
+}
+
+int ora_push_f64(int dim, int order, int *ix, double *x, double *u, double *q, int i0, int i1,
+                 double rqm, double *e, double *b, int *emf_size, int *emf_off, double *j,
+                 int *j_size, int *j_off, double *dx, double dt, double *ene)
+{
+    push_f64_t f = push_table_f64(dim, order);
+    if (!f) return -1;
+    f(ix, x, u, q, &i0, &i1, &rqm, e, b, emf_size, emf_off, j, j_size, j_off, dx, &dt, ene);
+    return 0;
+}
+
+/* ---------------------------------------------------------------- particle phases ------- */
+
+/* periodic single-node wrap of cell indices (source/spec/os-spec-boundary.f03:1280-1290) */
+void ora_wrap(int dim, const int *nx, int np, int *ix)
+{
+    for (int p = 0; p < np; p++)
+        for (int d = 0; d < dim; d++) {
+            int *c = &ix[dim * p + d];
+            if (*c < 1) *c += nx[d];
+            else if (*c > nx[d]) *c -= nx[d];
+        }
+}
+
+/* stable counting sort destination of each particle, by cell with x fastest
+ * (source/spec/os-species.f03:388-505); new_idx is 0-based */
+void ora_sort_index(int dim, const int *nx, int np, const int *ix, int *new_idx)
+{
+    long ncell = 1;
+    for (int d = 0; d < dim; d++) ncell *= nx[d];
+    long *cnt = (long *)calloc((size_t)ncell, sizeof(long));
+    for (int p = 0; p < np; p++) {
+        long c = ix[dim * p] - 1;
+        if (dim > 1) c += (long)nx[0] * (ix[dim * p + 1] - 1);
+        if (dim > 2) c += (long)nx[0] * nx[1] * (ix[dim * p + 2] - 1);
+        new_idx[p] = (int)c;
+        cnt[c]++;
+    }
+    long s = 0;
+    for (long c = 0; c < ncell; c++) {
+        long t = cnt[c];
+        cnt[c] = s;
+        s += t;
+    }
+    for (int p = 0; p < np; p++) new_idx[p] = (int)(cnt[new_idx[p]]++);
+    free(cnt);
+}
+
+/* ---------------------------------------------------------------- seeded load ----------- */
+/*
+ * Mersenne Twister as seeded by OSIRIS (source/random/os-random-mt.f03:84-149): the first
+ * state word is seed XOR 0x80000000 and the read index starts at N (1-based), so the first
+ * draw tempers the last initialisation word before the first regeneration.
+ */
+void ora_mt_seed(ora_mt *r, int seed)
+{
+    r->mt[0] = (uint32_t)seed ^ 0x80000000u;
+    for (int i = 1; i < 624; i++)
+        r->mt[i] = 1812433253u * (r->mt[i - 1] ^ (r->mt[i - 1] >> 30)) + (uint32_t)i;
+    r->mti = 623; /* 0-based position of the next word */
+    r->have_gauss = 0;
+    r->gauss = 0.0;
+}
+
+int32_t ora_mt_int32(ora_mt *r)
+{
+    static const uint32_t mag[2] = {0u, 0x9908b0dfu};
+    if (r->mti >= 624) {
+        int k;
+        uint32_t y;
+        for (k = 0; k < 624 - 397; k++) {
+            y = (r->mt[k] & 0x80000000u) | (r->mt[k + 1] & 0x7fffffffu);
+            r->mt[k] = r->mt[k + 397] ^ (y >> 1) ^ mag[y & 1u];
+        }
+        for (; k < 623; k++) {
+            y = (r->mt[k] & 0x80000000u) | (r->mt[k + 1] & 0x7fffffffu);
+            r->mt[k] = r->mt[k + (397 - 624)] ^ (y >> 1) ^ mag[y & 1u];
+        }
+        y = (r->mt[623] & 0x80000000u) | (r->mt[0] & 0x7fffffffu);
+        r->mt[623] = r->mt[396] ^ (y >> 1) ^ mag[y & 1u];
+        r->mti = 0;
+    }
+    uint32_t y = r->mt[r->mti++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return (int32_t)y;
+}
+
+/* polar Box-Muller gaussian (source/random/os-random-class.f03:348-392) */
+double ora_gaussian(ora_mt *r)
+{
+    if (r->have_gauss) {
+        r->have_gauss = 0;
+        return r->gauss;
+    }
+    double v1, v2, rsq;
+    do {
+        v1 = ((double)ora_mt_int32(r) + 0.5) * (1.0 / 2147483648.0);
+        v2 = ((double)ora_mt_int32(r) + 0.5) * (1.0 / 2147483648.0);
+        rsq = v1 * v1 + v2 * v2;
+    } while (!(rsq < 1.0 && rsq > 0.0));
+    double fac = sqrt(-2.0 * log(rsq) / rsq);
+    r->gauss = v1 * fac;
+    r->have_gauss = 1;
+    return v2 * fac;
+}
+
+/*
+ * Regular-lattice load of one species over the whole periodic box
+ * (source/spec/psource/os-psource-std.f03:759-1120): ppc_d particles per cell along each axis
+ * at in-cell offsets (2i-1-n)/(2n); cells visited with x slowest; charge = den * sign(1/ppc,rqm)
+ * with den = 1 + amp*cos(2 pi kmode x1_phys / L1) (amp = 0 gives a uniform plasma); momenta
+ * uth*gaussian per component followed by the relativistic fluid boost ufl
+ * (source/spec/os-spec-udist.f03:452-850, uniform ufl branch).  Returns the particle count.
+ */
+#define LOAD_BODY(R)                                                                          \
+    int ppc = 1;                                                                              \
+    for (int d = 0; d < dim; d++) ppc *= ppc_d[d];                                             \
+    R pvol = (R)(rqm < 0 ? -1.0 : 1.0) * ((R)1.0 / (R)ppc);                                   \
+    double pos[3][64];                                                                        \
+    for (int d = 0; d < dim; d++) {                                                            \
+        R half = (R)0.5 / (R)ppc_d[d];                                                        \
+        for (int i = 1; i <= ppc_d[d]; i++) pos[d][i - 1] = (double)((R)(2 * i - 1 - ppc_d[d]) * half); \
+    }                                                                                         \
+    int n = 0;                                                                                \
+    int c3n = dim > 2 ? nx[2] : 1, c2n = dim > 1 ? nx[1] : 1;                                  \
+    int p3n = dim > 2 ? ppc_d[2] : 1, p2n = dim > 1 ? ppc_d[1] : 1;                            \
+    double L1 = nx[0] * dx[0];                                                                \
+    for (int c1 = 1; c1 <= nx[0]; c1++)                                                       \
+        for (int c2 = 1; c2 <= c2n; c2++)                                                     \
+            for (int c3 = 1; c3 <= c3n; c3++)                                                 \
+                for (int a = 0; a < ppc_d[0]; a++)                                            \
+                    for (int bb = 0; bb < p2n; bb++)                                          \
+                        for (int cc = 0; cc < p3n; cc++) {                                    \
+                            int ci[3] = {c1, c2, c3}, pi[3] = {a, bb, cc};                    \
+                            for (int d = 0; d < dim; d++) {                                    \
+                                x[dim * n + d] = (R)pos[d][pi[d]];                            \
+                                ix[dim * n + d] = ci[d];                                      \
+                            }                                                                 \
+                            double xp = (c1 - 0.5 + pos[0][a]) * dx[0];                       \
+                            R den = (R)(1.0 + amp * cos(2.0 * M_PI * kmode * xp / L1));        \
+                            q[n] = den * pvol;                                                \
+                            n++;                                                              \
+                        }                                                                     \
+    R ufa = (R)1.0 / (sqrtf_or_sqrt((R)1 + (R)ufl[0] * (R)ufl[0] + (R)ufl[1] * (R)ufl[1] +    \
+                                     (R)ufl[2] * (R)ufl[2]) + (R)1);                           \
+    for (int p = 0; p < n; p++) {                                                             \
+        u[3 * p + 0] = (R)((R)uth[0] * ora_gaussian(rng));                                    \
+        u[3 * p + 1] = (R)((R)uth[1] * ora_gaussian(rng));                                    \
+        u[3 * p + 2] = (R)((R)uth[2] * ora_gaussian(rng));                                    \
+        R g = sqrtf_or_sqrt((R)1 + u[3 * p] * u[3 * p] + u[3 * p + 1] * u[3 * p + 1] +         \
+                            u[3 * p + 2] * u[3 * p + 2]);                                     \
+        R bq = ufa * (u[3 * p] * (R)ufl[0] + u[3 * p + 1] * (R)ufl[1] + u[3 * p + 2] * (R)ufl[2]) + g; \
+        u[3 * p + 0] = u[3 * p + 0] + bq * (R)ufl[0];                                         \
+        u[3 * p + 1] = u[3 * p + 1] + bq * (R)ufl[1];                                         \
+        u[3 * p + 2] = u[3 * p + 2] + bq * (R)ufl[2];                                         \
+    }                                                                                         \
+    return n;
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+int ora_load_f32(ora_mt *rng, int dim, const int *nx, const int *ppc_d, const double *dx,
+                 double rqm, const double *uth, const double *ufl, double amp, double kmode,
+                 int *ix, float *x, float *u, float *q)
+{
+#define sqrtf_or_sqrt sqrtf
+    LOAD_BODY(float)
+#undef sqrtf_or_sqrt
+}
+
+int ora_load_f64(ora_mt *rng, int dim, const int *nx, const int *ppc_d, const double *dx,
+                 double rqm, const double *uth, const double *ufl, double amp, double kmode,
+                 int *ix, double *x, double *u, double *q)
+{
+#define sqrtf_or_sqrt sqrt
+    LOAD_BODY(double)
+#undef sqrtf_or_sqrt
+}
+
+/* ---------------------------------------------------------------- divergence ------------ */
+/* div of the staggered E (or J) into div[] (one value per interior point, x fastest)
+ * (source/vdf/os-vdf-math.f90:1013-1073, offset 0), in double */
+#define DIV_BODY(R)                                                                           \
+    int sz0 = nx[0] + gcl[0] + gcu[0];                                                        \
+    int sz1 = dim > 1 ? nx[1] + gcl[1] + gcu[1] : 1;                                          \
+    int n2 = dim > 1 ? nx[1] : 1, n3 = dim > 2 ? nx[2] : 1;                                   \
+    long o = 0;                                                                               \
+    for (int i3 = 1; i3 <= n3; i3++)                                                          \
+        for (int i2 = 1; i2 <= n2; i2++)                                                      \
+            for (int i1 = 1; i1 <= nx[0]; i1++) {                                             \
+                long c = (i1 - 1 + gcl[0]);                                                   \
+                if (dim > 1) c += (long)sz0 * (i2 - 1 + gcl[1]);                              \
+                if (dim > 2) c += (long)sz0 * sz1 * (i3 - 1 + gcl[2]);                        \
+                double v = ((double)f[3 * c] - (double)f[3 * (c - 1)]) / dx[0];                \
+                if (dim > 1) v += ((double)f[3 * c + 1] - (double)f[3 * (c - sz0) + 1]) / dx[1]; \
+                if (dim > 2)                                                                  \
+                    v += ((double)f[3 * c + 2] - (double)f[3 * (c - (long)sz0 * sz1) + 2]) / dx[2]; \
+                div[o++] = v;                                                                 \
+            }
+
+void ora_div_f32(int dim, const int *nx, const int *gcl, const int *gcu, const float *f,
+                 const double *dx, double *div)
+{
+    DIV_BODY(float)
+}
+
+void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const double *f,
+                 const double *dx, double *div)
+{
+    DIV_BODY(double)
+}
+
+/* ---------------------------------------------------------------- full step ------------- */
+/*
+ * One time step in the phase order of iter_sim (source/os-simulation.f03:498-666) for a single
+ * periodic node: E/B guard replace -> per species push+deposit (OpenMP particle split with a
+ * private current grid per thread and an ordered reduction, source/particles/os-particles.f03:
+ * 1416-1443 and source/spec/os-spec-vpush.f03:380-397) -> particle wrap -> optional cell sort ->
+ * current guard fold -> Yee.  ene[s] receives the time-centred kinetic energy sum of species s
+ * (before the rqm*dV normalisation).
+ */
+#define STEP_BODY(R, SFXN)                                                                    \
+    int gsz = 3;                                                                              \
+    for (int d = 0; d < dim; d++) gsz *= nx[d] + gcl[d] + gcu[d];                             \
+    int emf_size[3], emf_off[3];                                                              \
+    for (int d = 0; d < 3; d++) {                                                             \
+        emf_size[d] = d < dim ? nx[d] + gcl[d] + gcu[d] : 1;                                  \
+        emf_off[d] = d < dim ? gcl[d] : 0;                                                    \
+    }                                                                                         \
+    ora_periodic_##SFXN(dim, nx, gcl, gcu, e, 0);                                             \
+    ora_periodic_##SFXN(dim, nx, gcl, gcu, b, 0);                                             \
+    memset(j, 0, sizeof(R) * (size_t)gsz);                                                    \
+    int nt = nthreads < 1 ? 1 : nthreads;                                                     \
+    R *jt = nt > 1 ? (R *)calloc((size_t)gsz * (nt - 1), sizeof(R)) : 0;                     \
+    for (int s = 0; s < nspec; s++) {                                                         \
+        double *et = (double *)calloc((size_t)nt, sizeof(double));                            \
+        int chunk = (np[s] + nt - 1) / nt;                                                    \
+        chunk = ((chunk + 15) / 16) * 16;                                                     \
+        _Pragma("omp parallel for num_threads(nt) schedule(static,1)")                        \
+        for (int t = 0; t < nt; t++) {                                                        \
+            int a = t * chunk + 1, bnd = (t + 1) * chunk < np[s] ? (t + 1) * chunk : np[s];    \
+            R *jj = t == 0 ? j : jt + (size_t)gsz * (t - 1);                                  \
+            if (bnd >= a)                                                                     \
+                ora_push_##SFXN(dim, order, ix[s], x[s], u[s], q[s], a, bnd, rqm[s], e, b,    \
+                                emf_size, emf_off, jj, emf_size, emf_off, (double *)dx, dt,   \
+                                &et[t]);                                                      \
+        }                                                                                     \
+        ene[s] = 0.0;                                                                         \
+        for (int t = 0; t < nt; t++) ene[s] += et[t];                                         \
+        free(et);                                                                             \
+        ora_wrap(dim, nx, np[s], ix[s]);                                                      \
+    }                                                                                         \
+    if (nt > 1) {                                                                             \
+        _Pragma("omp parallel for num_threads(nt) schedule(static)")                          \
+        for (long i = 0; i < gsz; i++)                                                        \
+            for (int t = 1; t < nt; t++) j[i] += jt[(size_t)gsz * (t - 1) + i];                \
+        free(jt);                                                                             \
+    }                                                                                         \
+    ora_periodic_##SFXN(dim, nx, gcl, gcu, j, 1);                                             \
+    ora_yee_advance_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt);                               \
+    return 0;
+
+int ora_step_f32(int dim, int order, const int *nx, const int *gcl, const int *gcu,
+                 const double *dx, double dt, float *e, float *b, float *j, int nspec,
+                 const int *np, int **ix, float **x, float **u, float **q, const float *rqm,
+                 double *ene, int nthreads)
+{
+    STEP_BODY(float, f32)
+}
+
+int ora_step_f64(int dim, int order, const int *nx, const int *gcl, const int *gcu,
+                 const double *dx, double dt, double *e, double *b, double *j, int nspec,
+                 const int *np, int **ix, double **x, double **u, double **q,
+                 const double *rqm, double *ene, int nthreads)
+{
+    STEP_BODY(double, f64)
+}
+
+int ora_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

@@ -1,0 +1,70 @@
+/*
+ * pic_oracle.h -- TEST INFRASTRUCTURE ONLY: declarations of the CPU parity oracle
+ * (pic_oracle.c).  Loaded from Python through ctypes by tests/, __graft_entry__.smoke() and
+ * the CPU-baseline leg of bench.py; never linked by the product library.
+ */
+#ifndef PIC_ORACLE_H
+#define PIC_ORACLE_H
+
+#include <stdint.h>
+
+typedef struct {
+    uint32_t mt[624];
+    int mti;
+    int have_gauss;
+    double gauss;
+} ora_mt;
+
+/* push + deposit with the reference argument conventions (1-based inclusive [i0, i1];
+ * fields include guard cells; emf_off = lower guard-cell count) */
+int ora_push_f32(int dim, int order, int *ix, float *x, float *u, float *q, int i0, int i1,
+                 float rqm, float *e, float *b, int *emf_size, int *emf_off, float *j,
+                 int *j_size, int *j_off, double *dx, double dt, double *ene);
+int ora_push_f64(int dim, int order, int *ix, double *x, double *u, double *q, int i0, int i1,
+                 double rqm, double *e, double *b, int *emf_size, int *emf_off, double *j,
+                 int *j_size, int *j_off, double *dx, double dt, double *ene);
+
+void ora_yee_advance_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *e,
+                         float *b, const float *j, const double *dx, double dt);
+void ora_yee_advance_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *e,
+                         double *b, const double *j, const double *dx, double dt);
+void ora_periodic_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f, int add);
+void ora_periodic_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f, int add);
+void ora_field_energy_f32(int dim, const int *nx, const int *gcl, const int *gcu,
+                          const float *f, const double *dx, double *out);
+void ora_field_energy_f64(int dim, const int *nx, const int *gcl, const int *gcu,
+                          const double *f, const double *dx, double *out);
+void ora_deposit_rho_f32(int dim, int order, const int *nx, const int *gcl, const int *gcu,
+                         double *rho, int np, const int *ix, const float *x, const float *q);
+void ora_deposit_rho_f64(int dim, int order, const int *nx, const int *gcl, const int *gcu,
+                         double *rho, int np, const int *ix, const double *x, const double *q);
+void ora_div_f32(int dim, const int *nx, const int *gcl, const int *gcu, const float *f,
+                 const double *dx, double *div);
+void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const double *f,
+                 const double *dx, double *div);
+void ora_spline_weights_f64(int order, double x, double *w);
+
+void ora_wrap(int dim, const int *nx, int np, int *ix);
+void ora_sort_index(int dim, const int *nx, int np, const int *ix, int *new_idx);
+
+void ora_mt_seed(ora_mt *r, int seed);
+int32_t ora_mt_int32(ora_mt *r);
+double ora_gaussian(ora_mt *r);
+int ora_load_f32(ora_mt *rng, int dim, const int *nx, const int *ppc_d, const double *dx,
+                 double rqm, const double *uth, const double *ufl, double amp, double kmode,
+                 int *ix, float *x, float *u, float *q);
+int ora_load_f64(ora_mt *rng, int dim, const int *nx, const int *ppc_d, const double *dx,
+                 double rqm, const double *uth, const double *ufl, double amp, double kmode,
+                 int *ix, double *x, double *u, double *q);
+
+int ora_step_f32(int dim, int order, const int *nx, const int *gcl, const int *gcu,
+                 const double *dx, double dt, float *e, float *b, float *j, int nspec,
+                 const int *np, int **ix, float **x, float **u, float **q, const float *rqm,
+                 double *ene, int nthreads);
+int ora_step_f64(int dim, int order, const int *nx, const int *gcl, const int *gcu,
+                 const double *dx, double dt, double *e, double *b, double *j, int nspec,
+                 const int *np, int **ix, double **x, double **u, double **q,
+                 const double *rqm, double *ene, int nthreads);
+int ora_max_threads(void);
+
+#endif

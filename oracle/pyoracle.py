@@ -1,0 +1,285 @@
+"""ctypes front end of the CPU parity oracle -- TEST INFRASTRUCTURE ONLY.
+
+Loads ``oracle/liboracle.so`` (the plain-C restatement, pic_oracle.c) and, where it was built,
+``oracle/_ref/libref_{f32,f64}.so`` (the reference's own AVX2 kernels compiled from source;
+x86_64 only).  Arrays follow the reference memory layout:
+
+* particles: ``ix`` int32 (N, dim), ``x`` (N, dim), ``u`` (N, 3), ``q`` (N,) -- the C-order
+  view of the Fortran arrays ``ix(dim, N)``, ``x(dim, N)``, ``p(3, N)``, ``q(N)``;
+* grids: (size_z, size_y, size_x, 3) -- the C-order view of ``f(3, size_x, size_y, size_z)``
+  with ``size = nx + gcl + gcu`` guard cells (source/vdf/os-vdf-define.f03:35-116).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import platform
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+REFERENCE_SRC = "/root/reference"
+
+# guard cells required by each interpolation order (source/particles/os-particles.f03:321-360)
+GUARD = {1: (1, 2), 2: (2, 3), 3: (3, 4), 4: (4, 5)}
+
+_lib = None
+_ref = {}
+
+
+def build(with_ref: bool = True) -> None:
+    """Compile the oracle (and, on x86_64 with the reference sources present, oracle/_ref)."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    if with_ref and platform.machine() in ("x86_64", "AMD64") and os.path.isdir(REFERENCE_SRC):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "OSIRIS_REF=" + REFERENCE_SRC],
+                       check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build(with_ref=False)
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+def ref_lib(prec: str):
+    """The reference's compiled AVX2 kernels, or None where they could not be built."""
+    if prec not in _ref:
+        path = os.path.join(REF_DIR, f"libref_{prec}.so")
+        _ref[prec] = C.CDLL(path) if os.path.exists(path) else None
+    return _ref[prec]
+
+
+P = C.c_void_p
+I = C.c_int
+D = C.c_double
+
+
+def _declare(L):
+    L.ora_push_f32.argtypes = [I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P, P, D, P]
+    L.ora_push_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, P]
+    for s in ("f32", "f64"):
+        getattr(L, f"ora_yee_advance_{s}").argtypes = [I, P, P, P, P, P, P, P, D]
+        getattr(L, f"ora_periodic_{s}").argtypes = [I, P, P, P, P, I]
+        getattr(L, f"ora_field_energy_{s}").argtypes = [I, P, P, P, P, P, P]
+        getattr(L, f"ora_deposit_rho_{s}").argtypes = [I, I, P, P, P, P, I, P, P, P]
+        getattr(L, f"ora_div_{s}").argtypes = [I, P, P, P, P, P, P]
+        getattr(L, f"ora_load_{s}").argtypes = [P, I, P, P, P, D, P, P, D, D, P, P, P, P]
+        getattr(L, f"ora_step_{s}").argtypes = [I, I, P, P, P, P, D, P, P, P, I, P, P, P, P, P,
+                                                P, P, I]
+    L.ora_wrap.argtypes = [I, P, I, P]
+    L.ora_sort_index.argtypes = [I, P, I, P, P]
+    L.ora_mt_seed.argtypes = [P, I]
+    L.ora_mt_int32.argtypes = [P]
+    L.ora_mt_int32.restype = C.c_int32
+    L.ora_gaussian.argtypes = [P]
+    L.ora_gaussian.restype = D
+    L.ora_load_f32.restype = I
+    L.ora_load_f64.restype = I
+    L.ora_max_threads.restype = I
+
+
+def _p(a):
+    return a.ctypes.data_as(P) if a is not None else None
+
+
+def _i32(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.int32))
+
+
+def _f64(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float64))
+
+
+def dtype_of(prec: str):
+    return np.float32 if prec == "f32" else np.float64
+
+
+# ------------------------------------------------------------------------------ grids
+
+class Grid:
+    """Periodic box with the guard cells the interpolation order needs."""
+
+    def __init__(self, nx, order, dx):
+        self.dim = len(nx)
+        self.nx = list(nx)
+        self.order = order
+        gl, gu = GUARD[order]
+        self.gcl = [gl] * self.dim
+        self.gcu = [gu] * self.dim
+        self.size = [n + gl + gu for n in self.nx]
+        self.dx = list(dx)
+
+    @property
+    def shape(self):
+        return tuple(reversed(self.size)) + (3,)
+
+    def zeros(self, prec):
+        return np.zeros(self.shape, dtype=dtype_of(prec))
+
+    def interior(self, f):
+        """View of the interior points 1..nx of a grid array."""
+        sl = tuple(slice(gl, gl + n) for gl, n in zip(reversed(self.gcl), reversed(self.nx)))
+        return f[sl]
+
+    def args(self):
+        return _i32(self.nx), _i32(self.gcl), _i32(self.gcu)
+
+
+# ------------------------------------------------------------------------------ push
+
+def push(prec, dim, order, ix, x, u, q, i0, i1, rqm, e, b, j, emf_size, emf_off, dx, dt,
+         impl="oracle"):
+    """One vadvance_deposit call; arrays are updated in place; returns the energy sum."""
+    ene = np.zeros(1, dtype=np.float64)
+    es, eo = _i32(emf_size), _i32(emf_off)
+    dxa = _f64(list(dx) + [0.0] * (3 - len(dx)))
+    if impl == "oracle":
+        f = getattr(lib(), f"ora_push_{prec}")
+        rc = f(dim, order, _p(ix), _p(x), _p(u), _p(q), int(i0), int(i1), rqm, _p(e), _p(b),
+               _p(es), _p(eo), _p(j), _p(es), _p(eo), _p(dxa), float(dt), _p(ene))
+        if rc != 0:
+            raise ValueError("bad dim/order")
+    else:
+        L = ref_lib(prec)
+        if L is None:
+            raise RuntimeError("reference kernels not built (oracle/_ref)")
+        name = {1: "1d", 2: "2d", 3: "3d"}[dim]
+        f = getattr(L, f"vadvance_deposit_{name}_s{order}_")
+        ctype = C.c_float if prec == "f32" else C.c_double
+        a0, a1, rq, dtv = C.c_int(int(i0)), C.c_int(int(i1)), ctype(rqm), C.c_double(dt)
+        f(_p(ix), _p(x), _p(u), _p(q), C.byref(a0), C.byref(a1), C.byref(rq), _p(e), _p(b),
+          _p(es), _p(eo), _p(j), _p(es), _p(eo), _p(dxa), C.byref(dtv), _p(ene))
+    return float(ene[0])
+
+
+# ------------------------------------------------------------------------------ grid phases
+
+def yee_advance(g: Grid, prec, e, b, j, dt):
+    nx, gl, gu = g.args()
+    getattr(lib(), f"ora_yee_advance_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), _p(e), _p(b),
+                                               _p(j), _p(_f64(g.dx + [0.0] * 3)), float(dt))
+
+
+def periodic(g: Grid, prec, f, add):
+    nx, gl, gu = g.args()
+    getattr(lib(), f"ora_periodic_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), _p(f), int(add))
+
+
+def field_energy(g: Grid, prec, f):
+    nx, gl, gu = g.args()
+    out = np.zeros(3)
+    getattr(lib(), f"ora_field_energy_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), _p(f),
+                                                _p(_f64(g.dx + [0.0] * 3)), _p(out))
+    return out
+
+
+def deposit_rho(g: Grid, prec, ix, x, q):
+    nx, gl, gu = g.args()
+    rho = np.zeros(g.shape, dtype=np.float64)
+    getattr(lib(), f"ora_deposit_rho_{prec}")(g.dim, g.order, _p(nx), _p(gl), _p(gu), _p(rho),
+                                               len(q), _p(ix), _p(x), _p(q))
+    return rho
+
+
+def div(g: Grid, prec, f):
+    nx, gl, gu = g.args()
+    out = np.zeros(tuple(reversed(g.nx)), dtype=np.float64)
+    getattr(lib(), f"ora_div_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), _p(f),
+                                       _p(_f64(g.dx + [0.0] * 3)), _p(out))
+    return out
+
+
+def wrap(g: Grid, ix):
+    lib().ora_wrap(g.dim, _p(_i32(g.nx)), ix.shape[0], _p(ix))
+
+
+def sort_index(g: Grid, ix):
+    idx = np.zeros(ix.shape[0], dtype=np.int32)
+    lib().ora_sort_index(g.dim, _p(_i32(g.nx)), ix.shape[0], _p(ix), _p(idx))
+    return idx
+
+
+# ------------------------------------------------------------------------------ RNG / load
+
+class MT(C.Structure):
+    _fields_ = [("mt", C.c_uint32 * 624), ("mti", C.c_int), ("have_gauss", C.c_int),
+                ("gauss", C.c_double)]
+
+
+def mt_new(seed: int) -> MT:
+    r = MT()
+    lib().ora_mt_seed(C.byref(r), int(seed))
+    return r
+
+
+def mt_int32(r: MT) -> int:
+    return lib().ora_mt_int32(C.byref(r))
+
+
+def gaussian(r: MT) -> float:
+    return lib().ora_gaussian(C.byref(r))
+
+
+def load(rng: MT, prec, dim, nx, ppc, dx, rqm, uth, ufl, amp=0.0, kmode=1.0):
+    """Lattice load of one species (returns ix, x, u, q)."""
+    n = int(np.prod(nx)) * int(np.prod(ppc))
+    dt_ = dtype_of(prec)
+    ix = np.zeros((n, dim), np.int32)
+    x = np.zeros((n, dim), dt_)
+    u = np.zeros((n, 3), dt_)
+    q = np.zeros(n, dt_)
+    got = getattr(lib(), f"ora_load_{prec}")(C.byref(rng), dim, _p(_i32(nx)), _p(_i32(ppc)),
+                                              _p(_f64(list(dx) + [0.0] * 3)), float(rqm),
+                                              _p(_f64(uth)), _p(_f64(ufl)), float(amp),
+                                              float(kmode), _p(ix), _p(x), _p(u), _p(q))
+    assert got == n
+    return ix, x, u, q
+
+
+# ------------------------------------------------------------------------------ full step
+
+def step(g: Grid, prec, e, b, j, species, dt, nthreads=1):
+    """One full periodic time step; species = list of dicts with ix, x, u, q, rqm.
+    Returns the per-species time-centred energy sums."""
+    nx, gl, gu = g.args()
+    ns = len(species)
+    np_ = _i32([len(s["q"]) for s in species])
+    PA = P * ns
+    ixs = PA(*[_p(s["ix"]) for s in species])
+    xs = PA(*[_p(s["x"]) for s in species])
+    us = PA(*[_p(s["u"]) for s in species])
+    qs = PA(*[_p(s["q"]) for s in species])
+    rqm = np.asarray([s["rqm"] for s in species], dtype=dtype_of(prec))
+    ene = np.zeros(ns)
+    getattr(lib(), f"ora_step_{prec}")(g.dim, g.order, _p(nx), _p(gl), _p(gu),
+                                        _p(_f64(g.dx + [0.0] * 3)), float(dt), _p(e), _p(b),
+                                        _p(j), ns, _p(np_), ixs, xs, us, qs, _p(rqm),
+                                        _p(ene), int(nthreads))
+    return ene
+
+
+def max_threads() -> int:
+    return lib().ora_max_threads()
+
+
+def aligned(shape, dtype, align=64):
+    """Zeroed array whose data pointer is `align`-byte aligned (the reference kernels use
+    aligned 256-bit loads)."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape)) * dtype.itemsize
+    buf = np.zeros(n + align, dtype=np.uint8)
+    off = (-buf.ctypes.data) % align
+    return buf[off:off + n].view(dtype).reshape(shape)
+
+
+def aligned_copy(a, align=64):
+    out = aligned(a.shape, a.dtype, align)
+    out[...] = a
+    return out
