@@ -1,0 +1,362 @@
+"""Benchmark of the OSIRIS PIC time step on GB300: particle-steps/s of the 2D two-stream
+workload (512 x 512 cells, two electron species x 32 particles per cell drifting at +-0.2 c,
+uth = 0.01 c, 1e-3 density perturbation, quadratic splines, dx = 0.05, dt = 0.035), mixed
+precision (FP32 particles and fields) on the tiled engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
+
+One step = one full time step (guard replace, push + deposit + tile migration of both species,
+current fold, Yee B/2-E-B/2), replayed from a CUDA graph.  Particle data (16.8 M particles,
+537 MB per buffer) is far larger than L2, so no flush is needed between steps.
+
+JSON line keys beyond the base contract:
+  roofline      the push kernel (dominant): algorithmic bytes per launch / its CUDA-event time
+  cpu_baseline  the CPU oracle port on this host's cores, on a bounded sample of the workload
+  e2e           the same metric through the reference-facing host-array C ABI
+                (osg_vadvance_deposit_f32 per species, osg_periodic, osg_yee_advance) on pinned
+                host buffers, every copy inside the timed region
+  fp64_plain    the plain FP64 engine on the same workload (the "plain FP64 GPU form")
+--impl reference times the CPU oracle port (the reference's CPU path restated; the
+reference's own AVX2 kernels do not build on this Arm host) with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(workload="2D two-stream 512x512, 2 species x 32 ppc, quadratic, FP32 mixed",
+                nx=[512, 512], ppc=[8, 4], dx=[0.05, 0.05], dt=0.035, uth=0.01, ufl=0.2,
+                amp=1e-3, order=2, seed=2)
+METRIC = "particle-steps/s"
+# algorithmic bytes (FP32 2D): particle read 32 B + write 28 B; per cell E,B gather 24 B + J 12 B
+BYTES_PER_PARTICLE = 60
+BYTES_PER_CELL_PUSH = 36
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per push launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "push_tiled_c2.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.device)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_species(osg, prec):
+    w = WORKLOAD
+    r = osg.Rng(w["seed"])
+    return [osg.load_lattice(r, prec, w["nx"], w["ppc"], w["dx"], -1.0, [w["uth"]] * 3,
+                             [s * w["ufl"], 0.0, 0.0], w["amp"], 1.0) for s in (1.0, -1.0)]
+
+
+def cpu_oracle_rate(target_s, nthreads, steps=None):
+    """CPU oracle (port) particle-steps/s on a square sub-box of the workload (same density,
+    parameters and phases), sized so the timed part takes about target_s seconds."""
+    from oracle import pyoracle as po
+    po.build(with_ref=False)
+    w = WORKLOAD
+
+    def setup(n):
+        r = po.mt_new(w["seed"])
+        sp = []
+        for s in (1.0, -1.0):
+            ix, x, u, q = po.load(r, "f32", 2, [n, n], w["ppc"], w["dx"], -1.0, [w["uth"]] * 3,
+                                  [s * w["ufl"], 0.0, 0.0], w["amp"], 1.0)
+            sp.append(dict(ix=ix, x=x, u=u, q=q, rqm=-1.0))
+        g = po.Grid([n, n], w["order"], w["dx"])
+        return g, sp, g.zeros("f32"), g.zeros("f32"), g.zeros("f32")
+
+    g, sp, e, b, j = setup(64)
+    t = time.perf_counter()
+    po.step(g, "f32", e, b, j, sp, w["dt"], nthreads=nthreads, fast=True)
+    rate = 2 * 64 * 64 * 32 / (time.perf_counter() - t)
+    nstep = steps or 3
+    n = int(np.sqrt(rate * target_s / nstep / 64))
+    n = max(32, min(512, n // 16 * 16))
+    g, sp, e, b, j = setup(n)
+    npart = sum(len(s["q"]) for s in sp)
+    po.step(g, "f32", e, b, j, sp, w["dt"], nthreads=nthreads, fast=True)
+    t = time.perf_counter()
+    for _ in range(nstep):
+        po.step(g, "f32", e, b, j, sp, w["dt"], nthreads=nthreads, fast=True)
+    el = time.perf_counter() - t
+    return npart * nstep / el, f"{n}x{n} cells ({npart} particles), {nstep} full steps", el
+
+
+def e2e_host(osg, sp_host, steps):
+    """Drop-in flow on host buffers, as an unchanged OSIRIS host would drive the library: field
+    guard replace, per species osg_vadvance_deposit_f32 and the periodic particle boundary,
+    current fold and Yee through the host-array C ABI (all copies in the timed part)."""
+    w = WORKLOAD
+    nx, order = w["nx"], w["order"]
+    gl, gu = osg.GUARD[order]
+    size = [n + gl + gu for n in nx]
+    shape = tuple(reversed(size)) + (3,)
+    e = osg.pinned_empty(shape, np.float32)
+    b = osg.pinned_empty(shape, np.float32)
+    j = osg.pinned_empty(shape, np.float32)
+    e[...] = 0
+    b[...] = 0
+    pin = []
+    for ix, x, u, q in sp_host:
+        arrs = []
+        for a in (ix, x, u, q):
+            p = osg.pinned_empty(a.shape, a.dtype)
+            p[...] = a
+            arrs.append(p)
+        pin.append(arrs)
+    npart = sum(len(s[3]) for s in sp_host)
+    gbytes = int(np.prod(shape)) * 4
+
+    def one_step():
+        osg.periodic(2, nx, [gl] * 2, [gu] * 2, e, 0)
+        osg.periodic(2, nx, [gl] * 2, [gu] * 2, b, 0)
+        j[...] = 0
+        for ix, x, u, q in pin:
+            osg.vadvance_deposit(2, order, ix, x, u, q, 1, len(q), -1.0, e, b, size, [gl] * 2, j,
+                                 size, [gl] * 2, w["dx"], w["dt"])
+            osg.particle_wrap(nx, ix)
+        osg.periodic(2, nx, [gl] * 2, [gu] * 2, j, 1)
+        osg.yee_advance(2, nx, [gl] * 2, [gu] * 2, e, b, j, w["dx"], w["dt"])
+
+    one_step()
+    t = time.perf_counter()
+    for _ in range(steps):
+        one_step()
+    el = time.perf_counter() - t
+    # bytes moved per step (counted from the arrays each call copies)
+    h2d = 2 * gbytes + sum(len(p[3]) * 32 + 3 * gbytes for p in pin) + gbytes + 3 * gbytes
+    d2h = 2 * gbytes + sum(len(p[3]) * 28 + gbytes + 12 for p in pin) + gbytes + 2 * gbytes
+    for arrs in pin:
+        for a in arrs:
+            osg.pinned_free(a)
+    for a in (e, b, j):
+        osg.pinned_free(a)
+    return npart * steps / el, h2d, d2h, steps
+
+
+def run_native(args):
+    rank = _env_int("RANK", 0)
+    world = _env_int("WORLD_SIZE", 1)
+    local = _env_int("LOCAL_RANK", 0)
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+        dist = (torch, tdist)
+    import __graft_entry__ as ge
+    ge.build_native()
+    import osiris_gb300 as osg
+    osg.set_device(local)
+    w = WORKLOAD
+    sp = load_species(osg, 32)
+    npart = sum(len(s[3]) for s in sp)
+    ncell = int(np.prod(w["nx"]))
+    # slabs of 4x the mean tile load: the two-stream instability bunches particles up to
+    # ~2.4x the mean per 8x8 tile around saturation, and the timed region has no re-binning
+    sim = osg.Simulation(w["nx"], w["dx"], w["dt"], order=w["order"], precision=32,
+                         engine=osg.ENGINE_TILED, capacity=4.0)
+    for s in sp:
+        sim.add_species(-1.0, *s)
+    sim.step(args.warmup)
+    if dist:
+        dist[1].barrier()
+    with Clocks(local) as clk:
+        ms = sim.time_steps(args.steps)
+    if dist:
+        t = dist[0].tensor([ms], device="cuda")
+        dist[1].all_reduce(t, op=dist[1].ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * npart * args.steps / (ms / 1e3)
+    prof = sim.profile(5)
+    launches = sim.launches_per_step() * args.steps
+    kin, fld = sim.energy()
+    occupancy = sim.tile_occupancy()
+    sim.close()
+    if rank != 0:
+        if dist:
+            dist[1].destroy_process_group()
+        return
+    peak, peak_kind = peaks()
+    push_bytes = npart * BYTES_PER_PARTICLE + ncell * BYTES_PER_CELL_PUSH
+    achieved = push_bytes / (prof["push"] * 1e-3) / 1e9
+    traffic = profile_traffic()
+    # plain FP64 GPU form on the same workload
+    sp64 = load_species(osg, 64)
+    sim64 = osg.Simulation(w["nx"], w["dx"], w["dt"], order=w["order"], precision=64,
+                           engine=osg.ENGINE_PLAIN, n_sort=25)
+    for s in sp64:
+        sim64.add_species(-1.0, *s)
+    sim64.step(3)
+    n64 = max(10, min(args.steps, 50))
+    ms64 = sim64.time_steps(n64)
+    sim64.close()
+    v64 = npart * n64 / (ms64 / 1e3)
+    # end to end through the host-array C ABI
+    e2e_v, h2d, d2h, e2e_steps = e2e_host(osg, sp, max(3, min(args.steps, 10)))
+    # CPU baseline (oracle port) on rank 0
+    from oracle import pyoracle as po
+    nthr = po.max_threads()
+    cpu_v, cpu_sample, _ = cpu_oracle_rate(15.0, nthr)
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w["workload"], "cells": w["nx"], "particles": npart,
+                   "species": 2, "ppc_per_species": 32, "interpolation": "quadratic",
+                   "dx": w["dx"], "dt": w["dt"], "engine": "tiled", "graph": True,
+                   "l2": "inputs larger than L2 (537 MB particle buffer per step)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "kernel": "k_push_tiled<2,2>", "traffic": traffic,
+                     "algorithmic_bytes_per_launch": push_bytes,
+                     "launch_ms": prof["push"]},
+        "phase_ms": prof,
+        "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": nthr, "kind": "port",
+                         "sample": cpu_sample},
+        "e2e": {"value": e2e_v, "unit": METRIC, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+                "path": "osg_vadvance_deposit_f32 + osg_particle_wrap per species, "
+                        "osg_periodic x3, osg_yee_advance; pinned host buffers"},
+        "fp64_plain": {"value": v64, "unit": METRIC, "steps": n64,
+                       "ratio_mixed_over_fp64": value / world / v64},
+        "gpu_launches": launches,
+        "tile_occupancy_max": occupancy,
+        "clocks": clk.summary(),
+        "energy": {"kinetic": [float(v) for v in kin], "field": [float(v) for v in fld]},
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist[1].destroy_process_group()
+
+
+def run_reference(args):
+    rank = _env_int("RANK", 0)
+    if rank != 0:
+        return
+    from oracle import pyoracle as po
+    po.build(with_ref=False)
+    nthr = po.max_threads()
+    # each step of this arm is a bounded sample: a sub-box of the workload sized so that the
+    # whole --steps run takes about two minutes
+    budget = 120.0
+    v, sample, el = cpu_oracle_rate(budget, nthr, steps=args.steps)
+    ms_step = el / args.steps * 1e3
+    line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": _env_int("WORLD_SIZE", 1),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD["workload"], "sample": sample},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": nthr, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_native(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,190 @@
+/*
+ * osiris_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the OSIRIS particle-in-cell
+ * time step: particle push (Boris), charge-conserving current deposition (orders 1-4), guard
+ * cell fold/replace and the Yee field advance.
+ *
+ * Two layers:
+ *
+ *  1. Drop-in entry points with the reference's arguments and semantics, on HOST arrays in the
+ *     reference memory layout.  They copy to the GPU, run the kernels and copy back, so a
+ *     Fortran build of OSIRIS can call them in place of its SIMD kernels / Yee solver:
+ *       osg_vadvance_deposit_{f32,f64}  replaces FNAME(vadvance_deposit_{1d,2d,3d}_s{1..4})
+ *           source/simd/os-spec-push-avx2.c:255,471,1141 (single),
+ *           source/simd/os-spec-push-avx2d.c:263,481,1127 (double);
+ *           Fortran call sites source/spec/os-spec-vpush.f03:70-95,144-169,294-319.
+ *           The exact reference symbol names (vadvance_deposit_2d_s2_ ...) are exported by the
+ *           shim libraries libosiris_gb300_single.so / libosiris_gb300_double.so
+ *           (include/osiris_gb300_fortran.h).
+ *       osg_yee_advance_{f32,f64}       replaces advance_yee
+ *           source/emf/solver/os-emf-solver-yee.f03:542-568 (dbdt/dedt :102-138,211-251,
+ *           287-326,385-428)
+ *       osg_periodic_{f32,f64}          replaces update_periodic_vdf (single-node periodic,
+ *           p_vdf_add / p_vdf_replace) source/vdf/os-vdf-comm.f90:142-326, 665-722
+ *
+ *  2. A device-resident simulation handle (osg_sim_*): particles, fields and current stay in
+ *     HBM between steps; one call advances N full time steps (phase order of iter_sim,
+ *     source/os-simulation.f03:498-666); host copies happen only when the caller asks for
+ *     state or diagnostics.  Two particle engines:
+ *       OSG_ENGINE_PLAIN  reference particle layout, one thread per particle, global atomics
+ *                         (the "plain" GPU form; used in FP64 and FP32)
+ *       OSG_ENGINE_TILED  particles binned by spatial tile, fields staged in shared memory,
+ *                         shared-memory current accumulation, per-step tile migration (FP32)
+ *
+ * All functions return OSG_OK (0) or a negative OSG_ERR_* code; osg_last_error() gives the
+ * text of the calling thread's last error.  No function exits the process.
+ */
+#ifndef OSIRIS_GB300_H
+#define OSIRIS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OSG_OK 0
+#define OSG_ERR_ARG (-1)      /* invalid argument (dimension, order, sizes, pointers) */
+#define OSG_ERR_CUDA (-2)     /* CUDA runtime error (no device, launch failure, ...) */
+#define OSG_ERR_OVERFLOW (-3) /* a tile ran out of particle slots */
+#define OSG_ERR_RANGE (-4)    /* a particle cell index left the valid range */
+#define OSG_ERR_STATE (-5)    /* call out of sequence (e.g. no species) */
+#define OSG_ERR_NOMEM (-6)    /* device or host allocation failed */
+
+#define OSG_ENGINE_PLAIN 0
+#define OSG_ENGINE_TILED 1
+
+const char *osg_last_error(void);
+int osg_version(void);
+int osg_device_count(void);
+/* select the CUDA device used by the calling thread's subsequent calls */
+int osg_set_device(int device);
+/* page-locked host memory for the host-array entry points (fast copies); NULL on failure */
+void *osg_host_alloc(size_t bytes);
+int osg_host_free(void *p);
+
+/* ---------------------------------------------------------------- drop-in, host arrays --- */
+
+/* Push particles [i0, i1] (1-based, inclusive) of one species and ADD their current into j;
+ * *ene += sum over particles of q * u^2/(gamma+1) at the half step.  ix/x/u/q: Fortran
+ * ix(dim,N), x(dim,N), p(3,N), q(N); efield/bfield/j: f(3, size(1), size(2), size(3)) with
+ * emf_offset / j_offset = number of lower guard cells.  dim 1..3, order 1..4.
+ * Unlike the SIMD kernels, nothing is written past particle i1 (no padding contract). */
+int osg_vadvance_deposit_f32(int dim, int order, int *ix, float *x, float *u, float *q,
+                             int i0, int i1, float rqm, const float *efield,
+                             const float *bfield, const int *emf_size, const int *emf_offset,
+                             float *j, const int *j_size, const int *j_offset,
+                             const double *dx, double dt, double *ene);
+int osg_vadvance_deposit_f64(int dim, int order, int *ix, double *x, double *u, double *q,
+                             int i0, int i1, double rqm, const double *efield,
+                             const double *bfield, const int *emf_size, const int *emf_offset,
+                             double *j, const int *j_size, const int *j_offset,
+                             const double *dx, double dt, double *ene);
+
+/* Same on arrays that already live in device memory, asynchronous on `stream`
+ * (cudaStream_t, NULL = default stream).  d_ene is a device double that is incremented. */
+int osg_vadvance_deposit_dev_f32(int dim, int order, int *ix, float *x, float *u,
+                                 const float *q, long np, float rqm, const float *efield,
+                                 const float *bfield, const int *emf_size,
+                                 const int *emf_offset, float *j, const int *j_size,
+                                 const int *j_offset, const double *dx, double dt,
+                                 double *d_ene, void *stream);
+int osg_vadvance_deposit_dev_f64(int dim, int order, int *ix, double *x, double *u,
+                                 const double *q, long np, double rqm, const double *efield,
+                                 const double *bfield, const int *emf_size,
+                                 const int *emf_offset, double *j, const int *j_size,
+                                 const int *j_offset, const double *dx, double dt,
+                                 double *d_ene, void *stream);
+
+/* Yee advance (B half step, E full step, B half step) on host arrays with guard cells. */
+int osg_yee_advance_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *e,
+                        float *b, const float *j, const double *dx, double dt);
+int osg_yee_advance_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *e,
+                        double *b, const double *j, const double *dx, double dt);
+
+/* Single-node periodic guard update of a 3-component grid: add = 1 folds guard cells into
+ * their periodic image and writes the sum to both (current); add = 0 copies the periodic
+ * image into the guard cells (fields). */
+int osg_periodic_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f, int add);
+int osg_periodic_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f,
+                     int add);
+
+/* Periodic particle boundary of a single node on HOST arrays: cell indices that left
+ * [1, nx] are shifted by +-nx (replaces the periodic branch of phys_boundary_species,
+ * source/spec/os-spec-boundary.f03:1280-1290; host code, no GPU). */
+int osg_particle_wrap(int dim, const int *nx, long np, int *ix);
+
+/* ---------------------------------------------------------------- seeded particle load --- */
+
+/* Regular lattice load of one species over a periodic box, OSIRIS algorithm
+ * (source/spec/psource/os-psource-std.f03:759-1120, source/spec/os-spec-udist.f03:452-850,
+ * Mersenne Twister source/random/os-random-mt.f03:84-149, polar gaussian
+ * source/random/os-random-class.f03:348-392).  The generator state lives in *rng (opaque,
+ * OSG_RNG_BYTES bytes, initialised by osg_rng_seed); successive species share it like the
+ * reference's global generator.  den(x1) = 1 + amp cos(2 pi kmode x1 / L1).
+ * Writes nx.prod * ppc.prod particles; precision 32 or 64 selects float/double x, u, q. */
+#define OSG_RNG_BYTES 2512
+int osg_rng_seed(void *rng, int seed);
+long osg_load_lattice(void *rng, int precision, int dim, const int *nx, const int *ppc,
+                      const double *dx, double rqm, const double *uth, const double *ufl,
+                      double amp, double kmode, int *ix, void *x, void *u, void *q);
+
+/* ---------------------------------------------------------------- device-resident sim --- */
+
+typedef struct osg_sim osg_sim;
+
+typedef struct {
+    int dim;          /* 2 or 3 */
+    int order;        /* interpolation order 1..4 */
+    int precision;    /* 32 (mixed: FP32 particles/fields, FP64 diagnostics) or 64 */
+    int engine;       /* OSG_ENGINE_PLAIN or OSG_ENGINE_TILED (TILED needs precision 32) */
+    int nx[3];        /* cells per axis */
+    double dx[3];     /* cell size */
+    double dt;        /* time step (checked against the Courant limit) */
+    int tile[3];      /* tile shape in cells (TILED; 0 = automatic) */
+    int n_sort;       /* PLAIN: cell sort every n_sort steps (0 = never) */
+    double capacity;  /* TILED: slots per tile as a multiple of the mean load (0 = 3.0) */
+} osg_config;
+
+int osg_sim_create(const osg_config *cfg, osg_sim **out);
+int osg_sim_destroy(osg_sim *s);
+/* Add a species from host arrays (reference layout); x/u/q are float for precision 32 and
+ * double for 64. Returns the species index (>= 0) or an error code. */
+int osg_sim_add_species(osg_sim *s, double rqm, long np, const int *ix, const void *x,
+                        const void *u, const void *q);
+/* Guard-celled host fields (reference layout, precision of the sim); NULL leaves as is. */
+int osg_sim_set_fields(osg_sim *s, const void *e, const void *b);
+int osg_sim_get_fields(osg_sim *s, void *e, void *b, void *j);
+int osg_sim_num_particles(osg_sim *s, int species, long *np);
+/* Copy one species back to host arrays (tile order for the TILED engine). */
+int osg_sim_get_species(osg_sim *s, int species, int *ix, void *x, void *u, void *q);
+/* Advance n full time steps (captured once as a CUDA graph per step shape and replayed).
+ * TILED: afterwards, if any tile slab is more than 70% full, all species are re-binned into
+ * larger slabs (a host round trip) so the following steps cannot overflow. */
+int osg_sim_step(osg_sim *s, int nsteps);
+/* TILED: largest fraction of used particle slots over all tiles and species (0 for PLAIN). */
+int osg_sim_tile_occupancy(osg_sim *s, double *max_frac);
+/* Launch n steps without waiting for them (bench/timing); osg_sim_sync waits and reports
+ * any error raised on the device. */
+int osg_sim_step_async(osg_sim *s, int nsteps);
+int osg_sim_sync(osg_sim *s);
+void *osg_sim_stream(osg_sim *s);
+/* FP64 diagnostics: kinetic[ns] time-centred energy of the last step (rqm * dV applied),
+ * field[6] = 0.5 dV sum of E1..3^2 and B1..3^2. */
+int osg_sim_energy(osg_sim *s, double *kinetic, double *field);
+/* FP64 charge check: max over cells of |div E - rho| (rho of all species, order-matched
+ * shape); the caller compares it with its value at t = 0 to verify conservation. */
+int osg_sim_gauss_residual(osg_sim *s, double *max_abs, double *l2);
+/* Average device time per launch of each phase over the last profiled steps (ms):
+ * [0] push+deposit, [1] current fold, [2] Yee, [3] guard replace, [4] migration/sort. */
+int osg_sim_profile(osg_sim *s, int nsteps, float *ms_phase);
+/* Number of kernel launches one step issues (for launch accounting). */
+int osg_sim_launches_per_step(osg_sim *s);
+/* Run n steps bracketed by CUDA events on the simulation's stream; *ms = device time. */
+int osg_sim_time_steps(osg_sim *s, int nsteps, float *ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

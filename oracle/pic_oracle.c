@@ -406,6 +406,9 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
         emf_size[d] = d < dim ? nx[d] + gcl[d] + gcu[d] : 1;                                  \
         emf_off[d] = d < dim ? gcl[d] : 0;                                                    \
     }                                                                                         \
+    /* the single-precision reference pushes with dt rounded to p_k_part                      \
+       (dtcycle = real(dt, p_k_part), source/spec/os-spec-vpush.f03:365) */                    \
+    const double dtp = sizeof(R) == 4 ? (double)(float)dt : dt;                               \
     ora_periodic_##SFXN(dim, nx, gcl, gcu, e, 0);                                             \
     ora_periodic_##SFXN(dim, nx, gcl, gcu, b, 0);                                             \
     memset(j, 0, sizeof(R) * (size_t)gsz);                                                    \
@@ -421,7 +424,7 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
             R *jj = t == 0 ? j : jt + (size_t)gsz * (t - 1);                                  \
             if (bnd >= a)                                                                     \
                 ora_push_##SFXN(dim, order, ix[s], x[s], u[s], q[s], a, bnd, rqm[s], e, b,    \
-                                emf_size, emf_off, jj, emf_size, emf_off, (double *)dx, dt,   \
+                                emf_size, emf_off, jj, emf_size, emf_off, (double *)dx, dtp,  \
                                 &et[t]);                                                      \
         }                                                                                     \
         ene[s] = 0.0;                                                                         \

@@ -32,7 +32,7 @@ _ref = {}
 
 def build(with_ref: bool = True) -> None:
     """Compile the oracle (and, on x86_64 with the reference sources present, oracle/_ref)."""
-    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so", "liboracle_fast.so"], check=True)
     if with_ref and platform.machine() in ("x86_64", "AMD64") and os.path.isdir(REFERENCE_SRC):
         subprocess.run(["make", "-s", "-C", HERE, "ref", "OSIRIS_REF=" + REFERENCE_SRC],
                        check=True)
@@ -46,6 +46,21 @@ def lib():
         _lib = C.CDLL(LIB_PATH)
         _declare(_lib)
     return _lib
+
+
+_fast = None
+
+
+def fast_lib():
+    """The same oracle compiled with -O3 -ffast-math: the timed CPU baseline only."""
+    global _fast, _lib
+    if _fast is None:
+        path = os.path.join(HERE, "liboracle_fast.so")
+        if not os.path.exists(path):
+            build(with_ref=False)
+        _fast = C.CDLL(path)
+        _declare(_fast)
+    return _fast
 
 
 def ref_lib(prec: str):
@@ -245,9 +260,10 @@ def load(rng: MT, prec, dim, nx, ppc, dx, rqm, uth, ufl, amp=0.0, kmode=1.0):
 
 # ------------------------------------------------------------------------------ full step
 
-def step(g: Grid, prec, e, b, j, species, dt, nthreads=1):
+def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False):
     """One full periodic time step; species = list of dicts with ix, x, u, q, rqm.
-    Returns the per-species time-centred energy sums."""
+    Returns the per-species time-centred energy sums.  fast=True runs the -O3 -ffast-math
+    build (timing only)."""
     nx, gl, gu = g.args()
     ns = len(species)
     np_ = _i32([len(s["q"]) for s in species])
@@ -258,7 +274,7 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1):
     qs = PA(*[_p(s["q"]) for s in species])
     rqm = np.asarray([s["rqm"] for s in species], dtype=dtype_of(prec))
     ene = np.zeros(ns)
-    getattr(lib(), f"ora_step_{prec}")(g.dim, g.order, _p(nx), _p(gl), _p(gu),
+    getattr(fast_lib() if fast else lib(), f"ora_step_{prec}")(g.dim, g.order, _p(nx), _p(gl), _p(gu),
                                         _p(_f64(g.dx + [0.0] * 3)), float(dt), _p(e), _p(b),
                                         _p(j), ns, _p(np_), ixs, xs, us, qs, _p(rqm),
                                         _p(ene), int(nthreads))

@@ -1,0 +1,359 @@
+"""osiris_gb300 -- GB300 (sm_103a) implementation of the OSIRIS particle-in-cell time step.
+
+Python front end of the C ABI in ``include/osiris_gb300.h`` (ctypes over the in-tree
+``libosiris_gb300.so``).  Two layers, mirroring the reference:
+
+* drop-in calls with the reference's arguments on host arrays in the reference layout:
+  :func:`vadvance_deposit` (FNAME(vadvance_deposit_{1d,2d,3d}_sN), source/simd/
+  os-spec-push-avx2{,d}.c), :func:`yee_advance` (advance_yee, source/emf/solver/
+  os-emf-solver-yee.f03:542-568), :func:`periodic` (update_periodic_vdf, source/vdf/
+  os-vdf-comm.f90:142-326);
+* :class:`Simulation`, a device-resident time stepper (phase order of iter_sim,
+  source/os-simulation.f03:498-666) with the plain (reference layout, FP64 or FP32) and the
+  tiled (FP32) particle engines.
+
+Array conventions (C-order views of the Fortran arrays): particles ``ix`` int32 (N, dim),
+``x`` (N, dim), ``u`` (N, 3), ``q`` (N,); grids (size_z, size_y, size_x, 3) with
+``size = nx + gcl + gcu``.  Errors raise :class:`OsirisGB300Error`; there is no CPU fallback:
+if the library is missing or no GPU is present the calls fail.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libosiris_gb300.so")
+
+OSG_OK = 0
+ENGINE_PLAIN = 0
+ENGINE_TILED = 1
+RNG_BYTES = 2512
+
+# guard cells per interpolation order (source/particles/os-particles.f03:321-360)
+GUARD = {1: (1, 2), 2: (2, 3), 3: (3, 4), 4: (4, 5)}
+
+
+class OsirisGB300Error(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"osiris_gb300 error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """The loaded native library (built by ``__graft_entry__.build()`` / osiris_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OsirisGB300Error(-2, f"native library not built: {LIB_PATH}")
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+P, I, L, D, F = C.c_void_p, C.c_int, C.c_long, C.c_double, C.c_float
+
+
+class Config(C.Structure):
+    _fields_ = [("dim", I), ("order", I), ("precision", I), ("engine", I), ("nx", I * 3),
+                ("dx", D * 3), ("dt", D), ("tile", I * 3), ("n_sort", I), ("capacity", D)]
+
+
+def _declare(lb):
+    lb.osg_last_error.restype = C.c_char_p
+    lb.osg_version.restype = I
+    lb.osg_device_count.restype = I
+    lb.osg_host_alloc.argtypes = [C.c_size_t]
+    lb.osg_host_alloc.restype = P
+    lb.osg_host_free.argtypes = [P]
+    lb.osg_vadvance_deposit_f32.argtypes = [I, I, P, P, P, P, I, I, F, P, P, P, P, P, P, P, P, D, P]
+    lb.osg_vadvance_deposit_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, P]
+    for s in ("f32", "f64"):
+        getattr(lb, f"osg_yee_advance_{s}").argtypes = [I, P, P, P, P, P, P, P, D]
+        getattr(lb, f"osg_periodic_{s}").argtypes = [I, P, P, P, P, I]
+    lb.osg_particle_wrap.argtypes = [I, P, L, P]
+    lb.osg_rng_seed.argtypes = [P, I]
+    lb.osg_load_lattice.argtypes = [P, I, I, P, P, P, D, P, P, D, D, P, P, P, P]
+    lb.osg_load_lattice.restype = L
+    lb.osg_sim_create.argtypes = [C.POINTER(Config), C.POINTER(P)]
+    lb.osg_sim_destroy.argtypes = [P]
+    lb.osg_sim_add_species.argtypes = [P, D, L, P, P, P, P]
+    lb.osg_sim_set_fields.argtypes = [P, P, P]
+    lb.osg_sim_get_fields.argtypes = [P, P, P, P]
+    lb.osg_sim_num_particles.argtypes = [P, I, C.POINTER(L)]
+    lb.osg_sim_get_species.argtypes = [P, I, P, P, P, P]
+    lb.osg_sim_step.argtypes = [P, I]
+    lb.osg_sim_step_async.argtypes = [P, I]
+    lb.osg_sim_sync.argtypes = [P]
+    lb.osg_sim_stream.argtypes = [P]
+    lb.osg_sim_stream.restype = P
+    lb.osg_sim_energy.argtypes = [P, P, P]
+    lb.osg_sim_gauss_residual.argtypes = [P, C.POINTER(D), C.POINTER(D)]
+    lb.osg_sim_profile.argtypes = [P, I, P]
+    lb.osg_sim_launches_per_step.argtypes = [P]
+    lb.osg_sim_time_steps.argtypes = [P, I, C.POINTER(F)]
+    lb.osg_sim_tile_occupancy.argtypes = [P, C.POINTER(D)]
+    lb.osg_set_device.argtypes = [I]
+
+
+def _check(rc):
+    if rc < 0:
+        raise OsirisGB300Error(rc, lib().osg_last_error().decode(errors="replace"))
+    return rc
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(P)
+
+
+def _i32(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.int32))
+
+
+def _f64(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float64))
+
+
+def _prec(a):
+    if a.dtype == np.float32:
+        return "f32"
+    if a.dtype == np.float64:
+        return "f64"
+    raise TypeError("real arrays must be float32 or float64")
+
+
+def _need(a, dtype, name):
+    if not (isinstance(a, np.ndarray) and a.dtype == dtype and a.flags.c_contiguous
+            and a.flags.writeable):
+        raise TypeError(f"{name} must be a writable C-contiguous {np.dtype(dtype)} array")
+
+
+# ------------------------------------------------------------------------ drop-in calls
+
+def vadvance_deposit(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_size,
+                     emf_offset, j, j_size, j_offset, dx, dt):
+    """Push particles i0..i1 (1-based, inclusive) and add their current into ``j``.
+
+    Same arguments and in-place semantics as FNAME(vadvance_deposit_<dim>d_s<order>);
+    returns the time-centred energy sum the reference adds into ``*ene``."""
+    prec = _prec(x)
+    dt_ = np.float32 if prec == "f32" else np.float64
+    _need(ix, np.int32, "ix")
+    for a, n in ((x, "x"), (u, "u"), (q, "q"), (j, "j")):
+        _need(a, dt_, n)
+    for a, n in ((efield, "efield"), (bfield, "bfield")):
+        if a.dtype != dt_ or not a.flags.c_contiguous:
+            raise TypeError(f"{n} must be C-contiguous {np.dtype(dt_)}")
+    ene = np.zeros(1)
+    f = getattr(lib(), f"osg_vadvance_deposit_{prec}")
+    _check(f(dim, order, _p(ix), _p(x), _p(u), _p(q), int(i0), int(i1), rqm, _p(efield),
+             _p(bfield), _p(_i32(emf_size)), _p(_i32(emf_offset)), _p(j), _p(_i32(j_size)),
+             _p(_i32(j_offset)), _p(_f64(list(dx) + [0.0] * (3 - len(dx)))), float(dt),
+             _p(ene)))
+    return float(ene[0])
+
+
+def yee_advance(dim, nx, gcl, gcu, e, b, j, dx, dt):
+    """B half step, E full step, B half step on guard-celled host grids (in place)."""
+    prec = _prec(e)
+    _check(getattr(lib(), f"osg_yee_advance_{prec}")(
+        dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)), _p(e), _p(b), _p(j),
+        _p(_f64(list(dx) + [0.0] * 3)), float(dt)))
+
+
+def periodic(dim, nx, gcl, gcu, f, add):
+    """Single-node periodic guard update (add=1: fold, add=0: replace), in place."""
+    prec = _prec(f)
+    _check(getattr(lib(), f"osg_periodic_{prec}")(dim, _p(_i32(nx)), _p(_i32(gcl)),
+                                                   _p(_i32(gcu)), _p(f), int(add)))
+
+
+def particle_wrap(nx, ix):
+    """Periodic particle boundary on host cell indices (in place)."""
+    _need(ix, np.int32, "ix")
+    _check(lib().osg_particle_wrap(len(nx), _p(_i32(nx)), ix.shape[0], _p(ix)))
+
+
+def pinned_empty(shape, dtype):
+    """numpy array on page-locked host memory (freed when the array is collected)."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape)) * dtype.itemsize
+    ptr = lib().osg_host_alloc(max(n, 1))
+    if not ptr:
+        raise OsirisGB300Error(-6, lib().osg_last_error().decode(errors="replace"))
+    buf = (C.c_char * max(n, 1)).from_address(ptr)
+    arr = np.frombuffer(buf, dtype=np.uint8, count=n).view(dtype).reshape(shape)
+    _Pinned.keep[id(arr)] = ptr
+    return arr
+
+
+class _Pinned:
+    keep = {}
+
+
+def pinned_free(arr):
+    ptr = _Pinned.keep.pop(id(arr), None)
+    if ptr:
+        lib().osg_host_free(ptr)
+
+
+# ------------------------------------------------------------------------ seeded load
+
+class Rng:
+    """OSIRIS-seeded Mersenne Twister state shared by successive species loads."""
+
+    def __init__(self, seed):
+        self.buf = np.zeros(RNG_BYTES, dtype=np.uint8)
+        _check(lib().osg_rng_seed(_p(self.buf), int(seed)))
+
+
+def load_lattice(rng, precision, nx, ppc, dx, rqm, uth, ufl, amp=0.0, kmode=1.0):
+    """Regular-lattice species over the periodic box; returns (ix, x, u, q)."""
+    dim = len(nx)
+    n = int(np.prod(nx)) * int(np.prod(ppc))
+    dt_ = np.float32 if precision == 32 else np.float64
+    ix = np.zeros((n, dim), np.int32)
+    x = np.zeros((n, dim), dt_)
+    u = np.zeros((n, 3), dt_)
+    q = np.zeros(n, dt_)
+    got = lib().osg_load_lattice(_p(rng.buf), precision, dim, _p(_i32(nx)), _p(_i32(ppc)),
+                                 _p(_f64(list(dx) + [0.0] * 3)), float(rqm), _p(_f64(uth)),
+                                 _p(_f64(ufl)), float(amp), float(kmode), _p(ix), _p(x), _p(u),
+                                 _p(q))
+    _check(got)
+    assert got == n
+    return ix, x, u, q
+
+
+# ------------------------------------------------------------------------ simulation
+
+class Simulation:
+    """Device-resident periodic PIC simulation (fields + species stay on the GPU)."""
+
+    def __init__(self, nx, dx, dt, order=2, precision=32, engine=ENGINE_TILED, tile=None,
+                 n_sort=0, capacity=0.0):
+        self.dim = len(nx)
+        self.nx = list(nx)
+        self.order = order
+        self.precision = precision
+        self.dtype = np.float32 if precision == 32 else np.float64
+        gl, gu = GUARD[order]
+        self.gcl, self.gcu = [gl] * self.dim, [gu] * self.dim
+        self.size = [n + gl + gu for n in self.nx]
+        cfg = Config()
+        cfg.dim, cfg.order, cfg.precision, cfg.engine = self.dim, order, precision, engine
+        for d in range(self.dim):
+            cfg.nx[d] = nx[d]
+            cfg.dx[d] = dx[d]
+            cfg.tile[d] = (tile[d] if tile else 0)
+        cfg.dt = dt
+        cfg.n_sort = n_sort
+        cfg.capacity = capacity
+        self.cfg = cfg
+        self.dx = list(dx)
+        self.dt = dt
+        self.h = P()
+        _check(lib().osg_sim_create(C.byref(cfg), C.byref(self.h)))
+        self.nspecies = 0
+        self.rqm = []
+
+    def close(self):
+        if self.h:
+            lib().osg_sim_destroy(self.h)
+            self.h = P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def grid_shape(self):
+        return tuple(reversed(self.size)) + (3,)
+
+    def add_species(self, rqm, ix, x, u, q):
+        ix, x, u, q = (np.ascontiguousarray(ix, np.int32), np.ascontiguousarray(x, self.dtype),
+                       np.ascontiguousarray(u, self.dtype), np.ascontiguousarray(q, self.dtype))
+        k = _check(lib().osg_sim_add_species(self.h, float(rqm), len(q), _p(ix), _p(x), _p(u),
+                                             _p(q)))
+        self.nspecies += 1
+        self.rqm.append(rqm)
+        return k
+
+    def set_fields(self, e=None, b=None):
+        e = None if e is None else np.ascontiguousarray(e, self.dtype)
+        b = None if b is None else np.ascontiguousarray(b, self.dtype)
+        _check(lib().osg_sim_set_fields(self.h, _p(e), _p(b)))
+
+    def fields(self):
+        e, b, j = (np.zeros(self.grid_shape, self.dtype) for _ in range(3))
+        _check(lib().osg_sim_get_fields(self.h, _p(e), _p(b), _p(j)))
+        return e, b, j
+
+    def num_particles(self, k):
+        n = L()
+        _check(lib().osg_sim_num_particles(self.h, k, C.byref(n)))
+        return n.value
+
+    def species(self, k):
+        n = self.num_particles(k)
+        ix = np.zeros((n, self.dim), np.int32)
+        x = np.zeros((n, self.dim), self.dtype)
+        u = np.zeros((n, 3), self.dtype)
+        q = np.zeros(n, self.dtype)
+        _check(lib().osg_sim_get_species(self.h, k, _p(ix), _p(x), _p(u), _p(q)))
+        return ix, x, u, q
+
+    def step(self, n=1):
+        _check(lib().osg_sim_step(self.h, int(n)))
+
+    def step_async(self, n=1):
+        _check(lib().osg_sim_step_async(self.h, int(n)))
+
+    def sync(self):
+        _check(lib().osg_sim_sync(self.h))
+
+    @property
+    def stream(self):
+        return lib().osg_sim_stream(self.h)
+
+    def energy(self):
+        kin = np.zeros(16)
+        fld = np.zeros(6)
+        _check(lib().osg_sim_energy(self.h, _p(kin), _p(fld)))
+        return kin[: self.nspecies], fld
+
+    def gauss_residual(self):
+        m, l2 = D(), D()
+        _check(lib().osg_sim_gauss_residual(self.h, C.byref(m), C.byref(l2)))
+        return m.value, l2.value
+
+    def profile(self, n):
+        ms = np.zeros(5, np.float32)
+        _check(lib().osg_sim_profile(self.h, int(n), _p(ms)))
+        return {"push": float(ms[0]), "fold": float(ms[1]), "yee": float(ms[2]),
+                "replace": float(ms[3]), "sort": float(ms[4])}
+
+    def launches_per_step(self):
+        return lib().osg_sim_launches_per_step(self.h)
+
+    def tile_occupancy(self):
+        m = D()
+        _check(lib().osg_sim_tile_occupancy(self.h, C.byref(m)))
+        return m.value
+
+    def time_steps(self, n):
+        """Run n steps between two CUDA events on the simulation stream; returns device ms."""
+        ms = F()
+        _check(lib().osg_sim_time_steps(self.h, int(n), C.byref(ms)))
+        return float(ms.value)
+
+
+def set_device(device):
+    _check(lib().osg_set_device(int(device)))

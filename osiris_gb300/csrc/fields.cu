@@ -1,0 +1,370 @@
+// fields.cu -- grid kernels of the time step on the reference field layout (3 components
+// fastest, guard cells included): Yee B half step / E full step, single-node periodic guard
+// fold (current) and replace (fields), and the FP64 diagnostics (field energy, charge density
+// deposit, divergence).
+//
+//   dbdt 2D/3D      source/emf/solver/os-emf-solver-yee.f03:102-138, :211-251
+//   dedt 2D/3D      source/emf/solver/os-emf-solver-yee.f03:287-326, :385-428
+//   advance_yee     source/emf/solver/os-emf-solver-yee.f03:542-568
+//   periodic add / replace   source/vdf/os-vdf-comm.f90:142-326 (one direction per launch,
+//                            directions in order as update_boundary_vdf :665-722)
+//   field energy    source/emf/diagnostics/os-emf-diagnostics.f03:42-58
+//   rho deposit     source/spec/os-spec-charge.f90:500-600
+//   divergence      source/vdf/os-vdf-math.f90:1013-1073
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "fields.cuh"
+#include "pic_math.cuh"
+
+namespace osg {
+
+// Fortran indices (i1,i2,i3) of flat point n of the box [lo, lo + ext) in each axis
+__device__ __forceinline__ void unflat(long n, const int *lo, const int *ext, int &i1, int &i2,
+                                       int &i3)
+{
+    i1 = lo[0] + (int)(n % ext[0]);
+    long r = n / ext[0];
+    i2 = lo[1] + (int)(r % ext[1]);
+    i3 = lo[2] + (int)(r / ext[1]);
+}
+
+__device__ __forceinline__ long pos(const GridDesc &g, int i1, int i2, int i3)
+{
+    return 3L * ((long)(i1 - 1 + g.gcl[0]) +
+                 (long)g.size[0] * ((i2 - 1 + g.gcl[1]) + (long)g.size[1] * (i3 - 1 + g.gcl[2])));
+}
+
+struct Box {
+    int lo[3], ext[3];
+    long n;
+};
+
+static Box make_box(const GridDesc &g, int lo, int hi_off)
+{
+    // points lo .. nx + hi_off along active axes, single point 1 on inactive ones
+    Box b;
+    b.n = 1;
+    for (int d = 0; d < 3; d++) {
+        if (d < g.dim) {
+            b.lo[d] = lo;
+            b.ext[d] = g.nx[d] + hi_off - lo + 1;
+        } else {
+            b.lo[d] = 1;
+            b.ext[d] = 1;
+        }
+        b.n *= b.ext[d];
+    }
+    return b;
+}
+
+template <typename T, int DIM>
+__global__ void k_dbdt(GridDesc g, Box box, T *__restrict__ b, const T *__restrict__ e, T d1, T d2,
+                       T d3)
+{
+    OSG_GRID_LOOP(n, box.n)
+    {
+        int i1, i2, i3;
+        unflat(n, box.lo, box.ext, i1, i2, i3);
+        const long p = pos(g, i1, i2, i3);
+        const long sx = 3, sy = g.stride(1), sz = g.stride(2);
+        if constexpr (DIM == 2) {
+            b[p + 0] = b[p + 0] - d2 * (e[p + sy + 2] - e[p + 2]);
+            b[p + 1] = b[p + 1] + d1 * (e[p + sx + 2] - e[p + 2]);
+            b[p + 2] = b[p + 2] - d1 * (e[p + sx + 1] - e[p + 1]) + d2 * (e[p + sy + 0] - e[p + 0]);
+        } else if constexpr (DIM == 3) {
+            b[p + 0] = b[p + 0] - d2 * (e[p + sy + 2] - e[p + 2]) + d3 * (e[p + sz + 1] - e[p + 1]);
+            b[p + 1] = b[p + 1] + d1 * (e[p + sx + 2] - e[p + 2]) - d3 * (e[p + sz + 0] - e[p + 0]);
+            b[p + 2] = b[p + 2] - d1 * (e[p + sx + 1] - e[p + 1]) + d2 * (e[p + sy + 0] - e[p + 0]);
+        } else {
+            b[p + 1] = b[p + 1] + d1 * (e[p + sx + 2] - e[p + 2]);
+            b[p + 2] = b[p + 2] - d1 * (e[p + sx + 1] - e[p + 1]);
+        }
+    }
+}
+
+template <typename T, int DIM>
+__global__ void k_dedt(GridDesc g, Box box, T *__restrict__ e, const T *__restrict__ b,
+                       const T *__restrict__ j, T dti, T d1, T d2, T d3)
+{
+    OSG_GRID_LOOP(n, box.n)
+    {
+        int i1, i2, i3;
+        unflat(n, box.lo, box.ext, i1, i2, i3);
+        const long p = pos(g, i1, i2, i3);
+        const long sx = 3, sy = g.stride(1), sz = g.stride(2);
+        if constexpr (DIM == 2) {
+            e[p + 0] = e[p + 0] - dti * j[p + 0] + d2 * (b[p + 2] - b[p - sy + 2]);
+            e[p + 1] = e[p + 1] - dti * j[p + 1] - d1 * (b[p + 2] - b[p - sx + 2]);
+            e[p + 2] = e[p + 2] - dti * j[p + 2] + d1 * (b[p + 1] - b[p - sx + 1]) -
+                       d2 * (b[p + 0] - b[p - sy + 0]);
+        } else if constexpr (DIM == 3) {
+            e[p + 0] = e[p + 0] - dti * j[p + 0] + d2 * (b[p + 2] - b[p - sy + 2]) -
+                       d3 * (b[p + 1] - b[p - sz + 1]);
+            e[p + 1] = e[p + 1] - dti * j[p + 1] + d3 * (b[p + 0] - b[p - sz + 0]) -
+                       d1 * (b[p + 2] - b[p - sx + 2]);
+            e[p + 2] = e[p + 2] - dti * j[p + 2] + d1 * (b[p + 1] - b[p - sx + 1]) -
+                       d2 * (b[p + 0] - b[p - sy + 0]);
+        } else {
+            e[p + 0] = e[p + 0] - dti * j[p + 0];
+            e[p + 1] = e[p + 1] - dti * j[p + 1] - d1 * (b[p + 2] - b[p - sx + 2]);
+            e[p + 2] = e[p + 2] - dti * j[p + 2] + d1 * (b[p + 1] - b[p - sx + 1]);
+        }
+    }
+}
+
+template <typename T>
+static void launch_dbdt(const GridDesc &g, T *b, const T *e, const double *dx, double dt,
+                        cudaStream_t st)
+{
+    Box box = make_box(g, 0, 1);
+    const T d1 = (T)(dt / dx[0]), d2 = g.dim > 1 ? (T)(dt / dx[1]) : T(0),
+            d3 = g.dim > 2 ? (T)(dt / dx[2]) : T(0);
+    const unsigned nb = blocks_for(box.n, 256);
+    if (g.dim == 2) k_dbdt<T, 2><<<nb, 256, 0, st>>>(g, box, b, e, d1, d2, d3);
+    else if (g.dim == 3) k_dbdt<T, 3><<<nb, 256, 0, st>>>(g, box, b, e, d1, d2, d3);
+    else k_dbdt<T, 1><<<nb, 256, 0, st>>>(g, box, b, e, d1, d2, d3);
+}
+
+template <typename T>
+static void launch_dedt(const GridDesc &g, T *e, const T *b, const T *j, const double *dx,
+                        double dt, cudaStream_t st)
+{
+    Box box = make_box(g, 1, 1);
+    const T dti = (T)dt, d1 = (T)(dt / dx[0]), d2 = g.dim > 1 ? (T)(dt / dx[1]) : T(0),
+            d3 = g.dim > 2 ? (T)(dt / dx[2]) : T(0);
+    const unsigned nb = blocks_for(box.n, 256);
+    if (g.dim == 2) k_dedt<T, 2><<<nb, 256, 0, st>>>(g, box, e, b, j, dti, d1, d2, d3);
+    else if (g.dim == 3) k_dedt<T, 3><<<nb, 256, 0, st>>>(g, box, e, b, j, dti, d1, d2, d3);
+    else k_dedt<T, 1><<<nb, 256, 0, st>>>(g, box, e, b, j, dti, d1, d2, d3);
+}
+
+template <typename T>
+void yee_advance(const GridDesc &g, T *e, T *b, const T *j, const double *dx, double dt,
+                 cudaStream_t st)
+{
+    launch_dbdt(g, b, e, dx, dt / 2.0, st);
+    launch_dedt(g, e, b, j, dx, dt, st);
+    launch_dbdt(g, b, e, dx, dt / 2.0, st);
+}
+
+// One direction of the periodic update.  Thread n handles one guard point (lower or upper
+// side along axis `d`, full range along the others) and its periodic image.
+template <typename T>
+__global__ void k_periodic_dir(GridDesc g, int d, int add, T *__restrict__ f, long n_lo, long n_all)
+{
+    OSG_GRID_LOOP(n, n_all)
+    {
+        const bool lower = n < n_lo;
+        const long m = lower ? n : n - n_lo;
+        int lo[3], ext[3];
+        for (int a = 0; a < 3; a++) {
+            if (a >= g.dim) {
+                lo[a] = 1;
+                ext[a] = 1;
+            } else if (a == d) {
+                lo[a] = lower ? 1 - g.gcl[a] : g.nx[a] + 1;
+                ext[a] = lower ? g.gcl[a] : g.gcu[a];
+            } else {
+                lo[a] = 1 - g.gcl[a];
+                ext[a] = g.size[a];
+            }
+        }
+        int i[3];
+        unflat(m, lo, ext, i[0], i[1], i[2]);
+        const long pg = pos(g, i[0], i[1], i[2]);
+        i[d] += lower ? g.nx[d] : -g.nx[d];
+        const long pi = pos(g, i[0], i[1], i[2]);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            if (add) {
+                const T v = f[pg + c] + f[pi + c];
+                f[pg + c] = v;
+                f[pi + c] = v;
+            } else {
+                f[pg + c] = f[pi + c];
+            }
+        }
+    }
+}
+
+template <typename T>
+void periodic_update(const GridDesc &g, T *f, int add, cudaStream_t st)
+{
+    for (int d = 0; d < g.dim; d++) {
+        long other = 1;
+        for (int a = 0; a < g.dim; a++)
+            if (a != d) other *= g.size[a];
+        const long n_lo = other * g.gcl[d], n_all = n_lo + other * g.gcu[d];
+        k_periodic_dir<T><<<blocks_for(n_all, 256), 256, 0, st>>>(g, d, add, f, n_lo, n_all);
+    }
+}
+
+// sum over the interior of each component squared, accumulated in double:
+// out[c] += sum f_c^2 (caller applies 0.5 dV)
+template <typename T>
+__global__ void k_sumsq(GridDesc g, Box box, const T *__restrict__ f, double *out)
+{
+    double s0 = 0, s1 = 0, s2 = 0;
+    OSG_GRID_LOOP(n, box.n)
+    {
+        int i1, i2, i3;
+        unflat(n, box.lo, box.ext, i1, i2, i3);
+        const long p = pos(g, i1, i2, i3);
+        const double a = f[p], b = f[p + 1], c = f[p + 2];
+        s0 += a * a;
+        s1 += b * b;
+        s2 += c * c;
+    }
+    s0 = block_sum(s0);
+    s1 = block_sum(s1);
+    s2 = block_sum(s2);
+    if (threadIdx.x == 0) {
+        atomicAdd(out + 0, s0);
+        atomicAdd(out + 1, s1);
+        atomicAdd(out + 2, s2);
+    }
+}
+
+template <typename T>
+void field_sumsq(const GridDesc &g, const T *f, double *d_out, cudaStream_t st)
+{
+    Box box = make_box(g, 1, 0);
+    unsigned nb = blocks_for(box.n, 256);
+    if (nb > 1216) nb = 1216;
+    k_sumsq<T><<<nb, 256, 0, st>>>(g, box, f, d_out);
+}
+
+// charge density of particles (reference layout) into component 0 of a double grid with the
+// same guard cells; shape of the interpolation order, support starting at 1 - OFFSET
+template <typename T, int DIM, int ORD>
+__global__ void k_rho(GridDesc g, const int *__restrict__ ix, const T *__restrict__ x,
+                      const T *__restrict__ q, long np, double *rho, int *status)
+{
+    constexpr int NP = ORD + 1, LP = 1 - Stencil<ORD>::OFS;
+    OSG_GRID_LOOP(p, np)
+    {
+        double w[3][NP];
+        int c[3] = {1, 1, 1};
+        bool ok = true;
+        for (int d = 0; d < DIM; d++) {
+            c[d] = ix[DIM * p + d];
+            ok = ok && (c[d] + LP - 1 + g.gcl[d] >= 0) && (c[d] + LP + NP - 1 - 1 + g.gcl[d] < g.size[d]);
+            const double xx = (double)x[DIM * p + d];
+            const double a = 0.5 - xx, b = 0.5 + xx;
+            if constexpr (ORD == 1) { w[d][0] = a; w[d][1] = b; }
+            else if constexpr (ORD == 2) { w[d][0] = 0.5 * a * a; w[d][1] = fma(a, b, 0.5); w[d][2] = 0.5 * b * b; }
+            else if constexpr (ORD == 3) {
+                w[d][0] = a * a * a / 6.0; w[d][1] = fma(0.5, b * b * b, 2.0 / 3.0 - b * b);
+                w[d][2] = fma(0.5, a * a * a, 2.0 / 3.0 - a * a); w[d][3] = b * b * b / 6.0;
+            } else {
+                const double ab = a * b;
+                w[d][0] = a * a * a * a / 24.0; w[d][1] = fma(a, fma(a, 1.5 + ab, 1.0), 0.25) / 6.0;
+                w[d][2] = fma(ab, fma(0.25, ab, 0.5), 11.0 / 24.0);
+                w[d][3] = fma(b, fma(b, 1.5 + ab, 1.0), 0.25) / 6.0; w[d][4] = b * b * b * b / 24.0;
+            }
+        }
+        if (!ok) {
+            atomicOr(status, 1);
+            continue;
+        }
+        const double qq = (double)q[p];
+        const int n2 = DIM > 1 ? NP : 1, n3 = DIM > 2 ? NP : 1;
+        for (int k3 = 0; k3 < n3; k3++)
+            for (int k2 = 0; k2 < n2; k2++)
+                for (int k1 = 0; k1 < NP; k1++) {
+                    double wt = qq * w[0][k1];
+                    if (DIM > 1) wt *= w[1][k2];
+                    if (DIM > 2) wt *= w[2][k3];
+                    const long pp = pos(g, c[0] + LP + k1, DIM > 1 ? c[1] + LP + k2 : 1,
+                                        DIM > 2 ? c[2] + LP + k3 : 1);
+                    atomicAdd(rho + pp, wt);
+                }
+    }
+}
+
+template <typename T>
+int deposit_rho(const GridDesc &g, int order, const int *ix, const T *x, const T *q, long np,
+                double *rho, int *status, cudaStream_t st)
+{
+    if (np <= 0) return OSG_OK;
+    unsigned nb = blocks_for(np, 256);
+    if (nb > 4096) nb = 4096;
+#define OSG_CASE(D, O)                                                                        \
+    if (g.dim == D && order == O) {                                                           \
+        k_rho<T, D, O><<<nb, 256, 0, st>>>(g, ix, x, q, np, rho, status);                     \
+        return OSG_OK;                                                                        \
+    }
+    OSG_CASE(2, 1) OSG_CASE(2, 2) OSG_CASE(2, 3) OSG_CASE(2, 4)
+    OSG_CASE(3, 1) OSG_CASE(3, 2) OSG_CASE(3, 3) OSG_CASE(3, 4)
+#undef OSG_CASE
+    set_error("rho deposit: unsupported dim %d order %d", g.dim, order);
+    return OSG_ERR_ARG;
+}
+
+// residual r = div E - (rho - rho_ref) on interior points; accumulates max |r| (as ordered
+// bits) and sum r^2
+template <typename T>
+__global__ void k_gauss(GridDesc g, Box box, const T *__restrict__ e, const double *__restrict__ rho,
+                        const double *__restrict__ rho_ref, double rdx0, double rdx1, double rdx2,
+                        unsigned long long *maxbits, double *l2)
+{
+    double s = 0.0, m = 0.0;
+    OSG_GRID_LOOP(n, box.n)
+    {
+        int i1, i2, i3;
+        unflat(n, box.lo, box.ext, i1, i2, i3);
+        const long p = pos(g, i1, i2, i3);
+        double dv = ((double)e[p] - (double)e[p - 3]) * rdx0;
+        if (g.dim > 1) dv += ((double)e[p + 1] - (double)e[p - g.stride(1) + 1]) * rdx1;
+        if (g.dim > 2) dv += ((double)e[p + 2] - (double)e[p - g.stride(2) + 2]) * rdx2;
+        const double r = dv - (rho[p] - (rho_ref ? rho_ref[p] : 0.0));
+        s += r * r;
+        m = fmax(m, fabs(r));
+    }
+    s = block_sum(s);
+    // block max through the ordered bit pattern of non-negative doubles
+    __shared__ double mx[32];
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) mx[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)((blockDim.x + 31) >> 5); w++) m = fmax(m, mx[w]);
+        atomicAdd(l2, s);
+        atomicMax(maxbits, (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+template <typename T>
+void gauss_residual(const GridDesc &g, const T *e, const double *rho, const double *rho_ref,
+                    const double *dx, unsigned long long *d_max, double *d_l2, cudaStream_t st)
+{
+    Box box = make_box(g, 1, 0);
+    unsigned nb = blocks_for(box.n, 256);
+    if (nb > 1216) nb = 1216;
+    k_gauss<T><<<nb, 256, 0, st>>>(g, box, e, rho, rho_ref, 1.0 / dx[0],
+                                   g.dim > 1 ? 1.0 / dx[1] : 0.0, g.dim > 2 ? 1.0 / dx[2] : 0.0,
+                                   d_max, d_l2);
+}
+
+
+template void yee_advance<float>(const GridDesc &, float *, float *, const float *,
+                                 const double *, double, cudaStream_t);
+template void yee_advance<double>(const GridDesc &, double *, double *, const double *,
+                                  const double *, double, cudaStream_t);
+template void periodic_update<float>(const GridDesc &, float *, int, cudaStream_t);
+template void periodic_update<double>(const GridDesc &, double *, int, cudaStream_t);
+template void field_sumsq<float>(const GridDesc &, const float *, double *, cudaStream_t);
+template void field_sumsq<double>(const GridDesc &, const double *, double *, cudaStream_t);
+template int deposit_rho<float>(const GridDesc &, int, const int *, const float *,
+                                const float *, long, double *, int *, cudaStream_t);
+template int deposit_rho<double>(const GridDesc &, int, const int *, const double *,
+                                 const double *, long, double *, int *, cudaStream_t);
+template void gauss_residual<float>(const GridDesc &, const float *, const double *,
+                                    const double *, const double *, unsigned long long *,
+                                    double *, cudaStream_t);
+template void gauss_residual<double>(const GridDesc &, const double *, const double *,
+                                     const double *, const double *, unsigned long long *,
+                                     double *, cudaStream_t);
+
+} // namespace osg

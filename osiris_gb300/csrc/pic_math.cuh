@@ -1,0 +1,386 @@
+// pic_math.cuh -- per-particle arithmetic of the OSIRIS push and charge-conserving deposit,
+// for float (mixed-precision path) and double (plain FP64 path).
+//
+// Every expression keeps the rounding structure of the reference SIMD kernels: a fused
+// multiply-add appears exactly where the reference uses one, every other product and sum is
+// rounded on its own (the library is compiled with -fmad=false so nvcc does not contract).
+// Division and square root are the IEEE-rounded operations (no fast-math), so a particle's
+// new position, cell and momentum are bit-identical to the reference CPU kernels.
+//
+//   B-spline weights         source/simd/splines-avx2.h
+//   longitudinal weights     source/simd/os-spec-current-avx2d.c:17-110
+//   Boris rotation + energy  source/simd/os-spec-push-avx2d.c:98-154
+//   1/gamma                  source/simd/os-spec-push-avx2d.c:163-168
+//   cell trim                source/simd/os-spec-push-avx2d.c:53-64
+//   trajectory split         source/simd/split-vec.h:105-265 (2D), :266-718 (3D)
+#pragma once
+
+#include <cstdint>
+
+namespace osg {
+
+__device__ __forceinline__ float fmaR(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmaR(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float sqrtR(float a) { return sqrtf(a); }
+__device__ __forceinline__ double sqrtR(double a) { return sqrt(a); }
+
+// grid offset of the interpolation stencil (1 + ORD/2, 3 for quartic)
+template <int ORD> struct Stencil {
+    static constexpr int NP = ORD + 1;
+    static constexpr int OFS = (ORD == 1) ? 1 : (ORD == 2) ? 2 : (ORD == 3) ? 2 : 3;
+};
+
+// B-spline weights at a cell-centred offset x in [-0.5, 0.5)
+template <int ORD, typename T>
+__device__ __forceinline__ void spline(T x, T *w)
+{
+    const T c1_2 = T(0.5);
+    if constexpr (ORD == 1) {
+        w[0] = c1_2 - x;
+        w[1] = c1_2 + x;
+    } else if constexpr (ORD == 2) {
+        T a = c1_2 - x, b = c1_2 + x;
+        w[0] = (a * a) * c1_2;
+        w[1] = fmaR(a, b, c1_2);
+        w[2] = (b * b) * c1_2;
+    } else if constexpr (ORD == 3) {
+        T a = c1_2 - x, b = c1_2 + x;
+        T a2 = a * a, b2 = b * b;
+        T a3 = a * a2, b3 = b * b2;
+        w[0] = T(1.0 / 6.0) * a3;
+        w[1] = fmaR(c1_2, b3, T(2.0 / 3.0) - b2);
+        w[2] = fmaR(c1_2, a3, T(2.0 / 3.0) - a2);
+        w[3] = T(1.0 / 6.0) * b3;
+    } else {
+        T a = c1_2 - x, b = c1_2 + x;
+        T ab = a * b, a2 = a * a, b2 = b * b;
+        w[0] = T(1.0 / 24.0) * (a2 * a2);
+        w[1] = T(1.0 / 6.0) * fmaR(a, fmaR(a, T(1.5) + ab, T(1.0)), T(0.25));
+        w[2] = fmaR(ab, fmaR(T(0.25), ab, c1_2), T(11.0 / 24.0));
+        w[3] = T(1.0 / 6.0) * fmaR(b, fmaR(b, T(1.5) + ab, T(1.0)), T(0.25));
+        w[4] = T(1.0 / 24.0) * (b2 * b2);
+    }
+}
+
+// weights at the half-shifted point (h = 1 when x < 0), for staggered field components
+template <int ORD, typename T>
+__device__ __forceinline__ void spline_h(T x, T h, T *w)
+{
+    T a = (T(1.0) - h) - x, b = h + x;
+    if constexpr (ORD == 1) {
+        w[0] = a;
+        w[1] = b;
+    } else if constexpr (ORD == 2) {
+        w[0] = (a * a) * T(0.5);
+        w[1] = fmaR(a, b, T(0.5));
+        w[2] = (b * b) * T(0.5);
+    } else if constexpr (ORD == 3) {
+        T a2 = a * a, b2 = b * b;
+        T a3 = a * a2, b3 = b * b2;
+        w[0] = T(1.0 / 6.0) * a3;
+        w[1] = fmaR(T(0.5), b3, T(2.0 / 3.0) - b2);
+        w[2] = fmaR(T(0.5), a3, T(2.0 / 3.0) - a2);
+        w[3] = T(1.0 / 6.0) * b3;
+    } else {
+        T ab = a * b, a2 = a * a, b2 = b * b;
+        w[0] = T(1.0 / 24.0) * (a2 * a2);
+        w[1] = T(1.0 / 6.0) * fmaR(a, fmaR(a, T(1.5) + ab, T(1.0)), T(0.25));
+        w[2] = fmaR(ab, fmaR(T(0.25), ab, T(0.5)), T(11.0 / 24.0));
+        w[3] = T(1.0 / 6.0) * fmaR(b, fmaR(b, T(1.5) + ab, T(1.0)), T(0.25));
+        w[4] = T(1.0 / 24.0) * (b2 * b2);
+    }
+}
+
+// charge-conserving weights along the motion (ORD values)
+template <int ORD, typename T>
+__device__ __forceinline__ void long_weights(T qn, T x0, T x1, T *w)
+{
+    T d = x1 - x0;
+    if constexpr (ORD == 1) {
+        w[0] = qn * d;
+    } else if constexpr (ORD == 2) {
+        T s = T(0.5) - x0, p = T(0.5) + x0;
+        T n = qn * d;
+        w[0] = n * fmaR(-T(0.5), d, s);
+        w[1] = n * fmaR(T(0.5), d, p);
+    } else if constexpr (ORD == 3) {
+        T s = T(0.5) - x0, p = T(0.5) + x0;
+        T d3 = T(1.0 / 3.0) * d;
+        T a0 = T(0.5) * fmaR(s, s, -(d * (s - d3)));
+        T a1 = fmaR(-d, x0 + d3, fmaR(-x0, x0, T(0.75)));
+        T a2 = T(0.5) * fmaR(p, p, d * (p + d3));
+        T n = qn * d;
+        w[0] = n * a0;
+        w[1] = n * a1;
+        w[2] = n * a2;
+    } else {
+        T s = T(0.5) - x0, p = T(0.5) + x0;
+        T t = x0 - T(1.0 / 6.0), u = x0 + T(1.0 / 6.0);
+        T s2 = s * s, s3 = s2 * s, p2 = p * p, p3 = p2 * p;
+        T d2 = d * T(0.5), d4 = d * T(0.25);
+        T a0 = T(1.0 / 6.0) * fmaR(d, fmaR(d, s - d4, -(T(1.5) * s2)), s3);
+        T a1 = fmaR(d, fmaR(d2, t + d4, fmaR(T(0.75), t * t, -T(1.0 / 3.0))),
+                    fmaR(T(0.5), p3, T(2.0 / 3.0) - p2));
+        T a2 = fmaR(-d, fmaR(d2, u + d4, fmaR(T(0.75), u * u, -T(1.0 / 3.0))),
+                    fmaR(T(0.5), s3, T(2.0 / 3.0) - s2));
+        T a3 = T(1.0 / 6.0) * fmaR(d, fmaR(d, p + d4, T(1.5) * p2), p3);
+        T n = qn * d;
+        w[0] = n * a0;
+        w[1] = n * a1;
+        w[2] = n * a2;
+        w[3] = n * a3;
+    }
+}
+
+// Boris momentum update; tem = dt / (2 rqm); returns the time-centred kinetic energy factor
+// u^2 / (gamma + 1) of the half-kicked momentum.
+template <typename T>
+__device__ __forceinline__ T boris(T tem, T e1, T e2, T e3, T b1, T b2, T b3, T &u1, T &u2,
+                                   T &u3)
+{
+    e1 = e1 * tem;
+    e2 = e2 * tem;
+    e3 = e3 * tem;
+    T ut1 = u1 + e1, ut2 = u2 + e2, ut3 = u3 + e3;
+    T utsq = fmaR(ut3, ut3, fmaR(ut2, ut2, ut1 * ut1));
+    T gam = sqrtR(utsq + T(1.0));
+    T ene = utsq / (gam + T(1.0));
+    T tg = tem / gam;
+    b1 = b1 * tg;
+    b2 = b2 * tg;
+    b3 = b3 * tg;
+    T v1 = fmaR(b3, ut2, ut1), v2 = fmaR(b1, ut3, ut2), v3 = fmaR(b2, ut1, ut3);
+    v1 = fmaR(-b2, ut3, v1);
+    v2 = fmaR(-b3, ut1, v2);
+    v3 = fmaR(-b1, ut2, v3);
+    T ot = fmaR(b1, b1, T(1.0));
+    ot = fmaR(b2, b2, ot);
+    ot = fmaR(b3, b3, ot);
+    ot = T(2.0) / ot;
+    b1 = b1 * ot;
+    b2 = b2 * ot;
+    b3 = b3 * ot;
+    ut1 = fmaR(b3, v2, ut1);
+    ut2 = fmaR(b1, v3, ut2);
+    ut3 = fmaR(b2, v1, ut3);
+    ut1 = fmaR(-b2, v3, ut1);
+    ut2 = fmaR(-b3, v1, ut2);
+    ut3 = fmaR(-b1, v2, ut3);
+    u1 = ut1 + e1;
+    u2 = ut2 + e2;
+    u3 = ut3 + e3;
+    return ene;
+}
+
+template <typename T>
+__device__ __forceinline__ T rgamma(T u1, T u2, T u3)
+{
+    return T(1.0) / sqrtR(fmaR(u3, u3, fmaR(u2, u2, fmaR(u1, u1, T(1.0)))));
+}
+
+// cell crossing of a pushed offset: +1 when x >= 0.5, -1 when x < -0.5
+template <typename T>
+__device__ __forceinline__ int trim(T x)
+{
+    return (x >= T(0.5) ? 1 : 0) - (x < T(-0.5) ? 1 : 0);
+}
+
+// ---------------------------------------------------------------------------------------
+// Virtual particles: trajectory segments that stay inside one cell, positions relative to
+// that cell (x0 start, x1 end), cell index i.  In 2D the out-of-plane velocity vz is split
+// in proportion to the segment fraction (the 2D deposit needs it for j3).
+// ---------------------------------------------------------------------------------------
+
+template <typename T> struct Seg2 {
+    T x0, x1, y0, y1, vz;
+    int i, j;
+};
+
+template <typename T> struct Seg3 {
+    T x0, x1, y0, y1, z0, z1;
+    int i, j, k;
+};
+
+// Split a 2D move into <= 3 in-cell segments (split-vec.h:105-265). s[0] is the first segment;
+// returns the number of segments.
+template <typename T>
+__device__ __forceinline__ int split2(Seg2<T> *s, int dix, int diy)
+{
+    Seg2<T> &v = s[0];
+    if (dix == 0 && diy == 0) return 1;
+    if (diy == 0) {
+        T xint = T(0.5 * dix);
+        T delta = (xint - v.x0) / (v.x1 - v.x0);
+        T yint = v.y0 + (v.y1 - v.y0) * delta;
+        Seg2<T> &w = s[1];
+        w.x0 = -xint; w.x1 = v.x1 - T(dix);
+        w.y0 = yint;  w.y1 = v.y1;
+        w.i = v.i + dix; w.j = v.j;
+        w.vz = v.vz * (T(1) - delta);
+        v.x1 = xint; v.y1 = yint; v.vz = v.vz * delta;
+        return 2;
+    }
+    if (dix == 0) {
+        T yint = T(0.5 * diy);
+        T delta = (yint - v.y0) / (v.y1 - v.y0);
+        T xint = v.x0 + (v.x1 - v.x0) * delta;
+        Seg2<T> &w = s[1];
+        w.x0 = xint;  w.x1 = v.x1;
+        w.y0 = -yint; w.y1 = v.y1 - T(diy);
+        w.i = v.i; w.j = v.j + diy;
+        w.vz = v.vz * (T(1) - delta);
+        v.x1 = xint; v.y1 = yint; v.vz = v.vz * delta;
+        return 2;
+    }
+    T xint = T(0.5 * dix);
+    T delta = (xint - v.x0) / (v.x1 - v.x0);
+    T yint = v.y0 + (v.y1 - v.y0) * delta;
+    if (yint >= T(-0.5) && yint < T(0.5)) {
+        // x face first, then y face inside the x-shifted cell
+        T vzint = v.vz * delta;
+        T vzint2 = v.vz * (T(1) - delta);
+        T yint2 = T(0.5 * diy);
+        delta = (yint2 - yint) / (v.y1 - yint);
+        T xint2 = -xint + (v.x1 - xint) * delta;
+        Seg2<T> &a = s[1];
+        a.x0 = -xint; a.x1 = xint2; a.y0 = yint; a.y1 = yint2;
+        a.i = v.i + dix; a.j = v.j; a.vz = vzint2 * delta;
+        Seg2<T> &b = s[2];
+        b.x0 = xint2; b.x1 = v.x1 - T(dix); b.y0 = -yint2; b.y1 = v.y1 - T(diy);
+        b.i = v.i + dix; b.j = v.j + diy; b.vz = vzint2 * (T(1) - delta);
+        v.x1 = xint; v.y1 = yint; v.vz = vzint;
+    } else {
+        // y face first
+        T vzint = v.vz * delta;
+        T yint2 = T(0.5 * diy);
+        delta = (yint2 - v.y0) / (yint - v.y0);
+        T xint2 = v.x0 + (xint - v.x0) * delta;
+        Seg2<T> &a = s[1];
+        a.x0 = xint2; a.x1 = xint; a.y0 = -yint2; a.y1 = yint - T(diy);
+        a.i = v.i; a.j = v.j + diy; a.vz = vzint * (T(1) - delta);
+        Seg2<T> &b = s[2];
+        b.x0 = -xint; b.x1 = v.x1 - T(dix); b.y0 = yint - T(diy); b.y1 = v.y1 - T(diy);
+        b.i = v.i + dix; b.j = v.j + diy; b.vz = v.vz - vzint;
+        v.x1 = xint2; v.y1 = yint2; v.vz = vzint * delta;
+    }
+    return 3;
+}
+
+// coordinate accessors for the axis-generic 3D split
+template <typename T> __device__ __forceinline__ T &c0(Seg3<T> &s, int a)
+{
+    return a == 0 ? s.x0 : (a == 1 ? s.y0 : s.z0);
+}
+template <typename T> __device__ __forceinline__ T &c1(Seg3<T> &s, int a)
+{
+    return a == 0 ? s.x1 : (a == 1 ? s.y1 : s.z1);
+}
+template <typename T> __device__ __forceinline__ int &ci(Seg3<T> &s, int a)
+{
+    return a == 0 ? s.i : (a == 1 ? s.j : s.k);
+}
+
+// one face crossing along axis a (split-vec.h cases 1, 2, 4)
+template <typename T>
+__device__ __forceinline__ void cut_one(Seg3<T> &v, Seg3<T> &w, int a, int d)
+{
+    T cint = T(0.5 * d);
+    T delta = (cint - c0(v, a)) / (c1(v, a) - c0(v, a));
+    T in[3];
+#pragma unroll
+    for (int b = 0; b < 3; b++) in[b] = (b == a) ? cint : c0(v, b) + (c1(v, b) - c0(v, b)) * delta;
+    w = v;
+    w.x0 = in[0]; w.y0 = in[1]; w.z0 = in[2];
+    c0(w, a) = -cint;
+    c1(w, a) = c1(v, a) - T(d);
+    ci(w, a) += d;
+    v.x1 = in[0]; v.y1 = in[1]; v.z1 = in[2];
+}
+
+// two face crossings along axes a < b (split-vec.h cases 3, 5, 6)
+template <typename T>
+__device__ __forceinline__ void cut_two(Seg3<T> &v, Seg3<T> &w0, Seg3<T> &w1, int a, int b,
+                                        int da, int db)
+{
+    const int o = 3 - a - b;
+    T aint = T(0.5 * da);
+    T delta = (aint - c0(v, a)) / (c1(v, a) - c0(v, a));
+    T bint = c0(v, b) + (c1(v, b) - c0(v, b)) * delta;
+    T oint = c0(v, o) + (c1(v, o) - c0(v, o)) * delta;
+    w0 = v;
+    w1 = v;
+    if (bint >= T(-0.5) && bint < T(0.5)) {
+        T bint2 = T(0.5 * db);
+        T del2 = (bint2 - bint) / (c1(v, b) - bint);
+        T aint2 = -aint + (c1(v, a) - aint) * del2;
+        T oint2 = oint + (c1(v, o) - oint) * del2;
+        c0(w0, a) = -aint; c1(w0, a) = aint2;
+        c0(w0, b) = bint;  c1(w0, b) = bint2;
+        c0(w0, o) = oint;  c1(w0, o) = oint2;
+        ci(w0, a) += da;
+        c0(w1, a) = aint2;  c1(w1, a) = c1(v, a) - T(da);
+        c0(w1, b) = -bint2; c1(w1, b) = c1(v, b) - T(db);
+        c0(w1, o) = oint2;  c1(w1, o) = c1(v, o);
+        ci(w1, a) += da; ci(w1, b) += db;
+        c1(v, a) = aint; c1(v, b) = bint; c1(v, o) = oint;
+    } else {
+        T bint2 = T(0.5 * db);
+        T del2 = (bint2 - c0(v, b)) / (bint - c0(v, b));
+        T aint2 = c0(v, a) + (aint - c0(v, a)) * del2;
+        T oint2 = c0(v, o) + (oint - c0(v, o)) * del2;
+        c0(w0, a) = aint2;  c1(w0, a) = aint;
+        c0(w0, b) = -bint2; c1(w0, b) = bint - T(db);
+        c0(w0, o) = oint2;  c1(w0, o) = oint;
+        ci(w0, b) += db;
+        c0(w1, a) = -aint;       c1(w1, a) = c1(v, a) - T(da);
+        c0(w1, b) = bint - T(db); c1(w1, b) = c1(v, b) - T(db);
+        c0(w1, o) = oint;        c1(w1, o) = c1(v, o);
+        ci(w1, a) += da; ci(w1, b) += db;
+        c1(v, a) = aint2; c1(v, b) = bint2; c1(v, o) = oint2;
+    }
+}
+
+// Split a 3D move into <= 4 in-cell segments; returns the count.
+template <typename T>
+__device__ __forceinline__ int split3(Seg3<T> *s, int dix, int diy, int diz)
+{
+    const int cross = (dix != 0) | ((diy != 0) << 1) | ((diz != 0) << 2);
+    switch (cross) {
+    case 0: return 1;
+    case 1: cut_one(s[0], s[1], 0, dix); return 2;
+    case 2: cut_one(s[0], s[1], 1, diy); return 2;
+    case 4: cut_one(s[0], s[1], 2, diz); return 2;
+    case 3: cut_two(s[0], s[1], s[2], 0, 1, dix, diy); return 3;
+    case 5: cut_two(s[0], s[1], s[2], 0, 2, dix, diz); return 3;
+    case 6: cut_two(s[0], s[1], s[2], 1, 2, diy, diz); return 3;
+    default: {
+        cut_two(s[0], s[1], s[2], 0, 1, dix, diy);
+        T zint = T(0.5 * diz);
+        int n = 3;
+#pragma unroll 1
+        for (int t = 0; t < 3; t++) {
+            Seg3<T> &c = s[t];
+            if (c.z1 < T(-0.5) || c.z1 >= T(0.5)) {
+                T delta = (zint - c.z0) / (c.z1 - c.z0);
+                T xi = c.x0 + (c.x1 - c.x0) * delta;
+                T yi = c.y0 + (c.y1 - c.y0) * delta;
+                Seg3<T> &w = s[3];
+                w.x0 = xi; w.x1 = c.x1; w.y0 = yi; w.y1 = c.y1;
+                w.z0 = -zint; w.z1 = c.z1 - T(diz);
+                w.i = c.i; w.j = c.j; w.k = c.k + diz;
+                c.x1 = xi; c.y1 = yi; c.z1 = zint;
+                for (int r = t + 1; r < 3; r++) {
+                    s[r].z0 = s[r].z0 - T(diz);
+                    s[r].z1 = s[r].z1 - T(diz);
+                    s[r].k += diz;
+                }
+                n = 4;
+                break;
+            }
+        }
+        return n;
+    }
+    }
+}
+
+} // namespace osg

@@ -1,0 +1,404 @@
+// push_plain.cu -- particle push + charge-conserving current deposition on the reference
+// particle layout (ix(dim,N), x(dim,N), p(3,N), q(N)) with one thread per particle and
+// global atomic current accumulation: the "plain" GPU form, in float and double.
+//
+// Reference algorithm: FNAME(vadvance_deposit_{1d,2d,3d}_sN), source/simd/
+// os-spec-push-avx2d.c:263-475 (1D), :481-775 (2D), :1127-1467 (3D) and the deposits
+// source/simd/os-spec-current-avx2d.c:189-278, :476-613, :854-1013.  Each thread gathers E and
+// B with the staggered B-spline stencil, does the Boris update, moves the particle, trims it
+// back into [-0.5, 0.5) of its new cell, splits the trajectory at cell faces and deposits the
+// charge-conserving current of every segment.
+//
+// Memory safety: a particle whose cell index would put any stencil point outside the arrays
+// is not pushed; the kernel raises OSG_STATUS_RANGE in the status word instead.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "pic_math.cuh"
+#include "push_plain.cuh"
+
+namespace osg {
+
+template <typename T, int ORD>
+__device__ __forceinline__ void deposit1(T *pj, T jn, T q, T x0, T x1, T vy, T vz, int i)
+{
+    constexpr int NP = ORD + 1;
+    T s0[NP], s1[NP], wl[ORD];
+    spline<ORD>(x0, s0);
+    spline<ORD>(x1, s1);
+    T qnx = q * jn, qvy = q * vy, qvz = q * vz;
+    long_weights<ORD>(qnx, x0, x1, wl);
+    T *p = pj + 3 * i;
+#pragma unroll
+    for (int k = 0; k < ORD; k++) atomicAdd(p + 3 * k, wl[k]);
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        T wp = T(0.5) * (s0[k] + s1[k]);
+        atomicAdd(p + 3 * k + 1, qvy * wp);
+        atomicAdd(p + 3 * k + 2, qvz * wp);
+    }
+}
+
+template <typename T, int ORD>
+__device__ __forceinline__ void deposit2(T *pj, long Dy, T jn0, T jn1, T q, const Seg2<T> &s)
+{
+    constexpr int NP = ORD + 1;
+    T s0x[NP], s1x[NP], s0y[NP], s1y[NP], wl1[ORD], wl2[ORD], wp1[NP], wp2[NP];
+    spline<ORD>(s.x0, s0x);
+    spline<ORD>(s.x1, s1x);
+    spline<ORD>(s.y0, s0y);
+    spline<ORD>(s.y1, s1y);
+    T qnx = q * jn0, qny = q * jn1;
+    T qvz = (q * s.vz) * T(1.0 / 3.0);
+    long_weights<ORD>(qnx, s.x0, s.x1, wl1);
+    long_weights<ORD>(qny, s.y0, s.y1, wl2);
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        wp1[k] = s0y[k] + s1y[k];
+        wp2[k] = s0x[k] + s1x[k];
+    }
+    T *p = pj + 3L * s.i + Dy * s.j;
+#pragma unroll
+    for (int k2 = 0; k2 < NP; k2++)
+#pragma unroll
+        for (int k1 = 0; k1 < ORD; k1++) atomicAdd(p + 3 * k1 + Dy * k2, wl1[k1] * wp1[k2]);
+#pragma unroll
+    for (int k2 = 0; k2 < ORD; k2++)
+#pragma unroll
+        for (int k1 = 0; k1 < NP; k1++) atomicAdd(p + 3 * k1 + Dy * k2 + 1, wl2[k2] * wp2[k1]);
+#pragma unroll
+    for (int k2 = 0; k2 < NP; k2++)
+#pragma unroll
+        for (int k1 = 0; k1 < NP; k1++) {
+            T t1 = fmaR(s1y[k2], s1x[k1], s0x[k1] * s0y[k2]);
+            T t2 = fmaR(s0y[k2], s1x[k1], s0x[k1] * s1y[k2]);
+            t1 = fmaR(t2, T(0.5), t1);
+            atomicAdd(p + 3 * k1 + Dy * k2 + 2, qvz * t1);
+        }
+}
+
+template <typename T, int ORD>
+__device__ __forceinline__ void deposit3(T *pj, long Dy, long Dz, T jn0, T jn1, T jn2, T q,
+                                         const Seg3<T> &s)
+{
+    constexpr int NP = ORD + 1;
+    T s0x[NP], s1x[NP], s0y[NP], s1y[NP], s0z[NP], s1z[NP], wl1[ORD], wl2[ORD], wl3[ORD];
+    spline<ORD>(s.x0, s0x);
+    spline<ORD>(s.x1, s1x);
+    spline<ORD>(s.y0, s0y);
+    spline<ORD>(s.y1, s1y);
+    spline<ORD>(s.z0, s0z);
+    spline<ORD>(s.z1, s1z);
+    long_weights<ORD>(q * jn0, s.x0, s.x1, wl1);
+    long_weights<ORD>(q * jn1, s.y0, s.y1, wl2);
+    long_weights<ORD>(q * jn2, s.z0, s.z1, wl3);
+    T *p = pj + 3L * s.i + Dy * s.j + Dz * s.k;
+    // perpendicular weights: wp(b, a) = s0a s0b + s1a s1b + (s0a s1b + s1a s0b) / 2
+#pragma unroll
+    for (int k3 = 0; k3 < NP; k3++)
+#pragma unroll
+        for (int k2 = 0; k2 < NP; k2++) {
+            T t1 = s0y[k2] * s0z[k3], t2 = s0y[k2] * s1z[k3];
+            t1 = fmaR(s1y[k2], s1z[k3], t1);
+            t2 = fmaR(s1y[k2], s0z[k3], t2);
+            T wp1 = fmaR(T(0.5), t2, t1);
+#pragma unroll
+            for (int k1 = 0; k1 < ORD; k1++)
+                atomicAdd(p + 3 * k1 + Dy * k2 + Dz * k3, wl1[k1] * wp1);
+        }
+#pragma unroll
+    for (int k3 = 0; k3 < NP; k3++)
+#pragma unroll
+        for (int k1 = 0; k1 < NP; k1++) {
+            T t1 = s0x[k1] * s0z[k3], t2 = s0x[k1] * s1z[k3];
+            t1 = fmaR(s1x[k1], s1z[k3], t1);
+            t2 = fmaR(s1x[k1], s0z[k3], t2);
+            T wp2 = fmaR(T(0.5), t2, t1);
+#pragma unroll
+            for (int k2 = 0; k2 < ORD; k2++)
+                atomicAdd(p + 3 * k1 + Dy * k2 + Dz * k3 + 1, wl2[k2] * wp2);
+        }
+#pragma unroll
+    for (int k2 = 0; k2 < NP; k2++)
+#pragma unroll
+        for (int k1 = 0; k1 < NP; k1++) {
+            T t1 = s0x[k1] * s0y[k2], t2 = s0x[k1] * s1y[k2];
+            t1 = fmaR(s1x[k1], s1y[k2], t1);
+            t2 = fmaR(s1x[k1], s0y[k2], t2);
+            T wp3 = fmaR(T(0.5), t2, t1);
+#pragma unroll
+            for (int k3 = 0; k3 < ORD; k3++)
+                atomicAdd(p + 3 * k1 + Dy * k2 + Dz * k3 + 2, wl3[k3] * wp3);
+        }
+}
+
+// A cell index c (Fortran, 1-based) is safe when every gather point and every deposit point
+// of the segments that can start from it lies inside [0, size) of the array:
+// points c - OFS .. c + NP - OFS + 1 map to positions c - OFS - 1 + off .. c + NP - OFS + off.
+template <int ORD>
+__device__ __forceinline__ bool cell_ok(int c, int off, int size)
+{
+    constexpr int NP = ORD + 1, OFS = Stencil<ORD>::OFS;
+    return c - OFS - 1 + off >= 0 && c + NP - OFS + off < size;
+}
+
+// periodic single-node wrap of a cell index (source/spec/os-spec-boundary.f03:1280-1290);
+// n = 0 leaves the index as pushed (the reference kernel itself does not wrap)
+__device__ __forceinline__ int wrap_cell(int c, int n)
+{
+    if (n > 0) {
+        if (c < 1) c += n;
+        else if (c > n) c -= n;
+    }
+    return c;
+}
+
+template <typename T, int DIM, int ORD>
+__global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
+{
+    constexpr int NP = ORD + 1;
+    const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    double my_ene = 0.0;
+    if (p < a.np) {
+        int c[DIM];
+        T x0[DIM];
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < DIM; d++) {
+            c[d] = a.ix[DIM * p + d];
+            x0[d] = a.x[DIM * p + d];
+            ok = ok && cell_ok<ORD>(c[d], a.emf_off[d], a.emf_size[d]) &&
+                 cell_ok<ORD>(c[d], a.j_off[d], a.j_size[d]);
+        }
+        if (!ok) {
+            atomicOr(a.status, OSG_STATUS_RANGE);
+        } else {
+            const T q = a.q[p];
+            T w[DIM][NP], wh[DIM][NP];
+            int ch[DIM];
+#pragma unroll
+            for (int d = 0; d < DIM; d++) {
+                spline<ORD>(x0[d], w[d]);
+                const bool neg = x0[d] < T(0);
+                ch[d] = c[d] - (neg ? 1 : 0);
+                spline_h<ORD>(x0[d], neg ? T(1) : T(0), wh[d]);
+            }
+            const T *__restrict__ e0 = a.efield;
+            const T *__restrict__ b0 = a.bfield;
+            T E1 = T(0), E2 = T(0), E3 = T(0), B1 = T(0), B2 = T(0), B3 = T(0);
+            if constexpr (DIM == 1) {
+#pragma unroll
+                for (int k = 0; k < NP; k++) {
+                    E1 = fmaR(__ldg(e0 + 3 * (ch[0] + k) + 0), wh[0][k], E1);
+                    E2 = fmaR(__ldg(e0 + 3 * (c[0] + k) + 1), w[0][k], E2);
+                    E3 = fmaR(__ldg(e0 + 3 * (c[0] + k) + 2), w[0][k], E3);
+                }
+#pragma unroll
+                for (int k = 0; k < NP; k++) {
+                    B1 = fmaR(__ldg(b0 + 3 * (c[0] + k) + 0), w[0][k], B1);
+                    B2 = fmaR(__ldg(b0 + 3 * (ch[0] + k) + 1), wh[0][k], B2);
+                    B3 = fmaR(__ldg(b0 + 3 * (ch[0] + k) + 2), wh[0][k], B3);
+                }
+            } else if constexpr (DIM == 2) {
+                const long Dy = a.emf_Dy;
+#pragma unroll
+                for (int k2 = 0; k2 < NP; k2++) {
+                    T f1 = T(0), f2 = T(0), f3 = T(0);
+#pragma unroll
+                    for (int k1 = 0; k1 < NP; k1++) {
+                        f1 = fmaR(__ldg(e0 + 3L * (ch[0] + k1) + Dy * (c[1] + k2) + 0), wh[0][k1], f1);
+                        f2 = fmaR(__ldg(e0 + 3L * (c[0] + k1) + Dy * (ch[1] + k2) + 1), w[0][k1], f2);
+                        f3 = fmaR(__ldg(e0 + 3L * (c[0] + k1) + Dy * (c[1] + k2) + 2), w[0][k1], f3);
+                    }
+                    E1 = fmaR(f1, w[1][k2], E1);
+                    E2 = fmaR(f2, wh[1][k2], E2);
+                    E3 = fmaR(f3, w[1][k2], E3);
+                }
+#pragma unroll
+                for (int k2 = 0; k2 < NP; k2++) {
+                    T f1 = T(0), f2 = T(0), f3 = T(0);
+#pragma unroll
+                    for (int k1 = 0; k1 < NP; k1++) {
+                        f1 = fmaR(__ldg(b0 + 3L * (c[0] + k1) + Dy * (ch[1] + k2) + 0), w[0][k1], f1);
+                        f2 = fmaR(__ldg(b0 + 3L * (ch[0] + k1) + Dy * (c[1] + k2) + 1), wh[0][k1], f2);
+                        f3 = fmaR(__ldg(b0 + 3L * (ch[0] + k1) + Dy * (ch[1] + k2) + 2), wh[0][k1], f3);
+                    }
+                    B1 = fmaR(f1, wh[1][k2], B1);
+                    B2 = fmaR(f2, w[1][k2], B2);
+                    B3 = fmaR(f3, wh[1][k2], B3);
+                }
+            } else {
+                const long Dy = a.emf_Dy, Dz = a.emf_Dz;
+#pragma unroll
+                for (int k3 = 0; k3 < NP; k3++) {
+                    T g1 = T(0), g2 = T(0), g3 = T(0);
+#pragma unroll
+                    for (int k2 = 0; k2 < NP; k2++) {
+                        T f1 = T(0), f2 = T(0), f3 = T(0);
+#pragma unroll
+                        for (int k1 = 0; k1 < NP; k1++) {
+                            f1 = fmaR(__ldg(e0 + 3L * (ch[0] + k1) + Dy * (c[1] + k2) + Dz * (c[2] + k3) + 0), wh[0][k1], f1);
+                            f2 = fmaR(__ldg(e0 + 3L * (c[0] + k1) + Dy * (ch[1] + k2) + Dz * (c[2] + k3) + 1), w[0][k1], f2);
+                            f3 = fmaR(__ldg(e0 + 3L * (c[0] + k1) + Dy * (c[1] + k2) + Dz * (ch[2] + k3) + 2), w[0][k1], f3);
+                        }
+                        g1 = fmaR(f1, w[1][k2], g1);
+                        g2 = fmaR(f2, wh[1][k2], g2);
+                        g3 = fmaR(f3, w[1][k2], g3);
+                    }
+                    E1 = fmaR(g1, w[2][k3], E1);
+                    E2 = fmaR(g2, w[2][k3], E2);
+                    E3 = fmaR(g3, wh[2][k3], E3);
+                }
+#pragma unroll
+                for (int k3 = 0; k3 < NP; k3++) {
+                    T g1 = T(0), g2 = T(0), g3 = T(0);
+#pragma unroll
+                    for (int k2 = 0; k2 < NP; k2++) {
+                        T f1 = T(0), f2 = T(0), f3 = T(0);
+#pragma unroll
+                        for (int k1 = 0; k1 < NP; k1++) {
+                            f1 = fmaR(__ldg(b0 + 3L * (c[0] + k1) + Dy * (ch[1] + k2) + Dz * (ch[2] + k3) + 0), w[0][k1], f1);
+                            f2 = fmaR(__ldg(b0 + 3L * (ch[0] + k1) + Dy * (c[1] + k2) + Dz * (ch[2] + k3) + 1), wh[0][k1], f2);
+                            f3 = fmaR(__ldg(b0 + 3L * (ch[0] + k1) + Dy * (ch[1] + k2) + Dz * (c[2] + k3) + 2), wh[0][k1], f3);
+                        }
+                        g1 = fmaR(f1, wh[1][k2], g1);
+                        g2 = fmaR(f2, w[1][k2], g2);
+                        g3 = fmaR(f3, wh[1][k2], g3);
+                    }
+                    B1 = fmaR(g1, wh[2][k3], B1);
+                    B2 = fmaR(g2, wh[2][k3], B2);
+                    B3 = fmaR(g3, w[2][k3], B3);
+                }
+            }
+            T u1 = a.u[3 * p], u2 = a.u[3 * p + 1], u3 = a.u[3 * p + 2];
+            const T ene = boris(a.tem, E1, E2, E3, B1, B2, B3, u1, u2, u3);
+            a.u[3 * p] = u1;
+            a.u[3 * p + 1] = u2;
+            a.u[3 * p + 2] = u3;
+            const T rg = rgamma(u1, u2, u3);
+            my_ene = (double)q * (double)ene;
+            const T v1 = u1 * rg, v2 = u2 * rg, v3 = u3 * rg;
+            if constexpr (DIM == 1) {
+                T x1 = fmaR(v1, a.dtdx[0], x0[0]);
+                int dix = trim(x1);
+                a.x[p] = x1 - T(dix);
+                a.ix[p] = wrap_cell(c[0] + dix, a.wrap[0]);
+                if (dix == 0) {
+                    deposit1<T, ORD>(a.j, a.jn[0], q, x0[0], x1, v2, v3, c[0]);
+                } else {
+                    T xint = T(0.5 * dix);
+                    T delta = (xint - x0[0]) / (x1 - x0[0]);
+                    deposit1<T, ORD>(a.j, a.jn[0], q, x0[0], xint, v2 * delta, v3 * delta, c[0]);
+                    deposit1<T, ORD>(a.j, a.jn[0], q, -xint, x1 - T(dix), v2 * (T(1) - delta),
+                                     v3 * (T(1) - delta), c[0] + dix);
+                }
+            } else if constexpr (DIM == 2) {
+                T x1 = fmaR(v1, a.dtdx[0], x0[0]);
+                T y1 = fmaR(v2, a.dtdx[1], x0[1]);
+                int dix = trim(x1), diy = trim(y1);
+                a.x[2 * p] = x1 - T(dix);
+                a.x[2 * p + 1] = y1 - T(diy);
+                a.ix[2 * p] = wrap_cell(c[0] + dix, a.wrap[0]);
+                a.ix[2 * p + 1] = wrap_cell(c[1] + diy, a.wrap[1]);
+                Seg2<T> s[3];
+                s[0].x0 = x0[0]; s[0].x1 = x1; s[0].y0 = x0[1]; s[0].y1 = y1;
+                s[0].vz = v3; s[0].i = c[0]; s[0].j = c[1];
+                const int ns = split2(s, dix, diy);
+                for (int t = 0; t < ns; t++)
+                    deposit2<T, ORD>(a.j, a.j_Dy, a.jn[0], a.jn[1], q, s[t]);
+            } else {
+                T x1 = fmaR(v1, a.dtdx[0], x0[0]);
+                T y1 = fmaR(v2, a.dtdx[1], x0[1]);
+                T z1 = fmaR(v3, a.dtdx[2], x0[2]);
+                int dix = trim(x1), diy = trim(y1), diz = trim(z1);
+                a.x[3 * p] = x1 - T(dix);
+                a.x[3 * p + 1] = y1 - T(diy);
+                a.x[3 * p + 2] = z1 - T(diz);
+                a.ix[3 * p] = wrap_cell(c[0] + dix, a.wrap[0]);
+                a.ix[3 * p + 1] = wrap_cell(c[1] + diy, a.wrap[1]);
+                a.ix[3 * p + 2] = wrap_cell(c[2] + diz, a.wrap[2]);
+                Seg3<T> s[4];
+                s[0].x0 = x0[0]; s[0].x1 = x1; s[0].y0 = x0[1]; s[0].y1 = y1;
+                s[0].z0 = x0[2]; s[0].z1 = z1; s[0].i = c[0]; s[0].j = c[1]; s[0].k = c[2];
+                const int ns = split3(s, dix, diy, diz);
+                for (int t = 0; t < ns; t++)
+                    deposit3<T, ORD>(a.j, a.j_Dy, a.j_Dz, a.jn[0], a.jn[1], a.jn[2], q, s[t]);
+            }
+        }
+    }
+    const double tot = block_sum(my_ene);
+    if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.ene, tot);
+}
+
+template <typename T>
+PlainPushArgs<T> make_plain_args(int dim, int order, int *ix, T *x, T *u, const T *q, long np,
+                                 T rqm, const T *e, const T *b, const int *emf_size,
+                                 const int *emf_off, T *j, const int *j_size, const int *j_off,
+                                 const double *dx, double dt, double *d_ene, int *d_status)
+{
+    PlainPushArgs<T> a;
+    const int OFS = order == 1 ? 1 : (order == 2 ? 2 : (order == 3 ? 2 : 3));
+    a.ix = ix; a.x = x; a.u = u; a.q = q; a.np = np;
+    a.tem = (T)(0.5 * dt / (double)rqm);
+    long eDy = 3L * emf_size[0], eDz = dim > 2 ? eDy * emf_size[1] : 0;
+    long jDy = 3L * j_size[0], jDz = dim > 2 ? jDy * j_size[1] : 0;
+    long eo = (emf_off[0] - OFS) * 3L, jo = (j_off[0] - OFS) * 3L;
+    if (dim > 1) { eo += (emf_off[1] - OFS) * eDy; jo += (j_off[1] - OFS) * jDy; }
+    if (dim > 2) { eo += (emf_off[2] - OFS) * eDz; jo += (j_off[2] - OFS) * jDz; }
+    a.efield = e + eo;
+    a.bfield = b + eo;
+    a.j = j + jo;
+    a.emf_Dy = eDy; a.emf_Dz = eDz; a.j_Dy = jDy; a.j_Dz = jDz;
+    for (int d = 0; d < 3; d++) {
+        a.emf_off[d] = d < dim ? emf_off[d] : 0;
+        a.emf_size[d] = d < dim ? emf_size[d] : 1;
+        a.j_off[d] = d < dim ? j_off[d] : 0;
+        a.j_size[d] = d < dim ? j_size[d] : 1;
+        a.dtdx[d] = d < dim ? (T)(dt / dx[d]) : T(0);
+        const double div = dim == 1 ? 1.0 : (dim == 2 ? 2.0 : 3.0);
+        a.jn[d] = d < dim ? (T)(dx[d] / dt / div) : T(0);
+    }
+    a.wrap[0] = a.wrap[1] = a.wrap[2] = 0;
+    a.ene = d_ene;
+    a.status = d_status;
+    return a;
+}
+
+template <typename T, int DIM, int ORD>
+static void launch_one(const PlainPushArgs<T> &a, cudaStream_t st)
+{
+    if (a.np <= 0) return;
+    k_push_plain<T, DIM, ORD><<<blocks_for(a.np, 256), 256, 0, st>>>(a);
+}
+
+template <typename T>
+int launch_plain_push(int dim, int order, const PlainPushArgs<T> &a, cudaStream_t st)
+{
+#define OSG_CASE(D, O)                                                                        \
+    if (dim == D && order == O) {                                                             \
+        launch_one<T, D, O>(a, st);                                                           \
+        return OSG_OK;                                                                        \
+    }
+    OSG_CASE(1, 1) OSG_CASE(1, 2) OSG_CASE(1, 3) OSG_CASE(1, 4)
+    OSG_CASE(2, 1) OSG_CASE(2, 2) OSG_CASE(2, 3) OSG_CASE(2, 4)
+    OSG_CASE(3, 1) OSG_CASE(3, 2) OSG_CASE(3, 3) OSG_CASE(3, 4)
+#undef OSG_CASE
+    set_error("unsupported dim %d / order %d", dim, order);
+    return OSG_ERR_ARG;
+}
+
+template PlainPushArgs<float> make_plain_args<float>(int, int, int *, float *, float *,
+                                                     const float *, long, float, const float *,
+                                                     const float *, const int *, const int *,
+                                                     float *, const int *, const int *,
+                                                     const double *, double, double *, int *);
+template PlainPushArgs<double> make_plain_args<double>(int, int, int *, double *, double *,
+                                                       const double *, long, double,
+                                                       const double *, const double *,
+                                                       const int *, const int *, double *,
+                                                       const int *, const int *,
+                                                       const double *, double, double *, int *);
+template int launch_plain_push<float>(int, int, const PlainPushArgs<float> &, cudaStream_t);
+template int launch_plain_push<double>(int, int, const PlainPushArgs<double> &, cudaStream_t);
+
+} // namespace osg

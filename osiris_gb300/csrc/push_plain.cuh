@@ -1,0 +1,42 @@
+// push_plain.cuh -- launch interface of the plain (one thread per particle) push + deposit.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace osg {
+
+// bits of the device status word shared by all kernels of a launch sequence
+enum : int {
+    OSG_STATUS_RANGE = 1,     // a particle cell index would reach outside the arrays
+    OSG_STATUS_OVERFLOW = 2,  // a tile had no free particle slot
+    OSG_STATUS_NAN = 4,       // non-finite value detected
+};
+
+template <typename T> struct PlainPushArgs {
+    int *ix;
+    T *x, *u;
+    const T *q;
+    long np;
+    T tem;                 // dt / (2 rqm), rounded from double as the reference does
+    T dtdx[3];             // dt / dx
+    T jn[3];               // current normalisation dx / dt / dim
+    const T *efield;       // shifted so that (cell, k) indexes the stencil directly
+    const T *bfield;
+    T *j;
+    long emf_Dy, emf_Dz, j_Dy, j_Dz;
+    int emf_off[3], emf_size[3], j_off[3], j_size[3];
+    int wrap[3];           // > 0: periodic wrap of the stored cell index into [1, wrap[d]]
+    double *ene;           // device accumulator (incremented)
+    int *status;           // device status word (OR of OSG_STATUS_*)
+};
+
+template <typename T>
+PlainPushArgs<T> make_plain_args(int dim, int order, int *ix, T *x, T *u, const T *q, long np,
+                                 T rqm, const T *e, const T *b, const int *emf_size,
+                                 const int *emf_off, T *j, const int *j_size, const int *j_off,
+                                 const double *dx, double dt, double *d_ene, int *d_status);
+
+template <typename T>
+int launch_plain_push(int dim, int order, const PlainPushArgs<T> &a, cudaStream_t st);
+
+} // namespace osg

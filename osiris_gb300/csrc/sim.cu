@@ -1,0 +1,749 @@
+// sim.cu -- device-resident simulation handle (osg_sim_*): particles, fields and current stay
+// in HBM; one call advances N time steps, each step replayed from a captured CUDA graph.
+//
+// Phase order of one step, as iter_sim (source/os-simulation.f03:498-666) on one periodic node:
+//   1. E, B guard replace          emf%update_boundary (:561) -> update_periodic_vdf replace
+//   2. J = 0; push + deposit       part%advance_deposit (:588), all species
+//   3. periodic particle wrap      part%update_boundary (:593) -- fused into the push
+//   4. cell sort every n_sort      sort_collide (:638) (plain engine) / tile migration, every
+//                                  step, fused into the push (tiled engine)
+//   5. J guard fold                jay%update_boundary (:652)
+//   6. Yee B/2, E, B/2             emf%advance (:661)
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "fields.cuh"
+#include "push_plain.cuh"
+#include "tiled.cuh"
+
+namespace osg {
+
+struct PlainSpecies {
+    int *ix = nullptr;
+    void *x = nullptr, *u = nullptr, *q = nullptr;
+};
+
+} // namespace osg
+
+struct osg_sim {
+    osg_config cfg;
+    osg::GridDesc g;
+    int gl = 0, gu = 0;
+    int esz = 4;                 // bytes per real
+    cudaStream_t st = nullptr;
+    void *e = nullptr, *b = nullptr, *j = nullptr;
+    double *d_ene = nullptr;     // [OSG_MAX_SPECIES] kinetic accumulators of the last step
+    int *d_status = nullptr;
+    double *d_diag = nullptr;    // 16 doubles of diagnostic scratch
+    double *d_rho = nullptr, *d_rho0 = nullptr;
+    long step_n = 0;
+    std::vector<double> rqm;
+    std::vector<long> np;
+    std::vector<osg::PlainSpecies> plain;
+    // plain-engine sort scratch
+    int *d_cell_cnt = nullptr;
+    int *d_scan_tmp = nullptr;
+    void *d_sort_buf = nullptr;
+    size_t sort_buf_bytes = 0;
+    // tiled engine
+    osg::TiledState *tiled = nullptr;
+    // graphs: [parity][sort]
+    cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    bool graphs_dirty = true;
+    int launches_per_step = 0;
+};
+
+namespace osg {
+
+static const int MAX_SPECIES = 16;
+
+// ------------------------------------------------------------------------ cell sort (plain)
+
+template <int DIM>
+__global__ void k_cell_count(const int *__restrict__ ix, long np, GridDesc g, int *cnt)
+{
+    OSG_GRID_LOOP(p, np)
+    {
+        long key = ix[DIM * p] - 1;
+        if (DIM > 1) key += (long)g.nx[0] * (ix[DIM * p + 1] - 1);
+        if (DIM > 2) key += (long)g.nx[0] * g.nx[1] * (ix[DIM * p + 2] - 1);
+        atomicAdd(cnt + key, 1);
+    }
+}
+
+// exclusive scan of n ints in place, three kernels: per-block scan, scan of block sums,
+// add back
+__global__ void k_scan_block(int *a, long n, int *block_sums)
+{
+    __shared__ int ws[32];
+    const long i = (long)blockIdx.x * 1024 + threadIdx.x;
+    int v = i < n ? a[i] : 0;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int s = ws[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        ws[lane] = s;
+    }
+    __syncthreads();
+    const int incl = x + (w > 0 ? ws[w - 1] : 0);
+    if (i < n) a[i] = incl - v;
+    if (threadIdx.x == 1023) block_sums[blockIdx.x] = incl;
+}
+
+__global__ void k_scan_sums(int *s, int nb)
+{
+    // single block of 1024 threads, sequential over chunks
+    __shared__ int ws[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nb; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int v = i < nb ? s[i] : 0;
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) ws[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int t = ws[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            ws[lane] = t;
+        }
+        __syncthreads();
+        const int incl = x + (w > 0 ? ws[w - 1] : 0);
+        const int c = carry;
+        if (i < nb) s[i] = c + incl - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = c + incl;
+        __syncthreads();
+    }
+}
+
+__global__ void k_scan_add(int *a, long n, const int *block_sums)
+{
+    const long i = (long)blockIdx.x * 1024 + threadIdx.x;
+    if (i < n && blockIdx.x > 0) a[i] += block_sums[blockIdx.x];
+}
+
+void exclusive_scan(int *a, long n, int *tmp, cudaStream_t st)
+{
+    const int nb = (int)((n + 1023) / 1024);
+    k_scan_block<<<nb, 1024, 0, st>>>(a, n, tmp);
+    k_scan_sums<<<1, 1024, 0, st>>>(tmp, nb);
+    k_scan_add<<<nb, 1024, 0, st>>>(a, n, tmp);
+}
+
+template <typename T, int DIM>
+__global__ void k_cell_scatter(const int *__restrict__ ix, const T *__restrict__ x,
+                               const T *__restrict__ u, const T *__restrict__ q, long np,
+                               GridDesc g, int *next, int *ix2, T *x2, T *u2, T *q2)
+{
+    OSG_GRID_LOOP(p, np)
+    {
+        long key = ix[DIM * p] - 1;
+        if (DIM > 1) key += (long)g.nx[0] * (ix[DIM * p + 1] - 1);
+        if (DIM > 2) key += (long)g.nx[0] * g.nx[1] * (ix[DIM * p + 2] - 1);
+        const long s = atomicAdd(next + key, 1);
+        for (int d = 0; d < DIM; d++) {
+            ix2[DIM * s + d] = ix[DIM * p + d];
+            x2[DIM * s + d] = x[DIM * p + d];
+        }
+        u2[3 * s] = u[3 * p];
+        u2[3 * s + 1] = u[3 * p + 1];
+        u2[3 * s + 2] = u[3 * p + 2];
+        q2[s] = q[p];
+    }
+}
+
+long ncells(const GridDesc &g) { return (long)g.nx[0] * g.nx[1] * g.nx[2]; }
+
+template <typename T>
+static int sort_species(osg_sim *s, int k, cudaStream_t st)
+{
+    const long np = s->np[k];
+    if (np <= 0) return OSG_OK;
+    const int dim = s->cfg.dim;
+    PlainSpecies &p = s->plain[k];
+    const long nc = ncells(s->g);
+    char *buf = (char *)s->d_sort_buf;
+    int *ix2 = (int *)buf;
+    T *x2 = (T *)(buf + sizeof(int) * dim * np);
+    T *u2 = x2 + dim * np;
+    T *q2 = u2 + 3 * np;
+    OSG_CUDA(cudaMemsetAsync(s->d_cell_cnt, 0, sizeof(int) * nc, st));
+    unsigned nb = blocks_for(np, 256);
+    if (nb > 8192) nb = 8192;
+    if (dim == 2) k_cell_count<2><<<nb, 256, 0, st>>>(p.ix, np, s->g, s->d_cell_cnt);
+    else k_cell_count<3><<<nb, 256, 0, st>>>(p.ix, np, s->g, s->d_cell_cnt);
+    exclusive_scan(s->d_cell_cnt, nc, s->d_scan_tmp, st);
+    if (dim == 2)
+        k_cell_scatter<T, 2><<<nb, 256, 0, st>>>(p.ix, (T *)p.x, (T *)p.u, (T *)p.q, np, s->g,
+                                                 s->d_cell_cnt, ix2, x2, u2, q2);
+    else
+        k_cell_scatter<T, 3><<<nb, 256, 0, st>>>(p.ix, (T *)p.x, (T *)p.u, (T *)p.q, np, s->g,
+                                                 s->d_cell_cnt, ix2, x2, u2, q2);
+    OSG_CUDA(cudaMemcpyAsync(p.ix, ix2, sizeof(int) * dim * np, cudaMemcpyDeviceToDevice, st));
+    OSG_CUDA(cudaMemcpyAsync(p.x, x2, sizeof(T) * dim * np, cudaMemcpyDeviceToDevice, st));
+    OSG_CUDA(cudaMemcpyAsync(p.u, u2, sizeof(T) * 3 * np, cudaMemcpyDeviceToDevice, st));
+    OSG_CUDA(cudaMemcpyAsync(p.q, q2, sizeof(T) * np, cudaMemcpyDeviceToDevice, st));
+    return OSG_OK;
+}
+
+// ------------------------------------------------------------------------ one step
+
+struct PhaseEvents {
+    cudaEvent_t ev[8];
+};
+
+template <typename T>
+static int enqueue_step(osg_sim *s, int parity, bool with_sort, PhaseEvents *pe)
+{
+    cudaStream_t st = s->st;
+    const osg_config &c = s->cfg;
+    const int ns = (int)s->np.size();
+    int emf_size[3], emf_off[3];
+    for (int d = 0; d < 3; d++) {
+        emf_size[d] = s->g.size[d];
+        emf_off[d] = s->g.gcl[d];
+    }
+    int launches = 0;
+    // the single-precision reference pushes with dt rounded to p_k_part
+    // (dtcycle = real(dt, p_k_part), source/spec/os-spec-vpush.f03:365)
+    const double push_dt = sizeof(T) == 4 ? (double)(float)c.dt : c.dt;
+    if (pe) OSG_CUDA(cudaEventRecord(pe->ev[0], st));
+    periodic_update<T>(s->g, (T *)s->e, 0, st);
+    periodic_update<T>(s->g, (T *)s->b, 0, st);
+    launches += 2 * c.dim;
+    if (pe) OSG_CUDA(cudaEventRecord(pe->ev[1], st));
+    OSG_CUDA(cudaMemsetAsync(s->j, 0, (size_t)s->esz * 3 * s->g.npoints(), st));
+    OSG_CUDA(cudaMemsetAsync(s->d_ene, 0, sizeof(double) * MAX_SPECIES, st));
+    if (c.engine == OSG_ENGINE_TILED) {
+        int rc = tiled_push(s->tiled, parity, (const float *)s->e, (const float *)s->b,
+                            (float *)s->j, s->d_ene, s->d_status, st, &launches);
+        if (rc) return rc;
+    } else {
+        for (int k = 0; k < ns; k++) {
+            if (s->np[k] <= 0) continue;
+            PlainSpecies &p = s->plain[k];
+            PlainPushArgs<T> a = make_plain_args<T>(
+                c.dim, c.order, p.ix, (T *)p.x, (T *)p.u, (const T *)p.q, s->np[k],
+                (T)s->rqm[k], (const T *)s->e, (const T *)s->b, emf_size, emf_off, (T *)s->j,
+                emf_size, emf_off, c.dx, push_dt, s->d_ene + k, s->d_status);
+            for (int d = 0; d < c.dim; d++) a.wrap[d] = c.nx[d];
+            int rc = launch_plain_push<T>(c.dim, c.order, a, st);
+            if (rc) return rc;
+            launches++;
+        }
+    }
+    if (pe) OSG_CUDA(cudaEventRecord(pe->ev[2], st));
+    if (with_sort && c.engine == OSG_ENGINE_PLAIN) {
+        for (int k = 0; k < ns; k++) {
+            int rc = sort_species<T>(s, k, st);
+            if (rc) return rc;
+            launches += 5;
+        }
+    }
+    if (pe) OSG_CUDA(cudaEventRecord(pe->ev[3], st));
+    periodic_update<T>(s->g, (T *)s->j, 1, st);
+    launches += c.dim;
+    if (pe) OSG_CUDA(cudaEventRecord(pe->ev[4], st));
+    yee_advance<T>(s->g, (T *)s->e, (T *)s->b, (const T *)s->j, c.dx, c.dt, st);
+    launches += 3;
+    if (pe) OSG_CUDA(cudaEventRecord(pe->ev[5], st));
+    OSG_CUDA(cudaGetLastError());
+    s->launches_per_step = launches;
+    return OSG_OK;
+}
+
+static int enqueue_step_any(osg_sim *s, int parity, bool with_sort, PhaseEvents *pe)
+{
+    return s->cfg.precision == 32 ? enqueue_step<float>(s, parity, with_sort, pe)
+                                  : enqueue_step<double>(s, parity, with_sort, pe);
+}
+
+static void drop_graphs(osg_sim *s)
+{
+    for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++)
+            if (s->gexec[a][b]) {
+                cudaGraphExecDestroy(s->gexec[a][b]);
+                s->gexec[a][b] = nullptr;
+            }
+    s->graphs_dirty = false;
+}
+
+static int get_graph(osg_sim *s, int parity, int sort, cudaGraphExec_t *out)
+{
+    if (s->graphs_dirty) drop_graphs(s);
+    if (!s->gexec[parity][sort]) {
+        cudaGraph_t gr;
+        OSG_CUDA(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_step_any(s, parity, sort != 0, nullptr);
+        cudaError_t ce = cudaStreamEndCapture(s->st, &gr);
+        if (rc) {
+            if (ce == cudaSuccess) cudaGraphDestroy(gr);
+            return rc;
+        }
+        OSG_CUDA(ce);
+        cudaError_t ie = cudaGraphInstantiate(&s->gexec[parity][sort], gr, 0);
+        cudaGraphDestroy(gr);
+        OSG_CUDA(ie);
+    }
+    *out = s->gexec[parity][sort];
+    return OSG_OK;
+}
+
+static bool sort_due(const osg_sim *s, long n)
+{
+    return s->cfg.engine == OSG_ENGINE_PLAIN && s->cfg.n_sort > 0 && n > 0 &&
+           (n % s->cfg.n_sort) == 0;
+}
+
+static int check_status(osg_sim *s)
+{
+    int h = 0;
+    OSG_CUDA(cudaMemcpyAsync(&h, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    OSG_CUDA(cudaStreamSynchronize(s->st));
+    if (h & OSG_STATUS_OVERFLOW) {
+        set_error("a tile ran out of particle slots (raise osg_config.capacity)");
+        return OSG_ERR_OVERFLOW;
+    }
+    if (h & OSG_STATUS_RANGE) {
+        set_error("a particle cell index left the grid");
+        return OSG_ERR_RANGE;
+    }
+    return OSG_OK;
+}
+
+template <typename T> static T *dalloc(size_t n, int *rc)
+{
+    void *p = nullptr;
+    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
+        set_error("cudaMalloc of %zu bytes failed", n * sizeof(T));
+        *rc = OSG_ERR_NOMEM;
+        return nullptr;
+    }
+    return (T *)p;
+}
+
+} // namespace osg
+
+using namespace osg;
+
+extern "C" {
+
+int osg_sim_create(const osg_config *cfg, osg_sim **out)
+{
+    OSG_CHECK(cfg && out, OSG_ERR_ARG, "null argument");
+    *out = nullptr;
+    OSG_CHECK(cfg->dim == 2 || cfg->dim == 3, OSG_ERR_ARG, "dim must be 2 or 3");
+    OSG_CHECK(cfg->order >= 1 && cfg->order <= 4, OSG_ERR_ARG, "order must be 1..4");
+    OSG_CHECK(cfg->precision == 32 || cfg->precision == 64, OSG_ERR_ARG,
+              "precision must be 32 or 64");
+    OSG_CHECK(cfg->engine == OSG_ENGINE_PLAIN || cfg->engine == OSG_ENGINE_TILED, OSG_ERR_ARG,
+              "unknown engine");
+    OSG_CHECK(!(cfg->engine == OSG_ENGINE_TILED && cfg->precision != 32), OSG_ERR_ARG,
+              "the tiled engine is single precision");
+    double cour = 0.0;
+    for (int d = 0; d < cfg->dim; d++) {
+        OSG_CHECK(cfg->nx[d] >= 2 * cfg->order + 1 && cfg->dx[d] > 0, OSG_ERR_ARG,
+                  "nx[%d] too small or dx <= 0", d);
+        cour += 1.0 / (cfg->dx[d] * cfg->dx[d]);
+    }
+    // Courant condition of the Yee solver (source/emf/solver/os-emf-solver-yee.f03:430-456)
+    OSG_CHECK(cfg->dt > 0 && cfg->dt <= std::sqrt(1.0 / cour), OSG_ERR_ARG,
+              "dt violates the Yee Courant limit %g", std::sqrt(1.0 / cour));
+    osg_sim *s = new osg_sim();
+    s->cfg = *cfg;
+    for (int d = cfg->dim; d < 3; d++) {
+        s->cfg.nx[d] = 1;
+        s->cfg.dx[d] = 1.0;
+    }
+    guard_cells(cfg->order, &s->gl, &s->gu);
+    int gcl[3] = {s->gl, s->gl, s->gl}, gcu[3] = {s->gu, s->gu, s->gu};
+    s->g = make_grid(cfg->dim, s->cfg.nx, gcl, gcu);
+    s->esz = cfg->precision == 32 ? 4 : 8;
+    int rc = OSG_OK;
+    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("no CUDA device / stream creation failed");
+        delete s;
+        return OSG_ERR_CUDA;
+    }
+    const size_t gbytes = (size_t)s->esz * 3 * s->g.npoints();
+    s->e = dalloc<char>(gbytes, &rc);
+    s->b = rc ? nullptr : dalloc<char>(gbytes, &rc);
+    s->j = rc ? nullptr : dalloc<char>(gbytes, &rc);
+    s->d_ene = rc ? nullptr : dalloc<double>(MAX_SPECIES, &rc);
+    s->d_status = rc ? nullptr : dalloc<int>(4, &rc);
+    s->d_diag = rc ? nullptr : dalloc<double>(16, &rc);
+    if (rc) {
+        osg_sim_destroy(s);
+        return rc;
+    }
+    cudaMemsetAsync(s->e, 0, gbytes, s->st);
+    cudaMemsetAsync(s->b, 0, gbytes, s->st);
+    cudaMemsetAsync(s->j, 0, gbytes, s->st);
+    cudaMemsetAsync(s->d_status, 0, 4 * sizeof(int), s->st);
+    cudaMemsetAsync(s->d_ene, 0, MAX_SPECIES * sizeof(double), s->st);
+    if (cfg->engine == OSG_ENGINE_TILED) {
+        rc = tiled_create(&s->tiled, s->cfg, s->g);
+        if (rc) {
+            osg_sim_destroy(s);
+            return rc;
+        }
+    }
+    if (cudaStreamSynchronize(s->st) != cudaSuccess) {
+        set_error("initialisation failed");
+        osg_sim_destroy(s);
+        return OSG_ERR_CUDA;
+    }
+    *out = s;
+    return OSG_OK;
+}
+
+int osg_sim_destroy(osg_sim *s)
+{
+    if (!s) return OSG_OK;
+    if (s->st) cudaStreamSynchronize(s->st);
+    drop_graphs(s);
+    for (auto &p : s->plain) {
+        cudaFree(p.ix);
+        cudaFree(p.x);
+        cudaFree(p.u);
+        cudaFree(p.q);
+    }
+    if (s->tiled) tiled_destroy(s->tiled);
+    cudaFree(s->e);
+    cudaFree(s->b);
+    cudaFree(s->j);
+    cudaFree(s->d_ene);
+    cudaFree(s->d_status);
+    cudaFree(s->d_diag);
+    cudaFree(s->d_rho);
+    cudaFree(s->d_rho0);
+    cudaFree(s->d_cell_cnt);
+    cudaFree(s->d_scan_tmp);
+    cudaFree(s->d_sort_buf);
+    if (s->st) cudaStreamDestroy(s->st);
+    delete s;
+    return OSG_OK;
+}
+
+int osg_sim_add_species(osg_sim *s, double rqm, long np, const int *ix, const void *x,
+                        const void *u, const void *q)
+{
+    OSG_CHECK(s, OSG_ERR_ARG, "null sim");
+    OSG_CHECK((int)s->np.size() < MAX_SPECIES, OSG_ERR_ARG, "too many species");
+    OSG_CHECK(rqm != 0.0, OSG_ERR_ARG, "rqm must be non-zero");
+    OSG_CHECK(np >= 0 && (np == 0 || (ix && x && u && q)), OSG_ERR_ARG, "bad particle arrays");
+    const int dim = s->cfg.dim;
+    for (long p = 0; p < np; p++)
+        for (int d = 0; d < dim; d++)
+            OSG_CHECK(ix[dim * p + d] >= 1 && ix[dim * p + d] <= s->cfg.nx[d], OSG_ERR_RANGE,
+                      "particle %ld: cell index out of [1, nx]", p);
+    const int k = (int)s->np.size();
+    int rc = OSG_OK;
+    if (s->cfg.engine == OSG_ENGINE_TILED) {
+        OSG_CHECK(s->step_n == 0, OSG_ERR_STATE,
+                  "the tiled engine takes species only before the first step");
+        rc = tiled_add_species(s->tiled, rqm, np, ix, (const float *)x, (const float *)u,
+                               (const float *)q, s->st);
+        if (rc) return rc;
+        s->plain.emplace_back();
+    } else {
+        PlainSpecies p;
+        const size_t n = np > 0 ? (size_t)np : 1;
+        p.ix = dalloc<int>(n * dim, &rc);
+        p.x = rc ? nullptr : dalloc<char>(n * dim * s->esz, &rc);
+        p.u = rc ? nullptr : dalloc<char>(n * 3 * s->esz, &rc);
+        p.q = rc ? nullptr : dalloc<char>(n * s->esz, &rc);
+        if (rc) {
+            cudaFree(p.ix);
+            cudaFree(p.x);
+            cudaFree(p.u);
+            return rc;
+        }
+        if (np > 0) {
+            OSG_CUDA(cudaMemcpyAsync(p.ix, ix, sizeof(int) * dim * np, cudaMemcpyHostToDevice, s->st));
+            OSG_CUDA(cudaMemcpyAsync(p.x, x, (size_t)s->esz * dim * np, cudaMemcpyHostToDevice, s->st));
+            OSG_CUDA(cudaMemcpyAsync(p.u, u, (size_t)s->esz * 3 * np, cudaMemcpyHostToDevice, s->st));
+            OSG_CUDA(cudaMemcpyAsync(p.q, q, (size_t)s->esz * np, cudaMemcpyHostToDevice, s->st));
+        }
+        s->plain.push_back(p);
+        // sort scratch sized for the largest species
+        const size_t need = ((size_t)sizeof(int) * dim + (size_t)s->esz * (dim + 4)) * n;
+        if (s->cfg.n_sort > 0 && need > s->sort_buf_bytes) {
+            cudaFree(s->d_sort_buf);
+            s->d_sort_buf = dalloc<char>(need, &rc);
+            if (rc) return rc;
+            s->sort_buf_bytes = need;
+        }
+        if (s->cfg.n_sort > 0 && !s->d_cell_cnt) {
+            const long nc = ncells(s->g);
+            s->d_cell_cnt = dalloc<int>(nc, &rc);
+            if (!rc) s->d_scan_tmp = dalloc<int>((nc + 1023) / 1024 + 1, &rc);
+            if (rc) return rc;
+        }
+    }
+    s->rqm.push_back(rqm);
+    s->np.push_back(np);
+    s->graphs_dirty = true;
+    OSG_CUDA(cudaStreamSynchronize(s->st));
+    return k;
+}
+
+int osg_sim_set_fields(osg_sim *s, const void *e, const void *b)
+{
+    OSG_CHECK(s, OSG_ERR_ARG, "null sim");
+    const size_t n = (size_t)s->esz * 3 * s->g.npoints();
+    if (e) OSG_CUDA(cudaMemcpyAsync(s->e, e, n, cudaMemcpyHostToDevice, s->st));
+    if (b) OSG_CUDA(cudaMemcpyAsync(s->b, b, n, cudaMemcpyHostToDevice, s->st));
+    OSG_CUDA(cudaStreamSynchronize(s->st));
+    return OSG_OK;
+}
+
+int osg_sim_get_fields(osg_sim *s, void *e, void *b, void *j)
+{
+    OSG_CHECK(s, OSG_ERR_ARG, "null sim");
+    const size_t n = (size_t)s->esz * 3 * s->g.npoints();
+    if (e) OSG_CUDA(cudaMemcpyAsync(e, s->e, n, cudaMemcpyDeviceToHost, s->st));
+    if (b) OSG_CUDA(cudaMemcpyAsync(b, s->b, n, cudaMemcpyDeviceToHost, s->st));
+    if (j) OSG_CUDA(cudaMemcpyAsync(j, s->j, n, cudaMemcpyDeviceToHost, s->st));
+    OSG_CUDA(cudaStreamSynchronize(s->st));
+    return OSG_OK;
+}
+
+int osg_sim_num_particles(osg_sim *s, int k, long *np)
+{
+    OSG_CHECK(s && np && k >= 0 && k < (int)s->np.size(), OSG_ERR_ARG, "bad species");
+    if (s->cfg.engine == OSG_ENGINE_TILED) return tiled_count(s->tiled, (int)(s->step_n & 1), k, np, s->st);
+    *np = s->np[k];
+    return OSG_OK;
+}
+
+int osg_sim_get_species(osg_sim *s, int k, int *ix, void *x, void *u, void *q)
+{
+    OSG_CHECK(s && k >= 0 && k < (int)s->np.size(), OSG_ERR_ARG, "bad species");
+    if (s->cfg.engine == OSG_ENGINE_TILED)
+        return tiled_get_species(s->tiled, (int)(s->step_n & 1), k, ix, (float *)x,
+                                 (float *)u, (float *)q, s->st);
+    const long np = s->np[k];
+    const int dim = s->cfg.dim;
+    PlainSpecies &p = s->plain[k];
+    if (np > 0) {
+        if (ix) OSG_CUDA(cudaMemcpyAsync(ix, p.ix, sizeof(int) * dim * np, cudaMemcpyDeviceToHost, s->st));
+        if (x) OSG_CUDA(cudaMemcpyAsync(x, p.x, (size_t)s->esz * dim * np, cudaMemcpyDeviceToHost, s->st));
+        if (u) OSG_CUDA(cudaMemcpyAsync(u, p.u, (size_t)s->esz * 3 * np, cudaMemcpyDeviceToHost, s->st));
+        if (q) OSG_CUDA(cudaMemcpyAsync(q, p.q, (size_t)s->esz * np, cudaMemcpyDeviceToHost, s->st));
+    }
+    OSG_CUDA(cudaStreamSynchronize(s->st));
+    return OSG_OK;
+}
+
+int osg_sim_step_async(osg_sim *s, int nsteps)
+{
+    OSG_CHECK(s && nsteps >= 0, OSG_ERR_ARG, "bad arguments");
+    OSG_CHECK(!s->np.empty(), OSG_ERR_STATE, "no species");
+    for (int i = 0; i < nsteps; i++) {
+        const int parity = (int)(s->step_n & 1);
+        const int sort = sort_due(s, s->step_n) ? 1 : 0;
+        cudaGraphExec_t ge;
+        int rc = get_graph(s, s->cfg.engine == OSG_ENGINE_TILED ? parity : 0, sort, &ge);
+        if (rc) return rc;
+        OSG_CUDA(cudaGraphLaunch(ge, s->st));
+        s->step_n++;
+    }
+    return OSG_OK;
+}
+
+int osg_sim_sync(osg_sim *s)
+{
+    OSG_CHECK(s, OSG_ERR_ARG, "null sim");
+    OSG_CUDA(cudaStreamSynchronize(s->st));
+    return check_status(s);
+}
+
+int osg_sim_step(osg_sim *s, int nsteps)
+{
+    int rc = osg_sim_step_async(s, nsteps);
+    if (rc) return rc;
+    rc = osg_sim_sync(s);
+    if (rc) return rc;
+    if (s->cfg.engine == OSG_ENGINE_TILED) {
+        // tile slabs filling up (density bunching): re-bin with room to spare before a tile
+        // can overflow; particles move at most one cell per step
+        double m = 0.0;
+        rc = tiled_occupancy(s->tiled, (int)(s->step_n & 1), &m, s->st);
+        if (rc) return rc;
+        if (m > 0.7) {
+            rc = tiled_regrow(s->tiled, (int)(s->step_n & 1), s->st);
+            if (rc) return rc;
+            s->graphs_dirty = true;
+        }
+    }
+    return OSG_OK;
+}
+
+int osg_sim_tile_occupancy(osg_sim *s, double *max_frac)
+{
+    OSG_CHECK(s && max_frac, OSG_ERR_ARG, "bad arguments");
+    *max_frac = 0.0;
+    if (s->cfg.engine != OSG_ENGINE_TILED) return OSG_OK;
+    return tiled_occupancy(s->tiled, (int)(s->step_n & 1), max_frac, s->st);
+}
+
+void *osg_sim_stream(osg_sim *s) { return s ? (void *)s->st : nullptr; }
+
+int osg_sim_energy(osg_sim *s, double *kinetic, double *field)
+{
+    OSG_CHECK(s, OSG_ERR_ARG, "null sim");
+    double dv = 1.0;
+    for (int d = 0; d < s->cfg.dim; d++) dv *= s->cfg.dx[d];
+    if (kinetic) {
+        double h[MAX_SPECIES];
+        OSG_CUDA(cudaMemcpyAsync(h, s->d_ene, sizeof(double) * MAX_SPECIES, cudaMemcpyDeviceToHost, s->st));
+        OSG_CUDA(cudaStreamSynchronize(s->st));
+        // get_energy normalisation, source/spec/os-spec-define.f03:1079-1084
+        for (size_t k = 0; k < s->np.size(); k++) kinetic[k] = h[k] * s->rqm[k] * dv;
+    }
+    if (field) {
+        OSG_CUDA(cudaMemsetAsync(s->d_diag, 0, 6 * sizeof(double), s->st));
+        if (s->cfg.precision == 32) {
+            field_sumsq<float>(s->g, (const float *)s->e, s->d_diag, s->st);
+            field_sumsq<float>(s->g, (const float *)s->b, s->d_diag + 3, s->st);
+        } else {
+            field_sumsq<double>(s->g, (const double *)s->e, s->d_diag, s->st);
+            field_sumsq<double>(s->g, (const double *)s->b, s->d_diag + 3, s->st);
+        }
+        OSG_CUDA(cudaGetLastError());
+        double h[6];
+        OSG_CUDA(cudaMemcpyAsync(h, s->d_diag, sizeof h, cudaMemcpyDeviceToHost, s->st));
+        OSG_CUDA(cudaStreamSynchronize(s->st));
+        for (int c = 0; c < 6; c++) field[c] = 0.5 * dv * h[c];
+    }
+    return OSG_OK;
+}
+
+int osg_sim_gauss_residual(osg_sim *s, double *max_abs, double *l2)
+{
+    OSG_CHECK(s, OSG_ERR_ARG, "null sim");
+    const size_t n = 3 * (size_t)s->g.npoints();
+    int rc = OSG_OK;
+    if (!s->d_rho) s->d_rho = dalloc<double>(n, &rc);
+    if (rc) return rc;
+    OSG_CUDA(cudaMemsetAsync(s->d_rho, 0, n * sizeof(double), s->st));
+    for (size_t k = 0; k < s->np.size(); k++) {
+        if (s->cfg.engine == OSG_ENGINE_TILED) {
+            rc = tiled_deposit_rho(s->tiled, (int)(s->step_n & 1), (int)k, s->d_rho,
+                                   s->d_status, s->st);
+        } else if (s->cfg.precision == 32) {
+            rc = deposit_rho<float>(s->g, s->cfg.order, s->plain[k].ix, (const float *)s->plain[k].x,
+                                    (const float *)s->plain[k].q, s->np[k], s->d_rho, s->d_status, s->st);
+        } else {
+            rc = deposit_rho<double>(s->g, s->cfg.order, s->plain[k].ix, (const double *)s->plain[k].x,
+                                     (const double *)s->plain[k].q, s->np[k], s->d_rho, s->d_status, s->st);
+        }
+        if (rc) return rc;
+    }
+    periodic_update<double>(s->g, s->d_rho, 1, s->st);
+    // div E reads the lower neighbour of the first interior cell: refresh the E guard cells
+    // (the next step starts with the same replace, so this changes nothing downstream)
+    if (s->cfg.precision == 32) periodic_update<float>(s->g, (float *)s->e, 0, s->st);
+    else periodic_update<double>(s->g, (double *)s->e, 0, s->st);
+    OSG_CUDA(cudaMemsetAsync(s->d_diag, 0, 2 * sizeof(double), s->st));
+    unsigned long long *dmax = (unsigned long long *)s->d_diag;
+    if (s->cfg.precision == 32)
+        gauss_residual<float>(s->g, (const float *)s->e, s->d_rho, nullptr, s->cfg.dx, dmax,
+                              s->d_diag + 1, s->st);
+    else
+        gauss_residual<double>(s->g, (const double *)s->e, s->d_rho, nullptr, s->cfg.dx, dmax,
+                               s->d_diag + 1, s->st);
+    OSG_CUDA(cudaGetLastError());
+    double h[2];
+    OSG_CUDA(cudaMemcpyAsync(h, s->d_diag, sizeof h, cudaMemcpyDeviceToHost, s->st));
+    OSG_CUDA(cudaStreamSynchronize(s->st));
+    unsigned long long bits;
+    memcpy(&bits, &h[0], sizeof bits);
+    double m;
+    memcpy(&m, &bits, sizeof m);
+    if (max_abs) *max_abs = m;
+    if (l2) *l2 = std::sqrt(h[1]);
+    return check_status(s);
+}
+
+int osg_sim_profile(osg_sim *s, int nsteps, float *ms_phase)
+{
+    OSG_CHECK(s && ms_phase && nsteps > 0, OSG_ERR_ARG, "bad arguments");
+    OSG_CHECK(!s->np.empty(), OSG_ERR_STATE, "no species");
+    PhaseEvents pe;
+    for (int i = 0; i < 6; i++) OSG_CUDA(cudaEventCreate(&pe.ev[i]));
+    float acc[5] = {0, 0, 0, 0, 0};
+    int rc = OSG_OK;
+    for (int it = 0; it < nsteps && !rc; it++) {
+        const int parity = (int)(s->step_n & 1);
+        rc = enqueue_step_any(s, parity, sort_due(s, s->step_n), &pe);
+        if (rc) break;
+        s->step_n++;
+        if (cudaEventSynchronize(pe.ev[5]) != cudaSuccess) {
+            set_error("profiled step failed");
+            rc = OSG_ERR_CUDA;
+            break;
+        }
+        float t;
+        cudaEventElapsedTime(&t, pe.ev[1], pe.ev[2]); acc[0] += t;   // push + deposit
+        cudaEventElapsedTime(&t, pe.ev[3], pe.ev[4]); acc[1] += t;   // fold
+        cudaEventElapsedTime(&t, pe.ev[4], pe.ev[5]); acc[2] += t;   // Yee
+        cudaEventElapsedTime(&t, pe.ev[0], pe.ev[1]); acc[3] += t;   // replace
+        cudaEventElapsedTime(&t, pe.ev[2], pe.ev[3]); acc[4] += t;   // sort
+    }
+    for (int i = 0; i < 6; i++) cudaEventDestroy(pe.ev[i]);
+    if (rc) return rc;
+    for (int i = 0; i < 5; i++) ms_phase[i] = acc[i] / nsteps;
+    return check_status(s);
+}
+
+int osg_sim_launches_per_step(osg_sim *s) { return s ? s->launches_per_step : 0; }
+
+int osg_sim_time_steps(osg_sim *s, int nsteps, float *ms)
+{
+    OSG_CHECK(s && ms && nsteps > 0, OSG_ERR_ARG, "bad arguments");
+    cudaEvent_t a, b;
+    OSG_CUDA(cudaEventCreate(&a));
+    OSG_CUDA(cudaEventCreate(&b));
+    int rc = OSG_OK;
+    if (cudaEventRecord(a, s->st) != cudaSuccess) rc = OSG_ERR_CUDA;
+    if (!rc) rc = osg_sim_step_async(s, nsteps);
+    if (!rc && cudaEventRecord(b, s->st) != cudaSuccess) rc = OSG_ERR_CUDA;
+    if (!rc && cudaEventSynchronize(b) != cudaSuccess) rc = OSG_ERR_CUDA;
+    if (!rc) cudaEventElapsedTime(ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc == OSG_ERR_CUDA) set_error("timed steps failed");
+    if (rc) return rc;
+    return check_status(s);
+}
+
+} // extern "C"

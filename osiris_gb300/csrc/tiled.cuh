@@ -1,0 +1,31 @@
+// tiled.cuh -- particle engine with particles binned by spatial tile (single precision).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace osg {
+
+struct TiledState;
+
+int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g);
+void tiled_destroy(TiledState *t);
+int tiled_add_species(TiledState *t, double rqm, long np, const int *ix, const float *x,
+                      const float *u, const float *q, cudaStream_t st);
+// one push + deposit + migration pass over all species; parity selects which particle buffer
+// is read (the other one is written)
+int tiled_push(TiledState *t, int parity, const float *e, const float *b, float *j,
+               double *d_ene, int *d_status, cudaStream_t st, int *launches);
+// `cur` = index (0/1) of the buffer that holds the current particles (step count & 1)
+int tiled_count(TiledState *t, int cur, int k, long *np, cudaStream_t st);
+int tiled_get_species(TiledState *t, int cur, int k, int *ix, float *x, float *u, float *q,
+                      cudaStream_t st);
+int tiled_deposit_rho(TiledState *t, int cur, int k, double *rho, int *status,
+                      cudaStream_t st);
+// largest live-slot fraction over all tiles and species
+int tiled_occupancy(TiledState *t, int cur, double *max_frac, cudaStream_t st);
+// re-bin all species into larger slabs (host round trip); keeps buffer `cur` current
+int tiled_regrow(TiledState *t, int cur, cudaStream_t st);
+
+} // namespace osg
