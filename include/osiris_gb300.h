@@ -81,6 +81,26 @@ int osg_vadvance_deposit_f64(int dim, int order, int *ix, double *x, double *u, 
                              double *j, const int *j_size, const int *j_offset,
                              const double *dx, double dt, double *ene);
 
+/* The same push for callers that cannot allocate device memory: hosts that give the whole GPU
+ * to their own pool allocator at start-up and treat a foreign cudaMalloc as an error, and
+ * stepping loops that budget device memory once and must not let a library allocate.  It has
+ * no counterpart in the reference.  All device staging lives in one file-scope array of
+ * OSG_NOALLOC_SCRATCH_BYTES, reserved on every GPU that loads the library until the process
+ * exits; nothing is allocated or freed.  A call whose particles and fields need more than that
+ * (roughly 4*dim + 20 bytes per particle plus three copies of the grid) is rejected with
+ * OSG_ERR_ARG; split the particle range into smaller calls.  The first call on a device looks
+ * up the array's address for that device; make it before any stream capture there.  Every
+ * call shares the array, so calls that overlap on the GPU (several host threads at once) race;
+ * each call clears what must start at zero and copies the rest in.  Runs on the calling
+ * thread's default stream (cudaStreamPerThread) and returns when the results are on the host. */
+#define OSG_NOALLOC_SCRATCH_BYTES (16u << 20)
+int osg_vadvance_deposit_noalloc_f32(int dim, int order, int *ix, float *x, float *u, float *q,
+                                     int i0, int i1, float rqm, const float *efield,
+                                     const float *bfield, const int *emf_size,
+                                     const int *emf_offset, float *j, const int *j_size,
+                                     const int *j_offset, const double *dx, double dt,
+                                     double *ene);
+
 /* Same on arrays that already live in device memory, asynchronous on `stream`
  * (cudaStream_t, NULL = default stream).  d_ene is a device double that is incremented. */
 int osg_vadvance_deposit_dev_f32(int dim, int order, int *ix, float *x, float *u,

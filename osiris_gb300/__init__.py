@@ -73,6 +73,8 @@ def _declare(lb):
     lb.osg_host_free.argtypes = [P]
     lb.osg_vadvance_deposit_f32.argtypes = [I, I, P, P, P, P, I, I, F, P, P, P, P, P, P, P, P, D, P]
     lb.osg_vadvance_deposit_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, P]
+    lb.osg_vadvance_deposit_noalloc_f32.argtypes = [I, I, P, P, P, P, I, I, F, P, P, P, P, P, P,
+                                                    P, P, D, P]
     for s in ("f32", "f64"):
         getattr(lb, f"osg_yee_advance_{s}").argtypes = [I, P, P, P, P, P, P, P, D]
         getattr(lb, f"osg_periodic_{s}").argtypes = [I, P, P, P, P, I]
@@ -155,6 +157,27 @@ def vadvance_deposit(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_s
              _p(bfield), _p(_i32(emf_size)), _p(_i32(emf_offset)), _p(j), _p(_i32(j_size)),
              _p(_i32(j_offset)), _p(_f64(list(dx) + [0.0] * (3 - len(dx)))), float(dt),
              _p(ene)))
+    return float(ene[0])
+
+
+NOALLOC_SCRATCH_BYTES = 16 << 20
+
+
+def vadvance_deposit_noalloc(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_size,
+                             emf_offset, j, j_size, j_offset, dx, dt):
+    """vadvance_deposit (float32 only) without any device allocation: the staging lives in a
+    fixed NOALLOC_SCRATCH_BYTES array of the library; larger calls raise (split i0..i1)."""
+    _need(ix, np.int32, "ix")
+    for a, n in ((x, "x"), (u, "u"), (q, "q"), (j, "j")):
+        _need(a, np.float32, n)
+    for a, n in ((efield, "efield"), (bfield, "bfield")):
+        if a.dtype != np.float32 or not a.flags.c_contiguous:
+            raise TypeError(f"{n} must be C-contiguous float32")
+    ene = np.zeros(1)
+    _check(lib().osg_vadvance_deposit_noalloc_f32(
+        dim, order, _p(ix), _p(x), _p(u), _p(q), int(i0), int(i1), rqm, _p(efield), _p(bfield),
+        _p(_i32(emf_size)), _p(_i32(emf_offset)), _p(j), _p(_i32(j_size)), _p(_i32(j_offset)),
+        _p(_f64(list(dx) + [0.0] * (3 - len(dx)))), float(dt), _p(ene)))
     return float(ene[0])
 
 
