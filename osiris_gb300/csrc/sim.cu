@@ -41,6 +41,7 @@ struct osg_sim {
     double *d_diag = nullptr;    // 16 doubles of diagnostic scratch
     double *d_rho = nullptr, *d_rho0 = nullptr;
     long step_n = 0;
+    int cur = 0;                 // tiled engine: particle buffer holding the current state
     std::vector<double> rqm;
     std::vector<long> np;
     std::vector<osg::PlainSpecies> plain;
@@ -266,6 +267,11 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, PhaseEvents *pe)
             launches += 5;
         }
     }
+    if (with_sort && c.engine == OSG_ENGINE_TILED) {
+        // the push wrote buffer 1 - parity; the sort brings it back, cell-ordered, to parity
+        int rc = tiled_sort(s->tiled, 1 - parity, st, &launches);
+        if (rc) return rc;
+    }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[3], st));
     periodic_update<T>(s->g, (T *)s->j, 1, st);
     launches += c.dim;
@@ -318,8 +324,13 @@ static int get_graph(osg_sim *s, int parity, int sort, cudaGraphExec_t *out)
 
 static bool sort_due(const osg_sim *s, long n)
 {
-    return s->cfg.engine == OSG_ENGINE_PLAIN && s->cfg.n_sort > 0 && n > 0 &&
-           (n % s->cfg.n_sort) == 0;
+    return s->cfg.n_sort > 0 && n > 0 && (n % s->cfg.n_sort) == 0;
+}
+
+// buffer bookkeeping of the tiled engine after one step
+static void advance_buffers(osg_sim *s, bool sorted)
+{
+    if (s->cfg.engine == OSG_ENGINE_TILED && !sorted) s->cur ^= 1;
 }
 
 static int check_status(osg_sim *s)
@@ -378,6 +389,10 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               "dt violates the Yee Courant limit %g", std::sqrt(1.0 / cour));
     osg_sim *s = new osg_sim();
     s->cfg = *cfg;
+    // n_sort: 0 = engine default (plain: every 25 steps, the reference's default n_sort,
+    // docs/reference/Species.md; tiled: every 20 steps), < 0 = never
+    if (s->cfg.n_sort == 0) s->cfg.n_sort = cfg->engine == OSG_ENGINE_TILED ? 20 : 25;
+    if (s->cfg.n_sort < 0) s->cfg.n_sort = 0;
     for (int d = cfg->dim; d < 3; d++) {
         s->cfg.nx[d] = 1;
         s->cfg.dx[d] = 1.0;
@@ -467,7 +482,7 @@ int osg_sim_add_species(osg_sim *s, double rqm, long np, const int *ix, const vo
     const int k = (int)s->np.size();
     int rc = OSG_OK;
     if (s->cfg.engine == OSG_ENGINE_TILED) {
-        OSG_CHECK(s->step_n == 0, OSG_ERR_STATE,
+        OSG_CHECK(s->step_n == 0 && s->cur == 0, OSG_ERR_STATE,
                   "the tiled engine takes species only before the first step");
         rc = tiled_add_species(s->tiled, rqm, np, ix, (const float *)x, (const float *)u,
                                (const float *)q, s->st);
@@ -539,7 +554,7 @@ int osg_sim_get_fields(osg_sim *s, void *e, void *b, void *j)
 int osg_sim_num_particles(osg_sim *s, int k, long *np)
 {
     OSG_CHECK(s && np && k >= 0 && k < (int)s->np.size(), OSG_ERR_ARG, "bad species");
-    if (s->cfg.engine == OSG_ENGINE_TILED) return tiled_count(s->tiled, (int)(s->step_n & 1), k, np, s->st);
+    if (s->cfg.engine == OSG_ENGINE_TILED) return tiled_count(s->tiled, s->cur, k, np, s->st);
     *np = s->np[k];
     return OSG_OK;
 }
@@ -548,7 +563,7 @@ int osg_sim_get_species(osg_sim *s, int k, int *ix, void *x, void *u, void *q)
 {
     OSG_CHECK(s && k >= 0 && k < (int)s->np.size(), OSG_ERR_ARG, "bad species");
     if (s->cfg.engine == OSG_ENGINE_TILED)
-        return tiled_get_species(s->tiled, (int)(s->step_n & 1), k, ix, (float *)x,
+        return tiled_get_species(s->tiled, s->cur, k, ix, (float *)x,
                                  (float *)u, (float *)q, s->st);
     const long np = s->np[k];
     const int dim = s->cfg.dim;
@@ -568,12 +583,13 @@ int osg_sim_step_async(osg_sim *s, int nsteps)
     OSG_CHECK(s && nsteps >= 0, OSG_ERR_ARG, "bad arguments");
     OSG_CHECK(!s->np.empty(), OSG_ERR_STATE, "no species");
     for (int i = 0; i < nsteps; i++) {
-        const int parity = (int)(s->step_n & 1);
+        const int parity = s->cfg.engine == OSG_ENGINE_TILED ? s->cur : 0;
         const int sort = sort_due(s, s->step_n) ? 1 : 0;
         cudaGraphExec_t ge;
-        int rc = get_graph(s, s->cfg.engine == OSG_ENGINE_TILED ? parity : 0, sort, &ge);
+        int rc = get_graph(s, parity, sort, &ge);
         if (rc) return rc;
         OSG_CUDA(cudaGraphLaunch(ge, s->st));
+        advance_buffers(s, sort != 0);
         s->step_n++;
     }
     return OSG_OK;
@@ -596,10 +612,10 @@ int osg_sim_step(osg_sim *s, int nsteps)
         // tile slabs filling up (density bunching): re-bin with room to spare before a tile
         // can overflow; particles move at most one cell per step
         double m = 0.0;
-        rc = tiled_occupancy(s->tiled, (int)(s->step_n & 1), &m, s->st);
+        rc = tiled_occupancy(s->tiled, s->cur, &m, s->st);
         if (rc) return rc;
         if (m > 0.7) {
-            rc = tiled_regrow(s->tiled, (int)(s->step_n & 1), s->st);
+            rc = tiled_regrow(s->tiled, s->cur, s->st);
             if (rc) return rc;
             s->graphs_dirty = true;
         }
@@ -612,7 +628,7 @@ int osg_sim_tile_occupancy(osg_sim *s, double *max_frac)
     OSG_CHECK(s && max_frac, OSG_ERR_ARG, "bad arguments");
     *max_frac = 0.0;
     if (s->cfg.engine != OSG_ENGINE_TILED) return OSG_OK;
-    return tiled_occupancy(s->tiled, (int)(s->step_n & 1), max_frac, s->st);
+    return tiled_occupancy(s->tiled, s->cur, max_frac, s->st);
 }
 
 void *osg_sim_stream(osg_sim *s) { return s ? (void *)s->st : nullptr; }
@@ -657,7 +673,7 @@ int osg_sim_gauss_residual(osg_sim *s, double *max_abs, double *l2)
     OSG_CUDA(cudaMemsetAsync(s->d_rho, 0, n * sizeof(double), s->st));
     for (size_t k = 0; k < s->np.size(); k++) {
         if (s->cfg.engine == OSG_ENGINE_TILED) {
-            rc = tiled_deposit_rho(s->tiled, (int)(s->step_n & 1), (int)k, s->d_rho,
+            rc = tiled_deposit_rho(s->tiled, s->cur, (int)k, s->d_rho,
                                    s->d_status, s->st);
         } else if (s->cfg.precision == 32) {
             rc = deposit_rho<float>(s->g, s->cfg.order, s->plain[k].ix, (const float *)s->plain[k].x,
@@ -703,9 +719,11 @@ int osg_sim_profile(osg_sim *s, int nsteps, float *ms_phase)
     float acc[5] = {0, 0, 0, 0, 0};
     int rc = OSG_OK;
     for (int it = 0; it < nsteps && !rc; it++) {
-        const int parity = (int)(s->step_n & 1);
-        rc = enqueue_step_any(s, parity, sort_due(s, s->step_n), &pe);
+        const int parity = s->cfg.engine == OSG_ENGINE_TILED ? s->cur : 0;
+        const bool sort = sort_due(s, s->step_n);
+        rc = enqueue_step_any(s, parity, sort, &pe);
         if (rc) break;
+        advance_buffers(s, sort);
         s->step_n++;
         if (cudaEventSynchronize(pe.ev[5]) != cudaSuccess) {
             set_error("profiled step failed");

@@ -282,20 +282,27 @@ __device__ __forceinline__ float transpose_reduce32(float (&t)[32])
 }
 
 // Warp-cooperative accumulation of one segment per lane into the shared current tile.
-// base = offset of the lane's stencil origin, or -1 when the lane has no segment.  The lanes
-// that share a cell are summed in registers first (transpose-reduce, one pass per distinct
-// cell of the warp), so every shared-memory add of a pass hits a distinct address: lanes of
-// a warp that deposit into the same cell never serialise on conflicting atomics.
+// base = offset of the lane's stencil origin, or -1 when the lane has no segment.  Lanes whose
+// cell is shared by at least `reduce_min` lanes of the warp are summed in registers first
+// (transpose-reduce, one pass per such cell), so every shared-memory add of a pass hits a
+// distinct address and lanes that deposit into the same cell never serialise on conflicting
+// atomics.  Lanes of sparsely populated cells (fewer peers) add their values directly: a
+// reduce pass costs about four times a direct pass, which only pays when many lanes share it.
 template <int DIM, int ORD>
 __device__ __forceinline__ void warp_deposit(float *sJ, int base, const float *v, int jsy,
-                                             int jsz)
+                                             int jsz, int reduce_min)
 {
     constexpr int NV = SegVals<DIM, ORD>::NV;
     constexpr int NB = (NV + 31) / 32;
     const unsigned lane = threadIdx.x & 31;
     const unsigned peers = __match_any_sync(FULL_MASK, base);
     const bool active = base >= 0;
-    unsigned rem = __ballot_sync(FULL_MASK, active && (__ffs(peers) - 1) == (int)lane);
+    const bool direct = active && __popc(peers) < reduce_min;
+    if (direct) {
+#pragma unroll
+        for (int i = 0; i < NV; i++) atomicAdd(sJ + base + seg_offset<DIM, ORD>(i, jsy, jsz), v[i]);
+    }
+    unsigned rem = __ballot_sync(FULL_MASK, active && !direct && (__ffs(peers) - 1) == (int)lane);
     while (rem) {
         const int l = __ffs(rem) - 1;
         rem &= rem - 1;
@@ -370,33 +377,50 @@ __device__ __forceinline__ int spread_index(int t, int nthr)
     return (t & 31) * (nthr >> 5) + (t >> 5);
 }
 
-// Deposit one segment per lane (rec = nullptr: no segment); warp-synchronous in 2D.
+// Deposit one segment per lane (rec = nullptr: no segment).  reduce_min > 32 selects plain
+// per-lane shared atomics (no warp-synchronous part); otherwise warp_deposit.  3D cubic and
+// quartic segments (144 and 300 values) always add directly: their values do not fit in
+// registers next to a reduce buffer.
+template <int DIM, int ORD>
+constexpr bool direct_only() { return DIM == 3 && ORD >= 3; }
+
 template <int DIM, int ORD>
 __device__ __forceinline__ void deposit_segment(float *sJ, const SegRec *rec, const float *jn,
-                                                int jsy, int jsz)
+                                                int jsy, int jsz, int reduce_min)
 {
-    if constexpr (DIM == 2) {
-        constexpr int NV = SegVals<2, ORD>::NV;
-        float v[NV];
-        int base = -1;
-        if (rec) {
+    if constexpr (DIM == 3) {
+        if (direct_only<DIM, ORD>() || reduce_min > 32) {
+            if (rec) {
+                Seg3<float> g;
+                g.x0 = rec->a[0]; g.x1 = rec->a[1]; g.y0 = rec->a[2]; g.y1 = rec->a[3];
+                g.z0 = rec->a[4]; g.z1 = rec->a[5]; g.i = g.j = g.k = 0;
+                seg_atomic3<ORD>(sJ + rec->base, g, rec->q, jn, jsy, jsz);
+            }
+            return;
+        }
+    }
+    if constexpr (!direct_only<DIM, ORD>()) {
+    constexpr int NV = SegVals<DIM, ORD>::NV;
+    float v[NV];
+    int base = -1;
+    if (rec) {
+        if constexpr (DIM == 2) {
             Seg2<float> g;
             g.x0 = rec->a[0]; g.x1 = rec->a[1]; g.y0 = rec->a[2]; g.y1 = rec->a[3];
             g.vz = rec->a[4]; g.i = 0; g.j = 0;
             seg_values2<ORD>(g, rec->q, jn[0], jn[1], v);
-            base = rec->base;
         } else {
-#pragma unroll
-            for (int k = 0; k < NV; k++) v[k] = 0.f;
-        }
-        warp_deposit<2, ORD>(sJ, base, v, jsy, jsz);
-    } else {
-        if (rec) {
             Seg3<float> g;
             g.x0 = rec->a[0]; g.x1 = rec->a[1]; g.y0 = rec->a[2]; g.y1 = rec->a[3];
             g.z0 = rec->a[4]; g.z1 = rec->a[5]; g.i = g.j = g.k = 0;
-            seg_atomic3<ORD>(sJ + rec->base, g, rec->q, jn, jsy, jsz);
+            seg_values3<ORD>(g, rec->q, jn, v);
         }
+        base = rec->base;
+    } else {
+#pragma unroll
+        for (int k = 0; k < NV; k++) v[k] = 0.f;
+    }
+    warp_deposit<DIM, ORD>(sJ, base, v, jsy, jsz, reduce_min);
     }
 }
 

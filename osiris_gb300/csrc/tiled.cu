@@ -67,6 +67,8 @@ struct TiledArgs {
     int nspec;
     double *ene;
     int *status;
+    int local_sort;    // write stayers of each block iteration in cell order
+    int reduce_min;    // warp-reduce a cell's segments when at least this many lanes share it
 };
 
 struct TiledState {
@@ -87,6 +89,8 @@ struct TiledState {
     size_t compact_bytes = 0;
     size_t smem_bytes = 0;
     int threads = 128;   // threads per push CTA (multiple of 32, <= 256)
+    int local_sort = 1;
+    int reduce_min = 2;
 };
 
 static const int MAX_TILED_SPECIES = 16;
@@ -276,21 +280,33 @@ __global__ void __launch_bounds__(256) k_push_tiled(TiledArgs a)
             //      sort over the tile's cells) so that next step the lanes of a warp mostly share
             //      a cell; particles that leave take one slot each in their destination tile.
             const bool stay = has && dest == tile;
-            int lcell = 0, rank = 0;
-            if (stay) {
-                lcell = cw[0] - t0[0];
-                if (DIM > 1) lcell += a.T[0] * (cw[1] - t0[1]);
-                if (DIM > 2) lcell += a.T[0] * a.T[1] * (cw[2] - t0[2]);
-                rank = atomicAdd(&cellCnt[lcell], 1);
-            }
-            __syncthreads();
-            if (threadIdx.x < 32) {
-                const int nstay = warp_exclusive_scan(cellCnt, ncell_tile);
-                if (threadIdx.x == 0) sStayBase = nstay ? atomicAdd(sd.out.cnt + tile, nstay) : 0;
-            }
-            __syncthreads();
             long slot = -1;
-            if (stay) slot = sStayBase + cellCnt[lcell] + rank;
+            if (a.local_sort) {
+                int lcell = 0, rank = 0;
+                if (stay) {
+                    lcell = cw[0] - t0[0];
+                    if (DIM > 1) lcell += a.T[0] * (cw[1] - t0[1]);
+                    if (DIM > 2) lcell += a.T[0] * a.T[1] * (cw[2] - t0[2]);
+                    rank = atomicAdd(&cellCnt[lcell], 1);
+                }
+                __syncthreads();
+                if (threadIdx.x < 32) {
+                    const int nstay = warp_exclusive_scan(cellCnt, ncell_tile);
+                    if (threadIdx.x == 0) sStayBase = nstay ? atomicAdd(sd.out.cnt + tile, nstay) : 0;
+                }
+                __syncthreads();
+                if (stay) slot = sStayBase + cellCnt[lcell] + rank;
+            } else {
+                // warp-aggregated slots in the own tile, particle order kept per warp
+                const unsigned ms = __ballot_sync(FULL_MASK, stay);
+                if (ms) {
+                    const int leader = __ffs(ms) - 1;
+                    int b0 = 0;
+                    if ((int)lane == leader) b0 = atomicAdd(sd.out.cnt + tile, __popc(ms));
+                    b0 = __shfl_sync(FULL_MASK, b0, leader);
+                    if (stay) slot = b0 + __popc(ms & ((1u << lane) - 1u));
+                }
+            }
             if (has && !stay) slot = atomicAdd(sd.out.cnt + dest, 1);
             if (has) {
                 if (slot >= cap) {
@@ -308,6 +324,7 @@ __global__ void __launch_bounds__(256) k_push_tiled(TiledArgs a)
                     sd.out.q[o] = q;
                 }
             }
+            if (!a.local_sort) __syncthreads();   // segment buffer complete
             // clear the spare counters for the next iteration
             int *spare = sCellCnt[bp ^ 1];
             for (int k = threadIdx.x; k < ncell_tile; k += nthr) spare[k] = 0;
@@ -316,9 +333,10 @@ __global__ void __launch_bounds__(256) k_push_tiled(TiledArgs a)
             const int nall = nthr + sNextra[bp];
             for (int r = 0; r * nthr < nall; r++) {
                 int sidx = r * nthr + threadIdx.x;
-                if (DIM == 3 && r == 0) sidx = spread_index(threadIdx.x, nthr);
+                if (DIM == 3 && r == 0 && (direct_only<DIM, ORD>() || a.reduce_min > 32)) sidx = spread_index(threadIdx.x, nthr);
                 const bool valid = sidx < nall && sSeg[sidx].base >= 0;
-                deposit_segment<DIM, ORD>(sJ, valid ? &sSeg[sidx] : nullptr, a.jn, jsy, jsz);
+                deposit_segment<DIM, ORD>(sJ, valid ? &sSeg[sidx] : nullptr, a.jn, jsy, jsz,
+                                          a.reduce_min);
             }
             __syncthreads();
         }
@@ -358,6 +376,57 @@ __global__ void k_bin(const int *__restrict__ ix, const float *__restrict__ x,
         out.u[2][o] = u[3 * p + 2];
         out.q[o] = q[p];
     }
+}
+
+// --------------------------------------------------------------------------------- sort
+// Full counting sort of every tile by cell (x fastest inside the tile): reads the slabs of
+// spec[s].in, writes spec[s].out.  The GPU counterpart of the reference's cell sort every
+// n_sort steps (source/spec/os-species.f03:269-505), per tile instead of over the whole box.
+__global__ void __launch_bounds__(256) k_tile_sort(TiledArgs a, int dim)
+{
+    extern __shared__ int hist[];
+    const long tile = blockIdx.x;
+    const SpeciesDev sd = a.spec[blockIdx.y];
+    const long cap = sd.cap;
+    int n = sd.in.cnt[tile];
+    if (n > cap) n = (int)cap;
+    const int ncell = a.T[0] * a.T[1] * a.T[2];
+    int t0[3];
+    {
+        long r = tile;
+        for (int d = 0; d < 3; d++) {
+            t0[d] = (int)(r % a.ntile[d]) * a.T[d] + 1;
+            r /= a.ntile[d];
+        }
+    }
+    for (int k = threadIdx.x; k < ncell; k += blockDim.x) hist[k] = 0;
+    __syncthreads();
+    const long base = tile * cap;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        int lc = sd.in.ix[0][base + i] - t0[0];
+        if (dim > 1) lc += a.T[0] * (sd.in.ix[1][base + i] - t0[1]);
+        if (dim > 2) lc += a.T[0] * a.T[1] * (sd.in.ix[2][base + i] - t0[2]);
+        atomicAdd(&hist[min(max(lc, 0), ncell - 1)], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) warp_exclusive_scan(hist, ncell);
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const long src = base + i;
+        int lc = sd.in.ix[0][src] - t0[0];
+        if (dim > 1) lc += a.T[0] * (sd.in.ix[1][src] - t0[1]);
+        if (dim > 2) lc += a.T[0] * a.T[1] * (sd.in.ix[2][src] - t0[2]);
+        const long dst = base + atomicAdd(&hist[min(max(lc, 0), ncell - 1)], 1);
+        for (int d = 0; d < dim; d++) {
+            sd.out.ix[d][dst] = sd.in.ix[d][src];
+            sd.out.x[d][dst] = sd.in.x[d][src];
+        }
+        sd.out.u[0][dst] = sd.in.u[0][src];
+        sd.out.u[1][dst] = sd.in.u[1][src];
+        sd.out.u[2][dst] = sd.in.u[2][src];
+        sd.out.q[dst] = sd.in.q[src];
+    }
+    if (threadIdx.x == 0) sd.out.cnt[tile] = n;
 }
 
 // slab -> reference layout (ix(dim,N), x(dim,N), p(3,N), q(N)) at offsets off[tile]
@@ -452,6 +521,8 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
         delete t;
         return OSG_ERR_ARG;
     }
+    if (const char *ev = getenv("OSG_LOCAL_SORT")) t->local_sort = atoi(ev) != 0;
+    if (const char *ev = getenv("OSG_REDUCE_MIN")) t->reduce_min = atoi(ev);
     if (const char *ev = getenv("OSG_PUSH_THREADS")) {
         const int v = atoi(ev);
         if (v >= 64 && v <= 256 && v % 32 == 0) t->threads = v;
@@ -647,6 +718,8 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     a.nspec = ns;
     a.ene = d_ene;
     a.status = d_status;
+    a.local_sort = t->local_sort;
+    a.reduce_min = t->reduce_min;
     const size_t sm = t->smem_bytes;
 #define OSG_TCASE(D, O)                                                                       \
     if (t->dim == D && t->order == O) {                                                       \
@@ -659,6 +732,20 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
 #undef OSG_TCASE
     set_error("tiled engine: unsupported dim %d order %d", t->dim, t->order);
     return OSG_ERR_ARG;
+}
+
+int tiled_sort(TiledState *t, int in_buf, cudaStream_t st, int *launches)
+{
+    const int ns = (int)t->rqm.size();
+    if (ns == 0) return OSG_OK;
+    TiledArgs a = base_args(t);
+    a.spec = t->d_tab[in_buf];
+    a.nspec = ns;
+    const int ncell = t->T[0] * t->T[1] * t->T[2];
+    dim3 grid((unsigned)t->ntiles, (unsigned)ns);
+    k_tile_sort<<<grid, 256, sizeof(int) * ncell, st>>>(a, t->dim);
+    *launches += 1;
+    return OSG_OK;
 }
 
 int tiled_count(TiledState *t, int cur, int k, long *np, cudaStream_t st)

@@ -50,9 +50,11 @@ def _setup(oracle, prec, dim, order, nx, ppc, seed, uth=0.3, ufl=0.2):
     return p, g, dx, dt, species, e, b
 
 
-def _compare(osg, oracle, prec, engine, dim, order, nx, ppc, steps, tol, tile=None, seed=5):
+def _compare(osg, oracle, prec, engine, dim, order, nx, ppc, steps, tol, tile=None, seed=5,
+             n_sort=0):
     p, g, dx, dt, species, e, b = _setup(oracle, prec, dim, order, nx, ppc, seed)
-    sim = osg.Simulation(nx, dx, dt, order=order, precision=prec, engine=engine, tile=tile)
+    sim = osg.Simulation(nx, dx, dt, order=order, precision=prec, engine=engine, tile=tile,
+                         n_sort=n_sort)
     sim.set_fields(e, b)
     for s in species:
         sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
@@ -98,6 +100,20 @@ def test_fp32_engines_match_oracle(osg, oracle, engine, dim, order, nx, tile, st
     eng = osg.ENGINE_TILED if engine == "tiled" else osg.ENGINE_PLAIN
     _compare(osg, oracle, 32, eng, dim, order, nx, [2] * dim, steps, tol,
              tile=tile if eng == osg.ENGINE_TILED else None)
+
+
+@pytest.mark.parametrize("local_sort", ["0", "1"])
+@pytest.mark.parametrize("n_sort", [1, 3, -1])
+@pytest.mark.parametrize("dim,order,nx,tile", [(2, 2, [32, 24], [8, 8]),
+                                               (3, 2, [16, 8, 8], [4, 4, 4])])
+def test_tiled_sort_schedules_match_oracle(osg, oracle, monkeypatch, local_sort, n_sort, dim,
+                                           order, nx, tile):
+    """The periodic per-tile cell sort (every n_sort steps; -1 = never) and the per-iteration
+    ordering of the particles that stay in their tile only reorder particles: 10 steps still
+    match the oracle, and the sort step keeps the particle buffers consistent."""
+    monkeypatch.setenv("OSG_LOCAL_SORT", local_sort)
+    _compare(osg, oracle, 32, osg.ENGINE_TILED, dim, order, nx, [2] * dim, 10, 5e-5, tile=tile,
+             n_sort=n_sort)
 
 
 @pytest.mark.parametrize("prec,engine,tol", [(64, "plain", 1e-11), (32, "tiled", 2e-4)])
