@@ -162,7 +162,7 @@ typedef struct {
     double dx[3];     /* cell size */
     double dt;        /* time step (checked against the Courant limit) */
     int tile[3];      /* tile shape in cells (TILED; 0 = automatic) */
-    int n_sort;       /* PLAIN: cell sort every n_sort steps (0 = never) */
+    int n_sort;       /* PLAIN: cell sort every n_sort steps (0 = never); TILED sorts every step */
     double capacity;  /* TILED: slots per tile as a multiple of the mean load (0 = 3.0) */
 } osg_config;
 

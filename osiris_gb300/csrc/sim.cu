@@ -267,11 +267,6 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, PhaseEvents *pe)
             launches += 5;
         }
     }
-    if (with_sort && c.engine == OSG_ENGINE_TILED) {
-        // the push wrote buffer 1 - parity; the sort brings it back, cell-ordered, to parity
-        int rc = tiled_sort(s->tiled, 1 - parity, st, &launches);
-        if (rc) return rc;
-    }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[3], st));
     periodic_update<T>(s->g, (T *)s->j, 1, st);
     launches += c.dim;
@@ -324,13 +319,14 @@ static int get_graph(osg_sim *s, int parity, int sort, cudaGraphExec_t *out)
 
 static bool sort_due(const osg_sim *s, long n)
 {
-    return s->cfg.n_sort > 0 && n > 0 && (n % s->cfg.n_sort) == 0;
+    return s->cfg.engine == OSG_ENGINE_PLAIN && s->cfg.n_sort > 0 && n > 0 &&
+           (n % s->cfg.n_sort) == 0;
 }
 
-// buffer bookkeeping of the tiled engine after one step
-static void advance_buffers(osg_sim *s, bool sorted)
+// buffer bookkeeping of the tiled engine after one step (the push writes the other buffer)
+static void advance_buffers(osg_sim *s)
 {
-    if (s->cfg.engine == OSG_ENGINE_TILED && !sorted) s->cur ^= 1;
+    if (s->cfg.engine == OSG_ENGINE_TILED) s->cur ^= 1;
 }
 
 static int check_status(osg_sim *s)
@@ -389,10 +385,6 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               "dt violates the Yee Courant limit %g", std::sqrt(1.0 / cour));
     osg_sim *s = new osg_sim();
     s->cfg = *cfg;
-    // n_sort: 0 = engine default (plain: every 25 steps, the reference's default n_sort,
-    // docs/reference/Species.md; tiled: every 20 steps), < 0 = never
-    if (s->cfg.n_sort == 0) s->cfg.n_sort = cfg->engine == OSG_ENGINE_TILED ? 20 : 25;
-    if (s->cfg.n_sort < 0) s->cfg.n_sort = 0;
     for (int d = cfg->dim; d < 3; d++) {
         s->cfg.nx[d] = 1;
         s->cfg.dx[d] = 1.0;
@@ -589,7 +581,7 @@ int osg_sim_step_async(osg_sim *s, int nsteps)
         int rc = get_graph(s, parity, sort, &ge);
         if (rc) return rc;
         OSG_CUDA(cudaGraphLaunch(ge, s->st));
-        advance_buffers(s, sort != 0);
+        advance_buffers(s);
         s->step_n++;
     }
     return OSG_OK;
@@ -723,7 +715,7 @@ int osg_sim_profile(osg_sim *s, int nsteps, float *ms_phase)
         const bool sort = sort_due(s, s->step_n);
         rc = enqueue_step_any(s, parity, sort, &pe);
         if (rc) break;
-        advance_buffers(s, sort);
+        advance_buffers(s);
         s->step_n++;
         if (cudaEventSynchronize(pe.ev[5]) != cudaSuccess) {
             set_error("profiled step failed");

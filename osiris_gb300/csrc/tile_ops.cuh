@@ -263,37 +263,94 @@ __device__ __forceinline__ int seg_offset(int vi, int jsy, int jsz)
     }
 }
 
-// Reduce 32 values held by every lane across the warp so that lane l ends with the warp sum
-// of value l (recursive halving: 31 shuffles for 32 sums).
-__device__ __forceinline__ float transpose_reduce32(float (&t)[32])
+// Reduce N <= 32 values held by every lane across the warp so that each lane ends with the
+// warp sum of one value (recursive halving with uneven halves: a step over N values exchanges
+// ceil(N/2) of them, so 21 values take 11+6+3+2+1 = 23 shuffles instead of 31).  The sum ends
+// in t[0]; transpose_slot<N>(lane) says which value that is (-1: none).
+template <int N, int D>
+__device__ __forceinline__ void transpose_step(float *t, unsigned lane)
 {
-    const unsigned lane = threadIdx.x & 31;
+    constexpr int M = (N + 1) / 2;
+    const bool upper = (lane & D) != 0;
 #pragma unroll
-    for (int step = 16; step >= 1; step >>= 1) {
-        const bool upper = (lane & step) != 0;
-#pragma unroll
-        for (int k = 0; k < step; k++) {
-            const float send = upper ? t[k] : t[k + step];
-            const float keep = upper ? t[k + step] : t[k];
-            t[k] = keep + __shfl_xor_sync(FULL_MASK, send, step);
-        }
+    for (int k = 0; k < M; k++) {
+        const float lo = t[k];
+        const float hi = (M + k < N) ? t[M + k] : 0.f;
+        const float send = upper ? lo : hi;
+        const float keep = upper ? hi : lo;
+        t[k] = keep + __shfl_xor_sync(FULL_MASK, send, D);
     }
+    if constexpr (D > 1) transpose_step<M, D / 2>(t, lane);
+}
+
+template <int N>
+__device__ __forceinline__ float transpose_reduce(float (&t)[N])
+{
+    static_assert(N >= 1 && N <= 32, "one batch holds at most 32 values");
+    transpose_step<N, 16>(t, threadIdx.x & 31);
     return t[0];
 }
+
+template <int N, int D>
+__device__ __forceinline__ int transpose_slot_step(unsigned lane, int lo, int n)
+{
+    constexpr int M = (N + 1) / 2;
+    if (lane & D) {
+        lo += M;
+        n -= M;
+    } else {
+        n = n < M ? n : M;
+    }
+    if constexpr (D > 1)
+        return transpose_slot_step<M, D / 2>(lane, lo, n);
+    else
+        return n > 0 ? lo : -1;
+}
+
+template <int N>
+__device__ __forceinline__ int transpose_slot(unsigned lane)
+{
+    return transpose_slot_step<N, 16>(lane, 0, N);
+}
+
+// Per-lane targets of the reduced sums of one segment: for batch b of 32 values, the offset
+// (in floats, from the stencil origin) of the value that lands in this lane, or -1.
+template <int DIM, int ORD> struct LaneSlots {
+    static constexpr int NV = SegVals<DIM, ORD>::NV;
+    static constexpr int NB = (NV + 31) / 32;
+    int off[NB];
+    __device__ __forceinline__ void init(int jsy, int jsz)
+    {
+        const unsigned lane = threadIdx.x & 31;
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            constexpr int REST = NV % 32 == 0 ? 32 : NV % 32;
+            const int slot = b < NB - 1 ? (int)lane : transpose_slot<REST>(lane);
+            off[b] = slot >= 0 ? seg_offset<DIM, ORD>(32 * b + slot, jsy, jsz) : -1;
+        }
+    }
+};
+
+// 2D: every warp of the push CTA owns a copy of the shared current tile
+template <int DIM>
+constexpr bool private_current() { return DIM == 2; }
 
 // Warp-cooperative accumulation of one segment per lane into the shared current tile.
 // base = offset of the lane's stencil origin, or -1 when the lane has no segment.  Lanes whose
 // cell is shared by at least `reduce_min` lanes of the warp are summed in registers first
-// (transpose-reduce, one pass per such cell), so every shared-memory add of a pass hits a
-// distinct address and lanes that deposit into the same cell never serialise on conflicting
-// atomics.  Lanes of sparsely populated cells (fewer peers) add their values directly: a
-// reduce pass costs about four times a direct pass, which only pays when many lanes share it.
+// (transpose-reduce, one pass per such cell): every add of a pass hits a distinct address, so
+// on a warp-private tile (2D) a pass is a plain read-modify-write and on the shared tile (3D)
+// its atomics never conflict.  Lanes of sparsely populated cells add their values directly
+// (shared atomics): a reduce pass costs several direct adds and only pays when enough lanes
+// share it.  Must be called by all 32 lanes.
 template <int DIM, int ORD>
 __device__ __forceinline__ void warp_deposit(float *sJ, int base, const float *v, int jsy,
-                                             int jsz, int reduce_min)
+                                             int jsz, int reduce_min,
+                                             const LaneSlots<DIM, ORD> &ls)
 {
     constexpr int NV = SegVals<DIM, ORD>::NV;
     constexpr int NB = (NV + 31) / 32;
+    constexpr bool PRIV = private_current<DIM>();
     const unsigned lane = threadIdx.x & 31;
     const unsigned peers = __match_any_sync(FULL_MASK, base);
     const bool active = base >= 0;
@@ -302,6 +359,7 @@ __device__ __forceinline__ void warp_deposit(float *sJ, int base, const float *v
 #pragma unroll
         for (int i = 0; i < NV; i++) atomicAdd(sJ + base + seg_offset<DIM, ORD>(i, jsy, jsz), v[i]);
     }
+    if (PRIV) __syncwarp();
     unsigned rem = __ballot_sync(FULL_MASK, active && !direct && (__ffs(peers) - 1) == (int)lane);
     while (rem) {
         const int l = __ffs(rem) - 1;
@@ -310,21 +368,33 @@ __device__ __forceinline__ void warp_deposit(float *sJ, int base, const float *v
         const bool mine = base == key;
 #pragma unroll
         for (int bch = 0; bch < NB; bch++) {
-            float t[32];
+            constexpr int REST = NV % 32 == 0 ? 32 : NV % 32;
+            float sum;
+            if (bch < NB - 1) {
+                float t[32];
 #pragma unroll
-            for (int k = 0; k < 32; k++) {
-                const int i = bch * 32 + k;
-                t[k] = (i < NV && mine) ? v[i < NV ? i : 0] : 0.f;
+                for (int k = 0; k < 32; k++) t[k] = mine ? v[bch * 32 + k] : 0.f;
+                sum = transpose_reduce<32>(t);
+            } else {
+                float t[REST];
+#pragma unroll
+                for (int k = 0; k < REST; k++) t[k] = mine ? v[bch * 32 + k] : 0.f;
+                sum = transpose_reduce<REST>(t);
             }
-            const float sum = transpose_reduce32(t);
-            const int i = bch * 32 + (int)lane;
-            if (i < NV) atomicAdd(sJ + key + seg_offset<DIM, ORD>(i, jsy, jsz), sum);
+            if (ls.off[bch] >= 0) {
+                float *pj = sJ + key + ls.off[bch];
+                if (PRIV)
+                    *pj += sum;
+                else
+                    atomicAdd(pj, sum);
+            }
         }
+        if (PRIV) __syncwarp();
     }
 }
 
 // ------------------------------------------------------------------------------------------
-// Segment records in the shared segment buffer: a = {x0, x1, y0, y1, z0, z1} (2D: a[4] = vz),
+// Segment record (held in registers): a = {x0, x1, y0, y1, z0, z1} (2D: a[4] = vz),
 // base = offset of the segment's stencil origin in the shared current tile (-1 = empty).
 // ------------------------------------------------------------------------------------------
 struct alignas(16) SegRec {
@@ -370,13 +440,6 @@ __device__ __forceinline__ int make_segments(SegRec *out, const float *xo, const
     }
 }
 
-// lane order that puts the particles of one warp nthr/32 slots apart (consecutive particles
-// usually share a cell; spreading them removes most shared-memory address conflicts)
-__device__ __forceinline__ int spread_index(int t, int nthr)
-{
-    return (t & 31) * (nthr >> 5) + (t >> 5);
-}
-
 // Deposit one segment per lane (rec = nullptr: no segment).  reduce_min > 32 selects plain
 // per-lane shared atomics (no warp-synchronous part); otherwise warp_deposit.  3D cubic and
 // quartic segments (144 and 300 values) always add directly: their values do not fit in
@@ -386,7 +449,8 @@ constexpr bool direct_only() { return DIM == 3 && ORD >= 3; }
 
 template <int DIM, int ORD>
 __device__ __forceinline__ void deposit_segment(float *sJ, const SegRec *rec, const float *jn,
-                                                int jsy, int jsz, int reduce_min)
+                                                int jsy, int jsz, int reduce_min,
+                                                const LaneSlots<DIM, ORD> &ls)
 {
     if constexpr (DIM == 3) {
         if (direct_only<DIM, ORD>() || reduce_min > 32) {
@@ -420,7 +484,7 @@ __device__ __forceinline__ void deposit_segment(float *sJ, const SegRec *rec, co
 #pragma unroll
         for (int k = 0; k < NV; k++) v[k] = 0.f;
     }
-    warp_deposit<DIM, ORD>(sJ, base, v, jsy, jsz, reduce_min);
+    warp_deposit<DIM, ORD>(sJ, base, v, jsy, jsz, reduce_min, ls);
     }
 }
 

@@ -2,24 +2,29 @@
 //
 // Layout in HBM: for every species two particle buffers (ping-pong), each a set of SoA
 // streams (cell index per axis, in-cell offset per axis, three momenta, charge) cut into
-// fixed-capacity slabs, one slab per tile; a per-tile count says how many slots are live.
+// fixed-capacity slabs, one slab per tile.  A slab holds the tile's particles sorted by cell in
+// slots [0, cnt) and the particles that arrived from other tiles during the last step in slots
+// [cap - arr, cap) (filled from the top).
 //
 // One push launch handles every species: CTA t owns tile t.  It stages E and B of the tile
-// plus the stencil halo in shared memory, zeroes a shared-memory current tile with its halo,
-// and for each species streams the tile's particles (coalesced SoA loads), gathers the fields
-// from shared memory, does the Boris push, moves, trims and periodically wraps the particle,
-// splits the trajectory at cell faces and accumulates the charge-conserving current of every
-// segment into the shared tile (shared-memory atomics), then writes the particle into the
-// slab of the tile that now contains it in the other buffer (warp-aggregated slot reservation
-// for particles that stay, one atomic per particle that leaves).  The shared current tile is
-// added to the global current at the end (the halo overlaps the neighbours' halos).
+// plus the stencil halo in shared memory and zeroes a shared current tile with its halo (one
+// copy per warp in 2D).  Per species, every warp streams chunks of the tile's particles
+// (coalesced SoA loads, the next chunk prefetched), gathers the fields from shared memory,
+// does the Boris push, moves, trims and periodically wraps the particle, splits the trajectory
+// at cell faces and accumulates the charge-conserving current of every segment into the shared
+// tile (warp transpose-reduce per cell, or direct shared adds).  Particles that stay are
+// written back to their own input slot and counted per cell; particles that leave are queued
+// in shared memory and then appended to the arrival region of their destination tile in the
+// other buffer.  A second pass counting-sorts the particles that stayed into the other buffer,
+// so every step starts from cell-sorted tiles.  The shared current tile is added to the global
+// current at the end (the halo overlaps the neighbours' halos).
 //
 // The per-particle arithmetic is the same as the plain engine (pic_math.cuh) and therefore the
 // same as the reference kernels FNAME(vadvance_deposit_{2d,3d}_sN) (source/simd/
 // os-spec-push-avx2.c:471-760, :1141-1480); only the order in which current contributions are
-// summed differs.  The particle migration replaces both the periodic particle boundary
-// (source/spec/os-spec-boundary.f03:1280-1290) and the cell sort (source/spec/os-species.f03:
-// 269-505): particles are re-binned by tile every step.
+// summed differs.  The migration and the per-step tile sort replace both the periodic particle
+// boundary (source/spec/os-spec-boundary.f03:1280-1290) and the cell sort every n_sort steps
+// (source/spec/os-species.f03:269-505).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -42,7 +47,8 @@ struct Slabs {
     float *x[3];
     float *u[3];
     float *q;
-    int *cnt;      // [ntiles]
+    int *cnt;      // [ntiles] particles in slots [0, cnt) of the slab, sorted by cell
+    int *arr;      // [ntiles] particles that arrived from other tiles, slots [cap - arr, cap)
 };
 
 struct SpeciesDev {
@@ -67,7 +73,6 @@ struct TiledArgs {
     int nspec;
     double *ene;
     int *status;
-    int local_sort;    // write stayers of each block iteration in cell order
     int reduce_min;    // warp-reduce a cell's segments when at least this many lanes share it
 };
 
@@ -84,17 +89,17 @@ struct TiledState {
     std::vector<void *> allocs;
     int *d_cnt[2] = {nullptr, nullptr};   // [MAX_TILED_SPECIES * ntiles] per buffer
     SpeciesDev *d_tab[2] = {nullptr, nullptr};
+    int *d_arr[2] = {nullptr, nullptr};   // arrival counters, [species][tile] per buffer
     int *d_off = nullptr;
     void *d_compact = nullptr;
     size_t compact_bytes = 0;
     size_t smem_bytes = 0;
     int threads = 128;   // threads per push CTA (multiple of 32, <= 256)
-    int local_sort = 1;
-    int reduce_min = 2;
+    int reduce_min = 2;  // set per dimension in tiled_create
 };
 
 static const int MAX_TILED_SPECIES = 16;
-static const int MAX_TILE_CELLS = 1024;   // cells per tile (shared counting-sort bins)
+static const int MAX_TILE_CELLS = 1024;   // cells per tile (bins of the per-tile cell sort)
 
 __device__ __forceinline__ int wrapc(int c, int n)
 {
@@ -124,11 +129,46 @@ __device__ __forceinline__ int warp_exclusive_scan(int *c, int n)
 }
 
 // --------------------------------------------------------------------------------- push
+static const int LEAVE_QUEUE = 256;   // particles per CTA and species queued for emigration
+
+// Write a particle that left its tile into an arrival slot (from the top of the slab) of its
+// destination tile in the output buffer.  The arrival region stays above the particles the
+// destination keeps this step: those are at most its input particles.
+template <int DIM>
+__device__ __forceinline__ void emigrate(const SpeciesDev &sd, long cap, long dest,
+                                         const int *cw, const float *xo, const float *un,
+                                         float q, int *status)
+{
+    const int k = atomicAdd(sd.out.arr + dest, 1);
+    const int room = (int)cap - sd.in.cnt[dest] - sd.in.arr[dest];
+    if (k >= room) {
+        atomicOr(status, OSG_STATUS_OVERFLOW);
+        return;
+    }
+    const long o = dest * cap + cap - 1 - k;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+        sd.out.ix[d][o] = cw[d];
+        sd.out.x[d][o] = xo[d];
+    }
+    sd.out.u[0][o] = un[0];
+    sd.out.u[1][o] = un[1];
+    sd.out.u[2][o] = un[2];
+    sd.out.q[o] = q;
+}
+
+// Every warp of the CTA runs its own pipeline over chunks of 32 particles of the tile, with no
+// block barrier inside the particle loop: load, gather, Boris, move, split, write the particle
+// to its new slot, then deposit the segments (round t takes the t-th segment of every lane).
+// In 2D every warp accumulates into its own copy of the current tile, so the warp-reduced
+// passes add with plain shared read-modify-writes; the copies are summed when the tile is
+// flushed.  In 3D the warps share one current tile (atomic adds).
 template <int DIM, int ORD>
 __global__ void __launch_bounds__(256) k_push_tiled(TiledArgs a)
 {
     constexpr int NP = ORD + 1, OFS = Stencil<ORD>::OFS;
     constexpr int MAXSEG = DIM == 2 ? 3 : 4;
+    constexpr bool PRIV = private_current<DIM>();
     extern __shared__ float smem[];
     const long tile = blockIdx.x;
     int t0[3], tc[3];
@@ -146,12 +186,14 @@ __global__ void __launch_bounds__(256) k_push_tiled(TiledArgs a)
         je[d] = d < DIM ? a.T[d] + NP + 1 : 1;
     }
     const int ne = ee[0] * ee[1] * ee[2], nj = je[0] * je[1] * je[2];
+    const int nthr = blockDim.x, nwarp = nthr >> 5, warp = threadIdx.x >> 5;
+    const int njall = 3 * nj * (PRIV ? nwarp : 1);
     float *sE = smem, *sB = smem + 3 * ne, *sJ = smem + 6 * ne;
     const long gsy = 3L * a.size[0], gsz = 3L * a.size[0] * a.size[1];
 
     // stage fields: local point l <-> Fortran cell t0 - OFS + l <-> global position
     // t0 - OFS + l - 1 + gcl (inside the guard cells for tiles at the box edge)
-    for (int idx = threadIdx.x; idx < 3 * ne; idx += blockDim.x) {
+    for (int idx = threadIdx.x; idx < 3 * ne; idx += nthr) {
         const int c = idx % 3, pnt = idx / 3;
         const int lx = pnt % ee[0], ly = (pnt / ee[0]) % ee[1], lz = pnt / (ee[0] * ee[1]);
         long gp = 3L * (t0[0] - OFS + lx - 1 + a.gcl[0]) + c;
@@ -160,63 +202,95 @@ __global__ void __launch_bounds__(256) k_push_tiled(TiledArgs a)
         sE[idx] = __ldg(a.e + gp);
         sB[idx] = __ldg(a.b + gp);
     }
-    for (int idx = threadIdx.x; idx < 3 * nj; idx += blockDim.x) sJ[idx] = 0.0f;
+    for (int idx = threadIdx.x; idx < njall; idx += nthr) sJ[idx] = 0.0f;
     __syncthreads();
 
     const int esy = 3 * ee[0], esz = 3 * ee[0] * ee[1];
     const int jsy = 3 * je[0], jsz = 3 * je[0] * je[1];
     const unsigned lane = threadIdx.x & 31;
+    float *sJw = PRIV ? sJ + 3 * nj * warp : sJ;
+    LaneSlots<DIM, ORD> ls;
+    ls.init(jsy, jsz);
+    // 3D direct deposits: every thread walks its own contiguous run of the cell-sorted tile,
+    // so the lanes of a warp sit in cells far apart and their shared-memory atomics seldom
+    // conflict; otherwise a warp takes 32 consecutive particles (mostly one cell)
+    const bool spread = DIM == 3 && (direct_only<DIM, ORD>() || a.reduce_min > 32);
 
-    // segment buffer: [0, blockDim) first segment of each thread's particle (particle order),
-    // [blockDim, MAXSEG * blockDim) the extra segments of split trajectories, compacted
-    SegRec *sSeg = reinterpret_cast<SegRec *>(smem + ((6 * ne + 3 * nj + 3) & ~3));
-    // per-iteration counters, double-buffered so the spare copy is cleared while the other is
-    // in use (three block barriers per iteration)
-    __shared__ int sNextra[2], sStayBase;
-    __shared__ int sCellCnt[2][MAX_TILE_CELLS];
-    const int nthr = blockDim.x;
-    const int ncell_tile = a.T[0] * a.T[1] * a.T[2];
-    for (int k = threadIdx.x; k < ncell_tile; k += nthr) sCellCnt[0][k] = sCellCnt[1][k] = 0;
-    if (threadIdx.x == 0) sNextra[0] = sNextra[1] = 0;
-    __syncthreads();
-    int it = 0;
+    __shared__ int sHist[MAX_TILE_CELLS];
+    // particles leaving the tile wait in a shared queue; after the pass they take their
+    // arrival slots all at once, so no warp waits on a global atomic inside the pass
+    __shared__ int sLeaveI[LEAVE_QUEUE][4];      // new cell per axis, destination tile
+    __shared__ float sLeaveF[LEAVE_QUEUE][8];    // offsets per axis, momenta, charge
+    __shared__ int sNleave;
+    const int ncell = a.T[0] * a.T[1] * a.T[2];
 
     for (int s = 0; s < a.nspec; s++) {
         const SpeciesDev sd = a.spec[s];
         const long cap = sd.cap;
         const long slab = tile * cap;
-        int cnt = sd.in.cnt[tile];
-        if (cnt > cap) cnt = (int)cap;
+        const int nst = min(sd.in.cnt[tile], (int)cap);
+        const int nar = min(sd.in.arr[tile], (int)cap - nst);
+        const int n = nst + nar;
+        for (int k = threadIdx.x; k < ncell; k += nthr) sHist[k] = 0;
+        if (threadIdx.x == 0) sNleave = 0;
+        __syncthreads();
         // per-thread partial energy in FP32 (the reference sums in single precision per
         // 464-particle chunk), summed over the block in double
         float my_ene = 0.f;
-        for (int base = 0; base < cnt; base += nthr, it++) {
-            const int bp = it & 1;
-            int *cellCnt = sCellCnt[bp];
-            const int i = base + threadIdx.x;
-            bool has = i < cnt;
-            int c[3] = {1, 1, 1}, cw[3] = {1, 1, 1}, di[3] = {0, 0, 0};
+        // ---- pass A: push every particle of the tile.  Particles that stay are written back
+        //      to their own slot of the input slab (this CTA owns it) and counted per new cell;
+        //      particles that leave take an arrival slot (from the top) of their destination
+        //      tile in the output buffer, and their input slot is marked empty (ix = 0).
+        // the particle of the next iteration is loaded while this one is pushed
+        const int nit = (n + nthr - 1) / nthr;
+        auto index = [&](int it) {
+            return spread ? (int)threadIdx.x * nit + it : it * nthr + (int)threadIdx.x;
+        };
+        int pf_c[3] = {1, 1, 1};
+        float pf_x[3] = {0, 0, 0}, pf_u[3] = {0, 0, 0}, pf_q = 0.0f;
+        auto prefetch = [&](int i) {
+            if (i < n) {
+                const long p = slab + (i < nst ? i : cap - 1 - (i - nst));
+#pragma unroll
+                for (int d = 0; d < DIM; d++) {
+                    pf_c[d] = sd.in.ix[d][p];
+                    pf_x[d] = sd.in.x[d][p];
+                }
+                pf_u[0] = sd.in.u[0][p];
+                pf_u[1] = sd.in.u[1][p];
+                pf_u[2] = sd.in.u[2][p];
+                pf_q = sd.in.q[p];
+            }
+        };
+        prefetch(index(0));
+        for (int it = 0; it < nit; it++) {
+            const int i = index(it);
+            bool has = i < n;
+            const long p = slab + (i < nst ? i : cap - 1 - (i - nst));
+            int c[3] = {1, 1, 1}, di[3] = {0, 0, 0};
             float xo[3] = {0, 0, 0}, x1[3] = {0, 0, 0}, un[3] = {0, 0, 0}, q = 0.0f;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                c[d] = pf_c[d];
+                xo[d] = pf_x[d];
+                un[d] = pf_u[d];
+            }
+            q = pf_q;
+            if (it + 1 < nit) prefetch(index(it + 1));
             if (has) {
-                const long p = slab + i;
                 bool ok = true;
 #pragma unroll
                 for (int d = 0; d < DIM; d++) {
-                    c[d] = sd.in.ix[d][p];
-                    xo[d] = sd.in.x[d][p];
                     const int lc = c[d] - t0[d];
                     ok = ok && lc >= 0 && lc < a.T[d];
                 }
-                un[0] = sd.in.u[0][p];
-                un[1] = sd.in.u[1][p];
-                un[2] = sd.in.u[2][p];
-                q = sd.in.q[p];
                 if (!ok) {
                     atomicOr(a.status, OSG_STATUS_RANGE);
+                    sd.in.ix[0][p] = 0;
                     has = false;
                 }
             }
-            // ---- phase 1: gather from the staged tile, Boris, move, split into segments
+            // ---- gather from the staged tile, Boris, move, split into segments
             int nseg = 0;
             SegRec sg[MAXSEG];
             if (has) {
@@ -245,108 +319,137 @@ __global__ void __launch_bounds__(256) k_push_tiled(TiledArgs a)
                                           c[1] - t0[1] + 1, DIM > 2 ? c[2] - t0[2] + 1 : 0,
                                           jsy, jsz);
             }
-            // primary segment in particle order, extras compacted after the primaries
-            sSeg[threadIdx.x] = sg[0];
-            if (!has) sSeg[threadIdx.x].base = -1;
-            {
-                const int nx_ = has ? nseg - 1 : 0;
-                int incl = nx_;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int y = __shfl_up_sync(FULL_MASK, incl, o);
-                    if ((int)lane >= o) incl += y;
-                }
-                const int wtot = __shfl_sync(FULL_MASK, incl, 31);
-                int wbase = 0;
-                if (lane == 31 && wtot) wbase = atomicAdd(&sNextra[bp], wtot);
-                wbase = __shfl_sync(FULL_MASK, wbase, 31);
-                int o = nthr + wbase + incl - nx_;
-                for (int t = 1; t < nseg; t++) sSeg[o++] = sg[t];
-            }
             // ---- new position, cell (periodically wrapped) and destination tile
-            long dest = -1;
-            if (has) {
-                long dt = 0, mul = 1;
+            {
+                long dest = -1;
+                int cw[3] = {1, 1, 1};
+                if (has) {
+                    long dt = 0, mul = 1;
 #pragma unroll
-                for (int d = 0; d < DIM; d++) {
-                    xo[d] = x1[d] - float(di[d]);
-                    cw[d] = wrapc(c[d] + di[d], a.nx[d]);
-                    dt += mul * ((cw[d] - 1) / a.T[d]);
-                    mul *= a.ntile[d];
+                    for (int d = 0; d < DIM; d++) {
+                        xo[d] = x1[d] - float(di[d]);
+                        cw[d] = wrapc(c[d] + di[d], a.nx[d]);
+                        dt += mul * ((cw[d] - 1) / a.T[d]);
+                        mul *= a.ntile[d];
+                    }
+                    dest = dt;
                 }
-                dest = dt;
-            }
-            // ---- migration.  Particles that stay are written in cell order (block counting
-            //      sort over the tile's cells) so that next step the lanes of a warp mostly share
-            //      a cell; particles that leave take one slot each in their destination tile.
-            const bool stay = has && dest == tile;
-            long slot = -1;
-            if (a.local_sort) {
-                int lcell = 0, rank = 0;
+                const bool stay = has && dest == tile;
+                int lcell = -1;
                 if (stay) {
+#pragma unroll
+                    for (int d = 0; d < DIM; d++) {
+                        sd.in.ix[d][p] = cw[d];
+                        sd.in.x[d][p] = xo[d];
+                    }
+                    sd.in.u[0][p] = un[0];
+                    sd.in.u[1][p] = un[1];
+                    sd.in.u[2][p] = un[2];
                     lcell = cw[0] - t0[0];
                     if (DIM > 1) lcell += a.T[0] * (cw[1] - t0[1]);
                     if (DIM > 2) lcell += a.T[0] * a.T[1] * (cw[2] - t0[2]);
-                    rank = atomicAdd(&cellCnt[lcell], 1);
                 }
-                __syncthreads();
-                if (threadIdx.x < 32) {
-                    const int nstay = warp_exclusive_scan(cellCnt, ncell_tile);
-                    if (threadIdx.x == 0) sStayBase = nstay ? atomicAdd(sd.out.cnt + tile, nstay) : 0;
-                }
-                __syncthreads();
-                if (stay) slot = sStayBase + cellCnt[lcell] + rank;
-            } else {
-                // warp-aggregated slots in the own tile, particle order kept per warp
-                const unsigned ms = __ballot_sync(FULL_MASK, stay);
-                if (ms) {
-                    const int leader = __ffs(ms) - 1;
-                    int b0 = 0;
-                    if ((int)lane == leader) b0 = atomicAdd(sd.out.cnt + tile, __popc(ms));
-                    b0 = __shfl_sync(FULL_MASK, b0, leader);
-                    if (stay) slot = b0 + __popc(ms & ((1u << lane) - 1u));
-                }
-            }
-            if (has && !stay) slot = atomicAdd(sd.out.cnt + dest, 1);
-            if (has) {
-                if (slot >= cap) {
-                    atomicOr(a.status, OSG_STATUS_OVERFLOW);
-                } else {
-                    const long o = dest * cap + slot;
+                const unsigned peers = __match_any_sync(FULL_MASK, lcell);
+                if (stay && (int)lane == __ffs(peers) - 1) atomicAdd(&sHist[lcell], __popc(peers));
+                const bool leave = has && !stay;
+                const unsigned ml = __ballot_sync(FULL_MASK, leave);
+                if (ml) {
+                    const int leader = __ffs(ml) - 1;
+                    int q0 = 0;
+                    if ((int)lane == leader) q0 = atomicAdd(&sNleave, __popc(ml));
+                    q0 = __shfl_sync(FULL_MASK, q0, leader);
+                    if (leave) {
+                        sd.in.ix[0][p] = 0;
+                        const int e = q0 + __popc(ml & ((1u << lane) - 1u));
+                        if (e < LEAVE_QUEUE) {
 #pragma unroll
-                    for (int d = 0; d < DIM; d++) {
-                        sd.out.ix[d][o] = cw[d];
-                        sd.out.x[d][o] = xo[d];
+                            for (int d = 0; d < 3; d++) {
+                                sLeaveI[e][d] = cw[d];
+                                sLeaveF[e][d] = xo[d];
+                                sLeaveF[e][3 + d] = un[d];
+                            }
+                            sLeaveI[e][3] = (int)dest;
+                            sLeaveF[e][6] = q;
+                        } else {
+                            emigrate<DIM>(sd, cap, dest, cw, xo, un, q, a.status);
+                        }
                     }
-                    sd.out.u[0][o] = un[0];
-                    sd.out.u[1][o] = un[1];
-                    sd.out.u[2][o] = un[2];
-                    sd.out.q[o] = q;
                 }
             }
-            if (!a.local_sort) __syncthreads();   // segment buffer complete
-            // clear the spare counters for the next iteration
-            int *spare = sCellCnt[bp ^ 1];
-            for (int k = threadIdx.x; k < ncell_tile; k += nthr) spare[k] = 0;
-            if (threadIdx.x == 0) sNextra[bp ^ 1] = 0;
-            // ---- phase 2: charge-conserving current of all segments into the shared tile
-            const int nall = nthr + sNextra[bp];
-            for (int r = 0; r * nthr < nall; r++) {
-                int sidx = r * nthr + threadIdx.x;
-                if (DIM == 3 && r == 0 && (direct_only<DIM, ORD>() || a.reduce_min > 32)) sidx = spread_index(threadIdx.x, nthr);
-                const bool valid = sidx < nall && sSeg[sidx].base >= 0;
-                deposit_segment<DIM, ORD>(sJ, valid ? &sSeg[sidx] : nullptr, a.jn, jsy, jsz,
-                                          a.reduce_min);
+            // ---- charge-conserving current of the segments into the shared tile
+#pragma unroll
+            for (int t = 0; t < MAXSEG; t++) {
+                const bool hs = has && t < nseg;
+                if (!__any_sync(FULL_MASK, hs)) break;
+                deposit_segment<DIM, ORD>(sJw, hs ? &sg[t] : nullptr, a.jn, jsy, jsz,
+                                          a.reduce_min, ls);
             }
-            __syncthreads();
         }
-        const double tot = block_sum((double)my_ene);
+        const double tot = block_sum((double)my_ene);   // (contains block barriers)
         if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.ene + s, tot);
+        // ---- the queued particles that left take their arrival slots
+        {
+            const int nq = min(sNleave, LEAVE_QUEUE);
+            for (int e = threadIdx.x; e < nq; e += nthr) {
+                int cw[3];
+                float xo[3], un[3];
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    cw[d] = sLeaveI[e][d];
+                    xo[d] = sLeaveF[e][d];
+                    un[d] = sLeaveF[e][3 + d];
+                }
+                emigrate<DIM>(sd, cap, sLeaveI[e][3], cw, xo, un, sLeaveF[e][6], a.status);
+            }
+        }
+        // ---- cell offsets of the particles that stayed
+        if (threadIdx.x < 32) {
+            const int nstay = warp_exclusive_scan(sHist, ncell);
+            if (threadIdx.x == 0) sd.out.cnt[tile] = nstay;
+        }
+        __syncthreads();
+        // ---- pass B: counting-sort the particles that stayed into the output slab, so that
+        //      every step starts from particles in cell order (consecutive lanes share a cell)
+        for (int base = 0; base < n; base += nthr) {
+            const int i = base + threadIdx.x;
+            const long p = slab + (i < nst ? i : cap - 1 - (i - nst));
+            int lcell = -1;
+            int cc[3] = {0, 0, 0};
+            if (i < n) {
+#pragma unroll
+                for (int d = 0; d < DIM; d++) cc[d] = sd.in.ix[d][p];
+                if (cc[0] != 0) {
+                    lcell = cc[0] - t0[0];
+                    if (DIM > 1) lcell += a.T[0] * (cc[1] - t0[1]);
+                    if (DIM > 2) lcell += a.T[0] * a.T[1] * (cc[2] - t0[2]);
+                }
+            }
+            const unsigned peers = __match_any_sync(FULL_MASK, lcell);
+            const int leader = __ffs(peers) - 1;
+            int first = 0;
+            if (lcell >= 0 && (int)lane == leader) first = atomicAdd(&sHist[lcell], __popc(peers));
+            first = __shfl_sync(FULL_MASK, first, leader);
+            if (lcell >= 0) {
+                const long o = slab + first + __popc(peers & ((1u << lane) - 1u));
+#pragma unroll
+                for (int d = 0; d < DIM; d++) {
+                    sd.out.ix[d][o] = cc[d];
+                    sd.out.x[d][o] = sd.in.x[d][p];
+                }
+                sd.out.u[0][o] = sd.in.u[0][p];
+                sd.out.u[1][o] = sd.in.u[1][p];
+                sd.out.u[2][o] = sd.in.u[2][p];
+                sd.out.q[o] = sd.in.q[p];
+            }
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    // ---- add the shared current tile (with halo) to the global current
-    for (int idx = threadIdx.x; idx < 3 * nj; idx += blockDim.x) {
-        const float v = sJ[idx];
+    // ---- add the shared current tile (with halo; summed over the warp copies in 2D) to the
+    //      global current
+    for (int idx = threadIdx.x; idx < 3 * nj; idx += nthr) {
+        float v = sJ[idx];
+        if (PRIV)
+            for (int w = 1; w < nwarp; w++) v += sJ[3 * nj * w + idx];
         if (v == 0.0f) continue;
         const int c = idx % 3, pnt = idx / 3;
         const int lx = pnt % je[0], ly = (pnt / je[0]) % je[1], lz = pnt / (je[0] * je[1]);
@@ -378,67 +481,15 @@ __global__ void k_bin(const int *__restrict__ ix, const float *__restrict__ x,
     }
 }
 
-// --------------------------------------------------------------------------------- sort
-// Full counting sort of every tile by cell (x fastest inside the tile): reads the slabs of
-// spec[s].in, writes spec[s].out.  The GPU counterpart of the reference's cell sort every
-// n_sort steps (source/spec/os-species.f03:269-505), per tile instead of over the whole box.
-__global__ void __launch_bounds__(256) k_tile_sort(TiledArgs a, int dim)
-{
-    extern __shared__ int hist[];
-    const long tile = blockIdx.x;
-    const SpeciesDev sd = a.spec[blockIdx.y];
-    const long cap = sd.cap;
-    int n = sd.in.cnt[tile];
-    if (n > cap) n = (int)cap;
-    const int ncell = a.T[0] * a.T[1] * a.T[2];
-    int t0[3];
-    {
-        long r = tile;
-        for (int d = 0; d < 3; d++) {
-            t0[d] = (int)(r % a.ntile[d]) * a.T[d] + 1;
-            r /= a.ntile[d];
-        }
-    }
-    for (int k = threadIdx.x; k < ncell; k += blockDim.x) hist[k] = 0;
-    __syncthreads();
-    const long base = tile * cap;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        int lc = sd.in.ix[0][base + i] - t0[0];
-        if (dim > 1) lc += a.T[0] * (sd.in.ix[1][base + i] - t0[1]);
-        if (dim > 2) lc += a.T[0] * a.T[1] * (sd.in.ix[2][base + i] - t0[2]);
-        atomicAdd(&hist[min(max(lc, 0), ncell - 1)], 1);
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) warp_exclusive_scan(hist, ncell);
-    __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const long src = base + i;
-        int lc = sd.in.ix[0][src] - t0[0];
-        if (dim > 1) lc += a.T[0] * (sd.in.ix[1][src] - t0[1]);
-        if (dim > 2) lc += a.T[0] * a.T[1] * (sd.in.ix[2][src] - t0[2]);
-        const long dst = base + atomicAdd(&hist[min(max(lc, 0), ncell - 1)], 1);
-        for (int d = 0; d < dim; d++) {
-            sd.out.ix[d][dst] = sd.in.ix[d][src];
-            sd.out.x[d][dst] = sd.in.x[d][src];
-        }
-        sd.out.u[0][dst] = sd.in.u[0][src];
-        sd.out.u[1][dst] = sd.in.u[1][src];
-        sd.out.u[2][dst] = sd.in.u[2][src];
-        sd.out.q[dst] = sd.in.q[src];
-    }
-    if (threadIdx.x == 0) sd.out.cnt[tile] = n;
-}
-
 // slab -> reference layout (ix(dim,N), x(dim,N), p(3,N), q(N)) at offsets off[tile]
 __global__ void k_compact(Slabs in, long cap, int dim, const int *__restrict__ off, int *ix,
                           float *x, float *u, float *q)
 {
     const long t = blockIdx.x;
-    int n = in.cnt[t];
-    if (n > cap) n = (int)cap;
+    const int nst = min(in.cnt[t], (int)cap), n = nst + min(in.arr[t], (int)cap - nst);
     const long o = off[t];
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const long src = t * cap + i, dst = o + i;
+        const long src = t * cap + (i < nst ? i : cap - 1 - (i - nst)), dst = o + i;
         for (int d = 0; d < dim; d++) {
             ix[dim * dst + d] = in.ix[d][src];
             x[dim * dst + d] = in.x[d][src];
@@ -474,7 +525,7 @@ static TiledArgs base_args(const TiledState *t)
     return a;
 }
 
-// shared memory of the push kernel: E and B tiles, the current tile, the segment buffer
+// shared memory of the push kernel: E and B tiles and the current tile (one per warp in 2D)
 static size_t smem_for(int dim, int order, const int *T, int threads)
 {
     const int NP = order + 1;
@@ -483,8 +534,8 @@ static size_t smem_for(int dim, int order, const int *T, int threads)
         ne *= (size_t)(T[d] + NP);
         nj *= (size_t)(T[d] + NP + 1);
     }
-    const size_t fields = ((6 * ne + 3 * nj + 3) & ~(size_t)3) * sizeof(float);
-    return fields + sizeof(SegRec) * (dim == 2 ? 3 : 4) * threads;
+    const size_t copies = dim == 2 ? (size_t)threads / 32 : 1;
+    return (6 * ne + 3 * nj * copies) * sizeof(float);
 }
 
 int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
@@ -516,12 +567,19 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
         t->ntile[d] = t->nx[d] / T;
         t->ntiles *= t->ntile[d];
     }
+    if (t->ntiles >= (1L << 30)) {
+        set_error("too many tiles (%ld)", t->ntiles);
+        delete t;
+        return OSG_ERR_ARG;
+    }
     if ((long)t->T[0] * t->T[1] * t->T[2] > MAX_TILE_CELLS) {
         set_error("a tile may hold at most %d cells", MAX_TILE_CELLS);
         delete t;
         return OSG_ERR_ARG;
     }
-    if (const char *ev = getenv("OSG_LOCAL_SORT")) t->local_sort = atoi(ev) != 0;
+    // 2D: warp-reduce every cell that two or more lanes share; 3D (54..300 values per segment,
+    // lanes of one warp spread over the tile): direct shared atomics measured faster
+    t->reduce_min = t->dim == 2 ? 2 : 33;
     if (const char *ev = getenv("OSG_REDUCE_MIN")) t->reduce_min = atoi(ev);
     if (const char *ev = getenv("OSG_PUSH_THREADS")) {
         const int v = atoi(ev);
@@ -552,12 +610,14 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
     }
     for (int p = 0; p < 2; p++) {
         if (cudaMalloc(&t->d_cnt[p], sizeof(int) * MAX_TILED_SPECIES * t->ntiles) != cudaSuccess ||
+            cudaMalloc(&t->d_arr[p], sizeof(int) * MAX_TILED_SPECIES * t->ntiles) != cudaSuccess ||
             cudaMalloc(&t->d_tab[p], sizeof(SpeciesDev) * MAX_TILED_SPECIES) != cudaSuccess) {
             tiled_destroy(t);
             set_error("tile count allocation failed");
             return OSG_ERR_NOMEM;
         }
         cudaMemset(t->d_cnt[p], 0, sizeof(int) * MAX_TILED_SPECIES * t->ntiles);
+        cudaMemset(t->d_arr[p], 0, sizeof(int) * MAX_TILED_SPECIES * t->ntiles);
     }
     if (cudaMalloc(&t->d_off, sizeof(int) * t->ntiles) != cudaSuccess) {
         tiled_destroy(t);
@@ -574,6 +634,7 @@ void tiled_destroy(TiledState *t)
     for (void *p : t->allocs) cudaFree(p);
     for (int p = 0; p < 2; p++) {
         cudaFree(t->d_cnt[p]);
+        cudaFree(t->d_arr[p]);
         cudaFree(t->d_tab[p]);
     }
     cudaFree(t->d_off);
@@ -664,6 +725,8 @@ int tiled_add_species(TiledState *t, double rqm, long np, const int *ix, const f
         }
         s.q = (float *)(mem + o);
         s.cnt = t->d_cnt[p] + (size_t)k * t->ntiles;
+        s.arr = t->d_arr[p] + (size_t)k * t->ntiles;
+        OSG_CUDA(cudaMemsetAsync(s.arr, 0, sizeof(int) * t->ntiles, st));
         t->buf[p].push_back(s);
     }
     t->rqm.push_back(rqm);
@@ -709,7 +772,8 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
 {
     const int ns = (int)t->rqm.size();
     if (ns == 0) return OSG_OK;
-    OSG_CUDA(cudaMemsetAsync(t->d_cnt[1 - parity], 0, sizeof(int) * MAX_TILED_SPECIES * t->ntiles, st));
+    // the push writes every tile's sorted count and adds arrivals to zeroed counters
+    OSG_CUDA(cudaMemsetAsync(t->d_arr[1 - parity], 0, sizeof(int) * MAX_TILED_SPECIES * t->ntiles, st));
     TiledArgs a = base_args(t);
     a.e = e;
     a.b = b;
@@ -718,7 +782,6 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     a.nspec = ns;
     a.ene = d_ene;
     a.status = d_status;
-    a.local_sort = t->local_sort;
     a.reduce_min = t->reduce_min;
     const size_t sm = t->smem_bytes;
 #define OSG_TCASE(D, O)                                                                       \
@@ -734,29 +797,32 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     return OSG_ERR_ARG;
 }
 
-int tiled_sort(TiledState *t, int in_buf, cudaStream_t st, int *launches)
+// particles per tile of species k in buffer `cur` (sorted part + arrivals, as the kernels read it)
+static int tile_counts(TiledState *t, int cur, int k, std::vector<int> &n, cudaStream_t st)
 {
-    const int ns = (int)t->rqm.size();
-    if (ns == 0) return OSG_OK;
-    TiledArgs a = base_args(t);
-    a.spec = t->d_tab[in_buf];
-    a.nspec = ns;
-    const int ncell = t->T[0] * t->T[1] * t->T[2];
-    dim3 grid((unsigned)t->ntiles, (unsigned)ns);
-    k_tile_sort<<<grid, 256, sizeof(int) * ncell, st>>>(a, t->dim);
-    *launches += 1;
+    std::vector<int> c(t->ntiles), r(t->ntiles);
+    OSG_CUDA(cudaMemcpyAsync(c.data(), t->buf[cur][k].cnt, sizeof(int) * t->ntiles,
+                             cudaMemcpyDeviceToHost, st));
+    OSG_CUDA(cudaMemcpyAsync(r.data(), t->buf[cur][k].arr, sizeof(int) * t->ntiles,
+                             cudaMemcpyDeviceToHost, st));
+    OSG_CUDA(cudaStreamSynchronize(st));
+    n.resize(t->ntiles);
+    const long cap = t->cap[k];
+    for (long i = 0; i < t->ntiles; i++) {
+        const long nst = std::min<long>(c[i], cap);
+        n[i] = (int)(nst + std::min<long>(r[i], cap - nst));
+    }
     return OSG_OK;
 }
 
 int tiled_count(TiledState *t, int cur, int k, long *np, cudaStream_t st)
 {
     OSG_CHECK(k >= 0 && k < (int)t->rqm.size(), OSG_ERR_ARG, "bad species");
-    std::vector<int> c(t->ntiles);
-    OSG_CUDA(cudaMemcpyAsync(c.data(), t->buf[cur][k].cnt, sizeof(int) * t->ntiles,
-                             cudaMemcpyDeviceToHost, st));
-    OSG_CUDA(cudaStreamSynchronize(st));
+    std::vector<int> c;
+    int rc = tile_counts(t, cur, k, c, st);
+    if (rc) return rc;
     long n = 0;
-    for (long i = 0; i < t->ntiles; i++) n += std::min<long>(c[i], t->cap[k]);
+    for (long i = 0; i < t->ntiles; i++) n += c[i];
     *np = n;
     return OSG_OK;
 }
@@ -764,14 +830,13 @@ int tiled_count(TiledState *t, int cur, int k, long *np, cudaStream_t st)
 // compact species k of buffer `cur` into the reference layout in device scratch; returns count
 static int compact(TiledState *t, int cur, int k, cudaStream_t st, long *np_out)
 {
-    std::vector<int> c(t->ntiles), off(t->ntiles);
-    OSG_CUDA(cudaMemcpyAsync(c.data(), t->buf[cur][k].cnt, sizeof(int) * t->ntiles,
-                             cudaMemcpyDeviceToHost, st));
-    OSG_CUDA(cudaStreamSynchronize(st));
+    std::vector<int> c, off(t->ntiles);
+    int rc = tile_counts(t, cur, k, c, st);
+    if (rc) return rc;
     long n = 0;
     for (long i = 0; i < t->ntiles; i++) {
         off[i] = (int)n;
-        n += std::min<long>(c[i], t->cap[k]);
+        n += c[i];
     }
     const int dim = t->dim;
     const size_t need = (size_t)(n > 0 ? n : 1) * (sizeof(int) * dim + sizeof(float) * (dim + 4));
@@ -819,11 +884,10 @@ int tiled_get_species(TiledState *t, int cur, int k, int *ix, float *x, float *u
 int tiled_occupancy(TiledState *t, int cur, double *max_frac, cudaStream_t st)
 {
     double m = 0.0;
-    std::vector<int> c(t->ntiles);
     for (size_t k = 0; k < t->rqm.size(); k++) {
-        OSG_CUDA(cudaMemcpyAsync(c.data(), t->buf[cur][k].cnt, sizeof(int) * t->ntiles,
-                                 cudaMemcpyDeviceToHost, st));
-        OSG_CUDA(cudaStreamSynchronize(st));
+        std::vector<int> c;
+        int rc = tile_counts(t, cur, (int)k, c, st);
+        if (rc) return rc;
         for (long i = 0; i < t->ntiles; i++) m = std::max(m, (double)c[i] / (double)t->cap[k]);
     }
     *max_frac = m;
@@ -856,8 +920,10 @@ int tiled_regrow(TiledState *t, int cur, cudaStream_t st)
     t->buf[1].clear();
     t->rqm.clear();
     t->cap.clear();
-    for (int p = 0; p < 2; p++)
+    for (int p = 0; p < 2; p++) {
         OSG_CUDA(cudaMemsetAsync(t->d_cnt[p], 0, sizeof(int) * MAX_TILED_SPECIES * t->ntiles, st));
+        OSG_CUDA(cudaMemsetAsync(t->d_arr[p], 0, sizeof(int) * MAX_TILED_SPECIES * t->ntiles, st));
+    }
     for (int k = 0; k < ns; k++) {
         const long n = (long)q[k].size();
         int rc = tiled_add_species(t, rqm[k], n, ix[k].data(), x[k].data(), u[k].data(),
@@ -868,9 +934,12 @@ int tiled_regrow(TiledState *t, int cur, cudaStream_t st)
         // the particles were binned into buffer 0; the caller's next step reads buffer `cur`
         for (int k = 0; k < ns; k++) std::swap(t->buf[0][k], t->buf[1][k]);
         std::swap(t->d_cnt[0], t->d_cnt[1]);
+        std::swap(t->d_arr[0], t->d_arr[1]);
         for (int k = 0; k < ns; k++) {
-            t->buf[0][k].cnt = t->d_cnt[0] + (size_t)k * t->ntiles;
-            t->buf[1][k].cnt = t->d_cnt[1] + (size_t)k * t->ntiles;
+            for (int p = 0; p < 2; p++) {
+                t->buf[p][k].cnt = t->d_cnt[p] + (size_t)k * t->ntiles;
+                t->buf[p][k].arr = t->d_arr[p] + (size_t)k * t->ntiles;
+            }
         }
         return upload_tables(t, st);
     }

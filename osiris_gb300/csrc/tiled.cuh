@@ -17,8 +17,6 @@ int tiled_add_species(TiledState *t, double rqm, long np, const int *ix, const f
 // is read (the other one is written)
 int tiled_push(TiledState *t, int parity, const float *e, const float *b, float *j,
                double *d_ene, int *d_status, cudaStream_t st, int *launches);
-// full per-tile counting sort by cell: reads buffer in_buf, writes buffer 1 - in_buf
-int tiled_sort(TiledState *t, int in_buf, cudaStream_t st, int *launches);
 // `cur` = index (0/1) of the buffer that holds the current particles
 int tiled_count(TiledState *t, int cur, int k, long *np, cudaStream_t st);
 int tiled_get_species(TiledState *t, int cur, int k, int *ix, float *x, float *u, float *q,

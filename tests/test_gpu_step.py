@@ -102,18 +102,18 @@ def test_fp32_engines_match_oracle(osg, oracle, engine, dim, order, nx, tile, st
              tile=tile if eng == osg.ENGINE_TILED else None)
 
 
-@pytest.mark.parametrize("local_sort", ["0", "1"])
-@pytest.mark.parametrize("n_sort", [1, 3, -1])
+@pytest.mark.parametrize("reduce_min,threads", [("0", "128"), ("2", "128"), ("33", "128"),
+                                                 ("2", "64"), ("2", "256")])
 @pytest.mark.parametrize("dim,order,nx,tile", [(2, 2, [32, 24], [8, 8]),
                                                (3, 2, [16, 8, 8], [4, 4, 4])])
-def test_tiled_sort_schedules_match_oracle(osg, oracle, monkeypatch, local_sort, n_sort, dim,
-                                           order, nx, tile):
-    """The periodic per-tile cell sort (every n_sort steps; -1 = never) and the per-iteration
-    ordering of the particles that stay in their tile only reorder particles: 10 steps still
-    match the oracle, and the sort step keeps the particle buffers consistent."""
-    monkeypatch.setenv("OSG_LOCAL_SORT", local_sort)
-    _compare(osg, oracle, 32, osg.ENGINE_TILED, dim, order, nx, [2] * dim, 10, 5e-5, tile=tile,
-             n_sort=n_sort)
+def test_tiled_deposit_modes_match_oracle(osg, oracle, monkeypatch, reduce_min, threads, dim,
+                                          order, nx, tile):
+    """The three deposit modes of the tiled push (warp-reduce every cell, direct adds for
+    cells of one lane, direct adds only) and the CTA sizes only reorder the current sums and
+    the particles: 10 steps still match the oracle."""
+    monkeypatch.setenv("OSG_REDUCE_MIN", reduce_min)
+    monkeypatch.setenv("OSG_PUSH_THREADS", threads)
+    _compare(osg, oracle, 32, osg.ENGINE_TILED, dim, order, nx, [2] * dim, 10, 5e-5, tile=tile)
 
 
 @pytest.mark.parametrize("prec,engine,tol", [(64, "plain", 1e-11), (32, "tiled", 2e-4)])
