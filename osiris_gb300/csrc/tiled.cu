@@ -94,7 +94,7 @@ struct TiledState {
     void *d_compact = nullptr;
     size_t compact_bytes = 0;
     size_t smem_bytes = 0;
-    int threads = 128;   // threads per push CTA (multiple of 32, <= 256)
+    int threads = 256;   // threads per push CTA (multiple of 32, <= 256)
     int reduce_min = 2;  // set per dimension in tiled_create
 };
 
@@ -163,8 +163,14 @@ __device__ __forceinline__ void emigrate(const SpeciesDev &sd, long cap, long de
 // In 2D every warp accumulates into its own copy of the current tile, so the warp-reduced
 // passes add with plain shared read-modify-writes; the copies are summed when the tile is
 // flushed.  In 3D the warps share one current tile (atomic adds).
+// CTAs of up to 256 threads.  2D linear/quadratic: three resident CTAs per SM (at most 85
+// registers per thread, measured fastest on GB300); 2D quartic: one (it needs ~250 registers
+// without spilling); otherwise two
 template <int DIM, int ORD>
-__global__ void __launch_bounds__(256) k_push_tiled(TiledArgs a)
+constexpr int push_min_blocks() { return DIM == 2 ? (ORD <= 2 ? 3 : (ORD == 3 ? 2 : 1)) : 2; }
+
+template <int DIM, int ORD>
+__global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>()) k_push_tiled(TiledArgs a)
 {
     constexpr int NP = ORD + 1, OFS = Stencil<ORD>::OFS;
     constexpr int MAXSEG = DIM == 2 ? 3 : 4;
