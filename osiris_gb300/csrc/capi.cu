@@ -12,6 +12,10 @@
 // calling thread gets its own stream and its own grow-only set of device buffers.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <thread>
+#include <vector>
+
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -36,13 +40,26 @@ void set_error(const char *fmt, ...)
 // per-thread device staging for the host-array entry points
 struct Staging {
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;          // second stream of the chunked host-array push
+    cudaEvent_t ev[2] = {nullptr, nullptr};
     void *buf[8] = {nullptr};
     size_t cap[8] = {0};
     ~Staging()
     {
         for (int i = 0; i < 8; i++)
             if (buf[i]) cudaFree(buf[i]);
+        for (int i = 0; i < 2; i++)
+            if (ev[i]) cudaEventDestroy(ev[i]);
+        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
+    }
+    int streams()
+    {
+        if (!stream) OSG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        if (!side) OSG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; i++)
+            if (!ev[i]) OSG_CUDA(cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming));
+        return OSG_OK;
     }
     int get(int slot, size_t bytes, void **out)
     {
@@ -94,27 +111,41 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
     if ((rc = g_stage.get(5, sizeof(T) * ge, &d_b))) return rc;
     if ((rc = g_stage.get(6, sizeof(T) * gj, &d_j))) return rc;
     if ((rc = g_stage.get(7, 64, &d_misc))) return rc;
-    cudaStream_t st = g_stage.stream;
+    if ((rc = g_stage.streams())) return rc;
+    cudaStream_t st = g_stage.stream, side = g_stage.side;
     const long o = (long)i0 - 1;
     double *d_ene = (double *)d_misc;
     int *d_status = (int *)((char *)d_misc + 16);
     OSG_CUDA(cudaMemsetAsync(d_misc, 0, 64, st));
-    OSG_CUDA(cudaMemcpyAsync(d_ix, ix + dim * o, sizeof(int) * dim * np, cudaMemcpyHostToDevice, st));
-    OSG_CUDA(cudaMemcpyAsync(d_x, x + dim * o, sizeof(T) * dim * np, cudaMemcpyHostToDevice, st));
-    OSG_CUDA(cudaMemcpyAsync(d_u, u + 3 * o, sizeof(T) * 3 * np, cudaMemcpyHostToDevice, st));
-    OSG_CUDA(cudaMemcpyAsync(d_q, q + o, sizeof(T) * np, cudaMemcpyHostToDevice, st));
     OSG_CUDA(cudaMemcpyAsync(d_e, e, sizeof(T) * ge, cudaMemcpyHostToDevice, st));
     OSG_CUDA(cudaMemcpyAsync(d_b, b, sizeof(T) * ge, cudaMemcpyHostToDevice, st));
     OSG_CUDA(cudaMemcpyAsync(d_j, j, sizeof(T) * gj, cudaMemcpyHostToDevice, st));
-    PlainPushArgs<T> a = make_plain_args<T>(dim, order, (int *)d_ix, (T *)d_x, (T *)d_u,
-                                            (const T *)d_q, np, rqm, (const T *)d_e,
-                                            (const T *)d_b, emf_size, emf_off, (T *)d_j, j_size,
-                                            j_off, dx, dt, d_ene, d_status);
-    if ((rc = launch_plain_push<T>(dim, order, a, st))) return rc;
-    OSG_CUDA(cudaGetLastError());
-    OSG_CUDA(cudaMemcpyAsync(ix + dim * o, d_ix, sizeof(int) * dim * np, cudaMemcpyDeviceToHost, st));
-    OSG_CUDA(cudaMemcpyAsync(x + dim * o, d_x, sizeof(T) * dim * np, cudaMemcpyDeviceToHost, st));
-    OSG_CUDA(cudaMemcpyAsync(u + 3 * o, d_u, sizeof(T) * 3 * np, cudaMemcpyDeviceToHost, st));
+    OSG_CUDA(cudaEventRecord(g_stage.ev[0], st));
+    OSG_CUDA(cudaStreamWaitEvent(side, g_stage.ev[0], 0));
+    // The particle range goes in chunks on two streams, so the copies of one chunk overlap the
+    // push of the other (per-particle results do not depend on the chunking; the current and
+    // energy sums are atomic either way).
+    const long chunk = np > (4L << 20) ? (np + 7) / 8 : np;
+    for (long c0 = 0, k = 0; c0 < np; c0 += chunk, k++) {
+        const long n = std::min(chunk, np - c0), h = o + c0;
+        cudaStream_t cs = (k & 1) ? side : st;
+        int *cix = (int *)d_ix + dim * c0;
+        T *cx = (T *)d_x + dim * c0, *cu = (T *)d_u + 3 * c0, *cq = (T *)d_q + c0;
+        OSG_CUDA(cudaMemcpyAsync(cix, ix + dim * h, sizeof(int) * dim * n, cudaMemcpyHostToDevice, cs));
+        OSG_CUDA(cudaMemcpyAsync(cx, x + dim * h, sizeof(T) * dim * n, cudaMemcpyHostToDevice, cs));
+        OSG_CUDA(cudaMemcpyAsync(cu, u + 3 * h, sizeof(T) * 3 * n, cudaMemcpyHostToDevice, cs));
+        OSG_CUDA(cudaMemcpyAsync(cq, q + h, sizeof(T) * n, cudaMemcpyHostToDevice, cs));
+        PlainPushArgs<T> a = make_plain_args<T>(dim, order, cix, cx, cu, (const T *)cq, n, rqm,
+                                                (const T *)d_e, (const T *)d_b, emf_size, emf_off,
+                                                (T *)d_j, j_size, j_off, dx, dt, d_ene, d_status);
+        if ((rc = launch_plain_push<T>(dim, order, a, cs))) return rc;
+        OSG_CUDA(cudaGetLastError());
+        OSG_CUDA(cudaMemcpyAsync(ix + dim * h, cix, sizeof(int) * dim * n, cudaMemcpyDeviceToHost, cs));
+        OSG_CUDA(cudaMemcpyAsync(x + dim * h, cx, sizeof(T) * dim * n, cudaMemcpyDeviceToHost, cs));
+        OSG_CUDA(cudaMemcpyAsync(u + 3 * h, cu, sizeof(T) * 3 * n, cudaMemcpyDeviceToHost, cs));
+    }
+    OSG_CUDA(cudaEventRecord(g_stage.ev[1], side));
+    OSG_CUDA(cudaStreamWaitEvent(st, g_stage.ev[1], 0));
     OSG_CUDA(cudaMemcpyAsync(j, d_j, sizeof(T) * gj, cudaMemcpyDeviceToHost, st));
     double h_ene = 0.0;
     int h_status = 0;
@@ -295,12 +326,41 @@ int osg_yee_advance_f64(int dim, const int *nx, const int *gcl, const int *gcu, 
 int osg_particle_wrap(int dim, const int *nx, long np, int *ix)
 {
     OSG_CHECK(dim >= 1 && dim <= 3 && nx && (np == 0 || ix), OSG_ERR_ARG, "bad arguments");
-    for (long p = 0; p < np; p++)
-        for (int d = 0; d < dim; d++) {
-            int &c = ix[dim * p + d];
-            if (c < 1) c += nx[d];
-            else if (c > nx[d]) c -= nx[d];
+    // branch-free per axis so the loop vectorises; large arrays are split over host threads
+    const int n0 = nx[0], n1 = dim > 1 ? nx[1] : 1, n2 = dim > 2 ? nx[2] : 1;
+    auto wrap_range = [=](long p0, long p1) {
+        int *c = ix + (long)dim * p0;
+        const long m = (long)dim * (p1 - p0);
+        if (dim == 1) {
+            for (long k = 0; k < m; k++) c[k] += (c[k] < 1 ? n0 : 0) - (c[k] > n0 ? n0 : 0);
+        } else if (dim == 2) {
+            for (long k = 0; k < m; k += 2) {
+                c[k] += (c[k] < 1 ? n0 : 0) - (c[k] > n0 ? n0 : 0);
+                c[k + 1] += (c[k + 1] < 1 ? n1 : 0) - (c[k + 1] > n1 ? n1 : 0);
+            }
+        } else {
+            for (long k = 0; k < m; k += 3) {
+                c[k] += (c[k] < 1 ? n0 : 0) - (c[k] > n0 ? n0 : 0);
+                c[k + 1] += (c[k + 1] < 1 ? n1 : 0) - (c[k + 1] > n1 ? n1 : 0);
+                c[k + 2] += (c[k + 2] < 1 ? n2 : 0) - (c[k + 2] > n2 ? n2 : 0);
+            }
         }
+    };
+    unsigned nt = std::thread::hardware_concurrency();
+    if (nt == 0) nt = 1;
+    if (nt > 32) nt = 32;
+    if (np < (1L << 20)) nt = 1;
+    if (nt == 1) {
+        wrap_range(0, np);
+        return OSG_OK;
+    }
+    std::vector<std::thread> pool;
+    const long chunk = (np + nt - 1) / nt;
+    for (unsigned t = 0; t < nt; t++) {
+        const long p0 = (long)t * chunk, p1 = std::min(np, p0 + chunk);
+        if (p0 < p1) pool.emplace_back(wrap_range, p0, p1);
+    }
+    for (auto &th : pool) th.join();
     return OSG_OK;
 }
 
