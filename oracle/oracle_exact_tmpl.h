@@ -1,0 +1,176 @@
+/*
+ * oracle_exact_tmpl.h -- TEST INFRASTRUCTURE ONLY (parity checker, never shipped).
+ *
+ * Scalar CPU restatement of the OSIRIS "exact" momentum update (push_type = "exact",
+ * dudt_exact, source/spec/os-spec-extpush.f03:40-348, after arXiv:2007.07556): the momentum
+ * is advanced by the analytic solution of the Lorentz force in the fields seen by the
+ * particle, held constant over the step, with the proper time of the step found by Newton
+ * iterations (at most p_iter_max = 10, relative tolerance iter_tol, default 1e-3,
+ * source/spec/os-spec-define.f03:471).  Helpers restated: get_t_light (:352-391), get_t
+ * (:395-430), trig_func (:720-760), hyper_func (:763-803), dot4 (:806-814), get_fu
+ * (:817-830).  The spin and radiation-reaction branches are not on this path.
+ *
+ * Included by pic_oracle.c once per precision with R / SFX / K / SQRT set.  The arithmetic
+ * follows the Fortran source's precision rules: p_k_part expressions in R, every
+ * `_p_double` literal and the internals of trig_func / hyper_func in double, a double value
+ * assigned to a p_k_part variable rounded to R; Fortran evaluates a + b + c as (a + b) + c.
+ */
+
+#ifndef PASTE3
+#define PASTE3_(a, b, c) a##b##c
+#define PASTE3(a, b, c) PASTE3_(a, b, c)
+#endif
+#define EXN(name) PASTE3(name, _, SFX)
+
+static inline R EXN(exabs)(R v) { return v < K(0.0) ? -v : v; }
+
+/* F u for the field tensor F = (E, B) (already scaled by q/m) and a four-vector
+ * u = (u1, u2, u3, u4 = gamma); get_fu (:817-830) */
+static inline void EXN(exfu)(const R *ep, const R *bp, const R *u, R *f)
+{
+    f[3] = (ep[0] * u[0] + ep[1] * u[1]) + ep[2] * u[2];
+    f[0] = (ep[0] * u[3] + bp[2] * u[1]) - bp[1] * u[2];
+    f[1] = (ep[1] * u[3] - bp[2] * u[0]) + bp[0] * u[2];
+    f[2] = (ep[2] * u[3] + bp[1] * u[0]) - bp[0] * u[1];
+}
+
+/* cos x, sin x / x, (cos x - 1) / x^2 (trig_func, :720-760) */
+static inline void EXN(extrig)(R x, R *cn, R *snc, R *cnc)
+{
+    const double xd = (double)x, x2 = xd * xd;
+    if (fabs(xd) < 0.007367081148666) {
+        const double x4 = x2 * x2;
+        *cn = (R)((1.0 - 0.5 * x2) + 0.041666666666667 * x4);
+        *snc = (R)((1.0 - 0.166666666666667 * x2) + 0.008333333333333 * x4);
+        *cnc = (R)((-0.5 + 0.041666666666667 * x2) - 0.001388888888889 * x4);
+    } else {
+        const double t1 = tan(0.5 * xd), t2 = t1 * t1, t3 = 1.0 / (1.0 + t2);
+        const double cnd = (1.0 - t2) * t3;
+        *cn = (R)cnd;
+        *snc = (R)(((2.0 * t1) * t3) / xd);
+        *cnc = (R)((cnd - 1.0) / x2);
+    }
+}
+
+/* cosh x, sinh x / x, (cosh x - 1) / x^2 (hyper_func, :763-803) */
+static inline void EXN(exhyp)(R x, R *ch, R *shc, R *chc)
+{
+    const double xd = (double)x, x2 = xd * xd;
+    if (fabs(xd) < 0.007367081148666) {
+        const double x4 = x2 * x2;
+        *ch = (R)((1.0 + 0.5 * x2) + 0.041666666666667 * x4);
+        *shc = (R)((1.0 + 0.166666666666667 * x2) + 0.008333333333333 * x4);
+        *chc = (R)((0.5 + 0.041666666666667 * x2) + 0.001388888888889 * x4);
+    } else {
+        const double t1 = tanh(0.5 * xd), t2 = t1 * t1, t3 = 1.0 / (1.0 - t2);
+        const double chd = (1.0 + t2) * t3;
+        *ch = (R)chd;
+        *shc = (R)(((2.0 * t1) * t3) / xd);
+        *chc = (R)((chd - 1.0) / x2);
+    }
+}
+
+/* Exact momentum update of one particle.  ep / bp: interpolated fields already multiplied by
+ * qm = 1 / rqm (in R); u: momentum (in/out); dt: the double time step; tol: iter_tol.
+ * Returns 1 when the particle was pushed, 0 in a weak field (e^2 + b^2 < 1e-12: the reference
+ * leaves such a particle's momentum unchanged). */
+static int EXN(ora_exact_u)(const R *ep, const R *bp, R *u, double dt, double tol)
+{
+    const double rel_tol = 1.0e-12, weak_fld_tol = 1.0e-12;
+    const R e2 = (ep[0] * ep[0] + ep[1] * ep[1]) + ep[2] * ep[2];
+    const R b2 = (bp[0] * bp[0] + bp[1] * bp[1]) + bp[2] * bp[2];
+    if ((double)(e2 + b2) < weak_fld_tol) return 0;
+    const R inv1 = e2 - b2;
+    const R inv2 = (ep[0] * bp[0] + ep[1] * bp[1]) + ep[2] * bp[2];
+    const R tmp = SQRT(inv1 * inv1 + (K(4.0) * inv2) * inv2);
+    const R k2 = K(0.5) * (inv1 + tmp), kk = SQRT(k2);
+    const R o2 = K(0.5) * (-inv1 + tmp), oo = SQRT(o2);
+    R u0[4], fu0[4], f2u0[4];
+    u0[0] = u[0];
+    u0[1] = u[1];
+    u0[2] = u[2];
+    u0[3] = SQRT(((K(1.0) + u0[0] * u0[0]) + u0[1] * u0[1]) + u0[2] * u0[2]);
+    EXN(exfu)(ep, bp, u0, fu0);
+    EXN(exfu)(ep, bp, fu0, f2u0);
+    if ((double)k2 < rel_tol && (double)o2 < rel_tol) {
+        /* light-like field: get_t_light (:352-391) */
+        R f3u0[4];
+        EXN(exfu)(ep, bp, f2u0, f3u0);
+        R t1 = (R)(dt / (double)u0[3]), t = t1, c1 = K(0.0), c2 = K(0.0);
+        int iter = 0;
+        for (;;) {
+            const R t2 = t1 * t1, t3 = t2 * t1;
+            c1 = (R)(0.5 * (double)t2);
+            c2 = (R)(0.166666666666667 * (double)t3);
+            const R fa = (t1 * u0[3] + c1 * fu0[3]) + c2 * f2u0[3];
+            const double fb = ((0.041666666666667 * (double)t3) * (double)t1) * (double)f3u0[3];
+            const R fun = (R)(((double)fa + fb) - dt);
+            const R dfun = ((u0[3] + t1 * fu0[3]) + c1 * f2u0[3]) + c2 * f3u0[3];
+            t = t1 - fun / dfun;
+            iter++;
+            if ((double)(EXN(exabs)(t - t1) / t1) < tol || iter > 10) break;
+            t1 = t;
+        }
+        for (int c = 0; c < 3; c++) u[c] = ((u0[c] + t * fu0[c]) + c1 * f2u0[c]) + c2 * f3u0[c];
+        return 1;
+    }
+    /* general field: subspace decomposition and get_t (:395-430) */
+    const R k2o2 = k2 + o2;
+    R uk0[4], uo0[4], fuk0[4], fuo0[4];
+    for (int c = 0; c < 4; c++) {
+        uk0[c] = (f2u0[c] + o2 * u0[c]) / k2o2;
+        uo0[c] = u0[c] - uk0[c];
+    }
+    EXN(exfu)(ep, bp, uk0, fuk0);
+    for (int c = 0; c < 4; c++) fuo0[c] = fu0[c] - fuk0[c];
+    R t0 = (R)(dt / (double)(uk0[3] + uo0[3])), t = t0;
+    R ch_k, shc_k, chc_k, cn_o, snc_o, cnc_o;
+    int iter = 0;
+    for (;;) {
+        EXN(extrig)(oo * t0, &cn_o, &snc_o, &cnc_o);
+        EXN(exhyp)(kk * t0, &ch_k, &shc_k, &chc_k);
+        const R fa = (uk0[3] * shc_k + (fuk0[3] * chc_k) * t0) * t0 +
+                     (uo0[3] * snc_o - (fuo0[3] * cnc_o) * t0) * t0;
+        const R fun = (R)((double)fa - dt);
+        const R dfun = ((uk0[3] * ch_k + (fuk0[3] * shc_k) * t0) + uo0[3] * cn_o) +
+                       (fuo0[3] * snc_o) * t0;
+        t = t0 - fun / dfun;
+        iter++;
+        if ((double)(EXN(exabs)(t - t0) / t0) < tol || iter > 10) break;
+        t0 = t;
+    }
+    for (int c = 0; c < 3; c++) {
+        const R uk = uk0[c] * ch_k + (fuk0[c] * shc_k) * t;
+        const R uo = uo0[c] * cn_o + (fuo0[c] * snc_o) * t;
+        u[c] = uk + uo;
+    }
+    return 1;
+}
+
+/* Momentum update of n particles with given (unscaled) fields ep(3,n), bp(3,n): qm = 1/rqm
+ * scaling as dudt_exact (:76-86), then ora_exact_u; *ene += sum q (gamma - 1) of the new
+ * momenta, accumulated in double (:335-344). */
+void EXN(ora_dudt_exact)(int n, const R *e, const R *b, R *u, const R *q, R rqm, double dt,
+                         double tol, double *ene)
+{
+    const R qm = K(1.0) / rqm;
+    double loc = 0.0;
+    for (int i = 0; i < n; i++) {
+        R ep[3], bp[3];
+        for (int c = 0; c < 3; c++) {
+            ep[c] = e[3 * i + c] * qm;
+            bp[c] = b[3 * i + c] * qm;
+        }
+        EXN(ora_exact_u)(ep, bp, u + 3 * i, dt, tol);
+        const R g = SQRT(((K(1.0) + u[3 * i] * u[3 * i]) + u[3 * i + 1] * u[3 * i + 1]) +
+                         u[3 * i + 2] * u[3 * i + 2]);
+        loc += (double)(q[i] * (g - K(1.0)));
+    }
+    *ene += loc;
+}
+
+/* Selected momentum update of the push restatement below (0 = Boris, 1 = exact) and the
+ * exact pusher's tolerance; set by ora_push_exact_* around one call. */
+static int EXN(ora_pusher) = 0;
+static double EXN(ora_iter_tol) = 1.0e-3;
+static double EXN(ora_push_dt) = 0.0;

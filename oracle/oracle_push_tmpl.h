@@ -184,6 +184,29 @@ static inline void OFN(boris)(R tem, R e1, R e2, R e3, R b1, R b2, R b3,
     *u3 = ut3 + e3;
 }
 
+/* Momentum update selected for this call: Boris (time-centred energy factor u^2/(gamma+1) in
+ * *en), or the exact pusher (oracle_exact_tmpl.h) with the fields scaled by q/m as dudt_exact
+ * does (source/spec/os-spec-extpush.f03:76-86): *en = 0 and q (gamma - 1) of the new momentum
+ * (:335-344) is added to the double accumulator *eacc. */
+static inline void OFN(dudt)(R tem, R rqm, R e1, R e2, R e3, R b1, R b2, R b3,
+                             R *u1, R *u2, R *u3, R *en, R qp, double *eacc)
+{
+    if (!EXN(ora_pusher)) {
+        OFN(boris)(tem, e1, e2, e3, b1, b2, b3, u1, u2, u3, en);
+        return;
+    }
+    const R qm = K(1.0) / rqm;
+    R ep[3], bp[3], uu[3];
+    ep[0] = e1 * qm; ep[1] = e2 * qm; ep[2] = e3 * qm;
+    bp[0] = b1 * qm; bp[1] = b2 * qm; bp[2] = b3 * qm;
+    uu[0] = *u1; uu[1] = *u2; uu[2] = *u3;
+    EXN(ora_exact_u)(ep, bp, uu, EXN(ora_push_dt), EXN(ora_iter_tol));
+    *u1 = uu[0]; *u2 = uu[1]; *u3 = uu[2];
+    const R g = SQRT(((K(1.0) + uu[0] * uu[0]) + uu[1] * uu[1]) + uu[2] * uu[2]);
+    *eacc += (double)(qp * (g - K(1.0)));
+    *en = K(0.0);
+}
+
 static inline R OFN(rgamma)(R u1, R u2, R u3)
 {
     return K(1.0) / SQRT(FMA(u3, u3, FMA(u2, u2, FMA(u1, u1, K(1.0)))));
@@ -250,6 +273,7 @@ void OFN(ora_vadvance_deposit_1d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R
     for (int c0 = 0; c0 < np; c0 += cache) {
         int cn = np - c0 < cache ? np - c0 : cache;
         R acc[VW];
+        double eacc = 0.0;
         for (int l = 0; l < VW; l++) acc[l] = K(0.0);
         int nvp = 0;
         for (int g = 0; g < cn; g += VW) {
@@ -277,7 +301,7 @@ void OFN(ora_vadvance_deposit_1d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R
                     B3 = FMA(b0[3 * (ih + k) + 2], wxh[k], B3);
                 }
                 R u1 = u[3 * p], u2 = u[3 * p + 1], u3 = u[3 * p + 2], en;
-                OFN(boris)(tem, E1, E2, E3, B1, B2, B3, &u1, &u2, &u3, &en);
+                OFN(dudt)(tem, *rqm, E1, E2, E3, B1, B2, B3, &u1, &u2, &u3, &en, q[p], &eacc);
                 u[3 * p] = u1; u[3 * p + 1] = u2; u[3 * p + 2] = u3;
                 R rg = OFN(rgamma)(u1, u2, u3);
                 acc[l] = FMA(q[p], en, acc[l]);
@@ -306,6 +330,7 @@ void OFN(ora_vadvance_deposit_1d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R
         }
         OFN(dep1d)(j, j_off, jn, buf, nvp);
         *ene += (double)OFN(lane_reduce)(acc);
+        *ene += eacc;
     }
     free(buf);
 }
@@ -438,6 +463,7 @@ void OFN(ora_vadvance_deposit_2d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R
     for (int c0 = 0; c0 < np; c0 += cache) {
         int cn = np - c0 < cache ? np - c0 : cache;
         R acc[VW];
+        double eacc = 0.0;
         for (int l = 0; l < VW; l++) acc[l] = K(0.0);
         int nvp = 0;
         for (int g = 0; g < cn; g += VW) {
@@ -481,7 +507,7 @@ void OFN(ora_vadvance_deposit_2d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R
                     B3 = FMA(f3, wyh[k2], B3);
                 }
                 R u1 = u[3 * p], u2 = u[3 * p + 1], u3 = u[3 * p + 2], en;
-                OFN(boris)(tem, E1, E2, E3, B1, B2, B3, &u1, &u2, &u3, &en);
+                OFN(dudt)(tem, *rqm, E1, E2, E3, B1, B2, B3, &u1, &u2, &u3, &en, q[p], &eacc);
                 u[3 * p] = u1; u[3 * p + 1] = u2; u[3 * p + 2] = u3;
                 R rg = OFN(rgamma)(u1, u2, u3);
                 acc[l] = FMA(q[p], en, acc[l]);
@@ -504,6 +530,7 @@ void OFN(ora_vadvance_deposit_2d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R
         }
         OFN(dep2d)(j, j_size, j_off, jn, buf, nvp);
         *ene += (double)OFN(lane_reduce)(acc);
+        *ene += eacc;
     }
     free(buf);
 }
@@ -723,6 +750,7 @@ void OFN(ora_vadvance_deposit_3d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R
     for (int c0 = 0; c0 < np; c0 += cache) {
         int cn = np - c0 < cache ? np - c0 : cache;
         R acc[VW];
+        double eacc = 0.0;
         for (int l = 0; l < VW; l++) acc[l] = K(0.0);
         int nvp = 0;
         for (int g = 0; g < cn; g += VW) {
@@ -780,7 +808,7 @@ void OFN(ora_vadvance_deposit_3d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R
                     B3 = FMA(g3, wz[k3], B3);
                 }
                 R u1 = u[3 * p], u2 = u[3 * p + 1], u3 = u[3 * p + 2], en;
-                OFN(boris)(tem, E1, E2, E3, B1, B2, B3, &u1, &u2, &u3, &en);
+                OFN(dudt)(tem, *rqm, E1, E2, E3, B1, B2, B3, &u1, &u2, &u3, &en, q[p], &eacc);
                 u[3 * p] = u1; u[3 * p + 1] = u2; u[3 * p + 2] = u3;
                 R rg = OFN(rgamma)(u1, u2, u3);
                 acc[l] = FMA(q[p], en, acc[l]);
@@ -805,6 +833,7 @@ void OFN(ora_vadvance_deposit_3d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R
         }
         OFN(dep3d)(j, j_size, j_off, jn, buf, nvp);
         *ene += (double)OFN(lane_reduce)(acc);
+        *ene += eacc;
     }
     free(buf);
 }

@@ -63,6 +63,8 @@ void ora_spline_weights_f64(int order, double x, double *w)
 #define FMA fmaf
 #define SQRT sqrtf
 
+#include "oracle_exact_tmpl.h"
+
 #define ORD 1
 #define OFS 1
 #include "oracle_push_tmpl.h"
@@ -99,6 +101,8 @@ void ora_spline_weights_f64(int order, double x, double *w)
 #define K(v) ((double)(v))
 #define FMA fma
 #define SQRT sqrt
+
+#include "oracle_exact_tmpl.h"
 
 #define ORD 1
 #define OFS 1
@@ -182,6 +186,35 @@ int ora_push_f64(int dim, int order, int *ix, double *x, double *u, double *q, i
     if (!f) return -1;
     f(ix, x, u, q, &i0, &i1, &rqm, e, b, emf_size, emf_off, j, j_size, j_off, dx, &dt, ene);
     return 0;
+}
+
+/* push with the exact momentum update (push_type = "exact"): momentum as dudt_exact with the
+ * double step dt and tolerance tol, position and deposit as the push above with dt */
+int ora_push_exact_f32(int dim, int order, int *ix, float *x, float *u, float *q, int i0, int i1,
+                       float rqm, float *e, float *b, int *emf_size, int *emf_off, float *j,
+                       int *j_size, int *j_off, double *dx, double dt, double tol, double *ene)
+{
+    ora_pusher_f32 = 1;
+    ora_push_dt_f32 = dt;
+    ora_iter_tol_f32 = tol;
+    int rc = ora_push_f32(dim, order, ix, x, u, q, i0, i1, rqm, e, b, emf_size, emf_off, j,
+                          j_size, j_off, dx, dt, ene);
+    ora_pusher_f32 = 0;
+    return rc;
+}
+
+int ora_push_exact_f64(int dim, int order, int *ix, double *x, double *u, double *q, int i0,
+                       int i1, double rqm, double *e, double *b, int *emf_size, int *emf_off,
+                       double *j, int *j_size, int *j_off, double *dx, double dt, double tol,
+                       double *ene)
+{
+    ora_pusher_f64 = 1;
+    ora_push_dt_f64 = dt;
+    ora_iter_tol_f64 = tol;
+    int rc = ora_push_f64(dim, order, ix, x, u, q, i0, i1, rqm, e, b, emf_size, emf_off, j,
+                          j_size, j_off, dx, dt, ene);
+    ora_pusher_f64 = 0;
+    return rc;
 }
 
 /* ---------------------------------------------------------------- particle phases ------- */
@@ -398,7 +431,7 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
  * current guard fold -> Yee.  ene[s] receives the time-centred kinetic energy sum of species s
  * (before the rqm*dV normalisation).
  */
-#define STEP_BODY(R, SFXN)                                                                    \
+#define STEP_BODY(R, SFXN, EXACT, TOL)                                                        \
     int gsz = 3;                                                                              \
     for (int d = 0; d < dim; d++) gsz *= nx[d] + gcl[d] + gcu[d];                             \
     int emf_size[3], emf_off[3];                                                              \
@@ -406,9 +439,13 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
         emf_size[d] = d < dim ? nx[d] + gcl[d] + gcu[d] : 1;                                  \
         emf_off[d] = d < dim ? gcl[d] : 0;                                                    \
     }                                                                                         \
-    /* the single-precision reference pushes with dt rounded to p_k_part                      \
-       (dtcycle = real(dt, p_k_part), source/spec/os-spec-vpush.f03:365) */                    \
-    const double dtp = sizeof(R) == 4 ? (double)(float)dt : dt;                               \
+    /* the single-precision SIMD push gets dt rounded to p_k_part (dtcycle = real(dt, p_k_part),\
+       source/spec/os-spec-vpush.f03:365); the Fortran push used with the exact pusher keeps  \
+       the double dt (dt_dx = real(gdt/dx, p_k_part), source/spec/os-spec-push.f03:1459-1460) */\
+    const double dtp = (sizeof(R) == 4 && !(EXACT)) ? (double)(float)dt : dt;                 \
+    ora_pusher_##SFXN = (EXACT);                                                              \
+    ora_push_dt_##SFXN = dt;                                                                  \
+    ora_iter_tol_##SFXN = (TOL);                                                              \
     ora_periodic_##SFXN(dim, nx, gcl, gcu, e, 0);                                             \
     ora_periodic_##SFXN(dim, nx, gcl, gcu, b, 0);                                             \
     memset(j, 0, sizeof(R) * (size_t)gsz);                                                    \
@@ -438,6 +475,7 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
             for (int t = 1; t < nt; t++) j[i] += jt[(size_t)gsz * (t - 1) + i];                \
         free(jt);                                                                             \
     }                                                                                         \
+    ora_pusher_##SFXN = 0;                                                                    \
     ora_periodic_##SFXN(dim, nx, gcl, gcu, j, 1);                                             \
     ora_yee_advance_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt);                               \
     return 0;
@@ -447,7 +485,7 @@ int ora_step_f32(int dim, int order, const int *nx, const int *gcl, const int *g
                  const int *np, int **ix, float **x, float **u, float **q, const float *rqm,
                  double *ene, int nthreads)
 {
-    STEP_BODY(float, f32)
+    STEP_BODY(float, f32, 0, 1e-3)
 }
 
 int ora_step_f64(int dim, int order, const int *nx, const int *gcl, const int *gcu,
@@ -455,7 +493,24 @@ int ora_step_f64(int dim, int order, const int *nx, const int *gcl, const int *g
                  const int *np, int **ix, double **x, double **u, double **q,
                  const double *rqm, double *ene, int nthreads)
 {
-    STEP_BODY(double, f64)
+    STEP_BODY(double, f64, 0, 1e-3)
+}
+
+/* the same step with the exact momentum update (push_type = "exact") at tolerance tol */
+int ora_step_exact_f32(int dim, int order, const int *nx, const int *gcl, const int *gcu,
+                       const double *dx, double dt, float *e, float *b, float *j, int nspec,
+                       const int *np, int **ix, float **x, float **u, float **q,
+                       const float *rqm, double *ene, int nthreads, double tol)
+{
+    STEP_BODY(float, f32, 1, tol)
+}
+
+int ora_step_exact_f64(int dim, int order, const int *nx, const int *gcl, const int *gcu,
+                       const double *dx, double dt, double *e, double *b, double *j, int nspec,
+                       const int *np, int **ix, double **x, double **u, double **q,
+                       const double *rqm, double *ene, int nthreads, double tol)
+{
+    STEP_BODY(double, f64, 1, tol)
 }
 
 int ora_max_threads(void)

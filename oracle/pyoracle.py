@@ -79,6 +79,11 @@ D = C.c_double
 def _declare(L):
     L.ora_push_f32.argtypes = [I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P, P, D, P]
     L.ora_push_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, P]
+    L.ora_push_exact_f32.argtypes = [I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P, P,
+                                     D, D, P]
+    L.ora_push_exact_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, D, P]
+    L.ora_dudt_exact_f32.argtypes = [I, P, P, P, P, C.c_float, D, D, P]
+    L.ora_dudt_exact_f64.argtypes = [I, P, P, P, P, D, D, D, P]
     for s in ("f32", "f64"):
         getattr(L, f"ora_yee_advance_{s}").argtypes = [I, P, P, P, P, P, P, P, D]
         getattr(L, f"ora_periodic_{s}").argtypes = [I, P, P, P, P, I]
@@ -88,6 +93,8 @@ def _declare(L):
         getattr(L, f"ora_load_{s}").argtypes = [P, I, P, P, P, D, P, P, D, D, P, P, P, P]
         getattr(L, f"ora_step_{s}").argtypes = [I, I, P, P, P, P, D, P, P, P, I, P, P, P, P, P,
                                                 P, P, I]
+        getattr(L, f"ora_step_exact_{s}").argtypes = [I, I, P, P, P, P, D, P, P, P, I, P, P, P,
+                                                      P, P, P, P, I, D]
     L.ora_wrap.argtypes = [I, P, I, P]
     L.ora_sort_index.argtypes = [I, P, I, P, P]
     L.ora_mt_seed.argtypes = [P, I]
@@ -150,12 +157,22 @@ class Grid:
 # ------------------------------------------------------------------------------ push
 
 def push(prec, dim, order, ix, x, u, q, i0, i1, rqm, e, b, j, emf_size, emf_off, dx, dt,
-         impl="oracle"):
-    """One vadvance_deposit call; arrays are updated in place; returns the energy sum."""
+         impl="oracle", pusher="boris", iter_tol=1e-3):
+    """One vadvance_deposit call; arrays are updated in place; returns the energy sum.
+    pusher="exact" replaces the Boris momentum update by dudt_exact (energy: q (gamma - 1))."""
     ene = np.zeros(1, dtype=np.float64)
     es, eo = _i32(emf_size), _i32(emf_off)
     dxa = _f64(list(dx) + [0.0] * (3 - len(dx)))
-    if impl == "oracle":
+    if pusher == "exact":
+        if impl != "oracle":
+            raise ValueError("the reference kernels have no exact pusher")
+        f = getattr(lib(), f"ora_push_exact_{prec}")
+        rc = f(dim, order, _p(ix), _p(x), _p(u), _p(q), int(i0), int(i1), rqm, _p(e), _p(b),
+               _p(es), _p(eo), _p(j), _p(es), _p(eo), _p(dxa), float(dt), float(iter_tol),
+               _p(ene))
+        if rc != 0:
+            raise ValueError("bad dim/order")
+    elif impl == "oracle":
         f = getattr(lib(), f"ora_push_{prec}")
         rc = f(dim, order, _p(ix), _p(x), _p(u), _p(q), int(i0), int(i1), rqm, _p(e), _p(b),
                _p(es), _p(eo), _p(j), _p(es), _p(eo), _p(dxa), float(dt), _p(ene))
@@ -171,6 +188,15 @@ def push(prec, dim, order, ix, x, u, q, i0, i1, rqm, e, b, j, emf_size, emf_off,
         a0, a1, rq, dtv = C.c_int(int(i0)), C.c_int(int(i1)), ctype(rqm), C.c_double(dt)
         f(_p(ix), _p(x), _p(u), _p(q), C.byref(a0), C.byref(a1), C.byref(rq), _p(e), _p(b),
           _p(es), _p(eo), _p(j), _p(es), _p(eo), _p(dxa), C.byref(dtv), _p(ene))
+    return float(ene[0])
+
+
+def dudt_exact(prec, e, b, u, q, rqm, dt, iter_tol=1e-3):
+    """Exact momentum update of n particles in given fields e (n,3), b (n,3); u updated in
+    place; returns sum q (gamma - 1) of the new momenta."""
+    ene = np.zeros(1, dtype=np.float64)
+    f = getattr(lib(), f"ora_dudt_exact_{prec}")
+    f(len(q), _p(e), _p(b), _p(u), _p(q), rqm, float(dt), float(iter_tol), _p(ene))
     return float(ene[0])
 
 
@@ -260,10 +286,12 @@ def load(rng: MT, prec, dim, nx, ppc, dx, rqm, uth, ufl, amp=0.0, kmode=1.0):
 
 # ------------------------------------------------------------------------------ full step
 
-def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False):
+def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="boris",
+         iter_tol=1e-3):
     """One full periodic time step; species = list of dicts with ix, x, u, q, rqm.
-    Returns the per-species time-centred energy sums.  fast=True runs the -O3 -ffast-math
-    build (timing only)."""
+    Returns the per-species energy sums (Boris: time-centred u^2/(gamma+1); exact pusher:
+    gamma - 1 of the new momentum; both times q).  fast=True runs the -O3 -ffast-math build
+    (timing only)."""
     nx, gl, gu = g.args()
     ns = len(species)
     np_ = _i32([len(s["q"]) for s in species])
@@ -274,10 +302,13 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False):
     qs = PA(*[_p(s["q"]) for s in species])
     rqm = np.asarray([s["rqm"] for s in species], dtype=dtype_of(prec))
     ene = np.zeros(ns)
-    getattr(fast_lib() if fast else lib(), f"ora_step_{prec}")(g.dim, g.order, _p(nx), _p(gl), _p(gu),
-                                        _p(_f64(g.dx + [0.0] * 3)), float(dt), _p(e), _p(b),
-                                        _p(j), ns, _p(np_), ixs, xs, us, qs, _p(rqm),
-                                        _p(ene), int(nthreads))
+    L = fast_lib() if fast else lib()
+    args = (g.dim, g.order, _p(nx), _p(gl), _p(gu), _p(_f64(g.dx + [0.0] * 3)), float(dt), _p(e),
+            _p(b), _p(j), ns, _p(np_), ixs, xs, us, qs, _p(rqm), _p(ene), int(nthreads))
+    if pusher == "exact":
+        getattr(L, f"ora_step_exact_{prec}")(*args, float(iter_tol))
+    else:
+        getattr(L, f"ora_step_{prec}")(*args)
     return ene
 
 
