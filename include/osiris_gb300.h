@@ -54,6 +54,9 @@ extern "C" {
 #define OSG_ENGINE_PLAIN 0
 #define OSG_ENGINE_TILED 1
 
+#define OSG_PUSHER_BORIS 0   /* push_type = "simd" / "standard" (Boris) */
+#define OSG_PUSHER_EXACT 1   /* push_type = "exact" (analytic, source/spec/os-spec-extpush.f03) */
+
 const char *osg_last_error(void);
 int osg_version(void);
 int osg_device_count(void);
@@ -80,6 +83,28 @@ int osg_vadvance_deposit_f64(int dim, int order, int *ix, double *x, double *u, 
                              const double *bfield, const int *emf_size, const int *emf_offset,
                              double *j, const int *j_size, const int *j_offset,
                              const double *dx, double dt, double *ene);
+
+/* The same particle advance with the exact momentum update of push_type = "exact"
+ * (dudt_exact, source/spec/os-spec-extpush.f03:40-348, reached through advance_deposit_{1d,2d,
+ * 3d}, source/spec/os-spec-push.f03:1363-1605, with this%dudt => dudt_exact,
+ * source/spec/os-species.f03:1432-1433): the Lorentz force in the interpolated fields is
+ * integrated analytically over the step, its proper time found by at most 10 Newton
+ * iterations to relative tolerance iter_tol (reference default 1e-3,
+ * source/spec/os-spec-define.f03:471).  dt is the double time step (momentum and dt/dx, as
+ * the Fortran path); position update, split and deposit as osg_vadvance_deposit_*.  *ene +=
+ * sum of q (gamma - 1) of the new momenta (the energy dudt_exact reports). */
+int osg_advance_deposit_exact_f32(int dim, int order, int *ix, float *x, float *u, float *q,
+                                  int i0, int i1, float rqm, const float *efield,
+                                  const float *bfield, const int *emf_size,
+                                  const int *emf_offset, float *j, const int *j_size,
+                                  const int *j_offset, const double *dx, double dt,
+                                  double iter_tol, double *ene);
+int osg_advance_deposit_exact_f64(int dim, int order, int *ix, double *x, double *u, double *q,
+                                  int i0, int i1, double rqm, const double *efield,
+                                  const double *bfield, const int *emf_size,
+                                  const int *emf_offset, double *j, const int *j_size,
+                                  const int *j_offset, const double *dx, double dt,
+                                  double iter_tol, double *ene);
 
 /* The same push for callers that cannot allocate device memory: hosts that give the whole GPU
  * to their own pool allocator at start-up and treat a foreign cudaMalloc as an error, and
@@ -164,6 +189,8 @@ typedef struct {
     int tile[3];      /* tile shape in cells (TILED; 0 = automatic) */
     int n_sort;       /* PLAIN: cell sort every n_sort steps (0 = never); TILED sorts every step */
     double capacity;  /* TILED: slots per tile as a multiple of the mean load (0 = 3.0) */
+    int pusher;       /* OSG_PUSHER_BORIS (0) or OSG_PUSHER_EXACT (1) */
+    double iter_tol;  /* exact pusher: Newton tolerance (0 = the reference default 1e-3) */
 } osg_config;
 
 int osg_sim_create(const osg_config *cfg, osg_sim **out);
@@ -189,7 +216,8 @@ int osg_sim_tile_occupancy(osg_sim *s, double *max_frac);
 int osg_sim_step_async(osg_sim *s, int nsteps);
 int osg_sim_sync(osg_sim *s);
 void *osg_sim_stream(osg_sim *s);
-/* FP64 diagnostics: kinetic[ns] time-centred energy of the last step (rqm * dV applied),
+/* FP64 diagnostics: kinetic[ns] kinetic energy of the last step (rqm * dV applied; Boris:
+ * time-centred, exact pusher: of the new momenta, as each reference pusher reports it),
  * field[6] = 0.5 dV sum of E1..3^2 and B1..3^2. */
 int osg_sim_energy(osg_sim *s, double *kinetic, double *field);
 /* FP64 charge check: max over cells of |div E - rho| (rho of all species, order-matched

@@ -30,6 +30,8 @@ LIB_PATH = os.path.join(HERE, "libosiris_gb300.so")
 OSG_OK = 0
 ENGINE_PLAIN = 0
 ENGINE_TILED = 1
+PUSHER_BORIS = 0
+PUSHER_EXACT = 1
 RNG_BYTES = 2512
 
 # guard cells per interpolation order (source/particles/os-particles.f03:321-360)
@@ -61,7 +63,8 @@ P, I, L, D, F = C.c_void_p, C.c_int, C.c_long, C.c_double, C.c_float
 
 class Config(C.Structure):
     _fields_ = [("dim", I), ("order", I), ("precision", I), ("engine", I), ("nx", I * 3),
-                ("dx", D * 3), ("dt", D), ("tile", I * 3), ("n_sort", I), ("capacity", D)]
+                ("dx", D * 3), ("dt", D), ("tile", I * 3), ("n_sort", I), ("capacity", D),
+                ("pusher", I), ("iter_tol", D)]
 
 
 def _declare(lb):
@@ -73,6 +76,10 @@ def _declare(lb):
     lb.osg_host_free.argtypes = [P]
     lb.osg_vadvance_deposit_f32.argtypes = [I, I, P, P, P, P, I, I, F, P, P, P, P, P, P, P, P, D, P]
     lb.osg_vadvance_deposit_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, P]
+    lb.osg_advance_deposit_exact_f32.argtypes = [I, I, P, P, P, P, I, I, F, P, P, P, P, P, P, P,
+                                                 P, D, D, P]
+    lb.osg_advance_deposit_exact_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P,
+                                                 P, D, D, P]
     lb.osg_vadvance_deposit_noalloc_f32.argtypes = [I, I, P, P, P, P, I, I, F, P, P, P, P, P, P,
                                                     P, P, D, P]
     for s in ("f32", "f64"):
@@ -138,11 +145,14 @@ def _need(a, dtype, name):
 # ------------------------------------------------------------------------ drop-in calls
 
 def vadvance_deposit(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_size,
-                     emf_offset, j, j_size, j_offset, dx, dt):
+                     emf_offset, j, j_size, j_offset, dx, dt, pusher=PUSHER_BORIS,
+                     iter_tol=1e-3):
     """Push particles i0..i1 (1-based, inclusive) and add their current into ``j``.
 
     Same arguments and in-place semantics as FNAME(vadvance_deposit_<dim>d_s<order>);
-    returns the time-centred energy sum the reference adds into ``*ene``."""
+    returns the time-centred energy sum the reference adds into ``*ene``.  With
+    ``pusher=PUSHER_EXACT`` the momentum update is the exact pusher (push_type = "exact",
+    osg_advance_deposit_exact_*) and the energy is sum q (gamma - 1) of the new momenta."""
     prec = _prec(x)
     dt_ = np.float32 if prec == "f32" else np.float64
     _need(ix, np.int32, "ix")
@@ -152,11 +162,14 @@ def vadvance_deposit(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_s
         if a.dtype != dt_ or not a.flags.c_contiguous:
             raise TypeError(f"{n} must be C-contiguous {np.dtype(dt_)}")
     ene = np.zeros(1)
-    f = getattr(lib(), f"osg_vadvance_deposit_{prec}")
-    _check(f(dim, order, _p(ix), _p(x), _p(u), _p(q), int(i0), int(i1), rqm, _p(efield),
-             _p(bfield), _p(_i32(emf_size)), _p(_i32(emf_offset)), _p(j), _p(_i32(j_size)),
-             _p(_i32(j_offset)), _p(_f64(list(dx) + [0.0] * (3 - len(dx)))), float(dt),
-             _p(ene)))
+    args = (dim, order, _p(ix), _p(x), _p(u), _p(q), int(i0), int(i1), rqm, _p(efield),
+            _p(bfield), _p(_i32(emf_size)), _p(_i32(emf_offset)), _p(j), _p(_i32(j_size)),
+            _p(_i32(j_offset)), _p(_f64(list(dx) + [0.0] * (3 - len(dx)))), float(dt))
+    if pusher == PUSHER_EXACT:
+        _check(getattr(lib(), f"osg_advance_deposit_exact_{prec}")(*args, float(iter_tol),
+                                                                    _p(ene)))
+    else:
+        _check(getattr(lib(), f"osg_vadvance_deposit_{prec}")(*args, _p(ene)))
     return float(ene[0])
 
 
@@ -259,7 +272,7 @@ class Simulation:
     """Device-resident periodic PIC simulation (fields + species stay on the GPU)."""
 
     def __init__(self, nx, dx, dt, order=2, precision=32, engine=ENGINE_TILED, tile=None,
-                 n_sort=0, capacity=0.0):
+                 n_sort=0, capacity=0.0, pusher=PUSHER_BORIS, iter_tol=0.0):
         self.dim = len(nx)
         self.nx = list(nx)
         self.order = order
@@ -277,6 +290,8 @@ class Simulation:
         cfg.dt = dt
         cfg.n_sort = n_sort
         cfg.capacity = capacity
+        cfg.pusher = pusher
+        cfg.iter_tol = iter_tol
         self.cfg = cfg
         self.dx = list(dx)
         self.dt = dt

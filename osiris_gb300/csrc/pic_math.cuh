@@ -383,4 +383,133 @@ __device__ __forceinline__ int split3(Seg3<T> *s, int dix, int diy, int diz)
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// Exact momentum update (push_type = "exact"; dudt_exact, source/spec/os-spec-extpush.f03:
+// 40-348, after arXiv:2007.07556): the Lorentz force in the fields seen by the particle, held
+// constant over the step, is integrated analytically; the proper time of the step comes from
+// Newton iterations (get_t_light :352-391, get_t :395-430; at most 10, relative tolerance
+// tol).  Precision as the Fortran source: T (p_k_part) arithmetic, every double literal and
+// the insides of trig_func / hyper_func (:720-803) in double, rounded to T on assignment.
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void ex_fu(const T *ep, const T *bp, const T *u, T *f)
+{
+    f[3] = (ep[0] * u[0] + ep[1] * u[1]) + ep[2] * u[2];
+    f[0] = (ep[0] * u[3] + bp[2] * u[1]) - bp[1] * u[2];
+    f[1] = (ep[1] * u[3] - bp[2] * u[0]) + bp[0] * u[2];
+    f[2] = (ep[2] * u[3] + bp[1] * u[0]) - bp[0] * u[1];
+}
+
+// cos x, sin x / x, (cos x - 1) / x^2  (hyp = true: cosh x, sinh x / x, (cosh x - 1) / x^2)
+template <typename T, bool HYP>
+__device__ __forceinline__ void ex_circ(T x, T &c, T &sc, T &cc)
+{
+    const double xd = (double)x, x2 = xd * xd;
+    const double s = HYP ? 1.0 : -1.0;
+    if (fabs(xd) < 0.007367081148666) {
+        const double x4 = x2 * x2;
+        c = (T)((1.0 + s * 0.5 * x2) + 0.041666666666667 * x4);
+        sc = (T)((1.0 + s * 0.166666666666667 * x2) + 0.008333333333333 * x4);
+        cc = (T)((s * 0.5 + 0.041666666666667 * x2) + s * 0.001388888888889 * x4);
+    } else {
+        const double t1 = HYP ? tanh(0.5 * xd) : tan(0.5 * xd), t2 = t1 * t1;
+        const double t3 = 1.0 / (1.0 - s * t2);
+        const double cd = (1.0 + s * t2) * t3;
+        c = (T)cd;
+        sc = (T)(((2.0 * t1) * t3) / xd);
+        cc = (T)((cd - 1.0) / x2);
+    }
+}
+
+// ep, bp: interpolated fields times q/m; u: momentum (in/out); dt: the double time step.
+// Returns false (momentum unchanged) in a weak field, e^2 + b^2 < 1e-12.
+template <typename T>
+__device__ __noinline__ bool exact_u(const T *ep, const T *bp, T *u, double dt, double tol)
+{
+    const T e2 = (ep[0] * ep[0] + ep[1] * ep[1]) + ep[2] * ep[2];
+    const T b2 = (bp[0] * bp[0] + bp[1] * bp[1]) + bp[2] * bp[2];
+    if ((double)(e2 + b2) < 1.0e-12) return false;
+    const T inv1 = e2 - b2;
+    const T inv2 = (ep[0] * bp[0] + ep[1] * bp[1]) + ep[2] * bp[2];
+    const T tmp = sqrtR(inv1 * inv1 + (T(4.0) * inv2) * inv2);
+    const T k2 = T(0.5) * (inv1 + tmp), kk = sqrtR(k2);
+    const T o2 = T(0.5) * (-inv1 + tmp), oo = sqrtR(o2);
+    T u0[4], fu0[4], f2u0[4];
+    u0[0] = u[0];
+    u0[1] = u[1];
+    u0[2] = u[2];
+    u0[3] = sqrtR(((T(1.0) + u0[0] * u0[0]) + u0[1] * u0[1]) + u0[2] * u0[2]);
+    ex_fu(ep, bp, u0, fu0);
+    ex_fu(ep, bp, fu0, f2u0);
+    if ((double)k2 < 1.0e-12 && (double)o2 < 1.0e-12) {
+        T f3u0[4];
+        ex_fu(ep, bp, f2u0, f3u0);
+        T t1 = (T)(dt / (double)u0[3]), t = t1, c1 = T(0), c2 = T(0);
+        for (int iter = 1;; iter++) {
+            const T t2 = t1 * t1, t3 = t2 * t1;
+            c1 = (T)(0.5 * (double)t2);
+            c2 = (T)(0.166666666666667 * (double)t3);
+            const T fa = (t1 * u0[3] + c1 * fu0[3]) + c2 * f2u0[3];
+            const double fb = ((0.041666666666667 * (double)t3) * (double)t1) * (double)f3u0[3];
+            const T fun = (T)(((double)fa + fb) - dt);
+            const T dfun = ((u0[3] + t1 * fu0[3]) + c1 * f2u0[3]) + c2 * f3u0[3];
+            t = t1 - fun / dfun;
+            const T rel = (t - t1) < T(0) ? (t1 - t) / t1 : (t - t1) / t1;
+            if ((double)rel < tol || iter > 10) break;
+            t1 = t;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) u[c] = ((u0[c] + t * fu0[c]) + c1 * f2u0[c]) + c2 * f3u0[c];
+        return true;
+    }
+    const T k2o2 = k2 + o2;
+    T uk0[4], uo0[4], fuk0[4], fuo0[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        uk0[c] = (f2u0[c] + o2 * u0[c]) / k2o2;
+        uo0[c] = u0[c] - uk0[c];
+    }
+    ex_fu(ep, bp, uk0, fuk0);
+#pragma unroll
+    for (int c = 0; c < 4; c++) fuo0[c] = fu0[c] - fuk0[c];
+    T t0 = (T)(dt / (double)(uk0[3] + uo0[3])), t = t0;
+    T ch_k, shc_k, chc_k, cn_o, snc_o, cnc_o;
+    for (int iter = 1;; iter++) {
+        ex_circ<T, false>(oo * t0, cn_o, snc_o, cnc_o);
+        ex_circ<T, true>(kk * t0, ch_k, shc_k, chc_k);
+        const T fa = (uk0[3] * shc_k + (fuk0[3] * chc_k) * t0) * t0 +
+                     (uo0[3] * snc_o - (fuo0[3] * cnc_o) * t0) * t0;
+        const T fun = (T)((double)fa - dt);
+        const T dfun = ((uk0[3] * ch_k + (fuk0[3] * shc_k) * t0) + uo0[3] * cn_o) +
+                       (fuo0[3] * snc_o) * t0;
+        t = t0 - fun / dfun;
+        const T rel = (t - t0) < T(0) ? (t0 - t) / t0 : (t - t0) / t0;
+        if ((double)rel < tol || iter > 10) break;
+        t0 = t;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const T uk = uk0[c] * ch_k + (fuk0[c] * shc_k) * t;
+        const T uo = uo0[c] * cn_o + (fuo0[c] * snc_o) * t;
+        u[c] = uk + uo;
+    }
+    return true;
+}
+
+// Exact momentum update from the unscaled interpolated fields (scaled by qm = 1/rqm as
+// dudt_exact does, :76-86); returns q (gamma - 1) of the new momentum (its energy, :335-344).
+template <typename T>
+__device__ __forceinline__ T exact_push(T qm, double dt, double tol, T e1, T e2, T e3, T b1,
+                                        T b2, T b3, T q, T &u1, T &u2, T &u3)
+{
+    const T ep[3] = {e1 * qm, e2 * qm, e3 * qm}, bp[3] = {b1 * qm, b2 * qm, b3 * qm};
+    T u[3] = {u1, u2, u3};
+    exact_u<T>(ep, bp, u, dt, tol);
+    u1 = u[0];
+    u2 = u[1];
+    u3 = u[2];
+    const T g = sqrtR(((T(1.0) + u1 * u1) + u2 * u2) + u3 * u3);
+    return q * (g - T(1.0));
+}
+
 } // namespace osg

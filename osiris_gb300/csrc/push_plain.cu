@@ -271,12 +271,17 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
                 }
             }
             T u1 = a.u[3 * p], u2 = a.u[3 * p + 1], u3 = a.u[3 * p + 2];
-            const T ene = boris(a.tem, E1, E2, E3, B1, B2, B3, u1, u2, u3);
+            if (a.pusher == OSG_PUSHER_EXACT) {
+                my_ene = (double)exact_push<T>(a.qm, a.dt_full, a.iter_tol, E1, E2, E3, B1, B2,
+                                               B3, q, u1, u2, u3);
+            } else {
+                const T ene = boris(a.tem, E1, E2, E3, B1, B2, B3, u1, u2, u3);
+                my_ene = (double)q * (double)ene;
+            }
             a.u[3 * p] = u1;
             a.u[3 * p + 1] = u2;
             a.u[3 * p + 2] = u3;
             const T rg = rgamma(u1, u2, u3);
-            my_ene = (double)q * (double)ene;
             const T v1 = u1 * rg, v2 = u2 * rg, v3 = u3 * rg;
             if constexpr (DIM == 1) {
                 T x1 = fmaR(v1, a.dtdx[0], x0[0]);
@@ -359,6 +364,10 @@ PlainPushArgs<T> make_plain_args(int dim, int order, int *ix, T *x, T *u, const 
         a.jn[d] = d < dim ? (T)(dx[d] / dt / div) : T(0);
     }
     a.wrap[0] = a.wrap[1] = a.wrap[2] = 0;
+    a.pusher = OSG_PUSHER_BORIS;
+    a.qm = T(1) / rqm;
+    a.dt_full = dt;
+    a.iter_tol = 1.0e-3;
     a.ene = d_ene;
     a.status = d_status;
     return a;

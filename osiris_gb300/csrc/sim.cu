@@ -233,7 +233,10 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, PhaseEvents *pe)
     int launches = 0;
     // the single-precision reference pushes with dt rounded to p_k_part
     // (dtcycle = real(dt, p_k_part), source/spec/os-spec-vpush.f03:365)
-    const double push_dt = sizeof(T) == 4 ? (double)(float)c.dt : c.dt;
+    // (the Fortran push the exact pusher runs in keeps the double dt,
+    //  source/spec/os-spec-push.f03:1459-1460)
+    const bool exact = c.pusher == OSG_PUSHER_EXACT;
+    const double push_dt = (sizeof(T) == 4 && !exact) ? (double)(float)c.dt : c.dt;
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[0], st));
     periodic_update<T>(s->g, (T *)s->e, 0, st);
     periodic_update<T>(s->g, (T *)s->b, 0, st);
@@ -254,6 +257,8 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, PhaseEvents *pe)
                 (T)s->rqm[k], (const T *)s->e, (const T *)s->b, emf_size, emf_off, (T *)s->j,
                 emf_size, emf_off, c.dx, push_dt, s->d_ene + k, s->d_status);
             for (int d = 0; d < c.dim; d++) a.wrap[d] = c.nx[d];
+            a.pusher = c.pusher;
+            a.iter_tol = c.iter_tol;
             int rc = launch_plain_push<T>(c.dim, c.order, a, st);
             if (rc) return rc;
             launches++;
@@ -374,6 +379,9 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               "unknown engine");
     OSG_CHECK(!(cfg->engine == OSG_ENGINE_TILED && cfg->precision != 32), OSG_ERR_ARG,
               "the tiled engine is single precision");
+    OSG_CHECK(cfg->pusher == OSG_PUSHER_BORIS || cfg->pusher == OSG_PUSHER_EXACT, OSG_ERR_ARG,
+              "unknown pusher");
+    OSG_CHECK(cfg->iter_tol >= 0, OSG_ERR_ARG, "iter_tol must be >= 0");
     double cour = 0.0;
     for (int d = 0; d < cfg->dim; d++) {
         OSG_CHECK(cfg->nx[d] >= 2 * cfg->order + 1 && cfg->dx[d] > 0, OSG_ERR_ARG,
@@ -385,6 +393,7 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               "dt violates the Yee Courant limit %g", std::sqrt(1.0 / cour));
     osg_sim *s = new osg_sim();
     s->cfg = *cfg;
+    if (s->cfg.iter_tol <= 0) s->cfg.iter_tol = 1.0e-3;
     for (int d = cfg->dim; d < 3; d++) {
         s->cfg.nx[d] = 1;
         s->cfg.dx[d] = 1.0;

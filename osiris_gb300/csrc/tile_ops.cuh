@@ -2,6 +2,8 @@
 // per-segment current values, and the warp-cooperative shared-memory current accumulation.
 #pragma once
 
+#include <climits>
+
 #include "pic_math.cuh"
 
 namespace osg {
@@ -485,6 +487,114 @@ __device__ __forceinline__ void deposit_segment(float *sJ, const SegRec *rec, co
         for (int k = 0; k < NV; k++) v[k] = 0.f;
     }
     warp_deposit<DIM, ORD>(sJ, base, v, jsy, jsz, reduce_min, ls);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// 2D segments that cross a cell face.  Few per warp iteration and scattered over the lanes,
+// they wait in a per-warp queue and are deposited 32 at a time: sorted by cell, summed per
+// cell with a segmented warp reduction, one add per cell and value.
+// ------------------------------------------------------------------------------------------
+template <int ORD>
+__device__ __forceinline__ Seg2<float> seg2_of(const SegRec &r)
+{
+    Seg2<float> g;
+    g.x0 = r.a[0]; g.x1 = r.a[1]; g.y0 = r.a[2]; g.y1 = r.a[3];
+    g.vz = r.a[4]; g.i = 0; g.j = 0;
+    return g;
+}
+
+// Segmented warp sum of one 2D segment's values per lane: lanes with equal `base` form
+// contiguous groups (the lanes are sorted by cell); the first lane of each group adds the
+// group's sums to the shared tile at `base` (-1: lanes without a segment).  Must be called by
+// all 32 lanes.
+template <int ORD>
+__device__ __forceinline__ void flush_runs2(float *sJ, float *acc, int base, int jsy)
+{
+    constexpr int NV = SegVals<2, ORD>::NV;
+    const int lane = (int)(threadIdx.x & 31);
+    const int prev = __shfl_up_sync(FULL_MASK, base, 1);
+    const bool head = lane == 0 || prev != base;
+    const unsigned heads = __ballot_sync(FULL_MASK, head);
+    const unsigned above = lane == 31 ? 0u : (heads & (0xffffffffu << (lane + 1)));
+    const int seg_end = above ? __ffs(above) - 1 : 32;
+    // after the step with distance o, a lane holds the sum over [lane, lane + 2o) of its group
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const bool take = lane + o < seg_end;
+        if (!__any_sync(FULL_MASK, take)) break;
+#pragma unroll
+        for (int i = 0; i < NV; i++) {
+            const float t = __shfl_down_sync(FULL_MASK, acc[i], o);
+            if (take) acc[i] += t;
+        }
+    }
+    if (head && base >= 0) {
+        float *pj = sJ + base;
+#pragma unroll
+        for (int i = 0; i < NV; i++) atomicAdd(pj + seg_offset<2, ORD>(i, jsy, 0), acc[i]);
+    }
+}
+
+// Per-warp queue (shared memory) of 2D segments waiting to be deposited by a full warp: the
+// segments that do not go to a lane's register sum (face crossings, particles of a run that
+// passed into the next cell, arrivals) are few per iteration and scattered over the lanes;
+// queued, they are deposited 32 at a time with every lane busy.  Crossings of one cell mostly
+// land in the same neighbour cell, so a batch is first sorted by cell (warp bitonic sort) and
+// summed per cell with the segmented reduction; one lane per cell adds to the shared tile.
+constexpr int SEGQ = 64;
+
+// append r for every lane with put; qn (warp-uniform) is the queue length
+__device__ __forceinline__ void segq_push(SegRec *sq, int &qn, bool put, const SegRec &r)
+{
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(FULL_MASK, put);
+    if (put) sq[qn + __popc(m & ((1u << lane) - 1u))] = r;
+    qn += __popc(m);
+}
+
+// ascending sort of one int per lane across the warp (bitonic network, 15 exchange steps)
+__device__ __forceinline__ int warp_sort32(int v)
+{
+    const int lane = (int)(threadIdx.x & 31);
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const int o = __shfl_xor_sync(FULL_MASK, v, j);
+            const bool keep_min = ((lane & k) == 0) == ((lane & j) == 0);
+            v = keep_min ? min(v, o) : max(v, o);
+        }
+    }
+    return v;
+}
+
+// deposit the top 32 entries while at least nmin (>= 1) are queued
+template <int ORD>
+__device__ __forceinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int nmin,
+                                           const float *jn, int jsy)
+{
+    constexpr int NV = SegVals<2, ORD>::NV;
+    const int lane = (int)(threadIdx.x & 31);
+    while (qn >= nmin) {
+        const int take = qn < 32 ? qn : 32, first = qn - take;
+        __syncwarp();
+        // key = stencil origin * 32 + entry (unique); idle lanes sort last
+        const int key = warp_sort32(lane < take ? sq[first + lane].base * 32 + lane : INT_MAX);
+        const bool act = key != INT_MAX;
+        float v[NV];
+        int base = -1;
+        if (act) {
+            const SegRec r = sq[first + (key & 31)];
+            seg_values2<ORD>(seg2_of<ORD>(r), r.q, jn[0], jn[1], v);
+            base = r.base;
+        } else {
+#pragma unroll
+            for (int i = 0; i < NV; i++) v[i] = 0.f;
+        }
+        __syncwarp();
+        qn = first;
+        flush_runs2<ORD>(sJ, v, base, jsy);
     }
 }
 

@@ -228,6 +228,10 @@ __global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>()) k_push_tiled
     __shared__ int sLeaveI[LEAVE_QUEUE][4];      // new cell per axis, destination tile
     __shared__ float sLeaveF[LEAVE_QUEUE][8];    // offsets per axis, momenta, charge
     __shared__ int sNleave;
+    // 2D: per-warp queues of segments for full-warp deposits (dynamic shared memory after the
+    // current tile, 16-byte aligned)
+    SegRec *sQ = reinterpret_cast<SegRec *>(smem + ((6 * ne + njall + 3) & ~3)) + warp * SEGQ;
+    int qn = 0;
     const int ncell = a.T[0] * a.T[1] * a.T[2];
 
     for (int s = 0; s < a.nspec; s++) {
@@ -247,16 +251,13 @@ __global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>()) k_push_tiled
         //      to their own slot of the input slab (this CTA owns it) and counted per new cell;
         //      particles that leave take an arrival slot (from the top) of their destination
         //      tile in the output buffer, and their input slot is marked empty (ix = 0).
+        auto slot = [&](int i) { return slab + (i < nst ? i : cap - 1 - (i - nst)); };
         // the particle of the next iteration is loaded while this one is pushed
-        const int nit = (n + nthr - 1) / nthr;
-        auto index = [&](int it) {
-            return spread ? (int)threadIdx.x * nit + it : it * nthr + (int)threadIdx.x;
-        };
         int pf_c[3] = {1, 1, 1};
         float pf_x[3] = {0, 0, 0}, pf_u[3] = {0, 0, 0}, pf_q = 0.0f;
-        auto prefetch = [&](int i) {
-            if (i < n) {
-                const long p = slab + (i < nst ? i : cap - 1 - (i - nst));
+        auto prefetch = [&](int i, int lim) {
+            if (i < lim) {
+                const long p = slot(i);
 #pragma unroll
                 for (int d = 0; d < DIM; d++) {
                     pf_c[d] = sd.in.ix[d][p];
@@ -268,13 +269,8 @@ __global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>()) k_push_tiled
                 pf_q = sd.in.q[p];
             }
         };
-        prefetch(index(0));
-        for (int it = 0; it < nit; it++) {
-            const int i = index(it);
-            bool has = i < n;
-            const long p = slab + (i < nst ? i : cap - 1 - (i - nst));
-            int c[3] = {1, 1, 1}, di[3] = {0, 0, 0};
-            float xo[3] = {0, 0, 0}, x1[3] = {0, 0, 0}, un[3] = {0, 0, 0}, q = 0.0f;
+        // take the prefetched particle into registers
+        auto take = [&](int *c, float *xo, float *un, float &q) {
 #pragma unroll
             for (int d = 0; d < 3; d++) {
                 c[d] = pf_c[d];
@@ -282,7 +278,14 @@ __global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>()) k_push_tiled
                 un[d] = pf_u[d];
             }
             q = pf_q;
-            if (it + 1 < nit) prefetch(index(it + 1));
+        };
+        // Push one particle (slot p; has = false: an idle lane), split its motion into in-cell
+        // segments sg[0..nseg), and write it back (stays in the tile) or queue it (leaves).
+        // Returns nseg, or -1 for an idle lane.  Warp-collective: every lane calls it.
+        auto push_one = [&](bool has, long p, int *c, float *xo, float *un, float q,
+                            SegRec *sg) -> int {
+            int di[3] = {0, 0, 0};
+            float x1[3] = {0, 0, 0};
             if (has) {
                 bool ok = true;
 #pragma unroll
@@ -298,7 +301,6 @@ __global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>()) k_push_tiled
             }
             // ---- gather from the staged tile, Boris, move, split into segments
             int nseg = 0;
-            SegRec sg[MAXSEG];
             if (has) {
                 float w[DIM][NP], wh[DIM][NP];
                 int lf[DIM], lh[DIM];
@@ -326,71 +328,94 @@ __global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>()) k_push_tiled
                                           jsy, jsz);
             }
             // ---- new position, cell (periodically wrapped) and destination tile
-            {
-                long dest = -1;
-                int cw[3] = {1, 1, 1};
-                if (has) {
-                    long dt = 0, mul = 1;
+            long dest = -1;
+            int cw[3] = {1, 1, 1};
+            if (has) {
+                long dt = 0, mul = 1;
 #pragma unroll
-                    for (int d = 0; d < DIM; d++) {
-                        xo[d] = x1[d] - float(di[d]);
-                        cw[d] = wrapc(c[d] + di[d], a.nx[d]);
-                        dt += mul * ((cw[d] - 1) / a.T[d]);
-                        mul *= a.ntile[d];
-                    }
-                    dest = dt;
+                for (int d = 0; d < DIM; d++) {
+                    xo[d] = x1[d] - float(di[d]);
+                    cw[d] = wrapc(c[d] + di[d], a.nx[d]);
+                    dt += mul * ((cw[d] - 1) / a.T[d]);
+                    mul *= a.ntile[d];
                 }
-                const bool stay = has && dest == tile;
-                int lcell = -1;
-                if (stay) {
+                dest = dt;
+            }
+            const bool stay = has && dest == tile;
+            int lcell = -1;
+            if (stay) {
 #pragma unroll
-                    for (int d = 0; d < DIM; d++) {
-                        sd.in.ix[d][p] = cw[d];
-                        sd.in.x[d][p] = xo[d];
-                    }
-                    sd.in.u[0][p] = un[0];
-                    sd.in.u[1][p] = un[1];
-                    sd.in.u[2][p] = un[2];
-                    lcell = cw[0] - t0[0];
-                    if (DIM > 1) lcell += a.T[0] * (cw[1] - t0[1]);
-                    if (DIM > 2) lcell += a.T[0] * a.T[1] * (cw[2] - t0[2]);
+                for (int d = 0; d < DIM; d++) {
+                    sd.in.ix[d][p] = cw[d];
+                    sd.in.x[d][p] = xo[d];
                 }
-                const unsigned peers = __match_any_sync(FULL_MASK, lcell);
-                if (stay && (int)lane == __ffs(peers) - 1) atomicAdd(&sHist[lcell], __popc(peers));
-                const bool leave = has && !stay;
-                const unsigned ml = __ballot_sync(FULL_MASK, leave);
-                if (ml) {
-                    const int leader = __ffs(ml) - 1;
-                    int q0 = 0;
-                    if ((int)lane == leader) q0 = atomicAdd(&sNleave, __popc(ml));
-                    q0 = __shfl_sync(FULL_MASK, q0, leader);
-                    if (leave) {
-                        sd.in.ix[0][p] = 0;
-                        const int e = q0 + __popc(ml & ((1u << lane) - 1u));
-                        if (e < LEAVE_QUEUE) {
+                sd.in.u[0][p] = un[0];
+                sd.in.u[1][p] = un[1];
+                sd.in.u[2][p] = un[2];
+                lcell = cw[0] - t0[0];
+                if (DIM > 1) lcell += a.T[0] * (cw[1] - t0[1]);
+                if (DIM > 2) lcell += a.T[0] * a.T[1] * (cw[2] - t0[2]);
+            }
+            const unsigned peers = __match_any_sync(FULL_MASK, lcell);
+            if (stay && (int)lane == __ffs(peers) - 1) atomicAdd(&sHist[lcell], __popc(peers));
+            const bool leave = has && !stay;
+            const unsigned ml = __ballot_sync(FULL_MASK, leave);
+            if (ml) {
+                const int leader = __ffs(ml) - 1;
+                int q0 = 0;
+                if ((int)lane == leader) q0 = atomicAdd(&sNleave, __popc(ml));
+                q0 = __shfl_sync(FULL_MASK, q0, leader);
+                if (leave) {
+                    sd.in.ix[0][p] = 0;
+                    const int e = q0 + __popc(ml & ((1u << lane) - 1u));
+                    if (e < LEAVE_QUEUE) {
 #pragma unroll
-                            for (int d = 0; d < 3; d++) {
-                                sLeaveI[e][d] = cw[d];
-                                sLeaveF[e][d] = xo[d];
-                                sLeaveF[e][3 + d] = un[d];
-                            }
-                            sLeaveI[e][3] = (int)dest;
-                            sLeaveF[e][6] = q;
-                        } else {
-                            emigrate<DIM>(sd, cap, dest, cw, xo, un, q, a.status);
+                        for (int d = 0; d < 3; d++) {
+                            sLeaveI[e][d] = cw[d];
+                            sLeaveF[e][d] = xo[d];
+                            sLeaveF[e][3 + d] = un[d];
                         }
+                        sLeaveI[e][3] = (int)dest;
+                        sLeaveF[e][6] = q;
+                    } else {
+                        emigrate<DIM>(sd, cap, dest, cw, xo, un, q, a.status);
                     }
                 }
             }
-            // ---- charge-conserving current of the segments into the shared tile
+            return has ? nseg : -1;
+        };
+        const int nit = (n + nthr - 1) / nthr;
+        auto index = [&](int it) {
+            return spread ? (int)threadIdx.x * nit + it : it * nthr + (int)threadIdx.x;
+        };
+        prefetch(index(0), n);
+        for (int it = 0; it < nit; it++) {
+            const int i = index(it);
+            SegRec sg[MAXSEG];
+            int c[3];
+            float xo[3], un[3], q;
+            take(c, xo, un, q);
+            if (it + 1 < nit) prefetch(index(it + 1), n);
+            const int ns = push_one(i < n, slot(i), c, xo, un, q, sg);
+            // ---- charge-conserving current of the segments into the shared tile.  The first
+            //      segment (in the particle's own cell, shared by neighbouring lanes of the
+            //      cell-sorted tile) is warp-reduced per cell; in 2D the others (face
+            //      crossings, few and scattered) wait in the warp's queue for a full-warp,
+            //      cell-sorted deposit
 #pragma unroll
             for (int t = 0; t < MAXSEG; t++) {
-                const bool hs = has && t < nseg;
+                const bool hs = t < ns;
+                if (DIM == 2 && t > 0) {
+                    segq_push(sQ, qn, hs, sg[t]);
+                    if (qn >= 32) segq_drain<ORD>(sJw, sQ, qn, 32, a.jn, jsy);
+                    continue;
+                }
                 if (!__any_sync(FULL_MASK, hs)) break;
                 deposit_segment<DIM, ORD>(sJw, hs ? &sg[t] : nullptr, a.jn, jsy, jsz,
                                           a.reduce_min, ls);
             }
         }
+        if (DIM == 2) segq_drain<ORD>(sJw, sQ, qn, 1, a.jn, jsy);
         const double tot = block_sum((double)my_ene);   // (contains block barriers)
         if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.ene + s, tot);
         // ---- the queued particles that left take their arrival slots
@@ -541,7 +566,9 @@ static size_t smem_for(int dim, int order, const int *T, int threads)
         nj *= (size_t)(T[d] + NP + 1);
     }
     const size_t copies = dim == 2 ? (size_t)threads / 32 : 1;
-    return (6 * ne + 3 * nj * copies) * sizeof(float);
+    const size_t nf = (6 * ne + 3 * nj * copies + 3) & ~(size_t)3;
+    const size_t queues = dim == 2 ? (size_t)(threads / 32) * SEGQ * sizeof(SegRec) : 0;
+    return nf * sizeof(float) + queues;
 }
 
 int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
