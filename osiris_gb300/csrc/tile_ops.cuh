@@ -10,6 +10,20 @@ namespace osg {
 
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
+// *hi += v, with the rounding error of the addition accumulated in *lo (two-sum: the pair
+// hi + lo keeps the sum of all added values to about twice the float precision).  Plain
+// read-modify-write: the caller owns the address (a warp-private tile, no other lane of the
+// same instruction on it).  Used for the warp-reduced cell sums, which carry most of a tile's
+// current; the scattered single adds (lone lanes, face crossings) are FP32 atomics.
+__device__ __forceinline__ void comp_add(float *hi, float *lo, float v)
+{
+    const float a = *hi, t = a + v;
+    const float bv = t - a;
+    const float err = (a - (t - bv)) + (v - bv);
+    *hi = t;
+    *lo += err;
+}
+
 // Staggered gather from a shared-memory tile of E (or B) stored as [z][y][x][3].
 // lf = local point of the particle's cell in the stencil frame, lh = lf - (x < 0).
 // E1 (h,f,f) E2 (f,h,f) E3 (f,f,h); B1 (f,h,h) B2 (h,f,h) B3 (h,h,f)  (2D: drop the z entry)
@@ -348,7 +362,7 @@ constexpr bool private_current() { return DIM == 2; }
 template <int DIM, int ORD>
 __device__ __forceinline__ void warp_deposit(float *sJ, int base, const float *v, int jsy,
                                              int jsz, int reduce_min,
-                                             const LaneSlots<DIM, ORD> &ls)
+                                             const LaneSlots<DIM, ORD> &ls, int jlo)
 {
     constexpr int NV = SegVals<DIM, ORD>::NV;
     constexpr int NB = (NV + 31) / 32;
@@ -386,7 +400,7 @@ __device__ __forceinline__ void warp_deposit(float *sJ, int base, const float *v
             if (ls.off[bch] >= 0) {
                 float *pj = sJ + key + ls.off[bch];
                 if (PRIV)
-                    *pj += sum;
+                    comp_add(pj, pj + jlo, sum);
                 else
                     atomicAdd(pj, sum);
             }
@@ -452,7 +466,7 @@ constexpr bool direct_only() { return DIM == 3 && ORD >= 3; }
 template <int DIM, int ORD>
 __device__ __forceinline__ void deposit_segment(float *sJ, const SegRec *rec, const float *jn,
                                                 int jsy, int jsz, int reduce_min,
-                                                const LaneSlots<DIM, ORD> &ls)
+                                                const LaneSlots<DIM, ORD> &ls, int jlo)
 {
     if constexpr (DIM == 3) {
         if (direct_only<DIM, ORD>() || reduce_min > 32) {
@@ -486,7 +500,7 @@ __device__ __forceinline__ void deposit_segment(float *sJ, const SegRec *rec, co
 #pragma unroll
         for (int k = 0; k < NV; k++) v[k] = 0.f;
     }
-    warp_deposit<DIM, ORD>(sJ, base, v, jsy, jsz, reduce_min, ls);
+    warp_deposit<DIM, ORD>(sJ, base, v, jsy, jsz, reduce_min, ls, jlo);
     }
 }
 

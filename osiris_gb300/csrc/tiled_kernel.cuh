@@ -1,0 +1,545 @@
+// tiled_kernel.cuh -- device side of the tiled particle engine: slab layout, launch arguments
+// and the push + deposit + migration kernel k_push_tiled<DIM, ORD, PUSHER>.  Included by
+// tiled.cu (Boris instantiations, host code) and tiled_exact.cu (exact-pusher instantiations),
+// so the two sets compile in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "pic_math.cuh"
+#include "push_plain.cuh"
+#include "tile_ops.cuh"
+
+namespace osg {
+
+struct Slabs {
+    int *ix[3];
+    float *x[3];
+    float *u[3];
+    float *q;
+    int *cnt;      // [ntiles] particles in slots [0, cnt) of the slab, sorted by cell
+    int *arr;      // [ntiles] particles that arrived from other tiles, slots [cap - arr, cap)
+};
+
+struct SpeciesDev {
+    Slabs in, out;
+    float tem;     // dt / (2 rqm) (Boris)
+    float qm;      // 1 / rqm (exact pusher)
+    long cap;      // slots per tile
+};
+
+struct TiledArgs {
+    int T[3];          // tile shape (cells)
+    int ntile[3];      // tiles per axis
+    int nx[3];         // cells per axis
+    int gcl[3];        // global guard cells (lower)
+    int size[3];       // global grid extent incl. guards
+    float dtdx[3];
+    float jn[3];
+    const float *e;
+    const float *b;
+    float *j;
+    const SpeciesDev *spec;
+    int nspec;
+    double *ene;
+    int *status;
+    int reduce_min;    // warp-reduce a cell's segments when at least this many lanes share it
+    double dt_full;    // exact pusher: the double time step and the Newton tolerance
+    double iter_tol;
+    // current of every tile with its halo, [tile][3 * points] (hi) and its compensation (lo,
+    // 2D), summed in FP64 in tile order by k_tile_fold
+    float *tile_hi;
+    float *tile_lo;
+};
+
+static const int MAX_TILED_SPECIES = 16;
+static const int MAX_TILE_CELLS = 1024;   // cells per tile (bins of the per-tile cell sort)
+
+__device__ __forceinline__ int wrapc(int c, int n)
+{
+    return c < 1 ? c + n : (c > n ? c - n : c);
+}
+
+// In-place exclusive scan of n ints in shared memory by one warp; returns the total.
+__device__ __forceinline__ int warp_exclusive_scan(int *c, int n)
+{
+    const int lane = threadIdx.x & 31, per = (n + 31) >> 5;
+    const int lo = lane * per, hi = min(lo + per, n);
+    int mine = 0;
+    for (int k = lo; k < hi; k++) mine += c[k];
+    int incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    int run = incl - mine;
+    for (int k = lo; k < hi; k++) {
+        const int v = c[k];
+        c[k] = run;
+        run += v;
+    }
+    return __shfl_sync(0xffffffffu, incl, 31);
+}
+
+// --------------------------------------------------------------------------------- push
+static const int LEAVE_QUEUE = 256;   // particles per CTA and species queued for emigration
+
+// Write a particle that left its tile into an arrival slot (from the top of the slab) of its
+// destination tile in the output buffer.  The arrival region stays above the particles the
+// destination keeps this step: those are at most its input particles.
+template <int DIM>
+__device__ __forceinline__ void emigrate(const SpeciesDev &sd, long cap, long dest,
+                                         const int *cw, const float *xo, const float *un,
+                                         float q, int *status)
+{
+    const int k = atomicAdd(sd.out.arr + dest, 1);
+    const int room = (int)cap - sd.in.cnt[dest] - sd.in.arr[dest];
+    if (k >= room) {
+        atomicOr(status, OSG_STATUS_OVERFLOW);
+        return;
+    }
+    const long o = dest * cap + cap - 1 - k;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+        sd.out.ix[d][o] = cw[d];
+        sd.out.x[d][o] = xo[d];
+    }
+    sd.out.u[0][o] = un[0];
+    sd.out.u[1][o] = un[1];
+    sd.out.u[2][o] = un[2];
+    sd.out.q[o] = q;
+}
+
+// Every warp of the CTA runs its own pipeline over chunks of 32 particles of the tile, with no
+// block barrier inside the particle loop: load, gather, Boris, move, split, write the particle
+// to its new slot, then deposit the segments (round t takes the t-th segment of every lane).
+// In 2D every warp accumulates into its own copy of the current tile, so the warp-reduced
+// passes add with plain shared read-modify-writes; the copies are summed when the tile is
+// flushed.  In 3D the warps share one current tile (atomic adds).
+// CTAs of up to 256 threads.  2D linear/quadratic: three resident CTAs per SM (at most 85
+// registers per thread, measured fastest on GB300); 2D quartic: one (it needs ~250 registers
+// without spilling); otherwise two
+template <int DIM, int ORD>
+constexpr int push_min_blocks() { return DIM == 2 ? (ORD <= 2 ? 3 : (ORD == 3 ? 2 : 1)) : 2; }
+
+template <int DIM, int ORD, int PUSHER>
+__global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>()) k_push_tiled(TiledArgs a)
+{
+    constexpr int NP = ORD + 1, OFS = Stencil<ORD>::OFS;
+    constexpr int MAXSEG = DIM == 2 ? 3 : 4;
+    constexpr bool PRIV = private_current<DIM>();
+    extern __shared__ float smem[];
+    const long tile = blockIdx.x;
+    int t0[3], tc[3];
+    tc[0] = (int)(tile % a.ntile[0]);
+    tc[1] = DIM > 1 ? (int)((tile / a.ntile[0]) % a.ntile[1]) : 0;
+    tc[2] = DIM > 2 ? (int)(tile / ((long)a.ntile[0] * a.ntile[1])) : 0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) t0[d] = tc[d] * a.T[d] + 1;
+
+    // shared layout: E and B over ee points per axis, J over je points per axis, 3 comps each
+    int ee[3], je[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        ee[d] = d < DIM ? a.T[d] + NP : 1;
+        je[d] = d < DIM ? a.T[d] + NP + 1 : 1;
+    }
+    const int ne = ee[0] * ee[1] * ee[2], nj = je[0] * je[1] * je[2];
+    const int nthr = blockDim.x, nwarp = nthr >> 5, warp = threadIdx.x >> 5;
+    const int njall = 3 * nj * (PRIV ? nwarp : 1);
+    // 2D: the warp copies of the current tile keep a two-sum compensation at offset jlo
+    const int jlo = PRIV ? njall : 0;
+    float *sE = smem, *sB = smem + 3 * ne, *sJ = smem + 6 * ne;
+    const long gsy = 3L * a.size[0], gsz = 3L * a.size[0] * a.size[1];
+
+    // stage fields: local point l <-> Fortran cell t0 - OFS + l <-> global position
+    // t0 - OFS + l - 1 + gcl (inside the guard cells for tiles at the box edge)
+    for (int idx = threadIdx.x; idx < 3 * ne; idx += nthr) {
+        const int c = idx % 3, pnt = idx / 3;
+        const int lx = pnt % ee[0], ly = (pnt / ee[0]) % ee[1], lz = pnt / (ee[0] * ee[1]);
+        long gp = 3L * (t0[0] - OFS + lx - 1 + a.gcl[0]) + c;
+        if (DIM > 1) gp += gsy * (t0[1] - OFS + ly - 1 + a.gcl[1]);
+        if (DIM > 2) gp += gsz * (t0[2] - OFS + lz - 1 + a.gcl[2]);
+        sE[idx] = __ldg(a.e + gp);
+        sB[idx] = __ldg(a.b + gp);
+    }
+    for (int idx = threadIdx.x; idx < njall + jlo; idx += nthr) sJ[idx] = 0.0f;
+    __syncthreads();
+
+    const int esy = 3 * ee[0], esz = 3 * ee[0] * ee[1];
+    const int jsy = 3 * je[0], jsz = 3 * je[0] * je[1];
+    const unsigned lane = threadIdx.x & 31;
+    float *sJw = PRIV ? sJ + 3 * nj * warp : sJ;
+    LaneSlots<DIM, ORD> ls;
+    ls.init(jsy, jsz);
+    // 3D direct deposits: every thread walks its own contiguous run of the cell-sorted tile,
+    // so the lanes of a warp sit in cells far apart and their shared-memory atomics seldom
+    // conflict; otherwise a warp takes 32 consecutive particles (mostly one cell)
+    const bool spread = DIM == 3 && (direct_only<DIM, ORD>() || a.reduce_min > 32);
+
+    __shared__ int sHist[MAX_TILE_CELLS];
+    // particles leaving the tile wait in a shared queue; after the pass they take their
+    // arrival slots all at once, so no warp waits on a global atomic inside the pass
+    __shared__ int sLeaveI[LEAVE_QUEUE][4];      // new cell per axis, destination tile
+    __shared__ float sLeaveF[LEAVE_QUEUE][8];    // offsets per axis, momenta, charge
+    __shared__ int sNleave;
+    // 2D: per-warp queues of segments for full-warp deposits (dynamic shared memory after the
+    // current tile, 16-byte aligned)
+    SegRec *sQ = reinterpret_cast<SegRec *>(smem + ((6 * ne + njall + jlo + 3) & ~3)) + warp * SEGQ;
+    int qn = 0;
+    const int ncell = a.T[0] * a.T[1] * a.T[2];
+
+    for (int s = 0; s < a.nspec; s++) {
+        const SpeciesDev sd = a.spec[s];
+        const long cap = sd.cap;
+        const long slab = tile * cap;
+        const int nst = min(sd.in.cnt[tile], (int)cap);
+        const int nar = min(sd.in.arr[tile], (int)cap - nst);
+        const int n = nst + nar;
+        for (int k = threadIdx.x; k < ncell; k += nthr) sHist[k] = 0;
+        if (threadIdx.x == 0) sNleave = 0;
+        __syncthreads();
+        // per-thread partial energy in FP32 (the reference sums in single precision per
+        // 464-particle chunk), summed over the block in double
+        float my_ene = 0.f;
+        // ---- pass A: push every particle of the tile.  Particles that stay are written back
+        //      to their own slot of the input slab (this CTA owns it) and counted per new cell;
+        //      particles that leave take an arrival slot (from the top) of their destination
+        //      tile in the output buffer, and their input slot is marked empty (ix = 0).
+        auto slot = [&](int i) { return slab + (i < nst ? i : cap - 1 - (i - nst)); };
+        // the particle of the next iteration is loaded while this one is pushed
+        int pf_c[3] = {1, 1, 1};
+        float pf_x[3] = {0, 0, 0}, pf_u[3] = {0, 0, 0}, pf_q = 0.0f;
+        auto prefetch = [&](int i, int lim) {
+            if (i < lim) {
+                const long p = slot(i);
+#pragma unroll
+                for (int d = 0; d < DIM; d++) {
+                    pf_c[d] = sd.in.ix[d][p];
+                    pf_x[d] = sd.in.x[d][p];
+                }
+                pf_u[0] = sd.in.u[0][p];
+                pf_u[1] = sd.in.u[1][p];
+                pf_u[2] = sd.in.u[2][p];
+                pf_q = sd.in.q[p];
+            }
+        };
+        // take the prefetched particle into registers
+        auto take = [&](int *c, float *xo, float *un, float &q) {
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                c[d] = pf_c[d];
+                xo[d] = pf_x[d];
+                un[d] = pf_u[d];
+            }
+            q = pf_q;
+        };
+        // Push one particle (slot p; has = false: an idle lane), split its motion into in-cell
+        // segments sg[0..nseg), and write it back (stays in the tile) or queue it (leaves).
+        // Returns nseg, or -1 for an idle lane.  Warp-collective: every lane calls it.
+        auto push_one = [&](bool has, long p, int *c, float *xo, float *un, float q,
+                            SegRec *sg) -> int {
+            int di[3] = {0, 0, 0};
+            float x1[3] = {0, 0, 0};
+            if (has) {
+                bool ok = true;
+#pragma unroll
+                for (int d = 0; d < DIM; d++) {
+                    const int lc = c[d] - t0[d];
+                    ok = ok && lc >= 0 && lc < a.T[d];
+                }
+                if (!ok) {
+                    atomicOr(a.status, OSG_STATUS_RANGE);
+                    sd.in.ix[0][p] = 0;
+                    has = false;
+                }
+            }
+            // ---- gather from the staged tile, Boris, move, split into segments
+            int nseg = 0;
+            if (has) {
+                float w[DIM][NP], wh[DIM][NP];
+                int lf[DIM], lh[DIM];
+#pragma unroll
+                for (int d = 0; d < DIM; d++) {
+                    spline<ORD>(xo[d], w[d]);
+                    const bool neg = xo[d] < 0.0f;
+                    lf[d] = c[d] - t0[d] + 1;
+                    lh[d] = lf[d] - (neg ? 1 : 0);
+                    spline_h<ORD>(xo[d], neg ? 1.0f : 0.0f, wh[d]);
+                }
+                float E1, E2, E3, B1, B2, B3;
+                gather_tile<DIM, ORD>(sE, sB, esy, esz, lf, lh, w, wh, E1, E2, E3, B1, B2, B3);
+                if constexpr (PUSHER == OSG_PUSHER_EXACT) {
+                    my_ene += exact_push<float>(sd.qm, a.dt_full, a.iter_tol, E1, E2, E3, B1,
+                                                B2, B3, q, un[0], un[1], un[2]);
+                } else {
+                    const float ene = boris(sd.tem, E1, E2, E3, B1, B2, B3, un[0], un[1], un[2]);
+                    my_ene = fmaf(q, ene, my_ene);
+                }
+                const float rg = rgamma(un[0], un[1], un[2]);
+                const float vv[3] = {un[0] * rg, un[1] * rg, un[2] * rg};
+#pragma unroll
+                for (int d = 0; d < DIM; d++) {
+                    x1[d] = fmaf(vv[d], a.dtdx[d], xo[d]);
+                    di[d] = trim(x1[d]);
+                }
+                nseg = make_segments<DIM>(sg, xo, x1, di, vv[2], q, c[0] - t0[0] + 1,
+                                          c[1] - t0[1] + 1, DIM > 2 ? c[2] - t0[2] + 1 : 0,
+                                          jsy, jsz);
+            }
+            // ---- new position, cell (periodically wrapped) and destination tile
+            long dest = -1;
+            int cw[3] = {1, 1, 1};
+            if (has) {
+                long dt = 0, mul = 1;
+#pragma unroll
+                for (int d = 0; d < DIM; d++) {
+                    xo[d] = x1[d] - float(di[d]);
+                    cw[d] = wrapc(c[d] + di[d], a.nx[d]);
+                    dt += mul * ((cw[d] - 1) / a.T[d]);
+                    mul *= a.ntile[d];
+                }
+                dest = dt;
+            }
+            const bool stay = has && dest == tile;
+            int lcell = -1;
+            if (stay) {
+#pragma unroll
+                for (int d = 0; d < DIM; d++) {
+                    sd.in.ix[d][p] = cw[d];
+                    sd.in.x[d][p] = xo[d];
+                }
+                sd.in.u[0][p] = un[0];
+                sd.in.u[1][p] = un[1];
+                sd.in.u[2][p] = un[2];
+                lcell = cw[0] - t0[0];
+                if (DIM > 1) lcell += a.T[0] * (cw[1] - t0[1]);
+                if (DIM > 2) lcell += a.T[0] * a.T[1] * (cw[2] - t0[2]);
+            }
+            const unsigned peers = __match_any_sync(FULL_MASK, lcell);
+            if (stay && (int)lane == __ffs(peers) - 1) atomicAdd(&sHist[lcell], __popc(peers));
+            const bool leave = has && !stay;
+            const unsigned ml = __ballot_sync(FULL_MASK, leave);
+            if (ml) {
+                const int leader = __ffs(ml) - 1;
+                int q0 = 0;
+                if ((int)lane == leader) q0 = atomicAdd(&sNleave, __popc(ml));
+                q0 = __shfl_sync(FULL_MASK, q0, leader);
+                if (leave) {
+                    sd.in.ix[0][p] = 0;
+                    const int e = q0 + __popc(ml & ((1u << lane) - 1u));
+                    if (e < LEAVE_QUEUE) {
+#pragma unroll
+                        for (int d = 0; d < 3; d++) {
+                            sLeaveI[e][d] = cw[d];
+                            sLeaveF[e][d] = xo[d];
+                            sLeaveF[e][3 + d] = un[d];
+                        }
+                        sLeaveI[e][3] = (int)dest;
+                        sLeaveF[e][6] = q;
+                    } else {
+                        emigrate<DIM>(sd, cap, dest, cw, xo, un, q, a.status);
+                    }
+                }
+            }
+            return has ? nseg : -1;
+        };
+        const int nit = (n + nthr - 1) / nthr;
+        auto index = [&](int it) {
+            return spread ? (int)threadIdx.x * nit + it : it * nthr + (int)threadIdx.x;
+        };
+        prefetch(index(0), n);
+        for (int it = 0; it < nit; it++) {
+            const int i = index(it);
+            SegRec sg[MAXSEG];
+            int c[3];
+            float xo[3], un[3], q;
+            take(c, xo, un, q);
+            if (it + 1 < nit) prefetch(index(it + 1), n);
+            const int ns = push_one(i < n, slot(i), c, xo, un, q, sg);
+            // ---- charge-conserving current of the segments into the shared tile.  The first
+            //      segment (in the particle's own cell, shared by neighbouring lanes of the
+            //      cell-sorted tile) is warp-reduced per cell; in 2D the others (face
+            //      crossings, few and scattered) wait in the warp's queue for a full-warp,
+            //      cell-sorted deposit
+#pragma unroll
+            for (int t = 0; t < MAXSEG; t++) {
+                const bool hs = t < ns;
+                if (DIM == 2 && t > 0) {
+                    segq_push(sQ, qn, hs, sg[t]);
+                    if (qn >= 32) segq_drain<ORD>(sJw, sQ, qn, 32, a.jn, jsy);
+                    continue;
+                }
+                if (!__any_sync(FULL_MASK, hs)) break;
+                deposit_segment<DIM, ORD>(sJw, hs ? &sg[t] : nullptr, a.jn, jsy, jsz,
+                                          a.reduce_min, ls, jlo);
+            }
+        }
+        if (DIM == 2) segq_drain<ORD>(sJw, sQ, qn, 1, a.jn, jsy);
+        const double tot = block_sum((double)my_ene);   // (contains block barriers)
+        if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.ene + s, tot);
+        // ---- the queued particles that left take their arrival slots
+        {
+            const int nq = min(sNleave, LEAVE_QUEUE);
+            for (int e = threadIdx.x; e < nq; e += nthr) {
+                int cw[3];
+                float xo[3], un[3];
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    cw[d] = sLeaveI[e][d];
+                    xo[d] = sLeaveF[e][d];
+                    un[d] = sLeaveF[e][3 + d];
+                }
+                emigrate<DIM>(sd, cap, sLeaveI[e][3], cw, xo, un, sLeaveF[e][6], a.status);
+            }
+        }
+        // ---- cell offsets of the particles that stayed
+        if (threadIdx.x < 32) {
+            const int nstay = warp_exclusive_scan(sHist, ncell);
+            if (threadIdx.x == 0) sd.out.cnt[tile] = nstay;
+        }
+        __syncthreads();
+        // ---- pass B: counting-sort the particles that stayed into the output slab, so that
+        //      every step starts from particles in cell order (consecutive lanes share a cell)
+        for (int base = 0; base < n; base += nthr) {
+            const int i = base + threadIdx.x;
+            const long p = slab + (i < nst ? i : cap - 1 - (i - nst));
+            int lcell = -1;
+            int cc[3] = {0, 0, 0};
+            if (i < n) {
+#pragma unroll
+                for (int d = 0; d < DIM; d++) cc[d] = sd.in.ix[d][p];
+                if (cc[0] != 0) {
+                    lcell = cc[0] - t0[0];
+                    if (DIM > 1) lcell += a.T[0] * (cc[1] - t0[1]);
+                    if (DIM > 2) lcell += a.T[0] * a.T[1] * (cc[2] - t0[2]);
+                }
+            }
+            const unsigned peers = __match_any_sync(FULL_MASK, lcell);
+            const int leader = __ffs(peers) - 1;
+            int first = 0;
+            if (lcell >= 0 && (int)lane == leader) first = atomicAdd(&sHist[lcell], __popc(peers));
+            first = __shfl_sync(FULL_MASK, first, leader);
+            if (lcell >= 0) {
+                const long o = slab + first + __popc(peers & ((1u << lane) - 1u));
+#pragma unroll
+                for (int d = 0; d < DIM; d++) {
+                    sd.out.ix[d][o] = cc[d];
+                    sd.out.x[d][o] = sd.in.x[d][p];
+                }
+                sd.out.u[0][o] = sd.in.u[0][p];
+                sd.out.u[1][o] = sd.in.u[1][p];
+                sd.out.u[2][o] = sd.in.u[2][p];
+                sd.out.q[o] = sd.in.q[p];
+            }
+        }
+        __syncthreads();
+    }
+    // ---- store the tile's current (with halo) for the tile-ordered FP64 re-summation: in 2D
+    //      the warp copies and their compensations are summed in double and kept as a float
+    //      pair (hi, lo); in 3D the single shared tile is stored as it is
+    {
+        float *th = a.tile_hi + tile * (3L * nj);
+        float *tl = PRIV ? a.tile_lo + tile * (3L * nj) : nullptr;
+        for (int idx = threadIdx.x; idx < 3 * nj; idx += nthr) {
+            if (PRIV) {
+                double v = 0.0;
+                for (int w = 0; w < nwarp; w++)
+                    v += (double)sJ[3 * nj * w + idx] + (double)sJ[jlo + 3 * nj * w + idx];
+                const float hi = (float)v;
+                th[idx] = hi;
+                tl[idx] = (float)(v - (double)hi);
+            } else {
+                th[idx] = sJ[idx];
+            }
+        }
+    }
+}
+
+// Deterministic current flush: every point of the global current (guard cells included) is
+// the FP64 sum, in increasing tile order, of the tile currents (hi + lo) whose halo covers it,
+// rounded once to float.  A tile with origin cell t0 = tc * T + 1 covers the global positions
+// [tc * T - OFS + gcl, tc * T - OFS + gcl + je) along each axis (je = T + ORD + 2 points).
+template <int DIM>
+__global__ void k_tile_fold(const float *__restrict__ th, const float *__restrict__ tl,
+                            float *__restrict__ j, int3 size, int3 T, int3 ntile, int3 je,
+                            int3 gcl, int ofs, long npts)
+{
+    OSG_GRID_LOOP(g, npts)
+    {
+        const int c = (int)(g % 3);
+        const long p = g / 3;
+        const int gx = (int)(p % size.x);
+        const int gy = DIM > 1 ? (int)((p / size.x) % size.y) : 0;
+        const int gz = DIM > 2 ? (int)(p / ((long)size.x * size.y)) : 0;
+        const int gp[3] = {gx, gy, gz};
+        const int Ta[3] = {T.x, T.y, T.z}, nt[3] = {ntile.x, ntile.y, ntile.z};
+        const int jea[3] = {je.x, je.y, je.z}, gl[3] = {gcl.x, gcl.y, gcl.z};
+        int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            if (d < DIM) {
+                // tiles tc with 0 <= gp - (tc * T - ofs + gl) < je
+                const int r = gp[d] + ofs - gl[d];
+                int a0 = r - jea[d] + 1;
+                a0 = a0 <= 0 ? 0 : (a0 + Ta[d] - 1) / Ta[d];
+                int a1 = r < 0 ? -1 : r / Ta[d];
+                lo[d] = a0;
+                hi[d] = a1 < nt[d] - 1 ? a1 : nt[d] - 1;
+            }
+        }
+        const int nj = jea[0] * (DIM > 1 ? jea[1] : 1) * (DIM > 2 ? jea[2] : 1);
+        double v = 0.0;
+        for (int tz = lo[2]; tz <= hi[2]; tz++)
+            for (int ty = lo[1]; ty <= hi[1]; ty++)
+                for (int tx = lo[0]; tx <= hi[0]; tx++) {
+                    const long tile = tx + (long)nt[0] * (ty + (long)nt[1] * tz);
+                    const int lx = gx - (tx * Ta[0] - ofs + gl[0]);
+                    const int ly = DIM > 1 ? gy - (ty * Ta[1] - ofs + gl[1]) : 0;
+                    const int lz = DIM > 2 ? gz - (tz * Ta[2] - ofs + gl[2]) : 0;
+                    const long o = tile * (3L * nj) + 3L * (lx + jea[0] * (ly + (long)jea[1] * lz)) + c;
+                    v += (double)th[o];
+                    if (tl) v += (double)tl[o];
+                }
+        j[g] = (float)v;
+    }
+}
+
+// Launch of the push kernel of one (dim, order) for each pusher, and the opt-in to its dynamic
+// shared memory (call outside stream capture).  tiled.cu defines the Boris pair, tiled_exact.cu
+// the exact-pusher pair.
+int push_tiled_launch_boris(int dim, int order, const TiledArgs &a, unsigned ntiles,
+                            int threads, size_t smem, cudaStream_t st);
+cudaError_t push_tiled_attr_boris(int dim, int order, int bytes);
+int push_tiled_launch_exact(int dim, int order, const TiledArgs &a, unsigned ntiles,
+                            int threads, size_t smem, cudaStream_t st);
+cudaError_t push_tiled_attr_exact(int dim, int order, int bytes);
+
+#define OSG_DEFINE_PUSH_TILED(P, LAUNCH, ATTR)                                                \
+    int LAUNCH(int dim, int order, const TiledArgs &a, unsigned ntiles, int threads,          \
+               size_t smem, cudaStream_t st)                                                  \
+    {                                                                                         \
+        OSG_PUSH_TILED_CASES(P, OSG_PUSH_TILED_LAUNCH)                                        \
+        set_error("tiled engine: unsupported dim %d order %d", dim, order);                  \
+        return OSG_ERR_ARG;                                                                   \
+    }                                                                                         \
+    cudaError_t ATTR(int dim, int order, int bytes)                                           \
+    {                                                                                         \
+        OSG_PUSH_TILED_CASES(P, OSG_PUSH_TILED_ATTR)                                          \
+        return cudaErrorInvalidValue;                                                         \
+    }
+#define OSG_PUSH_TILED_LAUNCH(D, O, P)                                                        \
+    if (dim == D && order == O) {                                                             \
+        k_push_tiled<D, O, P><<<ntiles, threads, smem, st>>>(a);                              \
+        return OSG_OK;                                                                        \
+    }
+#define OSG_PUSH_TILED_ATTR(D, O, P)                                                          \
+    if (dim == D && order == O)                                                               \
+        return cudaFuncSetAttribute(k_push_tiled<D, O, P>,                                    \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+#define OSG_PUSH_TILED_CASES(P, X)                                                            \
+    X(2, 1, P) X(2, 2, P) X(2, 3, P) X(2, 4, P) X(3, 1, P) X(3, 2, P) X(3, 3, P) X(3, 4, P)
+
+} // namespace osg

@@ -51,10 +51,11 @@ def _setup(oracle, prec, dim, order, nx, ppc, seed, uth=0.3, ufl=0.2):
 
 
 def _compare(osg, oracle, prec, engine, dim, order, nx, ppc, steps, tol, tile=None, seed=5,
-             n_sort=0):
+             n_sort=0, pusher="boris"):
     p, g, dx, dt, species, e, b = _setup(oracle, prec, dim, order, nx, ppc, seed)
     sim = osg.Simulation(nx, dx, dt, order=order, precision=prec, engine=engine, tile=tile,
-                         n_sort=n_sort)
+                         n_sort=n_sort,
+                         pusher=osg.PUSHER_EXACT if pusher == "exact" else osg.PUSHER_BORIS)
     sim.set_fields(e, b)
     for s in species:
         sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
@@ -64,7 +65,7 @@ def _compare(osg, oracle, prec, engine, dim, order, nx, ppc, steps, tol, tile=No
            for s in species]
     eo, bo, jo = e.copy(), b.copy(), g.zeros(p)
     for _ in range(steps):
-        ene_o = oracle.step(g, p, eo, bo, jo, ora, dt)
+        ene_o = oracle.step(g, p, eo, bo, jo, ora, dt, pusher=pusher)
     errs = {"E": _nerr(g.interior(eg), g.interior(eo)), "B": _nerr(g.interior(bg), g.interior(bo)),
             "J": _nerr(g.interior(jg), g.interior(jo))}
     for k, s in enumerate(ora):
