@@ -231,6 +231,51 @@ int osg_sim_launches_per_step(osg_sim *s);
 /* Run n steps bracketed by CUDA events on the simulation's stream; *ms = device time. */
 int osg_sim_time_steps(osg_sim *s, int nsteps, float *ms);
 
+/* ------------------------------------------------------------ batched independent boxes --- */
+
+/* Many independent periodic boxes of uneven size and particle load advanced together (mixed
+ * precision, tiled engine, Boris pusher): one persistent push launch takes the tiles of all
+ * boxes from a work list (heaviest boxes first), every field phase is one launch over all
+ * boxes, and each full step is replayed from one CUDA graph.  Each box runs the time step of
+ * osg_sim (phase order of iter_sim, source/os-simulation.f03:498-666) on its own fields.
+ * A tile shape or CTA size left at 0 is chosen by the autotuner on the first step (or on
+ * osg_batch_tuning): it times every candidate on a proxy batch of one box per distinct
+ * (size, particles per cell) class and keeps the fastest. */
+typedef struct osg_batch osg_batch;
+typedef struct {
+    int dim;          /* 2 or 3 */
+    int order;        /* interpolation order 1..4 */
+    double dt;        /* time step, shared by all boxes (Courant-checked per box) */
+    int tile[3];      /* tile shape in cells; 0 = autotuned */
+    int threads;      /* threads per push CTA (64..256, multiple of 32); 0 = autotuned */
+    double capacity;  /* slots per tile as a multiple of the mean load (0 = 3.0) */
+} osg_batch_config;
+
+int osg_batch_create(const osg_batch_config *cfg, osg_batch **out);
+int osg_batch_destroy(osg_batch *b);
+/* add a box (cells and cell size per axis); returns its index (>= 0) or an error code */
+int osg_batch_add_box(osg_batch *b, const int *nx, const double *dx);
+/* add a species to a box from host arrays (reference layout, float); the data are copied.
+ * Returns the species index (>= 0) or an error code.  Boxes and species come before the first
+ * step. */
+int osg_batch_add_species(osg_batch *b, int box, double rqm, long np, const int *ix,
+                          const float *x, const float *u, const float *q);
+/* builds the batch if needed (autotuning first when asked) and reports the tile shape and CTA
+ * size in use */
+int osg_batch_tuning(osg_batch *b, int *tile, int *threads);
+int osg_batch_step(osg_batch *b, int nsteps);
+/* n steps bracketed by CUDA events on the batch's stream; *ms = device time */
+int osg_batch_time_steps(osg_batch *b, int nsteps, float *ms);
+void *osg_batch_stream(osg_batch *b);
+int osg_batch_num_boxes(osg_batch *b);
+int osg_batch_launches_per_step(osg_batch *b);
+/* FP64 diagnostics of one box, as osg_sim_energy */
+int osg_batch_energy(osg_batch *b, int box, double *kinetic, double *field);
+int osg_batch_get_fields(osg_batch *b, int box, float *e, float *bf, float *j);
+int osg_batch_num_particles(osg_batch *b, int box, int species, long *np);
+int osg_batch_get_species(osg_batch *b, int box, int species, int *ix, float *x, float *u,
+                          float *q);
+
 #ifdef __cplusplus
 }
 #endif

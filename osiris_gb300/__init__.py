@@ -55,6 +55,7 @@ def lib():
             raise OsirisGB300Error(-2, f"native library not built: {LIB_PATH}")
         _lib = C.CDLL(LIB_PATH)
         _declare(_lib)
+        _declare_batch(_lib)
     return _lib
 
 
@@ -108,6 +109,29 @@ def _declare(lb):
     lb.osg_sim_time_steps.argtypes = [P, I, C.POINTER(F)]
     lb.osg_sim_tile_occupancy.argtypes = [P, C.POINTER(D)]
     lb.osg_set_device.argtypes = [I]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("dim", I), ("order", I), ("dt", D), ("tile", I * 3), ("threads", I),
+                ("capacity", D)]
+
+
+def _declare_batch(lb):
+    lb.osg_batch_create.argtypes = [P, P]
+    lb.osg_batch_destroy.argtypes = [P]
+    lb.osg_batch_add_box.argtypes = [P, P, P]
+    lb.osg_batch_add_species.argtypes = [P, I, D, L, P, P, P, P]
+    lb.osg_batch_tuning.argtypes = [P, P, P]
+    lb.osg_batch_step.argtypes = [P, I]
+    lb.osg_batch_time_steps.argtypes = [P, I, P]
+    lb.osg_batch_stream.argtypes = [P]
+    lb.osg_batch_stream.restype = P
+    lb.osg_batch_num_boxes.argtypes = [P]
+    lb.osg_batch_launches_per_step.argtypes = [P]
+    lb.osg_batch_energy.argtypes = [P, I, P, P]
+    lb.osg_batch_get_fields.argtypes = [P, I, P, P, P]
+    lb.osg_batch_num_particles.argtypes = [P, I, I, P]
+    lb.osg_batch_get_species.argtypes = [P, I, I, P, P, P, P]
 
 
 def _check(rc):
@@ -395,3 +419,91 @@ class Simulation:
 
 def set_device(device):
     _check(lib().osg_set_device(int(device)))
+
+
+class Batch:
+    """Many independent periodic boxes advanced together (osg_batch_*): one persistent push
+    launch over the tiles of all boxes, one launch per field phase, one CUDA graph per step.
+    ``tile``/``threads`` left at None/0 are chosen by the autotuner on the first step."""
+
+    def __init__(self, dim, order, dt, tile=None, threads=0, capacity=0.0):
+        cfg = BatchConfig()
+        cfg.dim, cfg.order, cfg.dt, cfg.threads, cfg.capacity = dim, order, dt, threads, capacity
+        for d in range(dim):
+            cfg.tile[d] = tile[d] if tile else 0
+        self.dim, self.order, self.dt = dim, order, dt
+        self.h = P()
+        _check(lib().osg_batch_create(C.byref(cfg), C.byref(self.h)))
+        self.boxes = []
+
+    def close(self):
+        if self.h:
+            lib().osg_batch_destroy(self.h)
+            self.h = P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_box(self, nx, dx):
+        rc = lib().osg_batch_add_box(self.h, _p(_i32(nx)), _p(_f64(dx)))
+        _check(min(rc, 0))
+        gl, gu = GUARD[self.order]
+        self.boxes.append(dict(nx=list(nx), dx=list(dx), size=[n + gl + gu for n in nx],
+                               species=0))
+        return rc
+
+    def add_species(self, box, rqm, ix, x, u, q):
+        _need(ix, np.int32, "ix")
+        for a, n in ((x, "x"), (u, "u"), (q, "q")):
+            _need(a, np.float32, n)
+        rc = lib().osg_batch_add_species(self.h, box, float(rqm), len(q), _p(ix), _p(x), _p(u),
+                                         _p(q))
+        _check(min(rc, 0))
+        self.boxes[box]["species"] += 1
+        return rc
+
+    def tuning(self):
+        t = np.zeros(3, np.int32)
+        th = C.c_int()
+        _check(lib().osg_batch_tuning(self.h, _p(t), C.byref(th)))
+        return [int(v) for v in t[: self.dim]], th.value
+
+    def step(self, n=1):
+        _check(lib().osg_batch_step(self.h, int(n)))
+
+    def time_steps(self, n):
+        ms = C.c_float()
+        _check(lib().osg_batch_time_steps(self.h, int(n), C.byref(ms)))
+        return ms.value
+
+    def launches_per_step(self):
+        return lib().osg_batch_launches_per_step(self.h)
+
+    def energy(self, box):
+        kin = np.zeros(max(1, self.boxes[box]["species"]))
+        fld = np.zeros(6)
+        _check(lib().osg_batch_energy(self.h, box, _p(kin), _p(fld)))
+        return kin[: self.boxes[box]["species"]], fld
+
+    def fields(self, box):
+        shape = tuple(reversed(self.boxes[box]["size"])) + (3,)
+        e, b, j = (np.zeros(shape, np.float32) for _ in range(3))
+        _check(lib().osg_batch_get_fields(self.h, box, _p(e), _p(b), _p(j)))
+        return e, b, j
+
+    def num_particles(self, box, k):
+        n = C.c_long()
+        _check(lib().osg_batch_num_particles(self.h, box, k, C.byref(n)))
+        return n.value
+
+    def species(self, box, k):
+        n = self.num_particles(box, k)
+        ix = np.zeros((n, self.dim), np.int32)
+        x = np.zeros((n, self.dim), np.float32)
+        u = np.zeros((n, 3), np.float32)
+        q = np.zeros(n, np.float32)
+        _check(lib().osg_batch_get_species(self.h, box, k, _p(ix), _p(x), _p(u), _p(q)))
+        return ix, x, u, q

@@ -26,7 +26,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "-I", ROOT]
 
-SOURCES = ["push_plain.cu", "fields.cu", "tiled.cu", "tiled_exact.cu", "sim.cu", "capi.cu", "noalloc.cu",
+SOURCES = ["push_plain.cu", "fields.cu", "tiled.cu", "tiled_exact.cu", "batch_push.cu", "batch.cu",
+           "sim.cu", "capi.cu", "noalloc.cu",
            "loader.cpp"]
 
 

@@ -19,48 +19,9 @@
 
 namespace osg {
 
-// Fortran indices (i1,i2,i3) of flat point n of the box [lo, lo + ext) in each axis
-__device__ __forceinline__ void unflat(long n, const int *lo, const int *ext, int &i1, int &i2,
-                                       int &i3)
-{
-    i1 = lo[0] + (int)(n % ext[0]);
-    long r = n / ext[0];
-    i2 = lo[1] + (int)(r % ext[1]);
-    i3 = lo[2] + (int)(r / ext[1]);
-}
-
-__device__ __forceinline__ long pos(const GridDesc &g, int i1, int i2, int i3)
-{
-    return 3L * ((long)(i1 - 1 + g.gcl[0]) +
-                 (long)g.size[0] * ((i2 - 1 + g.gcl[1]) + (long)g.size[1] * (i3 - 1 + g.gcl[2])));
-}
-
-struct Box {
-    int lo[3], ext[3];
-    long n;
-};
-
-static Box make_box(const GridDesc &g, int lo, int hi_off)
-{
-    // points lo .. nx + hi_off along active axes, single point 1 on inactive ones
-    Box b;
-    b.n = 1;
-    for (int d = 0; d < 3; d++) {
-        if (d < g.dim) {
-            b.lo[d] = lo;
-            b.ext[d] = g.nx[d] + hi_off - lo + 1;
-        } else {
-            b.lo[d] = 1;
-            b.ext[d] = 1;
-        }
-        b.n *= b.ext[d];
-    }
-    return b;
-}
-
 template <typename T, int DIM>
-__global__ void k_dbdt(GridDesc g, Box box, T *__restrict__ b, const T *__restrict__ e, T d1, T d2,
-                       T d3)
+__device__ __forceinline__ void dbdt_body(const GridDesc &g, const Box &box, T *__restrict__ b,
+                                          const T *__restrict__ e, T d1, T d2, T d3)
 {
     OSG_GRID_LOOP(n, box.n)
     {
@@ -84,8 +45,16 @@ __global__ void k_dbdt(GridDesc g, Box box, T *__restrict__ b, const T *__restri
 }
 
 template <typename T, int DIM>
-__global__ void k_dedt(GridDesc g, Box box, T *__restrict__ e, const T *__restrict__ b,
-                       const T *__restrict__ j, T dti, T d1, T d2, T d3)
+__global__ void k_dbdt(GridDesc g, Box box, T *__restrict__ b, const T *__restrict__ e, T d1, T d2,
+                       T d3)
+{
+    dbdt_body<T, DIM>(g, box, b, e, d1, d2, d3);
+}
+
+template <typename T, int DIM>
+__device__ __forceinline__ void dedt_body(const GridDesc &g, const Box &box, T *__restrict__ e,
+                                          const T *__restrict__ b, const T *__restrict__ j, T dti,
+                                          T d1, T d2, T d3)
 {
     OSG_GRID_LOOP(n, box.n)
     {
@@ -111,6 +80,13 @@ __global__ void k_dedt(GridDesc g, Box box, T *__restrict__ e, const T *__restri
             e[p + 2] = e[p + 2] - dti * j[p + 2] + d1 * (b[p + 1] - b[p - sx + 1]);
         }
     }
+}
+
+template <typename T, int DIM>
+__global__ void k_dedt(GridDesc g, Box box, T *__restrict__ e, const T *__restrict__ b,
+                       const T *__restrict__ j, T dti, T d1, T d2, T d3)
+{
+    dedt_body<T, DIM>(g, box, e, b, j, dti, d1, d2, d3);
 }
 
 template <typename T>
@@ -151,7 +127,8 @@ void yee_advance(const GridDesc &g, T *e, T *b, const T *j, const double *dx, do
 // One direction of the periodic update.  Thread n handles one guard point (lower or upper
 // side along axis `d`, full range along the others) and its periodic image.
 template <typename T>
-__global__ void k_periodic_dir(GridDesc g, int d, int add, T *__restrict__ f, long n_lo, long n_all)
+__device__ __forceinline__ void periodic_body(const GridDesc &g, int d, int add,
+                                              T *__restrict__ f, long n_lo, long n_all)
 {
     OSG_GRID_LOOP(n, n_all)
     {
@@ -186,6 +163,12 @@ __global__ void k_periodic_dir(GridDesc g, int d, int add, T *__restrict__ f, lo
             }
         }
     }
+}
+
+template <typename T>
+__global__ void k_periodic_dir(GridDesc g, int d, int add, T *__restrict__ f, long n_lo, long n_all)
+{
+    periodic_body<T>(g, d, add, f, n_lo, n_all);
 }
 
 template <typename T>
@@ -347,6 +330,87 @@ void gauss_residual(const GridDesc &g, const T *e, const double *rho, const doub
                                    d_max, d_l2);
 }
 
+
+
+// ------------------------------------------------------------------------ batched boxes
+FieldBox make_field_box(const GridDesc &g, float *e, float *b, float *j, const double *dx,
+                        double dt)
+{
+    FieldBox f;
+    f.g = g;
+    f.e = e;
+    f.b = b;
+    f.j = j;
+    const double h = dt / 2.0;
+    f.d1h = (float)(h / dx[0]);
+    f.d2h = g.dim > 1 ? (float)(h / dx[1]) : 0.0f;
+    f.d3h = g.dim > 2 ? (float)(h / dx[2]) : 0.0f;
+    f.dti = (float)dt;
+    f.d1 = (float)(dt / dx[0]);
+    f.d2 = g.dim > 1 ? (float)(dt / dx[1]) : 0.0f;
+    f.d3 = g.dim > 2 ? (float)(dt / dx[2]) : 0.0f;
+    return f;
+}
+
+template <int DIM>
+__global__ void k_batch_periodic(const FieldBox *__restrict__ boxes, int d, int which, int add)
+{
+    const FieldBox &fb = boxes[blockIdx.y];
+    float *f = which == 0 ? fb.e : (which == 1 ? fb.b : fb.j);
+    long other = 1;
+#pragma unroll
+    for (int a = 0; a < DIM; a++)
+        if (a != d) other *= fb.g.size[a];
+    const long n_lo = other * fb.g.gcl[d], n_all = n_lo + other * fb.g.gcu[d];
+    periodic_body<float>(fb.g, d, add, f, n_lo, n_all);
+}
+
+template <int DIM>
+__global__ void k_batch_dbdt(const FieldBox *__restrict__ boxes)
+{
+    const FieldBox &fb = boxes[blockIdx.y];
+    const Box box = make_box(fb.g, 0, 1);
+    dbdt_body<float, DIM>(fb.g, box, fb.b, fb.e, fb.d1h, fb.d2h, fb.d3h);
+}
+
+template <int DIM>
+__global__ void k_batch_dedt(const FieldBox *__restrict__ boxes)
+{
+    const FieldBox &fb = boxes[blockIdx.y];
+    const Box box = make_box(fb.g, 1, 1);
+    dedt_body<float, DIM>(fb.g, box, fb.e, fb.b, fb.j, fb.dti, fb.d1, fb.d2, fb.d3);
+}
+
+static unsigned batch_blocks(long n)
+{
+    long b = (n + 255) / 256;
+    if (b > 1024) b = 1024;   // grid-stride beyond that
+    return (unsigned)(b < 1 ? 1 : b);
+}
+
+void batch_periodic(const FieldBox *d_boxes, int nbox, int dim, int which, int add,
+                    long max_side, cudaStream_t st)
+{
+    const dim3 grid(batch_blocks(max_side), (unsigned)nbox);
+    for (int d = 0; d < dim; d++) {
+        if (dim == 2) k_batch_periodic<2><<<grid, 256, 0, st>>>(d_boxes, d, which, add);
+        else k_batch_periodic<3><<<grid, 256, 0, st>>>(d_boxes, d, which, add);
+    }
+}
+
+void batch_yee(const FieldBox *d_boxes, int nbox, int dim, long max_points, cudaStream_t st)
+{
+    const dim3 grid(batch_blocks(max_points), (unsigned)nbox);
+    if (dim == 2) {
+        k_batch_dbdt<2><<<grid, 256, 0, st>>>(d_boxes);
+        k_batch_dedt<2><<<grid, 256, 0, st>>>(d_boxes);
+        k_batch_dbdt<2><<<grid, 256, 0, st>>>(d_boxes);
+    } else {
+        k_batch_dbdt<3><<<grid, 256, 0, st>>>(d_boxes);
+        k_batch_dedt<3><<<grid, 256, 0, st>>>(d_boxes);
+        k_batch_dbdt<3><<<grid, 256, 0, st>>>(d_boxes);
+    }
+}
 
 template void yee_advance<float>(const GridDesc &, float *, float *, const float *,
                                  const double *, double, cudaStream_t);

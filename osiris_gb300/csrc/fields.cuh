@@ -7,9 +7,66 @@
 
 namespace osg {
 
+// Fortran indices (i1,i2,i3) of flat point n of the box [lo, lo + ext) in each axis
+__device__ __forceinline__ void unflat(long n, const int *lo, const int *ext, int &i1, int &i2,
+                                       int &i3)
+{
+    i1 = lo[0] + (int)(n % ext[0]);
+    long r = n / ext[0];
+    i2 = lo[1] + (int)(r % ext[1]);
+    i3 = lo[2] + (int)(r / ext[1]);
+}
+
+__device__ __forceinline__ long pos(const GridDesc &g, int i1, int i2, int i3)
+{
+    return 3L * ((long)(i1 - 1 + g.gcl[0]) +
+                 (long)g.size[0] * ((i2 - 1 + g.gcl[1]) + (long)g.size[1] * (i3 - 1 + g.gcl[2])));
+}
+
+struct Box {
+    int lo[3], ext[3];
+    long n;
+};
+
+__host__ __device__ inline Box make_box(const GridDesc &g, int lo, int hi_off)
+{
+    // points lo .. nx + hi_off along active axes, single point 1 on inactive ones
+    Box b;
+    b.n = 1;
+    for (int d = 0; d < 3; d++) {
+        if (d < g.dim) {
+            b.lo[d] = lo;
+            b.ext[d] = g.nx[d] + hi_off - lo + 1;
+        } else {
+            b.lo[d] = 1;
+            b.ext[d] = 1;
+        }
+        b.n *= b.ext[d];
+    }
+    return b;
+}
+
 template <typename T>
 void yee_advance(const GridDesc &g, T *e, T *b, const T *j, const double *dx, double dt,
                  cudaStream_t st);
+
+// One box of a batch of independent periodic boxes (single precision): its fields and the
+// Yee coefficients.  The batched launches take a device array of these, one box per
+// blockIdx.y, and run the same per-point code as the single-box kernels.
+struct FieldBox {
+    GridDesc g;
+    float *e, *b, *j;
+    float d1h, d2h, d3h;      // dt / 2 / dx: the B half steps
+    float dti, d1, d2, d3;    // dt and dt / dx: the E step
+};
+FieldBox make_field_box(const GridDesc &g, float *e, float *b, float *j, const double *dx,
+                        double dt);
+// periodic update of field `which` (0 = E, 1 = B, 2 = J) of every box, one launch per axis;
+// max_side = the largest guard-slab point count over the boxes
+void batch_periodic(const FieldBox *d_boxes, int nbox, int dim, int which, int add,
+                    long max_side, cudaStream_t st);
+// B half step, E step, B half step of every box; max_points = the largest box's point count
+void batch_yee(const FieldBox *d_boxes, int nbox, int dim, long max_points, cudaStream_t st);
 
 // add = 1: fold guard cells into their periodic images (current); add = 0: replace
 template <typename T> void periodic_update(const GridDesc &g, T *f, int add, cudaStream_t st);

@@ -397,6 +397,87 @@ int tiled_add_species(TiledState *t, double rqm, long np, const int *ix, const f
     return upload_tables(t, st);
 }
 
+TiledArgs tiled_args(TiledState *t, int parity, const float *e, const float *b, float *j,
+                     double *d_ene, int *d_status)
+{
+    TiledArgs a = base_args(t);
+    a.e = e;
+    a.b = b;
+    a.j = j;
+    a.spec = t->d_tab[parity];
+    a.nspec = (int)t->rqm.size();
+    a.ene = d_ene;
+    a.status = d_status;
+    a.reduce_min = t->reduce_min;
+    return a;
+}
+
+FoldBox tiled_fold_box(TiledState *t, float *j)
+{
+    const GridDesc &g = t->g;
+    FoldBox f;
+    f.th = t->tile_hi;
+    f.tl = t->tile_lo;
+    f.j = j;
+    f.size = make_int3(g.size[0], g.size[1], g.size[2]);
+    f.T = make_int3(t->T[0], t->T[1], t->T[2]);
+    f.ntile = make_int3(t->ntile[0], t->ntile[1], t->ntile[2]);
+    f.je = make_int3(t->T[0] + t->order + 2, t->T[1] + t->order + 2, t->T[2] + t->order + 2);
+    f.gcl = make_int3(g.gcl[0], g.gcl[1], g.gcl[2]);
+    f.ofs = t->order == 1 ? 1 : (t->order == 4 ? 3 : 2);
+    f.npts = 3 * g.npoints();
+    return f;
+}
+
+IntRange tiled_arrival_counters(TiledState *t, int parity)
+{
+    IntRange r;
+    r.p = t->d_arr[1 - parity];
+    r.n = (long)MAX_TILED_SPECIES * t->ntiles;
+    return r;
+}
+
+long tiled_ntiles(const TiledState *t) { return t->ntiles; }
+size_t tiled_smem(const TiledState *t) { return t->smem_bytes; }
+int tiled_threads(const TiledState *t) { return t->threads; }
+
+__global__ void k_zero_ranges(const IntRange *__restrict__ r)
+{
+    const IntRange q = r[blockIdx.y];
+    OSG_GRID_LOOP(i, q.n) q.p[i] = 0;
+}
+
+static unsigned grid_x(long n)
+{
+    long b = (n + 255) / 256;
+    return (unsigned)(b < 1 ? 1 : (b > 1024 ? 1024 : b));
+}
+
+void zero_ranges(const IntRange *d_ranges, int nrange, long max_n, cudaStream_t st)
+{
+    k_zero_ranges<<<dim3(grid_x(max_n), (unsigned)nrange), 256, 0, st>>>(d_ranges);
+}
+
+void batch_fold(const FoldBox *d_boxes, int nbox, int dim, long max_points, cudaStream_t st)
+{
+    const dim3 grid(grid_x(max_points), (unsigned)nbox);
+    if (dim == 2) k_batch_fold<2><<<grid, 256, 0, st>>>(d_boxes);
+    else k_batch_fold<3><<<grid, 256, 0, st>>>(d_boxes);
+}
+
+int tiled_set_threads(TiledState *t, int threads)
+{
+    OSG_CHECK(threads >= 64 && threads <= 256 && threads % 32 == 0, OSG_ERR_ARG,
+              "push CTA size must be a multiple of 32 in [64, 256]");
+    t->threads = threads;
+    t->smem_bytes = smem_for(t->dim, t->order, t->T, t->threads);
+    const cudaError_t ce = t->pusher == OSG_PUSHER_EXACT
+                               ? push_tiled_attr_exact(t->dim, t->order, (int)t->smem_bytes)
+                               : push_tiled_attr_boris(t->dim, t->order, (int)t->smem_bytes);
+    OSG_CHECK(ce == cudaSuccess, OSG_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(ce));
+    return OSG_OK;
+}
+
 int tiled_push(TiledState *t, int parity, const float *e, const float *b, float *j,
                double *d_ene, int *d_status, cudaStream_t st, int *launches)
 {
@@ -404,15 +485,7 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     if (ns == 0) return OSG_OK;
     // the push writes every tile's sorted count and adds arrivals to zeroed counters
     OSG_CUDA(cudaMemsetAsync(t->d_arr[1 - parity], 0, sizeof(int) * MAX_TILED_SPECIES * t->ntiles, st));
-    TiledArgs a = base_args(t);
-    a.e = e;
-    a.b = b;
-    a.j = j;
-    a.spec = t->d_tab[parity];
-    a.nspec = ns;
-    a.ene = d_ene;
-    a.status = d_status;
-    a.reduce_min = t->reduce_min;
+    const TiledArgs a = tiled_args(t, parity, e, b, j, d_ene, d_status);
     const size_t sm = t->smem_bytes;
     const int rc = t->pusher == OSG_PUSHER_EXACT
                        ? push_tiled_launch_exact(t->dim, t->order, a, (unsigned)t->ntiles,
@@ -421,23 +494,15 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
                                                  t->threads, sm, st);
     if (rc) return rc;
     // deterministic FP64 re-summation of the tile currents into the global current
-    const GridDesc &g = t->g;
-    const long npts = 3 * g.npoints();
-    const int3 size = make_int3(g.size[0], g.size[1], g.size[2]);
-    const int3 T = make_int3(t->T[0], t->T[1], t->T[2]);
-    const int3 nt = make_int3(t->ntile[0], t->ntile[1], t->ntile[2]);
-    const int3 je = make_int3(t->T[0] + t->order + 2, t->T[1] + t->order + 2,
-                              t->T[2] + t->order + 2);
-    const int3 gcl = make_int3(g.gcl[0], g.gcl[1], g.gcl[2]);
-    const int ofs = t->order == 1 ? 1 : (t->order == 4 ? 3 : 2);
-    unsigned nb = blocks_for(npts, 256);
+    const FoldBox f = tiled_fold_box(t, j);
+    unsigned nb = blocks_for(f.npts, 256);
     if (nb > 152 * 16) nb = 152 * 16;
     if (t->dim == 2)
-        k_tile_fold<2><<<nb, 256, 0, st>>>(t->tile_hi, t->tile_lo, j, size, T, nt, je, gcl, ofs,
-                                            npts);
+        k_tile_fold<2><<<nb, 256, 0, st>>>(f.th, f.tl, j, f.size, f.T, f.ntile, f.je, f.gcl,
+                                            f.ofs, f.npts);
     else
-        k_tile_fold<3><<<nb, 256, 0, st>>>(t->tile_hi, nullptr, j, size, T, nt, je, gcl, ofs,
-                                            npts);
+        k_tile_fold<3><<<nb, 256, 0, st>>>(f.th, f.tl, j, f.size, f.T, f.ntile, f.je, f.gcl,
+                                            f.ofs, f.npts);
     *launches += 2;
     return OSG_OK;
 }

@@ -28,4 +28,18 @@ int tiled_occupancy(TiledState *t, int cur, double *max_frac, cudaStream_t st);
 // re-bin all species into larger slabs (host round trip); keeps buffer `cur` current
 int tiled_regrow(TiledState *t, int cur, cudaStream_t st);
 
+// pieces of tiled_push for the batched engine (many boxes per launch)
+struct TiledArgs;
+struct FoldBox;
+struct IntRange;
+TiledArgs tiled_args(TiledState *t, int parity, const float *e, const float *b, float *j,
+                     double *d_ene, int *d_status);
+FoldBox tiled_fold_box(TiledState *t, float *j);
+IntRange tiled_arrival_counters(TiledState *t, int parity);
+long tiled_ntiles(const TiledState *t);
+size_t tiled_smem(const TiledState *t);
+int tiled_threads(const TiledState *t);
+// threads per push CTA (multiple of 32, 64..256); call before any step
+int tiled_set_threads(TiledState *t, int threads);
+
 } // namespace osg

@@ -124,14 +124,15 @@ __device__ __forceinline__ void emigrate(const SpeciesDev &sd, long cap, long de
 template <int DIM, int ORD>
 constexpr int push_min_blocks() { return DIM == 2 ? (ORD <= 2 ? 3 : (ORD == 3 ? 2 : 1)) : 2; }
 
+// The whole push of one tile by the calling CTA (all threads; contains block barriers; a CTA
+// that pushes several tiles in a row puts a block barrier between the calls).
 template <int DIM, int ORD, int PUSHER>
-__global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>()) k_push_tiled(TiledArgs a)
+__device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
 {
     constexpr int NP = ORD + 1, OFS = Stencil<ORD>::OFS;
     constexpr int MAXSEG = DIM == 2 ? 3 : 4;
     constexpr bool PRIV = private_current<DIM>();
     extern __shared__ float smem[];
-    const long tile = blockIdx.x;
     int t0[3], tc[3];
     tc[0] = (int)(tile % a.ntile[0]);
     tc[1] = DIM > 1 ? (int)((tile / a.ntile[0]) % a.ntile[1]) : 0;
@@ -458,14 +459,52 @@ __global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>()) k_push_tiled
     }
 }
 
+template <int DIM, int ORD, int PUSHER>
+__global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>()) k_push_tiled(TiledArgs a)
+{
+    push_tile<DIM, ORD, PUSHER>(a, blockIdx.x);
+}
+
+// Persistent push over many independent boxes in one launch: every CTA takes (box, tile)
+// items from a work list (heaviest tiles first) through an atomic counter until the list is
+// exhausted; the box's launch arguments are staged in shared memory per item.
+template <int DIM, int ORD, int PUSHER>
+__global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>())
+k_push_tiled_batch(const TiledArgs *__restrict__ boxes, const int2 *__restrict__ work, int nwork,
+                   int *counter)
+{
+    __shared__ TiledArgs sA;
+    __shared__ int sItem;
+    for (;;) {
+        if (threadIdx.x == 0) sItem = atomicAdd(counter, 1);
+        __syncthreads();
+        const int it = sItem;
+        if (it >= nwork) break;
+        const int2 w = work[it];
+        if (threadIdx.x == 0) sA = boxes[w.x];
+        __syncthreads();
+        push_tile<DIM, ORD, PUSHER>(sA, w.y);
+        __syncthreads();
+    }
+}
+
 // Deterministic current flush: every point of the global current (guard cells included) is
 // the FP64 sum, in increasing tile order, of the tile currents (hi + lo) whose halo covers it,
 // rounded once to float.  A tile with origin cell t0 = tc * T + 1 covers the global positions
 // [tc * T - OFS + gcl, tc * T - OFS + gcl + je) along each axis (je = T + ORD + 2 points).
+struct FoldBox {
+    const float *th, *tl;   // tile currents (tl: compensation, or null)
+    float *j;               // global current
+    int3 size, T, ntile, je, gcl;
+    int ofs;
+    long npts;              // 3 x grid points
+};
+
 template <int DIM>
-__global__ void k_tile_fold(const float *__restrict__ th, const float *__restrict__ tl,
-                            float *__restrict__ j, int3 size, int3 T, int3 ntile, int3 je,
-                            int3 gcl, int ofs, long npts)
+__device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
+                                               const float *__restrict__ tl,
+                                               float *__restrict__ j, int3 size, int3 T,
+                                               int3 ntile, int3 je, int3 gcl, int ofs, long npts)
 {
     OSG_GRID_LOOP(g, npts)
     {
@@ -507,6 +546,33 @@ __global__ void k_tile_fold(const float *__restrict__ th, const float *__restric
     }
 }
 
+template <int DIM>
+__global__ void k_tile_fold(const float *__restrict__ th, const float *__restrict__ tl,
+                            float *__restrict__ j, int3 size, int3 T, int3 ntile, int3 je,
+                            int3 gcl, int ofs, long npts)
+{
+    tile_fold_body<DIM>(th, tl, j, size, T, ntile, je, gcl, ofs, npts);
+}
+
+// the same for every box of a batch (box = blockIdx.y)
+template <int DIM>
+__global__ void k_batch_fold(const FoldBox *__restrict__ boxes)
+{
+    const FoldBox &f = boxes[blockIdx.y];
+    tile_fold_body<DIM>(f.th, f.tl, f.j, f.size, f.T, f.ntile, f.je, f.gcl, f.ofs, f.npts);
+}
+
+// zero n ints at p for every range of a device table (one launch; defined in tiled.cu)
+struct IntRange {
+    int *p;
+    long n;
+};
+void zero_ranges(const IntRange *d_ranges, int nrange, long max_n, cudaStream_t st);
+// batched fold of the tile currents of every box (defined in tiled.cu)
+void batch_fold(const FoldBox *d_boxes, int nbox, int dim, long max_points, cudaStream_t st);
+// CTAs of the batched push resident per SM (defined in batch_push.cu)
+int push_batch_occupancy(int dim, int order, int threads, size_t smem);
+
 // Launch of the push kernel of one (dim, order) for each pusher, and the opt-in to its dynamic
 // shared memory (call outside stream capture).  tiled.cu defines the Boris pair, tiled_exact.cu
 // the exact-pusher pair.
@@ -516,6 +582,11 @@ cudaError_t push_tiled_attr_boris(int dim, int order, int bytes);
 int push_tiled_launch_exact(int dim, int order, const TiledArgs &a, unsigned ntiles,
                             int threads, size_t smem, cudaStream_t st);
 cudaError_t push_tiled_attr_exact(int dim, int order, int bytes);
+// persistent launch over a (box, tile) work list (k_push_tiled_batch, Boris pusher; defined
+// in batch_push.cu)
+int push_batch_launch(int dim, int order, const TiledArgs *boxes, const int2 *work, int nwork,
+                      int *counter, unsigned grid, int threads, size_t smem, cudaStream_t st);
+cudaError_t push_batch_attr(int dim, int order, int bytes);
 
 #define OSG_DEFINE_PUSH_TILED(P, LAUNCH, ATTR)                                                \
     int LAUNCH(int dim, int order, const TiledArgs &a, unsigned ntiles, int threads,          \
@@ -530,6 +601,20 @@ cudaError_t push_tiled_attr_exact(int dim, int order, int bytes);
         OSG_PUSH_TILED_CASES(P, OSG_PUSH_TILED_ATTR)                                          \
         return cudaErrorInvalidValue;                                                         \
     }
+#define OSG_DEFINE_PUSH_BATCH(P)                                                              \
+    int push_batch_launch(int dim, int order, const TiledArgs *boxes, const int2 *work,       \
+                          int nwork, int *counter, unsigned grid, int threads, size_t smem,   \
+                          cudaStream_t st)                                                    \
+    {                                                                                         \
+        OSG_PUSH_TILED_CASES(P, OSG_PUSH_BATCH_LAUNCH)                                        \
+        set_error("batched engine: unsupported dim %d order %d", dim, order);                \
+        return OSG_ERR_ARG;                                                                   \
+    }                                                                                         \
+    cudaError_t push_batch_attr(int dim, int order, int bytes)                                \
+    {                                                                                         \
+        OSG_PUSH_TILED_CASES(P, OSG_PUSH_BATCH_ATTR)                                          \
+        return cudaErrorInvalidValue;                                                         \
+    }
 #define OSG_PUSH_TILED_LAUNCH(D, O, P)                                                        \
     if (dim == D && order == O) {                                                             \
         k_push_tiled<D, O, P><<<ntiles, threads, smem, st>>>(a);                              \
@@ -539,6 +624,15 @@ cudaError_t push_tiled_attr_exact(int dim, int order, int bytes);
     if (dim == D && order == O)                                                               \
         return cudaFuncSetAttribute(k_push_tiled<D, O, P>,                                    \
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+#define OSG_PUSH_BATCH_ATTR(D, O, P)                                                          \
+    if (dim == D && order == O)                                                               \
+        return cudaFuncSetAttribute(k_push_tiled_batch<D, O, P>,                              \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+#define OSG_PUSH_BATCH_LAUNCH(D, O, P)                                                        \
+    if (dim == D && order == O) {                                                             \
+        k_push_tiled_batch<D, O, P><<<grid, threads, smem, st>>>(boxes, work, nwork, counter); \
+        return OSG_OK;                                                                        \
+    }
 #define OSG_PUSH_TILED_CASES(P, X)                                                            \
     X(2, 1, P) X(2, 2, P) X(2, 3, P) X(2, 4, P) X(3, 1, P) X(3, 2, P) X(3, 3, P) X(3, 4, P)
 

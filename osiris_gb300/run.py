@@ -7,6 +7,10 @@ neutralising background):
   thermal     2D 128x128, 16 ppc, uth 0.1, quadratic, dx 0.05, dt 0.035          (FP64 plain)
   two_stream  2D 512x512, 2 x 32 ppc, +-0.2 c drift, uth 0.01, 1e-3 perturbation  (FP32 tiled)
   weibel      3D 128^3, 2 x 8 ppc, +-0.5 c along z, uth 0.05, cubic, dx 0.1, dt 0.05
+  batch       64 independent 2D thermal boxes in one batched engine: sizes drawn from
+              {64^2, 128^2, 256^2, 512^2}, ppc from {4, 16, 64}, uth uniform in [0.01, 0.2]
+              (MT19937 seed 4), quadratic, dx 0.05, dt 0.035, tile shape and CTA size
+              autotuned (--boxes N takes the first N boxes)
 Prints one JSON line per run with the device time per step and the energies.
 """
 from __future__ import annotations
@@ -52,9 +56,57 @@ def build_sim(cfg, engine=None, precision=None, tile=None, nx=None):
     return sim, n
 
 
+def batch_boxes(nbox=64, seed=4):
+    """The 64 box specifications of the batched workload: (nx, ppc per axis, uth)."""
+    r = np.random.RandomState(seed)
+    sizes = [64, 128, 256, 512]
+    ppcs = {4: [2, 2], 16: [4, 4], 64: [8, 8]}
+    out = []
+    for _ in range(nbox):
+        n = sizes[r.randint(len(sizes))]
+        ppc = [4, 16, 64][r.randint(3)]
+        uth = float(r.uniform(0.01, 0.2))
+        out.append(([n, n], ppcs[ppc], uth))
+    return out
+
+
+def build_batch(nbox=64, tile=None, threads=0):
+    """The batched thermal workload (one electron species per box over a fixed ion
+    background), seeded OSIRIS lattice load per box."""
+    bt = osg.Batch(2, 2, 0.035, tile=tile, threads=threads)
+    n = 0
+    for i, (nx, ppc, uth) in enumerate(batch_boxes()[:nbox]):
+        k = bt.add_box(nx, [0.05, 0.05])
+        r = osg.Rng(1000 + i)
+        ix, x, u, q = osg.load_lattice(r, 32, nx, ppc, [0.05, 0.05], -1.0, [uth] * 3,
+                                       [0.0, 0.0, 0.0])
+        bt.add_species(k, -1.0, ix, x, u, q)
+        n += len(q)
+    return bt, n
+
+
+def run_batch(args):
+    t0 = time.time()
+    bt, npart = build_batch(args.boxes, args.tile, args.threads or 0)
+    t_load = time.time() - t0
+    t0 = time.time()
+    tile, threads = bt.tuning()
+    t_tune = time.time() - t0
+    bt.step(args.warmup)
+    ms = bt.time_steps(args.steps)
+    print(json.dumps(dict(config="batch", boxes=args.boxes, particles=npart, steps=args.steps,
+                          ms_per_step=ms / args.steps,
+                          particle_steps_per_s=npart * args.steps / (ms / 1e3),
+                          launches_per_step=bt.launches_per_step(), tile=tile,
+                          threads=threads, load_s=t_load, tune_s=t_tune)))
+    bt.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--config", default="two_stream", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="two_stream", choices=sorted(CONFIGS) + ["batch"])
+    ap.add_argument("--boxes", type=int, default=64)
+    ap.add_argument("--threads", type=int)
     ap.add_argument("--nx", type=int, nargs="+")
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -62,6 +114,9 @@ def main():
     ap.add_argument("--precision", type=int, choices=[32, 64])
     ap.add_argument("--tile", type=int, nargs="+")
     args = ap.parse_args()
+    if args.config == "batch":
+        run_batch(args)
+        return
     cfg = CONFIGS[args.config]
     t0 = time.time()
     sim, npart = build_sim(cfg, args.engine, args.precision, args.tile, args.nx)
