@@ -174,6 +174,28 @@ long osg_load_lattice(void *rng, int precision, int dim, const int *nx, const in
                       const double *dx, double rqm, const double *uth, const double *ufl,
                       double amp, double kmode, int *ix, void *x, void *u, void *q);
 
+/* ---------------------------------------------------------------- laser launch --------- */
+
+/* A forward-propagating Gaussian laser pulse at t = 0: gaussian longitudinal envelope
+ * exp(-2 ((x1 - lon_x0) / lon_duration)^2) cut at |x1 - lon_x0| <= lon_range / 2, Hermite-
+ * Gaussian TEM00 transverse profile of waist per_w0 focused at x1 = per_focus around
+ * per_center (x2[, x3]), peak field omega0 * a0, polarisation angle pol from x2 (zpulse with
+ * lon_type = "gaussian", per_type = "gaussian", source/zpulse/os-zpulse-std.f03). */
+typedef struct {
+    double omega0, a0, pol;
+    double lon_x0, lon_duration, lon_range;
+    double per_w0, per_focus;
+    double per_center[2];
+} osg_zpulse;
+
+/* Add the pulse to host field arrays (reference layout with guard cells; float for precision
+ * 32, double for 64) of a box whose lower corner is xmin (launch_zpulse_2d/3d,
+ * source/zpulse/os-zpulse-std.f03:1072-1390: in 2D the E/B components are set, in 3D added).
+ * Host code only. */
+int osg_zpulse_launch(int precision, int dim, int order, const int *nx, const int *gcl,
+                      const int *gcu, const double *dx, const double *xmin, const osg_zpulse *zp,
+                      void *e, void *b);
+
 /* ---------------------------------------------------------------- device-resident sim --- */
 
 typedef struct osg_sim osg_sim;
@@ -226,6 +248,20 @@ int osg_sim_gauss_residual(osg_sim *s, double *max_abs, double *l2);
 /* Average device time per launch of each phase over the last profiled steps (ms):
  * [0] push+deposit, [1] current fold, [2] Yee, [3] guard replace, [4] migration/sort. */
 int osg_sim_profile(osg_sim *s, int nsteps, float *ms_phase);
+/* Moving window along x1 at the speed of light (TILED engine; call before the first step):
+ * every time the window has advanced one cell (the reference's move_boundary_space_global,
+ * source/os-space.f90:508-566) the fields shift one cell towards lower x1 with the new plane
+ * zeroed (move_window_vdf, source/vdf/os-vdf.f03:56-205), all cell indices shift by one and
+ * particles leaving at x1 < 1 are dropped (move_window_species, source/spec/os-species.f03:
+ * 171-229), and species `species` receives cold particles in the new x1 plane, ppc[d] per
+ * cell on the OSIRIS lattice with the density of the piecewise-linear profile (nprof <= 8
+ * points prof_x (global x1, increasing), prof_f; 0 outside) at the particle position
+ * (inject_std, source/spec/psource/os-psource-std.f03:759-1120, :23).  x1 becomes an open
+ * boundary: field guard cells zero, current beyond the edges dropped; x2 (x3) stay periodic. */
+int osg_sim_set_window(osg_sim *s, int species, const int *ppc, int nprof, const double *prof_x,
+                       const double *prof_f);
+/* cell moves of the window so far */
+int osg_sim_window_moves(osg_sim *s, long *moves);
 /* Number of kernel launches one step issues (for launch accounting). */
 int osg_sim_launches_per_step(osg_sim *s);
 /* Run n steps bracketed by CUDA events on the simulation's stream; *ms = device time. */

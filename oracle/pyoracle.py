@@ -330,3 +330,70 @@ def aligned_copy(a, align=64):
     out = aligned(a.shape, a.dtype, align)
     out[...] = a
     return out
+
+
+# ------------------------------------------------------------------------ laser launch
+
+def zpulse(dim, order, nx, dx, xmin, prec, omega0, a0, pol, lon_x0, lon_duration, lon_range,
+           per_w0, per_focus, per_center):
+    """Numpy restatement of the zpulse launch at t = 0 (forward, gaussian longitudinal,
+    Hermite-Gaussian TEM00 transverse; source/zpulse/os-zpulse-std.f03: launch_zpulse_2d
+    :1072-1212, launch_zpulse_3d :1218-1390, lon_envelope :2480-2561, per_envelope_2d/3d
+    :2599-3049).  Returns (e, b) on a zeroed grid with guard cells."""
+    gl, gu = GUARD[order]
+    size = [n + gl + gu for n in nx]
+    dt_ = dtype_of(prec)
+    half = order in (2, 4)
+    idx = [np.arange(sz) - gl + 1 for sz in size]      # Fortran cell index incl. guards
+    base = [xmin[d] + (dx[d] / 2 if half else 0.0) for d in range(dim)]
+    amp = omega0 * a0
+    k = omega0
+
+    def lon(z):
+        s_ = (z - lon_x0) / lon_duration
+        return np.where(np.abs(z - lon_x0) > lon_range / 2, 0.0, np.exp(-2 * (s_ * s_)))
+
+    def per(x1, x2, x3):
+        ox = x2 - per_center[0]
+        rho2 = ox * ox if dim == 2 else ox * ox + (x3 - per_center[1]) ** 2
+        z = x1 - per_focus
+        z0 = k * per_w0 ** 2 / 2
+        nz = z != 0
+        rwl2 = np.where(nz, z0 ** 2 / (z0 ** 2 + z ** 2), 1.0)
+        curv = np.where(nz, 0.5 * rho2 * z / (z ** 2 + z0 ** 2), 0.0)
+        gouy = np.where(nz, np.arctan2(z, z0), 0.0)
+        a = np.sqrt(rwl2) if dim == 3 else np.sqrt(np.sqrt(rwl2))
+        return a * np.exp(-rho2 * rwl2 / per_w0 ** 2) * np.cos(k * (x1 - lon_x0) + k * curv - gouy)
+
+    z = base[0] + (idx[0] - 1) * dx[0]
+    r1 = base[1] + (idx[1] - 1) * dx[1]
+    z2, r12 = z + dx[0] / 2, r1 + dx[1] / 2
+    cp, sp = np.cos(pol), np.sin(pol)
+    shape = tuple(reversed(size)) + (3,)
+    e = np.zeros(shape, dt_)
+    b = np.zeros(shape, dt_)
+    if dim == 2:
+        Z, R = np.meshgrid(z, r1, indexing="xy")
+        Z2, R2 = np.meshgrid(z2, r12, indexing="xy")
+        le, le2 = amp * lon(Z), amp * lon(Z2)
+        b[..., 1] = (-le2 * per(Z2, R, 0) * sp).astype(dt_)
+        b[..., 2] = (le2 * per(Z2, R2, 0) * cp).astype(dt_)
+        e[..., 1] = (le * per(Z, R2, 0) * cp).astype(dt_)
+        e[..., 2] = (le * per(Z, R, 0) * sp).astype(dt_)
+    else:
+        r2 = base[2] + (idx[2] - 1) * dx[2]
+        r22 = r2 + dx[2] / 2
+
+        def grid(a1, a2, a3):
+            A3, A2, A1 = np.meshgrid(a3, a2, a1, indexing="ij")
+            return A1, A2, A3
+
+        X1, X2, X3 = grid(z2, r1, r22)
+        b[..., 1] = b[..., 1] - (amp * lon(X1) * per(X1, X2, X3) * sp).astype(dt_)
+        X1, X2, X3 = grid(z2, r12, r2)
+        b[..., 2] = b[..., 2] + (amp * lon(X1) * per(X1, X2, X3) * cp).astype(dt_)
+        X1, X2, X3 = grid(z, r12, r2)
+        e[..., 1] = e[..., 1] + (amp * lon(X1) * per(X1, X2, X3) * cp).astype(dt_)
+        X1, X2, X3 = grid(z, r1, r22)
+        e[..., 2] = e[..., 2] + (amp * lon(X1) * per(X1, X2, X3) * sp).astype(dt_)
+    return e, b

@@ -116,7 +116,15 @@ class BatchConfig(C.Structure):
                 ("capacity", D)]
 
 
+class Zpulse(C.Structure):
+    _fields_ = [("omega0", D), ("a0", D), ("pol", D), ("lon_x0", D), ("lon_duration", D),
+                ("lon_range", D), ("per_w0", D), ("per_focus", D), ("per_center", D * 2)]
+
+
 def _declare_batch(lb):
+    lb.osg_zpulse_launch.argtypes = [I, I, I, P, P, P, P, P, P, P, P]
+    lb.osg_sim_set_window.argtypes = [P, I, P, I, P, P]
+    lb.osg_sim_window_moves.argtypes = [P, P]
     lb.osg_batch_create.argtypes = [P, P]
     lb.osg_batch_destroy.argtypes = [P]
     lb.osg_batch_add_box.argtypes = [P, P, P]
@@ -290,6 +298,23 @@ def load_lattice(rng, precision, nx, ppc, dx, rqm, uth, ufl, amp=0.0, kmode=1.0)
     return ix, x, u, q
 
 
+def zpulse_launch(order, nx, dx, xmin, e, b, omega0=1.0, a0=1.0, pol=0.0, lon_x0=0.0,
+                  lon_duration=1.0, lon_range=1.0, per_w0=1.0, per_focus=0.0,
+                  per_center=(0.0, 0.0)):
+    """Add a Gaussian laser pulse (t = 0, forward) to host E/B arrays (osg_zpulse_launch)."""
+    dim = len(nx)
+    prec = 32 if e.dtype == np.float32 else 64
+    gl, gu = GUARD[order]
+    zp = Zpulse(omega0, a0, pol, lon_x0, lon_duration, lon_range, per_w0, per_focus,
+                (D * 2)(*per_center))
+    for a, n in ((e, "e"), (b, "b")):
+        if a.dtype != e.dtype or not a.flags.c_contiguous:
+            raise TypeError(f"{n} must be C-contiguous like e")
+    _check(lib().osg_zpulse_launch(prec, dim, order, _p(_i32(nx)), _p(_i32([gl] * dim)),
+                                   _p(_i32([gu] * dim)), _p(_f64(dx)), _p(_f64(xmin)),
+                                   C.byref(zp), _p(e), _p(b)))
+
+
 # ------------------------------------------------------------------------ simulation
 
 class Simulation:
@@ -395,6 +420,17 @@ class Simulation:
         m, l2 = D(), D()
         _check(lib().osg_sim_gauss_residual(self.h, C.byref(m), C.byref(l2)))
         return m.value, l2.value
+
+    def set_window(self, species, ppc, prof_x, prof_f):
+        """Moving window along x1 at c; `species` receives cold particles (ppc per axis) in
+        the new cells with the piecewise-linear density profile (prof_x, prof_f)."""
+        _check(lib().osg_sim_set_window(self.h, species, _p(_i32(ppc)), len(prof_x),
+                                        _p(_f64(prof_x)), _p(_f64(prof_f))))
+
+    def window_moves(self):
+        n = C.c_long()
+        _check(lib().osg_sim_window_moves(self.h, C.byref(n)))
+        return n.value
 
     def profile(self, n):
         ms = np.zeros(5, np.float32)

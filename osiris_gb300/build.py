@@ -28,7 +28,7 @@ NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC
 
 SOURCES = ["push_plain.cu", "fields.cu", "tiled.cu", "tiled_exact.cu", "batch_push.cu", "batch.cu",
            "sim.cu", "capi.cu", "noalloc.cu",
-           "loader.cpp"]
+           "loader.cpp", "laser.cpp"]
 
 
 def nvcc() -> str:

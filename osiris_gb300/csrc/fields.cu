@@ -171,16 +171,72 @@ __global__ void k_periodic_dir(GridDesc g, int d, int add, T *__restrict__ f, lo
     periodic_body<T>(g, d, add, f, n_lo, n_all);
 }
 
+// Open boundary along axis d (moving window, x1): the guard slabs are zeroed, so fields see no
+// periodic image and current deposited beyond the edge is dropped.
 template <typename T>
-void periodic_update(const GridDesc &g, T *f, int add, cudaStream_t st)
+__global__ void k_open_dir(GridDesc g, int d, T *__restrict__ f, long n_lo, long n_all)
+{
+    OSG_GRID_LOOP(n, n_all)
+    {
+        const bool lower = n < n_lo;
+        const long m = lower ? n : n - n_lo;
+        int lo[3], ext[3];
+        for (int a = 0; a < 3; a++) {
+            if (a >= g.dim) {
+                lo[a] = 1;
+                ext[a] = 1;
+            } else if (a == d) {
+                lo[a] = lower ? 1 - g.gcl[a] : g.nx[a] + 1;
+                ext[a] = lower ? g.gcl[a] : g.gcu[a];
+            } else {
+                lo[a] = 1 - g.gcl[a];
+                ext[a] = g.size[a];
+            }
+        }
+        int i[3];
+        unflat(m, lo, ext, i[0], i[1], i[2]);
+        const long pg = pos(g, i[0], i[1], i[2]);
+#pragma unroll
+        for (int c = 0; c < 3; c++) f[pg + c] = T(0);
+    }
+}
+
+template <typename T>
+void periodic_update(const GridDesc &g, T *f, int add, cudaStream_t st, int open_mask)
 {
     for (int d = 0; d < g.dim; d++) {
         long other = 1;
         for (int a = 0; a < g.dim; a++)
             if (a != d) other *= g.size[a];
         const long n_lo = other * g.gcl[d], n_all = n_lo + other * g.gcu[d];
-        k_periodic_dir<T><<<blocks_for(n_all, 256), 256, 0, st>>>(g, d, add, f, n_lo, n_all);
+        if (open_mask & (1 << d))
+            k_open_dir<T><<<blocks_for(n_all, 256), 256, 0, st>>>(g, d, f, n_lo, n_all);
+        else
+            k_periodic_dir<T><<<blocks_for(n_all, 256), 256, 0, st>>>(g, d, add, f, n_lo, n_all);
     }
+}
+
+// Moving window: every point (guard cells included) takes the value one cell further along x1;
+// the last x1 plane becomes zero (move_window_vdf, source/vdf/os-vdf.f03:56-205).  Out of place.
+template <typename T>
+__global__ void k_shift_x(GridDesc g, const T *__restrict__ in, T *__restrict__ out, long n)
+{
+    OSG_GRID_LOOP(p, n)
+    {
+        const long pt = p / 3;
+        const int i1 = (int)(pt % g.size[0]);
+        out[p] = i1 + 1 < g.size[0] ? in[p + 3] : T(0);
+    }
+}
+
+template <typename T>
+void shift_window_x(const GridDesc &g, T *f, T *tmp, cudaStream_t st)
+{
+    const long n = 3 * g.npoints();
+    unsigned nb = blocks_for(n, 256);
+    if (nb > 152 * 32) nb = 152 * 32;
+    k_shift_x<T><<<nb, 256, 0, st>>>(g, f, tmp, n);
+    cudaMemcpyAsync(f, tmp, sizeof(T) * n, cudaMemcpyDeviceToDevice, st);
 }
 
 // sum over the interior of each component squared, accumulated in double:
@@ -416,8 +472,10 @@ template void yee_advance<float>(const GridDesc &, float *, float *, const float
                                  const double *, double, cudaStream_t);
 template void yee_advance<double>(const GridDesc &, double *, double *, const double *,
                                   const double *, double, cudaStream_t);
-template void periodic_update<float>(const GridDesc &, float *, int, cudaStream_t);
-template void periodic_update<double>(const GridDesc &, double *, int, cudaStream_t);
+template void periodic_update<float>(const GridDesc &, float *, int, cudaStream_t, int);
+template void periodic_update<double>(const GridDesc &, double *, int, cudaStream_t, int);
+template void shift_window_x<float>(const GridDesc &, float *, float *, cudaStream_t);
+template void shift_window_x<double>(const GridDesc &, double *, double *, cudaStream_t);
 template void field_sumsq<float>(const GridDesc &, const float *, double *, cudaStream_t);
 template void field_sumsq<double>(const GridDesc &, const double *, double *, cudaStream_t);
 template int deposit_rho<float>(const GridDesc &, int, const int *, const float *,

@@ -68,8 +68,14 @@ void batch_periodic(const FieldBox *d_boxes, int nbox, int dim, int which, int a
 // B half step, E step, B half step of every box; max_points = the largest box's point count
 void batch_yee(const FieldBox *d_boxes, int nbox, int dim, long max_points, cudaStream_t st);
 
-// add = 1: fold guard cells into their periodic images (current); add = 0: replace
-template <typename T> void periodic_update(const GridDesc &g, T *f, int add, cudaStream_t st);
+// add = 1: fold guard cells into their periodic images (current); add = 0: replace.  Axes set
+// in open_mask (bit d) are open instead: their guard slabs are zeroed.
+template <typename T>
+void periodic_update(const GridDesc &g, T *f, int add, cudaStream_t st, int open_mask = 0);
+
+// moving window: shift all of f one cell towards lower x1, zero the last x1 plane (tmp: a
+// scratch array of the same size)
+template <typename T> void shift_window_x(const GridDesc &g, T *f, T *tmp, cudaStream_t st);
 
 // d_out[0..2] += sum over interior points of component^2 (double)
 template <typename T>

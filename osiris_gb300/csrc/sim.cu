@@ -52,7 +52,12 @@ struct osg_sim {
     size_t sort_buf_bytes = 0;
     // tiled engine
     osg::TiledState *tiled = nullptr;
-    // graphs: [parity][sort]
+    // moving window along x1 (tiled engine)
+    bool window = false;
+    double xmoved = 0.0;         // window motion not yet turned into a cell move
+    long moves = 0;              // cell moves so far
+    void *shift_tmp = nullptr;   // scratch field array for the shift
+    // graphs: [parity][sort (plain) / window move (tiled)]
     cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     bool graphs_dirty = true;
     int launches_per_step = 0;
@@ -219,8 +224,12 @@ struct PhaseEvents {
     cudaEvent_t ev[8];
 };
 
+// with_sort: plain engine, cell sort after the push; shift: tiled engine with a moving
+// window, the step ends with a one-cell window move (move_boundary_space_global,
+// source/os-space.f90:508-566: in the reference the move opens the next step, whose push then
+// sees the moved window; here the push of this step already stores the moved cell indices)
 template <typename T>
-static int enqueue_step(osg_sim *s, int parity, bool with_sort, PhaseEvents *pe)
+static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, PhaseEvents *pe)
 {
     cudaStream_t st = s->st;
     const osg_config &c = s->cfg;
@@ -237,16 +246,17 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, PhaseEvents *pe)
     //  source/spec/os-spec-push.f03:1459-1460)
     const bool exact = c.pusher == OSG_PUSHER_EXACT;
     const double push_dt = (sizeof(T) == 4 && !exact) ? (double)(float)c.dt : c.dt;
+    const int open = s->window ? 1 : 0;   // x1 open while the window moves
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[0], st));
-    periodic_update<T>(s->g, (T *)s->e, 0, st);
-    periodic_update<T>(s->g, (T *)s->b, 0, st);
+    periodic_update<T>(s->g, (T *)s->e, 0, st, open);
+    periodic_update<T>(s->g, (T *)s->b, 0, st, open);
     launches += 2 * c.dim;
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[1], st));
     OSG_CUDA(cudaMemsetAsync(s->j, 0, (size_t)s->esz * 3 * s->g.npoints(), st));
     OSG_CUDA(cudaMemsetAsync(s->d_ene, 0, sizeof(double) * MAX_SPECIES, st));
     if (c.engine == OSG_ENGINE_TILED) {
         int rc = tiled_push(s->tiled, parity, (const float *)s->e, (const float *)s->b,
-                            (float *)s->j, s->d_ene, s->d_status, st, &launches);
+                            (float *)s->j, s->d_ene, s->d_status, st, &launches, shift ? 1 : 0);
         if (rc) return rc;
     } else {
         for (int k = 0; k < ns; k++) {
@@ -273,21 +283,29 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, PhaseEvents *pe)
         }
     }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[3], st));
-    periodic_update<T>(s->g, (T *)s->j, 1, st);
+    periodic_update<T>(s->g, (T *)s->j, 1, st, open);
     launches += c.dim;
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[4], st));
     yee_advance<T>(s->g, (T *)s->e, (T *)s->b, (const T *)s->j, c.dx, c.dt, st);
     launches += 3;
+    if (shift) {
+        shift_window_x<T>(s->g, (T *)s->e, (T *)s->shift_tmp, st);
+        shift_window_x<T>(s->g, (T *)s->b, (T *)s->shift_tmp, st);
+        launches += 2;
+        int rc = tiled_window_inject(s->tiled, parity, s->d_status, st, &launches);
+        if (rc) return rc;
+    }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[5], st));
     OSG_CUDA(cudaGetLastError());
     s->launches_per_step = launches;
     return OSG_OK;
 }
 
-static int enqueue_step_any(osg_sim *s, int parity, bool with_sort, PhaseEvents *pe)
+static int enqueue_step_any(osg_sim *s, int parity, bool with_sort, bool shift,
+                            PhaseEvents *pe)
 {
-    return s->cfg.precision == 32 ? enqueue_step<float>(s, parity, with_sort, pe)
-                                  : enqueue_step<double>(s, parity, with_sort, pe);
+    return s->cfg.precision == 32 ? enqueue_step<float>(s, parity, with_sort, shift, pe)
+                                  : enqueue_step<double>(s, parity, with_sort, shift, pe);
 }
 
 static void drop_graphs(osg_sim *s)
@@ -301,13 +319,15 @@ static void drop_graphs(osg_sim *s)
     s->graphs_dirty = false;
 }
 
+// variant: the plain engine's cell sort or the tiled engine's window move
 static int get_graph(osg_sim *s, int parity, int sort, cudaGraphExec_t *out)
 {
     if (s->graphs_dirty) drop_graphs(s);
     if (!s->gexec[parity][sort]) {
         cudaGraph_t gr;
         OSG_CUDA(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_step_any(s, parity, sort != 0, nullptr);
+        const bool tiled = s->cfg.engine == OSG_ENGINE_TILED;
+        int rc = enqueue_step_any(s, parity, !tiled && sort != 0, tiled && sort != 0, nullptr);
         cudaError_t ce = cudaStreamEndCapture(s->st, &gr);
         if (rc) {
             if (ce == cudaSuccess) cudaGraphDestroy(gr);
@@ -332,6 +352,22 @@ static bool sort_due(const osg_sim *s, long n)
 static void advance_buffers(osg_sim *s)
 {
     if (s->cfg.engine == OSG_ENGINE_TILED) s->cur ^= 1;
+}
+
+// Moving window: does the step about to run end with a cell move?  The reference adds dt to
+// the window motion at the start of every step and moves one cell once it reaches dx
+// (source/os-space.f90:529-550); xmoved here already holds the motion after the current
+// step's start, so the move that opens the next step is decided now.
+static bool window_move_next(osg_sim *s, bool commit)
+{
+    if (!s->window) return false;
+    const double xm = s->xmoved + s->cfg.dt;
+    const bool mv = xm >= s->cfg.dx[0];
+    if (commit) {
+        s->xmoved = mv ? xm - s->cfg.dx[0] : xm;
+        if (mv) s->moves++;
+    }
+    return mv;
 }
 
 static int check_status(osg_sim *s)
@@ -455,6 +491,7 @@ int osg_sim_destroy(osg_sim *s)
     cudaFree(s->e);
     cudaFree(s->b);
     cudaFree(s->j);
+    cudaFree(s->shift_tmp);
     cudaFree(s->d_ene);
     cudaFree(s->d_status);
     cudaFree(s->d_diag);
@@ -585,9 +622,9 @@ int osg_sim_step_async(osg_sim *s, int nsteps)
     OSG_CHECK(!s->np.empty(), OSG_ERR_STATE, "no species");
     for (int i = 0; i < nsteps; i++) {
         const int parity = s->cfg.engine == OSG_ENGINE_TILED ? s->cur : 0;
-        const int sort = sort_due(s, s->step_n) ? 1 : 0;
+        const int variant = (sort_due(s, s->step_n) || window_move_next(s, true)) ? 1 : 0;
         cudaGraphExec_t ge;
-        int rc = get_graph(s, parity, sort, &ge);
+        int rc = get_graph(s, parity, variant, &ge);
         if (rc) return rc;
         OSG_CUDA(cudaGraphLaunch(ge, s->st));
         advance_buffers(s);
@@ -621,6 +658,34 @@ int osg_sim_step(osg_sim *s, int nsteps)
             s->graphs_dirty = true;
         }
     }
+    return OSG_OK;
+}
+
+int osg_sim_set_window(osg_sim *s, int species, const int *ppc, int nprof, const double *prof_x,
+                       const double *prof_f)
+{
+    OSG_CHECK(s, OSG_ERR_ARG, "null sim");
+    OSG_CHECK(s->cfg.engine == OSG_ENGINE_TILED, OSG_ERR_ARG,
+              "the moving window runs on the tiled engine");
+    OSG_CHECK(s->step_n == 0, OSG_ERR_STATE, "set the window before the first step");
+    int rc = tiled_set_window(s->tiled, species, ppc, nprof, prof_x, prof_f);
+    if (rc) return rc;
+    if (!s->shift_tmp) {
+        const size_t bytes = (size_t)s->esz * 3 * s->g.npoints();
+        OSG_CUDA(cudaMalloc(&s->shift_tmp, bytes));
+    }
+    s->window = true;
+    // the reference adds dt to the window motion at the start of step 1 (no move: dt < dx)
+    s->xmoved = s->cfg.dt;
+    s->moves = 0;
+    s->graphs_dirty = true;
+    return OSG_OK;
+}
+
+int osg_sim_window_moves(osg_sim *s, long *moves)
+{
+    OSG_CHECK(s && moves, OSG_ERR_ARG, "bad arguments");
+    *moves = s->moves;
     return OSG_OK;
 }
 
@@ -722,7 +787,8 @@ int osg_sim_profile(osg_sim *s, int nsteps, float *ms_phase)
     for (int it = 0; it < nsteps && !rc; it++) {
         const int parity = s->cfg.engine == OSG_ENGINE_TILED ? s->cur : 0;
         const bool sort = sort_due(s, s->step_n);
-        rc = enqueue_step_any(s, parity, sort, &pe);
+        const bool move = window_move_next(s, true);
+        rc = enqueue_step_any(s, parity, sort, move, &pe);
         if (rc) break;
         advance_buffers(s);
         s->step_n++;

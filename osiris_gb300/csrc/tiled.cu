@@ -66,6 +66,14 @@ struct TiledState {
     double iter_tol = 1.0e-3;
     long nj_tile = 0;    // current points (x3 components) of a tile with its halo
     float *tile_hi = nullptr, *tile_lo = nullptr;
+    // moving window along x1 (open x1 boundary, injection into the new cells)
+    bool window = false;
+    int inj_species = -1;
+    int inj_ppc[3] = {1, 1, 1};
+    int nprof = 0;
+    double prof_x[8] = {0}, prof_f[8] = {0};
+    int *d_moved = nullptr;
+    std::vector<long> min_cap;   // per species: at least this many slots per tile
 };
 
 OSG_DEFINE_PUSH_TILED(OSG_PUSHER_BORIS, push_tiled_launch_boris, push_tiled_attr_boris)
@@ -269,6 +277,7 @@ void tiled_destroy(TiledState *t)
     cudaFree(t->d_compact);
     cudaFree(t->tile_hi);
     cudaFree(t->tile_lo);
+    cudaFree(t->d_moved);
     delete t;
 }
 
@@ -317,6 +326,7 @@ int tiled_add_species(TiledState *t, double rqm, long np, const int *ix, const f
     const int cmax = np > 0 ? *std::max_element(cnt.begin(), cnt.end()) : 0;
     const double mean = (double)np / (double)t->ntiles;
     long cap = (long)std::ceil(std::max(t->capacity * mean, 1.25 * cmax)) + 64;
+    if (k < (int)t->min_cap.size()) cap = std::max(cap, t->min_cap[k]);
     cap = (cap + 31) / 32 * 32;
     // stable counting sort by key -> slab slot of every particle
     std::vector<long> dst(np);
@@ -478,14 +488,95 @@ int tiled_set_threads(TiledState *t, int threads)
     return OSG_OK;
 }
 
+__global__ void k_count_move(int *moved)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) *moved += 1;
+}
+
+int tiled_set_window(TiledState *t, int species, const int *ppc, int nprof,
+                     const double *prof_x, const double *prof_f)
+{
+    OSG_CHECK(species >= 0 && species < (int)t->rqm.size(), OSG_ERR_ARG,
+              "window injection: bad species");
+    OSG_CHECK(nprof >= 1 && nprof <= 8 && prof_x && prof_f && ppc, OSG_ERR_ARG,
+              "window injection: 1..8 profile points");
+    for (int k = 1; k < nprof; k++)
+        OSG_CHECK(prof_x[k] > prof_x[k - 1], OSG_ERR_ARG, "profile points must increase");
+    for (int d = 0; d < t->dim; d++)
+        OSG_CHECK(ppc[d] >= 1 && ppc[d] <= 64, OSG_ERR_ARG, "bad particles per cell");
+    t->window = true;
+    t->inj_species = species;
+    for (int d = 0; d < 3; d++) t->inj_ppc[d] = d < t->dim ? ppc[d] : 1;
+    t->nprof = nprof;
+    for (int k = 0; k < nprof; k++) {
+        t->prof_x[k] = prof_x[k];
+        t->prof_f[k] = prof_f[k];
+    }
+    if (!t->d_moved) {
+        OSG_CUDA(cudaMalloc(&t->d_moved, sizeof(int)));
+        OSG_CUDA(cudaMemset(t->d_moved, 0, sizeof(int)));
+    }
+    // the injected plasma fills whole tiles: make room for 1.5 x a full tile
+    long per_tile = 1, per = 1;
+    for (int d = 0; d < t->dim; d++) {
+        per_tile *= t->T[d];
+        per *= t->inj_ppc[d];
+    }
+    const long need = (long)std::ceil(1.5 * (double)(per_tile * per)) + 64;
+    if ((int)t->min_cap.size() < (int)t->rqm.size()) t->min_cap.resize(t->rqm.size(), 0);
+    t->min_cap[species] = std::max(t->min_cap[species], need);
+    if (t->cap[species] < need) return tiled_regrow(t, 0, 0);
+    return OSG_OK;
+}
+
+// after a step that ended with a window move: count the move and inject the new x1 plane
+// into the buffer the push wrote (1 - parity)
+int tiled_window_inject(TiledState *t, int parity, int *d_status, cudaStream_t st,
+                        int *launches)
+{
+    k_count_move<<<1, 32, 0, st>>>(t->d_moved);
+    const int k = t->inj_species;
+    InjectArgs a;
+    memset(&a, 0, sizeof a);
+    a.out = t->buf[1 - parity][k];
+    a.cap = t->cap[k];
+    a.dim = t->dim;
+    int per = 1;
+    for (int d = 0; d < 3; d++) {
+        a.T[d] = t->T[d];
+        a.ntile[d] = t->ntile[d];
+        a.nx[d] = t->nx[d];
+        a.ppc[d] = t->inj_ppc[d];
+        if (d < t->dim) per *= t->inj_ppc[d];
+    }
+    a.dx1 = t->dx[0];
+    a.charge_unit = (t->rqm[k] < 0 ? -1.0 : 1.0) * (double)(1.0f / (float)per);
+    a.nprof = t->nprof;
+    for (int i = 0; i < t->nprof; i++) {
+        a.prof_x[i] = t->prof_x[i];
+        a.prof_f[i] = t->prof_f[i];
+    }
+    a.moved = t->d_moved;
+    a.status = d_status;
+    const long n = (long)(t->dim > 1 ? t->nx[1] : 1) * (t->dim > 2 ? t->nx[2] : 1) * per;
+    unsigned nb = blocks_for(n, 256);
+    if (nb > 4096) nb = 4096;
+    if (t->dim == 2) k_inject_x<2><<<nb, 256, 0, st>>>(a);
+    else k_inject_x<3><<<nb, 256, 0, st>>>(a);
+    *launches += 2;
+    return OSG_OK;
+}
+
 int tiled_push(TiledState *t, int parity, const float *e, const float *b, float *j,
-               double *d_ene, int *d_status, cudaStream_t st, int *launches)
+               double *d_ene, int *d_status, cudaStream_t st, int *launches, int shift)
 {
     const int ns = (int)t->rqm.size();
     if (ns == 0) return OSG_OK;
     // the push writes every tile's sorted count and adds arrivals to zeroed counters
     OSG_CUDA(cudaMemsetAsync(t->d_arr[1 - parity], 0, sizeof(int) * MAX_TILED_SPECIES * t->ntiles, st));
-    const TiledArgs a = tiled_args(t, parity, e, b, j, d_ene, d_status);
+    TiledArgs a = tiled_args(t, parity, e, b, j, d_ene, d_status);
+    a.open_x = t->window ? 1 : 0;
+    a.shift_x = t->window && shift ? 1 : 0;
     const size_t sm = t->smem_bytes;
     const int rc = t->pusher == OSG_PUSHER_EXACT
                        ? push_tiled_launch_exact(t->dim, t->order, a, (unsigned)t->ntiles,

@@ -15,8 +15,15 @@ int tiled_add_species(TiledState *t, double rqm, long np, const int *ix, const f
                       const float *u, const float *q, cudaStream_t st);
 // one push + deposit + migration pass over all species; parity selects which particle buffer
 // is read (the other one is written)
+// shift = 1: the step ends with a moving-window move (particles stored one cell lower in x1)
 int tiled_push(TiledState *t, int parity, const float *e, const float *b, float *j,
-               double *d_ene, int *d_status, cudaStream_t st, int *launches);
+               double *d_ene, int *d_status, cudaStream_t st, int *launches, int shift = 0);
+// moving window along x1 at c: open x1 boundary for the particles, and injection of cold
+// particles of `species` into the new last x1 plane with a piecewise-linear density profile
+int tiled_set_window(TiledState *t, int species, const int *ppc, int nprof,
+                     const double *prof_x, const double *prof_f);
+int tiled_window_inject(TiledState *t, int parity, int *d_status, cudaStream_t st,
+                        int *launches);
 // `cur` = index (0/1) of the buffer that holds the current particles
 int tiled_count(TiledState *t, int cur, int k, long *np, cudaStream_t st);
 int tiled_get_species(TiledState *t, int cur, int k, int *ix, float *x, float *u, float *q,

@@ -51,6 +51,11 @@ struct TiledArgs {
     // 2D), summed in FP64 in tile order by k_tile_fold
     float *tile_hi;
     float *tile_lo;
+    // moving window along x1: open_x = 1 makes x1 non-periodic; shift_x = 1 (a step that ends
+    // with a window move) stores every particle one cell lower in x1, particles that leave
+    // the box along x1 are dropped
+    int open_x;
+    int shift_x;
 };
 
 static const int MAX_TILED_SPECIES = 16;
@@ -298,11 +303,22 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
 #pragma unroll
                 for (int d = 0; d < DIM; d++) {
                     xo[d] = x1[d] - float(di[d]);
-                    cw[d] = wrapc(c[d] + di[d], a.nx[d]);
-                    dt += mul * ((cw[d] - 1) / a.T[d]);
-                    mul *= a.ntile[d];
+                    cw[d] = (d == 0 && a.open_x) ? c[d] + di[d] - a.shift_x
+                                                 : wrapc(c[d] + di[d], a.nx[d]);
                 }
-                dest = dt;
+                // (open x1: a particle outside [1, nx] has left the window; its current of
+                //  this step is already in the segments)
+                if (a.open_x && (cw[0] < 1 || cw[0] > a.nx[0])) {
+                    sd.in.ix[0][p] = 0;
+                    has = false;
+                } else {
+#pragma unroll
+                    for (int d = 0; d < DIM; d++) {
+                        dt += mul * ((cw[d] - 1) / a.T[d]);
+                        mul *= a.ntile[d];
+                    }
+                    dest = dt;
+                }
             }
             const bool stay = has && dest == tile;
             int lcell = -1;
@@ -345,7 +361,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                     }
                 }
             }
-            return has ? nseg : -1;
+            return nseg > 0 ? nseg : (has ? 0 : -1);
         };
         const int nit = (n + nthr - 1) / nthr;
         auto index = [&](int it) {
@@ -572,6 +588,88 @@ void zero_ranges(const IntRange *d_ranges, int nrange, long max_n, cudaStream_t 
 void batch_fold(const FoldBox *d_boxes, int nbox, int dim, long max_points, cudaStream_t st);
 // CTAs of the batched push resident per SM (defined in batch_push.cu)
 int push_batch_occupancy(int dim, int order, int threads, size_t smem);
+
+// Moving window: cold particles of one species in the new last x1 plane of cells (cells
+// (nx1, j, k)), ppc[d] per cell on the OSIRIS lattice, charge sign(1/ppc, rqm) * den with den
+// the piecewise-linear profile (prof_x, prof_f: n points, linear between them, 0 outside) at
+// the particle's global x1 = (moved + i1 - 0.5 + offset) * dx1, where moved counts the window
+// moves so far (injection of inject_std, source/spec/psource/os-psource-std.f03:759-1120; the
+// piecewise-linear profile :23).  Cells where den <= 0 get no particles.  New particles take
+// arrival slots (from the top) of their tile in the buffer the push just wrote.
+struct InjectArgs {
+    Slabs out;
+    long cap;
+    int T[3], ntile[3], nx[3], ppc[3], dim;
+    double dx1, charge_unit;
+    int nprof;
+    double prof_x[8], prof_f[8];
+    const int *moved;
+    int *status;
+};
+
+__device__ __forceinline__ double profile_pl(const InjectArgs &a, double x)
+{
+    if (a.nprof <= 0 || x < a.prof_x[0] || x > a.prof_x[a.nprof - 1]) return 0.0;
+    for (int k = 1; k < a.nprof; k++)
+        if (x <= a.prof_x[k]) {
+            const double w = (x - a.prof_x[k - 1]) / (a.prof_x[k] - a.prof_x[k - 1]);
+            return a.prof_f[k - 1] + w * (a.prof_f[k] - a.prof_f[k - 1]);
+        }
+    return a.prof_f[a.nprof - 1];
+}
+
+template <int DIM>
+__global__ void k_inject_x(InjectArgs a)
+{
+    const int py = DIM > 1 ? a.ppc[1] : 1, pz = DIM > 2 ? a.ppc[2] : 1;
+    const int per = a.ppc[0] * py * pz;
+    const int ny = DIM > 1 ? a.nx[1] : 1, nz = DIM > 2 ? a.nx[2] : 1;
+    const long n = (long)ny * nz * per;
+    const int moved = *a.moved;
+    OSG_GRID_LOOP(g, n)
+    {
+        const int sub = (int)(g % per);
+        const long cell = g / per;
+        const int cj = 1 + (int)(cell % ny), ck = 1 + (int)(cell / ny);
+        const int sa = sub / (py * pz), sb = (sub / pz) % py, sc = sub % pz;
+        const int sidx[3] = {sa, sb, sc};
+        float off[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const float half = 0.5f / (float)a.ppc[d];
+            off[d] = (float)(2 * (sidx[d] + 1) - 1 - a.ppc[d]) * half;
+        }
+        const double xg = ((double)moved + a.nx[0] - 0.5 + (double)off[0]) * a.dx1;
+        const float den = (float)profile_pl(a, xg);
+        if (!(den > 0.0f)) continue;
+        const int cw[3] = {a.nx[0], cj, ck};
+        long tile = 0, mul = 1;
+#pragma unroll
+        for (int d = 0; d < DIM; d++) {
+            tile += mul * ((cw[d] - 1) / a.T[d]);
+            mul *= a.ntile[d];
+        }
+        const int k = atomicAdd(a.out.arr + tile, 1);
+        const int room = (int)a.cap - min(a.out.cnt[tile], (int)a.cap);
+        if (k >= room) {
+            atomicOr(a.status, OSG_STATUS_OVERFLOW);
+            continue;
+        }
+        const long o = tile * a.cap + a.cap - 1 - k;
+#pragma unroll
+        for (int d = 0; d < DIM; d++) {
+            a.out.ix[d][o] = cw[d];
+            a.out.x[d][o] = off[d];
+        }
+        a.out.u[0][o] = 0.0f;
+        a.out.u[1][o] = 0.0f;
+        a.out.u[2][o] = 0.0f;
+        a.out.q[o] = den * (float)a.charge_unit;
+    }
+}
+
+// count of window moves (device counter read by the injection)
+__global__ void k_count_move(int *moved);
 
 // Launch of the push kernel of one (dim, order) for each pusher, and the opt-in to its dynamic
 // shared memory (call outside stream capture).  tiled.cu defines the Boris pair, tiled_exact.cu

@@ -7,6 +7,11 @@ neutralising background):
   thermal     2D 128x128, 16 ppc, uth 0.1, quadratic, dx 0.05, dt 0.035          (FP64 plain)
   two_stream  2D 512x512, 2 x 32 ppc, +-0.2 c drift, uth 0.01, 1e-3 perturbation  (FP32 tiled)
   weibel      3D 128^3, 2 x 8 ppc, +-0.5 c along z, uth 0.05, cubic, dx 0.1, dt 0.05
+  lwfa        3D laser wakefield with a moving window: 1024 x 128 x 128 cells, dx 0.2,
+              dy = dz = 0.6 c/w0, dt 0.18, 2 ppc electrons at n = 0.01 n_c (w_p = 0.1 w0)
+              after a 50-cell linear ramp starting at x1 = 150, a0 = 2 Gaussian pulse (waist
+              30, duration 10, centred at x1 = 130, focused at the ramp's end), cubic splines,
+              window moving at c (--nx scales the box)
   batch       64 independent 2D thermal boxes in one batched engine: sizes drawn from
               {64^2, 128^2, 256^2, 512^2}, ppc from {4, 16, 64}, uth uniform in [0.01, 0.2]
               (MT19937 seed 4), quadratic, dx 0.05, dt 0.035, tile shape and CTA size
@@ -54,6 +59,40 @@ def build_sim(cfg, engine=None, precision=None, tile=None, nx=None):
         sim.add_species(-1.0, ix, x, u, q)
         n += len(q)
     return sim, n
+
+
+LWFA = dict(nx=[1024, 128, 128], dx=[0.2, 0.6, 0.6], dt=0.18, order=3, ppc=[2, 1, 1],
+            n0=0.01, ramp_start=150.0, ramp_cells=50, a0=2.0, w0=30.0, duration=10.0,
+            x0=130.0)
+
+
+def build_lwfa(nx=None, tile=None):
+    """The laser-wakefield workload: seeded lattice load of the plasma already inside the box
+    (density from the profile), the pulse launched into E/B, the window set."""
+    c = LWFA
+    nx = nx or c["nx"]
+    dx = c["dx"]
+    ramp_end = c["ramp_start"] + c["ramp_cells"] * dx[0]
+    px, pf = [c["ramp_start"], ramp_end, 1e9], [0.0, c["n0"], c["n0"]]
+    sim = osg.Simulation(nx, dx, c["dt"], order=c["order"], precision=32,
+                         engine=osg.ENGINE_TILED, tile=tile or [8, 8, 8])
+    gl, gu = osg.GUARD[c["order"]]
+    shape = tuple(reversed([n + gl + gu for n in nx])) + (3,)
+    e, b = np.zeros(shape, np.float32), np.zeros(shape, np.float32)
+    osg.zpulse_launch(c["order"], nx, dx, [0.0] * 3, e, b, omega0=1.0, a0=c["a0"], pol=0.0,
+                      lon_x0=c["x0"], lon_duration=c["duration"], lon_range=4 * c["duration"],
+                      per_w0=c["w0"], per_focus=ramp_end,
+                      per_center=(nx[1] * dx[1] / 2, nx[2] * dx[2] / 2))
+    sim.set_fields(e, b)
+    ix, x, u, q = osg.load_lattice(osg.Rng(5), 32, nx, c["ppc"], dx, -1.0, [0.0] * 3,
+                                   [0.0] * 3)
+    xg = (ix[:, 0].astype(np.float64) - 0.5 + x[:, 0].astype(np.float64)) * dx[0]
+    den = np.interp(xg, px, pf, left=0.0, right=c["n0"]).astype(np.float32)
+    keep = den > 0
+    sim.add_species(-1.0, np.ascontiguousarray(ix[keep]), np.ascontiguousarray(x[keep]),
+                    np.ascontiguousarray(u[keep]), np.ascontiguousarray(q[keep] * den[keep]))
+    sim.set_window(0, c["ppc"], px, pf)
+    return sim, int(keep.sum())
 
 
 def batch_boxes(nbox=64, seed=4):
@@ -104,7 +143,8 @@ def run_batch(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--config", default="two_stream", choices=sorted(CONFIGS) + ["batch"])
+    ap.add_argument("--config", default="two_stream",
+                    choices=sorted(CONFIGS) + ["batch", "lwfa"])
     ap.add_argument("--boxes", type=int, default=64)
     ap.add_argument("--threads", type=int)
     ap.add_argument("--nx", type=int, nargs="+")
@@ -116,6 +156,21 @@ def main():
     args = ap.parse_args()
     if args.config == "batch":
         run_batch(args)
+        return
+    if args.config == "lwfa":
+        t0 = time.time()
+        sim, n0 = build_lwfa(args.nx, args.tile)
+        t_load = time.time() - t0
+        sim.step(args.warmup)
+        ms = sim.time_steps(args.steps)
+        n1 = sim.num_particles(0)
+        kin, fld = sim.energy()
+        print(json.dumps(dict(config="lwfa", nx=args.nx or LWFA["nx"], particles_start=n0,
+                              particles_end=n1, steps=args.steps, ms_per_step=ms / args.steps,
+                              particle_steps_per_s=n1 * args.steps / (ms / 1e3),
+                              window_moves=sim.window_moves(), load_s=t_load,
+                              kinetic=[float(v) for v in kin], field=[float(v) for v in fld])))
+        sim.close()
         return
     cfg = CONFIGS[args.config]
     t0 = time.time()
