@@ -54,6 +54,14 @@ extern "C" {
 #define OSG_ENGINE_PLAIN 0
 #define OSG_ENGINE_TILED 1
 
+/* current smoothing types (the deck's smooth type, source/vdf/os-vdf-smooth.f90:27-38) */
+#define OSG_SMOOTH_NONE 0
+#define OSG_SMOOTH_BINOMIAL 2
+#define OSG_SMOOTH_COMPENSATED 3
+#define OSG_SMOOTH_5PASS 4
+#define OSG_SMOOTH_TRI6 5
+#define OSG_SMOOTH_TRI8 6
+
 #define OSG_PUSHER_BORIS 0   /* push_type = "simd" / "standard" (Boris) */
 #define OSG_PUSHER_EXACT 1   /* push_type = "exact" (analytic, source/spec/os-spec-extpush.f03) */
 
@@ -154,6 +162,20 @@ int osg_periodic_f32(int dim, const int *nx, const int *gcl, const int *gcu, flo
 int osg_periodic_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f,
                      int add);
 
+/* Current smoothing of a 3-component grid on HOST arrays (smooth_vdf, source/vdf/
+ * os-vdf-smooth.f90:514-540; applied to the current after its guard fold,
+ * source/os-simulation.f03:651-657): along each axis d with type[d] != OSG_SMOOTH_NONE a
+ * (2 n + 1)-point filter over the points at least n from both ends of the array (guard cells
+ * included; the others are kept), axis after axis.  The coefficients are computed and kept in
+ * FP64 (setup_smooth, :373-467) and the sums are taken in FP64.  The array needs gcl >= n and
+ * gcu >= n + 1 guard cells for the filtered interior to be meaningful. */
+int osg_smooth_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f,
+                   const int *type, const int *order);
+int osg_smooth_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f,
+                   const int *type, const int *order);
+/* the normalised FP64 coefficients of one axis: c[0 .. 2 n], *n = the filter's order */
+int osg_smooth_coefficients(int type, int order, double *c, int *n);
+
 /* Periodic particle boundary of a single node on HOST arrays: cell indices that left
  * [1, nx] are shifted by +-nx (replaces the periodic branch of phys_boundary_species,
  * source/spec/os-spec-boundary.f03:1280-1290; host code, no GPU). */
@@ -213,6 +235,8 @@ typedef struct {
     double capacity;  /* TILED: slots per tile as a multiple of the mean load (0 = 3.0) */
     int pusher;       /* OSG_PUSHER_BORIS (0) or OSG_PUSHER_EXACT (1) */
     double iter_tol;  /* exact pusher: Newton tolerance (0 = the reference default 1e-3) */
+    int smooth_type;  /* current smoothing after the guard fold, OSG_SMOOTH_* (all axes) */
+    int smooth_order; /* its order (binomial: passes; compensated: >= 2; others fixed) */
 } osg_config;
 
 int osg_sim_create(const osg_config *cfg, osg_sim **out);
@@ -262,6 +286,8 @@ int osg_sim_set_window(osg_sim *s, int species, const int *ppc, int nprof, const
                        const double *prof_f);
 /* cell moves of the window so far */
 int osg_sim_window_moves(osg_sim *s, long *moves);
+/* guard cells per axis of the sim's grids (order-dependent, widened for smoothing) */
+int osg_sim_guard_cells(osg_sim *s, int *gcl, int *gcu);
 /* Number of kernel launches one step issues (for launch accounting). */
 int osg_sim_launches_per_step(osg_sim *s);
 /* Run n steps bracketed by CUDA events on the simulation's stream; *ms = device time. */

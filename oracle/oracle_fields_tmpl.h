@@ -18,6 +18,7 @@
  *   divergence        source/vdf/os-vdf-math.f90:1013-1073
  *   field energy      source/emf/diagnostics/os-emf-diagnostics.f03:42-58 (0.5*dV*sum f^2)
  *   kinetic energy    source/spec/os-spec-define.f03:1030-1086
+ *   smoothing         source/vdf/os-vdf-smooth.f90:639-1000 (filter_2d / filter_3d)
  */
 
 #define FN(name) PASTE3(name, _, SFX)
@@ -248,4 +249,55 @@ void FN(ora_deposit_rho)(int dim, int order, const int *nx, const int *gcl, cons
 }
 
 #undef AT
+
+/* Separable smoothing in place, filter_2d / filter_3d restated: along axis d (order n = ord[d]
+ * > 0, coefficients s[d][0 .. 2n] in R), every line of the array (all points of the other
+ * axes, guard cells included) is filtered over [lb + n, ub - n] with a sliding window of the
+ * original values: f = o(-n) s(-n); f = f + o(k) s(k), k = -n+1 .. n. */
+void FN(ora_smooth)(int dim, const int *nx, const int *gcl, const int *gcu, R *f, const int *ord,
+                    const R *coef /* [3][31] */)
+{
+    FN(ora_grid) g;
+    FN(grid_init)(&g, dim, nx, gcl, gcu);
+    for (int d = 0; d < dim; d++) {
+        const int n = ord[d];
+        if (n <= 0) continue;
+        const R *s = coef + 31 * d;
+        const long st = d == 0 ? 3 : (d == 1 ? 3L * g.size[0] : 3L * g.size[0] * g.size[1]);
+        const int len = g.size[d];
+        int others[2] = {0, 0}, k = 0;                      /* the other two axes */
+        for (int e = 0; e < 3; e++)
+            if (e != d && k < 2) others[k++] = e;
+        const int n1 = g.size[others[0]], n2 = dim > 2 ? g.size[others[1]] : 1;
+        R o[3][63];
+        for (int a = 0; a < n1; a++)
+            for (int b = 0; b < n2; b++) {
+                int pos[3] = {0, 0, 0};
+                pos[others[0]] = a;
+                if (dim > 2) pos[others[1]] = b;
+                const long base = 3L * (pos[0] + (long)g.size[0] * (pos[1] + (long)g.size[1] * pos[2]));
+                for (int c = 0; c < 3; c++) {
+                    for (int kk = -n; kk < n; kk++) o[c][kk + n] = f[base + c + (n + kk) * st];
+                    for (int i = n; i <= len - 1 - n; i++) {
+                        o[c][2 * n] = f[base + c + (i + n) * st];
+                        R v = o[c][0] * s[0];
+                        for (int kk = 1; kk <= 2 * n; kk++) v = v + o[c][kk] * s[kk];
+                        for (int kk = 0; kk < 2 * n; kk++) o[c][kk] = o[c][kk + 1];
+                        f[base + c + i * st] = v;
+                    }
+                }
+            }
+    }
+}
+
+/* smoothing applied after the current fold by the step below (order 0: none) */
+static int FN(step_smooth_ord)[3] = {0, 0, 0};
+static R FN(step_smooth_coef)[3 * 31];
+void FN(ora_set_smooth)(const int *ord, const R *coef)
+{
+    for (int d = 0; d < 3; d++) FN(step_smooth_ord)[d] = ord ? ord[d] : 0;
+    if (coef)
+        for (int i = 0; i < 3 * 31; i++) FN(step_smooth_coef)[i] = coef[i];
+}
+
 #undef FN

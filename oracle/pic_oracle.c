@@ -477,6 +477,9 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
     }                                                                                         \
     ora_pusher_##SFXN = 0;                                                                    \
     ora_periodic_##SFXN(dim, nx, gcl, gcu, j, 1);                                             \
+    if (step_smooth_ord_##SFXN[0] > 0)                                                       \
+        ora_smooth_##SFXN(dim, nx, gcl, gcu, j, step_smooth_ord_##SFXN,                      \
+                          step_smooth_coef_##SFXN);                                          \
     ora_yee_advance_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt);                               \
     return 0;
 

@@ -57,6 +57,12 @@ void ora_div_f32(int dim, const int *nx, const int *gcl, const int *gcu, const f
 void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const double *f,
                  const double *dx, double *div);
 void ora_spline_weights_f64(int order, double x, double *w);
+void ora_smooth_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f,
+                    const int *ord, const float *coef);
+void ora_smooth_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f,
+                    const int *ord, const double *coef);
+void ora_set_smooth_f32(const int *ord, const float *coef);
+void ora_set_smooth_f64(const int *ord, const double *coef);
 
 void ora_wrap(int dim, const int *nx, int np, int *ix);
 void ora_sort_index(int dim, const int *nx, int np, const int *ix, int *new_idx);

@@ -79,6 +79,9 @@ D = C.c_double
 def _declare(L):
     L.ora_push_f32.argtypes = [I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P, P, D, P]
     L.ora_push_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, P]
+    for s_ in ("f32", "f64"):
+        getattr(L, f"ora_smooth_{s_}").argtypes = [I, P, P, P, P, P, P]
+        getattr(L, f"ora_set_smooth_{s_}").argtypes = [P, P]
     L.ora_push_exact_f32.argtypes = [I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P, P,
                                      D, D, P]
     L.ora_push_exact_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, D, P]
@@ -128,11 +131,11 @@ def dtype_of(prec: str):
 class Grid:
     """Periodic box with the guard cells the interpolation order needs."""
 
-    def __init__(self, nx, order, dx):
+    def __init__(self, nx, order, dx, guard=None):
         self.dim = len(nx)
         self.nx = list(nx)
         self.order = order
-        gl, gu = GUARD[order]
+        gl, gu = guard if guard else GUARD[order]
         self.gcl = [gl] * self.dim
         self.gcu = [gu] * self.dim
         self.size = [n + gl + gu for n in self.nx]
@@ -287,7 +290,7 @@ def load(rng: MT, prec, dim, nx, ppc, dx, rqm, uth, ufl, amp=0.0, kmode=1.0):
 # ------------------------------------------------------------------------------ full step
 
 def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="boris",
-         iter_tol=1e-3):
+         iter_tol=1e-3, smooth=None):
     """One full periodic time step; species = list of dicts with ix, x, u, q, rqm.
     Returns the per-species energy sums (Boris: time-centred u^2/(gamma+1); exact pusher:
     gamma - 1 of the new momentum; both times q).  fast=True runs the -O3 -ffast-math build
@@ -303,12 +306,17 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     rqm = np.asarray([s["rqm"] for s in species], dtype=dtype_of(prec))
     ene = np.zeros(ns)
     L = fast_lib() if fast else lib()
+    if smooth is not None:
+        ordv, coef = _smooth_tables(g.dim, prec, [smooth[0]] * g.dim, [smooth[1]] * g.dim)
+        getattr(L, f"ora_set_smooth_{prec}")(_p(ordv), _p(coef))
     args = (g.dim, g.order, _p(nx), _p(gl), _p(gu), _p(_f64(g.dx + [0.0] * 3)), float(dt), _p(e),
             _p(b), _p(j), ns, _p(np_), ixs, xs, us, qs, _p(rqm), _p(ene), int(nthreads))
     if pusher == "exact":
         getattr(L, f"ora_step_exact_{prec}")(*args, float(iter_tol))
     else:
         getattr(L, f"ora_step_{prec}")(*args)
+    if smooth is not None:
+        getattr(L, f"ora_set_smooth_{prec}")(None, None)
     return ene
 
 
@@ -397,3 +405,76 @@ def zpulse(dim, order, nx, dx, xmin, prec, omega0, a0, pol, lon_x0, lon_duration
         X1, X2, X3 = grid(z, r1, r22)
         e[..., 2] = e[..., 2] + (amp * lon(X1) * per(X1, X2, X3) * sp).astype(dt_)
     return e, b
+
+
+# ------------------------------------------------------------------------ smoothing
+
+SMOOTH = dict(none=0, binomial=2, compensated=3, fivepass=4, tri6=5, tri8=6)
+
+
+def _combine_kernel3(k3, n):
+    """combine_kernel3 (source/vdf/os-vdf-smooth.f90:151-183): n 3-point kernels -> 2n+1."""
+    out = [0.0] * (2 * n + 1)
+    out[n] = 1.0
+    for k in range(n):
+        f1 = 0.0
+        for j in range(n - k, n + k + 2):
+            out[j - 1] = k3[k][2] * out[j] + out[j - 1]
+            f2 = k3[k][0] * out[j]
+            out[j] = k3[k][1] * out[j] + f1
+            f1 = f2
+    return out
+
+
+def smooth_coefficients(stype, order, prec="f64"):
+    """setup_smooth restated (source/vdf/os-vdf-smooth.f90:373-467): the normalised kernel of
+    one axis.  prec "f32" follows the single-precision build (coefficients held in float,
+    normalised with a double total); returns (n, list of 2n+1 floats)."""
+    if stype == 0:
+        return 0, [1.0]
+    if stype == 2:
+        n = order
+        k3 = [(1.0, 2.0, 1.0)] * n
+    elif stype == 3:
+        n = max(2, order)
+        comp = float(np.float32(np.float32(4.0) + np.float32(2.0) * np.float32(n - 1)) /
+                     np.float32(n - 1))
+        k3 = [(1.0, 2.0, 1.0)] * (n - 1) + [(-1.0, comp, -1.0)]
+    elif stype == 4:
+        n = 5
+        k3 = [(1.0, 2.0, 1.0)] * 4 + [(-5.0, 15.0, -5.0)]
+    elif stype == 5:
+        n, c = 3, [0.015625, -0.09375, 0.234375, 0.6875, 0.234375, -0.09375, 0.015625]
+    elif stype == 6:
+        n, c = 4, [-0.00390625, 0.03125, -0.109375, 0.21875, 0.7265625, 0.21875, -0.109375,
+                   0.03125, -0.00390625]
+    else:
+        raise ValueError("unknown smoothing type")
+    if stype in (2, 3, 4):
+        c = _combine_kernel3(k3, n)
+    if prec == "f32":
+        c = [float(np.float32(v)) for v in c]
+    total = 0.0
+    for v in c:
+        total = total + v
+    c = [v / total for v in c]
+    if prec == "f32":
+        c = [float(np.float32(v)) for v in c]
+    return n, c
+
+
+def _smooth_tables(dim, prec, types, orders):
+    ordv = np.zeros(3, np.int32)
+    coef = np.zeros(3 * 31, dtype_of(prec))
+    for d in range(dim):
+        n, c = smooth_coefficients(types[d], orders[d], prec)
+        ordv[d] = n
+        coef[31 * d: 31 * d + len(c)] = c
+    return ordv, coef
+
+
+def smooth(g: Grid, prec, f, types, orders):
+    """filter_2d/3d in place (source/vdf/os-vdf-smooth.f90:639-1000)."""
+    nx, gl, gu = g.args()
+    ordv, coef = _smooth_tables(g.dim, prec, types, orders)
+    getattr(lib(), f"ora_smooth_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), _p(f), _p(ordv), _p(coef))

@@ -32,6 +32,8 @@ ENGINE_PLAIN = 0
 ENGINE_TILED = 1
 PUSHER_BORIS = 0
 PUSHER_EXACT = 1
+SMOOTH_NONE, SMOOTH_BINOMIAL, SMOOTH_COMPENSATED = 0, 2, 3
+SMOOTH_5PASS, SMOOTH_TRI6, SMOOTH_TRI8 = 4, 5, 6
 RNG_BYTES = 2512
 
 # guard cells per interpolation order (source/particles/os-particles.f03:321-360)
@@ -65,7 +67,7 @@ P, I, L, D, F = C.c_void_p, C.c_int, C.c_long, C.c_double, C.c_float
 class Config(C.Structure):
     _fields_ = [("dim", I), ("order", I), ("precision", I), ("engine", I), ("nx", I * 3),
                 ("dx", D * 3), ("dt", D), ("tile", I * 3), ("n_sort", I), ("capacity", D),
-                ("pusher", I), ("iter_tol", D)]
+                ("pusher", I), ("iter_tol", D), ("smooth_type", I), ("smooth_order", I)]
 
 
 def _declare(lb):
@@ -125,6 +127,10 @@ def _declare_batch(lb):
     lb.osg_zpulse_launch.argtypes = [I, I, I, P, P, P, P, P, P, P, P]
     lb.osg_sim_set_window.argtypes = [P, I, P, I, P, P]
     lb.osg_sim_window_moves.argtypes = [P, P]
+    lb.osg_sim_guard_cells.argtypes = [P, P, P]
+    lb.osg_smooth_f32.argtypes = [I, P, P, P, P, P, P]
+    lb.osg_smooth_f64.argtypes = [I, P, P, P, P, P, P]
+    lb.osg_smooth_coefficients.argtypes = [I, I, P, P]
     lb.osg_batch_create.argtypes = [P, P]
     lb.osg_batch_destroy.argtypes = [P]
     lb.osg_batch_add_box.argtypes = [P, P, P]
@@ -315,13 +321,32 @@ def zpulse_launch(order, nx, dx, xmin, e, b, omega0=1.0, a0=1.0, pol=0.0, lon_x0
                                    C.byref(zp), _p(e), _p(b)))
 
 
+def smooth(dim, nx, gcl, gcu, f, types, orders):
+    """Current smoothing of a host grid in place (osg_smooth_*): per axis the type
+    (SMOOTH_*) and order; FP64 coefficients and sums."""
+    prec = _prec(f)
+    if not f.flags.c_contiguous:
+        raise TypeError("f must be C-contiguous")
+    _check(getattr(lib(), f"osg_smooth_{prec}")(dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)),
+                                                _p(f), _p(_i32(types)), _p(_i32(orders))))
+
+
+def smooth_coefficients(stype, order):
+    """The normalised FP64 filter coefficients of one axis (osg_smooth_coefficients)."""
+    c = np.zeros(31)
+    n = C.c_int()
+    _check(lib().osg_smooth_coefficients(int(stype), int(order), _p(c), C.byref(n)))
+    return n.value, c[: 2 * n.value + 1].copy()
+
+
 # ------------------------------------------------------------------------ simulation
 
 class Simulation:
     """Device-resident periodic PIC simulation (fields + species stay on the GPU)."""
 
     def __init__(self, nx, dx, dt, order=2, precision=32, engine=ENGINE_TILED, tile=None,
-                 n_sort=0, capacity=0.0, pusher=PUSHER_BORIS, iter_tol=0.0):
+                 n_sort=0, capacity=0.0, pusher=PUSHER_BORIS, iter_tol=0.0,
+                 smooth_type=SMOOTH_NONE, smooth_order=0):
         self.dim = len(nx)
         self.nx = list(nx)
         self.order = order
@@ -341,11 +366,18 @@ class Simulation:
         cfg.capacity = capacity
         cfg.pusher = pusher
         cfg.iter_tol = iter_tol
+        cfg.smooth_type = smooth_type
+        cfg.smooth_order = smooth_order
         self.cfg = cfg
         self.dx = list(dx)
         self.dt = dt
         self.h = P()
         _check(lib().osg_sim_create(C.byref(cfg), C.byref(self.h)))
+        # guard cells as created (wider than the interpolation needs when smoothing)
+        gcl, gcu = np.zeros(3, np.int32), np.zeros(3, np.int32)
+        _check(lib().osg_sim_guard_cells(self.h, _p(gcl), _p(gcu)))
+        self.gcl, self.gcu = [int(v) for v in gcl[: self.dim]], [int(v) for v in gcu[: self.dim]]
+        self.size = [n + a + b for n, a, b in zip(self.nx, self.gcl, self.gcu)]
         self.nspecies = 0
         self.rqm = []
 

@@ -26,6 +26,14 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "-I", ROOT]
 
+# The tiled (mixed-precision) Boris kernels use the approximate single-precision division and
+# square root (at most 2 ulp): measured 4% faster on the two-stream push, inside the mixed
+# engine's 1e-5 parity.  The drop-in and plain kernels keep IEEE rounding (bit-identical to the
+# reference), and so does the exact pusher: its k^2 = (inv1 + sqrt(inv1^2 + 4 inv2^2)) / 2 needs
+# the correctly rounded square root to stay >= 0 when E.B = 0 and |B| > |E|.
+FAST_DIV = ["-prec-div=false", "-prec-sqrt=false"]
+EXTRA = {"tiled.cu": FAST_DIV, "batch_push.cu": FAST_DIV}
+
 SOURCES = ["push_plain.cu", "fields.cu", "tiled.cu", "tiled_exact.cu", "batch_push.cu", "batch.cu",
            "sim.cu", "capi.cu", "noalloc.cu",
            "loader.cpp", "laser.cpp"]
@@ -51,7 +59,7 @@ def _compile(src: str, verbose: bool) -> str:
         os.path.join(ROOT, "include", "osiris_gb300.h")]
     if _newer(out, deps):
         return out
-    cmd = [nvcc()] + ARCH + NVFLAGS + ["-c", os.path.join(CSRC, src), "-o", out]
+    cmd = [nvcc()] + ARCH + NVFLAGS + EXTRA.get(src, []) + ["-c", os.path.join(CSRC, src), "-o", out]
     if src.endswith(".cpp"):
         cmd = [nvcc(), "-x", "c++"] + NVFLAGS + ["-c", os.path.join(CSRC, src), "-o", out]
     if verbose:

@@ -213,6 +213,41 @@ static int yee_host(int dim, const int *nx, const int *gcl, const int *gcu, T *e
     return OSG_OK;
 }
 
+static int smooth_spec(int dim, const int *type, const int *order, SmoothSpec *sp)
+{
+    memset(sp, 0, sizeof *sp);
+    for (int d = 0; d < dim; d++) {
+        int n = 0;
+        OSG_CHECK(smooth_coefficients(type[d], order[d], sp->c[d], &n) == OSG_OK, OSG_ERR_ARG,
+                  "bad smoothing type %d / order %d", type[d], order[d]);
+        sp->order[d] = n;
+    }
+    return OSG_OK;
+}
+
+template <typename T>
+static int smooth_host(int dim, const int *nx, const int *gcl, const int *gcu, T *f,
+                       const int *type, const int *order)
+{
+    OSG_CHECK(dim >= 1 && dim <= 3 && nx && gcl && gcu && f && type && order, OSG_ERR_ARG,
+              "bad arguments");
+    SmoothSpec sp;
+    int rc = smooth_spec(dim, type, order, &sp);
+    if (rc) return rc;
+    GridDesc g = make_grid(dim, nx, gcl, gcu);
+    const long n = g.npoints() * 3;
+    void *d_f, *d_t;
+    if ((rc = g_stage.get(5, sizeof(T) * n, &d_f))) return rc;
+    if ((rc = g_stage.get(6, sizeof(T) * n, &d_t))) return rc;
+    cudaStream_t st = g_stage.stream;
+    OSG_CUDA(cudaMemcpyAsync(d_f, f, sizeof(T) * n, cudaMemcpyHostToDevice, st));
+    smooth_field<T>(g, sp, (T *)d_f, (T *)d_t, st);
+    OSG_CUDA(cudaGetLastError());
+    OSG_CUDA(cudaMemcpyAsync(f, d_f, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+    OSG_CUDA(cudaStreamSynchronize(st));
+    return OSG_OK;
+}
+
 template <typename T>
 static int periodic_host(int dim, const int *nx, const int *gcl, const int *gcu, T *f, int add)
 {
@@ -389,6 +424,26 @@ int osg_particle_wrap(int dim, const int *nx, long np, int *ix)
         if (p0 < p1) pool.emplace_back(wrap_range, p0, p1);
     }
     for (auto &th : pool) th.join();
+    return OSG_OK;
+}
+
+int osg_smooth_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f,
+                   const int *type, const int *order)
+{
+    return smooth_host<float>(dim, nx, gcl, gcu, f, type, order);
+}
+
+int osg_smooth_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f,
+                   const int *type, const int *order)
+{
+    return smooth_host<double>(dim, nx, gcl, gcu, f, type, order);
+}
+
+int osg_smooth_coefficients(int type, int order, double *c, int *n)
+{
+    OSG_CHECK(c && n, OSG_ERR_ARG, "null argument");
+    OSG_CHECK(smooth_coefficients(type, order, c, n) == OSG_OK, OSG_ERR_ARG,
+              "bad smoothing type %d / order %d", type, order);
     return OSG_OK;
 }
 

@@ -468,12 +468,126 @@ void batch_yee(const FieldBox *d_boxes, int nbox, int dim, long max_points, cuda
     }
 }
 
+
+// ------------------------------------------------------------------------ smoothing
+// n 3-point kernels kern3[k] = {a, b, c} combined into one (2 nmax + 1)-point kernel
+// (combine_kernel3, source/vdf/os-vdf-smooth.f90:151-183)
+static void combine_kernel3(const double (*k3)[3], int n, int nmax, double *out)
+{
+    for (int i = 0; i < 2 * nmax + 1; i++) out[i] = 0.0;
+    out[nmax] = 1.0;
+    for (int k = 0; k < n; k++) {
+        double f1 = 0.0;
+        for (int j = nmax - k; j <= nmax + k + 1; j++) {
+            out[j - 1] = k3[k][2] * out[j] + out[j - 1];
+            const double f2 = k3[k][0] * out[j];
+            out[j] = k3[k][1] * out[j] + f1;
+            f1 = f2;
+        }
+    }
+}
+
+int smooth_coefficients(int type, int order, double *c, int *eff_order)
+{
+    double k3[15][3];
+    int n = 0;
+    switch (type) {
+    case OSG_SMOOTH_NONE:
+        *eff_order = 0;
+        return OSG_OK;
+    case OSG_SMOOTH_BINOMIAL:
+        if (order < 1 || order > 15) return OSG_ERR_ARG;
+        n = order;
+        for (int j = 0; j < n; j++) k3[j][0] = 1.0, k3[j][1] = 2.0, k3[j][2] = 1.0;
+        break;
+    case OSG_SMOOTH_COMPENSATED: {
+        n = order < 2 ? 2 : order;
+        if (n > 15) return OSG_ERR_ARG;
+        for (int j = 0; j < n - 1; j++) k3[j][0] = 1.0, k3[j][1] = 2.0, k3[j][2] = 1.0;
+        // comp = (4.0 + 2.0 * (order - 1)) / (order - 1): default-real literals, so the
+        // reference evaluates it in single precision (:418)
+        const float comp = (4.0f + 2.0f * (float)(n - 1)) / (float)(n - 1);
+        k3[n - 1][0] = -1.0, k3[n - 1][1] = (double)comp, k3[n - 1][2] = -1.0;
+        break;
+    }
+    case OSG_SMOOTH_5PASS:
+        n = 5;
+        for (int j = 0; j < 4; j++) k3[j][0] = 1.0, k3[j][1] = 2.0, k3[j][2] = 1.0;
+        k3[4][0] = -5.0, k3[4][1] = 15.0, k3[4][2] = -5.0;
+        break;
+    case OSG_SMOOTH_TRI6:
+    case OSG_SMOOTH_TRI8:
+        n = type == OSG_SMOOTH_TRI6 ? 3 : 4;
+        break;
+    default:
+        return OSG_ERR_ARG;
+    }
+    if (type == OSG_SMOOTH_TRI6) {
+        const double t[7] = {0.015625, -0.09375, 0.234375, 0.6875, 0.234375, -0.09375, 0.015625};
+        for (int i = 0; i < 7; i++) c[i] = t[i];
+    } else if (type == OSG_SMOOTH_TRI8) {
+        const double t[9] = {-0.00390625, 0.03125, -0.109375, 0.21875, 0.7265625,
+                             0.21875,     -0.109375, 0.03125, -0.00390625};
+        for (int i = 0; i < 9; i++) c[i] = t[i];
+    } else {
+        combine_kernel3(k3, n, n, c);
+    }
+    // normalise (:452-464)
+    double total = 0.0;
+    for (int i = 0; i < 2 * n + 1; i++) total = total + c[i];
+    for (int i = 0; i < 2 * n + 1; i++) c[i] = c[i] / total;
+    *eff_order = n;
+    return OSG_OK;
+}
+
+// one axis of the filter, out of place: points at least n from both ends of the axis (guard
+// cells included) get sum_k c[k] f(i + k - n) summed in double in the reference's order
+// (filter_2d/3d, :639-1000); the others are copied
+template <typename T>
+__global__ void k_smooth_dir(GridDesc g, int axis, int n, const T *__restrict__ in,
+                             T *__restrict__ out, long npts, SmoothSpec sp)
+{
+    OSG_GRID_LOOP(q, npts)
+    {
+        const long pt = q / 3;
+        const int j = (int)(axis == 0 ? pt % g.size[0]
+                                      : (axis == 1 ? (pt / g.size[0]) % g.size[1]
+                                                   : pt / ((long)g.size[0] * g.size[1])));
+        if (j < n || j > g.size[axis] - 1 - n) {
+            out[q] = in[q];
+            continue;
+        }
+        const long st = g.stride(axis);
+        const double *c = sp.c[axis];
+        double f = (double)in[q - n * st] * c[0];
+        for (int k = 1; k <= 2 * n; k++) f = f + (double)in[q + (k - n) * st] * c[k];
+        out[q] = (T)f;
+    }
+}
+
+template <typename T>
+void smooth_field(const GridDesc &g, const SmoothSpec &sp, T *f, T *tmp, cudaStream_t st)
+{
+    const long n = 3 * g.npoints();
+    unsigned nb = blocks_for(n, 256);
+    if (nb > 152 * 32) nb = 152 * 32;
+    for (int d = 0; d < g.dim; d++) {
+        if (sp.order[d] <= 0) continue;
+        k_smooth_dir<T><<<nb, 256, 0, st>>>(g, d, sp.order[d], f, tmp, n, sp);
+        cudaMemcpyAsync(f, tmp, sizeof(T) * n, cudaMemcpyDeviceToDevice, st);
+    }
+}
+
 template void yee_advance<float>(const GridDesc &, float *, float *, const float *,
                                  const double *, double, cudaStream_t);
 template void yee_advance<double>(const GridDesc &, double *, double *, const double *,
                                   const double *, double, cudaStream_t);
 template void periodic_update<float>(const GridDesc &, float *, int, cudaStream_t, int);
 template void periodic_update<double>(const GridDesc &, double *, int, cudaStream_t, int);
+template void smooth_field<float>(const GridDesc &, const SmoothSpec &, float *, float *,
+                                  cudaStream_t);
+template void smooth_field<double>(const GridDesc &, const SmoothSpec &, double *, double *,
+                                   cudaStream_t);
 template void shift_window_x<float>(const GridDesc &, float *, float *, cudaStream_t);
 template void shift_window_x<double>(const GridDesc &, double *, double *, cudaStream_t);
 template void field_sumsq<float>(const GridDesc &, const float *, double *, cudaStream_t);

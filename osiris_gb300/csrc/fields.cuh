@@ -73,6 +73,18 @@ void batch_yee(const FieldBox *d_boxes, int nbox, int dim, long max_points, cuda
 template <typename T>
 void periodic_update(const GridDesc &g, T *f, int add, cudaStream_t st, int open_mask = 0);
 
+// Current smoothing (smooth_vdf, source/vdf/os-vdf-smooth.f90:514-540): a separable filter of
+// 2 * order[d] + 1 points per axis with FP64 coefficients c[d][0 .. 2 order[d]].
+struct SmoothSpec {
+    int order[3];
+    double c[3][31];
+};
+// coefficients of one axis (setup_smooth, :373-467): type OSG_SMOOTH_*, order as the deck's
+int smooth_coefficients(int type, int order, double *c, int *eff_order);
+// filter f in place along every axis with order > 0 (tmp: scratch array of the same size)
+template <typename T>
+void smooth_field(const GridDesc &g, const SmoothSpec &sp, T *f, T *tmp, cudaStream_t st);
+
 // moving window: shift all of f one cell towards lower x1, zero the last x1 plane (tmp: a
 // scratch array of the same size)
 template <typename T> void shift_window_x(const GridDesc &g, T *f, T *tmp, cudaStream_t st);

@@ -11,6 +11,8 @@
 //   6. Yee B/2, E, B/2             emf%advance (:661)
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -56,7 +58,8 @@ struct osg_sim {
     bool window = false;
     double xmoved = 0.0;         // window motion not yet turned into a cell move
     long moves = 0;              // cell moves so far
-    void *shift_tmp = nullptr;   // scratch field array for the shift
+    void *shift_tmp = nullptr;   // scratch field array for the shift and the smoothing
+    osg::SmoothSpec smooth;      // current smoothing (order 0 per axis: none)
     // graphs: [parity][sort (plain) / window move (tiled)]
     cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     bool graphs_dirty = true;
@@ -285,6 +288,11 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[3], st));
     periodic_update<T>(s->g, (T *)s->j, 1, st, open);
     launches += c.dim;
+    if (s->smooth.order[0] > 0) {
+        // smooth currents after the boundary update (source/os-simulation.f03:651-657)
+        smooth_field<T>(s->g, s->smooth, (T *)s->j, (T *)s->shift_tmp, st);
+        launches += c.dim;
+    }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[4], st));
     yee_advance<T>(s->g, (T *)s->e, (T *)s->b, (const T *)s->j, c.dx, c.dt, st);
     launches += 3;
@@ -435,6 +443,23 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
         s->cfg.dx[d] = 1.0;
     }
     guard_cells(cfg->order, &s->gl, &s->gu);
+    {
+        int n = 0;
+        memset(&s->smooth, 0, sizeof s->smooth);
+        if (smooth_coefficients(cfg->smooth_type, cfg->smooth_order, s->smooth.c[0], &n)) {
+            set_error("bad smoothing type %d / order %d", cfg->smooth_type, cfg->smooth_order);
+            delete s;
+            return OSG_ERR_ARG;
+        }
+        for (int d = 0; d < cfg->dim; d++) {
+            s->smooth.order[d] = n;
+            for (int k = 0; k < 2 * n + 1; k++) s->smooth.c[d][k] = s->smooth.c[0][k];
+        }
+        // the filter needs n lower and n + 1 upper guard cells (the first upper guard cell of
+        // the current is used by the E advance), source/current/os-current-define.f03:198-206
+        s->gl = std::max(s->gl, n);
+        s->gu = std::max(s->gu, n + 1);
+    }
     int gcl[3] = {s->gl, s->gl, s->gl}, gcu[3] = {s->gu, s->gu, s->gu};
     s->g = make_grid(cfg->dim, s->cfg.nx, gcl, gcu);
     s->esz = cfg->precision == 32 ? 4 : 8;
@@ -451,6 +476,7 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
     s->d_ene = rc ? nullptr : dalloc<double>(MAX_SPECIES, &rc);
     s->d_status = rc ? nullptr : dalloc<int>(4, &rc);
     s->d_diag = rc ? nullptr : dalloc<double>(16, &rc);
+    if (!rc && s->smooth.order[0] > 0) s->shift_tmp = dalloc<char>(gbytes, &rc);
     if (rc) {
         osg_sim_destroy(s);
         return rc;
@@ -679,6 +705,16 @@ int osg_sim_set_window(osg_sim *s, int species, const int *ppc, int nprof, const
     s->xmoved = s->cfg.dt;
     s->moves = 0;
     s->graphs_dirty = true;
+    return OSG_OK;
+}
+
+int osg_sim_guard_cells(osg_sim *s, int *gcl, int *gcu)
+{
+    OSG_CHECK(s && gcl && gcu, OSG_ERR_ARG, "bad arguments");
+    for (int d = 0; d < s->cfg.dim; d++) {
+        gcl[d] = s->g.gcl[d];
+        gcu[d] = s->g.gcu[d];
+    }
     return OSG_OK;
 }
 

@@ -584,9 +584,11 @@ __device__ __forceinline__ int warp_sort32(int v)
 }
 
 // deposit the top 32 entries while at least nmin (>= 1) are queued
+// (kept out of line: it runs on a fraction of the iterations and its code would otherwise
+//  enlarge the particle loop)
 template <int ORD>
-__device__ __forceinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int nmin,
-                                           const float *jn, int jsy)
+__device__ __noinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int nmin,
+                                        const float *jn, int jsy)
 {
     constexpr int NV = SegVals<2, ORD>::NV;
     const int lane = (int)(threadIdx.x & 31);

@@ -19,10 +19,11 @@
 // so every step starts from cell-sorted tiles.  The shared current tile is added to the global
 // current at the end (the halo overlaps the neighbours' halos).
 //
-// The per-particle arithmetic is the same as the plain engine (pic_math.cuh) and therefore the
-// same as the reference kernels FNAME(vadvance_deposit_{2d,3d}_sN) (source/simd/
-// os-spec-push-avx2.c:471-760, :1141-1480); only the order in which current contributions are
-// summed differs.  The migration and the per-step tile sort replace both the periodic particle
+// The per-particle arithmetic is the plain engine's (pic_math.cuh), i.e. the reference kernels'
+// FNAME(vadvance_deposit_{2d,3d}_sN) (source/simd/os-spec-push-avx2.c:471-760, :1141-1480),
+// except that the tiled kernels are compiled with the approximate single-precision division
+// and square root (at most 2 ulp) and that the order in which current contributions are summed
+// differs.  The migration and the per-step tile sort replace both the periodic particle
 // boundary (source/spec/os-spec-boundary.f03:1280-1290) and the cell sort every n_sort steps
 // (source/spec/os-species.f03:269-505).
 #include <cuda_runtime.h>

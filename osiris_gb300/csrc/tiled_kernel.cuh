@@ -312,12 +312,21 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                     sd.in.ix[0][p] = 0;
                     has = false;
                 } else {
+                    // most particles stay in their tile: test that without dividing
+                    bool inside = true;
 #pragma unroll
-                    for (int d = 0; d < DIM; d++) {
-                        dt += mul * ((cw[d] - 1) / a.T[d]);
-                        mul *= a.ntile[d];
+                    for (int d = 0; d < DIM; d++)
+                        inside = inside && cw[d] >= t0[d] && cw[d] < t0[d] + a.T[d];
+                    if (inside) {
+                        dest = tile;
+                    } else {
+#pragma unroll
+                        for (int d = 0; d < DIM; d++) {
+                            dt += mul * ((cw[d] - 1) / a.T[d]);
+                            mul *= a.ntile[d];
+                        }
+                        dest = dt;
                     }
-                    dest = dt;
                 }
             }
             const bool stay = has && dest == tile;
