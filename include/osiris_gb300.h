@@ -64,6 +64,8 @@ extern "C" {
 
 #define OSG_PUSHER_BORIS 0   /* push_type = "simd" / "standard" (Boris) */
 #define OSG_PUSHER_EXACT 1   /* push_type = "exact" (analytic, source/spec/os-spec-extpush.f03) */
+#define OSG_PUSHER_VAY 2     /* push_type = "vay" (dudt_vay, source/spec/os-spec-push.f03) */
+#define OSG_PUSHER_HC 3      /* push_type = "cary" (Higuera-Cary, dudt_cary, same file) */
 
 const char *osg_last_error(void);
 int osg_version(void);
@@ -113,6 +115,22 @@ int osg_advance_deposit_exact_f64(int dim, int order, int *ix, double *x, double
                                   const int *emf_offset, double *j, const int *j_size,
                                   const int *j_offset, const double *dx, double dt,
                                   double iter_tol, double *ene);
+
+/* The particle advance of the Fortran path (advance_deposit_{1d,2d,3d},
+ * source/spec/os-spec-push.f03:1363-1605) with any momentum update: pusher OSG_PUSHER_BORIS,
+ * _EXACT (iter_tol), _VAY or _HC; dt is the double step (momentum and dt/dx).  Position
+ * update, split and deposit as osg_vadvance_deposit_*; *ene += the energy the chosen reference
+ * pusher reports (Boris and Vay: time-centred; exact: new momenta; HC: half-kicked). */
+int osg_advance_deposit_f32(int dim, int order, int *ix, float *x, float *u, float *q, int i0,
+                            int i1, float rqm, const float *efield, const float *bfield,
+                            const int *emf_size, const int *emf_offset, float *j,
+                            const int *j_size, const int *j_offset, const double *dx, double dt,
+                            int pusher, double iter_tol, double *ene);
+int osg_advance_deposit_f64(int dim, int order, int *ix, double *x, double *u, double *q,
+                            int i0, int i1, double rqm, const double *efield,
+                            const double *bfield, const int *emf_size, const int *emf_offset,
+                            double *j, const int *j_size, const int *j_offset, const double *dx,
+                            double dt, int pusher, double iter_tol, double *ene);
 
 /* The same push for callers that cannot allocate device memory: hosts that give the whole GPU
  * to their own pool allocator at start-up and treat a foreign cudaMalloc as an error, and
@@ -233,7 +251,7 @@ typedef struct {
     int tile[3];      /* tile shape in cells (TILED; 0 = automatic) */
     int n_sort;       /* PLAIN: cell sort every n_sort steps (0 = never); TILED sorts every step */
     double capacity;  /* TILED: slots per tile as a multiple of the mean load (0 = 3.0) */
-    int pusher;       /* OSG_PUSHER_BORIS (0) or OSG_PUSHER_EXACT (1) */
+    int pusher;       /* OSG_PUSHER_BORIS (0), _EXACT (1), _VAY (2) or _HC (3) */
     double iter_tol;  /* exact pusher: Newton tolerance (0 = the reference default 1e-3) */
     int smooth_type;  /* current smoothing after the guard fold, OSG_SMOOTH_* (all axes) */
     int smooth_order; /* its order (binomial: passes; compensated: >= 2; others fixed) */

@@ -147,15 +147,97 @@ static int EXN(ora_exact_u)(const R *ep, const R *bp, R *u, double dt, double to
     return 1;
 }
 
-/* Momentum update of n particles with given (unscaled) fields ep(3,n), bp(3,n): qm = 1/rqm
- * scaling as dudt_exact (:76-86), then ora_exact_u; *ene += sum q (gamma - 1) of the new
- * momenta, accumulated in double (:335-344). */
-void EXN(ora_dudt_exact)(int n, const R *e, const R *b, R *u, const R *q, R rqm, double dt,
-                         double tol, double *ene)
+/* Vay pusher (dudt_vay, source/spec/os-spec-push.f03:636-796): tem = real(0.5 dt / rqm)
+ * (:663); fields scaled by tem; returns q uc^2 / (gamma_c + 1) of the time-centred momentum
+ * uc = (u_old + u_new) / 2 (:772-790).  x**2 of the Fortran is x * x. */
+static R EXN(ora_vay_u)(R tem, const R *e, const R *b, R *u, R q)
+{
+    R ep[3], bp[3], tv[3], ut[3];
+    for (int c = 0; c < 3; c++) {
+        ep[c] = e[c] * tem;
+        bp[c] = b[c] * tem;
+    }
+    R rgam = K(1.0) / SQRT(((K(1.0) + u[0] * u[0]) + u[1] * u[1]) + u[2] * u[2]);
+    for (int c = 0; c < 3; c++) tv[c] = u[c] * rgam;
+    const R bpsq = (bp[0] * bp[0] + bp[1] * bp[1]) + bp[2] * bp[2];
+    ut[0] = ((u[0] + ep[0]) + tv[1] * bp[2]) - tv[2] * bp[1];
+    ut[1] = ((u[1] + ep[1]) + tv[2] * bp[0]) - tv[0] * bp[2];
+    ut[2] = ((u[2] + ep[2]) + tv[0] * bp[1]) - tv[1] * bp[0];
+    for (int c = 0; c < 3; c++) tv[c] = ut[c] + ep[c];
+    const R ustar = (tv[0] * bp[0] + tv[1] * bp[1]) + tv[2] * bp[2];
+    const R sigma = (((K(1.0) + tv[0] * tv[0]) + tv[1] * tv[1]) + tv[2] * tv[2]) - bpsq;
+    rgam = K(1.0) / SQRT(K(0.5) * (sigma + SQRT(sigma * sigma + K(4.0) * (bpsq + ustar * ustar))));
+    for (int c = 0; c < 3; c++) bp[c] = bp[c] * rgam;
+    const R spar = K(1.0) / (((K(1.0) + bp[0] * bp[0]) + bp[1] * bp[1]) + bp[2] * bp[2]);
+    const R uptp = (tv[0] * bp[0] + tv[1] * bp[1]) + tv[2] * bp[2];
+    const R uo[3] = {u[0], u[1], u[2]};
+    u[0] = spar * (((tv[0] + uptp * bp[0]) + tv[1] * bp[2]) - tv[2] * bp[1]);
+    u[1] = spar * (((tv[1] + uptp * bp[1]) + tv[2] * bp[0]) - tv[0] * bp[2]);
+    u[2] = spar * (((tv[2] + uptp * bp[2]) + tv[0] * bp[1]) - tv[1] * bp[0]);
+    R uc[3];
+    for (int c = 0; c < 3; c++) uc[c] = K(0.5) * (uo[c] + u[c]);
+    const R uc2 = (uc[0] * uc[0] + uc[1] * uc[1]) + uc[2] * uc[2];
+    const R gc = SQRT(uc2 + K(1.0));
+    return (q * uc2) / (gc + K(1.0));
+}
+
+/* Higuera-Cary pusher (dudt_cary, source/spec/os-spec-push.f03:1104-1253): tem =
+ * real(0.5 (dt / rqm)) (:1132); returns the energy term q u2 / (sqrt(gamma_minus^2) + 1)
+ * accumulated in double (:1150-1153). */
+static double EXN(ora_hc_u)(R tem, const R *e, const R *b, R *u, R q)
+{
+    R ep[3], bp[3], ut[3], pn[3];
+    for (int c = 0; c < 3; c++) {
+        ep[c] = e[c] * tem;
+        bp[c] = b[c] * tem;
+    }
+    for (int c = 0; c < 3; c++) ut[c] = u[c] + ep[c];
+    const R u2 = (ut[0] * ut[0] + ut[1] * ut[1]) + ut[2] * ut[2];
+    const R gm = (R)((double)u2 + 1.0);
+    const double ene = (double)(q * u2) / ((double)SQRT(gm) + 1.0);
+    const R bpsq = (bp[0] * bp[0] + bp[1] * bp[1]) + bp[2] * bp[2];
+    R bdu = (bp[0] * ut[0] + bp[1] * ut[1]) + bp[2] * ut[2];
+    bdu = bdu * bdu;
+    const R gmb = gm - bpsq;
+    const R gam = SQRT(K(0.5) * (gmb + SQRT(gmb * gmb + K(4.0) * (bpsq + bdu))));
+    for (int c = 0; c < 3; c++) bp[c] = bp[c] / gam;
+    pn[0] = ut[0] + ut[1] * bp[2];
+    pn[1] = ut[1] + ut[2] * bp[0];
+    pn[2] = ut[2] + ut[0] * bp[1];
+    pn[0] = pn[0] - ut[2] * bp[1];
+    pn[1] = pn[1] - ut[0] * bp[2];
+    pn[2] = pn[2] - ut[1] * bp[0];
+    const R otsq = K(2.0) / (((K(1.0) + bp[0] * bp[0]) + bp[1] * bp[1]) + bp[2] * bp[2]);
+    for (int c = 0; c < 3; c++) bp[c] = bp[c] * otsq;
+    ut[0] = ut[0] + pn[1] * bp[2];
+    ut[1] = ut[1] + pn[2] * bp[0];
+    ut[2] = ut[2] + pn[0] * bp[1];
+    ut[0] = ut[0] - pn[2] * bp[1];
+    ut[1] = ut[1] - pn[0] * bp[2];
+    ut[2] = ut[2] - pn[1] * bp[0];
+    for (int c = 0; c < 3; c++) u[c] = ut[c] + ep[c];
+    return ene;
+}
+
+/* Momentum update of n particles in given (unscaled) fields e(3,n), b(3,n) by pusher 1 (exact:
+ * fields times qm = 1/rqm as dudt_exact, :76-86, energy q (gamma - 1) of the new momenta),
+ * 2 (Vay) or 3 (Higuera-Cary) with their own tem and energy terms; *ene += the double sum. */
+void EXN(ora_dudt_pusher)(int pusher, int n, const R *e, const R *b, R *u, const R *q, R rqm,
+                          double dt, double tol, double *ene)
 {
     const R qm = K(1.0) / rqm;
     double loc = 0.0;
     for (int i = 0; i < n; i++) {
+        if (pusher == 2) {
+            loc += (double)EXN(ora_vay_u)((R)(0.5 * dt / (double)rqm), e + 3 * i, b + 3 * i,
+                                          u + 3 * i, q[i]);
+            continue;
+        }
+        if (pusher == 3) {
+            loc += EXN(ora_hc_u)((R)(0.5 * (dt / (double)rqm)), e + 3 * i, b + 3 * i, u + 3 * i,
+                                 q[i]);
+            continue;
+        }
         R ep[3], bp[3];
         for (int c = 0; c < 3; c++) {
             ep[c] = e[3 * i + c] * qm;
@@ -169,8 +251,15 @@ void EXN(ora_dudt_exact)(int n, const R *e, const R *b, R *u, const R *q, R rqm,
     *ene += loc;
 }
 
-/* Selected momentum update of the push restatement below (0 = Boris, 1 = exact) and the
- * exact pusher's tolerance; set by ora_push_exact_* around one call. */
+void EXN(ora_dudt_exact)(int n, const R *e, const R *b, R *u, const R *q, R rqm, double dt,
+                         double tol, double *ene)
+{
+    EXN(ora_dudt_pusher)(1, n, e, b, u, q, rqm, dt, tol, ene);
+}
+
+/* Selected momentum update of the push restatement below (0 = Boris, 1 = exact, 2 = Vay,
+ * 3 = Higuera-Cary), the exact pusher's tolerance and the double time step of the Fortran
+ * pushers; set by ora_push_pusher_* around one call. */
 static int EXN(ora_pusher) = 0;
 static double EXN(ora_iter_tol) = 1.0e-3;
 static double EXN(ora_push_dt) = 0.0;

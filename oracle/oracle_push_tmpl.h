@@ -195,6 +195,19 @@ static inline void OFN(dudt)(R tem, R rqm, R e1, R e2, R e3, R b1, R b2, R b3,
         OFN(boris)(tem, e1, e2, e3, b1, b2, b3, u1, u2, u3, en);
         return;
     }
+    if (EXN(ora_pusher) >= 2) {
+        /* Vay / Higuera-Cary: their own tem from the double dt, energy straight to *eacc */
+        const double dt = EXN(ora_push_dt);
+        const R e[3] = {e1, e2, e3}, b[3] = {b1, b2, b3};
+        R uu[3] = {*u1, *u2, *u3};
+        if (EXN(ora_pusher) == 2)
+            *eacc += (double)EXN(ora_vay_u)((R)(0.5 * dt / (double)rqm), e, b, uu, qp);
+        else
+            *eacc += EXN(ora_hc_u)((R)(0.5 * (dt / (double)rqm)), e, b, uu, qp);
+        *u1 = uu[0]; *u2 = uu[1]; *u3 = uu[2];
+        *en = K(0.0);
+        return;
+    }
     const R qm = K(1.0) / rqm;
     R ep[3], bp[3], uu[3];
     ep[0] = e1 * qm; ep[1] = e2 * qm; ep[2] = e3 * qm;

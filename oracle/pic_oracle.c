@@ -188,13 +188,15 @@ int ora_push_f64(int dim, int order, int *ix, double *x, double *u, double *q, i
     return 0;
 }
 
-/* push with the exact momentum update (push_type = "exact"): momentum as dudt_exact with the
- * double step dt and tolerance tol, position and deposit as the push above with dt */
-int ora_push_exact_f32(int dim, int order, int *ix, float *x, float *u, float *q, int i0, int i1,
-                       float rqm, float *e, float *b, int *emf_size, int *emf_off, float *j,
-                       int *j_size, int *j_off, double *dx, double dt, double tol, double *ene)
+/* push with another momentum update (pusher 1 exact, 2 Vay, 3 Higuera-Cary; the Fortran
+ * advance_deposit path): momentum with the double step dt (and tolerance tol, exact pusher),
+ * position and deposit as the push above with dt */
+int ora_push_pusher_f32(int pusher, int dim, int order, int *ix, float *x, float *u, float *q,
+                        int i0, int i1, float rqm, float *e, float *b, int *emf_size,
+                        int *emf_off, float *j, int *j_size, int *j_off, double *dx, double dt,
+                        double tol, double *ene)
 {
-    ora_pusher_f32 = 1;
+    ora_pusher_f32 = pusher;
     ora_push_dt_f32 = dt;
     ora_iter_tol_f32 = tol;
     int rc = ora_push_f32(dim, order, ix, x, u, q, i0, i1, rqm, e, b, emf_size, emf_off, j,
@@ -203,18 +205,35 @@ int ora_push_exact_f32(int dim, int order, int *ix, float *x, float *u, float *q
     return rc;
 }
 
-int ora_push_exact_f64(int dim, int order, int *ix, double *x, double *u, double *q, int i0,
-                       int i1, double rqm, double *e, double *b, int *emf_size, int *emf_off,
-                       double *j, int *j_size, int *j_off, double *dx, double dt, double tol,
-                       double *ene)
+int ora_push_pusher_f64(int pusher, int dim, int order, int *ix, double *x, double *u,
+                        double *q, int i0, int i1, double rqm, double *e, double *b,
+                        int *emf_size, int *emf_off, double *j, int *j_size, int *j_off,
+                        double *dx, double dt, double tol, double *ene)
 {
-    ora_pusher_f64 = 1;
+    ora_pusher_f64 = pusher;
     ora_push_dt_f64 = dt;
     ora_iter_tol_f64 = tol;
     int rc = ora_push_f64(dim, order, ix, x, u, q, i0, i1, rqm, e, b, emf_size, emf_off, j,
                           j_size, j_off, dx, dt, ene);
     ora_pusher_f64 = 0;
     return rc;
+}
+
+int ora_push_exact_f32(int dim, int order, int *ix, float *x, float *u, float *q, int i0, int i1,
+                       float rqm, float *e, float *b, int *emf_size, int *emf_off, float *j,
+                       int *j_size, int *j_off, double *dx, double dt, double tol, double *ene)
+{
+    return ora_push_pusher_f32(1, dim, order, ix, x, u, q, i0, i1, rqm, e, b, emf_size, emf_off,
+                               j, j_size, j_off, dx, dt, tol, ene);
+}
+
+int ora_push_exact_f64(int dim, int order, int *ix, double *x, double *u, double *q, int i0,
+                       int i1, double rqm, double *e, double *b, int *emf_size, int *emf_off,
+                       double *j, int *j_size, int *j_off, double *dx, double dt, double tol,
+                       double *ene)
+{
+    return ora_push_pusher_f64(1, dim, order, ix, x, u, q, i0, i1, rqm, e, b, emf_size, emf_off,
+                               j, j_size, j_off, dx, dt, tol, ene);
 }
 
 /* ---------------------------------------------------------------- particle phases ------- */
@@ -431,7 +450,7 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
  * current guard fold -> Yee.  ene[s] receives the time-centred kinetic energy sum of species s
  * (before the rqm*dV normalisation).
  */
-#define STEP_BODY(R, SFXN, EXACT, TOL)                                                        \
+#define STEP_BODY(R, SFXN, PUSHER, TOL)                                                        \
     int gsz = 3;                                                                              \
     for (int d = 0; d < dim; d++) gsz *= nx[d] + gcl[d] + gcu[d];                             \
     int emf_size[3], emf_off[3];                                                              \
@@ -440,10 +459,10 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
         emf_off[d] = d < dim ? gcl[d] : 0;                                                    \
     }                                                                                         \
     /* the single-precision SIMD push gets dt rounded to p_k_part (dtcycle = real(dt, p_k_part),\
-       source/spec/os-spec-vpush.f03:365); the Fortran push used with the exact pusher keeps  \
+       source/spec/os-spec-vpush.f03:365); the Fortran push used with the other pushers keeps \
        the double dt (dt_dx = real(gdt/dx, p_k_part), source/spec/os-spec-push.f03:1459-1460) */\
-    const double dtp = (sizeof(R) == 4 && !(EXACT)) ? (double)(float)dt : dt;                 \
-    ora_pusher_##SFXN = (EXACT);                                                              \
+    const double dtp = (sizeof(R) == 4 && !(PUSHER)) ? (double)(float)dt : dt;                \
+    ora_pusher_##SFXN = (PUSHER);                                                             \
     ora_push_dt_##SFXN = dt;                                                                  \
     ora_iter_tol_##SFXN = (TOL);                                                              \
     ora_periodic_##SFXN(dim, nx, gcl, gcu, e, 0);                                             \
@@ -499,21 +518,21 @@ int ora_step_f64(int dim, int order, const int *nx, const int *gcl, const int *g
     STEP_BODY(double, f64, 0, 1e-3)
 }
 
-/* the same step with the exact momentum update (push_type = "exact") at tolerance tol */
-int ora_step_exact_f32(int dim, int order, const int *nx, const int *gcl, const int *gcu,
-                       const double *dx, double dt, float *e, float *b, float *j, int nspec,
-                       const int *np, int **ix, float **x, float **u, float **q,
-                       const float *rqm, double *ene, int nthreads, double tol)
+/* the same step with another momentum update (pusher 1 exact, 2 Vay, 3 Higuera-Cary) */
+int ora_step_pusher_f32(int pusher, int dim, int order, const int *nx, const int *gcl,
+                        const int *gcu, const double *dx, double dt, float *e, float *b,
+                        float *j, int nspec, const int *np, int **ix, float **x, float **u,
+                        float **q, const float *rqm, double *ene, int nthreads, double tol)
 {
-    STEP_BODY(float, f32, 1, tol)
+    STEP_BODY(float, f32, pusher, tol)
 }
 
-int ora_step_exact_f64(int dim, int order, const int *nx, const int *gcl, const int *gcu,
-                       const double *dx, double dt, double *e, double *b, double *j, int nspec,
-                       const int *np, int **ix, double **x, double **u, double **q,
-                       const double *rqm, double *ene, int nthreads, double tol)
+int ora_step_pusher_f64(int pusher, int dim, int order, const int *nx, const int *gcl,
+                        const int *gcu, const double *dx, double dt, double *e, double *b,
+                        double *j, int nspec, const int *np, int **ix, double **x, double **u,
+                        double **q, const double *rqm, double *ene, int nthreads, double tol)
 {
-    STEP_BODY(double, f64, 1, tol)
+    STEP_BODY(double, f64, pusher, tol)
 }
 
 int ora_max_threads(void)

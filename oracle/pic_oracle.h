@@ -32,7 +32,11 @@ int ora_push_exact_f64(int dim, int order, int *ix, double *x, double *u, double
                        int i1, double rqm, double *e, double *b, int *emf_size, int *emf_off,
                        double *j, int *j_size, int *j_off, double *dx, double dt, double tol,
                        double *ene);
-/* exact momentum update of n particles in given fields e(3,n), b(3,n) */
+/* momentum update of n particles in given fields e(3,n), b(3,n): pusher 1 exact, 2 Vay, 3 HC */
+void ora_dudt_pusher_f32(int pusher, int n, const float *e, const float *b, float *u,
+                         const float *q, float rqm, double dt, double tol, double *ene);
+void ora_dudt_pusher_f64(int pusher, int n, const double *e, const double *b, double *u,
+                         const double *q, double rqm, double dt, double tol, double *ene);
 void ora_dudt_exact_f32(int n, const float *e, const float *b, float *u, const float *q,
                         float rqm, double dt, double tol, double *ene);
 void ora_dudt_exact_f64(int n, const double *e, const double *b, double *u, const double *q,
@@ -85,14 +89,22 @@ int ora_step_f64(int dim, int order, const int *nx, const int *gcl, const int *g
                  const double *dx, double dt, double *e, double *b, double *j, int nspec,
                  const int *np, int **ix, double **x, double **u, double **q,
                  const double *rqm, double *ene, int nthreads);
-int ora_step_exact_f32(int dim, int order, const int *nx, const int *gcl, const int *gcu,
-                       const double *dx, double dt, float *e, float *b, float *j, int nspec,
-                       const int *np, int **ix, float **x, float **u, float **q,
-                       const float *rqm, double *ene, int nthreads, double tol);
-int ora_step_exact_f64(int dim, int order, const int *nx, const int *gcl, const int *gcu,
-                       const double *dx, double dt, double *e, double *b, double *j, int nspec,
-                       const int *np, int **ix, double **x, double **u, double **q,
-                       const double *rqm, double *ene, int nthreads, double tol);
+int ora_step_pusher_f32(int pusher, int dim, int order, const int *nx, const int *gcl,
+                        const int *gcu, const double *dx, double dt, float *e, float *b,
+                        float *j, int nspec, const int *np, int **ix, float **x, float **u,
+                        float **q, const float *rqm, double *ene, int nthreads, double tol);
+int ora_step_pusher_f64(int pusher, int dim, int order, const int *nx, const int *gcl,
+                        const int *gcu, const double *dx, double dt, double *e, double *b,
+                        double *j, int nspec, const int *np, int **ix, double **x, double **u,
+                        double **q, const double *rqm, double *ene, int nthreads, double tol);
+int ora_push_pusher_f32(int pusher, int dim, int order, int *ix, float *x, float *u, float *q,
+                        int i0, int i1, float rqm, float *e, float *b, int *emf_size,
+                        int *emf_off, float *j, int *j_size, int *j_off, double *dx, double dt,
+                        double tol, double *ene);
+int ora_push_pusher_f64(int pusher, int dim, int order, int *ix, double *x, double *u,
+                        double *q, int i0, int i1, double rqm, double *e, double *b,
+                        int *emf_size, int *emf_off, double *j, int *j_size, int *j_off,
+                        double *dx, double dt, double tol, double *ene);
 int ora_max_threads(void);
 
 #endif

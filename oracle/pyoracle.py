@@ -25,6 +25,7 @@ REFERENCE_SRC = "/root/reference"
 
 # guard cells required by each interpolation order (source/particles/os-particles.f03:321-360)
 GUARD = {1: (1, 2), 2: (2, 3), 3: (3, 4), 4: (4, 5)}
+PUSHERS = {"boris": 0, "exact": 1, "vay": 2, "hc": 3}
 
 _lib = None
 _ref = {}
@@ -82,11 +83,14 @@ def _declare(L):
     for s_ in ("f32", "f64"):
         getattr(L, f"ora_smooth_{s_}").argtypes = [I, P, P, P, P, P, P]
         getattr(L, f"ora_set_smooth_{s_}").argtypes = [P, P]
-    L.ora_push_exact_f32.argtypes = [I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P, P,
-                                     D, D, P]
-    L.ora_push_exact_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, D, P]
+    L.ora_push_pusher_f32.argtypes = [I, I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P,
+                                      P, D, D, P]
+    L.ora_push_pusher_f64.argtypes = [I, I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, D,
+                                      P]
     L.ora_dudt_exact_f32.argtypes = [I, P, P, P, P, C.c_float, D, D, P]
     L.ora_dudt_exact_f64.argtypes = [I, P, P, P, P, D, D, D, P]
+    L.ora_dudt_pusher_f32.argtypes = [I, I, P, P, P, P, C.c_float, D, D, P]
+    L.ora_dudt_pusher_f64.argtypes = [I, I, P, P, P, P, D, D, D, P]
     for s in ("f32", "f64"):
         getattr(L, f"ora_yee_advance_{s}").argtypes = [I, P, P, P, P, P, P, P, D]
         getattr(L, f"ora_periodic_{s}").argtypes = [I, P, P, P, P, I]
@@ -96,8 +100,8 @@ def _declare(L):
         getattr(L, f"ora_load_{s}").argtypes = [P, I, P, P, P, D, P, P, D, D, P, P, P, P]
         getattr(L, f"ora_step_{s}").argtypes = [I, I, P, P, P, P, D, P, P, P, I, P, P, P, P, P,
                                                 P, P, I]
-        getattr(L, f"ora_step_exact_{s}").argtypes = [I, I, P, P, P, P, D, P, P, P, I, P, P, P,
-                                                      P, P, P, P, I, D]
+        getattr(L, f"ora_step_pusher_{s}").argtypes = [I, I, I, P, P, P, P, D, P, P, P, I, P, P,
+                                                       P, P, P, P, P, I, D]
     L.ora_wrap.argtypes = [I, P, I, P]
     L.ora_sort_index.argtypes = [I, P, I, P, P]
     L.ora_mt_seed.argtypes = [P, I]
@@ -162,17 +166,18 @@ class Grid:
 def push(prec, dim, order, ix, x, u, q, i0, i1, rqm, e, b, j, emf_size, emf_off, dx, dt,
          impl="oracle", pusher="boris", iter_tol=1e-3):
     """One vadvance_deposit call; arrays are updated in place; returns the energy sum.
-    pusher="exact" replaces the Boris momentum update by dudt_exact (energy: q (gamma - 1))."""
+    pusher "exact", "vay" or "hc" replaces the Boris momentum update by dudt_exact / dudt_vay /
+    dudt_cary with the double dt (the Fortran advance_deposit path)."""
     ene = np.zeros(1, dtype=np.float64)
     es, eo = _i32(emf_size), _i32(emf_off)
     dxa = _f64(list(dx) + [0.0] * (3 - len(dx)))
-    if pusher == "exact":
+    if pusher != "boris":
         if impl != "oracle":
-            raise ValueError("the reference kernels have no exact pusher")
-        f = getattr(lib(), f"ora_push_exact_{prec}")
-        rc = f(dim, order, _p(ix), _p(x), _p(u), _p(q), int(i0), int(i1), rqm, _p(e), _p(b),
-               _p(es), _p(eo), _p(j), _p(es), _p(eo), _p(dxa), float(dt), float(iter_tol),
-               _p(ene))
+            raise ValueError("the reference kernels have the Boris pusher only")
+        f = getattr(lib(), f"ora_push_pusher_{prec}")
+        rc = f(PUSHERS[pusher], dim, order, _p(ix), _p(x), _p(u), _p(q), int(i0), int(i1), rqm,
+               _p(e), _p(b), _p(es), _p(eo), _p(j), _p(es), _p(eo), _p(dxa), float(dt),
+               float(iter_tol), _p(ene))
         if rc != 0:
             raise ValueError("bad dim/order")
     elif impl == "oracle":
@@ -191,6 +196,16 @@ def push(prec, dim, order, ix, x, u, q, i0, i1, rqm, e, b, j, emf_size, emf_off,
         a0, a1, rq, dtv = C.c_int(int(i0)), C.c_int(int(i1)), ctype(rqm), C.c_double(dt)
         f(_p(ix), _p(x), _p(u), _p(q), C.byref(a0), C.byref(a1), C.byref(rq), _p(e), _p(b),
           _p(es), _p(eo), _p(j), _p(es), _p(eo), _p(dxa), C.byref(dtv), _p(ene))
+    return float(ene[0])
+
+
+def dudt(pusher, prec, e, b, u, q, rqm, dt, iter_tol=1e-3):
+    """Momentum update ("exact", "vay", "hc") of n particles in given fields e (n,3), b (n,3);
+    u updated in place; returns the energy sum the reference pusher reports."""
+    ene = np.zeros(1, dtype=np.float64)
+    f = getattr(lib(), f"ora_dudt_pusher_{prec}")
+    f(PUSHERS[pusher], len(q), _p(e), _p(b), _p(u), _p(q), rqm, float(dt), float(iter_tol),
+      _p(ene))
     return float(ene[0])
 
 
@@ -311,8 +326,8 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
         getattr(L, f"ora_set_smooth_{prec}")(_p(ordv), _p(coef))
     args = (g.dim, g.order, _p(nx), _p(gl), _p(gu), _p(_f64(g.dx + [0.0] * 3)), float(dt), _p(e),
             _p(b), _p(j), ns, _p(np_), ixs, xs, us, qs, _p(rqm), _p(ene), int(nthreads))
-    if pusher == "exact":
-        getattr(L, f"ora_step_exact_{prec}")(*args, float(iter_tol))
+    if pusher != "boris":
+        getattr(L, f"ora_step_pusher_{prec}")(PUSHERS[pusher], *args, float(iter_tol))
     else:
         getattr(L, f"ora_step_{prec}")(*args)
     if smooth is not None:

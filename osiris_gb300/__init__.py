@@ -32,6 +32,8 @@ ENGINE_PLAIN = 0
 ENGINE_TILED = 1
 PUSHER_BORIS = 0
 PUSHER_EXACT = 1
+PUSHER_VAY = 2
+PUSHER_HC = 3
 SMOOTH_NONE, SMOOTH_BINOMIAL, SMOOTH_COMPENSATED = 0, 2, 3
 SMOOTH_5PASS, SMOOTH_TRI6, SMOOTH_TRI8 = 4, 5, 6
 RNG_BYTES = 2512
@@ -83,6 +85,10 @@ def _declare(lb):
                                                  P, D, D, P]
     lb.osg_advance_deposit_exact_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P,
                                                  P, D, D, P]
+    lb.osg_advance_deposit_f32.argtypes = [I, I, P, P, P, P, I, I, F, P, P, P, P, P, P, P, P, D,
+                                           I, D, P]
+    lb.osg_advance_deposit_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D,
+                                           I, D, P]
     lb.osg_vadvance_deposit_noalloc_f32.argtypes = [I, I, P, P, P, P, I, I, F, P, P, P, P, P, P,
                                                     P, P, D, P]
     for s in ("f32", "f64"):
@@ -190,7 +196,9 @@ def vadvance_deposit(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_s
     Same arguments and in-place semantics as FNAME(vadvance_deposit_<dim>d_s<order>);
     returns the time-centred energy sum the reference adds into ``*ene``.  With
     ``pusher=PUSHER_EXACT`` the momentum update is the exact pusher (push_type = "exact",
-    osg_advance_deposit_exact_*) and the energy is sum q (gamma - 1) of the new momenta."""
+    osg_advance_deposit_exact_*) and the energy is sum q (gamma - 1) of the new momenta;
+    ``PUSHER_VAY`` / ``PUSHER_HC`` select the Vay and Higuera-Cary updates (push_type "vay",
+    "cary"; osg_advance_deposit_*) with the energy those reference pushers report."""
     prec = _prec(x)
     dt_ = np.float32 if prec == "f32" else np.float64
     _need(ix, np.int32, "ix")
@@ -206,6 +214,9 @@ def vadvance_deposit(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_s
     if pusher == PUSHER_EXACT:
         _check(getattr(lib(), f"osg_advance_deposit_exact_{prec}")(*args, float(iter_tol),
                                                                     _p(ene)))
+    elif pusher != PUSHER_BORIS:
+        _check(getattr(lib(), f"osg_advance_deposit_{prec}")(*args, int(pusher),
+                                                              float(iter_tol), _p(ene)))
     else:
         _check(getattr(lib(), f"osg_vadvance_deposit_{prec}")(*args, _p(ene)))
     return float(ene[0])

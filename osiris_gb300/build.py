@@ -34,7 +34,8 @@ NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC
 FAST_DIV = ["-prec-div=false", "-prec-sqrt=false"]
 EXTRA = {"tiled.cu": FAST_DIV, "batch_push.cu": FAST_DIV}
 
-SOURCES = ["push_plain.cu", "fields.cu", "tiled.cu", "tiled_exact.cu", "batch_push.cu", "batch.cu",
+SOURCES = ["push_plain.cu", "fields.cu", "tiled.cu", "tiled_exact.cu", "tiled_vay.cu", "tiled_hc.cu",
+           "batch_push.cu", "batch.cu",
            "sim.cu", "capi.cu", "noalloc.cu",
            "loader.cpp", "laser.cpp"]
 

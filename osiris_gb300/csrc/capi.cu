@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "fields.cuh"
+#include "pic_math.cuh"
 #include "push_plain.cuh"
 
 namespace osg {
@@ -91,7 +92,8 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
                      const int *j_size, const int *j_off, const double *dx, double dt,
                      double *ene, int pusher = OSG_PUSHER_BORIS, double iter_tol = 1.0e-3)
 {
-    OSG_CHECK(pusher == OSG_PUSHER_BORIS || (pusher == OSG_PUSHER_EXACT && iter_tol > 0),
+    OSG_CHECK(pusher >= OSG_PUSHER_BORIS && pusher <= OSG_PUSHER_HC &&
+                  (pusher != OSG_PUSHER_EXACT || iter_tol > 0),
               OSG_ERR_ARG, "bad pusher / iteration tolerance");
     OSG_CHECK(dim >= 1 && dim <= 3 && order >= 1 && order <= 4, OSG_ERR_ARG,
               "dim %d / order %d not supported", dim, order);
@@ -142,6 +144,8 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
                                                 (T *)d_j, j_size, j_off, dx, dt, d_ene, d_status);
         a.pusher = pusher;
         a.iter_tol = iter_tol;
+        if (pusher == OSG_PUSHER_VAY || pusher == OSG_PUSHER_HC)
+            a.tem = (T)pusher_tem(pusher, dt, (double)rqm);
         if ((rc = launch_plain_push<T>(dim, order, a, cs))) return rc;
         OSG_CUDA(cudaGetLastError());
         OSG_CUDA(cudaMemcpyAsync(ix + dim * h, cix, sizeof(int) * dim * n, cudaMemcpyDeviceToHost, cs));
@@ -350,6 +354,26 @@ int osg_advance_deposit_exact_f64(int dim, int order, int *ix, double *x, double
     return push_host<double>(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_size,
                              emf_offset, j, j_size, j_offset, dx, dt, ene, OSG_PUSHER_EXACT,
                              iter_tol);
+}
+
+int osg_advance_deposit_f32(int dim, int order, int *ix, float *x, float *u, float *q, int i0,
+                            int i1, float rqm, const float *efield, const float *bfield,
+                            const int *emf_size, const int *emf_offset, float *j,
+                            const int *j_size, const int *j_offset, const double *dx, double dt,
+                            int pusher, double iter_tol, double *ene)
+{
+    return push_host<float>(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_size,
+                            emf_offset, j, j_size, j_offset, dx, dt, ene, pusher, iter_tol);
+}
+
+int osg_advance_deposit_f64(int dim, int order, int *ix, double *x, double *u, double *q,
+                            int i0, int i1, double rqm, const double *efield,
+                            const double *bfield, const int *emf_size, const int *emf_offset,
+                            double *j, const int *j_size, const int *j_offset, const double *dx,
+                            double dt, int pusher, double iter_tol, double *ene)
+{
+    return push_host<double>(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_size,
+                             emf_offset, j, j_size, j_offset, dx, dt, ene, pusher, iter_tol);
 }
 
 int osg_vadvance_deposit_dev_f32(int dim, int order, int *ix, float *x, float *u,

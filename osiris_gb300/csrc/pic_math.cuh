@@ -17,6 +17,8 @@
 
 #include <cstdint>
 
+#include "../../include/osiris_gb300.h"
+
 namespace osg {
 
 __device__ __forceinline__ float fmaR(float a, float b, float c) { return fmaf(a, b, c); }
@@ -510,6 +512,91 @@ __device__ __forceinline__ T exact_push(T qm, double dt, double tol, T e1, T e2,
     u3 = u[2];
     const T g = sqrtR(((T(1.0) + u1 * u1) + u2 * u2) + u3 * u3);
     return q * (g - T(1.0));
+}
+
+// ---------------------------------------------------------------------------------------
+// Vay pusher (dudt_vay, source/spec/os-spec-push.f03:636-796; tem = real(0.5 dt / rqm),
+// :663) and Higuera-Cary pusher (dudt_cary, :1104-1253; tem = real(0.5 (dt / rqm)), :1132),
+// operation by operation as the Fortran (x**2 = x * x, a + b + c = (a + b) + c).  Both keep a
+// particle at the E x B drift velocity exactly.  They return the energy term each reference
+// pusher accumulates: Vay q uc^2 / (gamma_c + 1) of the time-centred momentum (in T), HC
+// q u^2 / (sqrt(1 + u^2) + 1) of the half-kicked momentum (in double).
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T vay_push(T tem, T e1, T e2, T e3, T b1, T b2, T b3, T q, T &u1,
+                                      T &u2, T &u3)
+{
+    const T ep[3] = {e1 * tem, e2 * tem, e3 * tem};
+    T bp[3] = {b1 * tem, b2 * tem, b3 * tem};
+    const T uo[3] = {u1, u2, u3};
+    T rgam = T(1.0) / sqrtR(((T(1.0) + u1 * u1) + u2 * u2) + u3 * u3);
+    T tv[3] = {u1 * rgam, u2 * rgam, u3 * rgam};
+    const T bpsq = (bp[0] * bp[0] + bp[1] * bp[1]) + bp[2] * bp[2];
+    T ut[3];
+    ut[0] = ((uo[0] + ep[0]) + tv[1] * bp[2]) - tv[2] * bp[1];
+    ut[1] = ((uo[1] + ep[1]) + tv[2] * bp[0]) - tv[0] * bp[2];
+    ut[2] = ((uo[2] + ep[2]) + tv[0] * bp[1]) - tv[1] * bp[0];
+#pragma unroll
+    for (int c = 0; c < 3; c++) tv[c] = ut[c] + ep[c];
+    const T ustar = (tv[0] * bp[0] + tv[1] * bp[1]) + tv[2] * bp[2];
+    const T sigma = (((T(1.0) + tv[0] * tv[0]) + tv[1] * tv[1]) + tv[2] * tv[2]) - bpsq;
+    rgam = T(1.0) / sqrtR(T(0.5) * (sigma + sqrtR(sigma * sigma + T(4.0) * (bpsq + ustar * ustar))));
+#pragma unroll
+    for (int c = 0; c < 3; c++) bp[c] = bp[c] * rgam;
+    const T spar = T(1.0) / (((T(1.0) + bp[0] * bp[0]) + bp[1] * bp[1]) + bp[2] * bp[2]);
+    const T uptp = (tv[0] * bp[0] + tv[1] * bp[1]) + tv[2] * bp[2];
+    u1 = spar * (((tv[0] + uptp * bp[0]) + tv[1] * bp[2]) - tv[2] * bp[1]);
+    u2 = spar * (((tv[1] + uptp * bp[1]) + tv[2] * bp[0]) - tv[0] * bp[2]);
+    u3 = spar * (((tv[2] + uptp * bp[2]) + tv[0] * bp[1]) - tv[1] * bp[0]);
+    const T uc[3] = {T(0.5) * (uo[0] + u1), T(0.5) * (uo[1] + u2), T(0.5) * (uo[2] + u3)};
+    const T uc2 = (uc[0] * uc[0] + uc[1] * uc[1]) + uc[2] * uc[2];
+    const T gc = sqrtR(uc2 + T(1.0));
+    return (q * uc2) / (gc + T(1.0));
+}
+
+template <typename T>
+__device__ __forceinline__ double hc_push(T tem, T e1, T e2, T e3, T b1, T b2, T b3, T q, T &u1,
+                                          T &u2, T &u3)
+{
+    const T ep[3] = {e1 * tem, e2 * tem, e3 * tem};
+    T bp[3] = {b1 * tem, b2 * tem, b3 * tem};
+    T ut[3] = {u1 + ep[0], u2 + ep[1], u3 + ep[2]};
+    const T usq = (ut[0] * ut[0] + ut[1] * ut[1]) + ut[2] * ut[2];
+    const T gm = (T)((double)usq + 1.0);
+    const double ene = (double)(q * usq) / ((double)sqrtR(gm) + 1.0);
+    const T bpsq = (bp[0] * bp[0] + bp[1] * bp[1]) + bp[2] * bp[2];
+    T bdu = (bp[0] * ut[0] + bp[1] * ut[1]) + bp[2] * ut[2];
+    bdu = bdu * bdu;
+    const T gmb = gm - bpsq;
+    const T gam = sqrtR(T(0.5) * (gmb + sqrtR(gmb * gmb + T(4.0) * (bpsq + bdu))));
+#pragma unroll
+    for (int c = 0; c < 3; c++) bp[c] = bp[c] / gam;
+    T pn[3];
+    pn[0] = ut[0] + ut[1] * bp[2];
+    pn[1] = ut[1] + ut[2] * bp[0];
+    pn[2] = ut[2] + ut[0] * bp[1];
+    pn[0] = pn[0] - ut[2] * bp[1];
+    pn[1] = pn[1] - ut[0] * bp[2];
+    pn[2] = pn[2] - ut[1] * bp[0];
+    const T otsq = T(2.0) / (((T(1.0) + bp[0] * bp[0]) + bp[1] * bp[1]) + bp[2] * bp[2]);
+#pragma unroll
+    for (int c = 0; c < 3; c++) bp[c] = bp[c] * otsq;
+    ut[0] = ut[0] + pn[1] * bp[2];
+    ut[1] = ut[1] + pn[2] * bp[0];
+    ut[2] = ut[2] + pn[0] * bp[1];
+    ut[0] = ut[0] - pn[2] * bp[1];
+    ut[1] = ut[1] - pn[0] * bp[2];
+    ut[2] = ut[2] - pn[1] * bp[0];
+    u1 = ut[0] + ep[0];
+    u2 = ut[1] + ep[1];
+    u3 = ut[2] + ep[2];
+    return ene;
+}
+
+// the pusher-specific tem of the Fortran pushers from the double dt and the species' rqm
+inline double pusher_tem(int pusher, double dt, double rqm)
+{
+    return pusher == OSG_PUSHER_HC ? 0.5 * (dt / rqm) : 0.5 * dt / rqm;
 }
 
 } // namespace osg

@@ -274,6 +274,10 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
             if (a.pusher == OSG_PUSHER_EXACT) {
                 my_ene = (double)exact_push<T>(a.qm, a.dt_full, a.iter_tol, E1, E2, E3, B1, B2,
                                                B3, q, u1, u2, u3);
+            } else if (a.pusher == OSG_PUSHER_VAY) {
+                my_ene = (double)vay_push<T>(a.tem, E1, E2, E3, B1, B2, B3, q, u1, u2, u3);
+            } else if (a.pusher == OSG_PUSHER_HC) {
+                my_ene = hc_push<T>(a.tem, E1, E2, E3, B1, B2, B3, q, u1, u2, u3);
             } else {
                 const T ene = boris(a.tem, E1, E2, E3, B1, B2, B3, u1, u2, u3);
                 my_ene = (double)q * (double)ene;

@@ -19,6 +19,7 @@
 
 #include "common.cuh"
 #include "fields.cuh"
+#include "pic_math.cuh"
 #include "push_plain.cuh"
 #include "tiled.cuh"
 
@@ -247,8 +248,8 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
     // (dtcycle = real(dt, p_k_part), source/spec/os-spec-vpush.f03:365)
     // (the Fortran push the exact pusher runs in keeps the double dt,
     //  source/spec/os-spec-push.f03:1459-1460)
-    const bool exact = c.pusher == OSG_PUSHER_EXACT;
-    const double push_dt = (sizeof(T) == 4 && !exact) ? (double)(float)c.dt : c.dt;
+    const bool fortran_push = c.pusher != OSG_PUSHER_BORIS;
+    const double push_dt = (sizeof(T) == 4 && !fortran_push) ? (double)(float)c.dt : c.dt;
     const int open = s->window ? 1 : 0;   // x1 open while the window moves
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[0], st));
     periodic_update<T>(s->g, (T *)s->e, 0, st, open);
@@ -272,6 +273,8 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
             for (int d = 0; d < c.dim; d++) a.wrap[d] = c.nx[d];
             a.pusher = c.pusher;
             a.iter_tol = c.iter_tol;
+            if (c.pusher == OSG_PUSHER_VAY || c.pusher == OSG_PUSHER_HC)
+                a.tem = (T)pusher_tem(c.pusher, push_dt, (double)(T)s->rqm[k]);
             int rc = launch_plain_push<T>(c.dim, c.order, a, st);
             if (rc) return rc;
             launches++;
@@ -423,7 +426,7 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               "unknown engine");
     OSG_CHECK(!(cfg->engine == OSG_ENGINE_TILED && cfg->precision != 32), OSG_ERR_ARG,
               "the tiled engine is single precision");
-    OSG_CHECK(cfg->pusher == OSG_PUSHER_BORIS || cfg->pusher == OSG_PUSHER_EXACT, OSG_ERR_ARG,
+    OSG_CHECK(cfg->pusher >= OSG_PUSHER_BORIS && cfg->pusher <= OSG_PUSHER_HC, OSG_ERR_ARG,
               "unknown pusher");
     OSG_CHECK(cfg->iter_tol >= 0, OSG_ERR_ARG, "iter_tol must be >= 0");
     double cour = 0.0;

@@ -127,7 +127,17 @@ __global__ void k_compact(Slabs in, long cap, int dim, const int *__restrict__ o
 // 1459-1460), as does the field solver.
 static double push_dt(const TiledState *t)
 {
-    return t->pusher == OSG_PUSHER_EXACT ? t->dt : (double)(float)t->dt;
+    return t->pusher != OSG_PUSHER_BORIS ? t->dt : (double)(float)t->dt;
+}
+
+static cudaError_t push_attr(int pusher, int dim, int order, int bytes)
+{
+    switch (pusher) {
+    case OSG_PUSHER_EXACT: return push_tiled_attr_exact(dim, order, bytes);
+    case OSG_PUSHER_VAY: return push_tiled_attr_vay(dim, order, bytes);
+    case OSG_PUSHER_HC: return push_tiled_attr_hc(dim, order, bytes);
+    default: return push_tiled_attr_boris(dim, order, bytes);
+    }
 }
 
 static TiledArgs base_args(const TiledState *t)
@@ -225,10 +235,7 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
     t->iter_tol = cfg.iter_tol > 0 ? cfg.iter_tol : 1.0e-3;
     // opt in to more than 48 KB of dynamic shared memory (outside any stream capture)
     {
-        const cudaError_t ce =
-            t->pusher == OSG_PUSHER_EXACT
-                ? push_tiled_attr_exact(t->dim, t->order, (int)t->smem_bytes)
-                : push_tiled_attr_boris(t->dim, t->order, (int)t->smem_bytes);
+        const cudaError_t ce = push_attr(t->pusher, t->dim, t->order, (int)t->smem_bytes);
         if (ce != cudaSuccess) {
             set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(ce));
             delete t;
@@ -290,7 +297,7 @@ static int upload_tables(TiledState *t, cudaStream_t st)
         for (int k = 0; k < ns; k++) {
             tab[k].in = t->buf[p][k];
             tab[k].out = t->buf[1 - p][k];
-            tab[k].tem = (float)(0.5 * push_dt(t) / (double)(float)t->rqm[k]);
+            tab[k].tem = (float)pusher_tem(t->pusher, push_dt(t), (double)(float)t->rqm[k]);
             tab[k].qm = 1.0f / (float)t->rqm[k];
             tab[k].cap = t->cap[k];
         }
@@ -482,9 +489,7 @@ int tiled_set_threads(TiledState *t, int threads)
               "push CTA size must be a multiple of 32 in [64, 256]");
     t->threads = threads;
     t->smem_bytes = smem_for(t->dim, t->order, t->T, t->threads);
-    const cudaError_t ce = t->pusher == OSG_PUSHER_EXACT
-                               ? push_tiled_attr_exact(t->dim, t->order, (int)t->smem_bytes)
-                               : push_tiled_attr_boris(t->dim, t->order, (int)t->smem_bytes);
+    const cudaError_t ce = push_attr(t->pusher, t->dim, t->order, (int)t->smem_bytes);
     OSG_CHECK(ce == cudaSuccess, OSG_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(ce));
     return OSG_OK;
 }
@@ -579,11 +584,14 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     a.open_x = t->window ? 1 : 0;
     a.shift_x = t->window && shift ? 1 : 0;
     const size_t sm = t->smem_bytes;
-    const int rc = t->pusher == OSG_PUSHER_EXACT
-                       ? push_tiled_launch_exact(t->dim, t->order, a, (unsigned)t->ntiles,
-                                                 t->threads, sm, st)
-                       : push_tiled_launch_boris(t->dim, t->order, a, (unsigned)t->ntiles,
-                                                 t->threads, sm, st);
+    const unsigned nt = (unsigned)t->ntiles;
+    int rc;
+    switch (t->pusher) {
+    case OSG_PUSHER_EXACT: rc = push_tiled_launch_exact(t->dim, t->order, a, nt, t->threads, sm, st); break;
+    case OSG_PUSHER_VAY: rc = push_tiled_launch_vay(t->dim, t->order, a, nt, t->threads, sm, st); break;
+    case OSG_PUSHER_HC: rc = push_tiled_launch_hc(t->dim, t->order, a, nt, t->threads, sm, st); break;
+    default: rc = push_tiled_launch_boris(t->dim, t->order, a, nt, t->threads, sm, st); break;
+    }
     if (rc) return rc;
     // deterministic FP64 re-summation of the tile currents into the global current
     const FoldBox f = tiled_fold_box(t, j);

@@ -55,7 +55,8 @@ def _compare(osg, oracle, prec, engine, dim, order, nx, ppc, steps, tol, tile=No
     p, g, dx, dt, species, e, b = _setup(oracle, prec, dim, order, nx, ppc, seed)
     sim = osg.Simulation(nx, dx, dt, order=order, precision=prec, engine=engine, tile=tile,
                          n_sort=n_sort,
-                         pusher=osg.PUSHER_EXACT if pusher == "exact" else osg.PUSHER_BORIS)
+                         pusher={"boris": osg.PUSHER_BORIS, "exact": osg.PUSHER_EXACT,
+                                 "vay": osg.PUSHER_VAY, "hc": osg.PUSHER_HC}[pusher])
     sim.set_fields(e, b)
     for s in species:
         sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])

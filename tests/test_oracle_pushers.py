@@ -1,0 +1,79 @@
+"""Known-answer tests of the oracle's Vay and Higuera-Cary momentum updates (dudt_vay,
+source/spec/os-spec-push.f03:636-796; dudt_cary, :1104-1253), restated from Fortran that cannot
+be run here: both keep |u| in a pure magnetic field, both keep a particle at the E x B drift
+velocity exactly for any step (their defining property), and both agree with the exact pusher
+to O(dt^3) per step; the step-level push with them conserves charge."""
+import numpy as np
+import pytest
+
+
+def _run(oracle, pusher, e, b, u0, dt, steps=1, prec="f64"):
+    dt_ = np.float32 if prec == "f32" else np.float64
+    u = np.array(u0, dtype=dt_, copy=True)
+    q = np.full(len(u), -1.0, dtype=dt_)
+    e = np.ascontiguousarray(e, dtype=dt_)
+    b = np.ascontiguousarray(b, dtype=dt_)
+    for _ in range(steps):
+        oracle.dudt(pusher, prec, e, b, u, q, -1.0, dt, 1e-12)
+    return u.astype(np.float64)
+
+
+@pytest.mark.parametrize("pusher", ["vay", "hc"])
+def test_pure_b_keeps_energy(oracle, pusher):
+    rng = np.random.default_rng(1)
+    u0 = rng.standard_normal((8, 3))
+    b = rng.standard_normal((8, 3))
+    u = _run(oracle, pusher, np.zeros_like(b), b, u0, 0.7, steps=50)
+    assert np.abs((u ** 2).sum(1) / (u0 ** 2).sum(1) - 1).max() < 1e-13
+
+
+@pytest.mark.parametrize("pusher", ["vay", "hc"])
+def test_exb_drift_is_kept(oracle, pusher):
+    e0, b0 = 0.6, 1.0                         # |E| < |B|: drift at v = E/B along x
+    v = e0 / b0
+    g = 1.0 / np.sqrt(1 - v * v)
+    u0 = np.array([[g * v, 0.0, 0.0]])
+    e = np.array([[0.0, e0, 0.0]])
+    b = np.array([[0.0, 0.0, b0]])
+    u = _run(oracle, pusher, e, b, u0, 0.9, steps=100)
+    assert np.abs(u - u0).max() < 1e-12
+
+
+@pytest.mark.parametrize("pusher", ["vay", "hc"])
+def test_second_order_against_exact(oracle, pusher):
+    rng = np.random.default_rng(4)
+    e = rng.standard_normal((6, 3)) * 0.5
+    b = rng.standard_normal((6, 3)) * 0.5
+    u0 = rng.standard_normal((6, 3)) * 0.5
+    errs = []
+    for dt in (0.02, 0.01):
+        ue = _run(oracle, "exact", e, b, u0, dt)
+        up = _run(oracle, pusher, e, b, u0, dt)
+        errs.append(np.abs(up - ue).max())
+    assert errs[1] < errs[0] / 6        # local error O(dt^3)
+    assert errs[0] < 1e-4
+
+
+@pytest.mark.parametrize("pusher", ["vay", "hc"])
+def test_push_with_pusher_conserves_charge(oracle, pusher):
+    dim, order, nx = 2, 2, [8, 7]
+    g = oracle.Grid(nx, order, [0.1] * dim)
+    ix, x, u, q = oracle.load(oracle.mt_new(3), "f64", dim, nx, [2] * dim, [0.1] * dim, -1.0,
+                              [0.8] * 3, [0.0] * 3)
+    rng = np.random.default_rng(1)
+    e = rng.standard_normal(g.shape) * 0.5
+    b = rng.standard_normal(g.shape) * 0.5
+    oracle.periodic(g, "f64", e, 0)
+    oracle.periodic(g, "f64", b, 0)
+    dt = 0.05
+    rho0 = oracle.deposit_rho(g, "f64", ix, x, q)
+    oracle.periodic(g, "f64", rho0, 1)
+    j = g.zeros("f64")
+    oracle.push("f64", dim, order, ix, x, u, q, 1, len(q), -1.0, e, b, j, g.size, g.gcl,
+                g.dx, dt, pusher=pusher)
+    oracle.wrap(g, ix)
+    oracle.periodic(g, "f64", j, 1)
+    rho1 = oracle.deposit_rho(g, "f64", ix, x, q)
+    oracle.periodic(g, "f64", rho1, 1)
+    drho = (g.interior(rho1)[..., 0] - g.interior(rho0)[..., 0]) / dt
+    assert np.abs(drho + oracle.div(g, "f64", j)).max() / np.abs(drho).max() < 1e-12
