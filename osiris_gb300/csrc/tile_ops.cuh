@@ -12,9 +12,8 @@ constexpr unsigned FULL_MASK = 0xffffffffu;
 
 // *hi += v, with the rounding error of the addition accumulated in *lo (two-sum: the pair
 // hi + lo keeps the sum of all added values to about twice the float precision).  Plain
-// read-modify-write: the caller owns the address (a warp-private tile, no other lane of the
-// same instruction on it).  Used for the warp-reduced cell sums, which carry most of a tile's
-// current; the scattered single adds (lone lanes, face crossings) are FP32 atomics.
+// read-modify-write: the caller owns the address (a warp-private current tile, no other lane
+// of the same instruction on it).
 __device__ __forceinline__ void comp_add(float *hi, float *lo, float v)
 {
     const float a = *hi, t = a + v;
@@ -347,26 +346,20 @@ template <int DIM, int ORD> struct LaneSlots {
     }
 };
 
-// 2D: every warp of the push CTA owns a copy of the shared current tile
-template <int DIM>
-constexpr bool private_current() { return DIM == 2; }
-
-// Warp-cooperative accumulation of one segment per lane into the shared current tile.
+// 3D warp-cooperative accumulation of one segment per lane into the shared current tile.
 // base = offset of the lane's stencil origin, or -1 when the lane has no segment.  Lanes whose
 // cell is shared by at least `reduce_min` lanes of the warp are summed in registers first
-// (transpose-reduce, one pass per such cell): every add of a pass hits a distinct address, so
-// on a warp-private tile (2D) a pass is a plain read-modify-write and on the shared tile (3D)
-// its atomics never conflict.  Lanes of sparsely populated cells add their values directly
-// (shared atomics): a reduce pass costs several direct adds and only pays when enough lanes
-// share it.  Must be called by all 32 lanes.
+// (transpose-reduce, one pass per such cell): every atomic of a pass hits a distinct address.
+// Lanes of sparsely populated cells add their values directly (shared atomics): a reduce pass
+// costs several direct adds and only pays when enough lanes share it.  Must be called by all
+// 32 lanes.
 template <int DIM, int ORD>
 __device__ __forceinline__ void warp_deposit(float *sJ, int base, const float *v, int jsy,
                                              int jsz, int reduce_min,
-                                             const LaneSlots<DIM, ORD> &ls, int jlo)
+                                             const LaneSlots<DIM, ORD> &ls)
 {
     constexpr int NV = SegVals<DIM, ORD>::NV;
     constexpr int NB = (NV + 31) / 32;
-    constexpr bool PRIV = private_current<DIM>();
     const unsigned lane = threadIdx.x & 31;
     const unsigned peers = __match_any_sync(FULL_MASK, base);
     const bool active = base >= 0;
@@ -375,7 +368,6 @@ __device__ __forceinline__ void warp_deposit(float *sJ, int base, const float *v
 #pragma unroll
         for (int i = 0; i < NV; i++) atomicAdd(sJ + base + seg_offset<DIM, ORD>(i, jsy, jsz), v[i]);
     }
-    if (PRIV) __syncwarp();
     unsigned rem = __ballot_sync(FULL_MASK, active && !direct && (__ffs(peers) - 1) == (int)lane);
     while (rem) {
         const int l = __ffs(rem) - 1;
@@ -397,15 +389,8 @@ __device__ __forceinline__ void warp_deposit(float *sJ, int base, const float *v
                 for (int k = 0; k < REST; k++) t[k] = mine ? v[bch * 32 + k] : 0.f;
                 sum = transpose_reduce<REST>(t);
             }
-            if (ls.off[bch] >= 0) {
-                float *pj = sJ + key + ls.off[bch];
-                if (PRIV)
-                    comp_add(pj, pj + jlo, sum);
-                else
-                    atomicAdd(pj, sum);
-            }
+            if (ls.off[bch] >= 0) atomicAdd(sJ + key + ls.off[bch], sum);
         }
-        if (PRIV) __syncwarp();
     }
 }
 
@@ -456,59 +441,166 @@ __device__ __forceinline__ int make_segments(SegRec *out, const float *xo, const
     }
 }
 
-// Deposit one segment per lane (rec = nullptr: no segment).  reduce_min > 32 selects plain
-// per-lane shared atomics (no warp-synchronous part); otherwise warp_deposit.  3D cubic and
+// 3D: deposit one segment per lane (rec = nullptr: no segment).  reduce_min > 32 selects
+// plain per-lane shared atomics (no warp-synchronous part); otherwise warp_deposit.  Cubic and
 // quartic segments (144 and 300 values) always add directly: their values do not fit in
 // registers next to a reduce buffer.
 template <int DIM, int ORD>
 constexpr bool direct_only() { return DIM == 3 && ORD >= 3; }
 
-template <int DIM, int ORD>
-__device__ __forceinline__ void deposit_segment(float *sJ, const SegRec *rec, const float *jn,
-                                                int jsy, int jsz, int reduce_min,
-                                                const LaneSlots<DIM, ORD> &ls, int jlo)
+template <int ORD>
+__device__ __forceinline__ void deposit_segment3(float *sJ, const SegRec *rec, const float *jn,
+                                                 int jsy, int jsz, int reduce_min,
+                                                 const LaneSlots<3, ORD> &ls)
 {
-    if constexpr (DIM == 3) {
-        if (direct_only<DIM, ORD>() || reduce_min > 32) {
-            if (rec) {
-                Seg3<float> g;
-                g.x0 = rec->a[0]; g.x1 = rec->a[1]; g.y0 = rec->a[2]; g.y1 = rec->a[3];
-                g.z0 = rec->a[4]; g.z1 = rec->a[5]; g.i = g.j = g.k = 0;
-                seg_atomic3<ORD>(sJ + rec->base, g, rec->q, jn, jsy, jsz);
-            }
-            return;
-        }
-    }
-    if constexpr (!direct_only<DIM, ORD>()) {
-    constexpr int NV = SegVals<DIM, ORD>::NV;
-    float v[NV];
-    int base = -1;
-    if (rec) {
-        if constexpr (DIM == 2) {
-            Seg2<float> g;
+    if (direct_only<3, ORD>() || reduce_min > 32) {
+        if (rec) {
+            Seg3<float> g;
             g.x0 = rec->a[0]; g.x1 = rec->a[1]; g.y0 = rec->a[2]; g.y1 = rec->a[3];
-            g.vz = rec->a[4]; g.i = 0; g.j = 0;
-            seg_values2<ORD>(g, rec->q, jn[0], jn[1], v);
-        } else {
+            g.z0 = rec->a[4]; g.z1 = rec->a[5]; g.i = g.j = g.k = 0;
+            seg_atomic3<ORD>(sJ + rec->base, g, rec->q, jn, jsy, jsz);
+        }
+        return;
+    }
+    if constexpr (!direct_only<3, ORD>()) {
+        constexpr int NV = SegVals<3, ORD>::NV;
+        float v[NV];
+        int base = -1;
+        if (rec) {
             Seg3<float> g;
             g.x0 = rec->a[0]; g.x1 = rec->a[1]; g.y0 = rec->a[2]; g.y1 = rec->a[3];
             g.z0 = rec->a[4]; g.z1 = rec->a[5]; g.i = g.j = g.k = 0;
             seg_values3<ORD>(g, rec->q, jn, v);
-        }
-        base = rec->base;
-    } else {
+            base = rec->base;
+        } else {
 #pragma unroll
-        for (int k = 0; k < NV; k++) v[k] = 0.f;
-    }
-    warp_deposit<DIM, ORD>(sJ, base, v, jsy, jsz, reduce_min, ls, jlo);
+            for (int k = 0; k < NV; k++) v[k] = 0.f;
+        }
+        warp_deposit<3, ORD>(sJ, base, v, jsy, jsz, reduce_min, ls);
     }
 }
 
 // ------------------------------------------------------------------------------------------
-// 2D segments that cross a cell face.  Few per warp iteration and scattered over the lanes,
-// they wait in a per-warp queue and are deposited 32 at a time: sorted by cell, summed per
-// cell with a segmented warp reduction, one add per cell and value.
+// 2D deposit through a per-warp scratch of segment values.  Every warp of the push CTA owns a
+// copy of the current tile (hi, with a two-sum compensation lo at offset jlo), so every add
+// below is a plain shared read-modify-write: no lane of the same instruction shares an address
+// (shared-memory FP32 atomics are compare-and-swap loops on this GPU).  Lanes write the NV
+// values of their segment as rows of the scratch (column-major: value k of row r at
+// k * SCR_LD + r, the row's stencil origin in a last column), 16 rows at a time; then lane k
+// sums column k.  The in-cell segments of a cell-sorted tile form runs of consecutive rows
+// with one stencil origin: lane k adds each run's sum once, so a warp pays one column pass
+// whatever the number of cells it covers.  Face-crossing segments (scattered, few) wait in a
+// per-warp queue and are added row by row, 32 at a time.
 // ------------------------------------------------------------------------------------------
+constexpr int SCR_ROWS = 16;
+constexpr int SCR_LD = 20;   // column stride: 16-byte aligned, 5 16-byte units (bank spread)
+
+// floats of one warp's scratch (NV value columns and the stencil-origin column)
+template <int ORD>
+constexpr int scratch_floats2() { return (SegVals<2, ORD>::NV + 1) * SCR_LD; }
+
+// offsets (from a stencil origin) of the columns this lane sums: lane, lane + 32, ...
+template <int ORD> struct ColSlots {
+    static constexpr int NV = SegVals<2, ORD>::NV;
+    static constexpr int NC = (NV + 31) / 32;
+    int off[NC];
+    __device__ __forceinline__ void init(int jsy)
+    {
+        const int lane = (int)(threadIdx.x & 31);
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+            off[c] = lane + 32 * c < NV ? seg_offset<2, ORD>(lane + 32 * c, jsy, 0) : 0;
+    }
+};
+
+// lanes 16 h .. 16 h + 15 write their values and stencil origin as rows 0..15
+template <int ORD>
+__device__ __forceinline__ void scratch_half2(float *scr, int h, int base, const float *v)
+{
+    constexpr int NV = SegVals<2, ORD>::NV;
+    const int lane = (int)(threadIdx.x & 31);
+    if ((lane >> 4) == h) {
+        const int r = lane & 15;
+#pragma unroll
+        for (int k = 0; k < NV; k++) scr[k * SCR_LD + r] = v[k];
+        reinterpret_cast<int *>(scr + NV * SCR_LD)[r] = base;
+    }
+}
+
+// In-cell segments of the warp (one per lane; base = stencil origin, -1 = none; v = values):
+// runs of equal base in lane order are summed per column and added once per run into the
+// warp's current tile.  A half of 16 rows inside one run is summed as a pairwise tree (so a
+// run of 2^k equal values sums exactly), rows around a run boundary one by one.  Must be
+// called by all 32 lanes.
+template <int ORD>
+__device__ __forceinline__ void cell_runs_deposit2(float *sJ, int jlo, float *scr, int base,
+                                                   const float *v, const ColSlots<ORD> &cs)
+{
+    constexpr int NV = SegVals<2, ORD>::NV;
+    constexpr int NC = ColSlots<ORD>::NC;
+    const int lane = (int)(threadIdx.x & 31);
+    const int prev = __shfl_up_sync(FULL_MASK, base, 1);
+    // bit r (r < 31): row r is the last of its run; row 31 ends the last run
+    const unsigned ends = __ballot_sync(FULL_MASK, lane > 0 && prev != base) >> 1;
+    const int last = __shfl_sync(FULL_MASK, base, 31);
+    const int *sb = reinterpret_cast<const int *>(scr + NV * SCR_LD);
+    float acc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) acc[c] = 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        scratch_half2<ORD>(scr, h, base, v);
+        __syncwarp();
+        const unsigned eh = (ends >> (SCR_ROWS * h)) & 0xffffu;
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const int col = lane + 32 * c;
+            if (col < NV) {
+                const float *cv = scr + col * SCR_LD;
+                const float4 *cv4 = reinterpret_cast<const float4 *>(cv);
+                if (eh == 0) {
+                    const float4 x0 = cv4[0], x1 = cv4[1], x2 = cv4[2], x3 = cv4[3];
+                    const float b0 = (x0.x + x0.y) + (x0.z + x0.w);
+                    const float b1 = (x1.x + x1.y) + (x1.z + x1.w);
+                    const float b2 = (x2.x + x2.y) + (x2.z + x2.w);
+                    const float b3 = (x3.x + x3.y) + (x3.z + x3.w);
+                    acc[c] += (b0 + b1) + (b2 + b3);
+                } else {
+                    float *hj = sJ + cs.off[c];
+                    float a = acc[c];
+#pragma unroll 1
+                    for (int b = 0; b < SCR_ROWS / 4; b++) {
+                        const unsigned e = (eh >> (4 * b)) & 0xfu;
+                        if (e == 0) {
+                            const float4 x = cv4[b];
+                            a += (x.x + x.y) + (x.z + x.w);
+                        } else {
+#pragma unroll 1
+                            for (int i = 0; i < 4; i++) {
+                                a += cv[4 * b + i];
+                                if (e & (1u << i)) {
+                                    const int key = sb[4 * b + i];
+                                    if (key >= 0) comp_add(hj + key, hj + jlo + key, a);
+                                    a = 0.f;
+                                }
+                            }
+                        }
+                    }
+                    acc[c] = a;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (last >= 0) {
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            float *hj = sJ + cs.off[c] + last;
+            if (lane + 32 * c < NV) comp_add(hj, hj + jlo, acc[c]);
+        }
+    }
+}
+
 template <int ORD>
 __device__ __forceinline__ Seg2<float> seg2_of(const SegRec &r)
 {
@@ -518,44 +610,9 @@ __device__ __forceinline__ Seg2<float> seg2_of(const SegRec &r)
     return g;
 }
 
-// Segmented warp sum of one 2D segment's values per lane: lanes with equal `base` form
-// contiguous groups (the lanes are sorted by cell); the first lane of each group adds the
-// group's sums to the shared tile at `base` (-1: lanes without a segment).  Must be called by
-// all 32 lanes.
-template <int ORD>
-__device__ __forceinline__ void flush_runs2(float *sJ, float *acc, int base, int jsy)
-{
-    constexpr int NV = SegVals<2, ORD>::NV;
-    const int lane = (int)(threadIdx.x & 31);
-    const int prev = __shfl_up_sync(FULL_MASK, base, 1);
-    const bool head = lane == 0 || prev != base;
-    const unsigned heads = __ballot_sync(FULL_MASK, head);
-    const unsigned above = lane == 31 ? 0u : (heads & (0xffffffffu << (lane + 1)));
-    const int seg_end = above ? __ffs(above) - 1 : 32;
-    // after the step with distance o, a lane holds the sum over [lane, lane + 2o) of its group
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const bool take = lane + o < seg_end;
-        if (!__any_sync(FULL_MASK, take)) break;
-#pragma unroll
-        for (int i = 0; i < NV; i++) {
-            const float t = __shfl_down_sync(FULL_MASK, acc[i], o);
-            if (take) acc[i] += t;
-        }
-    }
-    if (head && base >= 0) {
-        float *pj = sJ + base;
-#pragma unroll
-        for (int i = 0; i < NV; i++) atomicAdd(pj + seg_offset<2, ORD>(i, jsy, 0), acc[i]);
-    }
-}
-
-// Per-warp queue (shared memory) of 2D segments waiting to be deposited by a full warp: the
-// segments that do not go to a lane's register sum (face crossings, particles of a run that
-// passed into the next cell, arrivals) are few per iteration and scattered over the lanes;
-// queued, they are deposited 32 at a time with every lane busy.  Crossings of one cell mostly
-// land in the same neighbour cell, so a batch is first sorted by cell (warp bitonic sort) and
-// summed per cell with the segmented reduction; one lane per cell adds to the shared tile.
+// Per-warp queue (shared memory) of 2D face-crossing segments waiting to be deposited by a
+// full warp: few per iteration and scattered over the lanes; queued, their values are
+// computed 32 at a time with every lane busy.
 constexpr int SEGQ = 64;
 
 // append r for every lane with put; qn (warp-uniform) is the queue length
@@ -567,50 +624,53 @@ __device__ __forceinline__ void segq_push(SegRec *sq, int &qn, bool put, const S
     qn += __popc(m);
 }
 
-// ascending sort of one int per lane across the warp (bitonic network, 15 exchange steps)
-__device__ __forceinline__ int warp_sort32(int v)
-{
-    const int lane = (int)(threadIdx.x & 31);
-#pragma unroll
-    for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            const int o = __shfl_xor_sync(FULL_MASK, v, j);
-            const bool keep_min = ((lane & k) == 0) == ((lane & j) == 0);
-            v = keep_min ? min(v, o) : max(v, o);
-        }
-    }
-    return v;
-}
-
-// deposit the top 32 entries while at least nmin (>= 1) are queued
+// deposit the top 32 entries while at least nmin (>= 1) are queued: values into the scratch,
+// then row by row, lane k adding value k of the row (distinct addresses within every add;
+// plain FP32 adds: the crossings carry a small part of the current, and compensating them
+// measured 2.4% slower)
 // (kept out of line: it runs on a fraction of the iterations and its code would otherwise
 //  enlarge the particle loop)
 template <int ORD>
 __device__ __noinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int nmin,
-                                        const float *jn, int jsy)
+                                        const float *jn, float *scr, const ColSlots<ORD> &cs)
 {
     constexpr int NV = SegVals<2, ORD>::NV;
     const int lane = (int)(threadIdx.x & 31);
+    const int *sb = reinterpret_cast<const int *>(scr + NV * SCR_LD);
     while (qn >= nmin) {
         const int take = qn < 32 ? qn : 32, first = qn - take;
         __syncwarp();
-        // key = stencil origin * 32 + entry (unique); idle lanes sort last
-        const int key = warp_sort32(lane < take ? sq[first + lane].base * 32 + lane : INT_MAX);
-        const bool act = key != INT_MAX;
         float v[NV];
         int base = -1;
-        if (act) {
-            const SegRec r = sq[first + (key & 31)];
+        if (lane < take) {
+            const SegRec r = sq[first + lane];
             seg_values2<ORD>(seg2_of<ORD>(r), r.q, jn[0], jn[1], v);
             base = r.base;
         } else {
 #pragma unroll
             for (int i = 0; i < NV; i++) v[i] = 0.f;
         }
-        __syncwarp();
         qn = first;
-        flush_runs2<ORD>(sJ, v, base, jsy);
+#pragma unroll 1
+        for (int h = 0; 16 * h < take; h++) {
+            __syncwarp();
+            scratch_half2<ORD>(scr, h, base, v);
+            __syncwarp();
+            const int rows = min(take - 16 * h, 16);
+#pragma unroll
+            for (int c = 0; c < ColSlots<ORD>::NC; c++) {
+                const int col = lane + 32 * c;
+                if (col < NV) {
+                    const float *cv = scr + col * SCR_LD;
+                    float *hj = sJ + cs.off[c];
+#pragma unroll 1
+                    for (int r = 0; r < rows; r++) {
+                        hj[sb[r]] += cv[r];
+                    }
+                }
+            }
+        }
+        __syncwarp();
     }
 }
 

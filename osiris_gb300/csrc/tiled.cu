@@ -171,11 +171,18 @@ static size_t smem_for(int dim, int order, const int *T, int threads)
         ne *= (size_t)(T[d] + NP);
         nj *= (size_t)(T[d] + NP + 1);
     }
-    // 2D: one copy per warp, each with its two-sum compensation
-    const size_t copies = dim == 2 ? 2 * (size_t)threads / 32 : 1;
+    // 2D: one copy of the current tile per warp, each with its two-sum compensation, then per
+    // warp a value scratch and a queue of face-crossing segments; last the cell histogram
+    const size_t warps = (size_t)threads / 32;
+    const size_t copies = dim == 2 ? 2 * warps : 1;
     const size_t nf = (6 * ne + 3 * nj * copies + 3) & ~(size_t)3;
-    const size_t queues = dim == 2 ? (size_t)(threads / 32) * SEGQ * sizeof(SegRec) : 0;
-    return nf * sizeof(float) + queues;
+    size_t cells = 1;
+    for (int d = 0; d < dim; d++) cells *= (size_t)T[d];
+    const size_t hist = 2 * cells * sizeof(int);
+    if (dim != 2) return nf * sizeof(float) + hist;
+    const int nv = 2 * order * NP + NP * NP;
+    const size_t scratch = warps * (size_t)(nv + 1) * SCR_LD * sizeof(float);
+    return nf * sizeof(float) + scratch + warps * SEGQ * sizeof(SegRec) + hist;
 }
 
 int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
@@ -336,6 +343,11 @@ int tiled_add_species(TiledState *t, double rqm, long np, const int *ix, const f
     long cap = (long)std::ceil(std::max(t->capacity * mean, 1.25 * cmax)) + 64;
     if (k < (int)t->min_cap.size()) cap = std::max(cap, t->min_cap[k]);
     cap = (cap + 31) / 32 * 32;
+    if (cap > MAX_TILE_SLOTS) {
+        set_error("%ld particle slots per tile exceed the tile sort's limit of %ld: use smaller "
+                  "tiles", cap, MAX_TILE_SLOTS);
+        return OSG_ERR_ARG;
+    }
     // stable counting sort by key -> slab slot of every particle
     std::vector<long> dst(np);
     {

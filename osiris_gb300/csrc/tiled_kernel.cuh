@@ -60,6 +60,9 @@ struct TiledArgs {
 
 static const int MAX_TILED_SPECIES = 16;
 static const int MAX_TILE_CELLS = 1024;   // cells per tile (bins of the per-tile cell sort)
+// the sort key a stayer carries between the two passes: 1 + cell in the tile + rank << bits
+static const int SORT_CELL_BITS = 10;
+static const long MAX_TILE_SLOTS = (1L << (31 - SORT_CELL_BITS)) - 1;   // ranks that fit
 
 __device__ __forceinline__ int wrapc(int c, int n)
 {
@@ -89,7 +92,7 @@ __device__ __forceinline__ int warp_exclusive_scan(int *c, int n)
 }
 
 // --------------------------------------------------------------------------------- push
-static const int LEAVE_QUEUE = 256;   // particles per CTA and species queued for emigration
+static const int LEAVE_QUEUE = 128;   // particles per CTA and species queued for emigration
 
 // Write a particle that left its tile into an arrival slot (from the top of the slab) of its
 // destination tile in the output buffer.  The arrival region stays above the particles the
@@ -120,9 +123,9 @@ __device__ __forceinline__ void emigrate(const SpeciesDev &sd, long cap, long de
 // Every warp of the CTA runs its own pipeline over chunks of 32 particles of the tile, with no
 // block barrier inside the particle loop: load, gather, Boris, move, split, write the particle
 // to its new slot, then deposit the segments (round t takes the t-th segment of every lane).
-// In 2D every warp accumulates into its own copy of the current tile, so the warp-reduced
-// passes add with plain shared read-modify-writes; the copies are summed when the tile is
-// flushed.  In 3D the warps share one current tile (atomic adds).
+// In 2D every warp accumulates into its own copy of the current tile (with a two-sum
+// compensation), so its adds are plain shared read-modify-writes; the copies are summed when
+// the tile is flushed.  In 3D the warps share one current tile (atomic adds).
 // CTAs of up to 256 threads.  2D linear/quadratic: three resident CTAs per SM (at most 85
 // registers per thread, measured fastest on GB300); 2D quartic: one (it needs ~250 registers
 // without spilling); otherwise two
@@ -136,7 +139,6 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
 {
     constexpr int NP = ORD + 1, OFS = Stencil<ORD>::OFS;
     constexpr int MAXSEG = DIM == 2 ? 3 : 4;
-    constexpr bool PRIV = private_current<DIM>();
     extern __shared__ float smem[];
     int t0[3], tc[3];
     tc[0] = (int)(tile % a.ntile[0]);
@@ -154,9 +156,9 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     }
     const int ne = ee[0] * ee[1] * ee[2], nj = je[0] * je[1] * je[2];
     const int nthr = blockDim.x, nwarp = nthr >> 5, warp = threadIdx.x >> 5;
-    const int njall = 3 * nj * (PRIV ? nwarp : 1);
+    const int njall = 3 * nj * (DIM == 2 ? nwarp : 1);
     // 2D: the warp copies of the current tile keep a two-sum compensation at offset jlo
-    const int jlo = PRIV ? njall : 0;
+    const int jlo = DIM == 2 ? njall : 0;
     float *sE = smem, *sB = smem + 3 * ne, *sJ = smem + 6 * ne;
     const long gsy = 3L * a.size[0], gsz = 3L * a.size[0] * a.size[1];
 
@@ -172,30 +174,40 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
         sB[idx] = __ldg(a.b + gp);
     }
     for (int idx = threadIdx.x; idx < njall + jlo; idx += nthr) sJ[idx] = 0.0f;
-    __syncthreads();
-
-    const int esy = 3 * ee[0], esz = 3 * ee[0] * ee[1];
-    const int jsy = 3 * je[0], jsz = 3 * je[0] * je[1];
-    const unsigned lane = threadIdx.x & 31;
-    float *sJw = PRIV ? sJ + 3 * nj * warp : sJ;
-    LaneSlots<DIM, ORD> ls;
-    ls.init(jsy, jsz);
-    // 3D direct deposits: every thread walks its own contiguous run of the cell-sorted tile,
-    // so the lanes of a warp sit in cells far apart and their shared-memory atomics seldom
-    // conflict; otherwise a warp takes 32 consecutive particles (mostly one cell)
-    const bool spread = DIM == 3 && (direct_only<DIM, ORD>() || a.reduce_min > 32);
-
-    __shared__ int sHist[MAX_TILE_CELLS];
+    // dynamic shared memory after the current tile (16-byte aligned): 2D per-warp value scratch
+    // and queue of face-crossing segments, then two per-cell histograms of the tile sort (one
+    // per species, alternating, so the next one is cleared while the current one is used)
+    float *scr = smem + ((6 * ne + njall + jlo + 3) & ~3);
+    SegRec *sQ0 = reinterpret_cast<SegRec *>(scr + (DIM == 2 ? nwarp * scratch_floats2<ORD>() : 0));
+    int *sHist = reinterpret_cast<int *>(sQ0 + (DIM == 2 ? nwarp * SEGQ : 0));
+    const int ncell = a.T[0] * a.T[1] * a.T[2];
+    for (int k = threadIdx.x; k < ncell; k += nthr) sHist[k] = 0;
     // particles leaving the tile wait in a shared queue; after the pass they take their
     // arrival slots all at once, so no warp waits on a global atomic inside the pass
     __shared__ int sLeaveI[LEAVE_QUEUE][4];      // new cell per axis, destination tile
     __shared__ float sLeaveF[LEAVE_QUEUE][8];    // offsets per axis, momenta, charge
     __shared__ int sNleave;
-    // 2D: per-warp queues of segments for full-warp deposits (dynamic shared memory after the
-    // current tile, 16-byte aligned)
-    SegRec *sQ = reinterpret_cast<SegRec *>(smem + ((6 * ne + njall + jlo + 3) & ~3)) + warp * SEGQ;
+    // per-warp energy of every species, summed when the tile is done
+    __shared__ double sEne[MAX_TILED_SPECIES][8];
+    if (threadIdx.x == 0) sNleave = 0;
+    __syncthreads();
+
+    const int esy = 3 * ee[0], esz = 3 * ee[0] * ee[1];
+    const int jsy = 3 * je[0], jsz = 3 * je[0] * je[1];
+    const unsigned lane = threadIdx.x & 31;
+    float *sJw = DIM == 2 ? sJ + 3 * nj * warp : sJ;
+    LaneSlots<DIM, ORD> ls;
+    ColSlots<ORD> cs;
+    if constexpr (DIM == 3) ls.init(jsy, jsz);
+    else cs.init(jsy);
+    // 3D direct deposits: every thread walks its own contiguous run of the cell-sorted tile,
+    // so the lanes of a warp sit in cells far apart and their shared-memory atomics seldom
+    // conflict; otherwise a warp takes 32 consecutive particles (mostly one cell)
+    const bool spread = DIM == 3 && (direct_only<DIM, ORD>() || a.reduce_min > 32);
+
+    SegRec *sQ = sQ0 + warp * SEGQ;
+    scr += warp * scratch_floats2<ORD>();
     int qn = 0;
-    const int ncell = a.T[0] * a.T[1] * a.T[2];
 
     for (int s = 0; s < a.nspec; s++) {
         const SpeciesDev sd = a.spec[s];
@@ -204,14 +216,14 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
         const int nst = min(sd.in.cnt[tile], (int)cap);
         const int nar = min(sd.in.arr[tile], (int)cap - nst);
         const int n = nst + nar;
-        for (int k = threadIdx.x; k < ncell; k += nthr) sHist[k] = 0;
-        if (threadIdx.x == 0) sNleave = 0;
-        __syncthreads();
+        int *hist = sHist + (s & 1) * ncell;
         // per-thread partial energy in FP32 (the reference sums in single precision per
         // 464-particle chunk), summed over the block in double
         float my_ene = 0.f;
         // ---- pass A: push every particle of the tile.  Particles that stay are written back
-        //      to their own slot of the input slab (this CTA owns it) and counted per new cell;
+        //      to their own slot of the input slab (this CTA owns it) and counted per new cell,
+        //      their sort key (new cell in the tile, rank among that cell's stayers) in place
+        //      of the first cell index;
         //      particles that leave take an arrival slot (from the top) of their destination
         //      tile in the output buffer, and their input slot is marked empty (ix = 0).
         auto slot = [&](int i) { return slab + (i < nst ? i : cap - 1 - (i - nst)); };
@@ -338,20 +350,27 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
             const bool stay = has && dest == tile;
             int lcell = -1;
             if (stay) {
-#pragma unroll
-                for (int d = 0; d < DIM; d++) {
-                    sd.in.ix[d][p] = cw[d];
-                    sd.in.x[d][p] = xo[d];
-                }
-                sd.in.u[0][p] = un[0];
-                sd.in.u[1][p] = un[1];
-                sd.in.u[2][p] = un[2];
                 lcell = cw[0] - t0[0];
                 if (DIM > 1) lcell += a.T[0] * (cw[1] - t0[1]);
                 if (DIM > 2) lcell += a.T[0] * a.T[1] * (cw[2] - t0[2]);
             }
             const unsigned peers = __match_any_sync(FULL_MASK, lcell);
-            if (stay && (int)lane == __ffs(peers) - 1) atomicAdd(&sHist[lcell], __popc(peers));
+            const int pl = __ffs(peers) - 1;
+            int first = 0;
+            if (stay && (int)lane == pl) first = atomicAdd(&hist[lcell], __popc(peers));
+            first = __shfl_sync(FULL_MASK, first, pl);
+            if (stay) {
+                const int rank = first + __popc(peers & ((1u << lane) - 1u));
+                sd.in.ix[0][p] = 1 + lcell + (rank << SORT_CELL_BITS);
+#pragma unroll
+                for (int d = 0; d < DIM; d++) {
+                    if (d > 0) sd.in.ix[d][p] = cw[d];
+                    sd.in.x[d][p] = xo[d];
+                }
+                sd.in.u[0][p] = un[0];
+                sd.in.u[1][p] = un[1];
+                sd.in.u[2][p] = un[2];
+            }
             const bool leave = has && !stay;
             const unsigned ml = __ballot_sync(FULL_MASK, leave);
             if (ml) {
@@ -391,92 +410,142 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
             take(c, xo, un, q);
             if (it + 1 < nit) prefetch(index(it + 1), n);
             const int ns = push_one(i < n, slot(i), c, xo, un, q, sg);
-            // ---- charge-conserving current of the segments into the shared tile.  The first
-            //      segment (in the particle's own cell, shared by neighbouring lanes of the
-            //      cell-sorted tile) is warp-reduced per cell; in 2D the others (face
-            //      crossings, few and scattered) wait in the warp's queue for a full-warp,
-            //      cell-sorted deposit
+            // ---- charge-conserving current of the segments into the shared tile.  2D: the
+            //      first segment (in the particle's own cell, shared by neighbouring lanes of
+            //      the cell-sorted tile) is summed per run of lanes with one cell; the others
+            //      (face crossings, few and scattered) wait in the warp's queue for a
+            //      full-warp deposit.  3D: one warp-cooperative deposit per round
 #pragma unroll
             for (int t = 0; t < MAXSEG; t++) {
                 const bool hs = t < ns;
-                if (DIM == 2 && t > 0) {
-                    segq_push(sQ, qn, hs, sg[t]);
-                    if (qn >= 32) segq_drain<ORD>(sJw, sQ, qn, 32, a.jn, jsy);
-                    continue;
+                if constexpr (DIM == 2) {
+                    if (t > 0) {
+                        segq_push(sQ, qn, hs, sg[t]);
+                        if (qn >= 32) segq_drain<ORD>(sJw, sQ, qn, 32, a.jn, scr, cs);
+                        continue;
+                    }
+                    if (!__any_sync(FULL_MASK, hs)) break;
+                    constexpr int NV = SegVals<2, ORD>::NV;
+                    float v[NV];
+                    if (hs) {
+                        seg_values2<ORD>(seg2_of<ORD>(sg[0]), q, a.jn[0], a.jn[1], v);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < NV; k++) v[k] = 0.f;
+                    }
+                    cell_runs_deposit2<ORD>(sJw, jlo, scr, hs ? sg[0].base : -1, v, cs);
+                } else {
+                    if (!__any_sync(FULL_MASK, hs)) break;
+                    deposit_segment3<ORD>(sJ, hs ? &sg[t] : nullptr, a.jn, jsy, jsz,
+                                          a.reduce_min, ls);
                 }
-                if (!__any_sync(FULL_MASK, hs)) break;
-                deposit_segment<DIM, ORD>(sJw, hs ? &sg[t] : nullptr, a.jn, jsy, jsz,
-                                          a.reduce_min, ls, jlo);
             }
         }
-        if (DIM == 2) segq_drain<ORD>(sJw, sQ, qn, 1, a.jn, jsy);
-        const double tot = block_sum((double)my_ene);   // (contains block barriers)
-        if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.ene + s, tot);
-        // ---- the queued particles that left take their arrival slots
+        // ---- energy: per-warp partial (the tile's sum is taken when the tile is done)
+        {
+            double w = (double)my_ene;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(FULL_MASK, w, o);
+            if (lane == 0) sEne[s][warp] = w;
+        }
+        __syncthreads();   // the histogram and the leave queue are complete
+        // ---- warp 0: cell offsets of the particles that stayed; the other warps (meanwhile):
+        //      the queued particles that left take their arrival slots; everyone: clear the
+        //      next species' histogram
         {
             const int nq = min(sNleave, LEAVE_QUEUE);
-            for (int e = threadIdx.x; e < nq; e += nthr) {
-                int cw[3];
-                float xo[3], un[3];
-#pragma unroll
-                for (int d = 0; d < 3; d++) {
-                    cw[d] = sLeaveI[e][d];
-                    xo[d] = sLeaveF[e][d];
-                    un[d] = sLeaveF[e][3 + d];
-                }
-                emigrate<DIM>(sd, cap, sLeaveI[e][3], cw, xo, un, sLeaveF[e][6], a.status);
+            if (warp == 0) {
+                const int nstay = warp_exclusive_scan(hist, ncell);
+                if (threadIdx.x == 0) sd.out.cnt[tile] = nstay;
             }
-        }
-        // ---- cell offsets of the particles that stayed
-        if (threadIdx.x < 32) {
-            const int nstay = warp_exclusive_scan(sHist, ncell);
-            if (threadIdx.x == 0) sd.out.cnt[tile] = nstay;
-        }
-        __syncthreads();
-        // ---- pass B: counting-sort the particles that stayed into the output slab, so that
-        //      every step starts from particles in cell order (consecutive lanes share a cell)
-        for (int base = 0; base < n; base += nthr) {
-            const int i = base + threadIdx.x;
-            const long p = slab + (i < nst ? i : cap - 1 - (i - nst));
-            int lcell = -1;
-            int cc[3] = {0, 0, 0};
-            if (i < n) {
+            if (warp > 0 || nwarp == 1) {
+                const int e0 = nwarp == 1 ? (int)threadIdx.x : (int)threadIdx.x - 32;
+                const int es = nwarp == 1 ? nthr : nthr - 32;
+                for (int e = e0; e < nq; e += es) {
+                    int cw[3];
+                    float xo[3], un[3];
 #pragma unroll
-                for (int d = 0; d < DIM; d++) cc[d] = sd.in.ix[d][p];
-                if (cc[0] != 0) {
-                    lcell = cc[0] - t0[0];
-                    if (DIM > 1) lcell += a.T[0] * (cc[1] - t0[1]);
-                    if (DIM > 2) lcell += a.T[0] * a.T[1] * (cc[2] - t0[2]);
+                    for (int d = 0; d < 3; d++) {
+                        cw[d] = sLeaveI[e][d];
+                        xo[d] = sLeaveF[e][d];
+                        un[d] = sLeaveF[e][3 + d];
+                    }
+                    emigrate<DIM>(sd, cap, sLeaveI[e][3], cw, xo, un, sLeaveF[e][6], a.status);
                 }
             }
-            const unsigned peers = __match_any_sync(FULL_MASK, lcell);
-            const int leader = __ffs(peers) - 1;
-            int first = 0;
-            if (lcell >= 0 && (int)lane == leader) first = atomicAdd(&sHist[lcell], __popc(peers));
-            first = __shfl_sync(FULL_MASK, first, leader);
-            if (lcell >= 0) {
-                const long o = slab + first + __popc(peers & ((1u << lane) - 1u));
-#pragma unroll
-                for (int d = 0; d < DIM; d++) {
-                    sd.out.ix[d][o] = cc[d];
-                    sd.out.x[d][o] = sd.in.x[d][p];
-                }
-                sd.out.u[0][o] = sd.in.u[0][p];
-                sd.out.u[1][o] = sd.in.u[1][p];
-                sd.out.u[2][o] = sd.in.u[2][p];
-                sd.out.q[o] = sd.in.q[p];
-            }
+            int *next = sHist + ((s + 1) & 1) * ncell;
+            for (int k = threadIdx.x; k < ncell; k += nthr) next[k] = 0;
         }
         __syncthreads();
+        // ---- pass B: counting-sort the particles that stayed into the output slab (offset of
+        //      the cell + rank from the key), so that every step starts from particles in cell
+        //      order (consecutive lanes share a cell).  No step depends on another particle:
+        //      every thread loads two particles at once
+        for (int base = 0; base < n; base += 2 * nthr) {
+            long pp[2];
+            int key[2] = {0, 0}, c1[2] = {0, 0}, c2[2] = {0, 0};
+            float xx[2][3], uu[2][3], qq[2];
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const int i = base + j * nthr + (int)threadIdx.x;
+                pp[j] = slab + (i < nst ? i : cap - 1 - (i - nst));
+                if (i < n) {
+                    key[j] = sd.in.ix[0][pp[j]];
+                    if (DIM > 1) c1[j] = sd.in.ix[1][pp[j]];
+                    if (DIM > 2) c2[j] = sd.in.ix[2][pp[j]];
+#pragma unroll
+                    for (int d = 0; d < DIM; d++) xx[j][d] = sd.in.x[d][pp[j]];
+                    uu[j][0] = sd.in.u[0][pp[j]];
+                    uu[j][1] = sd.in.u[1][pp[j]];
+                    uu[j][2] = sd.in.u[2][pp[j]];
+                    qq[j] = sd.in.q[pp[j]];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                if (key[j] > 0) {
+                    const int kc = key[j] - 1;
+                    const int lc = kc & ((1 << SORT_CELL_BITS) - 1);
+                    const long o = slab + hist[lc] + (kc >> SORT_CELL_BITS);
+                    int ly = 0;
+                    if (DIM > 1) ly = c1[j] - t0[1];
+                    if (DIM > 2) ly += a.T[1] * (c2[j] - t0[2]);
+                    sd.out.ix[0][o] = t0[0] + lc - a.T[0] * ly;
+                    if (DIM > 1) sd.out.ix[1][o] = c1[j];
+                    if (DIM > 2) sd.out.ix[2][o] = c2[j];
+#pragma unroll
+                    for (int d = 0; d < DIM; d++) sd.out.x[d][o] = xx[j][d];
+                    sd.out.u[0][o] = uu[j][0];
+                    sd.out.u[1][o] = uu[j][1];
+                    sd.out.u[2][o] = uu[j][2];
+                    sd.out.q[o] = qq[j];
+                }
+            }
+        }
+        if (threadIdx.x == 0) sNleave = 0;
+        __syncthreads();
+    }
+    // ---- the face crossings still queued (the queue carries over from one species to the
+    //      next: its entries hold their own charge)
+    if constexpr (DIM == 2) {
+        segq_drain<ORD>(sJw, sQ, qn, 1, a.jn, scr, cs);
+        __syncthreads();
+    }
+    // ---- the tile's energy of every species (the per-warp partials, written before the last
+    //      block barrier)
+    if ((int)threadIdx.x < a.nspec) {
+        double tot = 0.0;
+        for (int w = 0; w < nwarp; w++) tot += sEne[threadIdx.x][w];
+        if (tot != 0.0) atomicAdd(a.ene + threadIdx.x, tot);
     }
     // ---- store the tile's current (with halo) for the tile-ordered FP64 re-summation: in 2D
     //      the warp copies and their compensations are summed in double and kept as a float
     //      pair (hi, lo); in 3D the single shared tile is stored as it is
     {
         float *th = a.tile_hi + tile * (3L * nj);
-        float *tl = PRIV ? a.tile_lo + tile * (3L * nj) : nullptr;
+        float *tl = DIM == 2 ? a.tile_lo + tile * (3L * nj) : nullptr;
         for (int idx = threadIdx.x; idx < 3 * nj; idx += nthr) {
-            if (PRIV) {
+            if constexpr (DIM == 2) {
                 double v = 0.0;
                 for (int w = 0; w < nwarp; w++)
                     v += (double)sJ[3 * nj * w + idx] + (double)sJ[jlo + 3 * nj * w + idx];
