@@ -106,6 +106,45 @@ __device__ __forceinline__ void gather_tile(const float *sE, const float *sB, in
     }
 }
 
+// 2D gather with paired FP32 FMAs (sm_100+ FFMA2: two independent IEEE fmas per instruction):
+// the six components share their stencils in pairs -- (E1, B2) weights (wh, w) in (x, y) and
+// the same points, (E2, B1) weights (w, wh) and the same points, (E3, B3) -- so every pair is
+// one paired fma per stencil point.  Same roundings as gather_tile.
+template <int ORD>
+__device__ __forceinline__ void gather_tile2_paired(const float *sE, const float *sB, int esy,
+                                                    const int *lf, const int *lh,
+                                                    const float (*w)[ORD + 1],
+                                                    const float (*wh)[ORD + 1], float &E1,
+                                                    float &E2, float &E3, float &B1, float &B2,
+                                                    float &B3)
+{
+    constexpr int NP = ORD + 1;
+    float2 eb12 = make_float2(0.f, 0.f);   // (E1, B2)
+    float2 eb21 = make_float2(0.f, 0.f);   // (E2, B1)
+    float2 eb33 = make_float2(0.f, 0.f);   // (E3, B3)
+#pragma unroll
+    for (int k2 = 0; k2 < NP; k2++) {
+        float2 f12 = make_float2(0.f, 0.f), f21 = make_float2(0.f, 0.f), f33 = make_float2(0.f, 0.f);
+        const int rf = esy * (lf[1] + k2), rh = esy * (lh[1] + k2);
+#pragma unroll
+        for (int k1 = 0; k1 < NP; k1++) {
+            const int xh = 3 * (lh[0] + k1), xf = 3 * (lf[0] + k1);
+            f12 = __ffma2_rn(make_float2(sE[xh + rf + 0], sB[xh + rf + 1]),
+                             make_float2(wh[0][k1], wh[0][k1]), f12);
+            f21 = __ffma2_rn(make_float2(sE[xf + rh + 1], sB[xf + rh + 0]),
+                             make_float2(w[0][k1], w[0][k1]), f21);
+            f33 = __ffma2_rn(make_float2(sE[xf + rf + 2], sB[xh + rh + 2]),
+                             make_float2(w[0][k1], wh[0][k1]), f33);
+        }
+        eb12 = __ffma2_rn(f12, make_float2(w[1][k2], w[1][k2]), eb12);
+        eb21 = __ffma2_rn(f21, make_float2(wh[1][k2], wh[1][k2]), eb21);
+        eb33 = __ffma2_rn(f33, make_float2(w[1][k2], wh[1][k2]), eb33);
+    }
+    E1 = eb12.x; B2 = eb12.y;
+    E2 = eb21.x; B1 = eb21.y;
+    E3 = eb33.x; B3 = eb33.y;
+}
+
 // ------------------------------------------------------------------------------------------
 // Current values of one segment, in a fixed order; seg_offset maps a value index to its
 // offset (in floats) from the stencil origin of the segment's cell in the shared tile.

@@ -102,8 +102,9 @@ __device__ __forceinline__ void emigrate(const SpeciesDev &sd, long cap, long de
                                          const int *cw, const float *xo, const float *un,
                                          float q, int *status)
 {
-    const int k = atomicAdd(sd.out.arr + dest, 1);
+    // (the destination's input counts are loaded before the atomic: one round trip for both)
     const int room = (int)cap - sd.in.cnt[dest] - sd.in.arr[dest];
+    const int k = atomicAdd(sd.out.arr + dest, 1);
     if (k >= room) {
         atomicOr(status, OSG_STATUS_OVERFLOW);
         return;
@@ -288,7 +289,10 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                     spline_h<ORD>(xo[d], neg ? 1.0f : 0.0f, wh[d]);
                 }
                 float E1, E2, E3, B1, B2, B3;
-                gather_tile<DIM, ORD>(sE, sB, esy, esz, lf, lh, w, wh, E1, E2, E3, B1, B2, B3);
+                if constexpr (DIM == 2)
+                    gather_tile2_paired<ORD>(sE, sB, esy, lf, lh, w, wh, E1, E2, E3, B1, B2, B3);
+                else
+                    gather_tile<DIM, ORD>(sE, sB, esy, esz, lf, lh, w, wh, E1, E2, E3, B1, B2, B3);
                 if constexpr (PUSHER == OSG_PUSHER_EXACT) {
                     my_ene += exact_push<float>(sd.qm, a.dt_full, a.iter_tol, E1, E2, E3, B1,
                                                 B2, B3, q, un[0], un[1], un[2]);
@@ -507,27 +511,40 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
             for (int k = threadIdx.x; k < ncell; k += nthr) next[k] = 0;
         }
         __syncthreads();
-        // ---- pass B
+        // ---- pass B (the next particles are loaded before the current ones are stored)
         for (int base = 0; base < n; base += PB * nthr) {
-            if (base > 0) pb_load(base);
+            int ck[PB], cc1[PB], cc2[PB];
+            float cx[PB][DIM], cu[PB][3], cq[PB];
 #pragma unroll
             for (int j = 0; j < PB; j++) {
-                if (key[j] > 0) {
-                    const int kc = key[j] - 1;
+                ck[j] = key[j];
+                cc1[j] = c1[j];
+                cc2[j] = c2[j];
+#pragma unroll
+                for (int d = 0; d < DIM; d++) cx[j][d] = xx[j][d];
+#pragma unroll
+                for (int d = 0; d < 3; d++) cu[j][d] = uu[j][d];
+                cq[j] = qq[j];
+            }
+            if (base + PB * nthr < n) pb_load(base + PB * nthr);
+#pragma unroll
+            for (int j = 0; j < PB; j++) {
+                if (ck[j] > 0) {
+                    const int kc = ck[j] - 1;
                     const int lc = kc & ((1 << SORT_CELL_BITS) - 1);
                     const long o = slab + hist[lc] + (kc >> SORT_CELL_BITS);
                     int ly = 0;
-                    if (DIM > 1) ly = c1[j] - t0[1];
-                    if (DIM > 2) ly += a.T[1] * (c2[j] - t0[2]);
+                    if (DIM > 1) ly = cc1[j] - t0[1];
+                    if (DIM > 2) ly += a.T[1] * (cc2[j] - t0[2]);
                     sd.out.ix[0][o] = t0[0] + lc - a.T[0] * ly;
-                    if (DIM > 1) sd.out.ix[1][o] = c1[j];
-                    if (DIM > 2) sd.out.ix[2][o] = c2[j];
+                    if (DIM > 1) sd.out.ix[1][o] = cc1[j];
+                    if (DIM > 2) sd.out.ix[2][o] = cc2[j];
 #pragma unroll
-                    for (int d = 0; d < DIM; d++) sd.out.x[d][o] = xx[j][d];
-                    sd.out.u[0][o] = uu[j][0];
-                    sd.out.u[1][o] = uu[j][1];
-                    sd.out.u[2][o] = uu[j][2];
-                    sd.out.q[o] = qq[j];
+                    for (int d = 0; d < DIM; d++) sd.out.x[d][o] = cx[j][d];
+                    sd.out.u[0][o] = cu[j][0];
+                    sd.out.u[1][o] = cu[j][1];
+                    sd.out.u[2][o] = cu[j][2];
+                    sd.out.q[o] = cq[j];
                 }
             }
         }
