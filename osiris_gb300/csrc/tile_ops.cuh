@@ -191,6 +191,43 @@ __device__ __forceinline__ void seg_values2(const Seg2<float> &g, float q, float
         }
 }
 
+// The same values for the mixed-precision (tiled) engine with fewer operations: the j3 term
+// qvz (s0x s0y + s1x s1y + (s0x s1y + s1x s0y) / 2) is factored as s0x A + s1x B with
+// A = qvz (s0y + s1y / 2), B = qvz (s1y + s0y / 2) (two operations per value instead of six;
+// the roundings differ from the reference's order by a few float ulps).
+template <int ORD>
+__device__ __forceinline__ void seg_values2_fast(const Seg2<float> &g, float q, float jn0,
+                                                 float jn1, float *v)
+{
+    constexpr int NP = ORD + 1;
+    float s0x[NP], s1x[NP], s0y[NP], s1y[NP], wl1[ORD], wl2[ORD];
+    spline<ORD>(g.x0, s0x);
+    spline<ORD>(g.x1, s1x);
+    spline<ORD>(g.y0, s0y);
+    spline<ORD>(g.y1, s1y);
+    const float qvz = (q * g.vz) * float(1.0 / 3.0);
+    long_weights<ORD>(q * jn0, g.x0, g.x1, wl1);
+    long_weights<ORD>(q * jn1, g.y0, g.y1, wl2);
+    int n = 0;
+#pragma unroll
+    for (int k2 = 0; k2 < NP; k2++) {
+        const float wp1 = s0y[k2] + s1y[k2];
+#pragma unroll
+        for (int k1 = 0; k1 < ORD; k1++) v[n++] = wl1[k1] * wp1;
+    }
+#pragma unroll
+    for (int k2 = 0; k2 < ORD; k2++)
+#pragma unroll
+        for (int k1 = 0; k1 < NP; k1++) v[n++] = wl2[k2] * (s0x[k1] + s1x[k1]);
+#pragma unroll
+    for (int k2 = 0; k2 < NP; k2++) {
+        const float A = qvz * fmaf(0.5f, s1y[k2], s0y[k2]);
+        const float B = qvz * fmaf(0.5f, s0y[k2], s1y[k2]);
+#pragma unroll
+        for (int k1 = 0; k1 < NP; k1++) v[n++] = fmaf(s1x[k1], B, s0x[k1] * A);
+    }
+}
+
 template <int ORD>
 __device__ __forceinline__ void seg_values3(const Seg3<float> &g, float q, const float *jn,
                                             float *v)
@@ -683,7 +720,7 @@ __device__ __noinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int nmin
         int base = -1;
         if (lane < take) {
             const SegRec r = sq[first + lane];
-            seg_values2<ORD>(seg2_of<ORD>(r), r.q, jn[0], jn[1], v);
+            seg_values2_fast<ORD>(seg2_of<ORD>(r), r.q, jn[0], jn[1], v);
             base = r.base;
         } else {
 #pragma unroll
@@ -703,9 +740,7 @@ __device__ __noinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int nmin
                     const float *cv = scr + col * SCR_LD;
                     float *hj = sJ + cs.off[c];
 #pragma unroll 1
-                    for (int r = 0; r < rows; r++) {
-                        hj[sb[r]] += cv[r];
-                    }
+                    for (int r = 0; r < rows; r++) hj[sb[r]] += cv[r];
                 }
             }
         }

@@ -432,7 +432,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                     constexpr int NV = SegVals<2, ORD>::NV;
                     float v[NV];
                     if (hs) {
-                        seg_values2<ORD>(seg2_of<ORD>(sg[0]), q, a.jn[0], a.jn[1], v);
+                        seg_values2_fast<ORD>(seg2_of<ORD>(sg[0]), q, a.jn[0], a.jn[1], v);
                     } else {
 #pragma unroll
                         for (int k = 0; k < NV; k++) v[k] = 0.f;
