@@ -373,6 +373,12 @@ int tiled_add_species(TiledState *t, double rqm, long np, const int *ix, const f
             return OSG_ERR_NOMEM;
         }
         t->allocs.push_back(mem);
+        // every tile's slab of every array starts on a 128-byte line (the push drops dead
+        // lines from L2 by address)
+        if (((uintptr_t)mem & 127) != 0 || (nslot * sizeof(float)) % 128 != 0 || cap % 32 != 0) {
+            set_error("particle slabs are not aligned to 128-byte lines");
+            return OSG_ERR_CUDA;
+        }
         size_t o = 0;
         for (int d = 0; d < dim; d++) {
             s.ix[d] = (int *)(mem + o); o += nslot * 4;

@@ -121,6 +121,32 @@ __device__ __forceinline__ void emigrate(const SpeciesDev &sd, long cap, long de
     sd.out.q[o] = q;
 }
 
+// After the sort, a tile's input slab is dead until the next step writes it as its output:
+// the cache lines the first pass dirtied (stayers written back to their own slots, [0, nst)
+// and the arrival region [cap - nar, cap)) are dropped from L2 without a write-back to DRAM.
+// A tile's slab of every array starts on a 128-byte line and spans whole lines (cap is a
+// multiple of 32 slots, every array of the allocation a multiple of 32 slots per tile).
+template <int DIM>
+__device__ __forceinline__ void discard_dead_slab(const Slabs &in, long slab, int nst, int nar,
+                                                  long cap)
+{
+    const int lo_lines = (nst + 31) >> 5;
+    const int cap_lines = (int)(cap >> 5);
+    const int hi_first = max((int)((cap - nar) >> 5), lo_lines);
+    const int nl = lo_lines + (nar > 0 ? cap_lines - hi_first : 0);
+    constexpr int NA = 2 * DIM + 3;   // ix, x and u are written back; q is not
+#pragma unroll
+    for (int arr = 0; arr < NA; arr++) {
+        const float *base = arr < DIM ? reinterpret_cast<const float *>(in.ix[arr])
+                                      : (arr < 2 * DIM ? in.x[arr - DIM] : in.u[arr - 2 * DIM]);
+        for (int l0 = threadIdx.x; l0 < nl; l0 += blockDim.x) {
+            const int line = l0 < lo_lines ? l0 : hi_first + (l0 - lo_lines);
+            const float *pa = base + slab + 32L * line;
+            asm volatile("discard.global.L2 [%0], 128;" ::"l"(pa) : "memory");
+        }
+    }
+}
+
 // Every warp of the CTA runs its own pipeline over chunks of 32 particles of the tile, with no
 // block barrier inside the particle loop: load, gather, Boris, move, split, write the particle
 // to its new slot, then deposit the segments (round t takes the t-th segment of every lane).
@@ -550,6 +576,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
         }
         if (threadIdx.x == 0) sNleave = 0;
         __syncthreads();
+        discard_dead_slab<DIM>(sd.in, slab, nst, nar, cap);
     }
     // ---- the face crossings still queued (the queue carries over from one species to the
     //      next: its entries hold their own charge)
