@@ -88,15 +88,17 @@ __global__ void k_bin(const int *__restrict__ ix, const float *__restrict__ x,
 {
     OSG_GRID_LOOP(p, np)
     {
-        const long o = dst[p];
+        int c[3] = {0, 0, 0};
+        float xo[3] = {0.f, 0.f, 0.f};
         for (int d = 0; d < dim; d++) {
-            out.ix[d][o] = ix[dim * p + d];
-            out.x[d][o] = x[dim * p + d];
+            c[d] = ix[dim * p + d];
+            xo[d] = x[dim * p + d];
         }
-        out.u[0][o] = u[3 * p];
-        out.u[1][o] = u[3 * p + 1];
-        out.u[2][o] = u[3 * p + 2];
-        out.q[o] = q[p];
+        const float un[3] = {u[3 * p], u[3 * p + 1], u[3 * p + 2]};
+        if (dim == 2)
+            store_rec<2>(out.rec, dst[p], c, xo, un, q[p]);
+        else
+            store_rec<3>(out.rec, dst[p], c, xo, un, q[p]);
     }
 }
 
@@ -109,14 +111,20 @@ __global__ void k_compact(Slabs in, long cap, int dim, const int *__restrict__ o
     const long o = off[t];
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const long src = t * cap + (i < nst ? i : cap - 1 - (i - nst)), dst = o + i;
+        int c[3];
+        float xo[3], un[3], qq;
+        if (dim == 2)
+            load_rec<2>(in.rec, src, c, xo, un, qq);
+        else
+            load_rec<3>(in.rec, src, c, xo, un, qq);
         for (int d = 0; d < dim; d++) {
-            ix[dim * dst + d] = in.ix[d][src];
-            x[dim * dst + d] = in.x[d][src];
+            ix[dim * dst + d] = c[d];
+            x[dim * dst + d] = xo[d];
         }
-        u[3 * dst] = in.u[0][src];
-        u[3 * dst + 1] = in.u[1][src];
-        u[3 * dst + 2] = in.u[2][src];
-        q[dst] = in.q[src];
+        u[3 * dst] = un[0];
+        u[3 * dst + 1] = un[1];
+        u[3 * dst + 2] = un[2];
+        q[dst] = qq;
     }
 }
 
@@ -366,30 +374,20 @@ int tiled_add_species(TiledState *t, double rqm, long np, const int *ix, const f
     for (int p = 0; p < 2; p++) {
         Slabs s;
         memset(&s, 0, sizeof s);
-        const size_t bytes = nslot * sizeof(float) * (2 * dim + 4);
+        const size_t bytes = nslot * sizeof(float) * (dim == 2 ? PRec<2>::N : PRec<3>::N);
         char *mem = nullptr;
         if (cudaMalloc(&mem, bytes) != cudaSuccess) {
             set_error("particle slab allocation of %zu bytes failed", bytes);
             return OSG_ERR_NOMEM;
         }
         t->allocs.push_back(mem);
-        // every tile's slab of every array starts on a 128-byte line (the push drops dead
-        // lines from L2 by address)
-        if (((uintptr_t)mem & 127) != 0 || (nslot * sizeof(float)) % 128 != 0 || cap % 32 != 0) {
+        // every tile's slab starts on a 128-byte line (the push drops dead lines from L2 by
+        // address)
+        if (((uintptr_t)mem & 127) != 0 || cap % 32 != 0) {
             set_error("particle slabs are not aligned to 128-byte lines");
             return OSG_ERR_CUDA;
         }
-        size_t o = 0;
-        for (int d = 0; d < dim; d++) {
-            s.ix[d] = (int *)(mem + o); o += nslot * 4;
-        }
-        for (int d = 0; d < dim; d++) {
-            s.x[d] = (float *)(mem + o); o += nslot * 4;
-        }
-        for (int c = 0; c < 3; c++) {
-            s.u[c] = (float *)(mem + o); o += nslot * 4;
-        }
-        s.q = (float *)(mem + o);
+        s.rec = (float *)mem;
         s.cnt = t->d_cnt[p] + (size_t)k * t->ntiles;
         s.arr = t->d_arr[p] + (size_t)k * t->ntiles;
         OSG_CUDA(cudaMemsetAsync(s.arr, 0, sizeof(int) * t->ntiles, st));

@@ -13,14 +13,73 @@
 
 namespace osg {
 
+// Particle records of the tiled engine, one per slot: 2D {ix1, ix2, x1, x2, u1, u2, u3, q}
+// (32 bytes), 3D {ix1, ix2, ix3, x1, x2, x3, u1, u2, u3, q, 0, 0} (48 bytes); the cell indices
+// are stored as int bits.  A 2D record moves as one 32-byte vector access (sm_100+
+// ld/st.global.v8: a warp's 32 records are 1 KB of whole lines, one instruction), a 3D record
+// as three 16-byte vectors.
+template <int DIM> struct PRec {
+    static constexpr int N = DIM == 2 ? 8 : 12;   // floats per record
+};
+
 struct Slabs {
-    int *ix[3];
-    float *x[3];
-    float *u[3];
-    float *q;
+    float *rec;    // records, slot i of tile t at t * cap + i
     int *cnt;      // [ntiles] particles in slots [0, cnt) of the slab, sorted by cell
     int *arr;      // [ntiles] particles that arrived from other tiles, slots [cap - arr, cap)
 };
+
+template <int DIM>
+__device__ __forceinline__ void load_rec(const float *rec, long p, int *c, float *x, float *u,
+                                         float &q)
+{
+    const float4 *r = reinterpret_cast<const float4 *>(rec + p * PRec<DIM>::N);
+    if constexpr (DIM == 2) {
+        float c0, c1;
+        asm volatile("ld.global.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=f"(c0), "=f"(c1), "=f"(x[0]), "=f"(x[1]), "=f"(u[0]), "=f"(u[1]),
+                       "=f"(u[2]), "=f"(q)
+                     : "l"(r)
+                     : "memory");
+        c[0] = __float_as_int(c0);
+        c[1] = __float_as_int(c1);
+    } else {
+        const float4 a = r[0], b = r[1], d = r[2];
+        c[0] = __float_as_int(a.x);
+        c[1] = __float_as_int(a.y);
+        c[2] = __float_as_int(a.z);
+        x[0] = a.w;
+        x[1] = b.x;
+        x[2] = b.y;
+        u[0] = b.z;
+        u[1] = b.w;
+        u[2] = d.x;
+        q = d.y;
+    }
+}
+
+template <int DIM>
+__device__ __forceinline__ void store_rec(float *rec, long p, const int *c, const float *x,
+                                          const float *u, float q)
+{
+    float4 *r = reinterpret_cast<float4 *>(rec + p * PRec<DIM>::N);
+    if constexpr (DIM == 2) {
+        asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(r),
+                     "f"(__int_as_float(c[0])), "f"(__int_as_float(c[1])), "f"(x[0]), "f"(x[1]),
+                     "f"(u[0]), "f"(u[1]), "f"(u[2]), "f"(q)
+                     : "memory");
+    } else {
+        r[0] = make_float4(__int_as_float(c[0]), __int_as_float(c[1]), __int_as_float(c[2]), x[0]);
+        r[1] = make_float4(x[1], x[2], u[0], u[1]);
+        r[2] = make_float4(u[2], q, 0.f, 0.f);
+    }
+}
+
+// first cell index of a record (0 marks an empty slot)
+template <int DIM>
+__device__ __forceinline__ int *rec_ix0(float *rec, long p)
+{
+    return reinterpret_cast<int *>(rec + p * PRec<DIM>::N);
+}
 
 struct SpeciesDev {
     Slabs in, out;
@@ -109,41 +168,28 @@ __device__ __forceinline__ void emigrate(const SpeciesDev &sd, long cap, long de
         atomicOr(status, OSG_STATUS_OVERFLOW);
         return;
     }
-    const long o = dest * cap + cap - 1 - k;
-#pragma unroll
-    for (int d = 0; d < DIM; d++) {
-        sd.out.ix[d][o] = cw[d];
-        sd.out.x[d][o] = xo[d];
-    }
-    sd.out.u[0][o] = un[0];
-    sd.out.u[1][o] = un[1];
-    sd.out.u[2][o] = un[2];
-    sd.out.q[o] = q;
+    store_rec<DIM>(sd.out.rec, dest * cap + cap - 1 - k, cw, xo, un, q);
 }
 
 // After the sort, a tile's input slab is dead until the next step writes it as its output:
 // the cache lines the first pass dirtied (stayers written back to their own slots, [0, nst)
 // and the arrival region [cap - nar, cap)) are dropped from L2 without a write-back to DRAM.
-// A tile's slab of every array starts on a 128-byte line and spans whole lines (cap is a
-// multiple of 32 slots, every array of the allocation a multiple of 32 slots per tile).
+// A tile's slab starts on a 128-byte line and spans whole lines (cap is a multiple of 32
+// slots of 32 or 48 bytes, the allocation 128-byte aligned).
 template <int DIM>
 __device__ __forceinline__ void discard_dead_slab(const Slabs &in, long slab, int nst, int nar,
                                                   long cap)
 {
-    const int lo_lines = (nst + 31) >> 5;
-    const int cap_lines = (int)(cap >> 5);
-    const int hi_first = max((int)((cap - nar) >> 5), lo_lines);
+    constexpr int RB = 4 * PRec<DIM>::N;   // bytes per record
+    const int lo_lines = (nst * RB + 127) >> 7;
+    const int cap_lines = (int)((cap * RB) >> 7);
+    const int hi_first = max((int)(((cap - nar) * RB) >> 7), lo_lines);
     const int nl = lo_lines + (nar > 0 ? cap_lines - hi_first : 0);
-    constexpr int NA = 2 * DIM + 3;   // ix, x and u are written back; q is not
-#pragma unroll
-    for (int arr = 0; arr < NA; arr++) {
-        const float *base = arr < DIM ? reinterpret_cast<const float *>(in.ix[arr])
-                                      : (arr < 2 * DIM ? in.x[arr - DIM] : in.u[arr - 2 * DIM]);
-        for (int l0 = threadIdx.x; l0 < nl; l0 += blockDim.x) {
-            const int line = l0 < lo_lines ? l0 : hi_first + (l0 - lo_lines);
-            const float *pa = base + slab + 32L * line;
-            asm volatile("discard.global.L2 [%0], 128;" ::"l"(pa) : "memory");
-        }
+    const char *base = reinterpret_cast<const char *>(in.rec + slab * PRec<DIM>::N);
+    for (int l0 = threadIdx.x; l0 < nl; l0 += blockDim.x) {
+        const int line = l0 < lo_lines ? l0 : hi_first + (l0 - lo_lines);
+        const char *pa = base + 128L * line;
+        asm volatile("discard.global.L2 [%0], 128;" ::"l"(pa) : "memory");
     }
 }
 
@@ -257,18 +303,10 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
         // the particle of the next iteration is loaded while this one is pushed
         int pf_c[3] = {1, 1, 1};
         float pf_x[3] = {0, 0, 0}, pf_u[3] = {0, 0, 0}, pf_q = 0.0f;
+        float *const rin = sd.in.rec;
         auto prefetch = [&](int i, int lim) {
             if (i < lim) {
-                const long p = slot(i);
-#pragma unroll
-                for (int d = 0; d < DIM; d++) {
-                    pf_c[d] = sd.in.ix[d][p];
-                    pf_x[d] = sd.in.x[d][p];
-                }
-                pf_u[0] = sd.in.u[0][p];
-                pf_u[1] = sd.in.u[1][p];
-                pf_u[2] = sd.in.u[2][p];
-                pf_q = sd.in.q[p];
+                load_rec<DIM>(rin, slot(i), pf_c, pf_x, pf_u, pf_q);
             }
         };
         // take the prefetched particle into registers
@@ -297,7 +335,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 }
                 if (!ok) {
                     atomicOr(a.status, OSG_STATUS_RANGE);
-                    sd.in.ix[0][p] = 0;
+                    *rec_ix0<DIM>(rin, p) = 0;
                     has = false;
                 }
             }
@@ -357,7 +395,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 // (open x1: a particle outside [1, nx] has left the window; its current of
                 //  this step is already in the segments)
                 if (a.open_x && (cw[0] < 1 || cw[0] > a.nx[0])) {
-                    sd.in.ix[0][p] = 0;
+                    *rec_ix0<DIM>(rin, p) = 0;
                     has = false;
                 } else {
                     // most particles stay in their tile: test that without dividing
@@ -391,15 +429,8 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
             first = __shfl_sync(FULL_MASK, first, pl);
             if (stay) {
                 const int rank = first + __popc(peers & ((1u << lane) - 1u));
-                sd.in.ix[0][p] = 1 + lcell + (rank << SORT_CELL_BITS);
-#pragma unroll
-                for (int d = 0; d < DIM; d++) {
-                    if (d > 0) sd.in.ix[d][p] = cw[d];
-                    sd.in.x[d][p] = xo[d];
-                }
-                sd.in.u[0][p] = un[0];
-                sd.in.u[1][p] = un[1];
-                sd.in.u[2][p] = un[2];
+                const int kc[3] = {1 + lcell + (rank << SORT_CELL_BITS), cw[1], cw[2]};
+                store_rec<DIM>(rin, p, kc, xo, un, q);
             }
             const bool leave = has && !stay;
             const unsigned ml = __ballot_sync(FULL_MASK, leave);
@@ -409,7 +440,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 if ((int)lane == leader) q0 = atomicAdd(&sNleave, __popc(ml));
                 q0 = __shfl_sync(FULL_MASK, q0, leader);
                 if (leave) {
-                    sd.in.ix[0][p] = 0;
+                    *rec_ix0<DIM>(rin, p) = 0;
                     const int e = q0 + __popc(ml & ((1u << lane) - 1u));
                     if (e < LEAVE_QUEUE) {
 #pragma unroll
@@ -496,15 +527,14 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 pp[j] = slab + (i < nst ? i : cap - 1 - (i - nst));
                 key[j] = 0;
                 if (i < n) {
-                    key[j] = sd.in.ix[0][pp[j]];
-                    if (DIM > 1) c1[j] = sd.in.ix[1][pp[j]];
-                    if (DIM > 2) c2[j] = sd.in.ix[2][pp[j]];
+                    int cc[3];
+                    float xr[3];
+                    load_rec<DIM>(rin, pp[j], cc, xr, uu[j], qq[j]);
+                    key[j] = cc[0];
+                    c1[j] = DIM > 1 ? cc[1] : 0;
+                    c2[j] = DIM > 2 ? cc[2] : 0;
 #pragma unroll
-                    for (int d = 0; d < DIM; d++) xx[j][d] = sd.in.x[d][pp[j]];
-                    uu[j][0] = sd.in.u[0][pp[j]];
-                    uu[j][1] = sd.in.u[1][pp[j]];
-                    uu[j][2] = sd.in.u[2][pp[j]];
-                    qq[j] = sd.in.q[pp[j]];
+                    for (int d = 0; d < DIM; d++) xx[j][d] = xr[d];
                 }
             }
         };
@@ -562,15 +592,8 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                     int ly = 0;
                     if (DIM > 1) ly = cc1[j] - t0[1];
                     if (DIM > 2) ly += a.T[1] * (cc2[j] - t0[2]);
-                    sd.out.ix[0][o] = t0[0] + lc - a.T[0] * ly;
-                    if (DIM > 1) sd.out.ix[1][o] = cc1[j];
-                    if (DIM > 2) sd.out.ix[2][o] = cc2[j];
-#pragma unroll
-                    for (int d = 0; d < DIM; d++) sd.out.x[d][o] = cx[j][d];
-                    sd.out.u[0][o] = cu[j][0];
-                    sd.out.u[1][o] = cu[j][1];
-                    sd.out.u[2][o] = cu[j][2];
-                    sd.out.q[o] = cq[j];
+                    const int oc[3] = {t0[0] + lc - a.T[0] * ly, cc1[j], cc2[j]};
+                    store_rec<DIM>(sd.out.rec, o, oc, cx[j], cu[j], cq[j]);
                 }
             }
         }
@@ -797,16 +820,9 @@ __global__ void k_inject_x(InjectArgs a)
             atomicOr(a.status, OSG_STATUS_OVERFLOW);
             continue;
         }
-        const long o = tile * a.cap + a.cap - 1 - k;
-#pragma unroll
-        for (int d = 0; d < DIM; d++) {
-            a.out.ix[d][o] = cw[d];
-            a.out.x[d][o] = off[d];
-        }
-        a.out.u[0][o] = 0.0f;
-        a.out.u[1][o] = 0.0f;
-        a.out.u[2][o] = 0.0f;
-        a.out.q[o] = den * (float)a.charge_unit;
+        const float u0[3] = {0.0f, 0.0f, 0.0f};
+        store_rec<DIM>(a.out.rec, tile * a.cap + a.cap - 1 - k, cw, off, u0,
+                       den * (float)a.charge_unit);
     }
 }
 
