@@ -63,6 +63,9 @@ struct TiledState {
     size_t smem_bytes = 0;
     int threads = 256;   // threads per push CTA (multiple of 32, <= 256)
     int reduce_min = 2;  // set per dimension in tiled_create
+    // drop dead slab lines from L2 after the sort; OSG_L2_DISCARD=0 turns it off (profiler
+    // kernel replay saves and restores device memory and needs the dropped lines defined)
+    int l2_discard = 1;
     int pusher = OSG_PUSHER_BORIS;
     double iter_tol = 1.0e-3;
     long nj_tile = 0;    // current points (x3 components) of a tile with its halo
@@ -167,6 +170,7 @@ static TiledArgs base_args(const TiledState *t)
     a.iter_tol = t->iter_tol;
     a.tile_hi = t->tile_hi;
     a.tile_lo = t->tile_lo;
+    a.discard = t->l2_discard;
     return a;
 }
 
@@ -236,6 +240,7 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
     // lanes of one warp spread over the tile): direct shared atomics measured faster
     t->reduce_min = t->dim == 2 ? 2 : 33;
     if (const char *ev = getenv("OSG_REDUCE_MIN")) t->reduce_min = atoi(ev);
+    if (const char *ev = getenv("OSG_L2_DISCARD")) t->l2_discard = atoi(ev) != 0;
     if (const char *ev = getenv("OSG_PUSH_THREADS")) {
         const int v = atoi(ev);
         if (v >= 64 && v <= 256 && v % 32 == 0) t->threads = v;

@@ -115,6 +115,9 @@ struct TiledArgs {
     // the box along x1 are dropped
     int open_x;
     int shift_x;
+    // 1: drop the dead input-slab lines from L2 after the sort (discard_dead_slab).  0 for
+    // multi-pass profiler replay, which saves and restores memory and needs it defined
+    int discard;
 };
 
 static const int MAX_TILED_SPECIES = 16;
@@ -599,7 +602,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
         }
         if (threadIdx.x == 0) sNleave = 0;
         __syncthreads();
-        discard_dead_slab<DIM>(sd.in, slab, nst, nar, cap);
+        if (a.discard) discard_dead_slab<DIM>(sd.in, slab, nst, nar, cap);
     }
     // ---- the face crossings still queued (the queue carries over from one species to the
     //      next: its entries hold their own charge)
