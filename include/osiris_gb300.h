@@ -66,6 +66,8 @@ extern "C" {
 #define OSG_PUSHER_EXACT 1   /* push_type = "exact" (analytic, source/spec/os-spec-extpush.f03) */
 #define OSG_PUSHER_VAY 2     /* push_type = "vay" (dudt_vay, source/spec/os-spec-push.f03) */
 #define OSG_PUSHER_HC 3      /* push_type = "cary" (Higuera-Cary, dudt_cary, same file) */
+#define OSG_PUSHER_FULLROT 4 /* push_type = "fullrot" (dudt_fullrot, same file) */
+#define OSG_PUSHER_EULER 5   /* push_type = "euler" (dudt_euler, same file) */
 
 const char *osg_last_error(void);
 int osg_version(void);
@@ -118,9 +120,10 @@ int osg_advance_deposit_exact_f64(int dim, int order, int *ix, double *x, double
 
 /* The particle advance of the Fortran path (advance_deposit_{1d,2d,3d},
  * source/spec/os-spec-push.f03:1363-1605) with any momentum update: pusher OSG_PUSHER_BORIS,
- * _EXACT (iter_tol), _VAY or _HC; dt is the double step (momentum and dt/dx).  Position
- * update, split and deposit as osg_vadvance_deposit_*; *ene += the energy the chosen reference
- * pusher reports (Boris and Vay: time-centred; exact: new momenta; HC: half-kicked). */
+ * _EXACT (iter_tol), _VAY, _HC, _FULLROT or _EULER; dt is the double step (momentum and
+ * dt/dx).  Position update, split and deposit as osg_vadvance_deposit_*; *ene += the energy the
+ * chosen reference pusher reports (Boris and Vay: time-centred; exact: new momenta; HC, full
+ * and Euler rotation: half-kicked). */
 int osg_advance_deposit_f32(int dim, int order, int *ix, float *x, float *u, float *q, int i0,
                             int i1, float rqm, const float *efield, const float *bfield,
                             const int *emf_size, const int *emf_offset, float *j,
@@ -251,7 +254,8 @@ typedef struct {
     int tile[3];      /* tile shape in cells (TILED; 0 = automatic) */
     int n_sort;       /* PLAIN: cell sort every n_sort steps (0 = never); TILED sorts every step */
     double capacity;  /* TILED: slots per tile as a multiple of the mean load (0 = 3.0) */
-    int pusher;       /* OSG_PUSHER_BORIS (0), _EXACT (1), _VAY (2) or _HC (3) */
+    int pusher;       /* OSG_PUSHER_BORIS (0), _EXACT (1), _VAY (2), _HC (3), _FULLROT (4),
+                         _EULER (5) */
     double iter_tol;  /* exact pusher: Newton tolerance (0 = the reference default 1e-3) */
     int smooth_type;  /* current smoothing after the guard fold, OSG_SMOOTH_* (all axes) */
     int smooth_order; /* its order (binomial: passes; compensated: >= 2; others fixed) */

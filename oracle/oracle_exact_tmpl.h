@@ -219,9 +219,80 @@ static double EXN(ora_hc_u)(R tem, const R *e, const R *b, R *u, R q)
     return ene;
 }
 
+/* Full-rotation pusher (dudt_fullrot, source/spec/os-spec-push.f03:83-231): Boris with the
+ * rotation vector scaled by tan(b)/b, so a pure magnetic field turns the momentum by the exact
+ * gyration angle.  tem = real(0.5 (dt / rqm)) (:112); tan(b)/b of b^2 by the reference's
+ * rational approximation, evaluated in double from the float b^2 and rounded back (:166-178);
+ * returns q u^2 / (gamma + 1) of the half-kicked momentum in double (:144-147). */
+static double EXN(ora_fullrot_u)(R tem, const R *e, const R *b, R *u, R q)
+{
+    R ep[3], ut[3], bp[3], p[3];
+    for (int c = 0; c < 3; c++) ep[c] = e[c] * tem;
+    for (int c = 0; c < 3; c++) ut[c] = u[c] + ep[c];
+    const R u2 = (ut[0] * ut[0] + ut[1] * ut[1]) + ut[2] * ut[2];
+    const R gamma = SQRT(u2 + K(1.0));
+    const double ene = (double)(q * u2) / ((double)gamma + 1.0);
+    const R tg = tem / gamma;
+    for (int c = 0; c < 3; c++) bp[c] = b[c] * tg;
+    const R b2 = (bp[0] * bp[0] + bp[1] * bp[1]) + bp[2] * bp[2];
+    const double d2 = (double)b2;
+    const R r = (R)(2005892.32789228135999056 +
+                    d2 * (-267559.850143894287032640 +
+                          d2 * (6870.7950060474599763728 - 35.8427314349709199363798 * d2)));
+    const R s = (R)(2005892.32789228136020125 +
+                    d2 * (-936190.626107988089080768 +
+                          d2 * (51482.0266564063006502261 + d2 * (d2 - 625.608053837898687047447))));
+    const R t = s != K(0.0) ? r / s : K(1.0);
+    for (int c = 0; c < 3; c++) bp[c] = bp[c] * t;
+    p[0] = (ut[0] + ut[1] * bp[2]) - ut[2] * bp[1];
+    p[1] = (ut[1] + ut[2] * bp[0]) - ut[0] * bp[2];
+    p[2] = (ut[2] + ut[0] * bp[1]) - ut[1] * bp[0];
+    const R sc = K(2.0) / (((K(1.0) + bp[0] * bp[0]) + bp[1] * bp[1]) + bp[2] * bp[2]);
+    for (int c = 0; c < 3; c++) bp[c] = bp[c] * sc;
+    ut[0] = (ut[0] + p[1] * bp[2]) - p[2] * bp[1];
+    ut[1] = (ut[1] + p[2] * bp[0]) - p[0] * bp[2];
+    ut[2] = (ut[2] + p[0] * bp[1]) - p[1] * bp[0];
+    for (int c = 0; c < 3; c++) u[c] = ut[c] + ep[c];
+    return ene;
+}
+
+/* Euler-rotation pusher (dudt_euler, :235-352): the magnetic rotation as an explicit rotation
+ * matrix from the quaternion (cos(w/2), -sin(w/2) b/|b|), w = |b| dt / (rqm gamma) with
+ * gam_tem = dt / (rqm gamma) in double from the float product rqm gamma (:289); tem as the
+ * full-rotation pusher; same energy term. */
+static double EXN(ora_euler_u)(R tem, R rqm, double dt, const R *e, const R *b, R *u, R q)
+{
+    R ep[3], ut[3], bp[3];
+    for (int c = 0; c < 3; c++) ep[c] = e[c] * tem;
+    for (int c = 0; c < 3; c++) ut[c] = u[c] + ep[c];
+    const R u2 = (ut[0] * ut[0] + ut[1] * ut[1]) + ut[2] * ut[2];
+    const R gamma = SQRT(u2 + K(1.0));
+    const double ene = (double)(q * u2) / ((double)gamma + 1.0);
+    const R gt = (R)(dt / (double)(rqm * gamma));
+    for (int c = 0; c < 3; c++) bp[c] = b[c] * gt;
+    const R b2 = (bp[0] * bp[0] + bp[1] * bp[1]) + bp[2] * bp[2];
+    const R bn = SQRT(b2);
+    R s = SIN(bn / K(2.0));
+    const R a = COS(bn / K(2.0));
+    s = b2 > K(0.0) ? -s / bn : K(-1.0);
+    const R qb = bp[0] * s, qc = bp[1] * s, qd = bp[2] * s;
+    const R r11 = ((a * a + qb * qb) - qc * qc) - qd * qd, r21 = K(2.0) * (qb * qc - a * qd),
+            r31 = K(2.0) * (qb * qd + a * qc);
+    const R r12 = K(2.0) * (qb * qc + a * qd), r22 = ((a * a + qc * qc) - qb * qb) - qd * qd,
+            r32 = K(2.0) * (qc * qd - a * qb);
+    const R r13 = K(2.0) * (qb * qd - a * qc), r23 = K(2.0) * (qc * qd + a * qb),
+            r33 = ((a * a + qd * qd) - qb * qb) - qc * qc;
+    const R pn[3] = {(r11 * ut[0] + r21 * ut[1]) + r31 * ut[2],
+                     (r12 * ut[0] + r22 * ut[1]) + r32 * ut[2],
+                     (r13 * ut[0] + r23 * ut[1]) + r33 * ut[2]};
+    for (int c = 0; c < 3; c++) u[c] = pn[c] + ep[c];
+    return ene;
+}
+
 /* Momentum update of n particles in given (unscaled) fields e(3,n), b(3,n) by pusher 1 (exact:
  * fields times qm = 1/rqm as dudt_exact, :76-86, energy q (gamma - 1) of the new momenta),
- * 2 (Vay) or 3 (Higuera-Cary) with their own tem and energy terms; *ene += the double sum. */
+ * 2 (Vay), 3 (Higuera-Cary), 4 (full rotation) or 5 (Euler rotation) with their own tem and
+ * energy terms; *ene += the double sum. */
 void EXN(ora_dudt_pusher)(int pusher, int n, const R *e, const R *b, R *u, const R *q, R rqm,
                           double dt, double tol, double *ene)
 {
@@ -236,6 +307,16 @@ void EXN(ora_dudt_pusher)(int pusher, int n, const R *e, const R *b, R *u, const
         if (pusher == 3) {
             loc += EXN(ora_hc_u)((R)(0.5 * (dt / (double)rqm)), e + 3 * i, b + 3 * i, u + 3 * i,
                                  q[i]);
+            continue;
+        }
+        if (pusher == 4) {
+            loc += EXN(ora_fullrot_u)((R)(0.5 * (dt / (double)rqm)), e + 3 * i, b + 3 * i,
+                                      u + 3 * i, q[i]);
+            continue;
+        }
+        if (pusher == 5) {
+            loc += EXN(ora_euler_u)((R)(0.5 * (dt / (double)rqm)), rqm, dt, e + 3 * i, b + 3 * i,
+                                    u + 3 * i, q[i]);
             continue;
         }
         R ep[3], bp[3];
@@ -258,7 +339,7 @@ void EXN(ora_dudt_exact)(int n, const R *e, const R *b, R *u, const R *q, R rqm,
 }
 
 /* Selected momentum update of the push restatement below (0 = Boris, 1 = exact, 2 = Vay,
- * 3 = Higuera-Cary), the exact pusher's tolerance and the double time step of the Fortran
+ * 3 = Higuera-Cary, 4 = full rotation, 5 = Euler rotation), the exact pusher's tolerance and the double time step of the Fortran
  * pushers; set by ora_push_pusher_* around one call. */
 static int EXN(ora_pusher) = 0;
 static double EXN(ora_iter_tol) = 1.0e-3;

@@ -62,6 +62,8 @@ void ora_spline_weights_f64(int order, double x, double *w)
 #define K(v) ((float)(v))
 #define FMA fmaf
 #define SQRT sqrtf
+#define SIN sinf
+#define COS cosf
 
 #include "oracle_exact_tmpl.h"
 
@@ -93,6 +95,8 @@ void ora_spline_weights_f64(int order, double x, double *w)
 #undef K
 #undef FMA
 #undef SQRT
+#undef SIN
+#undef COS
 
 /* ---------------------------------------------------------------- double precision ------ */
 #define R double
@@ -101,6 +105,8 @@ void ora_spline_weights_f64(int order, double x, double *w)
 #define K(v) ((double)(v))
 #define FMA fma
 #define SQRT sqrt
+#define SIN sin
+#define COS cos
 
 #include "oracle_exact_tmpl.h"
 
@@ -132,6 +138,8 @@ void ora_spline_weights_f64(int order, double x, double *w)
 #undef K
 #undef FMA
 #undef SQRT
+#undef SIN
+#undef COS
 
 /* ---------------------------------------------------------------- dispatch -------------- */
 
@@ -188,9 +196,9 @@ int ora_push_f64(int dim, int order, int *ix, double *x, double *u, double *q, i
     return 0;
 }
 
-/* push with another momentum update (pusher 1 exact, 2 Vay, 3 Higuera-Cary; the Fortran
- * advance_deposit path): momentum with the double step dt (and tolerance tol, exact pusher),
- * position and deposit as the push above with dt */
+/* push with another momentum update (pusher 1 exact, 2 Vay, 3 Higuera-Cary, 4 full rotation,
+ * 5 Euler rotation; the Fortran advance_deposit path): momentum with the double step dt (and
+ * tolerance tol, exact pusher), position and deposit as the push above with dt */
 int ora_push_pusher_f32(int pusher, int dim, int order, int *ix, float *x, float *u, float *q,
                         int i0, int i1, float rqm, float *e, float *b, int *emf_size,
                         int *emf_off, float *j, int *j_size, int *j_off, double *dx, double dt,
@@ -518,7 +526,8 @@ int ora_step_f64(int dim, int order, const int *nx, const int *gcl, const int *g
     STEP_BODY(double, f64, 0, 1e-3)
 }
 
-/* the same step with another momentum update (pusher 1 exact, 2 Vay, 3 Higuera-Cary) */
+/* the same step with another momentum update (pusher 1 exact, 2 Vay, 3 Higuera-Cary, 4 full
+ * rotation, 5 Euler rotation) */
 int ora_step_pusher_f32(int pusher, int dim, int order, const int *nx, const int *gcl,
                         const int *gcu, const double *dx, double dt, float *e, float *b,
                         float *j, int nspec, const int *np, int **ix, float **x, float **u,

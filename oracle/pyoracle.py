@@ -25,7 +25,7 @@ REFERENCE_SRC = "/root/reference"
 
 # guard cells required by each interpolation order (source/particles/os-particles.f03:321-360)
 GUARD = {1: (1, 2), 2: (2, 3), 3: (3, 4), 4: (4, 5)}
-PUSHERS = {"boris": 0, "exact": 1, "vay": 2, "hc": 3}
+PUSHERS = {"boris": 0, "exact": 1, "vay": 2, "hc": 3, "fullrot": 4, "euler": 5}
 
 _lib = None
 _ref = {}
@@ -200,7 +200,7 @@ def push(prec, dim, order, ix, x, u, q, i0, i1, rqm, e, b, j, emf_size, emf_off,
 
 
 def dudt(pusher, prec, e, b, u, q, rqm, dt, iter_tol=1e-3):
-    """Momentum update ("exact", "vay", "hc") of n particles in given fields e (n,3), b (n,3);
+    """Momentum update ("exact", "vay", "hc", "fullrot", "euler") of n particles in given fields e (n,3), b (n,3);
     u updated in place; returns the energy sum the reference pusher reports."""
     ene = np.zeros(1, dtype=np.float64)
     f = getattr(lib(), f"ora_dudt_pusher_{prec}")

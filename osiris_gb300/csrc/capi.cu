@@ -92,7 +92,7 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
                      const int *j_size, const int *j_off, const double *dx, double dt,
                      double *ene, int pusher = OSG_PUSHER_BORIS, double iter_tol = 1.0e-3)
 {
-    OSG_CHECK(pusher >= OSG_PUSHER_BORIS && pusher <= OSG_PUSHER_HC &&
+    OSG_CHECK(pusher >= OSG_PUSHER_BORIS && pusher <= OSG_PUSHER_EULER &&
                   (pusher != OSG_PUSHER_EXACT || iter_tol > 0),
               OSG_ERR_ARG, "bad pusher / iteration tolerance");
     OSG_CHECK(dim >= 1 && dim <= 3 && order >= 1 && order <= 4, OSG_ERR_ARG,
@@ -144,8 +144,7 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
                                                 (T *)d_j, j_size, j_off, dx, dt, d_ene, d_status);
         a.pusher = pusher;
         a.iter_tol = iter_tol;
-        if (pusher == OSG_PUSHER_VAY || pusher == OSG_PUSHER_HC)
-            a.tem = (T)pusher_tem(pusher, dt, (double)rqm);
+        if (pusher >= OSG_PUSHER_VAY) a.tem = (T)pusher_tem(pusher, dt, (double)rqm);
         if ((rc = launch_plain_push<T>(dim, order, a, cs))) return rc;
         OSG_CUDA(cudaGetLastError());
         OSG_CUDA(cudaMemcpyAsync(ix + dim * h, cix, sizeof(int) * dim * n, cudaMemcpyDeviceToHost, cs));

@@ -593,10 +593,93 @@ __device__ __forceinline__ double hc_push(T tem, T e1, T e2, T e3, T b1, T b2, T
     return ene;
 }
 
+// ---------------------------------------------------------------------------------------
+// Full-rotation pusher (dudt_fullrot, source/spec/os-spec-push.f03:83-231): Boris with the
+// rotation vector scaled by tan(b)/b (the reference's rational approximation in b^2,
+// evaluated in double from the T value of b^2 and rounded back to T, :166-178), so a uniform
+// magnetic field turns the momentum by the exact gyration angle.  Euler-rotation pusher
+// (dudt_euler, :235-352): the magnetic rotation as the matrix of the quaternion
+// (cos(w/2), -sin(w/2) b/|b|), w = |B| dt / (rqm gamma), the factor dt / (rqm gamma) in
+// double from the T product rqm gamma (:289).  tem = real(0.5 (dt / rqm)); both return
+// q u^2 / (gamma + 1) of the half-kicked momentum in double (:144-147, :278-281).
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ double fullrot_push(T tem, T e1, T e2, T e3, T b1, T b2, T b3, T q,
+                                               T &u1, T &u2, T &u3)
+{
+    const T ep[3] = {e1 * tem, e2 * tem, e3 * tem};
+    T ut[3] = {u1 + ep[0], u2 + ep[1], u3 + ep[2]};
+    const T usq = (ut[0] * ut[0] + ut[1] * ut[1]) + ut[2] * ut[2];
+    const T gamma = sqrtR(usq + T(1.0));
+    const double ene = (double)(q * usq) / ((double)gamma + 1.0);
+    const T tg = tem / gamma;
+    T bp[3] = {b1 * tg, b2 * tg, b3 * tg};
+    const T bsq = (bp[0] * bp[0] + bp[1] * bp[1]) + bp[2] * bp[2];
+    const double d2 = (double)bsq;
+    const T r = (T)(2005892.32789228135999056 +
+                    d2 * (-267559.850143894287032640 +
+                          d2 * (6870.7950060474599763728 - 35.8427314349709199363798 * d2)));
+    const T s = (T)(2005892.32789228136020125 +
+                    d2 * (-936190.626107988089080768 +
+                          d2 * (51482.0266564063006502261 + d2 * (d2 - 625.608053837898687047447))));
+    const T t = s != T(0.0) ? r / s : T(1.0);
+#pragma unroll
+    for (int c = 0; c < 3; c++) bp[c] = bp[c] * t;
+    const T p[3] = {(ut[0] + ut[1] * bp[2]) - ut[2] * bp[1], (ut[1] + ut[2] * bp[0]) - ut[0] * bp[2],
+                    (ut[2] + ut[0] * bp[1]) - ut[1] * bp[0]};
+    const T sc = T(2.0) / (((T(1.0) + bp[0] * bp[0]) + bp[1] * bp[1]) + bp[2] * bp[2]);
+#pragma unroll
+    for (int c = 0; c < 3; c++) bp[c] = bp[c] * sc;
+    ut[0] = (ut[0] + p[1] * bp[2]) - p[2] * bp[1];
+    ut[1] = (ut[1] + p[2] * bp[0]) - p[0] * bp[2];
+    ut[2] = (ut[2] + p[0] * bp[1]) - p[1] * bp[0];
+    u1 = ut[0] + ep[0];
+    u2 = ut[1] + ep[1];
+    u3 = ut[2] + ep[2];
+    return ene;
+}
+
+__device__ __forceinline__ float sinR(float x) { return sinf(x); }
+__device__ __forceinline__ double sinR(double x) { return sin(x); }
+__device__ __forceinline__ float cosR(float x) { return cosf(x); }
+__device__ __forceinline__ double cosR(double x) { return cos(x); }
+
+template <typename T>
+__device__ __forceinline__ double euler_push(T tem, T rqm, double dt, T e1, T e2, T e3, T b1,
+                                             T b2, T b3, T q, T &u1, T &u2, T &u3)
+{
+    const T ep[3] = {e1 * tem, e2 * tem, e3 * tem};
+    const T ut[3] = {u1 + ep[0], u2 + ep[1], u3 + ep[2]};
+    const T usq = (ut[0] * ut[0] + ut[1] * ut[1]) + ut[2] * ut[2];
+    const T gamma = sqrtR(usq + T(1.0));
+    const double ene = (double)(q * usq) / ((double)gamma + 1.0);
+    const T gt = (T)(dt / (double)(rqm * gamma));
+    const T bp[3] = {b1 * gt, b2 * gt, b3 * gt};
+    const T bsq = (bp[0] * bp[0] + bp[1] * bp[1]) + bp[2] * bp[2];
+    const T bn = sqrtR(bsq);
+    T s = sinR(bn / T(2.0));
+    const T a = cosR(bn / T(2.0));
+    s = bsq > T(0.0) ? -s / bn : T(-1.0);
+    const T qb = bp[0] * s, qc = bp[1] * s, qd = bp[2] * s;
+    const T r11 = ((a * a + qb * qb) - qc * qc) - qd * qd, r21 = T(2.0) * (qb * qc - a * qd),
+            r31 = T(2.0) * (qb * qd + a * qc);
+    const T r12 = T(2.0) * (qb * qc + a * qd), r22 = ((a * a + qc * qc) - qb * qb) - qd * qd,
+            r32 = T(2.0) * (qc * qd - a * qb);
+    const T r13 = T(2.0) * (qb * qd - a * qc), r23 = T(2.0) * (qc * qd + a * qb),
+            r33 = ((a * a + qd * qd) - qb * qb) - qc * qc;
+    u1 = ((r11 * ut[0] + r21 * ut[1]) + r31 * ut[2]) + ep[0];
+    u2 = ((r12 * ut[0] + r22 * ut[1]) + r32 * ut[2]) + ep[1];
+    u3 = ((r13 * ut[0] + r23 * ut[1]) + r33 * ut[2]) + ep[2];
+    return ene;
+}
+
 // the pusher-specific tem of the Fortran pushers from the double dt and the species' rqm
+// (Higuera-Cary, full and Euler rotation: 0.5 (dt / rqm); Boris and Vay: 0.5 dt / rqm)
 inline double pusher_tem(int pusher, double dt, double rqm)
 {
-    return pusher == OSG_PUSHER_HC ? 0.5 * (dt / rqm) : 0.5 * dt / rqm;
+    return pusher == OSG_PUSHER_HC || pusher == OSG_PUSHER_FULLROT || pusher == OSG_PUSHER_EULER
+               ? 0.5 * (dt / rqm)
+               : 0.5 * dt / rqm;
 }
 
 } // namespace osg

@@ -278,6 +278,11 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
                 my_ene = (double)vay_push<T>(a.tem, E1, E2, E3, B1, B2, B3, q, u1, u2, u3);
             } else if (a.pusher == OSG_PUSHER_HC) {
                 my_ene = hc_push<T>(a.tem, E1, E2, E3, B1, B2, B3, q, u1, u2, u3);
+            } else if (a.pusher == OSG_PUSHER_FULLROT) {
+                my_ene = fullrot_push<T>(a.tem, E1, E2, E3, B1, B2, B3, q, u1, u2, u3);
+            } else if (a.pusher == OSG_PUSHER_EULER) {
+                my_ene = euler_push<T>(a.tem, a.rqm, a.dt_full, E1, E2, E3, B1, B2, B3, q, u1,
+                                       u2, u3);
             } else {
                 const T ene = boris(a.tem, E1, E2, E3, B1, B2, B3, u1, u2, u3);
                 my_ene = (double)q * (double)ene;
@@ -370,6 +375,7 @@ PlainPushArgs<T> make_plain_args(int dim, int order, int *ix, T *x, T *u, const 
     a.wrap[0] = a.wrap[1] = a.wrap[2] = 0;
     a.pusher = OSG_PUSHER_BORIS;
     a.qm = T(1) / rqm;
+    a.rqm = rqm;
     a.dt_full = dt;
     a.iter_tol = 1.0e-3;
     a.ene = d_ene;

@@ -26,8 +26,9 @@ template <typename T> struct PlainPushArgs {
     long emf_Dy, emf_Dz, j_Dy, j_Dz;
     int emf_off[3], emf_size[3], j_off[3], j_size[3];
     int wrap[3];           // > 0: periodic wrap of the stored cell index into [1, wrap[d]]
-    int pusher;            // OSG_PUSHER_BORIS or OSG_PUSHER_EXACT
+    int pusher;            // OSG_PUSHER_*
     T qm;                  // 1 / rqm (exact pusher)
+    T rqm;                 // the species' rqm (Euler-rotation pusher)
     double dt_full;        // the double time step (exact pusher)
     double iter_tol;       // Newton tolerance of the exact pusher
     double *ene;           // device accumulator (incremented)

@@ -273,7 +273,7 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
             for (int d = 0; d < c.dim; d++) a.wrap[d] = c.nx[d];
             a.pusher = c.pusher;
             a.iter_tol = c.iter_tol;
-            if (c.pusher == OSG_PUSHER_VAY || c.pusher == OSG_PUSHER_HC)
+            if (c.pusher >= OSG_PUSHER_VAY)
                 a.tem = (T)pusher_tem(c.pusher, push_dt, (double)(T)s->rqm[k]);
             int rc = launch_plain_push<T>(c.dim, c.order, a, st);
             if (rc) return rc;
@@ -426,7 +426,7 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               "unknown engine");
     OSG_CHECK(!(cfg->engine == OSG_ENGINE_TILED && cfg->precision != 32), OSG_ERR_ARG,
               "the tiled engine is single precision");
-    OSG_CHECK(cfg->pusher >= OSG_PUSHER_BORIS && cfg->pusher <= OSG_PUSHER_HC, OSG_ERR_ARG,
+    OSG_CHECK(cfg->pusher >= OSG_PUSHER_BORIS && cfg->pusher <= OSG_PUSHER_EULER, OSG_ERR_ARG,
               "unknown pusher");
     OSG_CHECK(cfg->iter_tol >= 0, OSG_ERR_ARG, "iter_tol must be >= 0");
     double cour = 0.0;

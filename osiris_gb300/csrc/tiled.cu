@@ -147,6 +147,8 @@ static cudaError_t push_attr(int pusher, int dim, int order, int bytes)
     case OSG_PUSHER_EXACT: return push_tiled_attr_exact(dim, order, bytes);
     case OSG_PUSHER_VAY: return push_tiled_attr_vay(dim, order, bytes);
     case OSG_PUSHER_HC: return push_tiled_attr_hc(dim, order, bytes);
+    case OSG_PUSHER_FULLROT: return push_tiled_attr_fullrot(dim, order, bytes);
+    case OSG_PUSHER_EULER: return push_tiled_attr_euler(dim, order, bytes);
     default: return push_tiled_attr_boris(dim, order, bytes);
     }
 }
@@ -318,6 +320,7 @@ static int upload_tables(TiledState *t, cudaStream_t st)
             tab[k].in = t->buf[p][k];
             tab[k].out = t->buf[1 - p][k];
             tab[k].tem = (float)pusher_tem(t->pusher, push_dt(t), (double)(float)t->rqm[k]);
+            tab[k].rqm = (float)t->rqm[k];
             tab[k].qm = 1.0f / (float)t->rqm[k];
             tab[k].cap = t->cap[k];
         }
@@ -611,6 +614,8 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     case OSG_PUSHER_EXACT: rc = push_tiled_launch_exact(t->dim, t->order, a, nt, t->threads, sm, st); break;
     case OSG_PUSHER_VAY: rc = push_tiled_launch_vay(t->dim, t->order, a, nt, t->threads, sm, st); break;
     case OSG_PUSHER_HC: rc = push_tiled_launch_hc(t->dim, t->order, a, nt, t->threads, sm, st); break;
+    case OSG_PUSHER_FULLROT: rc = push_tiled_launch_fullrot(t->dim, t->order, a, nt, t->threads, sm, st); break;
+    case OSG_PUSHER_EULER: rc = push_tiled_launch_euler(t->dim, t->order, a, nt, t->threads, sm, st); break;
     default: rc = push_tiled_launch_boris(t->dim, t->order, a, nt, t->threads, sm, st); break;
     }
     if (rc) return rc;

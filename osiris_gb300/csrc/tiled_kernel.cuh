@@ -85,6 +85,7 @@ struct SpeciesDev {
     Slabs in, out;
     float tem;     // dt / (2 rqm) (Boris)
     float qm;      // 1 / rqm (exact pusher)
+    float rqm;     // rqm (Euler-rotation pusher)
     long cap;      // slots per tile
 };
 
@@ -369,6 +370,12 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 } else if constexpr (PUSHER == OSG_PUSHER_HC) {
                     my_ene += (float)hc_push<float>(sd.tem, E1, E2, E3, B1, B2, B3, q, un[0],
                                                     un[1], un[2]);
+                } else if constexpr (PUSHER == OSG_PUSHER_FULLROT) {
+                    my_ene += (float)fullrot_push<float>(sd.tem, E1, E2, E3, B1, B2, B3, q,
+                                                         un[0], un[1], un[2]);
+                } else if constexpr (PUSHER == OSG_PUSHER_EULER) {
+                    my_ene += (float)euler_push<float>(sd.tem, sd.rqm, a.dt_full, E1, E2, E3, B1,
+                                                       B2, B3, q, un[0], un[1], un[2]);
                 } else {
                     const float ene = boris(sd.tem, E1, E2, E3, B1, B2, B3, un[0], un[1], un[2]);
                     my_ene = fmaf(q, ene, my_ene);
@@ -834,8 +841,8 @@ __global__ void k_count_move(int *moved);
 
 // Launch of the push kernel of one (dim, order) for each pusher, and the opt-in to its dynamic
 // shared memory (call outside stream capture).  tiled.cu defines the Boris pair, tiled_exact.cu
-// the exact-pusher pair, tiled_vay.cu and tiled_hc.cu the Vay and Higuera-Cary pairs (one unit
-// each, so they compile in parallel).
+// the exact-pusher pair, tiled_vay.cu, tiled_hc.cu, tiled_fullrot.cu and tiled_euler.cu the
+// other pushers' pairs (one unit each, so they compile in parallel).
 int push_tiled_launch_boris(int dim, int order, const TiledArgs &a, unsigned ntiles,
                             int threads, size_t smem, cudaStream_t st);
 cudaError_t push_tiled_attr_boris(int dim, int order, int bytes);
@@ -848,6 +855,12 @@ cudaError_t push_tiled_attr_vay(int dim, int order, int bytes);
 int push_tiled_launch_hc(int dim, int order, const TiledArgs &a, unsigned ntiles, int threads,
                          size_t smem, cudaStream_t st);
 cudaError_t push_tiled_attr_hc(int dim, int order, int bytes);
+int push_tiled_launch_fullrot(int dim, int order, const TiledArgs &a, unsigned ntiles,
+                              int threads, size_t smem, cudaStream_t st);
+cudaError_t push_tiled_attr_fullrot(int dim, int order, int bytes);
+int push_tiled_launch_euler(int dim, int order, const TiledArgs &a, unsigned ntiles, int threads,
+                            size_t smem, cudaStream_t st);
+cudaError_t push_tiled_attr_euler(int dim, int order, int bytes);
 // persistent launch over a (box, tile) work list (k_push_tiled_batch, Boris pusher; defined
 // in batch_push.cu)
 int push_batch_launch(int dim, int order, const TiledArgs *boxes, const int2 *work, int nwork,

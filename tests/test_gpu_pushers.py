@@ -1,11 +1,12 @@
-"""GPU parity of the Vay and Higuera-Cary momentum updates (push_type "vay" and "cary",
-dudt_vay / dudt_cary) against the CPU oracle, through the drop-in entry point
-osg_advance_deposit_* and through both engines of the device-resident time step.
+"""GPU parity of the Vay, Higuera-Cary, full-rotation and Euler-rotation momentum updates
+(push_type "vay", "cary", "fullrot", "euler"; dudt_vay / dudt_cary / dudt_fullrot / dudt_euler)
+against the CPU oracle, through the drop-in entry point osg_advance_deposit_* and through both
+engines of the device-resident time step.
 
 Tolerances (normwise max|a-b|/max|b|) as for the Boris path: FP64 1e-12, FP32 1e-5 for one
 call or step, 5e-5 over 10 steps.  The drop-in cases use fields of rms 5 and momenta of rms 2,
-where each update differs from Boris's by more than the FP32 tolerance (2e-5 .. 4e-4), so the
-comparison pins the pusher and not only the deposit.
+where each update differs from Boris's by more than the FP32 tolerance, so the comparison pins
+the pusher and not only the deposit.
 """
 import numpy as np
 import pytest
@@ -36,7 +37,7 @@ def _pos(ix, x):
     return ix.astype(np.float64) + x.astype(np.float64)
 
 
-@pytest.mark.parametrize("pusher", ["vay", "hc"])
+@pytest.mark.parametrize("pusher", ["vay", "hc", "fullrot", "euler"])
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 @pytest.mark.parametrize("dim,order", [(1, 2), (2, 1), (2, 2), (2, 3), (3, 2), (3, 4)])
 def test_gpu_pusher_dropin_matches_oracle(osg, oracle, pusher, prec, dim, order):
@@ -50,7 +51,8 @@ def test_gpu_pusher_dropin_matches_oracle(osg, oracle, pusher, prec, dim, order)
     e = (rng.standard_normal(g.shape) * 5.0).astype(dt_)
     b = (rng.standard_normal(g.shape) * 5.0).astype(dt_)
     dt = 0.04
-    code = {"vay": osg.PUSHER_VAY, "hc": osg.PUSHER_HC}[pusher]
+    code = {"vay": osg.PUSHER_VAY, "hc": osg.PUSHER_HC, "fullrot": osg.PUSHER_FULLROT,
+            "euler": osg.PUSHER_EULER}[pusher]
     a = [v.copy() for v in (ix, x, u, q)]
     j_g = g.zeros(prec)
     ene_g = osg.vadvance_deposit(dim, order, *a, 1, len(q), -1.0, e, b, g.size, g.gcl, j_g,
@@ -69,7 +71,7 @@ def test_gpu_pusher_dropin_matches_oracle(osg, oracle, pusher, prec, dim, order)
     assert _nerr(a[2], ub[2]) > (1e-10 if prec == "f64" else TOL[prec])
 
 
-@pytest.mark.parametrize("pusher", ["vay", "hc"])
+@pytest.mark.parametrize("pusher", ["vay", "hc", "fullrot", "euler"])
 @pytest.mark.parametrize("steps", [1, 10])
 @pytest.mark.parametrize("dim,order,nx", [(2, 2, [24, 20]), (3, 3, [10, 10, 10])])
 def test_plain_fp64_pusher_matches_oracle(osg, oracle, pusher, dim, order, nx, steps):
@@ -77,7 +79,7 @@ def test_plain_fp64_pusher_matches_oracle(osg, oracle, pusher, dim, order, nx, s
              pusher=pusher)
 
 
-@pytest.mark.parametrize("pusher", ["vay", "hc"])
+@pytest.mark.parametrize("pusher", ["vay", "hc", "fullrot", "euler"])
 @pytest.mark.parametrize("steps,tol", [(1, 1e-5), (10, 5e-5)])
 @pytest.mark.parametrize("dim,order,nx,tile", [(2, 2, [32, 24], [8, 8]),
                                                (3, 2, [16, 8, 8], [4, 4, 4])])

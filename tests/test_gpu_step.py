@@ -56,7 +56,9 @@ def _compare(osg, oracle, prec, engine, dim, order, nx, ppc, steps, tol, tile=No
     sim = osg.Simulation(nx, dx, dt, order=order, precision=prec, engine=engine, tile=tile,
                          n_sort=n_sort,
                          pusher={"boris": osg.PUSHER_BORIS, "exact": osg.PUSHER_EXACT,
-                                 "vay": osg.PUSHER_VAY, "hc": osg.PUSHER_HC}[pusher])
+                                 "vay": osg.PUSHER_VAY, "hc": osg.PUSHER_HC,
+                                 "fullrot": osg.PUSHER_FULLROT,
+                                 "euler": osg.PUSHER_EULER}[pusher])
     sim.set_fields(e, b)
     for s in species:
         sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])

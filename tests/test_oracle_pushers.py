@@ -1,8 +1,10 @@
-"""Known-answer tests of the oracle's Vay and Higuera-Cary momentum updates (dudt_vay,
-source/spec/os-spec-push.f03:636-796; dudt_cary, :1104-1253), restated from Fortran that cannot
-be run here: both keep |u| in a pure magnetic field, both keep a particle at the E x B drift
-velocity exactly for any step (their defining property), and both agree with the exact pusher
-to O(dt^3) per step; the step-level push with them conserves charge."""
+"""Known-answer tests of the oracle's Vay, Higuera-Cary, full-rotation and Euler-rotation
+momentum updates (dudt_vay, source/spec/os-spec-push.f03:636-796; dudt_cary, :1104-1253;
+dudt_fullrot, :83-231; dudt_euler, :235-352), restated from Fortran that cannot be run here:
+all keep |u| in a pure magnetic field; Vay and Higuera-Cary keep a particle at the E x B drift
+velocity exactly for any step (their defining property); the two rotation pushers turn the
+momentum by the exact gyration angle in a uniform magnetic field (Boris does not); all agree
+with the exact pusher to O(dt^3) per step; the step-level push with them conserves charge."""
 import numpy as np
 import pytest
 
@@ -18,7 +20,7 @@ def _run(oracle, pusher, e, b, u0, dt, steps=1, prec="f64"):
     return u.astype(np.float64)
 
 
-@pytest.mark.parametrize("pusher", ["vay", "hc"])
+@pytest.mark.parametrize("pusher", ["vay", "hc", "fullrot", "euler"])
 def test_pure_b_keeps_energy(oracle, pusher):
     rng = np.random.default_rng(1)
     u0 = rng.standard_normal((8, 3))
@@ -39,7 +41,27 @@ def test_exb_drift_is_kept(oracle, pusher):
     assert np.abs(u - u0).max() < 1e-12
 
 
-@pytest.mark.parametrize("pusher", ["vay", "hc"])
+@pytest.mark.parametrize("pusher", ["fullrot", "euler"])
+def test_rotation_pushers_gyrate_by_the_exact_angle(oracle, pusher):
+    # u perpendicular to a uniform B along z: per step the exact gyration angle is
+    # |B| dt / (rqm gamma) (rqm = -1), which Boris only approximates (2 atan of half of it)
+    b0, dt, n = 1.3, 0.4, 25
+    u0 = np.array([[0.7, -0.2, 0.0]])
+    g = np.sqrt(1.0 + (u0 ** 2).sum())
+    b = np.array([[0.0, 0.0, b0]])
+    u = _run(oracle, pusher, np.zeros_like(b), b, u0, dt, steps=n)
+    th = n * (-(b0 * dt) / g)            # rotation u -> R(th) u  (u x B force for rqm = -1)
+    want = np.array([[u0[0, 0] * np.cos(th) + u0[0, 1] * np.sin(th),
+                      -u0[0, 0] * np.sin(th) + u0[0, 1] * np.cos(th), 0.0]])
+    assert np.abs(u - want).max() < 1e-12
+    # and not by the Boris angle 2 atan(theta / 2)
+    tb = n * (-2.0 * np.arctan(0.5 * b0 * dt / g))
+    boris = np.array([[u0[0, 0] * np.cos(tb) + u0[0, 1] * np.sin(tb),
+                       -u0[0, 0] * np.sin(tb) + u0[0, 1] * np.cos(tb), 0.0]])
+    assert np.abs(u - boris).max() > 1e-3
+
+
+@pytest.mark.parametrize("pusher", ["vay", "hc", "fullrot", "euler"])
 def test_second_order_against_exact(oracle, pusher):
     rng = np.random.default_rng(4)
     e = rng.standard_normal((6, 3)) * 0.5
@@ -54,7 +76,7 @@ def test_second_order_against_exact(oracle, pusher):
     assert errs[0] < 1e-4
 
 
-@pytest.mark.parametrize("pusher", ["vay", "hc"])
+@pytest.mark.parametrize("pusher", ["vay", "hc", "fullrot", "euler"])
 def test_push_with_pusher_conserves_charge(oracle, pusher):
     dim, order, nx = 2, 2, [8, 7]
     g = oracle.Grid(nx, order, [0.1] * dim)
