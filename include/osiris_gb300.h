@@ -310,6 +310,17 @@ int osg_sim_set_window(osg_sim *s, int species, const int *ppc, int nprof, const
 int osg_sim_window_moves(osg_sim *s, long *moves);
 /* guard cells per axis of the sim's grids (order-dependent, widened for smoothing) */
 int osg_sim_guard_cells(osg_sim *s, int *gcl, int *gcu);
+/* Checkpoint / restart of the device-resident state (the role of the reference's
+ * write_restart / read_restart, source/os-main.f03:299-343, for the objects on this path):
+ * the configuration, step count, moving-window state, every species' particles (reference
+ * layout, the run's precision) and E, B are written to one binary file; osg_sim_restore
+ * creates a simulation from it that continues the run.  The current is rebuilt by the next
+ * step.  Returns OSG_ERR_ARG for a file that is missing, truncated or not a checkpoint. */
+int osg_sim_checkpoint(osg_sim *s, const char *path);
+int osg_sim_restore(const char *path, osg_sim **out);
+/* the configuration a simulation runs with, its species count and their rqm (rqm may be
+ * null; else room for OSG_MAX_SPECIES values) */
+int osg_sim_get_config(osg_sim *s, osg_config *cfg, int *nspecies, double *rqm);
 /* Number of kernel launches one step issues (for launch accounting). */
 int osg_sim_launches_per_step(osg_sim *s);
 /* Run n steps bracketed by CUDA events on the simulation's stream; *ms = device time. */

@@ -136,6 +136,9 @@ def _declare_batch(lb):
     lb.osg_sim_set_window.argtypes = [P, I, P, I, P, P]
     lb.osg_sim_window_moves.argtypes = [P, P]
     lb.osg_sim_guard_cells.argtypes = [P, P, P]
+    lb.osg_sim_checkpoint.argtypes = [P, C.c_char_p]
+    lb.osg_sim_restore.argtypes = [C.c_char_p, C.POINTER(P)]
+    lb.osg_sim_get_config.argtypes = [P, C.POINTER(Config), C.POINTER(I), P]
     lb.osg_smooth_f32.argtypes = [I, P, P, P, P, P, P]
     lb.osg_smooth_f64.argtypes = [I, P, P, P, P, P, P]
     lb.osg_smooth_coefficients.argtypes = [I, I, P, P]
@@ -387,13 +390,39 @@ class Simulation:
         self.dt = dt
         self.h = P()
         _check(lib().osg_sim_create(C.byref(cfg), C.byref(self.h)))
+        self._guards()
+        self.nspecies = 0
+        self.rqm = []
+
+    def _guards(self):
         # guard cells as created (wider than the interpolation needs when smoothing)
         gcl, gcu = np.zeros(3, np.int32), np.zeros(3, np.int32)
         _check(lib().osg_sim_guard_cells(self.h, _p(gcl), _p(gcu)))
         self.gcl, self.gcu = [int(v) for v in gcl[: self.dim]], [int(v) for v in gcu[: self.dim]]
         self.size = [n + a + b for n, a, b in zip(self.nx, self.gcl, self.gcu)]
-        self.nspecies = 0
-        self.rqm = []
+
+    def checkpoint(self, path):
+        """Write the device-resident state to `path` (osg_sim_checkpoint)."""
+        _check(lib().osg_sim_checkpoint(self.h, os.fsencode(str(path))))
+
+    @classmethod
+    def restore(cls, path):
+        """A simulation that continues the run checkpointed in `path` (osg_sim_restore)."""
+        self = cls.__new__(cls)
+        self.h = P()
+        _check(lib().osg_sim_restore(os.fsencode(str(path)), C.byref(self.h)))
+        cfg, ns, rqm = Config(), I(), np.zeros(16)
+        _check(lib().osg_sim_get_config(self.h, C.byref(cfg), C.byref(ns), _p(rqm)))
+        self.cfg = cfg
+        self.dim, self.order, self.precision = cfg.dim, cfg.order, cfg.precision
+        self.dtype = np.float32 if cfg.precision == 32 else np.float64
+        self.nx = [int(cfg.nx[d]) for d in range(self.dim)]
+        self.dx = [float(cfg.dx[d]) for d in range(self.dim)]
+        self.dt = float(cfg.dt)
+        self._guards()
+        self.nspecies = int(ns.value)
+        self.rqm = [float(v) for v in rqm[: self.nspecies]]
+        return self
 
     def close(self):
         if self.h:

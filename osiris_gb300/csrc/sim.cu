@@ -14,6 +14,7 @@
 #include <algorithm>
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -708,6 +709,150 @@ int osg_sim_set_window(osg_sim *s, int species, const int *ppc, int nprof, const
     s->xmoved = s->cfg.dt;
     s->moves = 0;
     s->graphs_dirty = true;
+    return OSG_OK;
+}
+
+// ------------------------------------------------------------------------ checkpoint
+// File layout (native byte order, as the reference's restart files): the tag "OSGCKPT1", the
+// int size of osg_config and the struct, long step count, int window flag, double xmoved,
+// long window moves, the window's injection parameters (int species, int ppc[3], int nprof,
+// double prof_x[8], double prof_f[8]), int species count, then per species double rqm, long
+// np and its arrays in reference layout (ix(dim,np) int, x(dim,np), u(3,np), q(np) in the
+// run's precision), last long grid points and E(3,points), B(3,points) with guard cells.
+// The current is rebuilt by the next step and is not stored.
+namespace {
+
+struct CkptFile {
+    FILE *f = nullptr;
+    ~CkptFile()
+    {
+        if (f) fclose(f);
+    }
+};
+
+bool put(FILE *f, const void *p, size_t n) { return n == 0 || fwrite(p, 1, n, f) == n; }
+bool get(FILE *f, void *p, size_t n) { return n == 0 || fread(p, 1, n, f) == n; }
+
+const char CKPT_TAG[8] = {'O', 'S', 'G', 'C', 'K', 'P', 'T', '1'};
+
+} // namespace
+
+int osg_sim_checkpoint(osg_sim *s, const char *path)
+{
+    OSG_CHECK(s && path, OSG_ERR_ARG, "bad arguments");
+    CkptFile cf;
+    cf.f = fopen(path, "wb");
+    OSG_CHECK(cf.f, OSG_ERR_ARG, "cannot open %s for writing", path);
+    FILE *f = cf.f;
+    const int csz = (int)sizeof(osg_config), win = s->window ? 1 : 0;
+    int wsp = -1, wppc[3] = {1, 1, 1}, wn = 0;
+    double wx[8] = {0}, wf[8] = {0};
+    if (s->window) tiled_window_params(s->tiled, &wsp, wppc, &wn, wx, wf);
+    const int ns = (int)s->np.size();
+    bool ok = put(f, CKPT_TAG, 8) && put(f, &csz, sizeof csz) && put(f, &s->cfg, sizeof s->cfg) &&
+              put(f, &s->step_n, sizeof s->step_n) && put(f, &win, sizeof win) &&
+              put(f, &s->xmoved, sizeof s->xmoved) && put(f, &s->moves, sizeof s->moves) &&
+              put(f, &wsp, sizeof wsp) && put(f, wppc, sizeof wppc) && put(f, &wn, sizeof wn) &&
+              put(f, wx, sizeof wx) && put(f, wf, sizeof wf) && put(f, &ns, sizeof ns);
+    const int dim = s->cfg.dim;
+    for (int k = 0; ok && k < ns; k++) {
+        long np = 0;
+        int rc = osg_sim_num_particles(s, k, &np);
+        if (rc) return rc;
+        std::vector<int> ix((size_t)dim * np);
+        std::vector<char> x((size_t)s->esz * dim * np), u((size_t)s->esz * 3 * np),
+            q((size_t)s->esz * np);
+        if (np > 0 && (rc = osg_sim_get_species(s, k, ix.data(), x.data(), u.data(), q.data())))
+            return rc;
+        ok = put(f, &s->rqm[k], sizeof(double)) && put(f, &np, sizeof np) &&
+             put(f, ix.data(), ix.size() * sizeof(int)) && put(f, x.data(), x.size()) &&
+             put(f, u.data(), u.size()) && put(f, q.data(), q.size());
+    }
+    const long npt = (long)s->g.npoints();
+    std::vector<char> e((size_t)s->esz * 3 * npt), b(e.size());
+    if (ok) {
+        const int rc = osg_sim_get_fields(s, e.data(), b.data(), nullptr);
+        if (rc) return rc;
+        ok = put(f, &npt, sizeof npt) && put(f, e.data(), e.size()) && put(f, b.data(), b.size());
+    }
+    OSG_CHECK(ok && fflush(f) == 0, OSG_ERR_ARG, "write to %s failed", path);
+    return OSG_OK;
+}
+
+int osg_sim_restore(const char *path, osg_sim **out)
+{
+    OSG_CHECK(path && out, OSG_ERR_ARG, "bad arguments");
+    *out = nullptr;
+    CkptFile cf;
+    cf.f = fopen(path, "rb");
+    OSG_CHECK(cf.f, OSG_ERR_ARG, "cannot open %s", path);
+    FILE *f = cf.f;
+    char tag[8];
+    int csz = 0, win = 0, wsp = -1, wppc[3], wn = 0, ns = 0;
+    osg_config cfg;
+    long step_n = 0, moves = 0;
+    double xmoved = 0.0, wx[8], wf[8];
+    bool ok = get(f, tag, 8) && memcmp(tag, CKPT_TAG, 8) == 0 && get(f, &csz, sizeof csz) &&
+              csz == (int)sizeof(osg_config) && get(f, &cfg, sizeof cfg) &&
+              get(f, &step_n, sizeof step_n) && get(f, &win, sizeof win) &&
+              get(f, &xmoved, sizeof xmoved) && get(f, &moves, sizeof moves) &&
+              get(f, &wsp, sizeof wsp) && get(f, wppc, sizeof wppc) && get(f, &wn, sizeof wn) &&
+              get(f, wx, sizeof wx) && get(f, wf, sizeof wf) && get(f, &ns, sizeof ns);
+    OSG_CHECK(ok && ns >= 0 && ns <= MAX_SPECIES && step_n >= 0, OSG_ERR_ARG,
+              "%s is not a checkpoint of this library", path);
+    osg_sim *s = nullptr;
+    int rc = osg_sim_create(&cfg, &s);
+    if (rc) return rc;
+    const int dim = cfg.dim, esz = s->esz;
+    for (int k = 0; k < ns && rc == OSG_OK; k++) {
+        double rqm = 0.0;
+        long np = -1;
+        if (!(get(f, &rqm, sizeof rqm) && get(f, &np, sizeof np) && np >= 0)) {
+            rc = OSG_ERR_ARG;
+            break;
+        }
+        std::vector<int> ix((size_t)dim * np);
+        std::vector<char> x((size_t)esz * dim * np), u((size_t)esz * 3 * np), q((size_t)esz * np);
+        if (!(get(f, ix.data(), ix.size() * sizeof(int)) && get(f, x.data(), x.size()) &&
+              get(f, u.data(), u.size()) && get(f, q.data(), q.size()))) {
+            rc = OSG_ERR_ARG;
+            break;
+        }
+        rc = osg_sim_add_species(s, rqm, np, ix.data(), x.data(), u.data(), q.data());
+        if (rc > 0) rc = OSG_OK;   // the species index
+    }
+    long npt = 0;
+    if (rc == OSG_OK) {
+        std::vector<char> e((size_t)esz * 3 * s->g.npoints()), b(e.size());
+        if (!(get(f, &npt, sizeof npt) && npt == (long)s->g.npoints() && get(f, e.data(), e.size()) &&
+              get(f, b.data(), b.size())))
+            rc = OSG_ERR_ARG;
+        else
+            rc = osg_sim_set_fields(s, e.data(), b.data());
+    }
+    if (rc == OSG_OK && win) {
+        rc = osg_sim_set_window(s, wsp, wppc, wn, wx, wf);
+        if (rc == OSG_OK) rc = tiled_set_moves(s->tiled, moves, s->st);
+        s->xmoved = xmoved;
+        s->moves = moves;
+    }
+    if (rc != OSG_OK) {
+        osg_sim_destroy(s);
+        if (rc == OSG_ERR_ARG) set_error("%s: truncated or inconsistent checkpoint", path);
+        return rc;
+    }
+    s->step_n = step_n;
+    *out = s;
+    return OSG_OK;
+}
+
+int osg_sim_get_config(osg_sim *s, osg_config *cfg, int *nspecies, double *rqm)
+{
+    OSG_CHECK(s && cfg && nspecies, OSG_ERR_ARG, "bad arguments");
+    *cfg = s->cfg;
+    *nspecies = (int)s->np.size();
+    if (rqm)
+        for (int k = 0; k < *nspecies; k++) rqm[k] = s->rqm[k];
     return OSG_OK;
 }
 

@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
@@ -521,6 +522,29 @@ int tiled_set_threads(TiledState *t, int threads)
 __global__ void k_count_move(int *moved)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0) *moved += 1;
+}
+
+bool tiled_window_params(const TiledState *t, int *species, int *ppc, int *nprof,
+                         double *prof_x, double *prof_f)
+{
+    if (!t->window) return false;
+    *species = t->inj_species;
+    for (int d = 0; d < 3; d++) ppc[d] = t->inj_ppc[d];
+    *nprof = t->nprof;
+    for (int k = 0; k < 8; k++) {
+        prof_x[k] = t->prof_x[k];
+        prof_f[k] = t->prof_f[k];
+    }
+    return true;
+}
+
+int tiled_set_moves(TiledState *t, long moves, cudaStream_t st)
+{
+    OSG_CHECK(t->d_moved && moves >= 0 && moves <= INT_MAX, OSG_ERR_STATE, "no window");
+    const int m = (int)moves;
+    OSG_CUDA(cudaMemcpyAsync(t->d_moved, &m, sizeof(int), cudaMemcpyHostToDevice, st));
+    OSG_CUDA(cudaStreamSynchronize(st));
+    return OSG_OK;
 }
 
 int tiled_set_window(TiledState *t, int species, const int *ppc, int nprof,

@@ -24,6 +24,11 @@ int tiled_set_window(TiledState *t, int species, const int *ppc, int nprof,
                      const double *prof_x, const double *prof_f);
 int tiled_window_inject(TiledState *t, int parity, int *d_status, cudaStream_t st,
                         int *launches);
+// the window's injection parameters (false: no window), and the device count of window moves
+// (read by the injection) set to `moves` (restart)
+bool tiled_window_params(const TiledState *t, int *species, int *ppc, int *nprof,
+                         double *prof_x, double *prof_f);
+int tiled_set_moves(TiledState *t, long moves, cudaStream_t st);
 // `cur` = index (0/1) of the buffer that holds the current particles
 int tiled_count(TiledState *t, int cur, int k, long *np, cudaStream_t st);
 int tiled_get_species(TiledState *t, int cur, int k, int *ix, float *x, float *u, float *q,
