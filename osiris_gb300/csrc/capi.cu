@@ -13,6 +13,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -39,26 +42,32 @@ void set_error(const char *fmt, ...)
 }
 
 // per-thread device staging for the host-array entry points
+static const int SIDE_STREAMS = 3;
+
 struct Staging {
     cudaStream_t stream = nullptr;
-    cudaStream_t side = nullptr;          // second stream of the chunked host-array push
-    cudaEvent_t ev[2] = {nullptr, nullptr};
+    // further streams of the chunked host-array push (chunk k on stream k % 4): the copies in
+    // and out of some chunks overlap the pushes of others
+    cudaStream_t side[SIDE_STREAMS] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev[1 + SIDE_STREAMS] = {nullptr, nullptr, nullptr, nullptr};
     void *buf[8] = {nullptr};
     size_t cap[8] = {0};
     ~Staging()
     {
         for (int i = 0; i < 8; i++)
             if (buf[i]) cudaFree(buf[i]);
-        for (int i = 0; i < 2; i++)
+        for (int i = 0; i < 1 + SIDE_STREAMS; i++)
             if (ev[i]) cudaEventDestroy(ev[i]);
-        if (side) cudaStreamDestroy(side);
+        for (int i = 0; i < SIDE_STREAMS; i++)
+            if (side[i]) cudaStreamDestroy(side[i]);
         if (stream) cudaStreamDestroy(stream);
     }
     int streams()
     {
         if (!stream) OSG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-        if (!side) OSG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-        for (int i = 0; i < 2; i++)
+        for (int i = 0; i < SIDE_STREAMS; i++)
+            if (!side[i]) OSG_CUDA(cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking));
+        for (int i = 0; i < 1 + SIDE_STREAMS; i++)
             if (!ev[i]) OSG_CUDA(cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming));
         return OSG_OK;
     }
@@ -116,7 +125,8 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
     if ((rc = g_stage.get(6, sizeof(T) * gj, &d_j))) return rc;
     if ((rc = g_stage.get(7, 64, &d_misc))) return rc;
     if ((rc = g_stage.streams())) return rc;
-    cudaStream_t st = g_stage.stream, side = g_stage.side;
+    cudaStream_t st = g_stage.stream;
+    cudaStream_t all[1 + SIDE_STREAMS] = {st, g_stage.side[0], g_stage.side[1], g_stage.side[2]};
     const long o = (long)i0 - 1;
     double *d_ene = (double *)d_misc;
     int *d_status = (int *)((char *)d_misc + 16);
@@ -125,14 +135,14 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
     OSG_CUDA(cudaMemcpyAsync(d_b, b, sizeof(T) * ge, cudaMemcpyHostToDevice, st));
     OSG_CUDA(cudaMemcpyAsync(d_j, j, sizeof(T) * gj, cudaMemcpyHostToDevice, st));
     OSG_CUDA(cudaEventRecord(g_stage.ev[0], st));
-    OSG_CUDA(cudaStreamWaitEvent(side, g_stage.ev[0], 0));
-    // The particle range goes in chunks on two streams, so the copies of one chunk overlap the
-    // push of the other (per-particle results do not depend on the chunking; the current and
-    // energy sums are atomic either way).
-    const long chunk = np > (4L << 20) ? (np + 7) / 8 : np;
+    for (int i = 0; i < SIDE_STREAMS; i++) OSG_CUDA(cudaStreamWaitEvent(all[1 + i], g_stage.ev[0], 0));
+    // The particle range goes in chunks over four streams, so the copies in and out of some
+    // chunks overlap the pushes of others (per-particle results do not depend on the chunking;
+    // the current and energy sums are atomic either way).
+    const long chunk = np > (2L << 20) ? (np + 15) / 16 : np;
     for (long c0 = 0, k = 0; c0 < np; c0 += chunk, k++) {
         const long n = std::min(chunk, np - c0), h = o + c0;
-        cudaStream_t cs = (k & 1) ? side : st;
+        cudaStream_t cs = all[k % (1 + SIDE_STREAMS)];
         int *cix = (int *)d_ix + dim * c0;
         T *cx = (T *)d_x + dim * c0, *cu = (T *)d_u + 3 * c0, *cq = (T *)d_q + c0;
         OSG_CUDA(cudaMemcpyAsync(cix, ix + dim * h, sizeof(int) * dim * n, cudaMemcpyHostToDevice, cs));
@@ -151,8 +161,10 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
         OSG_CUDA(cudaMemcpyAsync(x + dim * h, cx, sizeof(T) * dim * n, cudaMemcpyDeviceToHost, cs));
         OSG_CUDA(cudaMemcpyAsync(u + 3 * h, cu, sizeof(T) * 3 * n, cudaMemcpyDeviceToHost, cs));
     }
-    OSG_CUDA(cudaEventRecord(g_stage.ev[1], side));
-    OSG_CUDA(cudaStreamWaitEvent(st, g_stage.ev[1], 0));
+    for (int i = 0; i < SIDE_STREAMS; i++) {
+        OSG_CUDA(cudaEventRecord(g_stage.ev[1 + i], all[1 + i]));
+        OSG_CUDA(cudaStreamWaitEvent(st, g_stage.ev[1 + i], 0));
+    }
     OSG_CUDA(cudaMemcpyAsync(j, d_j, sizeof(T) * gj, cudaMemcpyDeviceToHost, st));
     double h_ene = 0.0;
     int h_status = 0;
@@ -409,6 +421,93 @@ int osg_yee_advance_f64(int dim, const int *nx, const int *gcl, const int *gcu, 
     return yee_host<double>(dim, nx, gcl, gcu, e, b, j, dx, dt);
 }
 
+namespace {
+
+// Host worker threads started once and reused by every call (a wrap of 16 M particles takes
+// about a millisecond; starting threads per call would cost a sizeable part of it).  run(n, f)
+// calls f(0..n-1) spread over the workers and the calling thread and returns when all are done.
+class HostPool {
+  public:
+    static HostPool &get()
+    {
+        static HostPool pool;
+        return pool;
+    }
+    int size() const { return (int)workers_.size() + 1; }
+    void run(int n, const std::function<void(int)> &f)
+    {
+        std::lock_guard<std::mutex> one(call_);   // callers from several threads take turns
+        std::unique_lock<std::mutex> lk(m_);
+        job_ = &f;
+        njobs_ = n;
+        next_ = 0;
+        done_ = 0;
+        gen_++;
+        cv_.notify_all();
+        lk.unlock();
+        work();
+        lk.lock();
+        fin_.wait(lk, [&] { return done_ == njobs_; });
+        job_ = nullptr;
+    }
+
+  private:
+    HostPool()
+    {
+        unsigned nt = std::thread::hardware_concurrency();
+        if (nt == 0) nt = 1;
+        if (nt > 32) nt = 32;
+        for (unsigned t = 1; t < nt; t++) workers_.emplace_back([this] { loop(); });
+    }
+    ~HostPool()
+    {
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            stop_ = true;
+            cv_.notify_all();
+        }
+        for (auto &w : workers_) w.join();
+    }
+    void work()
+    {
+        for (;;) {
+            int i;
+            const std::function<void(int)> *f;
+            {
+                std::lock_guard<std::mutex> lk(m_);
+                if (!job_ || next_ >= njobs_) return;
+                i = next_++;
+                f = job_;
+            }
+            (*f)(i);
+            std::lock_guard<std::mutex> lk(m_);
+            if (++done_ == njobs_) fin_.notify_all();
+        }
+    }
+    void loop()
+    {
+        long seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(m_);
+                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+            }
+            work();
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex call_, m_;
+    std::condition_variable cv_, fin_;
+    const std::function<void(int)> *job_ = nullptr;
+    int njobs_ = 0, next_ = 0, done_ = 0;
+    long gen_ = 0;
+    bool stop_ = false;
+};
+
+} // namespace
+
 int osg_particle_wrap(int dim, const int *nx, long np, int *ix)
 {
     OSG_CHECK(dim >= 1 && dim <= 3 && nx && (np == 0 || ix), OSG_ERR_ARG, "bad arguments");
@@ -432,21 +531,17 @@ int osg_particle_wrap(int dim, const int *nx, long np, int *ix)
             }
         }
     };
-    unsigned nt = std::thread::hardware_concurrency();
-    if (nt == 0) nt = 1;
-    if (nt > 32) nt = 32;
-    if (np < (1L << 20)) nt = 1;
-    if (nt == 1) {
+    if (np < (1L << 20)) {
         wrap_range(0, np);
         return OSG_OK;
     }
-    std::vector<std::thread> pool;
-    const long chunk = (np + nt - 1) / nt;
-    for (unsigned t = 0; t < nt; t++) {
+    HostPool &pool = HostPool::get();
+    const int nparts = 4 * pool.size();
+    const long chunk = (np + nparts - 1) / nparts;
+    pool.run(nparts, [&](int t) {
         const long p0 = (long)t * chunk, p1 = std::min(np, p0 + chunk);
-        if (p0 < p1) pool.emplace_back(wrap_range, p0, p1);
-    }
-    for (auto &th : pool) th.join();
+        if (p0 < p1) wrap_range(p0, p1);
+    });
     return OSG_OK;
 }
 

@@ -16,6 +16,7 @@
 #include "common.cuh"
 #include "pic_math.cuh"
 #include "push_plain.cuh"
+#include "tile_ops.cuh"
 
 namespace osg {
 
@@ -153,12 +154,30 @@ __device__ __forceinline__ int wrap_cell(int c, int n)
     return c;
 }
 
+// FP32 2D orders whose per-warp value scratch (8 warps) fits 32 KB of static shared memory
+// deposit their in-cell segments by warp runs (cell_runs_deposit_global2): 2x faster on the
+// two-stream workload.  The others add every value with its own atomic (FP64: native double
+// atomics, and the runs measured 8% slower)
+template <typename T, int DIM, int ORD>
+constexpr bool plain_runs()
+{
+    return DIM == 2 && sizeof(T) == 4 && SegVals<2, ORD>::NV * SCR_LD * sizeof(T) * 8 <= 32768;
+}
+
 template <typename T, int DIM, int ORD>
 __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
 {
     constexpr int NP = ORD + 1;
+    constexpr bool RUNS = plain_runs<T, DIM, ORD>();
+    constexpr int NV = SegVals<2, ORD>::NV, NC = (NV + 31) / 32;
     const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
     double my_ene = 0.0;
+    long run_base = -1;   // RUNS: stencil origin of the in-cell segment in J (-1: none)
+    T rv[RUNS ? NV : 1];
+    if constexpr (RUNS) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) rv[k] = T(0);
+    }
     if (p < a.np) {
         int c[DIM];
         T x0[DIM];
@@ -318,8 +337,15 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
                 s[0].x0 = x0[0]; s[0].x1 = x1; s[0].y0 = x0[1]; s[0].y1 = y1;
                 s[0].vz = v3; s[0].i = c[0]; s[0].j = c[1];
                 const int ns = split2(s, dix, diy);
-                for (int t = 0; t < ns; t++)
-                    deposit2<T, ORD>(a.j, a.j_Dy, a.jn[0], a.jn[1], q, s[t]);
+                if constexpr (RUNS) {
+                    seg_values2<ORD, T>(s[0], q, a.jn[0], a.jn[1], rv);
+                    run_base = 3L * s[0].i + a.j_Dy * s[0].j;
+                    for (int t = 1; t < ns; t++)
+                        deposit2<T, ORD>(a.j, a.j_Dy, a.jn[0], a.jn[1], q, s[t]);
+                } else {
+                    for (int t = 0; t < ns; t++)
+                        deposit2<T, ORD>(a.j, a.j_Dy, a.jn[0], a.jn[1], q, s[t]);
+                }
             } else {
                 T x1 = fmaR(v1, a.dtdx[0], x0[0]);
                 T y1 = fmaR(v2, a.dtdx[1], x0[1]);
@@ -339,6 +365,16 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
                     deposit3<T, ORD>(a.j, a.j_Dy, a.j_Dz, a.jn[0], a.jn[1], a.jn[2], q, s[t]);
             }
         }
+    }
+    if constexpr (RUNS) {
+        __shared__ T sScr[8][NV * SCR_LD];
+        __shared__ long sBase[8][16];
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        int off[NC];
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+            off[c] = lane + 32 * c < NV ? seg_offset<2, ORD>(lane + 32 * c, (int)a.j_Dy, 0) : 0;
+        cell_runs_deposit_global2<T, ORD>(a.j, sScr[w], sBase[w], run_base, rv, off);
     }
     const double tot = block_sum(my_ene);
     if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.ene, tot);

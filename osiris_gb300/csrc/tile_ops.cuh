@@ -156,23 +156,22 @@ template <int DIM, int ORD> struct SegVals {
     static constexpr int NV = DIM == 2 ? 2 * ORD * NP + NP * NP : 3 * ORD * NP * NP;
 };
 
-template <int ORD>
-__device__ __forceinline__ void seg_values2(const Seg2<float> &g, float q, float jn0, float jn1,
-                                            float *v)
+template <int ORD, typename T = float>
+__device__ __forceinline__ void seg_values2(const Seg2<T> &g, T q, T jn0, T jn1, T *v)
 {
     constexpr int NP = ORD + 1;
-    float s0x[NP], s1x[NP], s0y[NP], s1y[NP], wl1[ORD], wl2[ORD];
+    T s0x[NP], s1x[NP], s0y[NP], s1y[NP], wl1[ORD], wl2[ORD];
     spline<ORD>(g.x0, s0x);
     spline<ORD>(g.x1, s1x);
     spline<ORD>(g.y0, s0y);
     spline<ORD>(g.y1, s1y);
-    const float qvz = (q * g.vz) * float(1.0 / 3.0);
+    const T qvz = (q * g.vz) * T(1.0 / 3.0);
     long_weights<ORD>(q * jn0, g.x0, g.x1, wl1);
     long_weights<ORD>(q * jn1, g.y0, g.y1, wl2);
     int n = 0;
 #pragma unroll
     for (int k2 = 0; k2 < NP; k2++) {
-        const float wp1 = s0y[k2] + s1y[k2];
+        const T wp1 = s0y[k2] + s1y[k2];
 #pragma unroll
         for (int k1 = 0; k1 < ORD; k1++) v[n++] = wl1[k1] * wp1;
     }
@@ -184,9 +183,9 @@ __device__ __forceinline__ void seg_values2(const Seg2<float> &g, float q, float
     for (int k2 = 0; k2 < NP; k2++)
 #pragma unroll
         for (int k1 = 0; k1 < NP; k1++) {
-            float t1 = fmaf(s1y[k2], s1x[k1], s0x[k1] * s0y[k2]);
-            const float t2 = fmaf(s0y[k2], s1x[k1], s0x[k1] * s1y[k2]);
-            t1 = fmaf(t2, 0.5f, t1);
+            T t1 = fmaR(s1y[k2], s1x[k1], s0x[k1] * s0y[k2]);
+            const T t2 = fmaR(s0y[k2], s1x[k1], s0x[k1] * s1y[k2]);
+            t1 = fmaR(t2, T(0.5), t1);
             v[n++] = qvz * t1;
         }
 }
@@ -744,6 +743,64 @@ __device__ __forceinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int n
             }
         }
         __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// 2D in-cell segments deposited into a global current array (the plain engine and the drop-in
+// push): one segment per lane, base = offset of its stencil origin in J (-1: none).  Runs of
+// lanes with one base (particles in cell order share cells) are summed per value through a
+// per-warp scratch of 16 rows (column-major, stride SCR_LD), and lane k adds each run's sum of
+// value k with one global atomic, instead of one atomic per particle and value.  Must be called
+// by all 32 lanes; off[c] = offset of value lane + 32 c from the stencil origin.
+// ------------------------------------------------------------------------------------------
+template <typename T, int ORD>
+__device__ __forceinline__ void cell_runs_deposit_global2(T *J, T *scr, long *sbase, long base,
+                                                          const T *v, const int *off)
+{
+    constexpr int NV = SegVals<2, ORD>::NV;
+    constexpr int NC = (NV + 31) / 32;
+    const int lane = (int)(threadIdx.x & 31);
+    const long prev = __shfl_up_sync(FULL_MASK, base, 1);
+    const unsigned ends = __ballot_sync(FULL_MASK, lane > 0 && prev != base) >> 1;
+    const long last = __shfl_sync(FULL_MASK, base, 31);
+    T acc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) acc[c] = T(0);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        if ((lane >> 4) == h) {
+            const int r = lane & 15;
+#pragma unroll
+            for (int k = 0; k < NV; k++) scr[k * SCR_LD + r] = v[k];
+            sbase[r] = base;
+        }
+        __syncwarp();
+        const unsigned eh = (ends >> (16 * h)) & 0xffffu;
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const int col = lane + 32 * c;
+            if (col < NV) {
+                const T *cv = scr + col * SCR_LD;
+                T a = acc[c];
+#pragma unroll 1
+                for (int r = 0; r < 16; r++) {
+                    a += cv[r];
+                    if (eh & (1u << r)) {
+                        const long key = sbase[r];
+                        if (key >= 0) atomicAdd(J + key + off[c], a);
+                        a = T(0);
+                    }
+                }
+                acc[c] = a;
+            }
+        }
+        __syncwarp();
+    }
+    if (last >= 0) {
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+            if (lane + 32 * c < NV) atomicAdd(J + last + off[c], acc[c]);
     }
 }
 
