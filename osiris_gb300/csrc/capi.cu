@@ -43,20 +43,21 @@ void set_error(const char *fmt, ...)
 
 // per-thread device staging for the host-array entry points
 static const int SIDE_STREAMS = 3;
+static const int PUSH_CHUNKS = 16;
 
 struct Staging {
     cudaStream_t stream = nullptr;
-    // further streams of the chunked host-array push (chunk k on stream k % 4): the copies in
-    // and out of some chunks overlap the pushes of others
+    // the chunked host-array push: copies in, pushes and copies out each on their own stream
+    // (side[0..2]), chunk by chunk, joined by per-chunk events
     cudaStream_t side[SIDE_STREAMS] = {nullptr, nullptr, nullptr};
-    cudaEvent_t ev[1 + SIDE_STREAMS] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[2 + 2 * PUSH_CHUNKS] = {nullptr};
     void *buf[8] = {nullptr};
     size_t cap[8] = {0};
     ~Staging()
     {
         for (int i = 0; i < 8; i++)
             if (buf[i]) cudaFree(buf[i]);
-        for (int i = 0; i < 1 + SIDE_STREAMS; i++)
+        for (int i = 0; i < 2 + 2 * PUSH_CHUNKS; i++)
             if (ev[i]) cudaEventDestroy(ev[i]);
         for (int i = 0; i < SIDE_STREAMS; i++)
             if (side[i]) cudaStreamDestroy(side[i]);
@@ -67,7 +68,7 @@ struct Staging {
         if (!stream) OSG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         for (int i = 0; i < SIDE_STREAMS; i++)
             if (!side[i]) OSG_CUDA(cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking));
-        for (int i = 0; i < 1 + SIDE_STREAMS; i++)
+        for (int i = 0; i < 2 + 2 * PUSH_CHUNKS; i++)
             if (!ev[i]) OSG_CUDA(cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming));
         return OSG_OK;
     }
@@ -126,7 +127,8 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
     if ((rc = g_stage.get(7, 64, &d_misc))) return rc;
     if ((rc = g_stage.streams())) return rc;
     cudaStream_t st = g_stage.stream;
-    cudaStream_t all[1 + SIDE_STREAMS] = {st, g_stage.side[0], g_stage.side[1], g_stage.side[2]};
+    cudaStream_t s_in = g_stage.side[0], s_push = g_stage.side[1], s_out = g_stage.side[2];
+    cudaEvent_t *ev = g_stage.ev;
     const long o = (long)i0 - 1;
     double *d_ene = (double *)d_misc;
     int *d_status = (int *)((char *)d_misc + 16);
@@ -134,37 +136,42 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
     OSG_CUDA(cudaMemcpyAsync(d_e, e, sizeof(T) * ge, cudaMemcpyHostToDevice, st));
     OSG_CUDA(cudaMemcpyAsync(d_b, b, sizeof(T) * ge, cudaMemcpyHostToDevice, st));
     OSG_CUDA(cudaMemcpyAsync(d_j, j, sizeof(T) * gj, cudaMemcpyHostToDevice, st));
-    OSG_CUDA(cudaEventRecord(g_stage.ev[0], st));
-    for (int i = 0; i < SIDE_STREAMS; i++) OSG_CUDA(cudaStreamWaitEvent(all[1 + i], g_stage.ev[0], 0));
-    // The particle range goes in chunks over four streams, so the copies in and out of some
-    // chunks overlap the pushes of others (per-particle results do not depend on the chunking;
+    OSG_CUDA(cudaEventRecord(ev[0], st));
+    OSG_CUDA(cudaStreamWaitEvent(s_in, ev[0], 0));
+    OSG_CUDA(cudaStreamWaitEvent(s_push, ev[0], 0));
+    OSG_CUDA(cudaStreamWaitEvent(s_out, ev[0], 0));
+    // The particle range goes in chunks through a three-stage pipeline: the copies in of chunk
+    // k + 1, the push of chunk k and the copies out of chunk k - 1 run at once, and neither
+    // copy direction waits for the other (per-particle results do not depend on the chunking;
     // the current and energy sums are atomic either way).
-    const long chunk = np > (2L << 20) ? (np + 15) / 16 : np;
+    const long nck = np > (2L << 20) ? PUSH_CHUNKS : 1;
+    const long chunk = (np + nck - 1) / nck;
     for (long c0 = 0, k = 0; c0 < np; c0 += chunk, k++) {
         const long n = std::min(chunk, np - c0), h = o + c0;
-        cudaStream_t cs = all[k % (1 + SIDE_STREAMS)];
         int *cix = (int *)d_ix + dim * c0;
         T *cx = (T *)d_x + dim * c0, *cu = (T *)d_u + 3 * c0, *cq = (T *)d_q + c0;
-        OSG_CUDA(cudaMemcpyAsync(cix, ix + dim * h, sizeof(int) * dim * n, cudaMemcpyHostToDevice, cs));
-        OSG_CUDA(cudaMemcpyAsync(cx, x + dim * h, sizeof(T) * dim * n, cudaMemcpyHostToDevice, cs));
-        OSG_CUDA(cudaMemcpyAsync(cu, u + 3 * h, sizeof(T) * 3 * n, cudaMemcpyHostToDevice, cs));
-        OSG_CUDA(cudaMemcpyAsync(cq, q + h, sizeof(T) * n, cudaMemcpyHostToDevice, cs));
+        OSG_CUDA(cudaMemcpyAsync(cix, ix + dim * h, sizeof(int) * dim * n, cudaMemcpyHostToDevice, s_in));
+        OSG_CUDA(cudaMemcpyAsync(cx, x + dim * h, sizeof(T) * dim * n, cudaMemcpyHostToDevice, s_in));
+        OSG_CUDA(cudaMemcpyAsync(cu, u + 3 * h, sizeof(T) * 3 * n, cudaMemcpyHostToDevice, s_in));
+        OSG_CUDA(cudaMemcpyAsync(cq, q + h, sizeof(T) * n, cudaMemcpyHostToDevice, s_in));
+        OSG_CUDA(cudaEventRecord(ev[2 + 2 * k], s_in));
+        OSG_CUDA(cudaStreamWaitEvent(s_push, ev[2 + 2 * k], 0));
         PlainPushArgs<T> a = make_plain_args<T>(dim, order, cix, cx, cu, (const T *)cq, n, rqm,
                                                 (const T *)d_e, (const T *)d_b, emf_size, emf_off,
                                                 (T *)d_j, j_size, j_off, dx, dt, d_ene, d_status);
         a.pusher = pusher;
         a.iter_tol = iter_tol;
         if (pusher >= OSG_PUSHER_VAY) a.tem = (T)pusher_tem(pusher, dt, (double)rqm);
-        if ((rc = launch_plain_push<T>(dim, order, a, cs))) return rc;
+        if ((rc = launch_plain_push<T>(dim, order, a, s_push))) return rc;
         OSG_CUDA(cudaGetLastError());
-        OSG_CUDA(cudaMemcpyAsync(ix + dim * h, cix, sizeof(int) * dim * n, cudaMemcpyDeviceToHost, cs));
-        OSG_CUDA(cudaMemcpyAsync(x + dim * h, cx, sizeof(T) * dim * n, cudaMemcpyDeviceToHost, cs));
-        OSG_CUDA(cudaMemcpyAsync(u + 3 * h, cu, sizeof(T) * 3 * n, cudaMemcpyDeviceToHost, cs));
+        OSG_CUDA(cudaEventRecord(ev[3 + 2 * k], s_push));
+        OSG_CUDA(cudaStreamWaitEvent(s_out, ev[3 + 2 * k], 0));
+        OSG_CUDA(cudaMemcpyAsync(ix + dim * h, cix, sizeof(int) * dim * n, cudaMemcpyDeviceToHost, s_out));
+        OSG_CUDA(cudaMemcpyAsync(x + dim * h, cx, sizeof(T) * dim * n, cudaMemcpyDeviceToHost, s_out));
+        OSG_CUDA(cudaMemcpyAsync(u + 3 * h, cu, sizeof(T) * 3 * n, cudaMemcpyDeviceToHost, s_out));
     }
-    for (int i = 0; i < SIDE_STREAMS; i++) {
-        OSG_CUDA(cudaEventRecord(g_stage.ev[1 + i], all[1 + i]));
-        OSG_CUDA(cudaStreamWaitEvent(st, g_stage.ev[1 + i], 0));
-    }
+    OSG_CUDA(cudaEventRecord(ev[1], s_out));
+    OSG_CUDA(cudaStreamWaitEvent(st, ev[1], 0));
     OSG_CUDA(cudaMemcpyAsync(j, d_j, sizeof(T) * gj, cudaMemcpyDeviceToHost, st));
     double h_ene = 0.0;
     int h_status = 0;
