@@ -259,6 +259,9 @@ typedef struct {
     double iter_tol;  /* exact pusher: Newton tolerance (0 = the reference default 1e-3) */
     int smooth_type;  /* current smoothing after the guard fold, OSG_SMOOTH_* (all axes) */
     int smooth_order; /* its order (binomial: passes; compensated: >= 2; others fixed) */
+    int walls;        /* bit d set: axis d is bounded by perfectly conducting walls (PEC
+                         fields, reflected current, specularly reflected particles; plain
+                         engine); clear: periodic */
 } osg_config;
 
 int osg_sim_create(const osg_config *cfg, osg_sim **out);

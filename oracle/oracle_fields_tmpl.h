@@ -141,11 +141,13 @@ void FN(ora_yee_advance)(int dim, const int *nx, const int *gcl, const int *gcu,
 
 /* update_periodic_vdf for every direction in order; add = 1 folds guard cells (current),
  * add = 0 replaces guard cells by the periodic image (fields). ncomp components per point. */
-void FN(ora_periodic)(int dim, const int *nx, const int *gcl, const int *gcu, R *f, int add)
+void FN(ora_periodic_skip)(int dim, const int *nx, const int *gcl, const int *gcu, R *f,
+                           int add, int skip)
 {
     FN(ora_grid) G, *g = &G;
     FN(grid_init)(g, dim, nx, gcl, gcu);
     for (int d = 0; d < dim; d++) {
+        if (skip & (1 << d)) continue;
         int lo[3], hi[3], ulo[3], uhi[3], sh[3] = {0, 0, 0};
         for (int e = 0; e < 3; e++) {
             if (e == d) {
@@ -188,6 +190,124 @@ void FN(ora_periodic)(int dim, const int *nx, const int *gcl, const int *gcu, R 
                         }
                     }
     }
+}
+
+void FN(ora_periodic)(int dim, const int *nx, const int *gcl, const int *gcu, R *f, int add)
+{
+    FN(ora_periodic_skip)(dim, nx, gcl, gcu, f, add, 0);
+}
+
+/* Perfectly conducting walls bounding the axes in `walls` (bit d), restated from the
+ * reference's tables (pec_bc_e/b_{1,2,3}d_odd/even, source/emf/boundary/os-emf-pec.f90;
+ * spec_bc_{1,2,3}d, source/current/os-current-boundary.f03) as the image rule they follow:
+ * along d a component sits at i - 1/2 (odd order) or i (even) when staggered along d (E_d,
+ * J_d; B_c for c != d), else at i - 1 (odd) or i - 1/2 (even); its image is the point mirrored
+ * about the wall (x_d = 0 below, x_d = nx_d above) with sign + for normal E and tangential
+ * B, J and - for tangential E and normal B, J.  kind 0 (E) and 1 (B) set the guard points
+ * from their images; kind 2 (J) adds the guard values into their images.  A point on the wall
+ * is its own image: set with sign - zeroes it; add doubles it (+) or zeroes it (-).  Axes in
+ * order, the lower wall before the upper, lines over the full extent of the other axes. */
+static int FN(wall_mirror)(int i, int nx, int lower, int stag, int odd)
+{
+    if (lower) return stag ? (odd ? 1 - i : -i) : (odd ? 2 - i : 1 - i);
+    return stag ? (odd ? 2 * nx + 1 - i : 2 * nx - i) : (odd ? 2 * nx + 2 - i : 2 * nx + 1 - i);
+}
+
+void FN(ora_walls)(int dim, const int *nx, const int *gcl, const int *gcu, R *f, int kind,
+                   int walls, int order)
+{
+    FN(ora_grid) G, *g = &G;
+    FN(grid_init)(g, dim, nx, gcl, gcu);
+    const int odd = order & 1;
+    for (int d = 0; d < dim; d++) {
+        if (!(walls & (1 << d))) continue;
+        const int n = g->nx[d];
+        for (int side = 0; side < 2; side++) {
+            const int lower = side == 0;
+            int lo[3], hi[3];
+            for (int a = 0; a < 3; a++) {
+                if (a == d || a >= dim) {
+                    lo[a] = hi[a] = 1;
+                } else {
+                    lo[a] = 1 - g->gcl[a];
+                    hi[a] = g->nx[a] + g->gcu[a];
+                }
+            }
+            const int i0 = lower ? 1 - g->gcl[d] : n + 1, i1 = lower ? 0 : n + g->gcu[d];
+            for (int a3 = lo[2]; a3 <= hi[2]; a3++)
+                for (int a2 = lo[1]; a2 <= hi[1]; a2++)
+                    for (int a1 = lo[0]; a1 <= hi[0]; a1++)
+                        for (int c = 0; c < 3; c++) {
+                            const int normal = c == d;
+                            const int stag = kind == 1 ? !normal : normal;
+                            const R sg = ((kind == 0) == normal) ? K(1.0) : K(-1.0);
+                            int ic[3] = {a1, a2, a3};
+                            for (int i = i0; i <= i1; i++) {
+                                ic[d] = i;
+                                const long pg = FN(gidx)(g, c, ic[0], ic[1], ic[2]);
+                                const int m = FN(wall_mirror)(i, n, lower, stag, odd);
+                                if (m == i) {
+                                    f[pg] = kind == 2 ? (sg > 0 ? K(2.0) * f[pg] : K(0.0))
+                                                      : (sg > 0 ? f[pg] : K(0.0));
+                                    continue;
+                                }
+                                ic[d] = m;
+                                const long pm = FN(gidx)(g, c, ic[0], ic[1], ic[2]);
+                                if (kind == 2)
+                                    f[pm] = f[pm] + sg * f[pg];
+                                else
+                                    f[pg] = sg * f[pm];
+                            }
+                            /* the wall point when it is inside the box */
+                            const int iw = lower ? ((!stag && odd) ? 1 : -1000000)
+                                                 : ((stag && !odd) ? n : -1000000);
+                            if (iw != -1000000) {
+                                ic[d] = iw;
+                                const long pw = FN(gidx)(g, c, ic[0], ic[1], ic[2]);
+                                f[pw] = kind == 2 ? (sg > 0 ? K(2.0) * f[pw] : K(0.0))
+                                                  : (sg > 0 ? f[pw] : K(0.0));
+                            }
+                        }
+        }
+    }
+}
+
+/* the Yee advance bounded by conducting walls: the images after every partial step
+ * (source/emf/solver/os-emf-solver-yee.f03:556-566) */
+void FN(ora_yee_advance_walls)(int dim, const int *nx, const int *gcl, const int *gcu, R *e,
+                               R *b, const R *j, const double *dx, double dt, int walls,
+                               int order)
+{
+    FN(ora_grid) G, *g = &G;
+    FN(grid_init)(g, dim, nx, gcl, gcu);
+    FN(dbdt)(g, b, e, dx, dt / 2.0);
+    FN(ora_walls)(dim, nx, gcl, gcu, b, 1, walls, order);
+    FN(dedt)(g, e, b, j, dx, dt);
+    FN(ora_walls)(dim, nx, gcl, gcu, e, 0, walls, order);
+    FN(dbdt)(g, b, e, dx, dt / 2.0);
+    FN(ora_walls)(dim, nx, gcl, gcu, b, 1, walls, order);
+}
+
+/* particle boundary after the push: periodic wrap, or along a walled axis specular
+ * reflection (p_bc_specular, source/spec/os-spec-boundary.f03:1293-1310: u_d -> -u_d, the
+ * particle to the edge cell at offset -x) */
+void FN(ora_particle_bound)(int dim, const int *nx, int np, int *ix, R *x, R *u, int walls)
+{
+    for (int p = 0; p < np; p++)
+        for (int d = 0; d < dim; d++) {
+            int *c = &ix[dim * p + d];
+            if (walls & (1 << d)) {
+                if (*c < 1 || *c > nx[d]) {
+                    *c = *c < 1 ? 1 : nx[d];
+                    x[dim * p + d] = -x[dim * p + d];
+                    u[3 * p + d] = -u[3 * p + d];
+                }
+            } else if (*c < 1) {
+                *c += nx[d];
+            } else if (*c > nx[d]) {
+                *c -= nx[d];
+            }
+        }
 }
 
 /* 0.5 * dV * sum over the interior of each component squared; out[0..2] = B1..B3 style
@@ -289,6 +409,10 @@ void FN(ora_smooth)(int dim, const int *nx, const int *gcl, const int *gcu, R *f
             }
     }
 }
+
+/* conducting walls of the step below (bit d: axis d walled; 0: periodic box) */
+static int FN(step_walls) = 0;
+void FN(ora_set_walls)(int walls) { FN(step_walls) = walls; }
 
 /* smoothing applied after the current fold by the step below (order 0: none) */
 static int FN(step_smooth_ord)[3] = {0, 0, 0};

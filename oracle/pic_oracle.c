@@ -473,8 +473,9 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
     ora_pusher_##SFXN = (PUSHER);                                                             \
     ora_push_dt_##SFXN = dt;                                                                  \
     ora_iter_tol_##SFXN = (TOL);                                                              \
-    ora_periodic_##SFXN(dim, nx, gcl, gcu, e, 0);                                             \
-    ora_periodic_##SFXN(dim, nx, gcl, gcu, b, 0);                                             \
+    const int walls = step_walls_##SFXN;                                                      \
+    ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, e, 0, walls);                                 \
+    ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, b, 0, walls);                                 \
     memset(j, 0, sizeof(R) * (size_t)gsz);                                                    \
     int nt = nthreads < 1 ? 1 : nthreads;                                                     \
     R *jt = nt > 1 ? (R *)calloc((size_t)gsz * (nt - 1), sizeof(R)) : 0;                     \
@@ -494,7 +495,7 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
         ene[s] = 0.0;                                                                         \
         for (int t = 0; t < nt; t++) ene[s] += et[t];                                         \
         free(et);                                                                             \
-        ora_wrap(dim, nx, np[s], ix[s]);                                                      \
+        ora_particle_bound_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], walls);                  \
     }                                                                                         \
     if (nt > 1) {                                                                             \
         _Pragma("omp parallel for num_threads(nt) schedule(static)")                          \
@@ -503,11 +504,15 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
         free(jt);                                                                             \
     }                                                                                         \
     ora_pusher_##SFXN = 0;                                                                    \
-    ora_periodic_##SFXN(dim, nx, gcl, gcu, j, 1);                                             \
+    ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, j, 1, walls);                                 \
+    if (walls) ora_walls_##SFXN(dim, nx, gcl, gcu, j, 2, walls, order);                       \
     if (step_smooth_ord_##SFXN[0] > 0)                                                       \
         ora_smooth_##SFXN(dim, nx, gcl, gcu, j, step_smooth_ord_##SFXN,                      \
                           step_smooth_coef_##SFXN);                                          \
-    ora_yee_advance_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt);                               \
+    if (walls)                                                                                \
+        ora_yee_advance_walls_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt, walls, order);      \
+    else                                                                                      \
+        ora_yee_advance_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt);                           \
     return 0;
 
 int ora_step_f32(int dim, int order, const int *nx, const int *gcl, const int *gcu,

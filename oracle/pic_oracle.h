@@ -48,6 +48,14 @@ void ora_yee_advance_f64(int dim, const int *nx, const int *gcl, const int *gcu,
                          double *b, const double *j, const double *dx, double dt);
 void ora_periodic_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f, int add);
 void ora_periodic_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f, int add);
+/* conducting walls on the axes in `walls`: kind 0 E / 1 B (guards set from images), 2 J (guards
+ * added into the box); the step functions below use the walls set by ora_set_walls_* */
+void ora_walls_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f, int kind,
+                   int walls, int order);
+void ora_walls_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f, int kind,
+                   int walls, int order);
+void ora_set_walls_f32(int walls);
+void ora_set_walls_f64(int walls);
 void ora_field_energy_f32(int dim, const int *nx, const int *gcl, const int *gcu,
                           const float *f, const double *dx, double *out);
 void ora_field_energy_f64(int dim, const int *nx, const int *gcl, const int *gcu,

@@ -83,6 +83,8 @@ def _declare(L):
     for s_ in ("f32", "f64"):
         getattr(L, f"ora_smooth_{s_}").argtypes = [I, P, P, P, P, P, P]
         getattr(L, f"ora_set_smooth_{s_}").argtypes = [P, P]
+        getattr(L, f"ora_walls_{s_}").argtypes = [I, P, P, P, P, I, I, I]
+        getattr(L, f"ora_set_walls_{s_}").argtypes = [I]
     L.ora_push_pusher_f32.argtypes = [I, I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P,
                                       P, D, D, P]
     L.ora_push_pusher_f64.argtypes = [I, I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, D,
@@ -304,9 +306,18 @@ def load(rng: MT, prec, dim, nx, ppc, dx, rqm, uth, ufl, amp=0.0, kmode=1.0):
 
 # ------------------------------------------------------------------------------ full step
 
+def walls(g: "Grid", prec, f, kind, mask):
+    """Conducting-wall images on the axes in `mask` (bit d), in place: kind 0 E, 1 B (guard
+    points set from their images), 2 J (guard values added into the box)."""
+    nx, gl, gu = g.args()
+    getattr(lib(), f"ora_walls_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), _p(f), int(kind),
+                                        int(mask), g.order)
+
+
 def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="boris",
-         iter_tol=1e-3, smooth=None):
-    """One full periodic time step; species = list of dicts with ix, x, u, q, rqm.
+         iter_tol=1e-3, smooth=None, walls=0):
+    """One full time step; species = list of dicts with ix, x, u, q, rqm.  walls (bit d):
+    axis d bounded by conducting walls instead of periodic.
     Returns the per-species energy sums (Boris: time-centred u^2/(gamma+1); exact pusher:
     gamma - 1 of the new momentum; both times q).  fast=True runs the -O3 -ffast-math build
     (timing only)."""
@@ -326,10 +337,14 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
         getattr(L, f"ora_set_smooth_{prec}")(_p(ordv), _p(coef))
     args = (g.dim, g.order, _p(nx), _p(gl), _p(gu), _p(_f64(g.dx + [0.0] * 3)), float(dt), _p(e),
             _p(b), _p(j), ns, _p(np_), ixs, xs, us, qs, _p(rqm), _p(ene), int(nthreads))
-    if pusher != "boris":
-        getattr(L, f"ora_step_pusher_{prec}")(PUSHERS[pusher], *args, float(iter_tol))
-    else:
-        getattr(L, f"ora_step_{prec}")(*args)
+    getattr(L, f"ora_set_walls_{prec}")(int(walls))
+    try:
+        if pusher != "boris":
+            getattr(L, f"ora_step_pusher_{prec}")(PUSHERS[pusher], *args, float(iter_tol))
+        else:
+            getattr(L, f"ora_step_{prec}")(*args)
+    finally:
+        getattr(L, f"ora_set_walls_{prec}")(0)
     if smooth is not None:
         getattr(L, f"ora_set_smooth_{prec}")(None, None)
     return ene

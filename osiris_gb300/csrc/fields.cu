@@ -13,6 +13,8 @@
 //   divergence      source/vdf/os-vdf-math.f90:1013-1073
 #include <cuda_runtime.h>
 
+#include <climits>
+
 #include "common.cuh"
 #include "fields.cuh"
 #include "pic_math.cuh"
@@ -115,13 +117,103 @@ static void launch_dedt(const GridDesc &g, T *e, const T *b, const T *j, const d
     else k_dedt<T, 1><<<nb, 256, 0, st>>>(g, box, e, b, j, dti, d1, d2, d3);
 }
 
+// ------------------------------------------------------------------------ conducting walls
+// Image rule of a perfectly conducting wall at the lower (x_d = 0) or upper (x_d = nx_d) edge of
+// axis d, for the field E (kind 0) and B (1), whose guard values are set from their mirror
+// points, and for the current J (2), whose guard values are added to their mirror points
+// (pec_bc_e/b_*d_odd/even, source/emf/boundary/os-emf-pec.f90; spec_bc_*d,
+// source/current/os-current-boundary.f03).  Along d a component sits at cell positions i - 1/2
+// (odd interpolation order) or i (even) when it is staggered along d (E_d, J_d, and B_c for
+// c != d), else at i - 1 (odd) or i - 1/2 (even); its mirror point reflects the position
+// about the wall.  The image carries sign + for normal E and tangential B and J, - for
+// tangential E and normal B and J.  A point on the wall is its own image: a set with sign -
+// zeroes it, an add doubles it (+) or zeroes it (-).  One thread per line along d (the full
+// extent of the other axes, guard cells included), so every point of a line is handled in
+// order by one thread.
+template <typename T>
+__device__ __forceinline__ int wall_mirror(int i, int nx, bool lower, bool stag, bool odd)
+{
+    if (lower) return stag ? (odd ? 1 - i : -i) : (odd ? 2 - i : 1 - i);
+    return stag ? (odd ? 2 * nx + 1 - i : 2 * nx - i) : (odd ? 2 * nx + 2 - i : 2 * nx + 1 - i);
+}
+
+template <typename T>
+__global__ void k_wall_dir(GridDesc g, int d, int side, int kind, int odd, T *__restrict__ f,
+                           long nlines)
+{
+    OSG_GRID_LOOP(n, nlines)
+    {
+        int lo[3], ext[3];
+        for (int a = 0; a < 3; a++) {
+            if (a >= g.dim || a == d) {
+                lo[a] = a == d ? 0 : 1;
+                ext[a] = 1;
+            } else {
+                lo[a] = 1 - g.gcl[a];
+                ext[a] = g.size[a];
+            }
+        }
+        int ic[3];
+        unflat(n, lo, ext, ic[0], ic[1], ic[2]);
+        const bool lower = side == 0;
+        const int nx = g.nx[d];
+        const int i0 = lower ? 1 - g.gcl[d] : nx + 1, i1 = lower ? 0 : nx + g.gcu[d];
+        for (int c = 0; c < 3; c++) {
+            const bool normal = c == d;
+            const bool stag = kind == 1 ? !normal : normal;
+            const T sg = (kind == 0) == normal ? T(1) : T(-1);
+            // the wall point, when it is not a guard point (odd order, unstaggered, lower
+            // wall: i = 1; even order, staggered, upper wall: i = nx)
+            const int iw = lower ? (!stag && odd ? 1 : INT_MIN) : (stag && !odd ? nx : INT_MIN);
+            for (int i = i0; i <= i1; i++) {
+                ic[d] = i;
+                const long pg = pos(g, ic[0], ic[1], ic[2]) + c;
+                const int m = wall_mirror<T>(i, nx, lower, stag, odd != 0);
+                if (m == i) {
+                    f[pg] = kind == 2 ? (sg > T(0) ? T(2) * f[pg] : T(0))
+                                      : (sg > T(0) ? f[pg] : T(0));
+                    continue;
+                }
+                ic[d] = m;
+                const long pm = pos(g, ic[0], ic[1], ic[2]) + c;
+                if (kind == 2)
+                    f[pm] += sg * f[pg];
+                else
+                    f[pg] = sg * f[pm];
+            }
+            if (iw != INT_MIN) {
+                ic[d] = iw;
+                const long pw = pos(g, ic[0], ic[1], ic[2]) + c;
+                f[pw] = kind == 2 ? (sg > T(0) ? T(2) * f[pw] : T(0)) : (sg > T(0) ? f[pw] : T(0));
+            }
+        }
+    }
+}
+
+template <typename T>
+void wall_update(const GridDesc &g, T *f, int kind, int walls, int order, cudaStream_t st)
+{
+    for (int d = 0; d < g.dim; d++) {
+        if (!(walls & (1 << d))) continue;
+        long nlines = 1;
+        for (int a = 0; a < g.dim; a++)
+            if (a != d) nlines *= g.size[a];
+        for (int side = 0; side < 2; side++)
+            k_wall_dir<T><<<blocks_for(nlines, 256), 256, 0, st>>>(g, d, side, kind, order & 1, f,
+                                                                   nlines);
+    }
+}
+
 template <typename T>
 void yee_advance(const GridDesc &g, T *e, T *b, const T *j, const double *dx, double dt,
-                 cudaStream_t st)
+                 cudaStream_t st, int walls, int order)
 {
     launch_dbdt(g, b, e, dx, dt / 2.0, st);
+    if (walls) wall_update(g, b, 1, walls, order, st);
     launch_dedt(g, e, b, j, dx, dt, st);
+    if (walls) wall_update(g, e, 0, walls, order, st);
     launch_dbdt(g, b, e, dx, dt / 2.0, st);
+    if (walls) wall_update(g, b, 1, walls, order, st);
 }
 
 // One direction of the periodic update.  Thread n handles one guard point (lower or upper
@@ -202,9 +294,11 @@ __global__ void k_open_dir(GridDesc g, int d, T *__restrict__ f, long n_lo, long
 }
 
 template <typename T>
-void periodic_update(const GridDesc &g, T *f, int add, cudaStream_t st, int open_mask)
+void periodic_update(const GridDesc &g, T *f, int add, cudaStream_t st, int open_mask,
+                     int skip_mask)
 {
     for (int d = 0; d < g.dim; d++) {
+        if (skip_mask & (1 << d)) continue;
         long other = 1;
         for (int a = 0; a < g.dim; a++)
             if (a != d) other *= g.size[a];
@@ -579,11 +673,13 @@ void smooth_field(const GridDesc &g, const SmoothSpec &sp, T *f, T *tmp, cudaStr
 }
 
 template void yee_advance<float>(const GridDesc &, float *, float *, const float *,
-                                 const double *, double, cudaStream_t);
+                                 const double *, double, cudaStream_t, int, int);
 template void yee_advance<double>(const GridDesc &, double *, double *, const double *,
-                                  const double *, double, cudaStream_t);
-template void periodic_update<float>(const GridDesc &, float *, int, cudaStream_t, int);
-template void periodic_update<double>(const GridDesc &, double *, int, cudaStream_t, int);
+                                  const double *, double, cudaStream_t, int, int);
+template void periodic_update<float>(const GridDesc &, float *, int, cudaStream_t, int, int);
+template void periodic_update<double>(const GridDesc &, double *, int, cudaStream_t, int, int);
+template void wall_update<float>(const GridDesc &, float *, int, int, int, cudaStream_t);
+template void wall_update<double>(const GridDesc &, double *, int, int, int, cudaStream_t);
 template void smooth_field<float>(const GridDesc &, const SmoothSpec &, float *, float *,
                                   cudaStream_t);
 template void smooth_field<double>(const GridDesc &, const SmoothSpec &, double *, double *,

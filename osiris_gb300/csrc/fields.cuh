@@ -46,9 +46,16 @@ __host__ __device__ inline Box make_box(const GridDesc &g, int lo, int hi_off)
     return b;
 }
 
+// B half step, E full step, B half step; the axes in `walls` (bit d) are bounded by perfectly
+// conducting walls, whose images are taken after every partial step as the reference's
+// update_boundary_b / update_boundary_e (source/emf/solver/os-emf-solver-yee.f03:556-566)
 template <typename T>
 void yee_advance(const GridDesc &g, T *e, T *b, const T *j, const double *dx, double dt,
-                 cudaStream_t st);
+                 cudaStream_t st, int walls = 0, int order = 2);
+// conducting-wall images along the axes in `walls`: kind 0 E, 1 B (guards set), 2 J (guards
+// added into the box)
+template <typename T>
+void wall_update(const GridDesc &g, T *f, int kind, int walls, int order, cudaStream_t st);
 
 // One box of a batch of independent periodic boxes (single precision): its fields and the
 // Yee coefficients.  The batched launches take a device array of these, one box per
@@ -69,9 +76,11 @@ void batch_periodic(const FieldBox *d_boxes, int nbox, int dim, int which, int a
 void batch_yee(const FieldBox *d_boxes, int nbox, int dim, long max_points, cudaStream_t st);
 
 // add = 1: fold guard cells into their periodic images (current); add = 0: replace.  Axes set
-// in open_mask (bit d) are open instead: their guard slabs are zeroed.
+// in open_mask (bit d) are open instead: their guard slabs are zeroed; axes in skip_mask
+// (conducting walls) are left alone.
 template <typename T>
-void periodic_update(const GridDesc &g, T *f, int add, cudaStream_t st, int open_mask = 0);
+void periodic_update(const GridDesc &g, T *f, int add, cudaStream_t st, int open_mask = 0,
+                     int skip_mask = 0);
 
 // Current smoothing (smooth_vdf, source/vdf/os-vdf-smooth.f90:514-540): a separable filter of
 // 2 * order[d] + 1 points per axis with FP64 coefficients c[d][0 .. 2 order[d]].

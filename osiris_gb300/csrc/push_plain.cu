@@ -154,6 +154,25 @@ __device__ __forceinline__ int wrap_cell(int c, int n)
     return c;
 }
 
+// New cell and offset of a particle along axis d: periodic wrap, or specular reflection at a
+// conducting wall (p_bc_specular, source/spec/os-spec-boundary.f03:1293-1310: the momentum
+// along d flips, the particle goes to the edge cell at the mirrored offset), after its current
+// was deposited along the unreflected path.
+template <typename T, int DIM>
+__device__ __forceinline__ void store_position(const PlainPushArgs<T> &a, long p, int d, int cn,
+                                               T xn)
+{
+    if (a.reflect[d] > 0 && (cn < 1 || cn > a.reflect[d])) {
+        cn = cn < 1 ? 1 : a.reflect[d];
+        xn = -xn;
+        a.u[3 * p + d] = -a.u[3 * p + d];
+    } else {
+        cn = wrap_cell(cn, a.wrap[d]);
+    }
+    a.x[DIM * p + d] = xn;
+    a.ix[DIM * p + d] = cn;
+}
+
 // FP32 2D orders whose per-warp value scratch (8 warps) fits 32 KB of static shared memory
 // deposit their in-cell segments by warp runs (cell_runs_deposit_global2): 2x faster on the
 // two-stream workload.  The others add every value with its own atomic (FP64: native double
@@ -314,8 +333,7 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
             if constexpr (DIM == 1) {
                 T x1 = fmaR(v1, a.dtdx[0], x0[0]);
                 int dix = trim(x1);
-                a.x[p] = x1 - T(dix);
-                a.ix[p] = wrap_cell(c[0] + dix, a.wrap[0]);
+                store_position<T, 1>(a, p, 0, c[0] + dix, x1 - T(dix));
                 if (dix == 0) {
                     deposit1<T, ORD>(a.j, a.jn[0], q, x0[0], x1, v2, v3, c[0]);
                 } else {
@@ -329,10 +347,8 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
                 T x1 = fmaR(v1, a.dtdx[0], x0[0]);
                 T y1 = fmaR(v2, a.dtdx[1], x0[1]);
                 int dix = trim(x1), diy = trim(y1);
-                a.x[2 * p] = x1 - T(dix);
-                a.x[2 * p + 1] = y1 - T(diy);
-                a.ix[2 * p] = wrap_cell(c[0] + dix, a.wrap[0]);
-                a.ix[2 * p + 1] = wrap_cell(c[1] + diy, a.wrap[1]);
+                store_position<T, 2>(a, p, 0, c[0] + dix, x1 - T(dix));
+                store_position<T, 2>(a, p, 1, c[1] + diy, y1 - T(diy));
                 Seg2<T> s[3];
                 s[0].x0 = x0[0]; s[0].x1 = x1; s[0].y0 = x0[1]; s[0].y1 = y1;
                 s[0].vz = v3; s[0].i = c[0]; s[0].j = c[1];
@@ -351,12 +367,9 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
                 T y1 = fmaR(v2, a.dtdx[1], x0[1]);
                 T z1 = fmaR(v3, a.dtdx[2], x0[2]);
                 int dix = trim(x1), diy = trim(y1), diz = trim(z1);
-                a.x[3 * p] = x1 - T(dix);
-                a.x[3 * p + 1] = y1 - T(diy);
-                a.x[3 * p + 2] = z1 - T(diz);
-                a.ix[3 * p] = wrap_cell(c[0] + dix, a.wrap[0]);
-                a.ix[3 * p + 1] = wrap_cell(c[1] + diy, a.wrap[1]);
-                a.ix[3 * p + 2] = wrap_cell(c[2] + diz, a.wrap[2]);
+                store_position<T, 3>(a, p, 0, c[0] + dix, x1 - T(dix));
+                store_position<T, 3>(a, p, 1, c[1] + diy, y1 - T(diy));
+                store_position<T, 3>(a, p, 2, c[2] + diz, z1 - T(diz));
                 Seg3<T> s[4];
                 s[0].x0 = x0[0]; s[0].x1 = x1; s[0].y0 = x0[1]; s[0].y1 = y1;
                 s[0].z0 = x0[2]; s[0].z1 = z1; s[0].i = c[0]; s[0].j = c[1]; s[0].k = c[2];
@@ -409,6 +422,7 @@ PlainPushArgs<T> make_plain_args(int dim, int order, int *ix, T *x, T *u, const 
         a.jn[d] = d < dim ? (T)(dx[d] / dt / div) : T(0);
     }
     a.wrap[0] = a.wrap[1] = a.wrap[2] = 0;
+    a.reflect[0] = a.reflect[1] = a.reflect[2] = 0;
     a.pusher = OSG_PUSHER_BORIS;
     a.qm = T(1) / rqm;
     a.rqm = rqm;

@@ -26,6 +26,8 @@ template <typename T> struct PlainPushArgs {
     long emf_Dy, emf_Dz, j_Dy, j_Dz;
     int emf_off[3], emf_size[3], j_off[3], j_size[3];
     int wrap[3];           // > 0: periodic wrap of the stored cell index into [1, wrap[d]]
+    int reflect[3];        // > 0: conducting walls at the edges of [1, reflect[d]]: specular
+                           // reflection of a particle that crossed one
     int pusher;            // OSG_PUSHER_*
     T qm;                  // 1 / rqm (exact pusher)
     T rqm;                 // the species' rqm (Euler-rotation pusher)

@@ -252,9 +252,11 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
     const bool fortran_push = c.pusher != OSG_PUSHER_BORIS;
     const double push_dt = (sizeof(T) == 4 && !fortran_push) ? (double)(float)c.dt : c.dt;
     const int open = s->window ? 1 : 0;   // x1 open while the window moves
+    // conducting walls: their guard cells hold the images set by the last field advance
+    const int walls = c.walls;
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[0], st));
-    periodic_update<T>(s->g, (T *)s->e, 0, st, open);
-    periodic_update<T>(s->g, (T *)s->b, 0, st, open);
+    periodic_update<T>(s->g, (T *)s->e, 0, st, open, walls);
+    periodic_update<T>(s->g, (T *)s->b, 0, st, open, walls);
     launches += 2 * c.dim;
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[1], st));
     OSG_CUDA(cudaMemsetAsync(s->j, 0, (size_t)s->esz * 3 * s->g.npoints(), st));
@@ -271,7 +273,10 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
                 c.dim, c.order, p.ix, (T *)p.x, (T *)p.u, (const T *)p.q, s->np[k],
                 (T)s->rqm[k], (const T *)s->e, (const T *)s->b, emf_size, emf_off, (T *)s->j,
                 emf_size, emf_off, c.dx, push_dt, s->d_ene + k, s->d_status);
-            for (int d = 0; d < c.dim; d++) a.wrap[d] = c.nx[d];
+            for (int d = 0; d < c.dim; d++) {
+                a.wrap[d] = (walls >> d) & 1 ? 0 : c.nx[d];
+                a.reflect[d] = (walls >> d) & 1 ? c.nx[d] : 0;
+            }
             a.pusher = c.pusher;
             a.iter_tol = c.iter_tol;
             if (c.pusher >= OSG_PUSHER_VAY)
@@ -290,16 +295,22 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
         }
     }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[3], st));
-    periodic_update<T>(s->g, (T *)s->j, 1, st, open);
+    periodic_update<T>(s->g, (T *)s->j, 1, st, open, walls);
     launches += c.dim;
+    if (walls) {
+        // current deposited beyond a wall comes back as its image (update_boundary_current,
+        // source/current/os-current-define.f03:683-725)
+        wall_update<T>(s->g, (T *)s->j, 2, walls, c.order, st);
+        launches += 2 * __builtin_popcount(walls);
+    }
     if (s->smooth.order[0] > 0) {
         // smooth currents after the boundary update (source/os-simulation.f03:651-657)
         smooth_field<T>(s->g, s->smooth, (T *)s->j, (T *)s->shift_tmp, st);
         launches += c.dim;
     }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[4], st));
-    yee_advance<T>(s->g, (T *)s->e, (T *)s->b, (const T *)s->j, c.dx, c.dt, st);
-    launches += 3;
+    yee_advance<T>(s->g, (T *)s->e, (T *)s->b, (const T *)s->j, c.dx, c.dt, st, walls, c.order);
+    launches += 3 + (walls ? 6 * __builtin_popcount(walls) : 0);
     if (shift) {
         shift_window_x<T>(s->g, (T *)s->e, (T *)s->shift_tmp, st);
         shift_window_x<T>(s->g, (T *)s->b, (T *)s->shift_tmp, st);
@@ -427,6 +438,12 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               "unknown engine");
     OSG_CHECK(!(cfg->engine == OSG_ENGINE_TILED && cfg->precision != 32), OSG_ERR_ARG,
               "the tiled engine is single precision");
+    OSG_CHECK(cfg->walls >= 0 && cfg->walls < (1 << cfg->dim), OSG_ERR_ARG,
+              "walls: a bit mask of the axes");
+    OSG_CHECK(cfg->walls == 0 || cfg->engine == OSG_ENGINE_PLAIN, OSG_ERR_ARG,
+              "conducting walls run on the plain engine");
+    OSG_CHECK(cfg->walls == 0 || cfg->smooth_type == OSG_SMOOTH_NONE, OSG_ERR_ARG,
+              "current smoothing next to conducting walls is not supported");
     OSG_CHECK(cfg->pusher >= OSG_PUSHER_BORIS && cfg->pusher <= OSG_PUSHER_EULER, OSG_ERR_ARG,
               "unknown pusher");
     OSG_CHECK(cfg->iter_tol >= 0, OSG_ERR_ARG, "iter_tol must be >= 0");
@@ -916,6 +933,8 @@ int osg_sim_energy(osg_sim *s, double *kinetic, double *field)
 int osg_sim_gauss_residual(osg_sim *s, double *max_abs, double *l2)
 {
     OSG_CHECK(s, OSG_ERR_ARG, "null sim");
+    OSG_CHECK(s->cfg.walls == 0, OSG_ERR_STATE,
+              "the Gauss residual is taken on periodic boxes (no conducting walls)");
     const size_t n = 3 * (size_t)s->g.npoints();
     int rc = OSG_OK;
     if (!s->d_rho) s->d_rho = dalloc<double>(n, &rc);

@@ -1,0 +1,64 @@
+"""GPU parity of conducting walls (osg_config.walls, plain engine) against the oracle's walled
+step: PEC field images after every partial field step, the current beyond a wall added back as
+its image, specular particle reflection.  FP64 1e-12 and FP32 1e-5 (after 1 and 10 steps), for
+walls along x1, x2 and both, odd and even interpolation orders.  Particles move fast enough
+(momenta of rms 0.6) that many reflect."""
+import numpy as np
+import pytest
+
+from test_gpu_step import _nerr, _setup
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def osg():
+    import __graft_entry__ as g
+    g.build_native()
+    import osiris_gb300
+    if osiris_gb300.lib().osg_device_count() < 1:
+        pytest.fail("no CUDA device visible")
+    return osiris_gb300
+
+
+def _run(osg, oracle, prec, order, mask, steps):
+    dim, nx = 2, [20, 16]
+    p, g, dx, dt, species, e, b = _setup(oracle, prec, dim, order, nx, [2, 2], 11, uth=0.6,
+                                         ufl=0.1)
+    sim = osg.Simulation(nx, dx, dt, order=order, precision=prec, engine=osg.ENGINE_PLAIN,
+                         walls=mask)
+    sim.set_fields(e, b)
+    for s in species:
+        sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
+    sim.step(steps)
+    eg, bg, jg = sim.fields()
+    ora = [{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s.items()}
+           for s in species]
+    eo, bo, jo = e.copy(), b.copy(), g.zeros(p)
+    for _ in range(steps):
+        oracle.step(g, p, eo, bo, jo, ora, dt, walls=mask)
+    errs = {"E": _nerr(g.interior(eg), g.interior(eo)), "B": _nerr(g.interior(bg), g.interior(bo)),
+            "J": _nerr(g.interior(jg), g.interior(jo))}
+    for k, s in enumerate(ora):
+        ix, x, u, q = sim.species(k)          # the plain engine keeps the particle order
+        errs[f"x{k}"] = _nerr(ix + x, s["ix"] + s["x"])
+        errs[f"u{k}"] = _nerr(u, s["u"])
+        assert ix.min() >= 1 and np.all(ix.max(axis=0) <= np.array(nx))
+    sim.close()
+    return errs
+
+
+@pytest.mark.parametrize("mask", [1, 2, 3])
+@pytest.mark.parametrize("order", [1, 2, 3])
+@pytest.mark.parametrize("prec,steps,tol", [(64, 1, 1e-12), (64, 10, 1e-12), (32, 1, 1e-5),
+                                            (32, 10, 5e-5)])
+def test_walls_match_oracle(osg, oracle, prec, steps, tol, order, mask):
+    errs = _run(osg, oracle, prec, order, mask, steps)
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, (bad, errs)
+
+
+def test_walls_need_the_plain_engine(osg):
+    with pytest.raises(osg.OsirisGB300Error):
+        osg.Simulation([16, 16], [0.1, 0.1], 0.05, order=2, precision=32,
+                       engine=osg.ENGINE_TILED, walls=1)
