@@ -180,6 +180,17 @@ int osg_yee_advance_f64(int dim, const int *nx, const int *gcl, const int *gcu, 
  * their periodic image and writes the sum to both (current); add = 0 copies the periodic
  * image into the guard cells (fields). */
 int osg_periodic_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f, int add);
+/* Perfectly conducting walls bounding the axes in `walls` (bit d), on a HOST array: kind 0 E and
+ * 1 B take their guard values from the image points (pec_bc_e/b_*d_odd/even,
+ * source/emf/boundary/os-emf-pec.f90, odd or even by the interpolation order), kind 2 J adds
+ * its guard values into the image points inside the box (spec_bc_*d,
+ * source/current/os-current-boundary.f03).  The image of a component is the point mirrored
+ * about the wall, with sign + for normal E and tangential B, J and - for tangential E and
+ * normal B, J. */
+int osg_walls_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f, int kind,
+                  int walls, int order);
+int osg_walls_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f, int kind,
+                  int walls, int order);
 int osg_periodic_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f,
                      int add);
 

@@ -97,6 +97,7 @@ def _declare(lb):
     for s in ("f32", "f64"):
         getattr(lb, f"osg_yee_advance_{s}").argtypes = [I, P, P, P, P, P, P, P, D]
         getattr(lb, f"osg_periodic_{s}").argtypes = [I, P, P, P, P, I]
+        getattr(lb, f"osg_walls_{s}").argtypes = [I, P, P, P, P, I, I, I]
     lb.osg_particle_wrap.argtypes = [I, P, L, P]
     lb.osg_rng_seed.argtypes = [P, I]
     lb.osg_load_lattice.argtypes = [P, I, I, P, P, P, D, P, P, D, D, P, P, P, P]
@@ -256,6 +257,14 @@ def yee_advance(dim, nx, gcl, gcu, e, b, j, dx, dt):
     _check(getattr(lib(), f"osg_yee_advance_{prec}")(
         dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)), _p(e), _p(b), _p(j),
         _p(_f64(list(dx) + [0.0] * 3)), float(dt)))
+
+
+def walls(dim, nx, gcl, gcu, f, kind, mask, order):
+    """Conducting-wall images on a host grid (osg_walls_*): kind 0 E, 1 B, 2 J; mask bit d
+    walls axis d."""
+    s = _prec(f)
+    _check(getattr(lib(), f"osg_walls_{s}")(dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)),
+                                            _p(f), int(kind), int(mask), int(order)))
 
 
 def periodic(dim, nx, gcl, gcu, f, add):

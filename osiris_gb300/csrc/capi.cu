@@ -271,6 +271,31 @@ static int smooth_host(int dim, const int *nx, const int *gcl, const int *gcu, T
 }
 
 template <typename T>
+static int walls_host(int dim, const int *nx, const int *gcl, const int *gcu, T *f, int kind,
+                      int walls, int order)
+{
+    OSG_CHECK(dim >= 1 && dim <= 3 && nx && gcl && gcu && f && kind >= 0 && kind <= 2 &&
+                  walls >= 0 && walls < (1 << dim) && order >= 1 && order <= 4,
+              OSG_ERR_ARG, "bad arguments");
+    for (int d = 0; d < dim; d++)
+        OSG_CHECK(gcl[d] >= 0 && gcu[d] >= 0 &&
+                      (!((walls >> d) & 1) || (gcu[d] >= 1 && nx[d] >= gcl[d] + gcu[d] + 2)),
+                  OSG_ERR_ARG, "a walled axis needs nx >= gcl + gcu + 2 and gcu >= 1");
+    GridDesc g = make_grid(dim, nx, gcl, gcu);
+    const long n = g.npoints() * 3;
+    void *d_f;
+    int rc;
+    if ((rc = g_stage.get(6, sizeof(T) * n, &d_f))) return rc;
+    cudaStream_t st = g_stage.stream;
+    OSG_CUDA(cudaMemcpyAsync(d_f, f, sizeof(T) * n, cudaMemcpyHostToDevice, st));
+    wall_update<T>(g, (T *)d_f, kind, walls, order, st);
+    OSG_CUDA(cudaGetLastError());
+    OSG_CUDA(cudaMemcpyAsync(f, d_f, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+    OSG_CUDA(cudaStreamSynchronize(st));
+    return OSG_OK;
+}
+
+template <typename T>
 static int periodic_host(int dim, const int *nx, const int *gcl, const int *gcu, T *f, int add)
 {
     OSG_CHECK(dim >= 1 && dim <= 3 && nx && gcl && gcu && f, OSG_ERR_ARG, "bad arguments");
@@ -570,6 +595,18 @@ int osg_smooth_coefficients(int type, int order, double *c, int *n)
     OSG_CHECK(smooth_coefficients(type, order, c, n) == OSG_OK, OSG_ERR_ARG,
               "bad smoothing type %d / order %d", type, order);
     return OSG_OK;
+}
+
+int osg_walls_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f, int kind,
+                  int walls, int order)
+{
+    return walls_host<float>(dim, nx, gcl, gcu, f, kind, walls, order);
+}
+
+int osg_walls_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f, int kind,
+                  int walls, int order)
+{
+    return walls_host<double>(dim, nx, gcl, gcu, f, kind, walls, order);
 }
 
 int osg_periodic_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f, int add)

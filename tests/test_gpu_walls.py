@@ -62,3 +62,15 @@ def test_walls_need_the_plain_engine(osg):
     with pytest.raises(osg.OsirisGB300Error):
         osg.Simulation([16, 16], [0.1, 0.1], 0.05, order=2, precision=32,
                        engine=osg.ENGINE_TILED, walls=1)
+
+
+@pytest.mark.parametrize("prec,order,kind,mask", [("f64", 1, 0, 1), ("f64", 2, 2, 3),
+                                                  ("f32", 3, 1, 2), ("f32", 4, 2, 1)])
+def test_host_array_walls_match_oracle(osg, oracle, prec, order, kind, mask):
+    g = oracle.Grid([12, 10], order, [0.1, 0.1])
+    dt_ = np.float32 if prec == "f32" else np.float64
+    f0 = np.random.default_rng(order + kind).standard_normal(g.shape).astype(dt_)
+    a, o = f0.copy(), f0.copy()
+    osg.walls(2, g.nx, g.gcl, g.gcu, a, kind, mask, order)
+    oracle.walls(g, prec, o, kind, mask)
+    assert np.array_equal(a, o)
