@@ -271,8 +271,8 @@ typedef struct {
     int smooth_type;  /* current smoothing after the guard fold, OSG_SMOOTH_* (all axes) */
     int smooth_order; /* its order (binomial: passes; compensated: >= 2; others fixed) */
     int walls;        /* bit d set: axis d is bounded by perfectly conducting walls (PEC
-                         fields, reflected current, specularly reflected particles; plain
-                         engine); clear: periodic */
+                         fields, reflected current, specularly reflected particles); clear:
+                         periodic */
 } osg_config;
 
 int osg_sim_create(const osg_config *cfg, osg_sim **out);

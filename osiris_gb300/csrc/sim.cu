@@ -440,8 +440,6 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               "the tiled engine is single precision");
     OSG_CHECK(cfg->walls >= 0 && cfg->walls < (1 << cfg->dim), OSG_ERR_ARG,
               "walls: a bit mask of the axes");
-    OSG_CHECK(cfg->walls == 0 || cfg->engine == OSG_ENGINE_PLAIN, OSG_ERR_ARG,
-              "conducting walls run on the plain engine");
     OSG_CHECK(cfg->walls == 0 || cfg->smooth_type == OSG_SMOOTH_NONE, OSG_ERR_ARG,
               "current smoothing next to conducting walls is not supported");
     OSG_CHECK(cfg->pusher >= OSG_PUSHER_BORIS && cfg->pusher <= OSG_PUSHER_EULER, OSG_ERR_ARG,

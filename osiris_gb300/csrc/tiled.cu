@@ -67,6 +67,7 @@ struct TiledState {
     // drop dead slab lines from L2 after the sort; OSG_L2_DISCARD=0 turns it off (profiler
     // kernel replay saves and restores device memory and needs the dropped lines defined)
     int l2_discard = 1;
+    int walls = 0;   // bit d: conducting walls on axis d
     int pusher = OSG_PUSHER_BORIS;
     double iter_tol = 1.0e-3;
     long nj_tile = 0;    // current points (x3 components) of a tile with its halo
@@ -174,6 +175,7 @@ static TiledArgs base_args(const TiledState *t)
     a.tile_hi = t->tile_hi;
     a.tile_lo = t->tile_lo;
     a.discard = t->l2_discard;
+    a.walls = t->walls;
     return a;
 }
 
@@ -208,6 +210,7 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
     t->g = g;
     t->dt = cfg.dt;
     t->capacity = cfg.capacity > 0 ? cfg.capacity : 3.0;
+    t->walls = cfg.walls;
     t->ntiles = 1;
     for (int d = 0; d < 3; d++) {
         t->nx[d] = d < cfg.dim ? cfg.nx[d] : 1;

@@ -116,6 +116,8 @@ struct TiledArgs {
     // the box along x1 are dropped
     int open_x;
     int shift_x;
+    // bit d: axis d is bounded by conducting walls (particles reflect specularly)
+    int walls;
     // 1: drop the dead input-slab lines from L2 after the sort (discard_dead_slab).  0 for
     // multi-pass profiler replay, which saves and restores memory and needs it defined
     int discard;
@@ -399,8 +401,19 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
 #pragma unroll
                 for (int d = 0; d < DIM; d++) {
                     xo[d] = x1[d] - float(di[d]);
-                    cw[d] = (d == 0 && a.open_x) ? c[d] + di[d] - a.shift_x
-                                                 : wrapc(c[d] + di[d], a.nx[d]);
+                    const int cn = c[d] + di[d];
+                    if ((a.walls >> d) & 1) {
+                        // conducting wall: specular reflection after the deposit of the
+                        // unreflected path (p_bc_specular, source/spec/os-spec-boundary.f03:
+                        // 1293-1310)
+                        cw[d] = cn < 1 ? 1 : (cn > a.nx[d] ? a.nx[d] : cn);
+                        if (cw[d] != cn) {
+                            xo[d] = -xo[d];
+                            un[d] = -un[d];
+                        }
+                    } else {
+                        cw[d] = (d == 0 && a.open_x) ? cn - a.shift_x : wrapc(cn, a.nx[d]);
+                    }
                 }
                 // (open x1: a particle outside [1, nx] has left the window; its current of
                 //  this step is already in the segments)

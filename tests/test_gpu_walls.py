@@ -1,5 +1,5 @@
-"""GPU parity of conducting walls (osg_config.walls, plain engine) against the oracle's walled
-step: PEC field images after every partial field step, the current beyond a wall added back as
+"""GPU parity of conducting walls (osg_config.walls, plain and tiled engines) against the
+oracle's walled step: PEC field images after every partial field step, the current beyond a wall added back as
 its image, specular particle reflection.  FP64 1e-12 and FP32 1e-5 (after 1 and 10 steps), for
 walls along x1, x2 and both, odd and even interpolation orders.  Particles move fast enough
 (momenta of rms 0.6) that many reflect."""
@@ -58,10 +58,39 @@ def test_walls_match_oracle(osg, oracle, prec, steps, tol, order, mask):
     assert not bad, (bad, errs)
 
 
-def test_walls_need_the_plain_engine(osg):
-    with pytest.raises(osg.OsirisGB300Error):
-        osg.Simulation([16, 16], [0.1, 0.1], 0.05, order=2, precision=32,
-                       engine=osg.ENGINE_TILED, walls=1)
+@pytest.mark.parametrize("mask", [1, 2, 3])
+@pytest.mark.parametrize("order", [2, 3])
+@pytest.mark.parametrize("steps,tol", [(1, 1e-5), (10, 5e-5)])
+def test_tiled_walls_match_oracle(osg, oracle, steps, tol, order, mask):
+    """The mixed-precision tiled engine between conducting walls (particles reflect in the tile
+    push; the fields and current take the same images as the plain engine)."""
+    dim, nx = 2, [32, 24]
+    p, g, dx, dt, species, e, b = _setup(oracle, 32, dim, order, nx, [2, 2], 12, uth=0.6,
+                                         ufl=0.1)
+    sim = osg.Simulation(nx, dx, dt, order=order, precision=32, engine=osg.ENGINE_TILED,
+                         tile=[8, 8], walls=mask)
+    sim.set_fields(e, b)
+    for s in species:
+        sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
+    sim.step(steps)
+    eg, bg, jg = sim.fields()
+    ora = [{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s.items()}
+           for s in species]
+    eo, bo, jo = e.copy(), b.copy(), g.zeros(p)
+    for _ in range(steps):
+        oracle.step(g, p, eo, bo, jo, ora, dt, walls=mask)
+    errs = {"E": _nerr(g.interior(eg), g.interior(eo)), "B": _nerr(g.interior(bg), g.interior(bo)),
+            "J": _nerr(g.interior(jg), g.interior(jo))}
+    for k, s in enumerate(ora):
+        ix, x, u, q = sim.species(k)
+        assert len(q) == len(s["q"])
+        a, o = np.argsort(q, kind="stable"), np.argsort(s["q"], kind="stable")
+        errs[f"x{k}"] = _nerr(ix[a] + x[a], s["ix"][o] + s["x"][o])
+        errs[f"u{k}"] = _nerr(u[a], s["u"][o])
+        assert ix.min() >= 1 and np.all(ix.max(axis=0) <= np.array(nx))
+    sim.close()
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, (bad, errs)
 
 
 @pytest.mark.parametrize("prec,order,kind,mask", [("f64", 1, 0, 1), ("f64", 2, 2, 3),
