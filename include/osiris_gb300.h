@@ -273,6 +273,10 @@ typedef struct {
     int walls;        /* bit d set: axis d is bounded by perfectly conducting walls (PEC
                          fields, reflected current, specularly reflected particles); clear:
                          periodic */
+    int open_fields;  /* bit d set (one axis at most): both edges of axis d are Lindman open
+                         boundaries (first-order Mur update of the tangential E, the
+                         reference's p_bc_lindman) and particles leaving through them are
+                         absorbed; not with walls, smoothing or the moving window */
 } osg_config;
 
 int osg_sim_create(const osg_config *cfg, osg_sim **out);

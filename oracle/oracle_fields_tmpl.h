@@ -288,6 +288,181 @@ void FN(ora_yee_advance_walls)(int dim, const int *nx, const int *gcl, const int
     FN(ora_walls)(dim, nx, gcl, gcu, b, 1, walls, order);
 }
 
+/* Lindman open boundaries at both edges of axis d (p_bc_lindman; the reference admits them
+ * along one axis only, source/emf/boundary/os-emf-boundary.f90:316-324), restated from
+ * source/emf/boundary/os-emf-lindman.f90.  The state holds, per interior point of the other
+ * axes (flat index m, the lower other axis fastest) and for 3 components, five buffer
+ * columns along d: slot 0 E at i_d = 0, 1 E at i_d = 1, 2 B at i_d = 0 (the lower wall
+ * buffers, range [0, 1], new_lindman :295-300) and 3 E at nx+1, 4 E at nx+2 (the upper one,
+ * range [nx, nx+2]); every slot starts at zero (new_wall, source/vdf/os-wall.f90:198-210).
+ *   E (after the E step, update_lindman_2d_e :454-535, 3d :604-750): for the two components
+ *     other than d, E(0) = S1 + k (S0 - E(1)), then S0 = E(0), S1 = E(1); above,
+ *     E(nx+2) = S3 + k (S4 - E(nx+1)), then S3 = E(nx+1), S4 = E(nx+2);
+ *     k = (1 - dt/dx_d) / (1 + dt/dx_d) (disp_corr, new_lindman :237-238).
+ *   B (after each B half step, update_lindman_2d_b :539-600, 3d :755-857): the lower B
+ *     buffer takes the Yee increment of the point i_d = 0 from the grid's E with
+ *     dt/dx * 0.5 (dtdxi, :236-241); nothing above.
+ *   guard update (update_emfbound_lindman :861-1042, after the buffers' own periodic update
+ *     along the other axes, update_boundary_lindman :352-368): E(0) and B(0), and E(nx+1),
+ *     all three components, over the full extent of the other axes (guard points from the
+ *     buffers' periodic images).  The normal component of a buffer is never written, so
+ *     E_d(0) and E_d(nx+1) become 0. */
+static int FN(step_open) = -1;
+static R *FN(step_lind) = 0;
+void FN(ora_set_open)(int axis, R *state)
+{
+    FN(step_open) = axis;
+    FN(step_lind) = state;
+}
+
+static void FN(lind_axes)(const FN(ora_grid) *g, int d, int *pa, int *pb)
+{
+    int k = 0, o[2] = {3, 3};
+    for (int a = 0; a < g->dim; a++)
+        if (a != d) o[k++] = a;
+    *pa = o[0];
+    *pb = o[1];
+}
+
+#define LS(st, s, m, c) (st)[3 * ((long)(s) * nperp + (m)) + (c)]
+
+static long FN(lind_nperp)(const FN(ora_grid) *g, int d)
+{
+    long n = 1;
+    for (int a = 0; a < g->dim; a++)
+        if (a != d) n *= g->nx[a];
+    return n;
+}
+
+/* grid index of component c at coordinate i along d and interior point (ia, ib) */
+static long FN(lind_at)(const FN(ora_grid) *g, int d, int pa, int pb, int c, int i, int ia, int ib)
+{
+    int ic[3] = {1, 1, 1};
+    ic[d] = i;
+    if (pa < 3) ic[pa] = ia;
+    if (pb < 3) ic[pb] = ib;
+    return FN(gidx)(g, c, ic[0], ic[1], ic[2]);
+}
+
+static void FN(lind_e)(const FN(ora_grid) *g, int d, R *e, R *st, R k)
+{
+    int pa, pb;
+    FN(lind_axes)(g, d, &pa, &pb);
+    const long nperp = FN(lind_nperp)(g, d);
+    const int na = pa < 3 ? g->nx[pa] : 1, nb = pb < 3 ? g->nx[pb] : 1, n = g->nx[d];
+    for (int ib = 1; ib <= nb; ib++)
+        for (int ia = 1; ia <= na; ia++) {
+            const long m = (ia - 1) + (long)na * (ib - 1);
+            for (int c = 0; c < 3; c++) {
+                if (c == d) continue;
+                const long p0 = FN(lind_at)(g, d, pa, pb, c, 0, ia, ib);
+                const long p1 = FN(lind_at)(g, d, pa, pb, c, 1, ia, ib);
+                e[p0] = LS(st, 1, m, c) + k * (LS(st, 0, m, c) - e[p1]);
+                LS(st, 0, m, c) = e[p0];
+                LS(st, 1, m, c) = e[p1];
+                const long q1 = FN(lind_at)(g, d, pa, pb, c, n + 1, ia, ib);
+                const long q2 = FN(lind_at)(g, d, pa, pb, c, n + 2, ia, ib);
+                e[q2] = LS(st, 3, m, c) + k * (LS(st, 4, m, c) - e[q1]);
+                LS(st, 3, m, c) = e[q1];
+                LS(st, 4, m, c) = e[q2];
+            }
+        }
+}
+
+static void FN(lind_b)(const FN(ora_grid) *g, int d, const R *e, R *st, const double *dx,
+                       double dt)
+{
+    int pa, pb;
+    FN(lind_axes)(g, d, &pa, &pb);
+    const long nperp = FN(lind_nperp)(g, d);
+    const int na = pa < 3 ? g->nx[pa] : 1, nb = pb < 3 ? g->nx[pb] : 1;
+    R h[3] = {K(0.0), K(0.0), K(0.0)};
+    for (int a = 0; a < g->dim; a++) h[a] = (R)(dt / dx[a]) * K(0.5);
+    for (int ib = 1; ib <= nb; ib++)
+        for (int ia = 1; ia <= na; ia++) {
+            const long m = (ia - 1) + (long)na * (ib - 1);
+            int ic[3] = {1, 1, 1};
+            ic[d] = 0;
+            if (pa < 3) ic[pa] = ia;
+            if (pb < 3) ic[pb] = ib;
+            /* E_c at the point and one cell up along axis a (a beyond dim: no derivative) */
+#define EV(c) e[FN(gidx)(g, c, ic[0], ic[1], ic[2])]
+#define EU(c, a) ((a) < g->dim ? e[FN(gidx)(g, c, ic[0] + ((a) == 0), ic[1] + ((a) == 1),     \
+                                            ic[2] + ((a) == 2))] : EV(c))
+            R *s = &LS(st, 2, m, 0);
+            s[0] = s[0] - h[1] * (EU(2, 1) - EV(2)) + h[2] * (EU(1, 2) - EV(1));
+            s[1] = s[1] - h[2] * (EU(0, 2) - EV(0)) + h[0] * (EU(2, 0) - EV(2));
+            s[2] = s[2] - h[0] * (EU(1, 0) - EV(1)) + h[1] * (EU(0, 1) - EV(0));
+#undef EV
+#undef EU
+        }
+}
+
+static void FN(lind_restore)(const FN(ora_grid) *g, int d, R *e, R *b, const R *st)
+{
+    int pa, pb;
+    FN(lind_axes)(g, d, &pa, &pb);
+    const long nperp = FN(lind_nperp)(g, d);
+    const int na = pa < 3 ? g->nx[pa] : 1, nb = pb < 3 ? g->nx[pb] : 1, n = g->nx[d];
+    const int la = pa < 3 ? 1 - g->gcl[pa] : 1, ua = pa < 3 ? na + g->gcu[pa] : 1;
+    const int lb = pb < 3 ? 1 - g->gcl[pb] : 1, ub = pb < 3 ? nb + g->gcu[pb] : 1;
+    for (int ib = lb; ib <= ub; ib++)
+        for (int ia = la; ia <= ua; ia++) {
+            const int wa = ((ia - 1) % na + na) % na, wb = ((ib - 1) % nb + nb) % nb;
+            const long m = wa + (long)na * wb;
+            for (int c = 0; c < 3; c++) {
+                e[FN(lind_at)(g, d, pa, pb, c, 0, ia, ib)] = LS(st, 0, m, c);
+                b[FN(lind_at)(g, d, pa, pb, c, 0, ia, ib)] = LS(st, 2, m, c);
+                e[FN(lind_at)(g, d, pa, pb, c, n + 1, ia, ib)] = LS(st, 3, m, c);
+            }
+        }
+}
+#undef LS
+
+/* the Yee advance with Lindman boundaries on axis d (update_boundary_b/e after every partial
+ * step, source/emf/solver/os-emf-solver-yee.f03:556-566) */
+void FN(ora_yee_advance_open)(int dim, const int *nx, const int *gcl, const int *gcu, R *e,
+                              R *b, const R *j, const double *dx, double dt, int d, R *st)
+{
+    FN(ora_grid) G, *g = &G;
+    FN(grid_init)(g, dim, nx, gcl, gcu);
+    const R k = (R)((1.0 - dt / dx[d]) / (1.0 + dt / dx[d]));
+    FN(dbdt)(g, b, e, dx, dt / 2.0);
+    FN(lind_b)(g, d, e, st, dx, dt);
+    FN(dedt)(g, e, b, j, dx, dt);
+    FN(lind_e)(g, d, e, st, k);
+    FN(dbdt)(g, b, e, dx, dt / 2.0);
+    FN(lind_b)(g, d, e, st, dx, dt);
+}
+
+/* guard update of E and B with Lindman boundaries on axis d: periodic along the others, then
+ * the boundary planes from the buffers */
+void FN(ora_open_guards)(int dim, const int *nx, const int *gcl, const int *gcu, R *e, R *b,
+                         int d, const R *st)
+{
+    FN(ora_grid) G, *g = &G;
+    FN(grid_init)(g, dim, nx, gcl, gcu);
+    FN(ora_periodic_skip)(dim, nx, gcl, gcu, e, 0, 1 << d);
+    FN(ora_periodic_skip)(dim, nx, gcl, gcu, b, 0, 1 << d);
+    FN(lind_restore)(g, d, e, b, st);
+}
+
+/* absorbing particle boundary along axis d (p_bc_absorbing: a particle that left the box is
+ * removed after its current was deposited, source/spec/os-spec-boundary.f03:501-511).  Here
+ * it stays in the arrays with charge and momentum 0, at offset 0 of the edge cell it left
+ * through; later steps still move it but, with charge 0, it deposits nothing. */
+void FN(ora_particle_absorb)(int dim, const int *nx, int np, int *ix, R *x, R *u, R *q, int d)
+{
+    for (int p = 0; p < np; p++) {
+        int *c = &ix[dim * p + d];
+        if (*c >= 1 && *c <= nx[d]) continue;
+        *c = *c < 1 ? 1 : nx[d];
+        x[dim * p + d] = K(0.0);
+        u[3 * p + 0] = u[3 * p + 1] = u[3 * p + 2] = K(0.0);
+        q[p] = K(0.0);
+    }
+}
+
 /* particle boundary after the push: periodic wrap, or along a walled axis specular
  * reflection (p_bc_specular, source/spec/os-spec-boundary.f03:1293-1310: u_d -> -u_d, the
  * particle to the edge cell at offset -x) */

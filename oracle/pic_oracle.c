@@ -474,8 +474,14 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
     ora_push_dt_##SFXN = dt;                                                                  \
     ora_iter_tol_##SFXN = (TOL);                                                              \
     const int walls = step_walls_##SFXN;                                                      \
-    ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, e, 0, walls);                                 \
-    ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, b, 0, walls);                                 \
+    const int oax = step_open_##SFXN; /* Lindman axis, -1: none */                            \
+    const int skip = walls | (oax >= 0 ? 1 << oax : 0);                                       \
+    if (oax >= 0) {                                                                           \
+        ora_open_guards_##SFXN(dim, nx, gcl, gcu, e, b, oax, step_lind_##SFXN);               \
+    } else {                                                                                  \
+        ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, e, 0, walls);                             \
+        ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, b, 0, walls);                             \
+    }                                                                                         \
     memset(j, 0, sizeof(R) * (size_t)gsz);                                                    \
     int nt = nthreads < 1 ? 1 : nthreads;                                                     \
     R *jt = nt > 1 ? (R *)calloc((size_t)gsz * (nt - 1), sizeof(R)) : 0;                     \
@@ -495,6 +501,8 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
         ene[s] = 0.0;                                                                         \
         for (int t = 0; t < nt; t++) ene[s] += et[t];                                         \
         free(et);                                                                             \
+        if (oax >= 0)                                                                         \
+            ora_particle_absorb_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], q[s], oax);         \
         ora_particle_bound_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], walls);                  \
     }                                                                                         \
     if (nt > 1) {                                                                             \
@@ -504,13 +512,16 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
         free(jt);                                                                             \
     }                                                                                         \
     ora_pusher_##SFXN = 0;                                                                    \
-    ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, j, 1, walls);                                 \
+    ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, j, 1, skip);                                  \
     if (walls) ora_walls_##SFXN(dim, nx, gcl, gcu, j, 2, walls, order);                       \
     if (step_smooth_ord_##SFXN[0] > 0)                                                       \
         ora_smooth_##SFXN(dim, nx, gcl, gcu, j, step_smooth_ord_##SFXN,                      \
                           step_smooth_coef_##SFXN);                                          \
     if (walls)                                                                                \
         ora_yee_advance_walls_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt, walls, order);      \
+    else if (oax >= 0)                                                                        \
+        ora_yee_advance_open_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt, oax,                 \
+                                    step_lind_##SFXN);                                        \
     else                                                                                      \
         ora_yee_advance_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt);                           \
     return 0;

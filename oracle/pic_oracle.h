@@ -56,6 +56,11 @@ void ora_walls_f64(int dim, const int *nx, const int *gcl, const int *gcu, doubl
                    int walls, int order);
 void ora_set_walls_f32(int walls);
 void ora_set_walls_f64(int walls);
+/* Lindman open boundaries at both edges of `axis` (-1: none) for the step functions below;
+ * `state` holds 15 reals per interior point of the other axes, zeroed before the first step
+ * and kept between steps */
+void ora_set_open_f32(int axis, float *state);
+void ora_set_open_f64(int axis, double *state);
 void ora_field_energy_f32(int dim, const int *nx, const int *gcl, const int *gcu,
                           const float *f, const double *dx, double *out);
 void ora_field_energy_f64(int dim, const int *nx, const int *gcl, const int *gcu,

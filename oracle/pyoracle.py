@@ -85,6 +85,7 @@ def _declare(L):
         getattr(L, f"ora_set_smooth_{s_}").argtypes = [P, P]
         getattr(L, f"ora_walls_{s_}").argtypes = [I, P, P, P, P, I, I, I]
         getattr(L, f"ora_set_walls_{s_}").argtypes = [I]
+        getattr(L, f"ora_set_open_{s_}").argtypes = [I, P]
     L.ora_push_pusher_f32.argtypes = [I, I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P,
                                       P, D, D, P]
     L.ora_push_pusher_f64.argtypes = [I, I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, D,
@@ -314,10 +315,22 @@ def walls(g: "Grid", prec, f, kind, mask):
                                         int(mask), g.order)
 
 
+def lindman_state(g: "Grid", prec, axis):
+    """Zeroed state of Lindman open boundaries at both edges of `axis` (15 reals per interior
+    point of the other axes), kept by the caller between steps."""
+    n = 1
+    for a in range(g.dim):
+        if a != axis:
+            n *= g.nx[a]
+    return np.zeros(15 * n, dtype=dtype_of(prec))
+
+
 def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="boris",
-         iter_tol=1e-3, smooth=None, walls=0):
+         iter_tol=1e-3, smooth=None, walls=0, open_fields=None):
     """One full time step; species = list of dicts with ix, x, u, q, rqm.  walls (bit d):
-    axis d bounded by conducting walls instead of periodic.
+    axis d bounded by conducting walls instead of periodic.  open_fields = (axis, state from
+    lindman_state): Lindman open boundaries at both edges of that axis, particles absorbed
+    there (left in the arrays with charge and momentum 0).
     Returns the per-species energy sums (Boris: time-centred u^2/(gamma+1); exact pusher:
     gamma - 1 of the new momentum; both times q).  fast=True runs the -O3 -ffast-math build
     (timing only)."""
@@ -338,6 +351,8 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     args = (g.dim, g.order, _p(nx), _p(gl), _p(gu), _p(_f64(g.dx + [0.0] * 3)), float(dt), _p(e),
             _p(b), _p(j), ns, _p(np_), ixs, xs, us, qs, _p(rqm), _p(ene), int(nthreads))
     getattr(L, f"ora_set_walls_{prec}")(int(walls))
+    if open_fields is not None:
+        getattr(L, f"ora_set_open_{prec}")(int(open_fields[0]), _p(open_fields[1]))
     try:
         if pusher != "boris":
             getattr(L, f"ora_step_pusher_{prec}")(PUSHERS[pusher], *args, float(iter_tol))
@@ -345,6 +360,7 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
             getattr(L, f"ora_step_{prec}")(*args)
     finally:
         getattr(L, f"ora_set_walls_{prec}")(0)
+        getattr(L, f"ora_set_open_{prec}")(-1, None)
     if smooth is not None:
         getattr(L, f"ora_set_smooth_{prec}")(None, None)
     return ene

@@ -72,7 +72,8 @@ class Config(C.Structure):
     _fields_ = [("dim", I), ("order", I), ("precision", I), ("engine", I), ("nx", I * 3),
                 ("dx", D * 3), ("dt", D), ("tile", I * 3), ("n_sort", I), ("capacity", D),
                 ("pusher", I), ("iter_tol", D), ("smooth_type", I), ("smooth_order", I),
-                ("walls", I)]
+                ("walls", I),
+                ("open_fields", I)]
 
 
 def _declare(lb):
@@ -373,7 +374,7 @@ class Simulation:
 
     def __init__(self, nx, dx, dt, order=2, precision=32, engine=ENGINE_TILED, tile=None,
                  n_sort=0, capacity=0.0, pusher=PUSHER_BORIS, iter_tol=0.0,
-                 smooth_type=SMOOTH_NONE, smooth_order=0, walls=0):
+                 smooth_type=SMOOTH_NONE, smooth_order=0, walls=0, open_fields=0):
         self.dim = len(nx)
         self.nx = list(nx)
         self.order = order
@@ -396,6 +397,7 @@ class Simulation:
         cfg.smooth_type = smooth_type
         cfg.smooth_order = smooth_order
         cfg.walls = walls
+        cfg.open_fields = open_fields
         self.cfg = cfg
         self.dx = list(dx)
         self.dt = dt

@@ -204,16 +204,161 @@ void wall_update(const GridDesc &g, T *f, int kind, int walls, int order, cudaSt
     }
 }
 
+// ------------------------------------------------------------------------ Lindman boundaries
+// Both edges of axis d are open (update_lindman_{2,3}d_e/b and update_emfbound_lindman,
+// source/emf/boundary/os-emf-lindman.f90:454-1042).  The state holds five buffer planes along
+// d -- slot 0 E at i_d = 0, 1 E at 1, 2 B at 0 (the lower buffers, range [0, 1]), 3 E at
+// nx+1, 4 E at nx+2 (the upper ones, range [nx, nx+2]) -- with 3 components per interior point
+// m of the other axes (the lower other axis fastest); element (slot, m, c) at
+// 3 * (slot * nperp + m) + c.  Only the components other than d of the E planes are ever
+// written, so their normal component stays at the zero the buffers start with.
+struct LindAxes {
+    int d, pa, pb;        // the open axis and the other two (3: none)
+    int na, nb;           // their interior extents (1 for none)
+    long nperp;           // na * nb
+};
+
+static LindAxes lind_axes(const GridDesc &g, int d)
+{
+    LindAxes L;
+    L.d = d;
+    int o[2] = {3, 3}, k = 0;
+    for (int a = 0; a < g.dim; a++)
+        if (a != d) o[k++] = a;
+    L.pa = o[0];
+    L.pb = o[1];
+    L.na = L.pa < 3 ? g.nx[L.pa] : 1;
+    L.nb = L.pb < 3 ? g.nx[L.pb] : 1;
+    L.nperp = (long)L.na * L.nb;
+    return L;
+}
+
+long lindman_state_size(const GridDesc &g, int axis) { return 15L * lind_axes(g, axis).nperp; }
+
+__device__ __forceinline__ long lind_pos(const GridDesc &g, const LindAxes &L, int i, int ia,
+                                         int ib)
+{
+    int ic[3] = {1, 1, 1};
+    ic[L.d] = i;
+    if (L.pa < 3) ic[L.pa] = ia;
+    if (L.pb < 3) ic[L.pb] = ib;
+    return pos(g, ic[0], ic[1], ic[2]);
+}
+
+// after the E step: first-order Mur update of the two tangential components on the planes
+// i_d = 0 (from i_d = 1) and i_d = nx+2 (from nx+1), with k = (1 - dt/dx_d) / (1 + dt/dx_d)
+template <typename T>
+__global__ void k_lindman_e(GridDesc g, LindAxes L, T *__restrict__ e, T *__restrict__ st, T k)
+{
+    OSG_GRID_LOOP(m, L.nperp)
+    {
+        const int ia = 1 + (int)(m % L.na), ib = 1 + (int)(m / L.na), n = g.nx[L.d];
+        const long p0 = lind_pos(g, L, 0, ia, ib), p1 = lind_pos(g, L, 1, ia, ib);
+        const long q1 = lind_pos(g, L, n + 1, ia, ib), q2 = lind_pos(g, L, n + 2, ia, ib);
+        T *s0 = st + 3 * (0 * L.nperp + m), *s1 = st + 3 * (1 * L.nperp + m);
+        T *s3 = st + 3 * (3 * L.nperp + m), *s4 = st + 3 * (4 * L.nperp + m);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            if (c == L.d) continue;
+            const T e1 = e[p1 + c];
+            const T e0 = s1[c] + k * (s0[c] - e1);
+            e[p0 + c] = e0;
+            s0[c] = e0;
+            s1[c] = e1;
+            const T f1 = e[q1 + c];
+            const T f2 = s3[c] + k * (s4[c] - f1);
+            e[q2 + c] = f2;
+            s3[c] = f1;
+            s4[c] = f2;
+        }
+    }
+}
+
+// after each B half step: the lower B buffer takes the Yee increment of the plane i_d = 0
+// (h = dt / dx * 0.5 per axis, 0 beyond dim)
+template <typename T>
+__global__ void k_lindman_b(GridDesc g, LindAxes L, const T *__restrict__ e, T *__restrict__ st,
+                            T h0, T h1, T h2)
+{
+    OSG_GRID_LOOP(m, L.nperp)
+    {
+        const int ia = 1 + (int)(m % L.na), ib = 1 + (int)(m / L.na);
+        const long p = lind_pos(g, L, 0, ia, ib);
+        const long u0 = p + 3, u1 = g.dim > 1 ? p + g.stride(1) : p,
+                   u2 = g.dim > 2 ? p + g.stride(2) : p;
+        T *s = st + 3 * (2 * L.nperp + m);
+        s[0] = s[0] - h1 * (e[u1 + 2] - e[p + 2]) + h2 * (e[u2 + 1] - e[p + 1]);
+        s[1] = s[1] - h2 * (e[u2 + 0] - e[p + 0]) + h0 * (e[u0 + 2] - e[p + 2]);
+        s[2] = s[2] - h0 * (e[u0 + 1] - e[p + 1]) + h1 * (e[u1 + 0] - e[p + 0]);
+    }
+}
+
+// the planes E(0), B(0) and E(nx+1), all components, over the full extent of the other axes;
+// a guard point takes the buffer value of its periodic image (the buffers' own periodic
+// update along the other axes, update_boundary_lindman :352-368)
+template <typename T>
+__global__ void k_lindman_restore(GridDesc g, LindAxes L, T *__restrict__ e, T *__restrict__ b,
+                                  const T *__restrict__ st, long nfull)
+{
+    OSG_GRID_LOOP(m, nfull)
+    {
+        const int fa = L.pa < 3 ? g.size[L.pa] : 1;
+        const int la = L.pa < 3 ? 1 - g.gcl[L.pa] : 1, lb = L.pb < 3 ? 1 - g.gcl[L.pb] : 1;
+        const int ia = la + (int)(m % fa), ib = lb + (int)(m / fa);
+        const int wa = ((ia - 1) % L.na + L.na) % L.na, wb = ((ib - 1) % L.nb + L.nb) % L.nb;
+        const long w = wa + (long)L.na * wb;
+        const long p0 = lind_pos(g, L, 0, ia, ib), q1 = lind_pos(g, L, g.nx[L.d] + 1, ia, ib);
+        const T *s0 = st + 3 * (0 * L.nperp + w), *s2 = st + 3 * (2 * L.nperp + w),
+                *s3 = st + 3 * (3 * L.nperp + w);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            e[p0 + c] = s0[c];
+            b[p0 + c] = s2[c];
+            e[q1 + c] = s3[c];
+        }
+    }
+}
+
+template <typename T>
+static void launch_lindman_b(const GridDesc &g, const LindAxes &L, const T *e, T *lind,
+                             const double *dx, double dt, cudaStream_t st)
+{
+    T h[3] = {T(0), T(0), T(0)};
+    for (int a = 0; a < g.dim; a++) h[a] = (T)(dt / dx[a]) * T(0.5);
+    k_lindman_b<T><<<blocks_for(L.nperp, 256), 256, 0, st>>>(g, L, e, lind, h[0], h[1], h[2]);
+}
+
+template <typename T>
+void open_guards(const GridDesc &g, T *e, T *b, int axis, const T *lind, cudaStream_t st)
+{
+    periodic_update<T>(g, e, 0, st, 0, 1 << axis);
+    periodic_update<T>(g, b, 0, st, 0, 1 << axis);
+    const LindAxes L = lind_axes(g, axis);
+    long nfull = 1;
+    if (L.pa < 3) nfull *= g.size[L.pa];
+    if (L.pb < 3) nfull *= g.size[L.pb];
+    k_lindman_restore<T><<<blocks_for(nfull, 256), 256, 0, st>>>(g, L, e, b, lind, nfull);
+}
+
 template <typename T>
 void yee_advance(const GridDesc &g, T *e, T *b, const T *j, const double *dx, double dt,
-                 cudaStream_t st, int walls, int order)
+                 cudaStream_t st, int walls, int order, int open_axis, T *lind)
 {
+    const bool open = open_axis >= 0 && lind;
+    LindAxes L{};
+    if (open) L = lind_axes(g, open_axis);
     launch_dbdt(g, b, e, dx, dt / 2.0, st);
     if (walls) wall_update(g, b, 1, walls, order, st);
+    if (open) launch_lindman_b(g, L, e, lind, dx, dt, st);
     launch_dedt(g, e, b, j, dx, dt, st);
     if (walls) wall_update(g, e, 0, walls, order, st);
+    if (open) {
+        const T k = (T)((1.0 - dt / dx[open_axis]) / (1.0 + dt / dx[open_axis]));
+        k_lindman_e<T><<<blocks_for(L.nperp, 256), 256, 0, st>>>(g, L, e, lind, k);
+    }
     launch_dbdt(g, b, e, dx, dt / 2.0, st);
     if (walls) wall_update(g, b, 1, walls, order, st);
+    if (open) launch_lindman_b(g, L, e, lind, dx, dt, st);
 }
 
 // One direction of the periodic update.  Thread n handles one guard point (lower or upper
@@ -673,9 +818,14 @@ void smooth_field(const GridDesc &g, const SmoothSpec &sp, T *f, T *tmp, cudaStr
 }
 
 template void yee_advance<float>(const GridDesc &, float *, float *, const float *,
-                                 const double *, double, cudaStream_t, int, int);
+                                 const double *, double, cudaStream_t, int, int, int, float *);
 template void yee_advance<double>(const GridDesc &, double *, double *, const double *,
-                                  const double *, double, cudaStream_t, int, int);
+                                  const double *, double, cudaStream_t, int, int, int,
+                                  double *);
+template void open_guards<float>(const GridDesc &, float *, float *, int, const float *,
+                                 cudaStream_t);
+template void open_guards<double>(const GridDesc &, double *, double *, int, const double *,
+                                  cudaStream_t);
 template void periodic_update<float>(const GridDesc &, float *, int, cudaStream_t, int, int);
 template void periodic_update<double>(const GridDesc &, double *, int, cudaStream_t, int, int);
 template void wall_update<float>(const GridDesc &, float *, int, int, int, cudaStream_t);

@@ -49,9 +49,22 @@ __host__ __device__ inline Box make_box(const GridDesc &g, int lo, int hi_off)
 // B half step, E full step, B half step; the axes in `walls` (bit d) are bounded by perfectly
 // conducting walls, whose images are taken after every partial step as the reference's
 // update_boundary_b / update_boundary_e (source/emf/solver/os-emf-solver-yee.f03:556-566)
+// With open_axis >= 0 both edges of that axis are Lindman open boundaries whose state
+// `lind` (lindman_state_size reals, zeroed before the first step) the E and B steps update
+// (update_boundary_b / update_boundary_e, the same lines).
 template <typename T>
 void yee_advance(const GridDesc &g, T *e, T *b, const T *j, const double *dx, double dt,
-                 cudaStream_t st, int walls = 0, int order = 2);
+                 cudaStream_t st, int walls = 0, int order = 2, int open_axis = -1,
+                 T *lind = nullptr);
+// Lindman open boundaries at both edges of one axis (p_bc_lindman,
+// source/emf/boundary/os-emf-lindman.f90).  Their state: 5 buffer planes along the axis
+// (E at 0 and 1, B at 0, E at nx+1 and nx+2), 3 components, per interior point of the other
+// axes.
+long lindman_state_size(const GridDesc &g, int axis);
+// guard update of E and B with Lindman boundaries on `axis`: periodic along the other axes,
+// then the boundary planes E(0), B(0), E(nx+1) from the state (update_emfbound_lindman)
+template <typename T>
+void open_guards(const GridDesc &g, T *e, T *b, int axis, const T *lind, cudaStream_t st);
 // conducting-wall images along the axes in `walls`: kind 0 E, 1 B (guards set), 2 J (guards
 // added into the box)
 template <typename T>

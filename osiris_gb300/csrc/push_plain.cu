@@ -157,12 +157,21 @@ __device__ __forceinline__ int wrap_cell(int c, int n)
 // New cell and offset of a particle along axis d: periodic wrap, or specular reflection at a
 // conducting wall (p_bc_specular, source/spec/os-spec-boundary.f03:1293-1310: the momentum
 // along d flips, the particle goes to the edge cell at the mirrored offset), after its current
-// was deposited along the unreflected path.
+// was deposited along the unreflected path; or absorption at an open edge (p_bc_absorbing,
+// :501-511: the reference removes the particle after its deposit; here it stays in the
+// arrays with charge and momentum 0 at offset 0 of the edge cell, and deposits nothing more).
 template <typename T, int DIM>
 __device__ __forceinline__ void store_position(const PlainPushArgs<T> &a, long p, int d, int cn,
                                                T xn)
 {
-    if (a.reflect[d] > 0 && (cn < 1 || cn > a.reflect[d])) {
+    if (a.absorb[d] > 0 && (cn < 1 || cn > a.absorb[d])) {
+        cn = cn < 1 ? 1 : a.absorb[d];
+        xn = T(0);
+        a.u[3 * p + 0] = T(0);
+        a.u[3 * p + 1] = T(0);
+        a.u[3 * p + 2] = T(0);
+        a.q_absorb[p] = T(0);
+    } else if (a.reflect[d] > 0 && (cn < 1 || cn > a.reflect[d])) {
         cn = cn < 1 ? 1 : a.reflect[d];
         xn = -xn;
         a.u[3 * p + d] = -a.u[3 * p + d];
@@ -423,6 +432,8 @@ PlainPushArgs<T> make_plain_args(int dim, int order, int *ix, T *x, T *u, const 
     }
     a.wrap[0] = a.wrap[1] = a.wrap[2] = 0;
     a.reflect[0] = a.reflect[1] = a.reflect[2] = 0;
+    a.absorb[0] = a.absorb[1] = a.absorb[2] = 0;
+    a.q_absorb = nullptr;
     a.pusher = OSG_PUSHER_BORIS;
     a.qm = T(1) / rqm;
     a.rqm = rqm;

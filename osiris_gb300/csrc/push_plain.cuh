@@ -28,6 +28,9 @@ template <typename T> struct PlainPushArgs {
     int wrap[3];           // > 0: periodic wrap of the stored cell index into [1, wrap[d]]
     int reflect[3];        // > 0: conducting walls at the edges of [1, reflect[d]]: specular
                            // reflection of a particle that crossed one
+    int absorb[3];         // > 0: open edges of [1, absorb[d]]: a particle that crossed one is
+                           // absorbed (charge and momentum set to 0 in q_absorb and u)
+    T *q_absorb;           // the charges, writable (only with an absorbing axis)
     int pusher;            // OSG_PUSHER_*
     T qm;                  // 1 / rqm (exact pusher)
     T rqm;                 // the species' rqm (Euler-rotation pusher)

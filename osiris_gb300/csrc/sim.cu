@@ -61,6 +61,8 @@ struct osg_sim {
     double xmoved = 0.0;         // window motion not yet turned into a cell move
     long moves = 0;              // cell moves so far
     void *shift_tmp = nullptr;   // scratch field array for the shift and the smoothing
+    int open_axis = -1;          // Lindman open boundaries at both edges of this axis
+    void *lind = nullptr;        // their state (lindman_state_size reals)
     osg::SmoothSpec smooth;      // current smoothing (order 0 per axis: none)
     // graphs: [parity][sort (plain) / window move (tiled)]
     cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
@@ -254,10 +256,19 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
     const int open = s->window ? 1 : 0;   // x1 open while the window moves
     // conducting walls: their guard cells hold the images set by the last field advance
     const int walls = c.walls;
+    // Lindman open boundaries: no periodic update along their axis, the boundary planes come
+    // from their state, the current beyond them is neither folded nor imaged
+    const int oax = s->open_axis;
+    const int skip = walls | (oax >= 0 ? 1 << oax : 0);
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[0], st));
-    periodic_update<T>(s->g, (T *)s->e, 0, st, open, walls);
-    periodic_update<T>(s->g, (T *)s->b, 0, st, open, walls);
-    launches += 2 * c.dim;
+    if (oax >= 0) {
+        open_guards<T>(s->g, (T *)s->e, (T *)s->b, oax, (const T *)s->lind, st);
+        launches += 2 * (c.dim - 1) + 1;
+    } else {
+        periodic_update<T>(s->g, (T *)s->e, 0, st, open, walls);
+        periodic_update<T>(s->g, (T *)s->b, 0, st, open, walls);
+        launches += 2 * c.dim;
+    }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[1], st));
     OSG_CUDA(cudaMemsetAsync(s->j, 0, (size_t)s->esz * 3 * s->g.npoints(), st));
     OSG_CUDA(cudaMemsetAsync(s->d_ene, 0, sizeof(double) * MAX_SPECIES, st));
@@ -274,9 +285,11 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
                 (T)s->rqm[k], (const T *)s->e, (const T *)s->b, emf_size, emf_off, (T *)s->j,
                 emf_size, emf_off, c.dx, push_dt, s->d_ene + k, s->d_status);
             for (int d = 0; d < c.dim; d++) {
-                a.wrap[d] = (walls >> d) & 1 ? 0 : c.nx[d];
+                a.wrap[d] = (skip >> d) & 1 ? 0 : c.nx[d];
                 a.reflect[d] = (walls >> d) & 1 ? c.nx[d] : 0;
+                a.absorb[d] = d == oax ? c.nx[d] : 0;
             }
+            a.q_absorb = (T *)p.q;
             a.pusher = c.pusher;
             a.iter_tol = c.iter_tol;
             if (c.pusher >= OSG_PUSHER_VAY)
@@ -295,8 +308,8 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
         }
     }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[3], st));
-    periodic_update<T>(s->g, (T *)s->j, 1, st, open, walls);
-    launches += c.dim;
+    periodic_update<T>(s->g, (T *)s->j, 1, st, open, skip);
+    launches += c.dim - (oax >= 0 ? 1 : 0);
     if (walls) {
         // current deposited beyond a wall comes back as its image (update_boundary_current,
         // source/current/os-current-define.f03:683-725)
@@ -309,8 +322,9 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
         launches += c.dim;
     }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[4], st));
-    yee_advance<T>(s->g, (T *)s->e, (T *)s->b, (const T *)s->j, c.dx, c.dt, st, walls, c.order);
-    launches += 3 + (walls ? 6 * __builtin_popcount(walls) : 0);
+    yee_advance<T>(s->g, (T *)s->e, (T *)s->b, (const T *)s->j, c.dx, c.dt, st, walls, c.order,
+                   oax, (T *)s->lind);
+    launches += 3 + (walls ? 6 * __builtin_popcount(walls) : 0) + (oax >= 0 ? 3 : 0);
     if (shift) {
         shift_window_x<T>(s->g, (T *)s->e, (T *)s->shift_tmp, st);
         shift_window_x<T>(s->g, (T *)s->b, (T *)s->shift_tmp, st);
@@ -442,6 +456,12 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               "walls: a bit mask of the axes");
     OSG_CHECK(cfg->walls == 0 || cfg->smooth_type == OSG_SMOOTH_NONE, OSG_ERR_ARG,
               "current smoothing next to conducting walls is not supported");
+    OSG_CHECK(cfg->open_fields >= 0 && cfg->open_fields < (1 << cfg->dim) &&
+                  (cfg->open_fields & (cfg->open_fields - 1)) == 0,
+              OSG_ERR_ARG, "open_fields: the bit of one axis (Lindman boundaries are admitted "
+                           "along one axis)");
+    OSG_CHECK(cfg->open_fields == 0 || (cfg->walls == 0 && cfg->smooth_type == OSG_SMOOTH_NONE),
+              OSG_ERR_ARG, "open boundaries combine with neither walls nor smoothing");
     OSG_CHECK(cfg->pusher >= OSG_PUSHER_BORIS && cfg->pusher <= OSG_PUSHER_EULER, OSG_ERR_ARG,
               "unknown pusher");
     OSG_CHECK(cfg->iter_tol >= 0, OSG_ERR_ARG, "iter_tol must be >= 0");
@@ -496,6 +516,12 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
     s->d_status = rc ? nullptr : dalloc<int>(4, &rc);
     s->d_diag = rc ? nullptr : dalloc<double>(16, &rc);
     if (!rc && s->smooth.order[0] > 0) s->shift_tmp = dalloc<char>(gbytes, &rc);
+    size_t lbytes = 0;
+    if (!rc && cfg->open_fields) {
+        s->open_axis = __builtin_ctz(cfg->open_fields);
+        lbytes = (size_t)s->esz * lindman_state_size(s->g, s->open_axis);
+        s->lind = dalloc<char>(lbytes, &rc);
+    }
     if (rc) {
         osg_sim_destroy(s);
         return rc;
@@ -503,6 +529,7 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
     cudaMemsetAsync(s->e, 0, gbytes, s->st);
     cudaMemsetAsync(s->b, 0, gbytes, s->st);
     cudaMemsetAsync(s->j, 0, gbytes, s->st);
+    if (s->lind) cudaMemsetAsync(s->lind, 0, lbytes, s->st);
     cudaMemsetAsync(s->d_status, 0, 4 * sizeof(int), s->st);
     cudaMemsetAsync(s->d_ene, 0, MAX_SPECIES * sizeof(double), s->st);
     if (cfg->engine == OSG_ENGINE_TILED) {
@@ -537,6 +564,7 @@ int osg_sim_destroy(osg_sim *s)
     cudaFree(s->b);
     cudaFree(s->j);
     cudaFree(s->shift_tmp);
+    cudaFree(s->lind);
     cudaFree(s->d_ene);
     cudaFree(s->d_status);
     cudaFree(s->d_diag);
@@ -713,6 +741,8 @@ int osg_sim_set_window(osg_sim *s, int species, const int *ppc, int nprof, const
     OSG_CHECK(s->cfg.engine == OSG_ENGINE_TILED, OSG_ERR_ARG,
               "the moving window runs on the tiled engine");
     OSG_CHECK(s->step_n == 0, OSG_ERR_STATE, "set the window before the first step");
+    OSG_CHECK(s->open_axis < 0, OSG_ERR_ARG, "the moving window does not combine with "
+                                             "Lindman open boundaries");
     int rc = tiled_set_window(s->tiled, species, ppc, nprof, prof_x, prof_f);
     if (rc) return rc;
     if (!s->shift_tmp) {
@@ -728,13 +758,16 @@ int osg_sim_set_window(osg_sim *s, int species, const int *ppc, int nprof, const
 }
 
 // ------------------------------------------------------------------------ checkpoint
-// File layout (native byte order, as the reference's restart files): the tag "OSGCKPT1", the
+// File layout (native byte order, as the reference's restart files): the tag "OSGCKPT2", the
 // int size of osg_config and the struct, long step count, int window flag, double xmoved,
 // long window moves, the window's injection parameters (int species, int ppc[3], int nprof,
 // double prof_x[8], double prof_f[8]), int species count, then per species double rqm, long
 // np and its arrays in reference layout (ix(dim,np) int, x(dim,np), u(3,np), q(np) in the
-// run's precision), last long grid points and E(3,points), B(3,points) with guard cells.
-// The current is rebuilt by the next step and is not stored.
+// run's precision), then long grid points and E(3,points), B(3,points) with guard cells, last,
+// with Lindman open boundaries, their state (lindman_state_size reals; the reference stores
+// its Lindman buffers in the restart file too, restart_write_lindman,
+// source/emf/boundary/os-emf-lindman.f90:135-156).  The current is rebuilt by the next step
+// and is not stored.
 namespace {
 
 struct CkptFile {
@@ -748,7 +781,7 @@ struct CkptFile {
 bool put(FILE *f, const void *p, size_t n) { return n == 0 || fwrite(p, 1, n, f) == n; }
 bool get(FILE *f, void *p, size_t n) { return n == 0 || fread(p, 1, n, f) == n; }
 
-const char CKPT_TAG[8] = {'O', 'S', 'G', 'C', 'K', 'P', 'T', '1'};
+const char CKPT_TAG[8] = {'O', 'S', 'G', 'C', 'K', 'P', 'T', '2'};
 
 } // namespace
 
@@ -789,6 +822,12 @@ int osg_sim_checkpoint(osg_sim *s, const char *path)
         const int rc = osg_sim_get_fields(s, e.data(), b.data(), nullptr);
         if (rc) return rc;
         ok = put(f, &npt, sizeof npt) && put(f, e.data(), e.size()) && put(f, b.data(), b.size());
+    }
+    if (ok && s->lind) {
+        std::vector<char> l((size_t)s->esz * lindman_state_size(s->g, s->open_axis));
+        OSG_CUDA(cudaMemcpyAsync(l.data(), s->lind, l.size(), cudaMemcpyDeviceToHost, s->st));
+        OSG_CUDA(cudaStreamSynchronize(s->st));
+        ok = put(f, l.data(), l.size());
     }
     OSG_CHECK(ok && fflush(f) == 0, OSG_ERR_ARG, "write to %s failed", path);
     return OSG_OK;
@@ -844,6 +883,17 @@ int osg_sim_restore(const char *path, osg_sim **out)
             rc = OSG_ERR_ARG;
         else
             rc = osg_sim_set_fields(s, e.data(), b.data());
+    }
+    if (rc == OSG_OK && s->lind) {
+        std::vector<char> l((size_t)esz * lindman_state_size(s->g, s->open_axis));
+        if (!get(f, l.data(), l.size())) {
+            rc = OSG_ERR_ARG;
+        } else if (cudaMemcpyAsync(s->lind, l.data(), l.size(), cudaMemcpyHostToDevice, s->st) !=
+                       cudaSuccess ||
+                   cudaStreamSynchronize(s->st) != cudaSuccess) {
+            set_error("upload of the Lindman state failed");
+            rc = OSG_ERR_CUDA;
+        }
     }
     if (rc == OSG_OK && win) {
         rc = osg_sim_set_window(s, wsp, wppc, wn, wx, wf);

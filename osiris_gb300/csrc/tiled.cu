@@ -68,6 +68,7 @@ struct TiledState {
     // kernel replay saves and restores device memory and needs the dropped lines defined)
     int l2_discard = 1;
     int walls = 0;   // bit d: conducting walls on axis d
+    int open_fields = 0;   // bit d: Lindman open boundaries on axis d (particles absorbed)
     int pusher = OSG_PUSHER_BORIS;
     double iter_tol = 1.0e-3;
     long nj_tile = 0;    // current points (x3 components) of a tile with its halo
@@ -211,6 +212,7 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
     t->dt = cfg.dt;
     t->capacity = cfg.capacity > 0 ? cfg.capacity : 3.0;
     t->walls = cfg.walls;
+    t->open_fields = cfg.open_fields;
     t->ntiles = 1;
     for (int d = 0; d < 3; d++) {
         t->nx[d] = d < cfg.dim ? cfg.nx[d] : 1;
@@ -632,7 +634,7 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     // the push writes every tile's sorted count and adds arrivals to zeroed counters
     OSG_CUDA(cudaMemsetAsync(t->d_arr[1 - parity], 0, sizeof(int) * MAX_TILED_SPECIES * t->ntiles, st));
     TiledArgs a = tiled_args(t, parity, e, b, j, d_ene, d_status);
-    a.open_x = t->window ? 1 : 0;
+    a.open = (t->window ? 1 : 0) | t->open_fields;
     a.shift_x = t->window && shift ? 1 : 0;
     const size_t sm = t->smem_bytes;
     const unsigned nt = (unsigned)t->ntiles;

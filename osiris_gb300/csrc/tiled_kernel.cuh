@@ -111,10 +111,11 @@ struct TiledArgs {
     // 2D), summed in FP64 in tile order by k_tile_fold
     float *tile_hi;
     float *tile_lo;
-    // moving window along x1: open_x = 1 makes x1 non-periodic; shift_x = 1 (a step that ends
-    // with a window move) stores every particle one cell lower in x1, particles that leave
-    // the box along x1 are dropped
-    int open_x;
+    // bit d: axis d is open (no periodic wrap): particles that leave the box along it are
+    // dropped (absorbed).  Bit 0 with the moving window along x1, or the axis of Lindman
+    // open boundaries.  shift_x = 1 (a step that ends with a window move) stores every
+    // particle one cell lower in x1
+    int open;
     int shift_x;
     // bit d: axis d is bounded by conducting walls (particles reflect specularly)
     int walls;
@@ -412,12 +413,17 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                             un[d] = -un[d];
                         }
                     } else {
-                        cw[d] = (d == 0 && a.open_x) ? cn - a.shift_x : wrapc(cn, a.nx[d]);
+                        cw[d] = ((a.open >> d) & 1) ? cn - (d == 0 ? a.shift_x : 0)
+                                                    : wrapc(cn, a.nx[d]);
                     }
                 }
-                // (open x1: a particle outside [1, nx] has left the window; its current of
-                //  this step is already in the segments)
-                if (a.open_x && (cw[0] < 1 || cw[0] > a.nx[0])) {
+                // (open axis: a particle outside [1, nx] has left the box or the window; its
+                //  current of this step is already in the segments)
+                bool gone = false;
+#pragma unroll
+                for (int d = 0; d < DIM; d++)
+                    gone = gone || (((a.open >> d) & 1) && (cw[d] < 1 || cw[d] > a.nx[d]));
+                if (gone) {
                     *rec_ix0<DIM>(rin, p) = 0;
                     has = false;
                 } else {
