@@ -68,6 +68,8 @@ extern "C" {
 #define OSG_PUSHER_HC 3      /* push_type = "cary" (Higuera-Cary, dudt_cary, same file) */
 #define OSG_PUSHER_FULLROT 4 /* push_type = "fullrot" (dudt_fullrot, same file) */
 #define OSG_PUSHER_EULER 5   /* push_type = "euler" (dudt_euler, same file) */
+#define OSG_PUSHER_COND_VAY 6 /* push_type = "cond_vay" (dudt_cond_vay, same file: Vay when the
+                                 particle's gamma exceeds 5, else Boris) */
 
 const char *osg_last_error(void);
 int osg_version(void);
@@ -266,7 +268,7 @@ typedef struct {
     int n_sort;       /* PLAIN: cell sort every n_sort steps (0 = never); TILED sorts every step */
     double capacity;  /* TILED: slots per tile as a multiple of the mean load (0 = 3.0) */
     int pusher;       /* OSG_PUSHER_BORIS (0), _EXACT (1), _VAY (2), _HC (3), _FULLROT (4),
-                         _EULER (5) */
+                         _EULER (5), _COND_VAY (6) */
     double iter_tol;  /* exact pusher: Newton tolerance (0 = the reference default 1e-3) */
     int smooth_type;  /* current smoothing after the guard fold, OSG_SMOOTH_* (all axes) */
     int smooth_order; /* its order (binomial: passes; compensated: >= 2; others fixed) */

@@ -181,6 +181,45 @@ static R EXN(ora_vay_u)(R tem, const R *e, const R *b, R *u, R q)
     return (q * uc2) / (gc + K(1.0));
 }
 
+/* Conditional Vay pusher (dudt_cond_vay, source/spec/os-spec-push.f03:800-1100): tem =
+ * real(0.5 dt / rqm) (:835).  A particle whose gamma of the old momentum, sqrt(1 + p1**2 +
+ * p2**2 + p3**2) left to right (:856), exceeds 5 takes the Vay update and its energy term
+ * (:883-1007); the others the Boris loops of the same routine (:1011-1094): half kick,
+ * energy q u2 / (gamma + 1) with the division in double, b scaled by tem / gamma, the
+ * rotation written as two passes per cross product, 2 / (((1 + b1**2) + b2**2) + b3**2),
+ * half kick. */
+static double EXN(ora_cond_vay_u)(R tem, const R *e, const R *b, R *u, R q)
+{
+    const R g0 = SQRT(((K(1.0) + u[0] * u[0]) + u[1] * u[1]) + u[2] * u[2]);
+    if (g0 > K(5.0)) return (double)EXN(ora_vay_u)(tem, e, b, u, q);
+    R ep[3], bp[3], ut[3], pn[3];
+    for (int c = 0; c < 3; c++) {
+        ep[c] = e[c] * tem;
+        ut[c] = u[c] + ep[c];
+    }
+    const R u2 = (ut[0] * ut[0] + ut[1] * ut[1]) + ut[2] * ut[2];
+    const R gam = SQRT(u2 + K(1.0));
+    const double ene = (double)(q * u2) / ((double)gam + 1.0);
+    const R gt = tem / gam;
+    for (int c = 0; c < 3; c++) bp[c] = b[c] * gt;
+    pn[0] = ut[0] + ut[1] * bp[2];
+    pn[1] = ut[1] + ut[2] * bp[0];
+    pn[2] = ut[2] + ut[0] * bp[1];
+    pn[0] = pn[0] - ut[2] * bp[1];
+    pn[1] = pn[1] - ut[0] * bp[2];
+    pn[2] = pn[2] - ut[1] * bp[0];
+    const R otsq = K(2.0) / (((K(1.0) + bp[0] * bp[0]) + bp[1] * bp[1]) + bp[2] * bp[2]);
+    for (int c = 0; c < 3; c++) bp[c] = bp[c] * otsq;
+    ut[0] = ut[0] + pn[1] * bp[2];
+    ut[1] = ut[1] + pn[2] * bp[0];
+    ut[2] = ut[2] + pn[0] * bp[1];
+    ut[0] = ut[0] - pn[2] * bp[1];
+    ut[1] = ut[1] - pn[0] * bp[2];
+    ut[2] = ut[2] - pn[1] * bp[0];
+    for (int c = 0; c < 3; c++) u[c] = ut[c] + ep[c];
+    return ene;
+}
+
 /* Higuera-Cary pusher (dudt_cary, source/spec/os-spec-push.f03:1104-1253): tem =
  * real(0.5 (dt / rqm)) (:1132); returns the energy term q u2 / (sqrt(gamma_minus^2) + 1)
  * accumulated in double (:1150-1153). */
@@ -291,7 +330,8 @@ static double EXN(ora_euler_u)(R tem, R rqm, double dt, const R *e, const R *b, 
 
 /* Momentum update of n particles in given (unscaled) fields e(3,n), b(3,n) by pusher 1 (exact:
  * fields times qm = 1/rqm as dudt_exact, :76-86, energy q (gamma - 1) of the new momenta),
- * 2 (Vay), 3 (Higuera-Cary), 4 (full rotation) or 5 (Euler rotation) with their own tem and
+ * 2 (Vay), 3 (Higuera-Cary), 4 (full rotation), 5 (Euler rotation) or 6 (conditional Vay)
+ * with their own tem and
  * energy terms; *ene += the double sum. */
 void EXN(ora_dudt_pusher)(int pusher, int n, const R *e, const R *b, R *u, const R *q, R rqm,
                           double dt, double tol, double *ene)
@@ -312,6 +352,11 @@ void EXN(ora_dudt_pusher)(int pusher, int n, const R *e, const R *b, R *u, const
         if (pusher == 4) {
             loc += EXN(ora_fullrot_u)((R)(0.5 * (dt / (double)rqm)), e + 3 * i, b + 3 * i,
                                       u + 3 * i, q[i]);
+            continue;
+        }
+        if (pusher == 6) {
+            loc += EXN(ora_cond_vay_u)((R)(0.5 * dt / (double)rqm), e + 3 * i, b + 3 * i,
+                                       u + 3 * i, q[i]);
             continue;
         }
         if (pusher == 5) {

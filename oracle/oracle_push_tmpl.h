@@ -196,7 +196,8 @@ static inline void OFN(dudt)(R tem, R rqm, R e1, R e2, R e3, R b1, R b2, R b3,
         return;
     }
     if (EXN(ora_pusher) >= 2) {
-        /* Vay / Higuera-Cary / full and Euler rotation: their own tem from the double dt,
+        /* Vay / Higuera-Cary / full and Euler rotation / conditional Vay: their own tem from
+         * the double dt,
          * energy straight to *eacc */
         const double dt = EXN(ora_push_dt);
         const R e[3] = {e1, e2, e3}, b[3] = {b1, b2, b3};
@@ -207,6 +208,8 @@ static inline void OFN(dudt)(R tem, R rqm, R e1, R e2, R e3, R b1, R b2, R b3,
             *eacc += EXN(ora_hc_u)((R)(0.5 * (dt / (double)rqm)), e, b, uu, qp);
         else if (EXN(ora_pusher) == 4)
             *eacc += EXN(ora_fullrot_u)((R)(0.5 * (dt / (double)rqm)), e, b, uu, qp);
+        else if (EXN(ora_pusher) == 6)
+            *eacc += EXN(ora_cond_vay_u)((R)(0.5 * dt / (double)rqm), e, b, uu, qp);
         else
             *eacc += EXN(ora_euler_u)((R)(0.5 * (dt / (double)rqm)), rqm, dt, e, b, uu, qp);
         *u1 = uu[0]; *u2 = uu[1]; *u3 = uu[2];

@@ -25,7 +25,8 @@ REFERENCE_SRC = "/root/reference"
 
 # guard cells required by each interpolation order (source/particles/os-particles.f03:321-360)
 GUARD = {1: (1, 2), 2: (2, 3), 3: (3, 4), 4: (4, 5)}
-PUSHERS = {"boris": 0, "exact": 1, "vay": 2, "hc": 3, "fullrot": 4, "euler": 5}
+PUSHERS = {"boris": 0, "exact": 1, "vay": 2, "hc": 3, "fullrot": 4, "euler": 5,
+           "cond_vay": 6}
 
 _lib = None
 _ref = {}

@@ -36,6 +36,7 @@ PUSHER_VAY = 2
 PUSHER_HC = 3
 PUSHER_FULLROT = 4
 PUSHER_EULER = 5
+PUSHER_COND_VAY = 6
 SMOOTH_NONE, SMOOTH_BINOMIAL, SMOOTH_COMPENSATED = 0, 2, 3
 SMOOTH_5PASS, SMOOTH_TRI6, SMOOTH_TRI8 = 4, 5, 6
 RNG_BYTES = 2512
@@ -205,9 +206,10 @@ def vadvance_deposit(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_s
     returns the time-centred energy sum the reference adds into ``*ene``.  With
     ``pusher=PUSHER_EXACT`` the momentum update is the exact pusher (push_type = "exact",
     osg_advance_deposit_exact_*) and the energy is sum q (gamma - 1) of the new momenta;
-    ``PUSHER_VAY`` / ``PUSHER_HC`` / ``PUSHER_FULLROT`` / ``PUSHER_EULER`` select the Vay,
-    Higuera-Cary, full-rotation and Euler-rotation updates (push_type "vay", "cary", "fullrot",
-    "euler"; osg_advance_deposit_*) with the energy those reference pushers report."""
+    ``PUSHER_VAY`` / ``PUSHER_HC`` / ``PUSHER_FULLROT`` / ``PUSHER_EULER`` /
+    ``PUSHER_COND_VAY`` select the Vay, Higuera-Cary, full-rotation, Euler-rotation and
+    conditional Vay updates (push_type "vay", "cary", "fullrot", "euler", "cond_vay";
+    osg_advance_deposit_*) with the energy those reference pushers report."""
     prec = _prec(x)
     dt_ = np.float32 if prec == "f32" else np.float64
     _need(ix, np.int32, "ix")

@@ -35,7 +35,7 @@ FAST_DIV = ["-prec-div=false", "-prec-sqrt=false"]
 EXTRA = {"tiled.cu": FAST_DIV, "batch_push.cu": FAST_DIV}
 
 SOURCES = ["push_plain.cu", "fields.cu", "tiled.cu", "tiled_exact.cu", "tiled_vay.cu", "tiled_hc.cu",
-           "tiled_fullrot.cu", "tiled_euler.cu",
+           "tiled_fullrot.cu", "tiled_euler.cu", "tiled_condvay.cu",
            "batch_push.cu", "batch.cu",
            "sim.cu", "capi.cu", "noalloc.cu",
            "loader.cpp", "laser.cpp"]

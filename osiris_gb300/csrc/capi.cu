@@ -102,7 +102,7 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
                      const int *j_size, const int *j_off, const double *dx, double dt,
                      double *ene, int pusher = OSG_PUSHER_BORIS, double iter_tol = 1.0e-3)
 {
-    OSG_CHECK(pusher >= OSG_PUSHER_BORIS && pusher <= OSG_PUSHER_EULER &&
+    OSG_CHECK(pusher >= OSG_PUSHER_BORIS && pusher <= OSG_PUSHER_COND_VAY &&
                   (pusher != OSG_PUSHER_EXACT || iter_tol > 0),
               OSG_ERR_ARG, "bad pusher / iteration tolerance");
     OSG_CHECK(dim >= 1 && dim <= 3 && order >= 1 && order <= 4, OSG_ERR_ARG,

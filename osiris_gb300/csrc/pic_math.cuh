@@ -554,6 +554,46 @@ __device__ __forceinline__ T vay_push(T tem, T e1, T e2, T e3, T b1, T b2, T b3,
     return (q * uc2) / (gc + T(1.0));
 }
 
+// Conditional Vay pusher (dudt_cond_vay, source/spec/os-spec-push.f03:800-1100): a particle
+// whose gamma of the old momentum exceeds 5 takes the Vay update (and its energy term), the
+// others the Fortran Boris update of the same routine -- half kick, rotation with
+// b tem / gamma and 2 / (1 + |b|^2), half kick -- with the energy q u^2 / (gamma + 1) of the
+// half-kicked momentum divided in double.  tem = real(0.5 dt / rqm) for both (:835).
+template <typename T>
+__device__ __forceinline__ double cond_vay_push(T tem, T e1, T e2, T e3, T b1, T b2, T b3, T q,
+                                                T &u1, T &u2, T &u3)
+{
+    const T g0 = sqrtR(((T(1.0) + u1 * u1) + u2 * u2) + u3 * u3);
+    if (g0 > T(5.0)) return (double)vay_push<T>(tem, e1, e2, e3, b1, b2, b3, q, u1, u2, u3);
+    const T ep[3] = {e1 * tem, e2 * tem, e3 * tem};
+    T ut[3] = {u1 + ep[0], u2 + ep[1], u3 + ep[2]};
+    const T usq = (ut[0] * ut[0] + ut[1] * ut[1]) + ut[2] * ut[2];
+    const T gam = sqrtR(usq + T(1.0));
+    const double ene = (double)(q * usq) / ((double)gam + 1.0);
+    const T gt = tem / gam;
+    T bp[3] = {b1 * gt, b2 * gt, b3 * gt};
+    T pn[3];
+    pn[0] = ut[0] + ut[1] * bp[2];
+    pn[1] = ut[1] + ut[2] * bp[0];
+    pn[2] = ut[2] + ut[0] * bp[1];
+    pn[0] = pn[0] - ut[2] * bp[1];
+    pn[1] = pn[1] - ut[0] * bp[2];
+    pn[2] = pn[2] - ut[1] * bp[0];
+    const T otsq = T(2.0) / (((T(1.0) + bp[0] * bp[0]) + bp[1] * bp[1]) + bp[2] * bp[2]);
+#pragma unroll
+    for (int c = 0; c < 3; c++) bp[c] = bp[c] * otsq;
+    ut[0] = ut[0] + pn[1] * bp[2];
+    ut[1] = ut[1] + pn[2] * bp[0];
+    ut[2] = ut[2] + pn[0] * bp[1];
+    ut[0] = ut[0] - pn[2] * bp[1];
+    ut[1] = ut[1] - pn[0] * bp[2];
+    ut[2] = ut[2] - pn[1] * bp[0];
+    u1 = ut[0] + ep[0];
+    u2 = ut[1] + ep[1];
+    u3 = ut[2] + ep[2];
+    return ene;
+}
+
 template <typename T>
 __device__ __forceinline__ double hc_push(T tem, T e1, T e2, T e3, T b1, T b2, T b3, T q, T &u1,
                                           T &u2, T &u3)

@@ -330,6 +330,8 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
             } else if (a.pusher == OSG_PUSHER_EULER) {
                 my_ene = euler_push<T>(a.tem, a.rqm, a.dt_full, E1, E2, E3, B1, B2, B3, q, u1,
                                        u2, u3);
+            } else if (a.pusher == OSG_PUSHER_COND_VAY) {
+                my_ene = cond_vay_push<T>(a.tem, E1, E2, E3, B1, B2, B3, q, u1, u2, u3);
             } else {
                 const T ene = boris(a.tem, E1, E2, E3, B1, B2, B3, u1, u2, u3);
                 my_ene = (double)q * (double)ene;

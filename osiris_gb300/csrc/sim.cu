@@ -462,7 +462,7 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
                            "along one axis)");
     OSG_CHECK(cfg->open_fields == 0 || (cfg->walls == 0 && cfg->smooth_type == OSG_SMOOTH_NONE),
               OSG_ERR_ARG, "open boundaries combine with neither walls nor smoothing");
-    OSG_CHECK(cfg->pusher >= OSG_PUSHER_BORIS && cfg->pusher <= OSG_PUSHER_EULER, OSG_ERR_ARG,
+    OSG_CHECK(cfg->pusher >= OSG_PUSHER_BORIS && cfg->pusher <= OSG_PUSHER_COND_VAY, OSG_ERR_ARG,
               "unknown pusher");
     OSG_CHECK(cfg->iter_tol >= 0, OSG_ERR_ARG, "iter_tol must be >= 0");
     double cour = 0.0;

@@ -152,6 +152,7 @@ static cudaError_t push_attr(int pusher, int dim, int order, int bytes)
     case OSG_PUSHER_HC: return push_tiled_attr_hc(dim, order, bytes);
     case OSG_PUSHER_FULLROT: return push_tiled_attr_fullrot(dim, order, bytes);
     case OSG_PUSHER_EULER: return push_tiled_attr_euler(dim, order, bytes);
+    case OSG_PUSHER_COND_VAY: return push_tiled_attr_cond_vay(dim, order, bytes);
     default: return push_tiled_attr_boris(dim, order, bytes);
     }
 }
@@ -645,6 +646,9 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     case OSG_PUSHER_HC: rc = push_tiled_launch_hc(t->dim, t->order, a, nt, t->threads, sm, st); break;
     case OSG_PUSHER_FULLROT: rc = push_tiled_launch_fullrot(t->dim, t->order, a, nt, t->threads, sm, st); break;
     case OSG_PUSHER_EULER: rc = push_tiled_launch_euler(t->dim, t->order, a, nt, t->threads, sm, st); break;
+    case OSG_PUSHER_COND_VAY:
+        rc = push_tiled_launch_cond_vay(t->dim, t->order, a, nt, t->threads, sm, st);
+        break;
     default: rc = push_tiled_launch_boris(t->dim, t->order, a, nt, t->threads, sm, st); break;
     }
     if (rc) return rc;

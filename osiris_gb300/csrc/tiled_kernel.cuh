@@ -379,6 +379,9 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 } else if constexpr (PUSHER == OSG_PUSHER_EULER) {
                     my_ene += (float)euler_push<float>(sd.tem, sd.rqm, a.dt_full, E1, E2, E3, B1,
                                                        B2, B3, q, un[0], un[1], un[2]);
+                } else if constexpr (PUSHER == OSG_PUSHER_COND_VAY) {
+                    my_ene += (float)cond_vay_push<float>(sd.tem, E1, E2, E3, B1, B2, B3, q,
+                                                          un[0], un[1], un[2]);
                 } else {
                     const float ene = boris(sd.tem, E1, E2, E3, B1, B2, B3, un[0], un[1], un[2]);
                     my_ene = fmaf(q, ene, my_ene);
@@ -880,6 +883,9 @@ cudaError_t push_tiled_attr_fullrot(int dim, int order, int bytes);
 int push_tiled_launch_euler(int dim, int order, const TiledArgs &a, unsigned ntiles, int threads,
                             size_t smem, cudaStream_t st);
 cudaError_t push_tiled_attr_euler(int dim, int order, int bytes);
+int push_tiled_launch_cond_vay(int dim, int order, const TiledArgs &a, unsigned ntiles,
+                               int threads, size_t smem, cudaStream_t st);
+cudaError_t push_tiled_attr_cond_vay(int dim, int order, int bytes);
 // persistent launch over a (box, tile) work list (k_push_tiled_batch, Boris pusher; defined
 // in batch_push.cu)
 int push_batch_launch(int dim, int order, const TiledArgs *boxes, const int2 *work, int nwork,

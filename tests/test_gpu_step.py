@@ -58,7 +58,8 @@ def _compare(osg, oracle, prec, engine, dim, order, nx, ppc, steps, tol, tile=No
                          pusher={"boris": osg.PUSHER_BORIS, "exact": osg.PUSHER_EXACT,
                                  "vay": osg.PUSHER_VAY, "hc": osg.PUSHER_HC,
                                  "fullrot": osg.PUSHER_FULLROT,
-                                 "euler": osg.PUSHER_EULER}[pusher])
+                                 "euler": osg.PUSHER_EULER,
+                                 "cond_vay": osg.PUSHER_COND_VAY}[pusher])
     sim.set_fields(e, b)
     for s in species:
         sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])

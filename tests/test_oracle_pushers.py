@@ -1,10 +1,12 @@
 """Known-answer tests of the oracle's Vay, Higuera-Cary, full-rotation and Euler-rotation
 momentum updates (dudt_vay, source/spec/os-spec-push.f03:636-796; dudt_cary, :1104-1253;
-dudt_fullrot, :83-231; dudt_euler, :235-352), restated from Fortran that cannot be run here:
+dudt_fullrot, :83-231; dudt_euler, :235-352; dudt_cond_vay, :800-1100), restated from Fortran
+that cannot be run here:
 all keep |u| in a pure magnetic field; Vay and Higuera-Cary keep a particle at the E x B drift
 velocity exactly for any step (their defining property); the two rotation pushers turn the
 momentum by the exact gyration angle in a uniform magnetic field (Boris does not); all agree
-with the exact pusher to O(dt^3) per step; the step-level push with them conserves charge."""
+with the exact pusher to O(dt^3) per step; the step-level push with them conserves charge; the
+conditional Vay pusher is the Vay update above gamma 5 and the Fortran Boris loops below."""
 import numpy as np
 import pytest
 
@@ -20,7 +22,7 @@ def _run(oracle, pusher, e, b, u0, dt, steps=1, prec="f64"):
     return u.astype(np.float64)
 
 
-@pytest.mark.parametrize("pusher", ["vay", "hc", "fullrot", "euler"])
+@pytest.mark.parametrize("pusher", ["vay", "hc", "fullrot", "euler", "cond_vay"])
 def test_pure_b_keeps_energy(oracle, pusher):
     rng = np.random.default_rng(1)
     u0 = rng.standard_normal((8, 3))
@@ -61,7 +63,7 @@ def test_rotation_pushers_gyrate_by_the_exact_angle(oracle, pusher):
     assert np.abs(u - boris).max() > 1e-3
 
 
-@pytest.mark.parametrize("pusher", ["vay", "hc", "fullrot", "euler"])
+@pytest.mark.parametrize("pusher", ["vay", "hc", "fullrot", "euler", "cond_vay"])
 def test_second_order_against_exact(oracle, pusher):
     rng = np.random.default_rng(4)
     e = rng.standard_normal((6, 3)) * 0.5
@@ -76,7 +78,7 @@ def test_second_order_against_exact(oracle, pusher):
     assert errs[0] < 1e-4
 
 
-@pytest.mark.parametrize("pusher", ["vay", "hc", "fullrot", "euler"])
+@pytest.mark.parametrize("pusher", ["vay", "hc", "fullrot", "euler", "cond_vay"])
 def test_push_with_pusher_conserves_charge(oracle, pusher):
     dim, order, nx = 2, 2, [8, 7]
     g = oracle.Grid(nx, order, [0.1] * dim)
@@ -99,3 +101,49 @@ def test_push_with_pusher_conserves_charge(oracle, pusher):
     oracle.periodic(g, "f64", rho1, 1)
     drho = (g.interior(rho1)[..., 0] - g.interior(rho0)[..., 0]) / dt
     assert np.abs(drho + oracle.div(g, "f64", j)).max() / np.abs(drho).max() < 1e-12
+
+
+def _fortran_boris(e, b, u, q, tem):
+    """The Boris loops of dudt_cond_vay (source/spec/os-spec-push.f03:1011-1094) in FP64, term
+    by term as the Fortran evaluates them."""
+    ep = e * tem
+    ut = u + ep
+    u2 = (ut[:, 0] ** 2 + ut[:, 1] ** 2) + ut[:, 2] ** 2
+    gam = np.sqrt(u2 + 1)
+    ene = (q * u2 / (gam + 1.0)).sum()
+    bp = b * (tem / gam)[:, None]
+    pn = np.empty_like(ut)
+    pn[:, 0] = ut[:, 0] + ut[:, 1] * bp[:, 2]
+    pn[:, 1] = ut[:, 1] + ut[:, 2] * bp[:, 0]
+    pn[:, 2] = ut[:, 2] + ut[:, 0] * bp[:, 1]
+    pn[:, 0] = pn[:, 0] - ut[:, 2] * bp[:, 1]
+    pn[:, 1] = pn[:, 1] - ut[:, 0] * bp[:, 2]
+    pn[:, 2] = pn[:, 2] - ut[:, 1] * bp[:, 0]
+    otsq = 2.0 / (((1.0 + bp[:, 0] ** 2) + bp[:, 1] ** 2) + bp[:, 2] ** 2)
+    bp = bp * otsq[:, None]
+    ut[:, 0] = ut[:, 0] + pn[:, 1] * bp[:, 2]
+    ut[:, 1] = ut[:, 1] + pn[:, 2] * bp[:, 0]
+    ut[:, 2] = ut[:, 2] + pn[:, 0] * bp[:, 1]
+    ut[:, 0] = ut[:, 0] - pn[:, 2] * bp[:, 1]
+    ut[:, 1] = ut[:, 1] - pn[:, 0] * bp[:, 2]
+    ut[:, 2] = ut[:, 2] - pn[:, 1] * bp[:, 0]
+    return ut + ep, ene
+
+
+def test_cond_vay_switches_at_gamma_5(oracle):
+    rng = np.random.default_rng(8)
+    n = 64
+    u0 = rng.standard_normal((n, 3)) * 3.0
+    e = rng.standard_normal((n, 3)) * 0.5
+    b = rng.standard_normal((n, 3)) * 0.5
+    dt = 0.3
+    g0 = np.sqrt(((1.0 + u0[:, 0] ** 2) + u0[:, 1] ** 2) + u0[:, 2] ** 2)
+    hot = g0 > 5
+    assert 0 < hot.sum() < n
+    uc = _run(oracle, "cond_vay", e, b, u0, dt)
+    uv = _run(oracle, "vay", e, b, u0, dt)
+    assert np.array_equal(uc[hot], uv[hot])
+    tem = 0.5 * dt / -1.0
+    ub, _ = _fortran_boris(e[~hot], b[~hot], u0[~hot].copy(), -np.ones((~hot).sum()), tem)
+    assert np.array_equal(uc[~hot], ub)
+    assert np.abs(uc[~hot] - uv[~hot]).max() > 1e-6
