@@ -402,30 +402,35 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
             int cw[3] = {1, 1, 1};
             if (has) {
                 long dt = 0, mul = 1;
+                int cn[3];
 #pragma unroll
                 for (int d = 0; d < DIM; d++) {
                     xo[d] = x1[d] - float(di[d]);
-                    const int cn = c[d] + di[d];
-                    if ((a.walls >> d) & 1) {
-                        // conducting wall: specular reflection after the deposit of the
-                        // unreflected path (p_bc_specular, source/spec/os-spec-boundary.f03:
-                        // 1293-1310)
-                        cw[d] = cn < 1 ? 1 : (cn > a.nx[d] ? a.nx[d] : cn);
-                        if (cw[d] != cn) {
-                            xo[d] = -xo[d];
-                            un[d] = -un[d];
+                    cn[d] = c[d] + di[d];
+                    cw[d] = wrapc(cn[d], a.nx[d]);
+                }
+                // non-periodic axes (a launch-uniform test, so the periodic box pays one branch)
+                bool gone = false;
+                if (a.walls | a.open) {
+#pragma unroll
+                    for (int d = 0; d < DIM; d++) {
+                        if ((a.walls >> d) & 1) {
+                            // conducting wall: specular reflection after the deposit of the
+                            // unreflected path (p_bc_specular,
+                            // source/spec/os-spec-boundary.f03:1293-1310)
+                            cw[d] = cn[d] < 1 ? 1 : (cn[d] > a.nx[d] ? a.nx[d] : cn[d]);
+                            if (cw[d] != cn[d]) {
+                                xo[d] = -xo[d];
+                                un[d] = -un[d];
+                            }
+                        } else if ((a.open >> d) & 1) {
+                            // open axis: a particle outside [1, nx] has left the box or the
+                            // window; its current of this step is already in the segments
+                            cw[d] = cn[d] - (d == 0 ? a.shift_x : 0);
+                            gone = gone || cw[d] < 1 || cw[d] > a.nx[d];
                         }
-                    } else {
-                        cw[d] = ((a.open >> d) & 1) ? cn - (d == 0 ? a.shift_x : 0)
-                                                    : wrapc(cn, a.nx[d]);
                     }
                 }
-                // (open axis: a particle outside [1, nx] has left the box or the window; its
-                //  current of this step is already in the segments)
-                bool gone = false;
-#pragma unroll
-                for (int d = 0; d < DIM; d++)
-                    gone = gone || (((a.open >> d) & 1) && (cw[d] < 1 || cw[d] > a.nx[d]));
                 if (gone) {
                     *rec_ix0<DIM>(rin, p) = 0;
                     has = false;
