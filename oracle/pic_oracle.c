@@ -196,6 +196,129 @@ int ora_push_f64(int dim, int order, int *ix, double *x, double *u, double *q, i
     return 0;
 }
 
+/* Philox4x32-10 (Salmon, Moraes, Dror and Shaw, "Parallel random numbers: as easy as 1, 2, 3",
+ * SC11): the counter-based stream the thermal-bath re-emission below draws from. */
+static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+    for (int r = 0; r < 10; r++) {
+        const uint64_t m0 = (uint64_t)0xD2511F53u * c[0], m1 = (uint64_t)0xCD9E8D57u * c[2];
+        const uint32_t hi0 = (uint32_t)(m0 >> 32), lo0 = (uint32_t)m0;
+        const uint32_t hi1 = (uint32_t)(m1 >> 32), lo1 = (uint32_t)m1;
+        const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+/* Thermal-bath particle boundary (p_bc_thermal, source/spec/os-spec-boundary.f03:1315-1387,
+ * thermal_bath :972-1067 with thermal_type "thermal") on the axes in `mask`, run on the pushed
+ * particles 1..np before any wrap: a particle outside [1, nx_d] is moved to the edge cell, takes
+ * uth_c times a Gaussian for the two other momentum components and uth_d times the
+ * half-Maxwellian sqrt(-2 ln v) into the box for the normal one, then the fluid momentum ufl
+ * (added relativistically only when all three components are non-zero, :1048-1063); its offset
+ * becomes xpos + u_d / gamma dt/dx_d delta (xpos = -1/2 below, the value just under 1/2
+ * above); and -q is deposited from the new position back along -u / gamma dt/dx (rev_current
+ * :1392-1440; in 2D the out-of-plane velocity keeps its sign), here as a Boris push of a
+ * virtual particle with momentum (-u1, -u2, u3) (2D) or -u (3D) through zero fields.  Axes in
+ * order.  The random numbers: one Philox4x32-10 call per re-emission, counter (p, p >> 32,
+ * step, d + 4 side code), key (seed, species); two Box-Muller Gaussians, the half-Maxwellian
+ * and delta from (r + 1/2) / 2^32 in double. */
+#define THERMAL_BODY(R, SFXN)                                                                 \
+    if (!mask || np <= 0) return;                                                            \
+    int gsz = 3;                                                                              \
+    for (int d = 0; d < dim; d++) gsz *= emf_size[d];                                        \
+    R *zero = (R *)calloc((size_t)gsz, sizeof(R));                                            \
+    const int saved = ora_pusher_##SFXN;                                                      \
+    ora_pusher_##SFXN = 0;                                                                    \
+    for (long p = 0; p < np; p++)                                                             \
+        for (int d = 0; d < dim; d++) {                                                       \
+            if (!((mask >> d) & 1)) continue;                                                 \
+            int *c = &ix[dim * p + d];                                                        \
+            if (*c >= 1 && *c <= nx[d]) continue;                                             \
+            const int lower = *c < 1, code = lower ? 1 : 2;                                   \
+            *c = lower ? 1 : nx[d];                                                           \
+            uint32_t r[4] = {(uint32_t)p, (uint32_t)((uint64_t)p >> 32), (uint32_t)step,      \
+                             (uint32_t)(d + 4 * code)};                                       \
+            philox4x32_10(r, seed, (uint32_t)species);                                        \
+            const double inv32 = 2.3283064365386963e-10;                                      \
+            const double v0 = (r[0] + 0.5) * inv32, v1 = (r[1] + 0.5) * inv32;               \
+            const double v2 = (r[2] + 0.5) * inv32, v3 = (r[3] + 0.5) * inv32;               \
+            const double rad = sqrt(-2.0 * log(v0)), th = 6.283185307179586 * v1;             \
+            const double gs[2] = {rad * cos(th), rad * sin(th)};                              \
+            R un[3];                                                                          \
+            for (int cc = 0, k = 0; cc < 3; cc++)                                             \
+                if (cc != d) un[cc] = (R)uth[cc] * (R)gs[k++];                                \
+            un[d] = (lower ? (R)1 : (R)-1) * (R)uth[d] * (R)sqrt(-2.0 * log(v2));             \
+            const R f1 = (R)ufl[0], f2 = (R)ufl[1], f3 = (R)ufl[2];                           \
+            if (f1 != 0 && f2 != 0 && f3 != 0) {                                              \
+                const R fa = (R)1 / ((R)1 + (R)sqrt((R)1 + f1 * f1 + f2 * f2 + f3 * f3));     \
+                const R gth = (R)sqrt((R)1 + un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);  \
+                const R fb = gth + fa * (f1 * un[0] + f2 * un[1] + f3 * un[2]);               \
+                un[0] = un[0] + fb * f1;                                                      \
+                un[1] = un[1] + fb * f2;                                                      \
+                un[2] = un[2] + fb * f3;                                                      \
+            }                                                                                 \
+            for (int cc = 0; cc < 3; cc++) u[3 * p + cc] = un[cc];                            \
+            const R rg = (R)1 / (R)sqrt((R)1 + un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);\
+            const R dtdx = (R)(dt / dx[d]);                                                   \
+            const R xpos = lower ? (R)-0.5 : (sizeof(R) == 4 ? (R)0.49999997f                 \
+                                                             : (R)0.49999999999999994);       \
+            x[dim * p + d] = xpos + (rg * un[d] * dtdx) * (R)v3;                              \
+            int vix[3];                                                                       \
+            R vx[3], vu[3], vq = -q[p];                                                       \
+            for (int k = 0; k < dim; k++) {                                                   \
+                vix[k] = ix[dim * p + k];                                                     \
+                vx[k] = x[dim * p + k];                                                       \
+            }                                                                                 \
+            vu[0] = -un[0];                                                                   \
+            vu[1] = -un[1];                                                                   \
+            vu[2] = dim == 3 ? -un[2] : un[2];                                                \
+            double ev = 0.0;                                                                  \
+            ora_push_##SFXN(dim, order, vix, vx, vu, &vq, 1, 1, rqm, zero, zero, emf_size,    \
+                            emf_off, j, emf_size, emf_off, (double *)dx, dt, &ev);            \
+        }                                                                                     \
+    ora_pusher_##SFXN = saved;                                                                \
+    free(zero);
+
+void ora_particle_thermal_f32(int dim, int order, const int *nx, int np, int *ix, float *x,
+                              float *u, float *q, float rqm, int *emf_size, int *emf_off,
+                              float *j, const double *dx, double dt, int mask,
+                              const double *uth, const double *ufl, uint32_t seed, int species,
+                              uint64_t step)
+{
+    THERMAL_BODY(float, f32)
+}
+
+void ora_particle_thermal_f64(int dim, int order, const int *nx, int np, int *ix, double *x,
+                              double *u, double *q, double rqm, int *emf_size, int *emf_off,
+                              double *j, const double *dx, double dt, int mask,
+                              const double *uth, const double *ufl, uint32_t seed, int species,
+                              uint64_t step)
+{
+    THERMAL_BODY(double, f64)
+}
+
+/* thermal-bath parameters of the step functions below (mask 0: none) */
+static int step_thermal = 0;
+static uint32_t step_seed = 0;
+static uint64_t step_count = 0;
+static double step_uth[3], step_ufl[3];
+void ora_set_thermal(int mask, const double *uth, const double *ufl, uint32_t seed,
+                     uint64_t step)
+{
+    step_thermal = mask;
+    step_seed = seed;
+    step_count = step;
+    for (int c = 0; c < 3; c++) {
+        step_uth[c] = uth ? uth[c] : 0.0;
+        step_ufl[c] = ufl ? ufl[c] : 0.0;
+    }
+}
+
 /* push with another momentum update (pusher 1 exact, 2 Vay, 3 Higuera-Cary, 4 full rotation,
  * 5 Euler rotation; the Fortran advance_deposit path): momentum with the double step dt (and
  * tolerance tol, exact pusher), position and deposit as the push above with dt */
@@ -501,6 +624,9 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
         ene[s] = 0.0;                                                                         \
         for (int t = 0; t < nt; t++) ene[s] += et[t];                                         \
         free(et);                                                                             \
+        ora_particle_thermal_##SFXN(dim, order, nx, np[s], ix[s], x[s], u[s], q[s], rqm[s],   \
+                                    emf_size, emf_off, j, dx, dtp, step_thermal, step_uth,    \
+                                    step_ufl, step_seed, s, step_count);                      \
         if (oax >= 0)                                                                         \
             ora_particle_absorb_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], q[s], oax);         \
         ora_particle_bound_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], walls);                  \

@@ -87,6 +87,7 @@ def _declare(L):
         getattr(L, f"ora_walls_{s_}").argtypes = [I, P, P, P, P, I, I, I]
         getattr(L, f"ora_set_walls_{s_}").argtypes = [I]
         getattr(L, f"ora_set_open_{s_}").argtypes = [I, P]
+    L.ora_set_thermal.argtypes = [I, P, P, C.c_uint32, C.c_uint64]
     L.ora_push_pusher_f32.argtypes = [I, I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P,
                                       P, D, D, P]
     L.ora_push_pusher_f64.argtypes = [I, I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, D,
@@ -327,11 +328,13 @@ def lindman_state(g: "Grid", prec, axis):
 
 
 def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="boris",
-         iter_tol=1e-3, smooth=None, walls=0, open_fields=None):
+         iter_tol=1e-3, smooth=None, walls=0, open_fields=None, thermal=None):
     """One full time step; species = list of dicts with ix, x, u, q, rqm.  walls (bit d):
     axis d bounded by conducting walls instead of periodic.  open_fields = (axis, state from
     lindman_state): Lindman open boundaries at both edges of that axis, particles absorbed
-    there (left in the arrays with charge and momentum 0).
+    there (left in the arrays with charge and momentum 0).  thermal = dict(mask, uth, ufl, seed,
+    step): particles crossing the edges of the axes in mask (walled or open) are re-emitted from
+    a thermal bath; step keys the random stream.
     Returns the per-species energy sums (Boris: time-centred u^2/(gamma+1); exact pusher:
     gamma - 1 of the new momentum; both times q).  fast=True runs the -O3 -ffast-math build
     (timing only)."""
@@ -354,6 +357,10 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     getattr(L, f"ora_set_walls_{prec}")(int(walls))
     if open_fields is not None:
         getattr(L, f"ora_set_open_{prec}")(int(open_fields[0]), _p(open_fields[1]))
+    if thermal is not None:
+        L.ora_set_thermal(int(thermal["mask"]), _p(_f64(thermal["uth"])),
+                          _p(_f64(thermal.get("ufl", [0.0] * 3))), int(thermal.get("seed", 0)),
+                          int(thermal["step"]))
     try:
         if pusher != "boris":
             getattr(L, f"ora_step_pusher_{prec}")(PUSHERS[pusher], *args, float(iter_tol))
@@ -362,6 +369,7 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     finally:
         getattr(L, f"ora_set_walls_{prec}")(0)
         getattr(L, f"ora_set_open_{prec}")(-1, None)
+        L.ora_set_thermal(0, None, None, 0, 0)
     if smooth is not None:
         getattr(L, f"ora_set_smooth_{prec}")(None, None)
     return ene

@@ -74,7 +74,8 @@ class Config(C.Structure):
                 ("dx", D * 3), ("dt", D), ("tile", I * 3), ("n_sort", I), ("capacity", D),
                 ("pusher", I), ("iter_tol", D), ("smooth_type", I), ("smooth_order", I),
                 ("walls", I),
-                ("open_fields", I)]
+                ("open_fields", I),
+                ("thermal", I), ("seed", C.c_uint), ("uth_bnd", D * 3), ("ufl_bnd", D * 3)]
 
 
 def _declare(lb):
@@ -376,7 +377,8 @@ class Simulation:
 
     def __init__(self, nx, dx, dt, order=2, precision=32, engine=ENGINE_TILED, tile=None,
                  n_sort=0, capacity=0.0, pusher=PUSHER_BORIS, iter_tol=0.0,
-                 smooth_type=SMOOTH_NONE, smooth_order=0, walls=0, open_fields=0):
+                 smooth_type=SMOOTH_NONE, smooth_order=0, walls=0, open_fields=0, thermal=0,
+                 uth_bnd=(0.0, 0.0, 0.0), ufl_bnd=(0.0, 0.0, 0.0), seed=0):
         self.dim = len(nx)
         self.nx = list(nx)
         self.order = order
@@ -400,6 +402,11 @@ class Simulation:
         cfg.smooth_order = smooth_order
         cfg.walls = walls
         cfg.open_fields = open_fields
+        cfg.thermal = thermal
+        cfg.seed = seed
+        for c in range(3):
+            cfg.uth_bnd[c] = uth_bnd[c]
+            cfg.ufl_bnd[c] = ufl_bnd[c]
         self.cfg = cfg
         self.dx = list(dx)
         self.dt = dt

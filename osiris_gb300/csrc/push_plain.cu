@@ -160,11 +160,18 @@ __device__ __forceinline__ int wrap_cell(int c, int n)
 // was deposited along the unreflected path; or absorption at an open edge (p_bc_absorbing,
 // :501-511: the reference removes the particle after its deposit; here it stays in the
 // arrays with charge and momentum 0 at offset 0 of the edge cell, and deposits nothing more).
+// A crossing of a thermal-bath edge returns 1 (lower) or 2 (upper) and leaves the cell outside
+// the box; thermal_reemit then moves the particle to the edge cell and sets its momentum and
+// offset (axis by axis, as the reference's boundary loop, which meets a particle crossing two
+// edges with the second axis not yet processed).
 template <typename T, int DIM>
-__device__ __forceinline__ void store_position(const PlainPushArgs<T> &a, long p, int d, int cn,
-                                               T xn)
+__device__ __forceinline__ int store_position(const PlainPushArgs<T> &a, long p, int d, int cn,
+                                              T xn)
 {
-    if (a.absorb[d] > 0 && (cn < 1 || cn > a.absorb[d])) {
+    int code = 0;
+    if (a.thermal[d] > 0 && (cn < 1 || cn > a.thermal[d])) {
+        code = cn < 1 ? 1 : 2;
+    } else if (a.absorb[d] > 0 && (cn < 1 || cn > a.absorb[d])) {
         cn = cn < 1 ? 1 : a.absorb[d];
         xn = T(0);
         a.u[3 * p + 0] = T(0);
@@ -180,6 +187,100 @@ __device__ __forceinline__ void store_position(const PlainPushArgs<T> &a, long p
     }
     a.x[DIM * p + d] = xn;
     a.ix[DIM * p + d] = cn;
+    return code << (2 * d);
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror and Shaw, "Parallel random numbers: as easy as 1, 2, 3",
+// SC11): ten rounds of two 32x32 -> 64-bit multiplies, the key bumped by the Weyl constants
+// between rounds.  A counter-based stream: every re-emission draws from its own counter.
+__device__ __forceinline__ void philox4x32_10(unsigned int c[4], unsigned int k0, unsigned int k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const unsigned int lo0 = 0xD2511F53u * c[0], hi0 = __umulhi(0xD2511F53u, c[0]);
+        const unsigned int lo1 = 0xCD9E8D57u * c[2], hi1 = __umulhi(0xCD9E8D57u, c[2]);
+        const unsigned int n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+// Thermal-bath re-emission of particle p after it crossed the edges coded in tb (2 bits per
+// axis: 1 lower, 2 upper), axis by axis (p_bc_thermal, source/spec/os-spec-boundary.f03:
+// 1315-1387, with thermal_bath :972-1067, thermal_type "thermal"):
+//  * momentum: uth_c times a Gaussian for the two other components, uth_d times a
+//    half-Maxwellian sqrt(-2 ln v) pointing into the box for the normal one, then the fluid
+//    momentum ufl added relativistically when all three of its components are non-zero;
+//  * offset along d: xpos + vperp delta, xpos = -1/2 (lower) or the float just below 1/2
+//    (upper), vperp = u_d / gamma dt/dx_d, delta uniform in (0, 1);
+//  * current: -q moved from the new position back along -u / gamma dt/dx (rev_current :1392-
+//    1440; in 2D the out-of-plane current keeps +u3, as the reference's).
+// The random numbers come from one Philox4x32-10 call per re-emission, counter (p, step, d and
+// side), key (seed, species): two Box-Muller Gaussians, the half-Maxwellian and delta, each
+// from (r + 1/2) / 2^32 in double.  The reference draws from its one sequential generator in
+// the order the boundary routine meets the particles; the distributions are the same.
+template <typename T, int DIM, int ORD>
+__device__ __noinline__ void thermal_reemit(const PlainPushArgs<T> &a, long p, T q, int tb)
+{
+    const double inv32 = 2.3283064365386963e-10;   // 2^-32
+    for (int d = 0; d < DIM; d++) {
+        const int code = (tb >> (2 * d)) & 3;
+        if (!code) continue;
+        const bool lower = code == 1;
+        a.ix[DIM * p + d] = lower ? 1 : a.thermal[d];
+        unsigned int r[4] = {(unsigned int)p, (unsigned int)((unsigned long long)p >> 32),
+                             (unsigned int)*a.step, (unsigned int)(d + 4 * code)};
+        philox4x32_10(r, a.rng_key[0], a.rng_key[1]);
+        const double v0 = (r[0] + 0.5) * inv32, v1 = (r[1] + 0.5) * inv32;
+        const double v2 = (r[2] + 0.5) * inv32, v3 = (r[3] + 0.5) * inv32;
+        const double rad = sqrt(-2.0 * log(v0)), th = 6.283185307179586 * v1;
+        const double gs[2] = {rad * cos(th), rad * sin(th)};
+        T un[3];
+        for (int c = 0, k = 0; c < 3; c++)
+            if (c != d) un[c] = a.uth_bnd[c] * (T)gs[k++];
+        un[d] = (lower ? T(1) : T(-1)) * a.uth_bnd[d] * (T)sqrt(-2.0 * log(v2));
+        const T f1 = a.ufl_bnd[0], f2 = a.ufl_bnd[1], f3 = a.ufl_bnd[2];
+        if (f1 != T(0) && f2 != T(0) && f3 != T(0)) {
+            const T fa = T(1) / (T(1) + sqrt(T(1) + f1 * f1 + f2 * f2 + f3 * f3));
+            const T gth = sqrt(T(1) + un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);
+            const T fb = gth + fa * (f1 * un[0] + f2 * un[1] + f3 * un[2]);
+            un[0] = un[0] + fb * f1;
+            un[1] = un[1] + fb * f2;
+            un[2] = un[2] + fb * f3;
+        }
+        for (int c = 0; c < 3; c++) a.u[3 * p + c] = un[c];
+        const T rg = T(1) / sqrt(T(1) + un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);
+        const T xpos = lower ? T(-0.5) : (sizeof(T) == 4 ? T(0.49999997f) : T(0.49999999999999994));
+        const T vperp = rg * un[d] * a.dtdx[d];
+        a.x[DIM * p + d] = xpos + vperp * (T)v3;
+        // the current of the way in: -q from the new position back to where it came from
+        T xn[3], xv[3];
+        int cc[3];
+        for (int k = 0; k < DIM; k++) {
+            xn[k] = a.x[DIM * p + k];
+            cc[k] = a.ix[DIM * p + k];
+            xv[k] = xn[k] - un[k] * rg * a.dtdx[k];
+        }
+        if constexpr (DIM == 2) {
+            Seg2<T> s[3];
+            s[0].x0 = xn[0]; s[0].x1 = xv[0]; s[0].y0 = xn[1]; s[0].y1 = xv[1];
+            s[0].vz = un[2] * rg; s[0].i = cc[0]; s[0].j = cc[1];
+            const int ns = split2(s, trim(xv[0]), trim(xv[1]));
+            for (int t = 0; t < ns; t++)
+                deposit2<T, ORD>(a.j, a.j_Dy, a.jn[0], a.jn[1], -q, s[t]);
+        } else if constexpr (DIM == 3) {
+            Seg3<T> s[4];
+            s[0].x0 = xn[0]; s[0].x1 = xv[0]; s[0].y0 = xn[1]; s[0].y1 = xv[1];
+            s[0].z0 = xn[2]; s[0].z1 = xv[2]; s[0].i = cc[0]; s[0].j = cc[1]; s[0].k = cc[2];
+            const int ns = split3(s, trim(xv[0]), trim(xv[1]), trim(xv[2]));
+            for (int t = 0; t < ns; t++)
+                deposit3<T, ORD>(a.j, a.j_Dy, a.j_Dz, a.jn[0], a.jn[1], a.jn[2], -q, s[t]);
+        }
+    }
 }
 
 // FP32 2D orders whose per-warp value scratch (8 warps) fits 32 KB of static shared memory
@@ -358,8 +459,8 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
                 T x1 = fmaR(v1, a.dtdx[0], x0[0]);
                 T y1 = fmaR(v2, a.dtdx[1], x0[1]);
                 int dix = trim(x1), diy = trim(y1);
-                store_position<T, 2>(a, p, 0, c[0] + dix, x1 - T(dix));
-                store_position<T, 2>(a, p, 1, c[1] + diy, y1 - T(diy));
+                const int tb = store_position<T, 2>(a, p, 0, c[0] + dix, x1 - T(dix)) |
+                               store_position<T, 2>(a, p, 1, c[1] + diy, y1 - T(diy));
                 Seg2<T> s[3];
                 s[0].x0 = x0[0]; s[0].x1 = x1; s[0].y0 = x0[1]; s[0].y1 = y1;
                 s[0].vz = v3; s[0].i = c[0]; s[0].j = c[1];
@@ -373,20 +474,22 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
                     for (int t = 0; t < ns; t++)
                         deposit2<T, ORD>(a.j, a.j_Dy, a.jn[0], a.jn[1], q, s[t]);
                 }
+                if (tb) thermal_reemit<T, 2, ORD>(a, p, q, tb);
             } else {
                 T x1 = fmaR(v1, a.dtdx[0], x0[0]);
                 T y1 = fmaR(v2, a.dtdx[1], x0[1]);
                 T z1 = fmaR(v3, a.dtdx[2], x0[2]);
                 int dix = trim(x1), diy = trim(y1), diz = trim(z1);
-                store_position<T, 3>(a, p, 0, c[0] + dix, x1 - T(dix));
-                store_position<T, 3>(a, p, 1, c[1] + diy, y1 - T(diy));
-                store_position<T, 3>(a, p, 2, c[2] + diz, z1 - T(diz));
+                const int tb = store_position<T, 3>(a, p, 0, c[0] + dix, x1 - T(dix)) |
+                               store_position<T, 3>(a, p, 1, c[1] + diy, y1 - T(diy)) |
+                               store_position<T, 3>(a, p, 2, c[2] + diz, z1 - T(diz));
                 Seg3<T> s[4];
                 s[0].x0 = x0[0]; s[0].x1 = x1; s[0].y0 = x0[1]; s[0].y1 = y1;
                 s[0].z0 = x0[2]; s[0].z1 = z1; s[0].i = c[0]; s[0].j = c[1]; s[0].k = c[2];
                 const int ns = split3(s, dix, diy, diz);
                 for (int t = 0; t < ns; t++)
                     deposit3<T, ORD>(a.j, a.j_Dy, a.j_Dz, a.jn[0], a.jn[1], a.jn[2], q, s[t]);
+                if (tb) thermal_reemit<T, 3, ORD>(a, p, q, tb);
             }
         }
     }
@@ -436,6 +539,12 @@ PlainPushArgs<T> make_plain_args(int dim, int order, int *ix, T *x, T *u, const 
     a.reflect[0] = a.reflect[1] = a.reflect[2] = 0;
     a.absorb[0] = a.absorb[1] = a.absorb[2] = 0;
     a.q_absorb = nullptr;
+    for (int d = 0; d < 3; d++) {
+        a.thermal[d] = 0;
+        a.uth_bnd[d] = a.ufl_bnd[d] = T(0);
+    }
+    a.step = nullptr;
+    a.rng_key[0] = a.rng_key[1] = 0;
     a.pusher = OSG_PUSHER_BORIS;
     a.qm = T(1) / rqm;
     a.rqm = rqm;

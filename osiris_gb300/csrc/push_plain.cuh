@@ -31,6 +31,11 @@ template <typename T> struct PlainPushArgs {
     int absorb[3];         // > 0: open edges of [1, absorb[d]]: a particle that crossed one is
                            // absorbed (charge and momentum set to 0 in q_absorb and u)
     T *q_absorb;           // the charges, writable (only with an absorbing axis)
+    int thermal[3];        // > 0: thermal-bath edges of [1, thermal[d]]: a particle that crossed
+                           // one is re-emitted with new momenta (thermal_reemit)
+    T uth_bnd[3], ufl_bnd[3];   // the bath's thermal and fluid momenta
+    const unsigned long long *step;   // device step counter (re-emission random stream)
+    unsigned int rng_key[2];          // the stream's key: seed, species
     int pusher;            // OSG_PUSHER_*
     T qm;                  // 1 / rqm (exact pusher)
     T rqm;                 // the species' rqm (Euler-rotation pusher)

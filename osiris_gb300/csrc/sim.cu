@@ -61,6 +61,7 @@ struct osg_sim {
     double xmoved = 0.0;         // window motion not yet turned into a cell move
     long moves = 0;              // cell moves so far
     void *shift_tmp = nullptr;   // scratch field array for the shift and the smoothing
+    unsigned long long *d_step = nullptr;   // step counter of the thermal-bath random stream
     int open_axis = -1;          // Lindman open boundaries at both edges of this axis
     void *lind = nullptr;        // their state (lindman_state_size reals)
     osg::SmoothSpec smooth;      // current smoothing (order 0 per axis: none)
@@ -231,6 +232,9 @@ struct PhaseEvents {
     cudaEvent_t ev[8];
 };
 
+// the thermal-bath random stream's step counter, advanced at the end of every step
+__global__ void k_step_tick(unsigned long long *step) { *step += 1; }
+
 // with_sort: plain engine, cell sort after the push; shift: tiled engine with a moving
 // window, the step ends with a one-cell window move (move_boundary_space_global,
 // source/os-space.f90:508-566: in the reference the move opens the next step, whose push then
@@ -290,6 +294,19 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
                 a.absorb[d] = d == oax ? c.nx[d] : 0;
             }
             a.q_absorb = (T *)p.q;
+            if (c.thermal) {
+                for (int d = 0; d < c.dim; d++) {
+                    a.thermal[d] = (c.thermal >> d) & 1 ? c.nx[d] : 0;
+                    if (a.thermal[d]) a.absorb[d] = a.reflect[d] = 0;
+                }
+                for (int d = 0; d < 3; d++) {
+                    a.uth_bnd[d] = (T)c.uth_bnd[d];
+                    a.ufl_bnd[d] = (T)c.ufl_bnd[d];
+                }
+                a.step = s->d_step;
+                a.rng_key[0] = c.seed;
+                a.rng_key[1] = (unsigned int)k;
+            }
             a.pusher = c.pusher;
             a.iter_tol = c.iter_tol;
             if (c.pusher >= OSG_PUSHER_VAY)
@@ -331,6 +348,10 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
         launches += 2;
         int rc = tiled_window_inject(s->tiled, parity, s->d_status, st, &launches);
         if (rc) return rc;
+    }
+    if (s->d_step) {
+        k_step_tick<<<1, 1, 0, st>>>(s->d_step);
+        launches++;
     }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[5], st));
     OSG_CUDA(cudaGetLastError());
@@ -462,6 +483,15 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
                            "along one axis)");
     OSG_CHECK(cfg->open_fields == 0 || (cfg->walls == 0 && cfg->smooth_type == OSG_SMOOTH_NONE),
               OSG_ERR_ARG, "open boundaries combine with neither walls nor smoothing");
+    OSG_CHECK(cfg->thermal >= 0 && (cfg->thermal & ~(cfg->walls | cfg->open_fields)) == 0,
+              OSG_ERR_ARG, "thermal: a bit mask of walled or open axes");
+    OSG_CHECK(cfg->thermal == 0 || cfg->engine == OSG_ENGINE_PLAIN, OSG_ERR_ARG,
+              "thermal-bath particle boundaries run on the plain engine");
+    if (cfg->thermal)
+        for (int d = 0; d < cfg->dim; d++)
+            OSG_CHECK(!((cfg->thermal >> d) & 1) || cfg->uth_bnd[d] > 0, OSG_ERR_ARG,
+                      "a thermal bath along axis %d needs uth_bnd[%d] > 0 (the reference's check)",
+                      d, d);
     OSG_CHECK(cfg->pusher >= OSG_PUSHER_BORIS && cfg->pusher <= OSG_PUSHER_COND_VAY, OSG_ERR_ARG,
               "unknown pusher");
     OSG_CHECK(cfg->iter_tol >= 0, OSG_ERR_ARG, "iter_tol must be >= 0");
@@ -517,6 +547,7 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
     s->d_diag = rc ? nullptr : dalloc<double>(16, &rc);
     if (!rc && s->smooth.order[0] > 0) s->shift_tmp = dalloc<char>(gbytes, &rc);
     size_t lbytes = 0;
+    if (!rc && cfg->thermal) s->d_step = dalloc<unsigned long long>(1, &rc);
     if (!rc && cfg->open_fields) {
         s->open_axis = __builtin_ctz(cfg->open_fields);
         lbytes = (size_t)s->esz * lindman_state_size(s->g, s->open_axis);
@@ -530,6 +561,7 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
     cudaMemsetAsync(s->b, 0, gbytes, s->st);
     cudaMemsetAsync(s->j, 0, gbytes, s->st);
     if (s->lind) cudaMemsetAsync(s->lind, 0, lbytes, s->st);
+    if (s->d_step) cudaMemsetAsync(s->d_step, 0, sizeof(unsigned long long), s->st);
     cudaMemsetAsync(s->d_status, 0, 4 * sizeof(int), s->st);
     cudaMemsetAsync(s->d_ene, 0, MAX_SPECIES * sizeof(double), s->st);
     if (cfg->engine == OSG_ENGINE_TILED) {
@@ -565,6 +597,7 @@ int osg_sim_destroy(osg_sim *s)
     cudaFree(s->j);
     cudaFree(s->shift_tmp);
     cudaFree(s->lind);
+    cudaFree(s->d_step);
     cudaFree(s->d_ene);
     cudaFree(s->d_status);
     cudaFree(s->d_diag);
@@ -907,6 +940,14 @@ int osg_sim_restore(const char *path, osg_sim **out)
         return rc;
     }
     s->step_n = step_n;
+    if (s->d_step) {
+        const unsigned long long v = (unsigned long long)step_n;
+        if (cudaMemcpy(s->d_step, &v, sizeof v, cudaMemcpyHostToDevice) != cudaSuccess) {
+            osg_sim_destroy(s);
+            set_error("upload of the step counter failed");
+            return OSG_ERR_CUDA;
+        }
+    }
     *out = s;
     return OSG_OK;
 }
