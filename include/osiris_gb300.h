@@ -188,7 +188,9 @@ int osg_periodic_f32(int dim, const int *nx, const int *gcl, const int *gcu, flo
  * its guard values into the image points inside the box (spec_bc_*d,
  * source/current/os-current-boundary.f03).  The image of a component is the point mirrored
  * about the wall, with sign + for normal E and tangential B, J and - for tangential E and
- * normal B, J. */
+ * normal B, J.  Kinds 3 (E) and 4 (B) are the walls of a perfect magnetic conductor
+ * (pmc_bc_e/b_*d_odd/even, source/emf/boundary/os-emf-pmc.f90): the same image points with
+ * the signs of E and B exchanged. */
 int osg_walls_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f, int kind,
                   int walls, int order);
 int osg_walls_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f, int kind,
@@ -285,6 +287,9 @@ typedef struct {
     unsigned int seed;      /* key of the re-emission random stream */
     double uth_bnd[3];      /* the bath's thermal momentum per component */
     double ufl_bnd[3];      /* its fluid momentum (added only when all three are non-zero) */
+    int pmc;          /* bit d set (d walled): the walls of axis d are perfect magnetic
+                         conductors (the reference's p_bc_pmc, "reflecting") instead of
+                         electric ones; the current and the particles are treated alike */
 } osg_config;
 
 int osg_sim_create(const osg_config *cfg, osg_sim **out);

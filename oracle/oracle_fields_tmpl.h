@@ -219,6 +219,10 @@ void FN(ora_walls)(int dim, const int *nx, const int *gcl, const int *gcu, R *f,
     FN(ora_grid) G, *g = &G;
     FN(grid_init)(g, dim, nx, gcl, gcu);
     const int odd = order & 1;
+    /* kinds 3 and 4: E and B of a perfect magnetic conductor (pmc_bc_e/b_*d_odd/even,
+     * source/emf/boundary/os-emf-pmc.f90), the same image points with the signs exchanged */
+    const int fk = kind >= 3 ? kind - 3 : kind;
+    const R flip = kind >= 3 ? K(-1.0) : K(1.0);
     for (int d = 0; d < dim; d++) {
         if (!(walls & (1 << d))) continue;
         const int n = g->nx[d];
@@ -239,21 +243,21 @@ void FN(ora_walls)(int dim, const int *nx, const int *gcl, const int *gcu, R *f,
                     for (int a1 = lo[0]; a1 <= hi[0]; a1++)
                         for (int c = 0; c < 3; c++) {
                             const int normal = c == d;
-                            const int stag = kind == 1 ? !normal : normal;
-                            const R sg = ((kind == 0) == normal) ? K(1.0) : K(-1.0);
+                            const int stag = fk == 1 ? !normal : normal;
+                            const R sg = (((fk == 0) == normal) ? K(1.0) : K(-1.0)) * flip;
                             int ic[3] = {a1, a2, a3};
                             for (int i = i0; i <= i1; i++) {
                                 ic[d] = i;
                                 const long pg = FN(gidx)(g, c, ic[0], ic[1], ic[2]);
                                 const int m = FN(wall_mirror)(i, n, lower, stag, odd);
                                 if (m == i) {
-                                    f[pg] = kind == 2 ? (sg > 0 ? K(2.0) * f[pg] : K(0.0))
+                                    f[pg] = fk == 2 ? (sg > 0 ? K(2.0) * f[pg] : K(0.0))
                                                       : (sg > 0 ? f[pg] : K(0.0));
                                     continue;
                                 }
                                 ic[d] = m;
                                 const long pm = FN(gidx)(g, c, ic[0], ic[1], ic[2]);
-                                if (kind == 2)
+                                if (fk == 2)
                                     f[pm] = f[pm] + sg * f[pg];
                                 else
                                     f[pg] = sg * f[pm];
@@ -264,7 +268,7 @@ void FN(ora_walls)(int dim, const int *nx, const int *gcl, const int *gcu, R *f,
                             if (iw != -1000000) {
                                 ic[d] = iw;
                                 const long pw = FN(gidx)(g, c, ic[0], ic[1], ic[2]);
-                                f[pw] = kind == 2 ? (sg > 0 ? K(2.0) * f[pw] : K(0.0))
+                                f[pw] = fk == 2 ? (sg > 0 ? K(2.0) * f[pw] : K(0.0))
                                                   : (sg > 0 ? f[pw] : K(0.0));
                             }
                         }
@@ -274,18 +278,32 @@ void FN(ora_walls)(int dim, const int *nx, const int *gcl, const int *gcu, R *f,
 
 /* the Yee advance bounded by conducting walls: the images after every partial step
  * (source/emf/solver/os-emf-solver-yee.f03:556-566) */
+/* E (kind 0) or B (1) images of every walled axis in order, the axes in pmc as perfect
+ * magnetic conductors */
+static void FN(walls_em)(int dim, const int *nx, const int *gcl, const int *gcu, R *f, int kind,
+                         int walls, int order, int pmc)
+{
+    for (int d = 0; d < dim; d++)
+        if (walls & (1 << d))
+            FN(ora_walls)(dim, nx, gcl, gcu, f, (pmc >> d) & 1 ? kind + 3 : kind, 1 << d, order);
+}
+
+static int FN(step_pmc) = 0;
+void FN(ora_set_pmc)(int pmc) { FN(step_pmc) = pmc; }
+
 void FN(ora_yee_advance_walls)(int dim, const int *nx, const int *gcl, const int *gcu, R *e,
                                R *b, const R *j, const double *dx, double dt, int walls,
                                int order)
 {
     FN(ora_grid) G, *g = &G;
     FN(grid_init)(g, dim, nx, gcl, gcu);
+    const int pmc = FN(step_pmc);
     FN(dbdt)(g, b, e, dx, dt / 2.0);
-    FN(ora_walls)(dim, nx, gcl, gcu, b, 1, walls, order);
+    FN(walls_em)(dim, nx, gcl, gcu, b, 1, walls, order, pmc);
     FN(dedt)(g, e, b, j, dx, dt);
-    FN(ora_walls)(dim, nx, gcl, gcu, e, 0, walls, order);
+    FN(walls_em)(dim, nx, gcl, gcu, e, 0, walls, order, pmc);
     FN(dbdt)(g, b, e, dx, dt / 2.0);
-    FN(ora_walls)(dim, nx, gcl, gcu, b, 1, walls, order);
+    FN(walls_em)(dim, nx, gcl, gcu, b, 1, walls, order, pmc);
 }
 
 /* Lindman open boundaries at both edges of axis d (p_bc_lindman; the reference admits them

@@ -55,6 +55,9 @@ void ora_walls_f32(int dim, const int *nx, const int *gcl, const int *gcu, float
 void ora_walls_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f, int kind,
                    int walls, int order);
 void ora_set_walls_f32(int walls);
+/* the walled axes in `pmc` are perfect magnetic conductors in the steps below */
+void ora_set_pmc_f32(int pmc);
+void ora_set_pmc_f64(int pmc);
 void ora_set_walls_f64(int walls);
 /* Lindman open boundaries at both edges of `axis` (-1: none) for the step functions below;
  * `state` holds 15 reals per interior point of the other axes, zeroed before the first step

@@ -86,6 +86,7 @@ def _declare(L):
         getattr(L, f"ora_set_smooth_{s_}").argtypes = [P, P]
         getattr(L, f"ora_walls_{s_}").argtypes = [I, P, P, P, P, I, I, I]
         getattr(L, f"ora_set_walls_{s_}").argtypes = [I]
+        getattr(L, f"ora_set_pmc_{s_}").argtypes = [I]
         getattr(L, f"ora_set_open_{s_}").argtypes = [I, P]
     L.ora_set_thermal.argtypes = [I, P, P, C.c_uint32, C.c_uint64]
     L.ora_push_pusher_f32.argtypes = [I, I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P,
@@ -311,7 +312,8 @@ def load(rng: MT, prec, dim, nx, ppc, dx, rqm, uth, ufl, amp=0.0, kmode=1.0):
 
 def walls(g: "Grid", prec, f, kind, mask):
     """Conducting-wall images on the axes in `mask` (bit d), in place: kind 0 E, 1 B (guard
-    points set from their images), 2 J (guard values added into the box)."""
+    points set from their images), 2 J (guard values added into the box); 3 E, 4 B of a perfect
+    magnetic conductor."""
     nx, gl, gu = g.args()
     getattr(lib(), f"ora_walls_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), _p(f), int(kind),
                                         int(mask), g.order)
@@ -328,13 +330,14 @@ def lindman_state(g: "Grid", prec, axis):
 
 
 def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="boris",
-         iter_tol=1e-3, smooth=None, walls=0, open_fields=None, thermal=None):
+         iter_tol=1e-3, smooth=None, walls=0, open_fields=None, thermal=None, pmc=0):
     """One full time step; species = list of dicts with ix, x, u, q, rqm.  walls (bit d):
     axis d bounded by conducting walls instead of periodic.  open_fields = (axis, state from
     lindman_state): Lindman open boundaries at both edges of that axis, particles absorbed
     there (left in the arrays with charge and momentum 0).  thermal = dict(mask, uth, ufl, seed,
     step): particles crossing the edges of the axes in mask (walled or open) are re-emitted from
-    a thermal bath; step keys the random stream.
+    a thermal bath; step keys the random stream.  pmc (bit d, d walled): perfect magnetic
+    instead of electric conductor walls.
     Returns the per-species energy sums (Boris: time-centred u^2/(gamma+1); exact pusher:
     gamma - 1 of the new momentum; both times q).  fast=True runs the -O3 -ffast-math build
     (timing only)."""
@@ -355,6 +358,7 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     args = (g.dim, g.order, _p(nx), _p(gl), _p(gu), _p(_f64(g.dx + [0.0] * 3)), float(dt), _p(e),
             _p(b), _p(j), ns, _p(np_), ixs, xs, us, qs, _p(rqm), _p(ene), int(nthreads))
     getattr(L, f"ora_set_walls_{prec}")(int(walls))
+    getattr(L, f"ora_set_pmc_{prec}")(int(pmc))
     if open_fields is not None:
         getattr(L, f"ora_set_open_{prec}")(int(open_fields[0]), _p(open_fields[1]))
     if thermal is not None:
@@ -368,6 +372,7 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
             getattr(L, f"ora_step_{prec}")(*args)
     finally:
         getattr(L, f"ora_set_walls_{prec}")(0)
+        getattr(L, f"ora_set_pmc_{prec}")(0)
         getattr(L, f"ora_set_open_{prec}")(-1, None)
         L.ora_set_thermal(0, None, None, 0, 0)
     if smooth is not None:

@@ -75,7 +75,8 @@ class Config(C.Structure):
                 ("pusher", I), ("iter_tol", D), ("smooth_type", I), ("smooth_order", I),
                 ("walls", I),
                 ("open_fields", I),
-                ("thermal", I), ("seed", C.c_uint), ("uth_bnd", D * 3), ("ufl_bnd", D * 3)]
+                ("thermal", I), ("seed", C.c_uint), ("uth_bnd", D * 3), ("ufl_bnd", D * 3),
+                ("pmc", I)]
 
 
 def _declare(lb):
@@ -264,8 +265,9 @@ def yee_advance(dim, nx, gcl, gcu, e, b, j, dx, dt):
 
 
 def walls(dim, nx, gcl, gcu, f, kind, mask, order):
-    """Conducting-wall images on a host grid (osg_walls_*): kind 0 E, 1 B, 2 J; mask bit d
-    walls axis d."""
+    """Conducting-wall images on a host grid (osg_walls_*): kind 0 E, 1 B, 2 J (perfect electric
+    conductor; the current's images serve both conductors), 3 E, 4 B (perfect magnetic
+    conductor); mask bit d walls axis d."""
     s = _prec(f)
     _check(getattr(lib(), f"osg_walls_{s}")(dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)),
                                             _p(f), int(kind), int(mask), int(order)))
@@ -378,7 +380,7 @@ class Simulation:
     def __init__(self, nx, dx, dt, order=2, precision=32, engine=ENGINE_TILED, tile=None,
                  n_sort=0, capacity=0.0, pusher=PUSHER_BORIS, iter_tol=0.0,
                  smooth_type=SMOOTH_NONE, smooth_order=0, walls=0, open_fields=0, thermal=0,
-                 uth_bnd=(0.0, 0.0, 0.0), ufl_bnd=(0.0, 0.0, 0.0), seed=0):
+                 uth_bnd=(0.0, 0.0, 0.0), ufl_bnd=(0.0, 0.0, 0.0), seed=0, pmc=0):
         self.dim = len(nx)
         self.nx = list(nx)
         self.order = order
@@ -403,6 +405,7 @@ class Simulation:
         cfg.walls = walls
         cfg.open_fields = open_fields
         cfg.thermal = thermal
+        cfg.pmc = pmc
         cfg.seed = seed
         for c in range(3):
             cfg.uth_bnd[c] = uth_bnd[c]

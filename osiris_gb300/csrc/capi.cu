@@ -274,7 +274,7 @@ template <typename T>
 static int walls_host(int dim, const int *nx, const int *gcl, const int *gcu, T *f, int kind,
                       int walls, int order)
 {
-    OSG_CHECK(dim >= 1 && dim <= 3 && nx && gcl && gcu && f && kind >= 0 && kind <= 2 &&
+    OSG_CHECK(dim >= 1 && dim <= 3 && nx && gcl && gcu && f && kind >= 0 && kind <= 4 &&
                   walls >= 0 && walls < (1 << dim) && order >= 1 && order <= 4,
               OSG_ERR_ARG, "bad arguments");
     for (int d = 0; d < dim; d++)

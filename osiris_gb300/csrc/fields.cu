@@ -158,10 +158,14 @@ __global__ void k_wall_dir(GridDesc g, int d, int side, int kind, int odd, T *__
         const bool lower = side == 0;
         const int nx = g.nx[d];
         const int i0 = lower ? 1 - g.gcl[d] : nx + 1, i1 = lower ? 0 : nx + g.gcu[d];
+        // kinds 3 and 4: E and B of a perfect magnetic conductor, the same mirror points with
+        // the signs of E and B exchanged (pmc_bc_e/b_*, source/emf/boundary/os-emf-pmc.f90)
+        const int fk = kind >= 3 ? kind - 3 : kind;
+        const T flip = kind >= 3 ? T(-1) : T(1);
         for (int c = 0; c < 3; c++) {
             const bool normal = c == d;
-            const bool stag = kind == 1 ? !normal : normal;
-            const T sg = (kind == 0) == normal ? T(1) : T(-1);
+            const bool stag = fk == 1 ? !normal : normal;
+            const T sg = ((fk == 0) == normal ? T(1) : T(-1)) * flip;
             // the wall point, when it is not a guard point (odd order, unstaggered, lower
             // wall: i = 1; even order, staggered, upper wall: i = nx)
             const int iw = lower ? (!stag && odd ? 1 : INT_MIN) : (stag && !odd ? nx : INT_MIN);
@@ -191,15 +195,17 @@ __global__ void k_wall_dir(GridDesc g, int d, int side, int kind, int odd, T *__
 }
 
 template <typename T>
-void wall_update(const GridDesc &g, T *f, int kind, int walls, int order, cudaStream_t st)
+void wall_update(const GridDesc &g, T *f, int kind, int walls, int order, cudaStream_t st,
+                 int pmc)
 {
     for (int d = 0; d < g.dim; d++) {
         if (!(walls & (1 << d))) continue;
         long nlines = 1;
         for (int a = 0; a < g.dim; a++)
             if (a != d) nlines *= g.size[a];
+        const int k = (kind < 2 && ((pmc >> d) & 1)) ? kind + 3 : kind;
         for (int side = 0; side < 2; side++)
-            k_wall_dir<T><<<blocks_for(nlines, 256), 256, 0, st>>>(g, d, side, kind, order & 1, f,
+            k_wall_dir<T><<<blocks_for(nlines, 256), 256, 0, st>>>(g, d, side, k, order & 1, f,
                                                                    nlines);
     }
 }
@@ -342,22 +348,22 @@ void open_guards(const GridDesc &g, T *e, T *b, int axis, const T *lind, cudaStr
 
 template <typename T>
 void yee_advance(const GridDesc &g, T *e, T *b, const T *j, const double *dx, double dt,
-                 cudaStream_t st, int walls, int order, int open_axis, T *lind)
+                 cudaStream_t st, int walls, int order, int open_axis, T *lind, int pmc)
 {
     const bool open = open_axis >= 0 && lind;
     LindAxes L{};
     if (open) L = lind_axes(g, open_axis);
     launch_dbdt(g, b, e, dx, dt / 2.0, st);
-    if (walls) wall_update(g, b, 1, walls, order, st);
+    if (walls) wall_update(g, b, 1, walls, order, st, pmc);
     if (open) launch_lindman_b(g, L, e, lind, dx, dt, st);
     launch_dedt(g, e, b, j, dx, dt, st);
-    if (walls) wall_update(g, e, 0, walls, order, st);
+    if (walls) wall_update(g, e, 0, walls, order, st, pmc);
     if (open) {
         const T k = (T)((1.0 - dt / dx[open_axis]) / (1.0 + dt / dx[open_axis]));
         k_lindman_e<T><<<blocks_for(L.nperp, 256), 256, 0, st>>>(g, L, e, lind, k);
     }
     launch_dbdt(g, b, e, dx, dt / 2.0, st);
-    if (walls) wall_update(g, b, 1, walls, order, st);
+    if (walls) wall_update(g, b, 1, walls, order, st, pmc);
     if (open) launch_lindman_b(g, L, e, lind, dx, dt, st);
 }
 
@@ -818,18 +824,19 @@ void smooth_field(const GridDesc &g, const SmoothSpec &sp, T *f, T *tmp, cudaStr
 }
 
 template void yee_advance<float>(const GridDesc &, float *, float *, const float *,
-                                 const double *, double, cudaStream_t, int, int, int, float *);
+                                 const double *, double, cudaStream_t, int, int, int, float *,
+                                 int);
 template void yee_advance<double>(const GridDesc &, double *, double *, const double *,
                                   const double *, double, cudaStream_t, int, int, int,
-                                  double *);
+                                  double *, int);
 template void open_guards<float>(const GridDesc &, float *, float *, int, const float *,
                                  cudaStream_t);
 template void open_guards<double>(const GridDesc &, double *, double *, int, const double *,
                                   cudaStream_t);
 template void periodic_update<float>(const GridDesc &, float *, int, cudaStream_t, int, int);
 template void periodic_update<double>(const GridDesc &, double *, int, cudaStream_t, int, int);
-template void wall_update<float>(const GridDesc &, float *, int, int, int, cudaStream_t);
-template void wall_update<double>(const GridDesc &, double *, int, int, int, cudaStream_t);
+template void wall_update<float>(const GridDesc &, float *, int, int, int, cudaStream_t, int);
+template void wall_update<double>(const GridDesc &, double *, int, int, int, cudaStream_t, int);
 template void smooth_field<float>(const GridDesc &, const SmoothSpec &, float *, float *,
                                   cudaStream_t);
 template void smooth_field<double>(const GridDesc &, const SmoothSpec &, double *, double *,

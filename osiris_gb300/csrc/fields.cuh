@@ -55,7 +55,7 @@ __host__ __device__ inline Box make_box(const GridDesc &g, int lo, int hi_off)
 template <typename T>
 void yee_advance(const GridDesc &g, T *e, T *b, const T *j, const double *dx, double dt,
                  cudaStream_t st, int walls = 0, int order = 2, int open_axis = -1,
-                 T *lind = nullptr);
+                 T *lind = nullptr, int pmc = 0);
 // Lindman open boundaries at both edges of one axis (p_bc_lindman,
 // source/emf/boundary/os-emf-lindman.f90).  Their state: 5 buffer planes along the axis
 // (E at 0 and 1, B at 0, E at nx+1 and nx+2), 3 components, per interior point of the other
@@ -66,9 +66,11 @@ long lindman_state_size(const GridDesc &g, int axis);
 template <typename T>
 void open_guards(const GridDesc &g, T *e, T *b, int axis, const T *lind, cudaStream_t st);
 // conducting-wall images along the axes in `walls`: kind 0 E, 1 B (guards set), 2 J (guards
-// added into the box)
+// added into the box); the axes in `pmc` are perfect magnetic instead of electric conductors
+// for E and B (kinds 3 and 4 name those images directly)
 template <typename T>
-void wall_update(const GridDesc &g, T *f, int kind, int walls, int order, cudaStream_t st);
+void wall_update(const GridDesc &g, T *f, int kind, int walls, int order, cudaStream_t st,
+                 int pmc = 0);
 
 // One box of a batch of independent periodic boxes (single precision): its fields and the
 // Yee coefficients.  The batched launches take a device array of these, one box per

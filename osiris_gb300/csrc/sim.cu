@@ -340,7 +340,7 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
     }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[4], st));
     yee_advance<T>(s->g, (T *)s->e, (T *)s->b, (const T *)s->j, c.dx, c.dt, st, walls, c.order,
-                   oax, (T *)s->lind);
+                   oax, (T *)s->lind, c.pmc);
     launches += 3 + (walls ? 6 * __builtin_popcount(walls) : 0) + (oax >= 0 ? 3 : 0);
     if (shift) {
         shift_window_x<T>(s->g, (T *)s->e, (T *)s->shift_tmp, st);
@@ -483,6 +483,8 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
                            "along one axis)");
     OSG_CHECK(cfg->open_fields == 0 || (cfg->walls == 0 && cfg->smooth_type == OSG_SMOOTH_NONE),
               OSG_ERR_ARG, "open boundaries combine with neither walls nor smoothing");
+    OSG_CHECK(cfg->pmc >= 0 && (cfg->pmc & ~cfg->walls) == 0, OSG_ERR_ARG,
+              "pmc: a bit mask of walled axes");
     OSG_CHECK(cfg->thermal >= 0 && (cfg->thermal & ~(cfg->walls | cfg->open_fields)) == 0,
               OSG_ERR_ARG, "thermal: a bit mask of walled or open axes");
     OSG_CHECK(cfg->thermal == 0 || cfg->engine == OSG_ENGINE_PLAIN, OSG_ERR_ARG,
