@@ -287,6 +287,9 @@ typedef struct {
     unsigned int seed;      /* key of the re-emission random stream */
     double uth_bnd[3];      /* the bath's thermal momentum per component */
     double ufl_bnd[3];      /* its fluid momentum (added only when all three are non-zero) */
+    int thermal_type; /* the bath's distribution (thermal_type): 0 "thermal" (Gaussian, normal
+                         component half-Maxwellian), 1 "random dir" (|uth| in a random
+                         direction), 2 "waterbag" (uniform in +-uth/2) */
     int pmc;          /* bit d set (d walled): the walls of axis d are perfect magnetic
                          conductors (the reference's p_bc_pmc, "reflecting") instead of
                          electric ones; the current and the particles are treated alike */

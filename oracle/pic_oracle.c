@@ -226,7 +226,10 @@ static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1)
  * virtual particle with momentum (-u1, -u2, u3) (2D) or -u (3D) through zero fields.  Axes in
  * order.  The random numbers: one Philox4x32-10 call per re-emission, counter (p, p >> 32,
  * step, d + 4 side code), key (seed, species); two Box-Muller Gaussians, the half-Maxwellian
- * and delta from (r + 1/2) / 2^32 in double. */
+ * and delta from (r + 1/2) / 2^32 in double.  ttype 1 ("random dir", :1026-1041): |uth| along
+ * a random direction, u3 = upar |uth|, the other two on a circle of radius
+ * sqrt(1 - upar) |uth| (the reference's expression); ttype 2 ("waterbag", :1016-1024):
+ * uth_c (v - 1/2) per component; both with the normal component turned into the box. */
 #define THERMAL_BODY(R, SFXN)                                                                 \
     if (!mask || np <= 0) return;                                                            \
     int gsz = 3;                                                                              \
@@ -247,12 +250,29 @@ static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1)
             const double inv32 = 2.3283064365386963e-10;                                      \
             const double v0 = (r[0] + 0.5) * inv32, v1 = (r[1] + 0.5) * inv32;               \
             const double v2 = (r[2] + 0.5) * inv32, v3 = (r[3] + 0.5) * inv32;               \
-            const double rad = sqrt(-2.0 * log(v0)), th = 6.283185307179586 * v1;             \
-            const double gs[2] = {rad * cos(th), rad * sin(th)};                              \
+            const R usign = lower ? (R)1 : (R)-1;                                             \
             R un[3];                                                                          \
-            for (int cc = 0, k = 0; cc < 3; cc++)                                             \
-                if (cc != d) un[cc] = (R)uth[cc] * (R)gs[k++];                                \
-            un[d] = (lower ? (R)1 : (R)-1) * (R)uth[d] * (R)sqrt(-2.0 * log(v2));             \
+            if (ttype == 1) {                                                                 \
+                const R ut = (R)sqrt((R)uth[0] * (R)uth[0] + (R)uth[1] * (R)uth[1] +          \
+                                     (R)uth[2] * (R)uth[2]);                                  \
+                const R upar = (R)(2.0 * v0 - 1.0);                                           \
+                const R uperp = (R)sqrt((R)1 - upar) * ut;                                    \
+                const R th = (R)(6.283185307179586 * v1);                                     \
+                un[0] = (R)cos(th) * uperp;                                                   \
+                un[1] = (R)sin(th) * uperp;                                                   \
+                un[2] = upar * ut;                                                            \
+                un[d] = usign * (R)fabs(un[d]);                                               \
+            } else if (ttype == 2) {                                                          \
+                const double w[3] = {v0, v1, v2};                                             \
+                for (int cc = 0; cc < 3; cc++) un[cc] = (R)uth[cc] * (R)(w[cc] - 0.5);         \
+                un[d] = usign * (R)fabs(un[d]);                                               \
+            } else {                                                                          \
+                const double rad = sqrt(-2.0 * log(v0)), th = 6.283185307179586 * v1;         \
+                const double gs[2] = {rad * cos(th), rad * sin(th)};                          \
+                for (int cc = 0, k = 0; cc < 3; cc++)                                         \
+                    if (cc != d) un[cc] = (R)uth[cc] * (R)gs[k++];                            \
+                un[d] = usign * (R)uth[d] * (R)sqrt(-2.0 * log(v2));                          \
+            }                                                                                 \
             const R f1 = (R)ufl[0], f2 = (R)ufl[1], f3 = (R)ufl[2];                           \
             if (f1 != 0 && f2 != 0 && f3 != 0) {                                              \
                 const R fa = (R)1 / ((R)1 + (R)sqrt((R)1 + f1 * f1 + f2 * f2 + f3 * f3));     \
@@ -288,7 +308,7 @@ void ora_particle_thermal_f32(int dim, int order, const int *nx, int np, int *ix
                               float *u, float *q, float rqm, int *emf_size, int *emf_off,
                               float *j, const double *dx, double dt, int mask,
                               const double *uth, const double *ufl, uint32_t seed, int species,
-                              uint64_t step)
+                              uint64_t step, int ttype)
 {
     THERMAL_BODY(float, f32)
 }
@@ -297,7 +317,7 @@ void ora_particle_thermal_f64(int dim, int order, const int *nx, int np, int *ix
                               double *u, double *q, double rqm, int *emf_size, int *emf_off,
                               double *j, const double *dx, double dt, int mask,
                               const double *uth, const double *ufl, uint32_t seed, int species,
-                              uint64_t step)
+                              uint64_t step, int ttype)
 {
     THERMAL_BODY(double, f64)
 }
@@ -306,10 +326,12 @@ void ora_particle_thermal_f64(int dim, int order, const int *nx, int np, int *ix
 static int step_thermal = 0;
 static uint32_t step_seed = 0;
 static uint64_t step_count = 0;
+static int step_ttype = 0;
 static double step_uth[3], step_ufl[3];
 void ora_set_thermal(int mask, const double *uth, const double *ufl, uint32_t seed,
-                     uint64_t step)
+                     uint64_t step, int ttype)
 {
+    step_ttype = ttype;
     step_thermal = mask;
     step_seed = seed;
     step_count = step;
@@ -626,7 +648,7 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
         free(et);                                                                             \
         ora_particle_thermal_##SFXN(dim, order, nx, np[s], ix[s], x[s], u[s], q[s], rqm[s],   \
                                     emf_size, emf_off, j, dx, dtp, step_thermal, step_uth,    \
-                                    step_ufl, step_seed, s, step_count);                      \
+                                    step_ufl, step_seed, s, step_count, step_ttype);          \
         if (oax >= 0)                                                                         \
             ora_particle_absorb_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], q[s], oax);         \
         ora_particle_bound_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], walls);                  \

@@ -65,7 +65,7 @@ void ora_set_walls_f64(int walls);
 /* thermal-bath particle boundary on the axes in `mask` for the step functions below (mask 0:
  * none); `step` keys the random stream of the next step */
 void ora_set_thermal(int mask, const double *uth, const double *ufl, uint32_t seed,
-                     uint64_t step);
+                     uint64_t step, int ttype);
 void ora_set_open_f32(int axis, float *state);
 void ora_set_open_f64(int axis, double *state);
 void ora_field_energy_f32(int dim, const int *nx, const int *gcl, const int *gcu,

@@ -88,7 +88,7 @@ def _declare(L):
         getattr(L, f"ora_set_walls_{s_}").argtypes = [I]
         getattr(L, f"ora_set_pmc_{s_}").argtypes = [I]
         getattr(L, f"ora_set_open_{s_}").argtypes = [I, P]
-    L.ora_set_thermal.argtypes = [I, P, P, C.c_uint32, C.c_uint64]
+    L.ora_set_thermal.argtypes = [I, P, P, C.c_uint32, C.c_uint64, I]
     L.ora_push_pusher_f32.argtypes = [I, I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P,
                                       P, D, D, P]
     L.ora_push_pusher_f64.argtypes = [I, I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, D,
@@ -335,7 +335,7 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     axis d bounded by conducting walls instead of periodic.  open_fields = (axis, state from
     lindman_state): Lindman open boundaries at both edges of that axis, particles absorbed
     there (left in the arrays with charge and momentum 0).  thermal = dict(mask, uth, ufl, seed,
-    step): particles crossing the edges of the axes in mask (walled or open) are re-emitted from
+    step, type: 0 thermal, 1 random dir, 2 waterbag): particles crossing the edges of the axes in mask (walled or open) are re-emitted from
     a thermal bath; step keys the random stream.  pmc (bit d, d walled): perfect magnetic
     instead of electric conductor walls.
     Returns the per-species energy sums (Boris: time-centred u^2/(gamma+1); exact pusher:
@@ -364,7 +364,7 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     if thermal is not None:
         L.ora_set_thermal(int(thermal["mask"]), _p(_f64(thermal["uth"])),
                           _p(_f64(thermal.get("ufl", [0.0] * 3))), int(thermal.get("seed", 0)),
-                          int(thermal["step"]))
+                          int(thermal["step"]), int(thermal.get("type", 0)))
     try:
         if pusher != "boris":
             getattr(L, f"ora_step_pusher_{prec}")(PUSHERS[pusher], *args, float(iter_tol))
@@ -374,7 +374,7 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
         getattr(L, f"ora_set_walls_{prec}")(0)
         getattr(L, f"ora_set_pmc_{prec}")(0)
         getattr(L, f"ora_set_open_{prec}")(-1, None)
-        L.ora_set_thermal(0, None, None, 0, 0)
+        L.ora_set_thermal(0, None, None, 0, 0, 0)
     if smooth is not None:
         getattr(L, f"ora_set_smooth_{prec}")(None, None)
     return ene

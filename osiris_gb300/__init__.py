@@ -76,7 +76,7 @@ class Config(C.Structure):
                 ("walls", I),
                 ("open_fields", I),
                 ("thermal", I), ("seed", C.c_uint), ("uth_bnd", D * 3), ("ufl_bnd", D * 3),
-                ("pmc", I)]
+                ("thermal_type", I), ("pmc", I)]
 
 
 def _declare(lb):
@@ -380,7 +380,8 @@ class Simulation:
     def __init__(self, nx, dx, dt, order=2, precision=32, engine=ENGINE_TILED, tile=None,
                  n_sort=0, capacity=0.0, pusher=PUSHER_BORIS, iter_tol=0.0,
                  smooth_type=SMOOTH_NONE, smooth_order=0, walls=0, open_fields=0, thermal=0,
-                 uth_bnd=(0.0, 0.0, 0.0), ufl_bnd=(0.0, 0.0, 0.0), seed=0, pmc=0):
+                 uth_bnd=(0.0, 0.0, 0.0), ufl_bnd=(0.0, 0.0, 0.0), seed=0, pmc=0,
+                 thermal_type=0):
         self.dim = len(nx)
         self.nx = list(nx)
         self.order = order
@@ -406,6 +407,7 @@ class Simulation:
         cfg.open_fields = open_fields
         cfg.thermal = thermal
         cfg.pmc = pmc
+        cfg.thermal_type = thermal_type
         cfg.seed = seed
         for c in range(3):
             cfg.uth_bnd[c] = uth_bnd[c]

@@ -211,7 +211,8 @@ __device__ __forceinline__ void philox4x32_10(unsigned int c[4], unsigned int k0
 
 // Thermal-bath re-emission of particle p after it crossed the edges coded in tb (2 bits per
 // axis: 1 lower, 2 upper), axis by axis (p_bc_thermal, source/spec/os-spec-boundary.f03:
-// 1315-1387, with thermal_bath :972-1067, thermal_type "thermal"):
+// 1315-1387, with thermal_bath :972-1067; thermal_type "thermal" below, "random dir" and
+// "waterbag" in the branches):
 //  * momentum: uth_c times a Gaussian for the two other components, uth_d times a
 //    half-Maxwellian sqrt(-2 ln v) pointing into the box for the normal one, then the fluid
 //    momentum ufl added relativistically when all three of its components are non-zero;
@@ -237,12 +238,32 @@ __device__ __noinline__ void thermal_reemit(const PlainPushArgs<T> &a, long p, T
         philox4x32_10(r, a.rng_key[0], a.rng_key[1]);
         const double v0 = (r[0] + 0.5) * inv32, v1 = (r[1] + 0.5) * inv32;
         const double v2 = (r[2] + 0.5) * inv32, v3 = (r[3] + 0.5) * inv32;
-        const double rad = sqrt(-2.0 * log(v0)), th = 6.283185307179586 * v1;
-        const double gs[2] = {rad * cos(th), rad * sin(th)};
+        const T usign = lower ? T(1) : T(-1);
         T un[3];
-        for (int c = 0, k = 0; c < 3; c++)
-            if (c != d) un[c] = a.uth_bnd[c] * (T)gs[k++];
-        un[d] = (lower ? T(1) : T(-1)) * a.uth_bnd[d] * (T)sqrt(-2.0 * log(v2));
+        if (a.thermal_type == 1) {
+            // "random dir": |uth| along a random direction, u3 = upar |uth| and the other two
+            // on a circle of radius sqrt(1 - upar) |uth| (the reference's expression, :1026-1041)
+            const T ut = sqrt(a.uth_bnd[0] * a.uth_bnd[0] + a.uth_bnd[1] * a.uth_bnd[1] +
+                              a.uth_bnd[2] * a.uth_bnd[2]);
+            const T upar = (T)(2.0 * v0 - 1.0);
+            const T uperp = sqrt(T(1) - upar) * ut;
+            const T th = (T)(6.283185307179586 * v1);
+            un[0] = cos(th) * uperp;
+            un[1] = sin(th) * uperp;
+            un[2] = upar * ut;
+            un[d] = usign * fabs(un[d]);
+        } else if (a.thermal_type == 2) {
+            // "waterbag": uniform in [-uth/2, uth/2) per component (:1016-1024)
+            const double w[3] = {v0, v1, v2};
+            for (int c = 0; c < 3; c++) un[c] = a.uth_bnd[c] * (T)(w[c] - 0.5);
+            un[d] = usign * fabs(un[d]);
+        } else {
+            const double rad = sqrt(-2.0 * log(v0)), th = 6.283185307179586 * v1;
+            const double gs[2] = {rad * cos(th), rad * sin(th)};
+            for (int c = 0, k = 0; c < 3; c++)
+                if (c != d) un[c] = a.uth_bnd[c] * (T)gs[k++];
+            un[d] = usign * a.uth_bnd[d] * (T)sqrt(-2.0 * log(v2));
+        }
         const T f1 = a.ufl_bnd[0], f2 = a.ufl_bnd[1], f3 = a.ufl_bnd[2];
         if (f1 != T(0) && f2 != T(0) && f3 != T(0)) {
             const T fa = T(1) / (T(1) + sqrt(T(1) + f1 * f1 + f2 * f2 + f3 * f3));
@@ -545,6 +566,7 @@ PlainPushArgs<T> make_plain_args(int dim, int order, int *ix, T *x, T *u, const 
     }
     a.step = nullptr;
     a.rng_key[0] = a.rng_key[1] = 0;
+    a.thermal_type = 0;
     a.pusher = OSG_PUSHER_BORIS;
     a.qm = T(1) / rqm;
     a.rqm = rqm;

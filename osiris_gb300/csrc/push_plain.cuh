@@ -34,6 +34,7 @@ template <typename T> struct PlainPushArgs {
     int thermal[3];        // > 0: thermal-bath edges of [1, thermal[d]]: a particle that crossed
                            // one is re-emitted with new momenta (thermal_reemit)
     T uth_bnd[3], ufl_bnd[3];   // the bath's thermal and fluid momenta
+    int thermal_type;           // 0 thermal, 1 random dir, 2 waterbag
     const unsigned long long *step;   // device step counter (re-emission random stream)
     unsigned int rng_key[2];          // the stream's key: seed, species
     int pusher;            // OSG_PUSHER_*

@@ -304,6 +304,7 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
                     a.ufl_bnd[d] = (T)c.ufl_bnd[d];
                 }
                 a.step = s->d_step;
+                a.thermal_type = c.thermal_type;
                 a.rng_key[0] = c.seed;
                 a.rng_key[1] = (unsigned int)k;
             }
@@ -489,6 +490,8 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               OSG_ERR_ARG, "thermal: a bit mask of walled or open axes");
     OSG_CHECK(cfg->thermal == 0 || cfg->engine == OSG_ENGINE_PLAIN, OSG_ERR_ARG,
               "thermal-bath particle boundaries run on the plain engine");
+    OSG_CHECK(cfg->thermal_type >= 0 && cfg->thermal_type <= 2, OSG_ERR_ARG,
+              "thermal_type: 0 thermal, 1 random dir, 2 waterbag");
     if (cfg->thermal)
         for (int d = 0; d < cfg->dim; d++)
             OSG_CHECK(!((cfg->thermal >> d) & 1) || cfg->uth_bnd[d] > 0, OSG_ERR_ARG,

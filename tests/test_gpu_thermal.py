@@ -21,25 +21,28 @@ def osg():
     return osiris_gb300
 
 
-CASES = [  # dim, prec, walls, open axis, thermal mask, ufl
-    (2, 64, 1, None, 1, (0.0, 0.0, 0.0)),
-    (2, 64, 3, None, 3, (0.05, 0.1, -0.1)),
-    (2, 32, 2, None, 2, (0.0, 0.0, 0.0)),
-    (2, 64, 0, 0, 1, (0.0, 0.0, 0.0)),
-    (2, 32, 0, 1, 2, (0.05, 0.1, -0.1)),
-    (3, 64, 5, None, 5, (0.0, 0.0, 0.0)),
+CASES = [  # dim, prec, walls, open axis, thermal mask, ufl, thermal type
+    (2, 64, 1, None, 1, (0.0, 0.0, 0.0), 0),
+    (2, 64, 3, None, 3, (0.05, 0.1, -0.1), 0),
+    (2, 32, 2, None, 2, (0.0, 0.0, 0.0), 0),
+    (2, 64, 0, 0, 1, (0.0, 0.0, 0.0), 0),
+    (2, 32, 0, 1, 2, (0.05, 0.1, -0.1), 0),
+    (3, 64, 5, None, 5, (0.0, 0.0, 0.0), 0),
+    (2, 64, 3, None, 3, (0.0, 0.0, 0.0), 1),
+    (2, 32, 1, None, 1, (0.0, 0.0, 0.0), 2),
+    (3, 64, 2, None, 2, (0.0, 0.0, 0.0), 2),
 ]
 
 
-@pytest.mark.parametrize("dim,prec,walls,oax,mask,ufl", CASES)
-def test_thermal_bath_matches_oracle(osg, oracle, dim, prec, walls, oax, mask, ufl):
+@pytest.mark.parametrize("dim,prec,walls,oax,mask,ufl,ttype", CASES)
+def test_thermal_bath_matches_oracle(osg, oracle, dim, prec, walls, oax, mask, ufl, ttype):
     nx = [20, 16] if dim == 2 else [10, 9, 8]
     p, g, dx, dt, species, e, b = _setup(oracle, prec, dim, 2, nx, [2] * dim, 21, uth=0.6,
                                          ufl=0.1)
     uth = (0.3, 0.2, 0.25)
     sim = osg.Simulation(nx, dx, dt, order=2, precision=prec, engine=osg.ENGINE_PLAIN,
                          walls=walls, open_fields=0 if oax is None else 1 << oax, thermal=mask,
-                         uth_bnd=uth, ufl_bnd=ufl, seed=77)
+                         uth_bnd=uth, ufl_bnd=ufl, seed=77, thermal_type=ttype)
     sim.set_fields(e, b)
     for s in species:
         sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
@@ -53,7 +56,7 @@ def test_thermal_bath_matches_oracle(osg, oracle, dim, prec, walls, oax, mask, u
     for k in range(steps):
         oracle.step(g, p, eo, bo, jo, ora, dt, walls=walls,
                     open_fields=None if oax is None else (oax, st),
-                    thermal=dict(mask=mask, uth=uth, ufl=ufl, seed=77, step=k))
+                    thermal=dict(mask=mask, uth=uth, ufl=ufl, seed=77, step=k, type=ttype))
     tol = 1e-12 if prec == 64 else 5e-5
     errs = {"E": _nerr(eg, eo), "B": _nerr(bg, bo), "J": _nerr(jg, jo)}
     for k, s in enumerate(ora):

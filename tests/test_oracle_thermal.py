@@ -89,3 +89,25 @@ def test_stream_is_keyed_by_counter(oracle):
     assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
     assert not np.any(res[0][0] == res[2][0])
     assert not np.any(res[0][0] == res[3][0])
+
+
+def test_waterbag_and_random_dir(oracle):
+    uth = [0.4, 0.3, 0.2]
+    g, sp = _crossers(oracle, "f64")
+    e, b, j = g.zeros("f64"), g.zeros("f64"), g.zeros("f64")
+    oracle.step(g, "f64", e, b, j, [sp], 0.05, walls=1,
+                thermal=dict(mask=1, uth=uth, seed=1, step=0, type=2))
+    u = sp["u"]
+    assert np.all(u[:, 0] >= 0)
+    for c in range(3):
+        assert np.abs(u[:, c]).max() <= uth[c] / 2 + 1e-12
+        assert np.abs(u[:, c]).max() > 0.45 * uth[c]
+    g, sp = _crossers(oracle, "f64")
+    oracle.step(g, "f64", e, b, j, [sp], 0.05, walls=1,
+                thermal=dict(mask=1, uth=uth, seed=1, step=0, type=1))
+    u = sp["u"]
+    ut = np.sqrt(sum(v * v for v in uth))
+    upar = u[:, 2] / ut
+    assert np.all(upar >= -1) and np.all(upar <= 1) and np.all(u[:, 0] >= 0)
+    # the reference's perpendicular radius sqrt(1 - upar) |uth|
+    assert np.allclose(np.hypot(u[:, 0], u[:, 1]), np.sqrt(1 - upar) * ut, rtol=1e-12)
