@@ -7,7 +7,7 @@ cells included (the boundary planes live there).
 * plain engine, 2D, FP64 1e-12 and FP32 1e-5 / 5e-5 (1 and 10 steps), orders 1-3, either axis;
   3D FP64 along x3;
 * tiled engine (FP32, particles removed rather than kept with charge 0): fields and the live
-  particles against the oracle;
+  particles against the oracle, in 2D and, with walls or open edges, in 3D;
 * a vacuum pulse leaves the box with less than 1e-4 of its energy left;
 * checkpoint / restore keeps the Lindman state: 4 + 4 steps equal 8 steps to 1e-12 (FP64
   atomics) with the same particles absorbed.
@@ -181,3 +181,45 @@ def test_checkpoint_keeps_the_lindman_state(osg, oracle, tmp_path):
     (ia, xa, ua, qa), (ib, xb, ub, qb) = got[1], want[1]
     assert np.array_equal(qa, qb)
     assert _nerr(ia + xa, ib + xb) <= 1e-12 and _nerr(ua, ub) <= 1e-12
+
+
+@pytest.mark.parametrize("walls,open_fields", [(0, 4), (5, 0), (3, 0)])
+def test_tiled_3d_bounded_matches_oracle(osg, oracle, walls, open_fields):
+    """3D tiled engine (FP32) with Lindman open edges or conducting walls, 6 steps."""
+    dim, nx = 3, [16, 8, 8]
+    p, g, dx, dt, species, e, b = _setup(oracle, 32, dim, 2, nx, [2] * 3, 14, uth=0.6,
+                                         ufl=0.1)
+    sim = osg.Simulation(nx, dx, dt, order=2, precision=32, engine=osg.ENGINE_TILED,
+                         tile=[4, 4, 4], walls=walls, open_fields=open_fields)
+    sim.set_fields(e, b)
+    for s in species:
+        sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
+    steps = 6
+    sim.step(steps)
+    eg, bg, jg = sim.fields()
+    ora = [{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s.items()}
+           for s in species]
+    eo, bo, jo = e.copy(), b.copy(), g.zeros(p)
+    axis = open_fields.bit_length() - 1
+    st = oracle.lindman_state(g, p, axis) if open_fields else None
+    for _ in range(steps):
+        oracle.step(g, p, eo, bo, jo, ora, dt, walls=walls,
+                    open_fields=(axis, st) if open_fields else None)
+    if open_fields:
+        errs = {"E": _nerr(eg, eo), "B": _nerr(bg, bo), "J": _nerr(jg, jo)}
+    else:
+        errs = {"E": _nerr(g.interior(eg), g.interior(eo)),
+                "B": _nerr(g.interior(bg), g.interior(bo)),
+                "J": _nerr(g.interior(jg), g.interior(jo))}
+    for k, s in enumerate(ora):
+        ix, x, u, q = sim.species(k)
+        live = s["q"] != 0
+        assert len(q) == int(live.sum())
+        a = np.argsort(q, kind="stable")
+        o = np.flatnonzero(live)[np.argsort(s["q"][live], kind="stable")]
+        errs[f"x{k}"] = _nerr(ix[a] + x[a], s["ix"][o] + s["x"][o])
+        errs[f"u{k}"] = _nerr(u[a], s["u"][o])
+        assert ix.min() >= 1 and np.all(ix.max(axis=0) <= np.array(nx))
+    sim.close()
+    bad = {k: v for k, v in errs.items() if not v <= 5e-5}
+    assert not bad, (bad, errs)
