@@ -1027,8 +1027,8 @@ int osg_sim_energy(osg_sim *s, double *kinetic, double *field)
 int osg_sim_gauss_residual(osg_sim *s, double *max_abs, double *l2)
 {
     OSG_CHECK(s, OSG_ERR_ARG, "null sim");
-    OSG_CHECK(s->cfg.walls == 0, OSG_ERR_STATE,
-              "the Gauss residual is taken on periodic boxes (no conducting walls)");
+    OSG_CHECK(s->cfg.walls == 0 && s->cfg.open_fields == 0, OSG_ERR_STATE,
+              "the Gauss residual is taken on periodic boxes (no walls or open edges)");
     const size_t n = 3 * (size_t)s->g.npoints();
     int rc = OSG_OK;
     if (!s->d_rho) s->d_rho = dalloc<double>(n, &rc);

@@ -223,3 +223,11 @@ def test_tiled_3d_bounded_matches_oracle(osg, oracle, walls, open_fields):
     sim.close()
     bad = {k: v for k, v in errs.items() if not v <= 5e-5}
     assert not bad, (bad, errs)
+
+
+def test_gauss_residual_refuses_open_edges(osg):
+    sim = osg.Simulation([16, 16], [0.1, 0.1], 0.03, order=2, precision=64,
+                         engine=osg.ENGINE_PLAIN, open_fields=2)
+    with pytest.raises(osg.OsirisGB300Error):
+        sim.gauss_residual()
+    sim.close()
