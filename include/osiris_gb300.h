@@ -191,6 +191,20 @@ int osg_periodic_f32(int dim, const int *nx, const int *gcl, const int *gcu, flo
  * normal B, J.  Kinds 3 (E) and 4 (B) are the walls of a perfect magnetic conductor
  * (pmc_bc_e/b_*d_odd/even, source/emf/boundary/os-emf-pmc.f90): the same image points with
  * the signs of E and B exchanged. */
+/* Lindman open boundaries at both edges of `axis`, on HOST arrays (dim 2 or 3, gcl >= 1,
+ * gcu >= 2), one phase per call: what 0 after the E step (update_lindman_{2,3}d_e,
+ * source/emf/boundary/os-emf-lindman.f90:454-750: first-order Mur update of the tangential E on
+ * the planes 0 and nx+2, the state's E planes refreshed), 1 after each B half step
+ * (update_lindman_{2,3}d_b :539-857: the lower B buffer takes the Yee increment of the plane 0
+ * from e; dt is the full step), 2 in the guard update (update_emfbound_lindman :861-1042:
+ * E(0), B(0) and E(nx+1) from the state, guard points of the other axes from its periodic
+ * images).  `state` holds 15 reals per interior point of the other axes, zeroed before the
+ * first step: five planes (E at 0 and 1, B at 0, E at nx+1 and nx+2) of 3 components, the
+ * point index with the lower other axis fastest. */
+int osg_lindman_f32(int dim, const int *nx, const int *gcl, const int *gcu, int axis, int what,
+                    float *e, float *b, float *state, const double *dx, double dt);
+int osg_lindman_f64(int dim, const int *nx, const int *gcl, const int *gcu, int axis, int what,
+                    double *e, double *b, double *state, const double *dx, double dt);
 int osg_walls_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f, int kind,
                   int walls, int order);
 int osg_walls_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f, int kind,

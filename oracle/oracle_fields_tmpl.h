@@ -465,6 +465,21 @@ void FN(ora_open_guards)(int dim, const int *nx, const int *gcl, const int *gcu,
     FN(lind_restore)(g, d, e, b, st);
 }
 
+/* one phase of the Lindman boundaries on axis d (what 0: after the E step, 1: after a B half
+ * step with the full dt, 2: the restore of the boundary planes) */
+void FN(ora_lindman_phase)(int dim, const int *nx, const int *gcl, const int *gcu, int d,
+                           int what, R *e, R *b, R *st, const double *dx, double dt)
+{
+    FN(ora_grid) G, *g = &G;
+    FN(grid_init)(g, dim, nx, gcl, gcu);
+    if (what == 0)
+        FN(lind_e)(g, d, e, st, (R)((1.0 - dt / dx[d]) / (1.0 + dt / dx[d])));
+    else if (what == 1)
+        FN(lind_b)(g, d, e, st, dx, dt);
+    else
+        FN(lind_restore)(g, d, e, b, st);
+}
+
 /* absorbing particle boundary along axis d (p_bc_absorbing: a particle that left the box is
  * removed after its current was deposited, source/spec/os-spec-boundary.f03:501-511).  Here
  * it stays in the arrays with charge and momentum 0, at offset 0 of the edge cell it left

@@ -66,6 +66,11 @@ void ora_set_walls_f64(int walls);
  * none); `step` keys the random stream of the next step */
 void ora_set_thermal(int mask, const double *uth, const double *ufl, uint32_t seed,
                      uint64_t step, int ttype);
+void ora_lindman_phase_f32(int dim, const int *nx, const int *gcl, const int *gcu, int d,
+                           int what, float *e, float *b, float *st, const double *dx, double dt);
+void ora_lindman_phase_f64(int dim, const int *nx, const int *gcl, const int *gcu, int d,
+                           int what, double *e, double *b, double *st, const double *dx,
+                           double dt);
 void ora_set_open_f32(int axis, float *state);
 void ora_set_open_f64(int axis, double *state);
 void ora_field_energy_f32(int dim, const int *nx, const int *gcl, const int *gcu,

@@ -88,6 +88,7 @@ def _declare(L):
         getattr(L, f"ora_set_walls_{s_}").argtypes = [I]
         getattr(L, f"ora_set_pmc_{s_}").argtypes = [I]
         getattr(L, f"ora_set_open_{s_}").argtypes = [I, P]
+        getattr(L, f"ora_lindman_phase_{s_}").argtypes = [I, P, P, P, I, I, P, P, P, P, D]
     L.ora_set_thermal.argtypes = [I, P, P, C.c_uint32, C.c_uint64, I]
     L.ora_push_pusher_f32.argtypes = [I, I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P,
                                       P, D, D, P]
@@ -327,6 +328,15 @@ def lindman_state(g: "Grid", prec, axis):
         if a != axis:
             n *= g.nx[a]
     return np.zeros(15 * n, dtype=dtype_of(prec))
+
+
+def lindman_phase(g: "Grid", prec, axis, what, e, b, state, dt):
+    """One phase of the Lindman boundaries on `axis`, in place (what 0 after the E step, 1
+    after a B half step, 2 the restore of the boundary planes)."""
+    nx, gl, gu = g.args()
+    getattr(lib(), f"ora_lindman_phase_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), int(axis),
+                                                 int(what), _p(e), _p(b), _p(state),
+                                                 _p(_f64(g.dx + [0.0] * 3)), float(dt))
 
 
 def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="boris",

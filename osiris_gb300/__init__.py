@@ -102,6 +102,7 @@ def _declare(lb):
         getattr(lb, f"osg_yee_advance_{s}").argtypes = [I, P, P, P, P, P, P, P, D]
         getattr(lb, f"osg_periodic_{s}").argtypes = [I, P, P, P, P, I]
         getattr(lb, f"osg_walls_{s}").argtypes = [I, P, P, P, P, I, I, I]
+        getattr(lb, f"osg_lindman_{s}").argtypes = [I, P, P, P, I, I, P, P, P, P, D]
     lb.osg_particle_wrap.argtypes = [I, P, L, P]
     lb.osg_rng_seed.argtypes = [P, I]
     lb.osg_load_lattice.argtypes = [P, I, I, P, P, P, D, P, P, D, D, P, P, P, P]
@@ -262,6 +263,16 @@ def yee_advance(dim, nx, gcl, gcu, e, b, j, dx, dt):
     _check(getattr(lib(), f"osg_yee_advance_{prec}")(
         dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)), _p(e), _p(b), _p(j),
         _p(_f64(list(dx) + [0.0] * 3)), float(dt)))
+
+
+def lindman(dim, nx, gcl, gcu, axis, what, e, b, state, dx, dt):
+    """One phase of the Lindman open boundaries on host arrays (osg_lindman_*): what 0 after
+    the E step, 1 after a B half step (dt the full step), 2 the restore of the boundary planes;
+    `state` (15 reals per interior point of the other axes) is kept by the caller."""
+    s = _prec(e)
+    _check(getattr(lib(), f"osg_lindman_{s}")(dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)),
+                                              int(axis), int(what), _p(e), _p(b), _p(state),
+                                              _p(_f64(list(dx) + [0.0] * 3)), float(dt)))
 
 
 def walls(dim, nx, gcl, gcu, f, kind, mask, order):

@@ -271,6 +271,37 @@ static int smooth_host(int dim, const int *nx, const int *gcl, const int *gcu, T
 }
 
 template <typename T>
+static int lindman_host(int dim, const int *nx, const int *gcl, const int *gcu, int axis,
+                        int what, T *e, T *b, T *state, const double *dx, double dt)
+{
+    OSG_CHECK(dim >= 2 && dim <= 3 && nx && gcl && gcu && e && state && dx && axis >= 0 &&
+                  axis < dim && what >= 0 && what <= 2 && (what != 2 || b),
+              OSG_ERR_ARG, "bad Lindman arguments");
+    for (int d = 0; d < dim; d++)
+        OSG_CHECK(nx[d] >= 1 && gcl[d] >= 1 && gcu[d] >= 2 && dx[d] > 0, OSG_ERR_ARG,
+                  "the Lindman planes need gcl >= 1 and gcu >= 2");
+    GridDesc g = make_grid(dim, nx, gcl, gcu);
+    const long n = g.npoints() * 3, ns = lindman_state_size(g, axis);
+    void *d_e, *d_b, *d_s;
+    int rc;
+    if ((rc = g_stage.get(4, sizeof(T) * n, &d_e))) return rc;
+    if ((rc = g_stage.get(5, sizeof(T) * n, &d_b))) return rc;
+    if ((rc = g_stage.get(6, sizeof(T) * ns, &d_s))) return rc;
+    cudaStream_t st = g_stage.stream;
+    OSG_CUDA(cudaMemcpyAsync(d_e, e, sizeof(T) * n, cudaMemcpyHostToDevice, st));
+    if (what == 2) OSG_CUDA(cudaMemcpyAsync(d_b, b, sizeof(T) * n, cudaMemcpyHostToDevice, st));
+    OSG_CUDA(cudaMemcpyAsync(d_s, state, sizeof(T) * ns, cudaMemcpyHostToDevice, st));
+    lindman_phase<T>(g, axis, what, (T *)d_e, (T *)d_b, (T *)d_s, dx, dt, st);
+    OSG_CUDA(cudaGetLastError());
+    if (what != 1) OSG_CUDA(cudaMemcpyAsync(e, d_e, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+    if (what == 2) OSG_CUDA(cudaMemcpyAsync(b, d_b, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+    if (what != 2)
+        OSG_CUDA(cudaMemcpyAsync(state, d_s, sizeof(T) * ns, cudaMemcpyDeviceToHost, st));
+    OSG_CUDA(cudaStreamSynchronize(st));
+    return OSG_OK;
+}
+
+template <typename T>
 static int walls_host(int dim, const int *nx, const int *gcl, const int *gcu, T *f, int kind,
                       int walls, int order)
 {
@@ -595,6 +626,18 @@ int osg_smooth_coefficients(int type, int order, double *c, int *n)
     OSG_CHECK(smooth_coefficients(type, order, c, n) == OSG_OK, OSG_ERR_ARG,
               "bad smoothing type %d / order %d", type, order);
     return OSG_OK;
+}
+
+int osg_lindman_f32(int dim, const int *nx, const int *gcl, const int *gcu, int axis, int what,
+                    float *e, float *b, float *state, const double *dx, double dt)
+{
+    return lindman_host<float>(dim, nx, gcl, gcu, axis, what, e, b, state, dx, dt);
+}
+
+int osg_lindman_f64(int dim, const int *nx, const int *gcl, const int *gcu, int axis, int what,
+                    double *e, double *b, double *state, const double *dx, double dt)
+{
+    return lindman_host<double>(dim, nx, gcl, gcu, axis, what, e, b, state, dx, dt);
 }
 
 int osg_walls_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f, int kind,

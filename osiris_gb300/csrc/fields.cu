@@ -347,6 +347,24 @@ void open_guards(const GridDesc &g, T *e, T *b, int axis, const T *lind, cudaStr
 }
 
 template <typename T>
+void lindman_phase(const GridDesc &g, int axis, int what, T *e, T *b, T *lind, const double *dx,
+                   double dt, cudaStream_t st)
+{
+    const LindAxes L = lind_axes(g, axis);
+    if (what == 0) {
+        const T k = (T)((1.0 - dt / dx[axis]) / (1.0 + dt / dx[axis]));
+        k_lindman_e<T><<<blocks_for(L.nperp, 256), 256, 0, st>>>(g, L, e, lind, k);
+    } else if (what == 1) {
+        launch_lindman_b(g, L, e, lind, dx, dt, st);
+    } else {
+        long nfull = 1;
+        if (L.pa < 3) nfull *= g.size[L.pa];
+        if (L.pb < 3) nfull *= g.size[L.pb];
+        k_lindman_restore<T><<<blocks_for(nfull, 256), 256, 0, st>>>(g, L, e, b, lind, nfull);
+    }
+}
+
+template <typename T>
 void yee_advance(const GridDesc &g, T *e, T *b, const T *j, const double *dx, double dt,
                  cudaStream_t st, int walls, int order, int open_axis, T *lind, int pmc)
 {
@@ -829,6 +847,10 @@ template void yee_advance<float>(const GridDesc &, float *, float *, const float
 template void yee_advance<double>(const GridDesc &, double *, double *, const double *,
                                   const double *, double, cudaStream_t, int, int, int,
                                   double *, int);
+template void lindman_phase<float>(const GridDesc &, int, int, float *, float *, float *,
+                                   const double *, double, cudaStream_t);
+template void lindman_phase<double>(const GridDesc &, int, int, double *, double *, double *,
+                                    const double *, double, cudaStream_t);
 template void open_guards<float>(const GridDesc &, float *, float *, int, const float *,
                                  cudaStream_t);
 template void open_guards<double>(const GridDesc &, double *, double *, int, const double *,

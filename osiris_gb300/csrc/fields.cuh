@@ -65,6 +65,12 @@ long lindman_state_size(const GridDesc &g, int axis);
 // then the boundary planes E(0), B(0), E(nx+1) from the state (update_emfbound_lindman)
 template <typename T>
 void open_guards(const GridDesc &g, T *e, T *b, int axis, const T *lind, cudaStream_t st);
+// one phase of the Lindman boundaries: 0 the Mur update of E and its planes after the E step,
+// 1 the lower B buffer after a B half step (dt the full step), 2 the restore of E(0), B(0),
+// E(nx+1) (guard points of the other axes from the state's periodic images)
+template <typename T>
+void lindman_phase(const GridDesc &g, int axis, int what, T *e, T *b, T *lind, const double *dx,
+                   double dt, cudaStream_t st);
 // conducting-wall images along the axes in `walls`: kind 0 E, 1 B (guards set), 2 J (guards
 // added into the box); the axes in `pmc` are perfect magnetic instead of electric conductors
 // for E and B (kinds 3 and 4 name those images directly)

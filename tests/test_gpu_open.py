@@ -231,3 +231,27 @@ def test_gauss_residual_refuses_open_edges(osg):
     with pytest.raises(osg.OsirisGB300Error):
         sim.gauss_residual()
     sim.close()
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-14), ("f32", 1e-6)])
+@pytest.mark.parametrize("dim,axis", [(2, 0), (2, 1), (3, 1)])
+@pytest.mark.parametrize("what", [0, 1, 2])
+def test_host_array_lindman_matches_oracle(osg, oracle, prec, tol, dim, axis, what):
+    """osg_lindman_* (one phase on host arrays) against the oracle's phase, from random fields
+    and a random state."""
+    nx = [12, 10] if dim == 2 else [8, 7, 6]
+    dx = [0.1, 0.12, 0.09][:dim]
+    g = oracle.Grid(nx, 2, dx)
+    dt_ = np.float32 if prec == "f32" else np.float64
+    rng = np.random.default_rng(10 * what + axis)
+    e0 = rng.standard_normal(g.shape).astype(dt_)
+    b0 = rng.standard_normal(g.shape).astype(dt_)
+    s0 = rng.standard_normal(oracle.lindman_state(g, prec, axis).shape).astype(dt_)
+    ea, ba, sa = e0.copy(), b0.copy(), s0.copy()
+    eo, bo, so = e0.copy(), b0.copy(), s0.copy()
+    dt = 0.03
+    osg.lindman(dim, g.nx, g.gcl, g.gcu, axis, what, ea, ba, sa, dx, dt)
+    oracle.lindman_phase(g, prec, axis, what, eo, bo, so, dt)
+    for a, o, a0 in ((ea, eo, e0), (ba, bo, b0), (sa, so, s0)):
+        assert _nerr(a, o) <= tol
+    assert not (np.array_equal(ea, e0) and np.array_equal(ba, b0) and np.array_equal(sa, s0))
