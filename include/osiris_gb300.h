@@ -76,6 +76,9 @@ int osg_version(void);
 int osg_device_count(void);
 /* select the CUDA device used by the calling thread's subsequent calls */
 int osg_set_device(int device);
+/* free and total device memory of the current device, in bytes (cudaMemGetInfo); a
+ * diagnostic with no counterpart in the reference */
+int osg_device_memory(size_t *free_bytes, size_t *total_bytes);
 /* page-locked host memory for the host-array entry points (fast copies); NULL on failure */
 void *osg_host_alloc(size_t bytes);
 int osg_host_free(void *p);
@@ -97,6 +100,28 @@ int osg_vadvance_deposit_f64(int dim, int order, int *ix, double *x, double *u, 
                              const double *bfield, const int *emf_size, const int *emf_offset,
                              double *j, const int *j_size, const int *j_offset,
                              const double *dx, double dt, double *ene);
+
+/* The 2D cylindrical push/deposit (x1 = z, x2 = r): replaces
+ * FNAME(vadvance_deposit_2d_cyl_s{1..4}) (source/simd/os-spec-push-avx2.c:762-1092,
+ * source/simd/os-spec-push-avx2d.c:777-1107), called from vadvance_deposit_2d_cyl
+ * (source/spec/os-spec-vpush.f03:190-255) for coordinates = p_cylindrical_b (:424-425).  Same
+ * arguments as osg_vadvance_deposit_* with dim = 2, plus ilb2 (after rqm, as the reference):
+ * the lower global cell of the node along x2 (this%my_nx_p(p_lower, 2)).  The Boris update and
+ * the axial move are the Cartesian ones; the radial move is done in double from the particle's
+ * global radius, and p_r, p_theta are rotated onto the new radial direction with p_theta
+ * scaled by r_old / r_new (angular momentum kept).  The current goes into j with the
+ * Cartesian 2D charge-conserving deposit, as the reference's (its 1/r normalisation is a
+ * later phase of the host). */
+int osg_vadvance_deposit_cyl_f32(int order, int *ix, float *x, float *u, float *q, int i0,
+                                 int i1, float rqm, int ilb2, const float *efield,
+                                 const float *bfield, const int *emf_size,
+                                 const int *emf_offset, float *j, const int *j_size,
+                                 const int *j_offset, const double *dx, double dt, double *ene);
+int osg_vadvance_deposit_cyl_f64(int order, int *ix, double *x, double *u, double *q, int i0,
+                                 int i1, double rqm, int ilb2, const double *efield,
+                                 const double *bfield, const int *emf_size,
+                                 const int *emf_offset, double *j, const int *j_size,
+                                 const int *j_offset, const double *dx, double dt, double *ene);
 
 /* The same particle advance with the exact momentum update of push_type = "exact"
  * (dudt_exact, source/spec/os-spec-extpush.f03:40-348, reached through advance_deposit_{1d,2d,
@@ -142,9 +167,11 @@ int osg_advance_deposit_f64(int dim, int order, int *ix, double *x, double *u, d
  * stepping loops that budget device memory once and must not let a library allocate.  It has
  * no counterpart in the reference.  All device staging lives in one file-scope array of
  * OSG_NOALLOC_SCRATCH_BYTES, reserved on every GPU that loads the library until the process
- * exits; nothing is allocated or freed.  A call whose particles and fields need more than that
- * (roughly 4*dim + 20 bytes per particle plus three copies of the grid) is rejected with
- * OSG_ERR_ARG; split the particle range into smaller calls.  The first call on a device looks
+ * exits; nothing is allocated or freed.  A call needs 8*dim + 16 bytes per particle (ix, x, u
+ * and q: 32 B in 2D, 40 B in 3D), three copies of the grid (E, B, J) and under 2 KB of
+ * alignment and counters; one that needs more than the array is rejected with OSG_ERR_ARG
+ * (for a quadratic 256x256 grid the limit is about 446,000 2D particles per call); split the
+ * particle range into smaller calls.  The first call on a device looks
  * up the array's address for that device; make it before any stream capture there.  Every
  * call shares the array, so calls that overlap on the GPU (several host threads at once) race;
  * each call clears what must start at zero and copies the rest in.  Runs on the calling

@@ -464,10 +464,14 @@ static void OFN(split2d)(OFN(vp2) *buf, int base, int gn, const int *dix, const 
     *extra = ne;
 }
 
-void OFN(ora_vadvance_deposit_2d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R *rqm,
-                                  R *e, R *b, int *emf_size, int *emf_off,
-                                  R *j, int *j_size, int *j_off,
-                                  double *dx, double *dt, double *ene)
+/* cyl = 1: the 2D cylindrical variant (x1 = z, x2 = r; vadvance_deposit_2d_cyl_sK,
+ * source/simd/os-spec-push-avx2d.c:777-1107, single precision os-spec-push-avx2.c:762-1092):
+ * the radial move and the angular-momentum correction of p_r, p_theta in double, from the
+ * global radial position of the particle (ilb2 = the node's lower global cell along x2) */
+static void OFN(push2d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R *rqm,
+                        R *e, R *b, int *emf_size, int *emf_off,
+                        R *j, int *j_size, int *j_off,
+                        double *dx, double *dt, double *ene, int cyl, int ilb2)
 {
     const R tem = (R)(0.5 * (*dt) / (*rqm));
     const R dtdx1 = (R)((*dt) / dx[0]), dtdx2 = (R)((*dt) / dx[1]);
@@ -533,7 +537,30 @@ void OFN(ora_vadvance_deposit_2d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R
                 R rg = OFN(rgamma)(u1, u2, u3);
                 acc[l] = FMA(q[p], en, acc[l]);
                 R v1 = u1 * rg, v2 = u2 * rg, v3 = u3 * rg;
-                R x1 = FMA(v1, dtdx1, x0), y1 = FMA(v2, dtdx2, y0);
+                R x1 = FMA(v1, dtdx1, x0), y1;
+                if (cyl) {
+                    /* :1034-1065: gix2 = iy0 + gshift2 (global cell), r_old = (y0 + gix2) dr,
+                     * x2_new = r_old + v2 dt, x3_new = v3 dt, r_new = |(x2_new, x3_new)|,
+                     * y1 = r_new / dr - gix2 (y0 if r_new == r_old); p_r, p_theta rotated
+                     * onto the new radial direction, p_theta scaled by r_old / r_new */
+                    const double gshift2 = (ORD == 1 || ORD == 3) ? (double)(ilb2 - 2)
+                                                                  : (double)(ilb2 - 2) - 0.5;
+                    const double gix2 = (double)jj + gshift2;
+                    const double r_old = ((double)y0 + gix2) * dx[1];
+                    const double x2n = fma((double)v2, *dt, r_old);
+                    const double x3n = (double)v3 * (*dt);
+                    const double r_new = sqrt(fma(x2n, x2n, x3n * x3n));
+                    const double y1d = (r_old == r_new) ? (double)y0
+                                                        : fma(r_new, 1.0 / dx[1], -gix2);
+                    y1 = (R)y1d;
+                    const double tmp = 1.0 / r_new;
+                    const double u2n = fma((double)u2, x2n, (double)u3 * x3n) * tmp;
+                    const double u3n = (double)u3 * (r_old * tmp);
+                    u[3 * p + 1] = (R)u2n;
+                    u[3 * p + 2] = (R)u3n;
+                } else {
+                    y1 = FMA(v2, dtdx2, y0);
+                }
                 OFN(vp2) *v = &buf[base + l];
                 v->x0 = x0; v->x1 = x1; v->y0 = y0; v->y1 = y1; v->q = q[p]; v->vz = v3;
                 v->i = i; v->j = jj;
@@ -554,6 +581,24 @@ void OFN(ora_vadvance_deposit_2d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R
         *ene += eacc;
     }
     free(buf);
+}
+
+void OFN(ora_vadvance_deposit_2d)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R *rqm,
+                                  R *e, R *b, int *emf_size, int *emf_off,
+                                  R *j, int *j_size, int *j_off,
+                                  double *dx, double *dt, double *ene)
+{
+    OFN(push2d)(ix, x, u, q, i0, i1, rqm, e, b, emf_size, emf_off, j, j_size, j_off, dx, dt,
+                ene, 0, 0);
+}
+
+void OFN(ora_vadvance_deposit_2d_cyl)(int *ix, R *x, R *u, R *q, int *i0, int *i1, R *rqm,
+                                      int *ilb2, R *e, R *b, int *emf_size, int *emf_off,
+                                      R *j, int *j_size, int *j_off,
+                                      double *dx, double *dt, double *ene)
+{
+    OFN(push2d)(ix, x, u, q, i0, i1, rqm, e, b, emf_size, emf_off, j, j_size, j_off, dx, dt,
+                ene, 1, *ilb2);
 }
 
 /* ========================================================================================

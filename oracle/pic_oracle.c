@@ -196,6 +196,26 @@ int ora_push_f64(int dim, int order, int *ix, double *x, double *u, double *q, i
     return 0;
 }
 
+#define ORA_CYL_DISPATCH(SFXN, RT)                                                            \
+    int ora_push_cyl_##SFXN(int order, int *ix, RT *x, RT *u, RT *q, int i0, int i1, RT rqm,  \
+                            int ilb2, RT *e, RT *b, int *emf_size, int *emf_off, RT *j,       \
+                            int *j_size, int *j_off, double *dx, double dt, double *ene)      \
+    {                                                                                         \
+        switch (order) {                                                                      \
+        case 1: ora_vadvance_deposit_2d_cyl_s1_##SFXN(ix, x, u, q, &i0, &i1, &rqm, &ilb2, e, \
+                    b, emf_size, emf_off, j, j_size, j_off, dx, &dt, ene); return 0;          \
+        case 2: ora_vadvance_deposit_2d_cyl_s2_##SFXN(ix, x, u, q, &i0, &i1, &rqm, &ilb2, e, \
+                    b, emf_size, emf_off, j, j_size, j_off, dx, &dt, ene); return 0;          \
+        case 3: ora_vadvance_deposit_2d_cyl_s3_##SFXN(ix, x, u, q, &i0, &i1, &rqm, &ilb2, e, \
+                    b, emf_size, emf_off, j, j_size, j_off, dx, &dt, ene); return 0;          \
+        case 4: ora_vadvance_deposit_2d_cyl_s4_##SFXN(ix, x, u, q, &i0, &i1, &rqm, &ilb2, e, \
+                    b, emf_size, emf_off, j, j_size, j_off, dx, &dt, ene); return 0;          \
+        }                                                                                     \
+        return -1;                                                                            \
+    }
+ORA_CYL_DISPATCH(f32, float)
+ORA_CYL_DISPATCH(f64, double)
+
 /* Philox4x32-10 (Salmon, Moraes, Dror and Shaw, "Parallel random numbers: as easy as 1, 2, 3",
  * SC11): the counter-based stream the thermal-bath re-emission below draws from. */
 static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1)

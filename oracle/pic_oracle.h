@@ -24,6 +24,15 @@ int ora_push_f64(int dim, int order, int *ix, double *x, double *u, double *q, i
                  double rqm, double *e, double *b, int *emf_size, int *emf_off, double *j,
                  int *j_size, int *j_off, double *dx, double dt, double *ene);
 
+/* the 2D cylindrical push + deposit (vadvance_deposit_2d_cyl_sK: x1 = z, x2 = r; ilb2 = the
+ * node's lower global cell along x2) */
+int ora_push_cyl_f32(int order, int *ix, float *x, float *u, float *q, int i0, int i1,
+                     float rqm, int ilb2, float *e, float *b, int *emf_size, int *emf_off,
+                     float *j, int *j_size, int *j_off, double *dx, double dt, double *ene);
+int ora_push_cyl_f64(int order, int *ix, double *x, double *u, double *q, int i0, int i1,
+                     double rqm, int ilb2, double *e, double *b, int *emf_size, int *emf_off,
+                     double *j, int *j_size, int *j_off, double *dx, double dt, double *ene);
+
 /* the same with the exact momentum update (push_type = "exact", dudt_exact) at tolerance tol */
 int ora_push_exact_f32(int dim, int order, int *ix, float *x, float *u, float *q, int i0, int i1,
                        float rqm, float *e, float *b, int *emf_size, int *emf_off, float *j,

@@ -21,7 +21,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_SRC = "/root/reference"
+# an OSIRIS source checkout, for building oracle/_ref (no default: set OSIRIS_REF)
+REFERENCE_SRC = os.environ.get("OSIRIS_REF", "")
 
 # guard cells required by each interpolation order (source/particles/os-particles.f03:321-360)
 GUARD = {1: (1, 2), 2: (2, 3), 3: (3, 4), 4: (4, 5)}
@@ -35,7 +36,8 @@ _ref = {}
 def build(with_ref: bool = True) -> None:
     """Compile the oracle (and, on x86_64 with the reference sources present, oracle/_ref)."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so", "liboracle_fast.so"], check=True)
-    if with_ref and platform.machine() in ("x86_64", "AMD64") and os.path.isdir(REFERENCE_SRC):
+    if (with_ref and platform.machine() in ("x86_64", "AMD64") and REFERENCE_SRC
+            and os.path.isdir(REFERENCE_SRC)):
         subprocess.run(["make", "-s", "-C", HERE, "ref", "OSIRIS_REF=" + REFERENCE_SRC],
                        check=True)
 
@@ -90,6 +92,9 @@ def _declare(L):
         getattr(L, f"ora_set_open_{s_}").argtypes = [I, P]
         getattr(L, f"ora_lindman_phase_{s_}").argtypes = [I, P, P, P, I, I, P, P, P, P, D]
     L.ora_set_thermal.argtypes = [I, P, P, C.c_uint32, C.c_uint64, I]
+    L.ora_push_cyl_f32.argtypes = [I, P, P, P, P, I, I, C.c_float, I, P, P, P, P, P, P, P, P, D,
+                                   P]
+    L.ora_push_cyl_f64.argtypes = [I, P, P, P, P, I, I, D, I, P, P, P, P, P, P, P, P, D, P]
     L.ora_push_pusher_f32.argtypes = [I, I, I, P, P, P, P, I, I, C.c_float, P, P, P, P, P, P, P,
                                       P, D, D, P]
     L.ora_push_pusher_f64.argtypes = [I, I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D, D,
@@ -203,6 +208,32 @@ def push(prec, dim, order, ix, x, u, q, i0, i1, rqm, e, b, j, emf_size, emf_off,
         a0, a1, rq, dtv = C.c_int(int(i0)), C.c_int(int(i1)), ctype(rqm), C.c_double(dt)
         f(_p(ix), _p(x), _p(u), _p(q), C.byref(a0), C.byref(a1), C.byref(rq), _p(e), _p(b),
           _p(es), _p(eo), _p(j), _p(es), _p(eo), _p(dxa), C.byref(dtv), _p(ene))
+    return float(ene[0])
+
+
+def push_cyl(prec, order, ix, x, u, q, i0, i1, rqm, ilb2, e, b, j, emf_size, emf_off, dx, dt,
+             impl="oracle"):
+    """One 2D cylindrical vadvance_deposit_2d_cyl_sK call (x1 = z, x2 = r; ilb2 = the lower
+    global cell of the node along x2); arrays updated in place; returns the energy sum."""
+    ene = np.zeros(1, dtype=np.float64)
+    es, eo = _i32(emf_size), _i32(emf_off)
+    dxa = _f64(list(dx) + [0.0] * (3 - len(dx)))
+    if impl == "oracle":
+        f = getattr(lib(), f"ora_push_cyl_{prec}")
+        rc = f(int(order), _p(ix), _p(x), _p(u), _p(q), int(i0), int(i1), rqm, int(ilb2),
+               _p(e), _p(b), _p(es), _p(eo), _p(j), _p(es), _p(eo), _p(dxa), float(dt), _p(ene))
+        if rc != 0:
+            raise ValueError("bad order")
+    else:
+        L = ref_lib(prec)
+        if L is None:
+            raise RuntimeError("reference kernels not built (oracle/_ref)")
+        f = getattr(L, f"vadvance_deposit_2d_cyl_s{order}_")
+        ctype = C.c_float if prec == "f32" else C.c_double
+        a0, a1, rq, dtv = C.c_int(int(i0)), C.c_int(int(i1)), ctype(rqm), C.c_double(dt)
+        lb = C.c_int(int(ilb2))
+        f(_p(ix), _p(x), _p(u), _p(q), C.byref(a0), C.byref(a1), C.byref(rq), C.byref(lb),
+          _p(e), _p(b), _p(es), _p(eo), _p(j), _p(es), _p(eo), _p(dxa), C.byref(dtv), _p(ene))
     return float(ene[0])
 
 

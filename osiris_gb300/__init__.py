@@ -83,6 +83,7 @@ def _declare(lb):
     lb.osg_last_error.restype = C.c_char_p
     lb.osg_version.restype = I
     lb.osg_device_count.restype = I
+    lb.osg_device_memory.argtypes = [P, P]
     lb.osg_host_alloc.argtypes = [C.c_size_t]
     lb.osg_host_alloc.restype = P
     lb.osg_host_free.argtypes = [P]
@@ -96,6 +97,10 @@ def _declare(lb):
                                            I, D, P]
     lb.osg_advance_deposit_f64.argtypes = [I, I, P, P, P, P, I, I, D, P, P, P, P, P, P, P, P, D,
                                            I, D, P]
+    lb.osg_vadvance_deposit_cyl_f32.argtypes = [I, P, P, P, P, I, I, F, I, P, P, P, P, P, P, P,
+                                                P, D, P]
+    lb.osg_vadvance_deposit_cyl_f64.argtypes = [I, P, P, P, P, I, I, D, I, P, P, P, P, P, P, P,
+                                                P, D, P]
     lb.osg_vadvance_deposit_noalloc_f32.argtypes = [I, I, P, P, P, P, I, I, F, P, P, P, P, P, P,
                                                     P, P, D, P]
     for s in ("f32", "f64"):
@@ -236,6 +241,27 @@ def vadvance_deposit(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_s
     return float(ene[0])
 
 
+def vadvance_deposit_cyl(order, ix, x, u, q, i0, i1, rqm, ilb2, efield, bfield, emf_size,
+                         emf_offset, j, j_size, j_offset, dx, dt):
+    """2D cylindrical push (x1 = z, x2 = r) of particles i0..i1 with the current added into
+    ``j``: FNAME(vadvance_deposit_2d_cyl_s<order>) (osg_vadvance_deposit_cyl_*); ilb2 is the
+    lower global cell along x2.  Returns the time-centred energy sum."""
+    prec = _prec(x)
+    dt_ = np.float32 if prec == "f32" else np.float64
+    _need(ix, np.int32, "ix")
+    for a, n in ((x, "x"), (u, "u"), (q, "q"), (j, "j")):
+        _need(a, dt_, n)
+    for a, n in ((efield, "efield"), (bfield, "bfield")):
+        if a.dtype != dt_ or not a.flags.c_contiguous:
+            raise TypeError(f"{n} must be C-contiguous {np.dtype(dt_)}")
+    ene = np.zeros(1)
+    _check(getattr(lib(), f"osg_vadvance_deposit_cyl_{prec}")(
+        int(order), _p(ix), _p(x), _p(u), _p(q), int(i0), int(i1), rqm, int(ilb2), _p(efield),
+        _p(bfield), _p(_i32(emf_size)), _p(_i32(emf_offset)), _p(j), _p(_i32(j_size)),
+        _p(_i32(j_offset)), _p(_f64(list(dx) + [0.0] * (3 - len(dx)))), float(dt), _p(ene)))
+    return float(ene[0])
+
+
 NOALLOC_SCRATCH_BYTES = 16 << 20
 
 
@@ -270,6 +296,17 @@ def lindman(dim, nx, gcl, gcu, axis, what, e, b, state, dx, dt):
     the E step, 1 after a B half step (dt the full step), 2 the restore of the boundary planes;
     `state` (15 reals per interior point of the other axes) is kept by the caller."""
     s = _prec(e)
+    dt_ = e.dtype
+    for a, n in ((e, "e"), (b, "b"), (state, "state")):
+        _need(a, dt_, n)
+    npts = 3 * int(np.prod([int(nx[d]) + int(gcl[d]) + int(gcu[d]) for d in range(dim)]))
+    if e.size != npts or b.size != npts:
+        raise ValueError(f"e and b must hold {npts} reals (3 x the guard-celled grid)")
+    if not 0 <= int(axis) < dim:
+        raise ValueError(f"axis {axis} outside 0..{dim - 1}")
+    nperp = int(np.prod([nx[d] for d in range(dim) if d != int(axis)])) if dim > 1 else 1
+    if state.size < 15 * nperp:
+        raise ValueError(f"state holds {state.size} reals, needs {15 * nperp}")
     _check(getattr(lib(), f"osg_lindman_{s}")(dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)),
                                               int(axis), int(what), _p(e), _p(b), _p(state),
                                               _p(_f64(list(dx) + [0.0] * 3)), float(dt)))
@@ -564,6 +601,13 @@ class Simulation:
         ms = F()
         _check(lib().osg_sim_time_steps(self.h, int(n), C.byref(ms)))
         return float(ms.value)
+
+
+def device_memory():
+    """(free, total) bytes of the current device (cudaMemGetInfo)."""
+    f, t = C.c_size_t(0), C.c_size_t(0)
+    _check(lib().osg_device_memory(C.byref(f), C.byref(t)))
+    return f.value, t.value
 
 
 def set_device(device):

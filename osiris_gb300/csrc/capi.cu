@@ -4,6 +4,9 @@
 //   osg_vadvance_deposit_*   replaces FNAME(vadvance_deposit_{1d,2d,3d}_s{1..4})
 //                            (source/simd/os-spec-push-avx2.c:255,471,1141;
 //                             source/simd/os-spec-push-avx2d.c:263,481,1127)
+//   osg_vadvance_deposit_cyl_*  replaces FNAME(vadvance_deposit_2d_cyl_s{1..4})
+//                            (source/simd/os-spec-push-avx2.c:762;
+//                             source/simd/os-spec-push-avx2d.c:777)
 //   osg_yee_advance_*        replaces advance_yee (source/emf/solver/os-emf-solver-yee.f03:542)
 //   osg_periodic_*           replaces update_periodic_vdf (source/vdf/os-vdf-comm.f90:142)
 //
@@ -100,7 +103,8 @@ template <typename T>
 static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int i1, T rqm,
                      const T *e, const T *b, const int *emf_size, const int *emf_off, T *j,
                      const int *j_size, const int *j_off, const double *dx, double dt,
-                     double *ene, int pusher = OSG_PUSHER_BORIS, double iter_tol = 1.0e-3)
+                     double *ene, int pusher = OSG_PUSHER_BORIS, double iter_tol = 1.0e-3,
+                     int cyl = 0, int ilb2 = 0)
 {
     OSG_CHECK(pusher >= OSG_PUSHER_BORIS && pusher <= OSG_PUSHER_COND_VAY &&
                   (pusher != OSG_PUSHER_EXACT || iter_tol > 0),
@@ -161,6 +165,11 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
                                                 (T *)d_j, j_size, j_off, dx, dt, d_ene, d_status);
         a.pusher = pusher;
         a.iter_tol = iter_tol;
+        if (cyl) {
+            a.cyl = 1;
+            a.cyl_gshift = (order == 1 || order == 3) ? (double)(ilb2 - 2)
+                                                      : (double)(ilb2 - 2) - 0.5;
+        }
         if (pusher >= OSG_PUSHER_VAY) a.tem = (T)pusher_tem(pusher, dt, (double)rqm);
         if ((rc = launch_plain_push<T>(dim, order, a, s_push))) return rc;
         OSG_CUDA(cudaGetLastError());
@@ -379,6 +388,13 @@ int osg_set_device(int device)
     return OSG_OK;
 }
 
+int osg_device_memory(size_t *free_bytes, size_t *total_bytes)
+{
+    OSG_CHECK(free_bytes && total_bytes, OSG_ERR_ARG, "null argument");
+    OSG_CUDA(cudaMemGetInfo(free_bytes, total_bytes));
+    return OSG_OK;
+}
+
 int osg_device_count(void)
 {
     int n = 0;
@@ -394,6 +410,30 @@ int osg_vadvance_deposit_f32(int dim, int order, int *ix, float *x, float *u, fl
 {
     return push_host<float>(dim, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_size,
                             emf_offset, j, j_size, j_offset, dx, dt, ene);
+}
+
+int osg_vadvance_deposit_cyl_f32(int order, int *ix, float *x, float *u, float *q, int i0,
+                                 int i1, float rqm, int ilb2, const float *efield,
+                                 const float *bfield, const int *emf_size,
+                                 const int *emf_offset, float *j, const int *j_size,
+                                 const int *j_offset, const double *dx, double dt, double *ene)
+{
+    OSG_CHECK(dx && dx[1] > 0, OSG_ERR_ARG, "dx[1] (the radial cell size) must be positive");
+    return push_host<float>(2, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_size,
+                            emf_offset, j, j_size, j_offset, dx, dt, ene, OSG_PUSHER_BORIS,
+                            1.0e-3, 1, ilb2);
+}
+
+int osg_vadvance_deposit_cyl_f64(int order, int *ix, double *x, double *u, double *q, int i0,
+                                 int i1, double rqm, int ilb2, const double *efield,
+                                 const double *bfield, const int *emf_size,
+                                 const int *emf_offset, double *j, const int *j_size,
+                                 const int *j_offset, const double *dx, double dt, double *ene)
+{
+    OSG_CHECK(dx && dx[1] > 0, OSG_ERR_ARG, "dx[1] (the radial cell size) must be positive");
+    return push_host<double>(2, order, ix, x, u, q, i0, i1, rqm, efield, bfield, emf_size,
+                             emf_offset, j, j_size, j_offset, dx, dt, ene, OSG_PUSHER_BORIS,
+                             1.0e-3, 1, ilb2);
 }
 
 int osg_vadvance_deposit_f64(int dim, int order, int *ix, double *x, double *u, double *q,

@@ -478,7 +478,29 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
                 }
             } else if constexpr (DIM == 2) {
                 T x1 = fmaR(v1, a.dtdx[0], x0[0]);
-                T y1 = fmaR(v2, a.dtdx[1], x0[1]);
+                T y1;
+                if (a.cyl) {
+                    // cylindrical radial move, in double as the reference (both precisions;
+                    // source/simd/os-spec-push-avx2d.c:1029-1065, os-spec-push-avx2.c:
+                    // 992-1080): from the global radius r_old the particle moves to
+                    // (r_old + v2 dt, v3 dt) in the (r, theta) plane; its new radius r_new
+                    // gives x2 (unchanged when r_new == r_old: cold plasma roundoff), and
+                    // p_r, p_theta turn onto the new radial direction (angular momentum
+                    // kept).  The deposit below keeps the Cartesian velocities.
+                    const double gix2 = (double)c[1] + a.cyl_gshift;
+                    const double r_old = ((double)x0[1] + gix2) * a.cyl_dr;
+                    const double x2n = fma((double)v2, a.dt_full, r_old);
+                    const double x3n = (double)v3 * a.dt_full;
+                    const double r_new = sqrt(fma(x2n, x2n, x3n * x3n));
+                    const double y1d = r_old == r_new ? (double)x0[1]
+                                                      : fma(r_new, a.cyl_rdr, -gix2);
+                    y1 = (T)y1d;
+                    const double tmp = 1.0 / r_new;
+                    a.u[3 * p + 1] = (T)(fma((double)u2, x2n, (double)u3 * x3n) * tmp);
+                    a.u[3 * p + 2] = (T)((double)u3 * (r_old * tmp));
+                } else {
+                    y1 = fmaR(v2, a.dtdx[1], x0[1]);
+                }
                 int dix = trim(x1), diy = trim(y1);
                 const int tb = store_position<T, 2>(a, p, 0, c[0] + dix, x1 - T(dix)) |
                                store_position<T, 2>(a, p, 1, c[1] + diy, y1 - T(diy));
@@ -571,6 +593,10 @@ PlainPushArgs<T> make_plain_args(int dim, int order, int *ix, T *x, T *u, const 
     a.qm = T(1) / rqm;
     a.rqm = rqm;
     a.dt_full = dt;
+    a.cyl = 0;
+    a.cyl_gshift = 0.0;
+    a.cyl_dr = dim > 1 ? dx[1] : 0.0;
+    a.cyl_rdr = dim > 1 ? 1.0 / dx[1] : 0.0;
     a.iter_tol = 1.0e-3;
     a.ene = d_ene;
     a.status = d_status;

@@ -40,7 +40,11 @@ template <typename T> struct PlainPushArgs {
     int pusher;            // OSG_PUSHER_*
     T qm;                  // 1 / rqm (exact pusher)
     T rqm;                 // the species' rqm (Euler-rotation pusher)
-    double dt_full;        // the double time step (exact pusher)
+    double dt_full;        // the double time step (exact pusher, cylindrical radial move)
+    int cyl;               // 1: 2D cylindrical (x1 = z, x2 = r): radial move and p_r, p_theta
+                           // correction in double (vadvance_deposit_2d_cyl_sK)
+    double cyl_gshift;     // global x2 cell of local cell 0: ilb2 - 2 (odd orders), - 2.5
+    double cyl_dr, cyl_rdr;   // dx2 and 1 / dx2
     double iter_tol;       // Newton tolerance of the exact pusher
     double *ene;           // device accumulator (incremented)
     int *status;           // device status word (OR of OSG_STATUS_*)

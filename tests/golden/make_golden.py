@@ -2,7 +2,7 @@
 
 Run from the repository root on an x86_64 machine that has the OSIRIS sources:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <osiris checkout>     # or OSIRIS_REF=<checkout>
 
 It builds ``oracle/_ref/libref_{f32,f64}.so`` from ``source/simd/os-spec-push-c.c`` and
 ``source/simd/os-spec-current-c.c`` of the reference (``make -C oracle ref``), runs every
@@ -13,6 +13,11 @@ The single-precision 3D cubic and quartic reference kernels deposit z planes at 
 (source/simd/os-spec-current-avx2.c:1096 and :1118 use ``k3*Dy`` where the other orders use
 ``k3*Dz``), so for those two fixtures the current is also computed with the double-precision
 reference on the same inputs (``j_ref64``), and the parity test uses that.
+
+The 2D cylindrical entry points ``vadvance_deposit_2d_cyl_s{1..4}_`` (x1 = z, x2 = r, with the
+node's lower global cell ``ilb2`` along x2) give ``push_2dcyl_s<order>_<prec>.npz`` on the same
+kind of input, with the particles kept off the axis (``ilb2`` = 3) and large azimuthal
+momenta, so the angular-momentum correction is exercised (``--cyl`` regenerates only these).
 
 A second set, ``mt_kat.npz``, holds the first draws of the OSIRIS-seeded Mersenne Twister for
 two seeds, computed with the C++ standard library's ``std::mt19937`` (an independent
@@ -64,6 +69,36 @@ def make_case(prec, dim, order, seed):
     return g, e, b, ix, x, u, q, rqm
 
 
+CYL_ILB2 = 3
+
+
+def run_ref_cyl(prec, order, g, e, b, ix, x, u, q, rqm):
+    a = [po.aligned_copy(v) for v in (ix, x, u, q)]
+    j = po.aligned(g.shape, po.dtype_of(prec))
+    ee, bb = po.aligned_copy(e), po.aligned_copy(b)
+    ene = po.push_cyl(prec, order, a[0], a[1], a[2], a[3], 1, NP, rqm, CYL_ILB2, ee, bb, j,
+                      g.size, g.gcl, g.dx, DT, impl="ref")
+    return a, j, ene
+
+
+def cyl_fixtures():
+    seed = 300
+    for prec in ("f64", "f32"):
+        for order in (1, 2, 3, 4):
+            seed += 1
+            g, e, b, ix, x, u, q, rqm = make_case(prec, 2, order, seed)
+            u[:NP, 2] *= 3.0            # strong azimuthal motion: the p_theta correction
+            a, j, ene = run_ref_cyl(prec, order, g, e, b, ix, x, u, q, rqm)
+            np.savez_compressed(
+                os.path.join(OUT, f"push_2dcyl_s{order}_{prec}.npz"),
+                nx=np.array(g.nx), dx=np.array(g.dx), dt=np.array(DT), np_=np.array(NP),
+                rqm=np.array(rqm), order=np.array(order), ilb2=np.array(CYL_ILB2),
+                e=e, b=b, ix_in=ix[:NP], x_in=x[:NP], u_in=u[:NP], q_in=q[:NP],
+                ix_out=np.asarray(a[0])[:NP], x_out=np.asarray(a[1])[:NP],
+                u_out=np.asarray(a[2])[:NP], j_out=np.asarray(j), ene=np.array(ene))
+            print(f"push_2dcyl_s{order}_{prec}.npz  ene={ene!r}")
+
+
 def run_ref(prec, dim, order, g, e, b, ix, x, u, q, rqm):
     a = [po.aligned_copy(v) for v in (ix, x, u, q)]
     j = po.aligned(g.shape, po.dtype_of(prec))
@@ -101,9 +136,17 @@ int main(){
 
 
 def main():
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    if args:
+        po.REFERENCE_SRC = args[0]
+    if not po.REFERENCE_SRC:
+        raise SystemExit("give the OSIRIS source checkout as the argument or in OSIRIS_REF")
     po.build(with_ref=True)
     if po.ref_lib("f64") is None or po.ref_lib("f32") is None:
         raise SystemExit("reference kernels could not be built (needs x86_64 + AVX2 + sources)")
+    if "--cyl" in sys.argv:
+        cyl_fixtures()
+        return
     seed = 100
     for prec in ("f64", "f32"):
         for dim in (1, 2, 3):
@@ -127,6 +170,7 @@ def main():
                     u_out=np.asarray(a[2])[:NP], j_out=np.asarray(j), ene=np.array(ene),
                     **extra)
                 print(f"push_{dim}d_s{order}_{prec}.npz  ene={ene!r}")
+    cyl_fixtures()
     mt_kat()
     print("mt_kat.npz")
 

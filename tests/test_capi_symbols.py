@@ -35,9 +35,15 @@ def test_main_library_exports(built):
 @pytest.mark.parametrize("prec", ["single", "double"])
 def test_fortran_shim_exports(built, prec):
     import osiris_gb300 as osg
-    names = _declared("osiris_gb300_fortran.h", r"OSG_FORTRAN_PUSH_DECL\((vadvance_deposit_\w+)\)")
+    names = _declared("osiris_gb300_fortran.h",
+                      r"OSG_FORTRAN_PUSH(?:_CYL)?_DECL\((vadvance_deposit_\w+)\)")
+    # every symbol the reference's Fortran bridge calls (source/spec/os-spec-vpush.f03:70-95,
+    # 144-169, 217-246, 294-319): 1d, 2d, 2d_cyl and 3d, orders 1-4
+    bridge = [f"vadvance_deposit_{g}_s{o}_" for g in ("1d", "2d", "2d_cyl", "3d")
+              for o in (1, 2, 3, 4)]
+    assert sorted(bridge) == names
     names += ["osg_fortran_status"]
-    assert len(names) == 13
+    assert len(names) == 17
     lb = ctypes.CDLL(os.path.join(osg.HERE, f"libosiris_gb300_{prec}.so"))
     missing = [n for n in names if not hasattr(lb, n)]
     assert not missing, missing

@@ -1,6 +1,7 @@
 """GPU parity of the drop-in push/deposit entry point (osg_vadvance_deposit_*, the C ABI that
-replaces FNAME(vadvance_deposit_{1d,2d,3d}_sN)) against the reference's own kernel outputs
-(golden fixtures) and against the CPU oracle.
+replaces FNAME(vadvance_deposit_{1d,2d,3d}_sN), and osg_vadvance_deposit_cyl_* for
+FNAME(vadvance_deposit_2d_cyl_sN)) against the reference's own kernel outputs (golden
+fixtures) and against the CPU oracle.
 
 Tolerances: particle positions, cell indices and momenta bit-identical (same roundings as the
 reference); current normwise max|a-b|/max|b| <= 1e-12 (FP64) and <= 1e-5 (FP32), the
@@ -15,7 +16,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = sorted(glob.glob(os.path.join(GOLD, "push_*.npz")))
+CASES = sorted(p for p in glob.glob(os.path.join(GOLD, "push_*.npz")) if "2dcyl" not in p)
+CYL = sorted(glob.glob(os.path.join(GOLD, "push_2dcyl_*.npz")))
 TOL_J = {"f32": 1e-5, "f64": 1e-12}
 TOL_E = {"f32": 1e-6, "f64": 1e-12}
 
@@ -55,6 +57,54 @@ def test_gpu_push_matches_reference_fixture(osg, path):
     jref = f["j_ref64"] if "j_ref64" in f.files else f["j_out"]
     assert _nerr(j, jref) <= TOL_J[prec]
     assert abs(ene - float(f["ene"])) <= TOL_E[prec] * abs(float(f["ene"]))
+
+
+@pytest.mark.parametrize("path", CYL, ids=[os.path.basename(p)[5:-4] for p in CYL])
+def test_gpu_cyl_push_matches_reference_fixture(osg, path):
+    f = np.load(path)
+    prec = "f32" if path.endswith("_f32.npz") else "f64"
+    order = int(f["order"])
+    gl, gu = osg.GUARD[order]
+    size = [n + gl + gu for n in f["nx"]]
+    ix, x, u, q = (np.array(f[k]) for k in ("ix_in", "x_in", "u_in", "q_in"))
+    j = np.zeros_like(f["e"])
+    ene = osg.vadvance_deposit_cyl(order, ix, x, u, q, 1, len(q), float(f["rqm"]),
+                                   int(f["ilb2"]), f["e"], f["b"], size, [gl] * 2, j, size,
+                                   [gl] * 2, list(f["dx"]), float(f["dt"]))
+    assert np.array_equal(ix, f["ix_out"])
+    assert np.array_equal(x, f["x_out"])
+    assert np.array_equal(u, f["u_out"])
+    assert _nerr(j, f["j_out"]) <= TOL_J[prec]
+    assert abs(ene - float(f["ene"])) <= TOL_E[prec] * abs(float(f["ene"]))
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_gpu_cyl_push_matches_oracle_subrange(osg, oracle, prec, order):
+    """A warm plasma off the axis (ilb2 = 4), pushing the sub-range [i0, i1] only, against the
+    oracle's cylindrical push on the same arrays."""
+    nx, dx = [12, 10], [0.1, 0.12]
+    g = oracle.Grid(nx, order, dx)
+    rng = np.random.default_rng(40 + order)
+    dt_ = np.float32 if prec == "f32" else np.float64
+    r = oracle.mt_new(12)
+    ix, x, u, q = oracle.load(r, prec, 2, nx, [2, 2], dx, -1.0, [0.6] * 3, [0.1, 0.0, 0.3])
+    e = (rng.standard_normal(g.shape) * 0.3).astype(dt_)
+    b = (rng.standard_normal(g.shape) * 0.3).astype(dt_)
+    n = len(q)
+    i0, i1 = 5, n - 3
+    a = [v.copy() for v in (ix, x, u, q)]
+    j_g = g.zeros(prec)
+    ene_g = osg.vadvance_deposit_cyl(order, *a, i0, i1, -1.0, 4, e, b, g.size, g.gcl, j_g,
+                                     g.size, g.gcl, dx, 0.04)
+    o = [v.copy() for v in (ix, x, u, q)]
+    j_o = g.zeros(prec)
+    ene_o = oracle.push_cyl(prec, order, *o, i0, i1, -1.0, 4, e, b, j_o, g.size, g.gcl, dx,
+                            0.04)
+    for k in range(3):
+        assert np.array_equal(a[k], o[k]), k
+    assert _nerr(j_g, j_o) <= TOL_J[prec]
+    assert abs(ene_g - ene_o) <= TOL_E[prec] * abs(ene_o)
 
 
 @pytest.mark.parametrize("prec", ["f32", "f64"])
