@@ -16,6 +16,9 @@ JSON line keys beyond the base contract:
                 (osg_vadvance_deposit_f32 per species, osg_periodic, osg_yee_advance) on pinned
                 host buffers, every copy inside the timed region
   fp64_plain    the plain FP64 engine on the same workload (the "plain FP64 GPU form")
+  fp64_error    normwise difference of E, B, J and the relative difference of the kinetic and
+                field energies between the mixed-precision (tiled FP32) and the plain FP64
+                engine after the same number of steps from the same load
 --impl reference times the CPU oracle port (the reference's CPU path restated; the
 reference's own AVX2 kernels do not build on this Arm host) with all host threads.
 """
@@ -60,16 +63,11 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per push launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "push_tiled_c2.md")
-    try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1].split()[0])
-    except OSError:
-        pass
-    return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one full-size push launch of this
+# workload, from one ncu capture (one metric pass, --clock-control none) of the current kernel;
+# the command and the figures are in profiles/push_tiled_c2.md.  None when no capture matches
+# the kernel as built.
+PUSH_TRAFFIC_BYTES = 1129720832
 
 
 class Clocks:
@@ -169,55 +167,10 @@ def cpu_oracle_rate(target_s, nthreads, steps=None):
 
 
 def e2e_host(osg, sp_host, steps):
-    """Drop-in flow on host buffers, as an unchanged OSIRIS host would drive the library: field
-    guard replace, per species osg_vadvance_deposit_f32 and the periodic particle boundary,
-    current fold and Yee through the host-array C ABI (all copies in the timed part)."""
+    """Drop-in flow on host buffers (osiris_gb300.run.dropin_steps), all copies timed."""
+    from osiris_gb300.run import dropin_steps
     w = WORKLOAD
-    nx, order = w["nx"], w["order"]
-    gl, gu = osg.GUARD[order]
-    size = [n + gl + gu for n in nx]
-    shape = tuple(reversed(size)) + (3,)
-    e = osg.pinned_empty(shape, np.float32)
-    b = osg.pinned_empty(shape, np.float32)
-    j = osg.pinned_empty(shape, np.float32)
-    e[...] = 0
-    b[...] = 0
-    pin = []
-    for ix, x, u, q in sp_host:
-        arrs = []
-        for a in (ix, x, u, q):
-            p = osg.pinned_empty(a.shape, a.dtype)
-            p[...] = a
-            arrs.append(p)
-        pin.append(arrs)
-    npart = sum(len(s[3]) for s in sp_host)
-    gbytes = int(np.prod(shape)) * 4
-
-    def one_step():
-        osg.periodic(2, nx, [gl] * 2, [gu] * 2, e, 0)
-        osg.periodic(2, nx, [gl] * 2, [gu] * 2, b, 0)
-        j[...] = 0
-        for ix, x, u, q in pin:
-            osg.vadvance_deposit(2, order, ix, x, u, q, 1, len(q), -1.0, e, b, size, [gl] * 2, j,
-                                 size, [gl] * 2, w["dx"], w["dt"])
-            osg.particle_wrap(nx, ix)
-        osg.periodic(2, nx, [gl] * 2, [gu] * 2, j, 1)
-        osg.yee_advance(2, nx, [gl] * 2, [gu] * 2, e, b, j, w["dx"], w["dt"])
-
-    one_step()
-    t = time.perf_counter()
-    for _ in range(steps):
-        one_step()
-    el = time.perf_counter() - t
-    # bytes moved per step (counted from the arrays each call copies)
-    h2d = 2 * gbytes + sum(len(p[3]) * 32 + 3 * gbytes for p in pin) + gbytes + 3 * gbytes
-    d2h = 2 * gbytes + sum(len(p[3]) * 28 + gbytes + 12 for p in pin) + gbytes + 2 * gbytes
-    for arrs in pin:
-        for a in arrs:
-            osg.pinned_free(a)
-    for a in (e, b, j):
-        osg.pinned_free(a)
-    return npart * steps / el, h2d, d2h, steps
+    return dropin_steps(sp_host, w["nx"], w["dx"], w["dt"], w["order"], steps)
 
 
 def run_native(args):
@@ -268,7 +221,7 @@ def run_native(args):
     peak, peak_kind = peaks()
     push_bytes = npart * BYTES_PER_PARTICLE + ncell * BYTES_PER_CELL_PUSH
     achieved = push_bytes / (prof["push"] * 1e-3) / 1e9
-    traffic = profile_traffic()
+    traffic = PUSH_TRAFFIC_BYTES
     # plain FP64 GPU form on the same workload
     sp64 = load_species(osg, 64)
     sim64 = osg.Simulation(w["nx"], w["dx"], w["dt"], order=w["order"], precision=64,
@@ -278,8 +231,25 @@ def run_native(args):
     sim64.step(3)
     n64 = max(10, min(args.steps, 50))
     ms64 = sim64.time_steps(n64)
-    sim64.close()
     v64 = npart * n64 / (ms64 / 1e3)
+    # error of the mixed-precision result against the FP64 build: the tiled FP32 engine from
+    # the same load, run for the same number of steps as the FP64 engine above
+    n_err = 3 + n64
+    sim32 = osg.Simulation(w["nx"], w["dx"], w["dt"], order=w["order"], precision=32,
+                           engine=osg.ENGINE_TILED, capacity=4.0)
+    for s in sp:
+        sim32.add_species(-1.0, *s)
+    sim32.step(n_err)
+    fp64_error = {"steps": n_err, "norm": "max|mixed - fp64| / max|fp64| over the grid"}
+    f32, f64 = sim32.fields(), sim64.fields()
+    for name, a, b in (("E", f32[0], f64[0]), ("B", f32[1], f64[1]), ("J", f32[2], f64[2])):
+        fp64_error[name] = float(np.abs(a.astype(np.float64) - b).max() / np.abs(b).max())
+    k32, fl32 = sim32.energy()
+    k64, fl64 = sim64.energy()
+    fp64_error["kinetic"] = float(abs(k32.sum() - k64.sum()) / abs(k64.sum()))
+    fp64_error["field"] = float(abs(fl32.sum() - fl64.sum()) / abs(fl64.sum()))
+    sim32.close()
+    sim64.close()
     # end to end through the host-array C ABI
     e2e_v, h2d, d2h, e2e_steps = e2e_host(osg, sp, max(3, min(args.steps, 10)))
     # CPU baseline (oracle port) on rank 0
@@ -309,6 +279,7 @@ def run_native(args):
                         "osg_periodic x3, osg_yee_advance; pinned host buffers"},
         "fp64_plain": {"value": v64, "unit": METRIC, "steps": n64,
                        "ratio_mixed_over_fp64": value / world / v64},
+        "fp64_error": fp64_error,
         "gpu_launches": launches,
         "tile_occupancy_max": occupancy,
         "clocks": clk.summary(),

@@ -16,7 +16,10 @@ neutralising background):
               {64^2, 128^2, 256^2, 512^2}, ppc from {4, 16, 64}, uth uniform in [0.01, 0.2]
               (MT19937 seed 4), quadratic, dx 0.05, dt 0.035, tile shape and CTA size
               autotuned (--boxes N takes the first N boxes)
-Prints one JSON line per run with the device time per step and the energies.
+Prints one JSON line per run with the device time per step and the energies.  --dropin (2D
+configurations) times the host-array drop-in flow instead, as an unchanged OSIRIS host drives
+it: per species osg_vadvance_deposit_f32 and the particle wrap, guard updates and Yee on host
+arrays, every copy included.
 """
 from __future__ import annotations
 
@@ -124,6 +127,59 @@ def build_batch(nbox=64, tile=None, threads=0):
     return bt, n
 
 
+def dropin_steps(sp_host, nx, dx, dt, order, steps):
+    """Drop-in flow on host buffers, as an unchanged OSIRIS host would drive the library: field
+    guard replace, per species osg_vadvance_deposit_f32 and the periodic particle boundary,
+    current fold and Yee through the host-array C ABI (2D, FP32; every copy inside the timed
+    part).  sp_host: per species (ix, x, u, q) host arrays, rqm -1.  Returns particle-steps/s,
+    the host-to-device and device-to-host bytes per step (counted from the arrays each call
+    copies) and the number of timed steps."""
+    gl, gu = osg.GUARD[order]
+    size = [n + gl + gu for n in nx]
+    shape = tuple(reversed(size)) + (3,)
+    e = osg.pinned_empty(shape, np.float32)
+    b = osg.pinned_empty(shape, np.float32)
+    j = osg.pinned_empty(shape, np.float32)
+    e[...] = 0
+    b[...] = 0
+    pin = []
+    for ix, x, u, q in sp_host:
+        arrs = []
+        for a in (ix, x, u, q):
+            p = osg.pinned_empty(a.shape, a.dtype)
+            p[...] = a
+            arrs.append(p)
+        pin.append(arrs)
+    npart = sum(len(s[3]) for s in sp_host)
+    gbytes = int(np.prod(shape)) * 4
+
+    def one_step():
+        osg.periodic(2, nx, [gl] * 2, [gu] * 2, e, 0)
+        osg.periodic(2, nx, [gl] * 2, [gu] * 2, b, 0)
+        j[...] = 0
+        for ix, x, u, q in pin:
+            osg.vadvance_deposit(2, order, ix, x, u, q, 1, len(q), -1.0, e, b, size, [gl] * 2, j,
+                                 size, [gl] * 2, dx, dt)
+            osg.particle_wrap(nx, ix)
+        osg.periodic(2, nx, [gl] * 2, [gu] * 2, j, 1)
+        osg.yee_advance(2, nx, [gl] * 2, [gu] * 2, e, b, j, dx, dt)
+
+    one_step()
+    t = time.perf_counter()
+    for _ in range(steps):
+        one_step()
+    el = time.perf_counter() - t
+    # bytes moved per step (counted from the arrays each call copies)
+    h2d = 2 * gbytes + sum(len(p[3]) * 32 + 3 * gbytes for p in pin) + gbytes + 3 * gbytes
+    d2h = 2 * gbytes + sum(len(p[3]) * 28 + gbytes + 12 for p in pin) + gbytes + 2 * gbytes
+    for arrs in pin:
+        for a in arrs:
+            osg.pinned_free(a)
+    for a in (e, b, j):
+        osg.pinned_free(a)
+    return npart * steps / el, h2d, d2h, steps
+
+
 def run_batch(args):
     t0 = time.time()
     bt, npart = build_batch(args.boxes, args.tile, args.threads or 0)
@@ -153,6 +209,10 @@ def main():
     ap.add_argument("--engine", choices=["tiled", "plain"])
     ap.add_argument("--precision", type=int, choices=[32, 64])
     ap.add_argument("--tile", type=int, nargs="+")
+    ap.add_argument("--dropin", action="store_true",
+                    help="2D configurations: time the host-array drop-in flow instead "
+                         "(osg_vadvance_deposit_f32 per species, guard updates and Yee on "
+                         "host arrays, all copies included)")
     args = ap.parse_args()
     if args.config == "batch":
         run_batch(args)
@@ -173,6 +233,17 @@ def main():
         sim.close()
         return
     cfg = CONFIGS[args.config]
+    if args.dropin:
+        nx = args.nx or cfg["nx"]
+        r = osg.Rng(cfg["seed"])
+        sp = [osg.load_lattice(r, 32, nx, cfg["ppc"], cfg["dx"], -1.0, [s["uth"]] * 3,
+                               s["ufl"], cfg["amp"], 1.0) for s in cfg["species"]]
+        rate, h2d, d2h, n = dropin_steps(sp, nx, cfg["dx"], cfg["dt"], cfg["order"], args.steps)
+        print(json.dumps(dict(config=args.config, path="host-array drop-in", nx=nx,
+                              particles=sum(len(s[3]) for s in sp), steps=n,
+                              particle_steps_per_s=rate, h2d_bytes_per_step=h2d,
+                              d2h_bytes_per_step=d2h)))
+        return
     t0 = time.time()
     sim, npart = build_sim(cfg, args.engine, args.precision, args.tile, args.nx)
     t_load = time.time() - t0

@@ -8,7 +8,10 @@ plain engine from the same seeded load.
   400 steps, 1e-10 in FP64);
 * the transverse magnetic energy (B1^2 + B2^2) grows at the same rate in both engines (log-
   linear fit over its growth phase, within 10%);
-* the total energy histories differ by less than 5e-3 of the initial total.
+* the total energy histories differ by less than 5e-3 of the initial total;
+* against the CPU oracle (the reference's CPU path restated, run in FP64 on the same load):
+  the FP32 tiled growth rate within 10% and its energy history within 5e-3, the FP64 plain
+  engine's growth rate within 1e-3 and its energy history within 1e-5.
 """
 import numpy as np
 import pytest
@@ -52,10 +55,33 @@ def _history(osg, prec, engine):
     return np.array(bt), np.array(tot), g0, np.array(gauss)
 
 
+def _oracle_history(oracle):
+    """The same run on the CPU oracle in FP64: transverse B energy and total energy every
+    EVERY steps."""
+    r = oracle.mt_new(3)
+    sp = []
+    for s in (1.0, -1.0):
+        ix, x, u, q = oracle.load(r, "f64", 3, NX, PPC, DX, -1.0, [0.05] * 3, [0.0, 0.0, s * 0.5])
+        sp.append(dict(ix=ix, x=x, u=u, q=q, rqm=-1.0))
+    g = oracle.Grid(NX, 3, DX)
+    e, b, j = g.zeros("f64"), g.zeros("f64"), g.zeros("f64")
+    dv = float(np.prod(DX))
+    nthr = oracle.max_threads()
+    bt, tot = [], []
+    for i in range(STEPS):
+        ene = oracle.step(g, "f64", e, b, j, sp, DT, nthreads=nthr)
+        if (i + 1) % EVERY == 0:
+            fe, fb = oracle.field_energy(g, "f64", e), oracle.field_energy(g, "f64", b)
+            bt.append(fb[0] + fb[1])
+            tot.append(float((ene * -1.0 * dv).sum() + fe.sum() + fb.sum()))
+    return np.array(bt), np.array(tot)
+
+
 @pytest.fixture(scope="module")
-def runs(osg):
+def runs(osg, oracle):
     return {"fp32": _history(osg, 32, osg.ENGINE_TILED),
-            "fp64": _history(osg, 64, osg.ENGINE_PLAIN)}
+            "fp64": _history(osg, 64, osg.ENGINE_PLAIN),
+            "oracle": _oracle_history(oracle)}
 
 
 def _growth(b):
@@ -91,3 +117,21 @@ def test_weibel_energy_history_matches_fp64(runs):
     print(f"total energy drift: FP32 tiled max {np.abs(d32).max():.3e}  "
           f"FP64 plain max {np.abs(d64).max():.3e}  max difference {np.abs(d32 - d64).max():.3e}")
     assert np.abs(d32 - d64).max() < 5e-3
+
+
+def test_weibel_growth_rate_and_energy_match_oracle(runs):
+    go, so = _growth(runs["oracle"][0])
+    g32, _ = _growth(runs["fp32"][0])
+    g64, _ = _growth(runs["fp64"][0])
+    to = runs["oracle"][1]
+    do = to / to[0] - 1.0
+    d32 = np.abs(runs["fp32"][1] / runs["fp32"][1][0] - 1.0 - do).max()
+    d64 = np.abs(runs["fp64"][1] / runs["fp64"][1][0] - 1.0 - do).max()
+    print(f"Weibel growth rate: oracle FP64 {go:.5f} (window {so[0]}-{so[-1]})  FP32 tiled "
+          f"{g32:.5f}  FP64 plain {g64:.5f}; energy history difference FP32 {d32:.3e}  "
+          f"FP64 {d64:.3e}")
+    assert go > 0.1
+    assert abs(g32 / go - 1.0) < 0.10
+    assert abs(g64 / go - 1.0) < 1e-3
+    assert d32 < 5e-3
+    assert d64 < 1e-5

@@ -6,8 +6,11 @@ pool allocator, or device memory is budgeted once before stepping): its device s
 fixed array inside the library.  Two calls in a row must each reproduce the regular entry point
 (bit-identical particles, current within the FP32 tolerance 1e-5 normwise, energy within 1e-6)
 -- the second call checks that nothing left in the shared array by the first leaks through --
-and a call too large for the array must be rejected with a clear error before any GPU work.
-This file is collected last so that a stop-at-first-failure run has run everything else first.
+and the second call must leave the device's free memory unchanged (nothing allocated).  A call
+just under the documented size limit (8*dim + 16 bytes per particle plus three grid copies)
+must succeed; one too large for the array must be rejected with a clear error before any GPU
+work.  This file is collected last so that a stop-at-first-failure run has run everything else
+first.
 """
 import numpy as np
 import pytest
@@ -53,8 +56,13 @@ def test_noalloc_matches_regular_entry_point_twice(osg, dim, order, nx, ppc):
         i0, i1 = 3, n - 2
         a = [v.copy() for v in parts]
         ja = j0.copy()
+        free0 = osg.device_memory()[0]
         ene_a = osg.vadvance_deposit_noalloc(dim, order, *a, i0, i1, -1.0, e, b, size, off, ja,
                                              size, off, [0.1] * dim, 0.04)
+        if call == 1:
+            # the first call set up the array's address (and loaded the kernels); the second
+            # may not take any device memory
+            assert osg.device_memory()[0] == free0, "the no-allocation entry point allocated"
         r = [v.copy() for v in parts]
         jr = j0.copy()
         ene_r = osg.vadvance_deposit(dim, order, *r, i0, i1, -1.0, e, b, size, off, jr, size,
@@ -65,13 +73,45 @@ def test_noalloc_matches_regular_entry_point_twice(osg, dim, order, nx, ppc):
         assert abs(ene_a - ene_r) <= 1e-6 * abs(ene_r), call
 
 
+def _limit_particles(osg, size, dim):
+    """Largest particle count one call can carry with this grid (8*dim + 16 bytes per particle,
+    three 256-byte-aligned grid copies, 256 bytes of counters, 256-byte alignment of the four
+    particle arrays)."""
+    a256 = lambda n: (n + 255) // 256 * 256
+    grid = a256(4 * 3 * int(np.prod(size)))
+    room = osg.NOALLOC_SCRATCH_BYTES - 256 - 3 * grid - 4 * 255
+    return room // (8 * dim + 16)
+
+
+def test_noalloc_accepts_a_call_just_under_its_limit(osg):
+    size = [13, 13]
+    n = _limit_particles(osg, size, 2)
+    rng = np.random.default_rng(5)
+    ix = rng.integers(1, 9, (n, 2)).astype(np.int32)
+    x = (rng.random((n, 2)) - 0.5).astype(np.float32)
+    u = (rng.standard_normal((n, 3)) * 0.1).astype(np.float32)
+    q = np.full(n, -1e-3, np.float32)
+    g = (rng.standard_normal((13, 13, 3)) * 0.1).astype(np.float32)
+    a = [v.copy() for v in (ix, x, u, q)]
+    ja = np.zeros_like(g)
+    osg.vadvance_deposit_noalloc(2, 2, *a, 1, n, -1.0, g, g, size, [2, 2], ja, size, [2, 2],
+                                 [0.1, 0.1], 0.04)
+    r = [v.copy() for v in (ix, x, u, q)]
+    jr = np.zeros_like(g)
+    osg.vadvance_deposit(2, 2, *r, 1, n, -1.0, g, g, size, [2, 2], jr, size, [2, 2],
+                         [0.1, 0.1], 0.04)
+    for k in range(3):
+        assert np.array_equal(a[k], r[k]), k
+    assert _nerr(ja, jr) <= 1e-5
+
+
 def test_noalloc_rejects_calls_larger_than_its_array(osg):
-    n = osg.NOALLOC_SCRATCH_BYTES // 16            # needs > 28 bytes per 2D particle
+    size = [13, 13]
+    n = _limit_particles(osg, size, 2) + 64        # 32 bytes per 2D particle: past the limit
     ix = np.ones((n, 2), np.int32) * 4
     x = np.zeros((n, 2), np.float32)
     u = np.zeros((n, 3), np.float32)
     q = np.zeros(n, np.float32)
-    size = [13, 13]
     g = np.zeros((13, 13, 3), np.float32)
     with pytest.raises(osg.OsirisGB300Error) as err:
         osg.vadvance_deposit_noalloc(2, 2, ix, x, u, q, 1, n, -1.0, g, g, size, [2, 2],
