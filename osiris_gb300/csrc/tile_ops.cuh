@@ -227,112 +227,6 @@ __device__ __forceinline__ void seg_values2_fast(const Seg2<float> &g, float q, 
     }
 }
 
-template <int ORD>
-__device__ __forceinline__ void seg_values3(const Seg3<float> &g, float q, const float *jn,
-                                            float *v)
-{
-    constexpr int NP = ORD + 1;
-    float s0x[NP], s1x[NP], s0y[NP], s1y[NP], s0z[NP], s1z[NP];
-    float wl1[ORD], wl2[ORD], wl3[ORD];
-    spline<ORD>(g.x0, s0x);
-    spline<ORD>(g.x1, s1x);
-    spline<ORD>(g.y0, s0y);
-    spline<ORD>(g.y1, s1y);
-    spline<ORD>(g.z0, s0z);
-    spline<ORD>(g.z1, s1z);
-    long_weights<ORD>(q * jn[0], g.x0, g.x1, wl1);
-    long_weights<ORD>(q * jn[1], g.y0, g.y1, wl2);
-    long_weights<ORD>(q * jn[2], g.z0, g.z1, wl3);
-    int n = 0;
-#pragma unroll
-    for (int k3 = 0; k3 < NP; k3++)
-#pragma unroll
-        for (int k2 = 0; k2 < NP; k2++) {
-            float t1 = s0y[k2] * s0z[k3], t2 = s0y[k2] * s1z[k3];
-            t1 = fmaf(s1y[k2], s1z[k3], t1);
-            t2 = fmaf(s1y[k2], s0z[k3], t2);
-            const float wp = fmaf(0.5f, t2, t1);
-#pragma unroll
-            for (int k1 = 0; k1 < ORD; k1++) v[n++] = wl1[k1] * wp;
-        }
-#pragma unroll
-    for (int k3 = 0; k3 < NP; k3++)
-#pragma unroll
-        for (int k2 = 0; k2 < ORD; k2++)
-#pragma unroll
-            for (int k1 = 0; k1 < NP; k1++) {
-                float t1 = s0x[k1] * s0z[k3], t2 = s0x[k1] * s1z[k3];
-                t1 = fmaf(s1x[k1], s1z[k3], t1);
-                t2 = fmaf(s1x[k1], s0z[k3], t2);
-                v[n++] = wl2[k2] * fmaf(0.5f, t2, t1);
-            }
-#pragma unroll
-    for (int k3 = 0; k3 < ORD; k3++)
-#pragma unroll
-        for (int k2 = 0; k2 < NP; k2++)
-#pragma unroll
-            for (int k1 = 0; k1 < NP; k1++) {
-                float t1 = s0x[k1] * s0y[k2], t2 = s0x[k1] * s1y[k2];
-                t1 = fmaf(s1x[k1], s1y[k2], t1);
-                t2 = fmaf(s1x[k1], s0y[k2], t2);
-                v[n++] = wl3[k3] * fmaf(0.5f, t2, t1);
-            }
-}
-
-// direct shared-memory accumulation of one 3D segment (pj = stencil origin)
-template <int ORD>
-__device__ __forceinline__ void seg_atomic3(float *pj, const Seg3<float> &g, float q,
-                                            const float *jn, int jsy, int jsz)
-{
-    constexpr int NP = ORD + 1;
-    float s0x[NP], s1x[NP], s0y[NP], s1y[NP], s0z[NP], s1z[NP];
-    float wl1[ORD], wl2[ORD], wl3[ORD];
-    spline<ORD>(g.x0, s0x);
-    spline<ORD>(g.x1, s1x);
-    spline<ORD>(g.y0, s0y);
-    spline<ORD>(g.y1, s1y);
-    spline<ORD>(g.z0, s0z);
-    spline<ORD>(g.z1, s1z);
-    long_weights<ORD>(q * jn[0], g.x0, g.x1, wl1);
-    long_weights<ORD>(q * jn[1], g.y0, g.y1, wl2);
-    long_weights<ORD>(q * jn[2], g.z0, g.z1, wl3);
-#pragma unroll
-    for (int k3 = 0; k3 < NP; k3++)
-#pragma unroll
-        for (int k2 = 0; k2 < NP; k2++) {
-            float t1 = s0y[k2] * s0z[k3], t2 = s0y[k2] * s1z[k3];
-            t1 = fmaf(s1y[k2], s1z[k3], t1);
-            t2 = fmaf(s1y[k2], s0z[k3], t2);
-            const float wp = fmaf(0.5f, t2, t1);
-#pragma unroll
-            for (int k1 = 0; k1 < ORD; k1++) atomicAdd(pj + 3 * k1 + jsy * k2 + jsz * k3, wl1[k1] * wp);
-        }
-#pragma unroll
-    for (int k3 = 0; k3 < NP; k3++)
-#pragma unroll
-        for (int k1 = 0; k1 < NP; k1++) {
-            float t1 = s0x[k1] * s0z[k3], t2 = s0x[k1] * s1z[k3];
-            t1 = fmaf(s1x[k1], s1z[k3], t1);
-            t2 = fmaf(s1x[k1], s0z[k3], t2);
-            const float wp = fmaf(0.5f, t2, t1);
-#pragma unroll
-            for (int k2 = 0; k2 < ORD; k2++)
-                atomicAdd(pj + 3 * k1 + jsy * k2 + jsz * k3 + 1, wl2[k2] * wp);
-        }
-#pragma unroll
-    for (int k2 = 0; k2 < NP; k2++)
-#pragma unroll
-        for (int k1 = 0; k1 < NP; k1++) {
-            float t1 = s0x[k1] * s0y[k2], t2 = s0x[k1] * s1y[k2];
-            t1 = fmaf(s1x[k1], s1y[k2], t1);
-            t2 = fmaf(s1x[k1], s0y[k2], t2);
-            const float wp = fmaf(0.5f, t2, t1);
-#pragma unroll
-            for (int k3 = 0; k3 < ORD; k3++)
-                atomicAdd(pj + 3 * k1 + jsy * k2 + jsz * k3 + 2, wl3[k3] * wp);
-        }
-}
-
 template <int DIM, int ORD>
 __device__ __forceinline__ int seg_offset(int vi, int jsy, int jsz)
 {
@@ -350,122 +244,6 @@ __device__ __forceinline__ int seg_offset(int vi, int jsy, int jsz)
         if (vi < B) return 3 * (vi % NP) + jsy * ((vi / NP) % ORD) + jsz * (vi / (ORD * NP)) + 1;
         vi -= B;
         return 3 * (vi % NP) + jsy * ((vi / NP) % NP) + jsz * (vi / (NP * NP)) + 2;
-    }
-}
-
-// Reduce N <= 32 values held by every lane across the warp so that each lane ends with the
-// warp sum of one value (recursive halving with uneven halves: a step over N values exchanges
-// ceil(N/2) of them, so 21 values take 11+6+3+2+1 = 23 shuffles instead of 31).  The sum ends
-// in t[0]; transpose_slot<N>(lane) says which value that is (-1: none).
-template <int N, int D>
-__device__ __forceinline__ void transpose_step(float *t, unsigned lane)
-{
-    constexpr int M = (N + 1) / 2;
-    const bool upper = (lane & D) != 0;
-#pragma unroll
-    for (int k = 0; k < M; k++) {
-        const float lo = t[k];
-        const float hi = (M + k < N) ? t[M + k] : 0.f;
-        const float send = upper ? lo : hi;
-        const float keep = upper ? hi : lo;
-        t[k] = keep + __shfl_xor_sync(FULL_MASK, send, D);
-    }
-    if constexpr (D > 1) transpose_step<M, D / 2>(t, lane);
-}
-
-template <int N>
-__device__ __forceinline__ float transpose_reduce(float (&t)[N])
-{
-    static_assert(N >= 1 && N <= 32, "one batch holds at most 32 values");
-    transpose_step<N, 16>(t, threadIdx.x & 31);
-    return t[0];
-}
-
-template <int N, int D>
-__device__ __forceinline__ int transpose_slot_step(unsigned lane, int lo, int n)
-{
-    constexpr int M = (N + 1) / 2;
-    if (lane & D) {
-        lo += M;
-        n -= M;
-    } else {
-        n = n < M ? n : M;
-    }
-    if constexpr (D > 1)
-        return transpose_slot_step<M, D / 2>(lane, lo, n);
-    else
-        return n > 0 ? lo : -1;
-}
-
-template <int N>
-__device__ __forceinline__ int transpose_slot(unsigned lane)
-{
-    return transpose_slot_step<N, 16>(lane, 0, N);
-}
-
-// Per-lane targets of the reduced sums of one segment: for batch b of 32 values, the offset
-// (in floats, from the stencil origin) of the value that lands in this lane, or -1.
-template <int DIM, int ORD> struct LaneSlots {
-    static constexpr int NV = SegVals<DIM, ORD>::NV;
-    static constexpr int NB = (NV + 31) / 32;
-    int off[NB];
-    __device__ __forceinline__ void init(int jsy, int jsz)
-    {
-        const unsigned lane = threadIdx.x & 31;
-#pragma unroll
-        for (int b = 0; b < NB; b++) {
-            constexpr int REST = NV % 32 == 0 ? 32 : NV % 32;
-            const int slot = b < NB - 1 ? (int)lane : transpose_slot<REST>(lane);
-            off[b] = slot >= 0 ? seg_offset<DIM, ORD>(32 * b + slot, jsy, jsz) : -1;
-        }
-    }
-};
-
-// 3D warp-cooperative accumulation of one segment per lane into the shared current tile.
-// base = offset of the lane's stencil origin, or -1 when the lane has no segment.  Lanes whose
-// cell is shared by at least `reduce_min` lanes of the warp are summed in registers first
-// (transpose-reduce, one pass per such cell): every atomic of a pass hits a distinct address.
-// Lanes of sparsely populated cells add their values directly (shared atomics): a reduce pass
-// costs several direct adds and only pays when enough lanes share it.  Must be called by all
-// 32 lanes.
-template <int DIM, int ORD>
-__device__ __forceinline__ void warp_deposit(float *sJ, int base, const float *v, int jsy,
-                                             int jsz, int reduce_min,
-                                             const LaneSlots<DIM, ORD> &ls)
-{
-    constexpr int NV = SegVals<DIM, ORD>::NV;
-    constexpr int NB = (NV + 31) / 32;
-    const unsigned lane = threadIdx.x & 31;
-    const unsigned peers = __match_any_sync(FULL_MASK, base);
-    const bool active = base >= 0;
-    const bool direct = active && __popc(peers) < reduce_min;
-    if (direct) {
-#pragma unroll
-        for (int i = 0; i < NV; i++) atomicAdd(sJ + base + seg_offset<DIM, ORD>(i, jsy, jsz), v[i]);
-    }
-    unsigned rem = __ballot_sync(FULL_MASK, active && !direct && (__ffs(peers) - 1) == (int)lane);
-    while (rem) {
-        const int l = __ffs(rem) - 1;
-        rem &= rem - 1;
-        const int key = __shfl_sync(FULL_MASK, base, l);
-        const bool mine = base == key;
-#pragma unroll
-        for (int bch = 0; bch < NB; bch++) {
-            constexpr int REST = NV % 32 == 0 ? 32 : NV % 32;
-            float sum;
-            if (bch < NB - 1) {
-                float t[32];
-#pragma unroll
-                for (int k = 0; k < 32; k++) t[k] = mine ? v[bch * 32 + k] : 0.f;
-                sum = transpose_reduce<32>(t);
-            } else {
-                float t[REST];
-#pragma unroll
-                for (int k = 0; k < REST; k++) t[k] = mine ? v[bch * 32 + k] : 0.f;
-                sum = transpose_reduce<REST>(t);
-            }
-            if (ls.off[bch] >= 0) atomicAdd(sJ + key + ls.off[bch], sum);
-        }
     }
 }
 
@@ -513,45 +291,6 @@ __device__ __forceinline__ int make_segments(SegRec *out, const float *xo, const
             out[t].base = 3 * sg[t].i + jsy * sg[t].j + jsz * sg[t].k;
         }
         return n;
-    }
-}
-
-// 3D: deposit one segment per lane (rec = nullptr: no segment).  reduce_min > 32 selects
-// plain per-lane shared atomics (no warp-synchronous part); otherwise warp_deposit.  Cubic and
-// quartic segments (144 and 300 values) always add directly: their values do not fit in
-// registers next to a reduce buffer.
-template <int DIM, int ORD>
-constexpr bool direct_only() { return DIM == 3 && ORD >= 3; }
-
-template <int ORD>
-__device__ __forceinline__ void deposit_segment3(float *sJ, const SegRec *rec, const float *jn,
-                                                 int jsy, int jsz, int reduce_min,
-                                                 const LaneSlots<3, ORD> &ls)
-{
-    if (direct_only<3, ORD>() || reduce_min > 32) {
-        if (rec) {
-            Seg3<float> g;
-            g.x0 = rec->a[0]; g.x1 = rec->a[1]; g.y0 = rec->a[2]; g.y1 = rec->a[3];
-            g.z0 = rec->a[4]; g.z1 = rec->a[5]; g.i = g.j = g.k = 0;
-            seg_atomic3<ORD>(sJ + rec->base, g, rec->q, jn, jsy, jsz);
-        }
-        return;
-    }
-    if constexpr (!direct_only<3, ORD>()) {
-        constexpr int NV = SegVals<3, ORD>::NV;
-        float v[NV];
-        int base = -1;
-        if (rec) {
-            Seg3<float> g;
-            g.x0 = rec->a[0]; g.x1 = rec->a[1]; g.y0 = rec->a[2]; g.y1 = rec->a[3];
-            g.z0 = rec->a[4]; g.z1 = rec->a[5]; g.i = g.j = g.k = 0;
-            seg_values3<ORD>(g, rec->q, jn, v);
-            base = rec->base;
-        } else {
-#pragma unroll
-            for (int k = 0; k < NV; k++) v[k] = 0.f;
-        }
-        warp_deposit<3, ORD>(sJ, base, v, jsy, jsz, reduce_min, ls);
     }
 }
 
@@ -744,6 +483,223 @@ __device__ __forceinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int n
         }
         __syncwarp();
     }
+}
+
+// ------------------------------------------------------------------------------------------
+// 3D deposit.  The CTA's current tile is one shared copy, accumulated exactly as 64-bit fixed
+// point (value x 2^S rounded to an integer; the host picks S so that no tile point can
+// overflow): every add is two native 32-bit integer atomics, the low word and then the high
+// word with the carry of the low one.  The tile sums therefore carry no rounding beyond the
+// one of each added value and do not depend on the order of the adds.
+// A warp deposits the segments of up to 32 rows together (its lanes' in-cell segments, or 32
+// queued face crossings): the rows write their values, CH3 at a time, into the warp's row
+// scratch (16 rows per pass); lane l owns columns 2l and 2l + 1 and sums them over each run
+// of consecutive rows with one stencil origin (the tile is sorted by cell, so a cell's
+// particles sit on neighbouring lanes), adding each run's sum once.  Within one add
+// instruction the lanes hold different values of one segment: their addresses differ.
+// ------------------------------------------------------------------------------------------
+constexpr int CH3 = 48;          // values per chunk
+constexpr int RS3 = 52;          // row stride in floats: 16-byte rows of 13 (odd) 16-byte
+                                 // units, so the 16-byte writes of 8 lanes hit distinct banks
+constexpr int SROWS3 = 16;       // rows per scratch pass (the two half warps in turn)
+constexpr int SEGQ3 = 48;        // queued face crossings per warp
+constexpr int SEGQ3_KEEP = 16;   // drain while more than this many wait (a round adds <= 32)
+
+constexpr int scratch_floats3() { return SROWS3 * RS3; }
+
+// exact add of v x scale, rounded to an integer, into the 64-bit fixed-point value (hi:lo)
+__device__ __forceinline__ void fx_add(unsigned *lo, unsigned *hi, float v, float scale)
+{
+    const long long f = __float2ll_rn(v * scale);
+    const unsigned fl = (unsigned)(unsigned long long)f;
+    const unsigned fh = (unsigned)((unsigned long long)f >> 32);
+    const unsigned old = atomicAdd(lo, fl);
+    atomicAdd(hi, fh + (old + fl < old ? 1u : 0u));
+}
+
+// B-spline weights at both ends and longitudinal weights (q jn folded in) of one 3D segment
+template <int ORD> struct Seg3W {
+    static constexpr int NP = ORD + 1;
+    float s0[3][NP], s1[3][NP], wl[3][ORD];
+};
+
+template <int ORD>
+__device__ __forceinline__ void seg3_weights(const SegRec &r, const float *jn, Seg3W<ORD> &w)
+{
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        spline<ORD>(r.a[2 * d], w.s0[d]);
+        spline<ORD>(r.a[2 * d + 1], w.s1[d]);
+        long_weights<ORD>(r.q * jn[d], r.a[2 * d], r.a[2 * d + 1], w.wl[d]);
+    }
+}
+
+// weight across the motion along axis pair (a, b): s0a s0b + s1a s1b + (s0a s1b + s1a s0b) / 2
+// (DEP_CURRENT_3D, source/spec/os-spec-current.f03:2800-2905)
+__device__ __forceinline__ float wperp(float s0a, float s1a, float s0b, float s1b)
+{
+    float t1 = s0a * s0b, t2 = s0a * s1b;
+    t1 = fmaf(s1a, s1b, t1);
+    t2 = fmaf(s1a, s0b, t2);
+    return fmaf(0.5f, t2, t1);
+}
+
+// values V0 .. V0 + N - 1 of a segment, in the seg_offset order
+//   j1 [k3][k2][k1 < ORD], j2 [k3][k2 < ORD][k1], j3 [k3 < ORD][k2][k1]
+template <int ORD, int V0, int N>
+__device__ __forceinline__ void seg3_chunk(const Seg3W<ORD> &w, float *v)
+{
+    constexpr int NP = ORD + 1, B = ORD * NP * NP;
+#pragma unroll
+    for (int k3 = 0; k3 < NP; k3++)
+#pragma unroll
+        for (int k2 = 0; k2 < NP; k2++)
+#pragma unroll
+            for (int k1 = 0; k1 < ORD; k1++) {
+                const int n = (k3 * NP + k2) * ORD + k1;
+                if (n >= V0 && n < V0 + N)
+                    v[n - V0] = w.wl[0][k1] * wperp(w.s0[1][k2], w.s1[1][k2], w.s0[2][k3],
+                                                    w.s1[2][k3]);
+            }
+#pragma unroll
+    for (int k3 = 0; k3 < NP; k3++)
+#pragma unroll
+        for (int k2 = 0; k2 < ORD; k2++)
+#pragma unroll
+            for (int k1 = 0; k1 < NP; k1++) {
+                const int n = B + (k3 * ORD + k2) * NP + k1;
+                if (n >= V0 && n < V0 + N)
+                    v[n - V0] = w.wl[1][k2] * wperp(w.s0[0][k1], w.s1[0][k1], w.s0[2][k3],
+                                                    w.s1[2][k3]);
+            }
+#pragma unroll
+    for (int k3 = 0; k3 < ORD; k3++)
+#pragma unroll
+        for (int k2 = 0; k2 < NP; k2++)
+#pragma unroll
+            for (int k1 = 0; k1 < NP; k1++) {
+                const int n = 2 * B + (k3 * NP + k2) * NP + k1;
+                if (n >= V0 && n < V0 + N)
+                    v[n - V0] = w.wl[2][k3] * wperp(w.s0[0][k1], w.s1[0][k1], w.s0[1][k2],
+                                                    w.s1[1][k2]);
+            }
+}
+
+// values V0 .. V0 + N - 1 of the segment into a scratch row, 16 at a time (only 16 values
+// live in registers)
+template <int ORD, int V0, int N, int S = 0>
+__device__ __forceinline__ void seg3_row(const Seg3W<ORD> &w, float *row)
+{
+    constexpr int M = N - S < 16 ? N - S : 16;
+    static_assert(M % 2 == 0, "rows are written in float pairs");
+    float v[M];
+    seg3_chunk<ORD, V0 + S, M>(w, v);
+#pragma unroll
+    for (int k = 0; k + 4 <= M; k += 4)
+        *reinterpret_cast<float4 *>(row + S + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+    if constexpr (M % 4 == 2)
+        *reinterpret_cast<float2 *>(row + S + M - 2) = make_float2(v[M - 2], v[M - 1]);
+    if constexpr (S + M < N) seg3_row<ORD, V0, N, S + M>(w, row);
+}
+
+// chunk C of rows_deposit3 (and the chunks after it)
+template <int ORD, int C>
+__device__ __forceinline__ void rows_chunk3(unsigned *Jl, unsigned *Jh, float *scr,
+                                            const Seg3W<ORD> &w, bool has, int b,
+                                            unsigned ends, int jsy, int jsz, float scale)
+{
+    constexpr int NV = SegVals<3, ORD>::NV;
+    constexpr int V0 = C * CH3;
+    constexpr int N = NV - V0 < CH3 ? NV - V0 : CH3;
+    static_assert(N % 2 == 0, "chunks hold whole column pairs");
+    const int lane = (int)(threadIdx.x & 31);
+    const int c0 = 2 * lane;   // the column pair this lane sums
+    const bool own = c0 < N;
+    int o0 = 0, o1 = 0;
+    if (own) {
+        o0 = seg_offset<3, ORD>(V0 + c0, jsy, jsz);
+        o1 = seg_offset<3, ORD>(V0 + c0 + 1, jsy, jsz);
+    }
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll 1
+    for (int h = 0; h < 2; h++) {
+        __syncwarp();
+        if ((lane >> 4) == h) {
+            float *row = scr + (lane & 15) * RS3;
+            if (has) {
+                seg3_row<ORD, V0, N>(w, row);
+            } else {
+#pragma unroll
+                for (int k = 0; k + 2 <= N; k += 2)
+                    *reinterpret_cast<float2 *>(row + k) = make_float2(0.f, 0.f);
+            }
+        }
+        __syncwarp();
+        const unsigned eh = ends >> (SROWS3 * h);
+#pragma unroll 4
+        for (int rr = 0; rr < SROWS3; rr++) {
+            if (own) acc = __fadd2_rn(acc, *reinterpret_cast<const float2 *>(scr + rr * RS3 + c0));
+            if ((eh >> rr) & 1u) {
+                const int rb = __shfl_sync(FULL_MASK, b, SROWS3 * h + rr);
+                if (own && rb >= 0) {
+                    fx_add(Jl + rb + o0, Jh + rb + o0, acc.x, scale);
+                    fx_add(Jl + rb + o1, Jh + rb + o1, acc.y, scale);
+                }
+                acc = make_float2(0.f, 0.f);
+            }
+        }
+    }
+    __syncwarp();
+    if constexpr (V0 + N < NV)
+        rows_chunk3<ORD, C + 1>(Jl, Jh, scr, w, has, b, ends, jsy, jsz, scale);
+}
+
+// Warp-collective deposit of one 3D segment per lane (has = false: none); base = offset of
+// the segment's stencil origin in the current tile.  Runs = maximal groups of consecutive
+// lanes with one base.  Not inlined: the push calls it from several places (the in-cell
+// segments, the queue drains), and one copy of its code keeps the kernel's instruction
+// footprint and register pressure down.
+template <int ORD>
+__device__ __noinline__ void rows_deposit3(unsigned *Jl, unsigned *Jh, float *scr,
+                                           const SegRec r, bool has, const float *jn, int jsy,
+                                           int jsz, float scale)
+{
+    const int lane = (int)(threadIdx.x & 31);
+    const int b = has ? r.base : -1;
+    const int nb = __shfl_down_sync(FULL_MASK, b, 1);
+    const unsigned ends = __ballot_sync(FULL_MASK, lane == 31 || nb != b);
+    Seg3W<ORD> w;
+    if (has) seg3_weights<ORD>(r, jn, w);
+    rows_chunk3<ORD, 0>(Jl, Jh, scr, w, has, b, ends, jsy, jsz, scale);
+}
+
+// deposit the top entries of the warp's queue of 3D face crossings (up to 32 at a time)
+// while more than keep wait
+template <int ORD>
+__device__ __forceinline__ void segq_drain3(unsigned *Jl, unsigned *Jh, float *scr, SegRec *sq,
+                                            int &qn, int keep, const float *jn, int jsy,
+                                            int jsz, float scale)
+{
+    const int lane = (int)(threadIdx.x & 31);
+    while (qn > keep) {
+        const int take = qn < 32 ? qn : 32, first = qn - take;
+        __syncwarp();
+        SegRec r{};
+        const bool has = lane < take;
+        if (has) r = sq[first + lane];
+        qn = first;
+        rows_deposit3<ORD>(Jl, Jh, scr, r, has, jn, jsy, jsz, scale);
+    }
+}
+
+// tile current point, fixed point (hi:lo) x inv_scale, as a float pair th + tl
+__device__ __forceinline__ void fx_to_pair(unsigned lo, unsigned hi, double inv_scale,
+                                           float &th, float &tl)
+{
+    const long long v = (long long)(((unsigned long long)hi << 32) | lo);
+    const double d = (double)v * inv_scale;
+    th = (float)d;
+    tl = (float)(d - (double)th);
 }
 
 // ------------------------------------------------------------------------------------------

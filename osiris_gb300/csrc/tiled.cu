@@ -53,6 +53,7 @@ struct TiledState {
     double dt = 0, dx[3] = {1, 1, 1};
     std::vector<double> rqm;
     std::vector<long> cap;
+    std::vector<double> qmax;   // per species: the largest |charge| a particle can carry
     std::vector<Slabs> buf[2];
     std::vector<void *> allocs;
     int *d_cnt[2] = {nullptr, nullptr};   // [MAX_TILED_SPECIES * ntiles] per buffer
@@ -63,7 +64,6 @@ struct TiledState {
     size_t compact_bytes = 0;
     size_t smem_bytes = 0;
     int threads = 256;   // threads per push CTA (multiple of 32, <= 256)
-    int reduce_min = 2;  // set per dimension in tiled_create
     // drop dead slab lines from L2 after the sort; OSG_L2_DISCARD=0 turns it off (profiler
     // kernel replay saves and restores device memory and needs the dropped lines defined)
     int l2_discard = 1;
@@ -157,6 +157,23 @@ static cudaError_t push_attr(int pusher, int dim, int order, int bytes)
     }
 }
 
+// 3D fixed-point tile current: a tile point receives at most 4 segments per particle of the
+// tile (at most cap slots per species), each value at most 3 |q| jn (weights along the motion
+// <= |q| jn, across it <= 3); the scale 2^S keeps that bound below 2^62.
+static void fx_scale_for(const TiledState *t, TiledArgs &a)
+{
+    double jn = 0.0;
+    for (int d = 0; d < t->dim; d++) jn = std::max(jn, (double)std::fabs(a.jn[d]));
+    double bound = 0.0;
+    for (size_t k = 0; k < t->cap.size() && k < t->qmax.size(); k++)
+        bound += (double)t->cap[k] * t->qmax[k];
+    bound *= 12.0 * jn;
+    int S = bound > 0.0 ? (int)std::floor(62.0 - std::log2(bound)) : 40;
+    S = std::max(-100, std::min(S, 100));
+    a.fx_scale = std::ldexp(1.0f, S);
+    a.fx_inv = std::ldexp(1.0, -S);
+}
+
 static TiledArgs base_args(const TiledState *t)
 {
     TiledArgs a;
@@ -178,10 +195,12 @@ static TiledArgs base_args(const TiledState *t)
     a.tile_lo = t->tile_lo;
     a.discard = t->l2_discard;
     a.walls = t->walls;
+    fx_scale_for(t, a);
     return a;
 }
 
-// shared memory of the push kernel: E and B tiles and the current tile (one per warp in 2D)
+// shared memory of the push kernel: E and B tiles and the current tile (one per warp with its
+// compensation in 2D; the low and high words of the fixed-point tile in 3D)
 static size_t smem_for(int dim, int order, const int *T, int threads)
 {
     const int NP = order + 1;
@@ -193,12 +212,14 @@ static size_t smem_for(int dim, int order, const int *T, int threads)
     // 2D: one copy of the current tile per warp, each with its two-sum compensation, then per
     // warp a value scratch and a queue of face-crossing segments; last the cell histogram
     const size_t warps = (size_t)threads / 32;
-    const size_t copies = dim == 2 ? 2 * warps : 1;
+    const size_t copies = dim == 2 ? 2 * warps : 2;
     const size_t nf = (6 * ne + 3 * nj * copies + 3) & ~(size_t)3;
     size_t cells = 1;
     for (int d = 0; d < dim; d++) cells *= (size_t)T[d];
     const size_t hist = 2 * cells * sizeof(int);
-    if (dim != 2) return nf * sizeof(float) + hist;
+    if (dim != 2)
+        return nf * sizeof(float) + warps * scratch_floats3() * sizeof(float) +
+               warps * SEGQ3 * sizeof(SegRec) + hist;
     const int nv = 2 * order * NP + NP * NP;
     const size_t scratch = warps * (size_t)(nv + 1) * SCR_LD * sizeof(float);
     return nf * sizeof(float) + scratch + warps * SEGQ * sizeof(SegRec) + hist;
@@ -222,7 +243,9 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
         if (d < cfg.dim) {
             T = cfg.tile[d];
             if (T <= 0) {
-                const int pref = 8;   // measured best on GB300 for 2D quadratic (C2)
+                // 8 x 8 measured best on GB300 for 2D quadratic; 3D 8 x 8 x 4 (the deposit's
+                // shared memory then allows two CTAs per SM)
+                const int pref = (cfg.dim == 3 && d == 2) ? 4 : 8;
                 for (T = pref; T > 1 && t->nx[d] % T; T >>= 1) {}
             }
             if (T < 1 || t->nx[d] % T) {
@@ -245,10 +268,6 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
         delete t;
         return OSG_ERR_ARG;
     }
-    // 2D: warp-reduce every cell that two or more lanes share; 3D (54..300 values per segment,
-    // lanes of one warp spread over the tile): direct shared atomics measured faster
-    t->reduce_min = t->dim == 2 ? 2 : 33;
-    if (const char *ev = getenv("OSG_REDUCE_MIN")) t->reduce_min = atoi(ev);
     if (const char *ev = getenv("OSG_L2_DISCARD")) t->l2_discard = atoi(ev) != 0;
     if (const char *ev = getenv("OSG_PUSH_THREADS")) {
         const int v = atoi(ev);
@@ -291,8 +310,7 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
     t->nj_tile = 3;
     for (int d = 0; d < t->dim; d++) t->nj_tile *= t->T[d] + t->order + 2;
     const size_t tb = sizeof(float) * (size_t)t->nj_tile * t->ntiles;
-    if (cudaMalloc(&t->tile_hi, tb) != cudaSuccess ||
-        (t->dim == 2 && cudaMalloc(&t->tile_lo, tb) != cudaSuccess)) {
+    if (cudaMalloc(&t->tile_hi, tb) != cudaSuccess || cudaMalloc(&t->tile_lo, tb) != cudaSuccess) {
         tiled_destroy(t);
         set_error("tile current allocation of %zu bytes failed", tb);
         return OSG_ERR_NOMEM;
@@ -410,6 +428,13 @@ int tiled_add_species(TiledState *t, double rqm, long np, const int *ix, const f
     }
     t->rqm.push_back(rqm);
     t->cap.push_back(cap);
+    {
+        // (a species re-binned by tiled_regrow keeps the bound it had)
+        double qm = 0.0;
+        for (long p = 0; p < np; p++) qm = std::max(qm, (double)std::fabs(q[p]));
+        if (k < (int)t->qmax.size()) t->qmax[k] = std::max(qm, t->qmax[k]);
+        else t->qmax.push_back(qm);
+    }
     // upload in reference layout, bin into buffer 0
     if (np > 0) {
         const size_t need = (size_t)np * (sizeof(int) * dim + sizeof(float) * (dim + 4));
@@ -457,7 +482,6 @@ TiledArgs tiled_args(TiledState *t, int parity, const float *e, const float *b, 
     a.nspec = (int)t->rqm.size();
     a.ene = d_ene;
     a.status = d_status;
-    a.reduce_min = t->reduce_min;
     return a;
 }
 
@@ -583,6 +607,10 @@ int tiled_set_window(TiledState *t, int species, const int *ppc, int nprof,
         per *= t->inj_ppc[d];
     }
     const long need = (long)std::ceil(1.5 * (double)(per_tile * per)) + 64;
+    // injected particles carry den / per, den at most the profile's largest value
+    double fmax = 0.0;
+    for (int k = 0; k < nprof; k++) fmax = std::max(fmax, std::fabs(prof_f[k]));
+    t->qmax[species] = std::max(t->qmax[species], fmax / (double)per);
     if ((int)t->min_cap.size() < (int)t->rqm.size()) t->min_cap.resize(t->rqm.size(), 0);
     t->min_cap[species] = std::max(t->min_cap[species], need);
     if (t->cap[species] < need) return tiled_regrow(t, 0, 0);

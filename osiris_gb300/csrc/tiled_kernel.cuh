@@ -104,13 +104,16 @@ struct TiledArgs {
     int nspec;
     double *ene;
     int *status;
-    int reduce_min;    // warp-reduce a cell's segments when at least this many lanes share it
     double dt_full;    // exact pusher: the double time step and the Newton tolerance
     double iter_tol;
-    // current of every tile with its halo, [tile][3 * points] (hi) and its compensation (lo,
-    // 2D), summed in FP64 in tile order by k_tile_fold
+    // current of every tile with its halo, [tile][3 * points] (hi) and its compensation (lo),
+    // summed in FP64 in tile order by k_tile_fold
     float *tile_hi;
     float *tile_lo;
+    // 3D: the tile current is accumulated as 64-bit fixed point, value x fx_scale (a power of
+    // two chosen so that no tile point can overflow); fx_inv = 1 / fx_scale
+    float fx_scale;
+    double fx_inv;
     // bit d: axis d is open (no periodic wrap): particles that leave the box along it are
     // dropped (absorbed).  Bit 0 with the moving window along x1, or the axis of Lindman
     // open boundaries.  shift_x = 1 (a step that ends with a window move) stores every
@@ -205,7 +208,8 @@ __device__ __forceinline__ void discard_dead_slab(const Slabs &in, long slab, in
 // to its new slot, then deposit the segments (round t takes the t-th segment of every lane).
 // In 2D every warp accumulates into its own copy of the current tile (with a two-sum
 // compensation), so its adds are plain shared read-modify-writes; the copies are summed when
-// the tile is flushed.  In 3D the warps share one current tile (atomic adds).
+// the tile is flushed.  In 3D the warps share one current tile, accumulated exactly in 64-bit
+// fixed point by integer atomics (rows_deposit3).
 // CTAs of up to 256 threads.  2D linear/quadratic: three resident CTAs per SM (at most 85
 // registers per thread, measured fastest on GB300); 2D quartic: one (it needs ~250 registers
 // without spilling); otherwise two
@@ -237,8 +241,9 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     const int ne = ee[0] * ee[1] * ee[2], nj = je[0] * je[1] * je[2];
     const int nthr = blockDim.x, nwarp = nthr >> 5, warp = threadIdx.x >> 5;
     const int njall = 3 * nj * (DIM == 2 ? nwarp : 1);
-    // 2D: the warp copies of the current tile keep a two-sum compensation at offset jlo
-    const int jlo = DIM == 2 ? njall : 0;
+    // 2D: the warp copies of the current tile keep a two-sum compensation at offset jlo;
+    // 3D: the low (offset 0) and high (offset jlo) words of the fixed-point tile current
+    const int jlo = njall;
     float *sE = smem, *sB = smem + 3 * ne, *sJ = smem + 6 * ne;
     const long gsy = 3L * a.size[0], gsz = 3L * a.size[0] * a.size[1];
 
@@ -254,12 +259,15 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
         sB[idx] = __ldg(a.b + gp);
     }
     for (int idx = threadIdx.x; idx < njall + jlo; idx += nthr) sJ[idx] = 0.0f;
-    // dynamic shared memory after the current tile (16-byte aligned): 2D per-warp value scratch
+    unsigned *sJl = reinterpret_cast<unsigned *>(sJ), *sJh = sJl + jlo;
+    // dynamic shared memory after the current tile (16-byte aligned): per-warp value scratch
     // and queue of face-crossing segments, then two per-cell histograms of the tile sort (one
     // per species, alternating, so the next one is cleared while the current one is used)
+    constexpr int SCRF = DIM == 2 ? scratch_floats2<ORD>() : scratch_floats3();
+    constexpr int QCAP = DIM == 2 ? SEGQ : SEGQ3;
     float *scr = smem + ((6 * ne + njall + jlo + 3) & ~3);
-    SegRec *sQ0 = reinterpret_cast<SegRec *>(scr + (DIM == 2 ? nwarp * scratch_floats2<ORD>() : 0));
-    int *sHist = reinterpret_cast<int *>(sQ0 + (DIM == 2 ? nwarp * SEGQ : 0));
+    SegRec *sQ0 = reinterpret_cast<SegRec *>(scr + nwarp * SCRF);
+    int *sHist = reinterpret_cast<int *>(sQ0 + nwarp * QCAP);
     const int ncell = a.T[0] * a.T[1] * a.T[2];
     for (int k = threadIdx.x; k < ncell; k += nthr) sHist[k] = 0;
     // particles leaving the tile wait in a shared queue; after the pass they take their
@@ -276,17 +284,11 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     const int jsy = 3 * je[0], jsz = 3 * je[0] * je[1];
     const unsigned lane = threadIdx.x & 31;
     float *sJw = DIM == 2 ? sJ + 3 * nj * warp : sJ;
-    LaneSlots<DIM, ORD> ls;
     ColSlots<ORD> cs;
-    if constexpr (DIM == 3) ls.init(jsy, jsz);
-    else cs.init(jsy);
-    // 3D direct deposits: every thread walks its own contiguous run of the cell-sorted tile,
-    // so the lanes of a warp sit in cells far apart and their shared-memory atomics seldom
-    // conflict; otherwise a warp takes 32 consecutive particles (mostly one cell)
-    const bool spread = DIM == 3 && (direct_only<DIM, ORD>() || a.reduce_min > 32);
+    if constexpr (DIM == 2) cs.init(jsy);
 
-    SegRec *sQ = sQ0 + warp * SEGQ;
-    scr += warp * scratch_floats2<ORD>();
+    SegRec *sQ = sQ0 + warp * QCAP;
+    scr += warp * SCRF;
     int qn = 0;
 
     for (int s = 0; s < a.nspec; s++) {
@@ -495,10 +497,10 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
             }
             return nseg > 0 ? nseg : (has ? 0 : -1);
         };
+        // a warp takes 32 consecutive particles of the cell-sorted tile (coalesced; mostly one
+        // cell)
         const int nit = (n + nthr - 1) / nthr;
-        auto index = [&](int it) {
-            return spread ? (int)threadIdx.x * nit + it : it * nthr + (int)threadIdx.x;
-        };
+        auto index = [&](int it) { return it * nthr + (int)threadIdx.x; };
         prefetch(index(0), n);
         for (int it = 0; it < nit; it++) {
             const int i = index(it);
@@ -508,11 +510,11 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
             take(c, xo, un, q);
             if (it + 1 < nit) prefetch(index(it + 1), n);
             const int ns = push_one(i < n, slot(i), c, xo, un, q, sg);
-            // ---- charge-conserving current of the segments into the shared tile.  2D: the
-            //      first segment (in the particle's own cell, shared by neighbouring lanes of
-            //      the cell-sorted tile) is summed per run of lanes with one cell; the others
+            // ---- charge-conserving current of the segments into the shared tile: the first
+            //      segment (in the particle's own cell, shared by neighbouring lanes of the
+            //      cell-sorted tile) is summed per run of lanes with one cell; the others
             //      (face crossings, few and scattered) wait in the warp's queue for a
-            //      full-warp deposit.  3D: one warp-cooperative deposit per round
+            //      full-warp deposit
 #pragma unroll
             for (int t = 0; t < MAXSEG; t++) {
                 const bool hs = t < ns;
@@ -533,9 +535,14 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                     }
                     cell_runs_deposit2<ORD>(sJw, jlo, scr, hs ? sg[0].base : -1, v, cs);
                 } else {
+                    if (t > 0) {
+                        segq_push(sQ, qn, hs, sg[t]);
+                        segq_drain3<ORD>(sJl, sJh, scr, sQ, qn, SEGQ3_KEEP, a.jn, jsy, jsz,
+                                         a.fx_scale);
+                        continue;
+                    }
                     if (!__any_sync(FULL_MASK, hs)) break;
-                    deposit_segment3<ORD>(sJ, hs ? &sg[t] : nullptr, a.jn, jsy, jsz,
-                                          a.reduce_min, ls);
+                    rows_deposit3<ORD>(sJl, sJh, scr, sg[0], hs, a.jn, jsy, jsz, a.fx_scale);
                 }
             }
         }
@@ -640,10 +647,9 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     }
     // ---- the face crossings still queued (the queue carries over from one species to the
     //      next: its entries hold their own charge)
-    if constexpr (DIM == 2) {
-        segq_drain<ORD>(sJw, sQ, qn, 1, a.jn, scr, cs);
-        __syncthreads();
-    }
+    if constexpr (DIM == 2) segq_drain<ORD>(sJw, sQ, qn, 1, a.jn, scr, cs);
+    else segq_drain3<ORD>(sJl, sJh, scr, sQ, qn, 0, a.jn, jsy, jsz, a.fx_scale);
+    __syncthreads();
     // ---- the tile's energy of every species (the per-warp partials, written before the last
     //      block barrier)
     if ((int)threadIdx.x < a.nspec) {
@@ -651,12 +657,12 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
         for (int w = 0; w < nwarp; w++) tot += sEne[threadIdx.x][w];
         if (tot != 0.0) atomicAdd(a.ene + threadIdx.x, tot);
     }
-    // ---- store the tile's current (with halo) for the tile-ordered FP64 re-summation: in 2D
-    //      the warp copies and their compensations are summed into a float pair (hi, lo); in
-    //      3D the single shared tile is stored as it is
+    // ---- store the tile's current (with halo) for the tile-ordered FP64 re-summation as a
+    //      float pair (hi, lo): in 2D the warp copies and their compensations summed, in 3D
+    //      the fixed-point tile converted
     {
         float *th = a.tile_hi + tile * (3L * nj);
-        float *tl = DIM == 2 ? a.tile_lo + tile * (3L * nj) : nullptr;
+        float *tl = a.tile_lo + tile * (3L * nj);
         for (int idx = threadIdx.x; idx < 3 * nj; idx += nthr) {
             if constexpr (DIM == 2) {
                 // error-free FP32 cascade (two-sum of the running sum with every copy; the
@@ -671,7 +677,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 th[idx] = t;
                 tl[idx] = lo - (t - hi);
             } else {
-                th[idx] = sJ[idx];
+                fx_to_pair(sJl[idx], sJh[idx], a.fx_inv, th[idx], tl[idx]);
             }
         }
     }

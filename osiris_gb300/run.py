@@ -78,7 +78,7 @@ def build_lwfa(nx=None, tile=None):
     ramp_end = c["ramp_start"] + c["ramp_cells"] * dx[0]
     px, pf = [c["ramp_start"], ramp_end, 1e9], [0.0, c["n0"], c["n0"]]
     sim = osg.Simulation(nx, dx, c["dt"], order=c["order"], precision=32,
-                         engine=osg.ENGINE_TILED, tile=tile or [8, 8, 8])
+                         engine=osg.ENGINE_TILED, tile=tile)
     gl, gu = osg.GUARD[c["order"]]
     shape = tuple(reversed([n + gl + gu for n in nx])) + (3,)
     e, b = np.zeros(shape, np.float32), np.zeros(shape, np.float32)

@@ -107,16 +107,15 @@ def test_fp32_engines_match_oracle(osg, oracle, engine, dim, order, nx, tile, st
              tile=tile if eng == osg.ENGINE_TILED else None)
 
 
-@pytest.mark.parametrize("reduce_min,threads", [("0", "128"), ("2", "128"), ("33", "128"),
-                                                 ("2", "64"), ("2", "256")])
+@pytest.mark.parametrize("threads", ["64", "128", "256"])
 @pytest.mark.parametrize("dim,order,nx,tile", [(2, 2, [32, 24], [8, 8]),
-                                               (3, 2, [16, 8, 8], [4, 4, 4])])
-def test_tiled_deposit_modes_match_oracle(osg, oracle, monkeypatch, reduce_min, threads, dim,
-                                          order, nx, tile):
-    """The three deposit modes of the tiled push (warp-reduce every cell, direct adds for
-    cells of one lane, direct adds only) and the CTA sizes only reorder the current sums and
-    the particles: 10 steps still match the oracle."""
-    monkeypatch.setenv("OSG_REDUCE_MIN", reduce_min)
+                                               (3, 1, [16, 8, 8], [4, 4, 4]),
+                                               (3, 2, [16, 8, 8], [4, 4, 4]),
+                                               (3, 4, [12, 12, 8], [4, 4, 4])])
+def test_tiled_cta_sizes_match_oracle(osg, oracle, monkeypatch, threads, dim, order, nx, tile):
+    """The CTA size of the tiled push only reorders the particles and the current sums (2D
+    per-warp copies; 3D fixed-point tile adds, whose sums do not depend on the order): 10 steps
+    still match the oracle."""
     monkeypatch.setenv("OSG_PUSH_THREADS", threads)
     _compare(osg, oracle, 32, osg.ENGINE_TILED, dim, order, nx, [2] * dim, 10, 5e-5, tile=tile)
 
