@@ -98,4 +98,23 @@ __device__ __forceinline__ double block_sum(double v)
     return v;
 }
 
+// the same in FP32 (for FP32 energy terms; FP64 arithmetic is slow on this GPU)
+__device__ __forceinline__ float block_sum_f(float v)
+{
+    __shared__ float warp_part_f[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) warp_part_f[wid] = v;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    v = (threadIdx.x < nw) ? warp_part_f[threadIdx.x] : 0.f;
+    if (wid == 0) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
+    __syncthreads();
+    return v;
+}
+
 } // namespace osg

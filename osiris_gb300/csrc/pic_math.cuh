@@ -211,7 +211,7 @@ __device__ __forceinline__ int split2(Seg2<T> *s, int dix, int diy)
     Seg2<T> &v = s[0];
     if (dix == 0 && diy == 0) return 1;
     if (diy == 0) {
-        T xint = T(0.5 * dix);
+        T xint = T(0.5) * T(dix);
         T delta = (xint - v.x0) / (v.x1 - v.x0);
         T yint = v.y0 + (v.y1 - v.y0) * delta;
         Seg2<T> &w = s[1];
@@ -223,7 +223,7 @@ __device__ __forceinline__ int split2(Seg2<T> *s, int dix, int diy)
         return 2;
     }
     if (dix == 0) {
-        T yint = T(0.5 * diy);
+        T yint = T(0.5) * T(diy);
         T delta = (yint - v.y0) / (v.y1 - v.y0);
         T xint = v.x0 + (v.x1 - v.x0) * delta;
         Seg2<T> &w = s[1];
@@ -234,14 +234,14 @@ __device__ __forceinline__ int split2(Seg2<T> *s, int dix, int diy)
         v.x1 = xint; v.y1 = yint; v.vz = v.vz * delta;
         return 2;
     }
-    T xint = T(0.5 * dix);
+    T xint = T(0.5) * T(dix);
     T delta = (xint - v.x0) / (v.x1 - v.x0);
     T yint = v.y0 + (v.y1 - v.y0) * delta;
     if (yint >= T(-0.5) && yint < T(0.5)) {
         // x face first, then y face inside the x-shifted cell
         T vzint = v.vz * delta;
         T vzint2 = v.vz * (T(1) - delta);
-        T yint2 = T(0.5 * diy);
+        T yint2 = T(0.5) * T(diy);
         delta = (yint2 - yint) / (v.y1 - yint);
         T xint2 = -xint + (v.x1 - xint) * delta;
         Seg2<T> &a = s[1];
@@ -254,7 +254,7 @@ __device__ __forceinline__ int split2(Seg2<T> *s, int dix, int diy)
     } else {
         // y face first
         T vzint = v.vz * delta;
-        T yint2 = T(0.5 * diy);
+        T yint2 = T(0.5) * T(diy);
         delta = (yint2 - v.y0) / (yint - v.y0);
         T xint2 = v.x0 + (xint - v.x0) * delta;
         Seg2<T> &a = s[1];
@@ -286,7 +286,7 @@ template <typename T> __device__ __forceinline__ int &ci(Seg3<T> &s, int a)
 template <typename T>
 __device__ __forceinline__ void cut_one(Seg3<T> &v, Seg3<T> &w, int a, int d)
 {
-    T cint = T(0.5 * d);
+    T cint = T(0.5) * T(d);
     T delta = (cint - c0(v, a)) / (c1(v, a) - c0(v, a));
     T in[3];
 #pragma unroll
@@ -305,14 +305,14 @@ __device__ __forceinline__ void cut_two(Seg3<T> &v, Seg3<T> &w0, Seg3<T> &w1, in
                                         int da, int db)
 {
     const int o = 3 - a - b;
-    T aint = T(0.5 * da);
+    T aint = T(0.5) * T(da);
     T delta = (aint - c0(v, a)) / (c1(v, a) - c0(v, a));
     T bint = c0(v, b) + (c1(v, b) - c0(v, b)) * delta;
     T oint = c0(v, o) + (c1(v, o) - c0(v, o)) * delta;
     w0 = v;
     w1 = v;
     if (bint >= T(-0.5) && bint < T(0.5)) {
-        T bint2 = T(0.5 * db);
+        T bint2 = T(0.5) * T(db);
         T del2 = (bint2 - bint) / (c1(v, b) - bint);
         T aint2 = -aint + (c1(v, a) - aint) * del2;
         T oint2 = oint + (c1(v, o) - oint) * del2;
@@ -326,7 +326,7 @@ __device__ __forceinline__ void cut_two(Seg3<T> &v, Seg3<T> &w0, Seg3<T> &w1, in
         ci(w1, a) += da; ci(w1, b) += db;
         c1(v, a) = aint; c1(v, b) = bint; c1(v, o) = oint;
     } else {
-        T bint2 = T(0.5 * db);
+        T bint2 = T(0.5) * T(db);
         T del2 = (bint2 - c0(v, b)) / (bint - c0(v, b));
         T aint2 = c0(v, a) + (aint - c0(v, a)) * del2;
         T oint2 = c0(v, o) + (oint - c0(v, o)) * del2;
@@ -357,7 +357,7 @@ __device__ __forceinline__ int split3(Seg3<T> *s, int dix, int diy, int diz)
     case 6: cut_two(s[0], s[1], s[2], 1, 2, diy, diz); return 3;
     default: {
         cut_two(s[0], s[1], s[2], 0, 1, dix, diy);
-        T zint = T(0.5 * diz);
+        T zint = T(0.5) * T(diz);
         int n = 3;
 #pragma unroll 1
         for (int t = 0; t < 3; t++) {

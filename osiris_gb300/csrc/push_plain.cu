@@ -322,6 +322,9 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
     constexpr int NV = SegVals<2, ORD>::NV, NC = (NV + 31) / 32;
     const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
     double my_ene = 0.0;
+    // FP32 Boris: the energy term q ene in FP32 (as the reference's single-precision kernels),
+    // summed per block in FP32 (FP64 arithmetic runs at a small fraction of the FP32 rate here)
+    float my_ene_f = 0.f;
     long run_base = -1;   // RUNS: stencil origin of the in-cell segment in J (-1: none)
     T rv[RUNS ? NV : 1];
     if constexpr (RUNS) {
@@ -456,7 +459,8 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
                 my_ene = cond_vay_push<T>(a.tem, E1, E2, E3, B1, B2, B3, q, u1, u2, u3);
             } else {
                 const T ene = boris(a.tem, E1, E2, E3, B1, B2, B3, u1, u2, u3);
-                my_ene = (double)q * (double)ene;
+                if constexpr (sizeof(T) == 4) my_ene_f = q * ene;
+                else my_ene = (double)q * (double)ene;
             }
             a.u[3 * p] = u1;
             a.u[3 * p + 1] = u2;
@@ -545,6 +549,13 @@ __global__ void __launch_bounds__(256) k_push_plain(PlainPushArgs<T> a)
         for (int c = 0; c < NC; c++)
             off[c] = lane + 32 * c < NV ? seg_offset<2, ORD>(lane + 32 * c, (int)a.j_Dy, 0) : 0;
         cell_runs_deposit_global2<T, ORD>(a.j, sScr[w], sBase[w], run_base, rv, off);
+    }
+    if constexpr (sizeof(T) == 4) {
+        if (a.pusher == OSG_PUSHER_BORIS) {
+            const float tot = block_sum_f(my_ene_f);
+            if (threadIdx.x == 0 && tot != 0.f) atomicAdd(a.ene, (double)tot);
+            return;
+        }
     }
     const double tot = block_sum(my_ene);
     if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.ene, tot);

@@ -507,12 +507,24 @@ constexpr int SEGQ3_KEEP = 16;   // drain while more than this many wait (a roun
 
 constexpr int scratch_floats3() { return SROWS3 * RS3; }
 
-// exact add of v x scale, rounded to an integer, into the 64-bit fixed-point value (hi:lo)
+// exact add of v x scale, rounded to an integer, into the 64-bit fixed-point value (hi:lo).
+// Only 32-bit conversions are used (64-bit ones run on this GPU's slow FP64 pipe): y = v x scale
+// (exact, |y| < 2^62 by the choice of scale) splits as yh 2^32 + r with yh = rint(y / 2^32)
+// and |r| <= 2^31, both exact in float (r holds at most the 24 bits of y below 2^32); the
+// integer (yh, rint(r)) is then the two's complement pair (low word rint(r), high word
+// yh - 1 when rint(r) < 0).
 __device__ __forceinline__ void fx_add(unsigned *lo, unsigned *hi, float v, float scale)
 {
-    const long long f = __float2ll_rn(v * scale);
-    const unsigned fl = (unsigned)(unsigned long long)f;
-    const unsigned fh = (unsigned)((unsigned long long)f >> 32);
+    const float y = v * scale;
+    float yh = rintf(y * 2.3283064365386963e-10f);     // y / 2^32
+    float r = fmaf(-yh, 4294967296.0f, y);              // exact
+    if (r >= 2147483648.0f) {                            // keep rint(r) inside int32
+        r -= 4294967296.0f;
+        yh += 1.0f;
+    }
+    const int ri = __float2int_rn(r);
+    const unsigned fl = (unsigned)ri;
+    const unsigned fh = (unsigned)(__float2int_rn(yh) + (ri >> 31));
     const unsigned old = atomicAdd(lo, fl);
     atomicAdd(hi, fh + (old + fl < old ? 1u : 0u));
 }
@@ -690,16 +702,6 @@ __device__ __forceinline__ void segq_drain3(unsigned *Jl, unsigned *Jh, float *s
         qn = first;
         rows_deposit3<ORD>(Jl, Jh, scr, r, has, jn, jsy, jsz, scale);
     }
-}
-
-// tile current point, fixed point (hi:lo) x inv_scale, as a float pair th + tl
-__device__ __forceinline__ void fx_to_pair(unsigned lo, unsigned hi, double inv_scale,
-                                           float &th, float &tl)
-{
-    const long long v = (long long)(((unsigned long long)hi << 32) | lo);
-    const double d = (double)v * inv_scale;
-    th = (float)d;
-    tl = (float)(d - (double)th);
 }
 
 // ------------------------------------------------------------------------------------------

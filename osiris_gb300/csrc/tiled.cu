@@ -159,19 +159,23 @@ static cudaError_t push_attr(int pusher, int dim, int order, int bytes)
 
 // 3D fixed-point tile current: a tile point receives at most 4 segments per particle of the
 // tile (at most cap slots per species), each value at most 3 |q| jn (weights along the motion
-// <= |q| jn, across it <= 3); the scale 2^S keeps that bound below 2^62.
-static void fx_scale_for(const TiledState *t, TiledArgs &a)
+// <= |q| jn, across it <= 3), and the fold adds at most 8 tiles per global point; the scale
+// 2^S keeps that bound below 2^62.
+static int fx_exponent(const TiledState *t)
 {
     double jn = 0.0;
-    for (int d = 0; d < t->dim; d++) jn = std::max(jn, (double)std::fabs(a.jn[d]));
+    for (int d = 0; d < t->dim; d++) jn = std::max(jn, t->dx[d] / push_dt(t) / 3.0);
     double bound = 0.0;
     for (size_t k = 0; k < t->cap.size() && k < t->qmax.size(); k++)
         bound += (double)t->cap[k] * t->qmax[k];
-    bound *= 12.0 * jn;
+    bound *= 12.0 * 8.0 * jn;
     int S = bound > 0.0 ? (int)std::floor(62.0 - std::log2(bound)) : 40;
-    S = std::max(-100, std::min(S, 100));
-    a.fx_scale = std::ldexp(1.0f, S);
-    a.fx_inv = std::ldexp(1.0, -S);
+    return std::max(-100, std::min(S, 100));
+}
+
+static void fx_scale_for(const TiledState *t, TiledArgs &a)
+{
+    a.fx_scale = std::ldexp(1.0f, fx_exponent(t));
 }
 
 static TiledArgs base_args(const TiledState *t)
@@ -499,6 +503,7 @@ FoldBox tiled_fold_box(TiledState *t, float *j)
     f.gcl = make_int3(g.gcl[0], g.gcl[1], g.gcl[2]);
     f.ofs = t->order == 1 ? 1 : (t->order == 4 ? 3 : 2);
     f.npts = 3 * g.npoints();
+    f.fx_inv = std::ldexp(1.0f, -fx_exponent(t));
     return f;
 }
 
@@ -680,16 +685,16 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     default: rc = push_tiled_launch_boris(t->dim, t->order, a, nt, t->threads, sm, st); break;
     }
     if (rc) return rc;
-    // deterministic FP64 re-summation of the tile currents into the global current
+    // deterministic re-summation of the tile currents into the global current
     const FoldBox f = tiled_fold_box(t, j);
     unsigned nb = blocks_for(f.npts, 256);
     if (nb > 152 * 16) nb = 152 * 16;
     if (t->dim == 2)
         k_tile_fold<2><<<nb, 256, 0, st>>>(f.th, f.tl, j, f.size, f.T, f.ntile, f.je, f.gcl,
-                                            f.ofs, f.npts);
+                                            f.ofs, f.npts, f.fx_inv);
     else
         k_tile_fold<3><<<nb, 256, 0, st>>>(f.th, f.tl, j, f.size, f.T, f.ntile, f.je, f.gcl,
-                                            f.ofs, f.npts);
+                                            f.ofs, f.npts, f.fx_inv);
     *launches += 2;
     return OSG_OK;
 }

@@ -111,9 +111,8 @@ struct TiledArgs {
     float *tile_hi;
     float *tile_lo;
     // 3D: the tile current is accumulated as 64-bit fixed point, value x fx_scale (a power of
-    // two chosen so that no tile point can overflow); fx_inv = 1 / fx_scale
+    // two chosen so that no tile point, nor the fold's sum of tiles, can overflow)
     float fx_scale;
-    double fx_inv;
     // bit d: axis d is open (no periodic wrap): particles that leave the box along it are
     // dropped (absorbed).  Bit 0 with the moving window along x1, or the axis of Lindman
     // open boundaries.  shift_x = 1 (a step that ends with a window move) stores every
@@ -276,7 +275,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     __shared__ float sLeaveF[LEAVE_QUEUE][8];    // offsets per axis, momenta, charge
     __shared__ int sNleave;
     // per-warp energy of every species, summed when the tile is done
-    __shared__ double sEne[MAX_TILED_SPECIES][8];
+    __shared__ float sEne[MAX_TILED_SPECIES][8];
     if (threadIdx.x == 0) sNleave = 0;
     __syncthreads();
 
@@ -300,7 +299,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
         const int n = nst + nar;
         int *hist = sHist + (s & 1) * ncell;
         // per-thread partial energy in FP32 (the reference sums in single precision per
-        // 464-particle chunk), summed over the block in double
+        // 464-particle chunk), summed per warp and per tile in FP32, across tiles in double
         float my_ene = 0.f;
         // ---- pass A: push every particle of the tile.  Particles that stay are written back
         //      to their own slot of the input slab (this CTA owns it) and counted per new cell,
@@ -548,7 +547,8 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
         }
         // ---- energy: per-warp partial (the tile's sum is taken when the tile is done)
         {
-            double w = (double)my_ene;
+            // FP32 (FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU)
+            float w = my_ene;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(FULL_MASK, w, o);
             if (lane == 0) sEne[s][warp] = w;
@@ -653,13 +653,13 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     // ---- the tile's energy of every species (the per-warp partials, written before the last
     //      block barrier)
     if ((int)threadIdx.x < a.nspec) {
-        double tot = 0.0;
+        float tot = 0.f;
         for (int w = 0; w < nwarp; w++) tot += sEne[threadIdx.x][w];
-        if (tot != 0.0) atomicAdd(a.ene + threadIdx.x, tot);
+        if (tot != 0.f) atomicAdd(a.ene + threadIdx.x, (double)tot);
     }
-    // ---- store the tile's current (with halo) for the tile-ordered FP64 re-summation as a
-    //      float pair (hi, lo): in 2D the warp copies and their compensations summed, in 3D
-    //      the fixed-point tile converted
+    // ---- store the tile's current (with halo) for the tile-ordered re-summation: in 2D the
+    //      warp copies and their compensations summed into a float pair (hi, lo); in 3D the
+    //      low and high words of the fixed-point tile
     {
         float *th = a.tile_hi + tile * (3L * nj);
         float *tl = a.tile_lo + tile * (3L * nj);
@@ -677,7 +677,9 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 th[idx] = t;
                 tl[idx] = lo - (t - hi);
             } else {
-                fx_to_pair(sJl[idx], sJh[idx], a.fx_inv, th[idx], tl[idx]);
+                // the fixed-point words as they are (k_tile_fold sums them as integers)
+                th[idx] = __uint_as_float(sJl[idx]);
+                tl[idx] = __uint_as_float(sJh[idx]);
             }
         }
     }
@@ -713,11 +715,14 @@ k_push_tiled_batch(const TiledArgs *__restrict__ boxes, const int2 *__restrict__
 }
 
 // Deterministic current flush: every point of the global current (guard cells included) is
-// the FP64 sum, in increasing tile order, of the tile currents (hi + lo) whose halo covers it,
-// rounded once to float.  A tile with origin cell t0 = tc * T + 1 covers the global positions
+// the sum of the tile currents whose halo covers it, rounded once to float.  2D: FP64 sum, in
+// increasing tile order, of the float pairs (hi + lo).  3D: exact 64-bit integer sum of the
+// fixed-point tile values (words lo, hi), converted with one rounding and scaled by fx_inv (a
+// power of two) -- no FP64 arithmetic, whose rate is low on this GPU.  A tile with origin cell t0 = tc * T + 1 covers the global positions
 // [tc * T - OFS + gcl, tc * T - OFS + gcl + je) along each axis (je = T + ORD + 2 points).
 struct FoldBox {
-    const float *th, *tl;   // tile currents (tl: compensation, or null)
+    const float *th, *tl;   // tile currents (2D: value and compensation; 3D: fixed-point words)
+    float fx_inv;           // 3D: 1 / the fixed-point scale
     float *j;               // global current
     int3 size, T, ntile, je, gcl;
     int ofs;
@@ -728,7 +733,8 @@ template <int DIM>
 __device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
                                                const float *__restrict__ tl,
                                                float *__restrict__ j, int3 size, int3 T,
-                                               int3 ntile, int3 je, int3 gcl, int ofs, long npts)
+                                               int3 ntile, int3 je, int3 gcl, int ofs, long npts,
+                                               float fx_inv)
 {
     OSG_GRID_LOOP(g, npts)
     {
@@ -755,6 +761,7 @@ __device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
         }
         const int nj = jea[0] * (DIM > 1 ? jea[1] : 1) * (DIM > 2 ? jea[2] : 1);
         double v = 0.0;
+        long long fx = 0;
         for (int tz = lo[2]; tz <= hi[2]; tz++)
             for (int ty = lo[1]; ty <= hi[1]; ty++)
                 for (int tx = lo[0]; tx <= hi[0]; tx++) {
@@ -763,19 +770,25 @@ __device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
                     const int ly = DIM > 1 ? gy - (ty * Ta[1] - ofs + gl[1]) : 0;
                     const int lz = DIM > 2 ? gz - (tz * Ta[2] - ofs + gl[2]) : 0;
                     const long o = tile * (3L * nj) + 3L * (lx + jea[0] * (ly + (long)jea[1] * lz)) + c;
-                    v += (double)th[o];
-                    if (tl) v += (double)tl[o];
+                    if constexpr (DIM == 3) {
+                        fx += (long long)(((unsigned long long)__float_as_uint(tl[o]) << 32) |
+                                          __float_as_uint(th[o]));
+                    } else {
+                        v += (double)th[o];
+                        if (tl) v += (double)tl[o];
+                    }
                 }
-        j[g] = (float)v;
+        if constexpr (DIM == 3) j[g] = __ll2float_rn(fx) * fx_inv;
+        else j[g] = (float)v;
     }
 }
 
 template <int DIM>
 __global__ void k_tile_fold(const float *__restrict__ th, const float *__restrict__ tl,
                             float *__restrict__ j, int3 size, int3 T, int3 ntile, int3 je,
-                            int3 gcl, int ofs, long npts)
+                            int3 gcl, int ofs, long npts, float fx_inv)
 {
-    tile_fold_body<DIM>(th, tl, j, size, T, ntile, je, gcl, ofs, npts);
+    tile_fold_body<DIM>(th, tl, j, size, T, ntile, je, gcl, ofs, npts, fx_inv);
 }
 
 // the same for every box of a batch (box = blockIdx.y)
@@ -783,7 +796,8 @@ template <int DIM>
 __global__ void k_batch_fold(const FoldBox *__restrict__ boxes)
 {
     const FoldBox &f = boxes[blockIdx.y];
-    tile_fold_body<DIM>(f.th, f.tl, f.j, f.size, f.T, f.ntile, f.je, f.gcl, f.ofs, f.npts);
+    tile_fold_body<DIM>(f.th, f.tl, f.j, f.size, f.T, f.ntile, f.je, f.gcl, f.ofs, f.npts,
+                        f.fx_inv);
 }
 
 // zero n ints at p for every range of a device table (one launch; defined in tiled.cu)

@@ -111,7 +111,7 @@ def test_fp32_engines_match_oracle(osg, oracle, engine, dim, order, nx, tile, st
 @pytest.mark.parametrize("dim,order,nx,tile", [(2, 2, [32, 24], [8, 8]),
                                                (3, 1, [16, 8, 8], [4, 4, 4]),
                                                (3, 2, [16, 8, 8], [4, 4, 4]),
-                                               (3, 4, [12, 12, 8], [4, 4, 4])])
+                                               (3, 4, [12, 12, 12], [4, 4, 4])])
 def test_tiled_cta_sizes_match_oracle(osg, oracle, monkeypatch, threads, dim, order, nx, tile):
     """The CTA size of the tiled push only reorders the particles and the current sums (2D
     per-warp copies; 3D fixed-point tile adds, whose sums do not depend on the order): 10 steps
