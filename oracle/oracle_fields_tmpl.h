@@ -622,6 +622,34 @@ void FN(ora_smooth)(int dim, const int *nx, const int *gcl, const int *gcu, R *f
 static int FN(step_walls) = 0;
 void FN(ora_set_walls)(int walls) { FN(step_walls) = walls; }
 
+/* moving window along x1 for the step below (0: periodic x1): no guard update of E, B or J
+ * along x1 (the p_bc_move_c boundary of the fields has no neighbour to exchange with,
+ * source/emf/boundary/os-emf-boundary.f90:779-820; the current's boundary type is p_bc_none,
+ * source/current/os-current-define.f03:240-251); particles are absorbed below cell 1 (:315 of
+ * source/spec/os-spec-boundary.f03) and reflected specularly above nx (:1276, 1293-1310) */
+static int FN(step_window) = 0;
+void FN(ora_set_window)(int on) { FN(step_window) = on ? 1 : 0; }
+
+/* the window's particle boundary along x1 on the pushed particles 1..np: above nx the particle
+ * goes to cell nx with x1 and u1 negated; below 1 it is absorbed, marked by a cell index
+ * ORA_GONE and zero charge and momentum (the caller removes it) */
+#define ORA_GONE (-(1 << 28))
+void FN(ora_particle_window)(int dim, const int *nx, int np, int *ix, R *x, R *u, R *q)
+{
+    for (int p = 0; p < np; p++) {
+        int *c = &ix[dim * p];
+        if (*c > nx[0]) {
+            *c = nx[0];
+            x[dim * p] = -x[dim * p];
+            u[3 * p] = -u[3 * p];
+        } else if (*c < 1) {
+            *c = ORA_GONE;
+            q[p] = K(0.0);
+            u[3 * p] = u[3 * p + 1] = u[3 * p + 2] = K(0.0);
+        }
+    }
+}
+
 /* smoothing applied after the current fold by the step below (order 0: none) */
 static int FN(step_smooth_ord)[3] = {0, 0, 0};
 static R FN(step_smooth_coef)[3 * 31];

@@ -640,12 +640,13 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
     ora_iter_tol_##SFXN = (TOL);                                                              \
     const int walls = step_walls_##SFXN;                                                      \
     const int oax = step_open_##SFXN; /* Lindman axis, -1: none */                            \
-    const int skip = walls | (oax >= 0 ? 1 << oax : 0);                                       \
+    const int win = step_window_##SFXN; /* moving window along x1 */                          \
+    const int skip = walls | (oax >= 0 ? 1 << oax : 0) | win;                                 \
     if (oax >= 0) {                                                                           \
         ora_open_guards_##SFXN(dim, nx, gcl, gcu, e, b, oax, step_lind_##SFXN);               \
     } else {                                                                                  \
-        ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, e, 0, walls);                             \
-        ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, b, 0, walls);                             \
+        ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, e, 0, walls | win);                       \
+        ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, b, 0, walls | win);                       \
     }                                                                                         \
     memset(j, 0, sizeof(R) * (size_t)gsz);                                                    \
     int nt = nthreads < 1 ? 1 : nthreads;                                                     \
@@ -671,6 +672,7 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
                                     step_ufl, step_seed, s, step_count, step_ttype);          \
         if (oax >= 0)                                                                         \
             ora_particle_absorb_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], q[s], oax);         \
+        if (win) ora_particle_window_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], q[s]);        \
         ora_particle_bound_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], walls);                  \
     }                                                                                         \
     if (nt > 1) {                                                                             \

@@ -68,6 +68,11 @@ void ora_set_walls_f32(int walls);
 void ora_set_pmc_f32(int pmc);
 void ora_set_pmc_f64(int pmc);
 void ora_set_walls_f64(int walls);
+/* moving window along x1 (on = 1) for the step functions below: no x1 guard update of E, B or
+ * J, particles absorbed below cell 1 (cell index set to ORA_GONE, -2^28) and reflected above
+ * nx */
+void ora_set_window_f32(int on);
+void ora_set_window_f64(int on);
 /* Lindman open boundaries at both edges of `axis` (-1: none) for the step functions below;
  * `state` holds 15 reals per interior point of the other axes, zeroed before the first step
  * and kept between steps */

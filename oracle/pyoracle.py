@@ -90,6 +90,7 @@ def _declare(L):
         getattr(L, f"ora_set_walls_{s_}").argtypes = [I]
         getattr(L, f"ora_set_pmc_{s_}").argtypes = [I]
         getattr(L, f"ora_set_open_{s_}").argtypes = [I, P]
+        getattr(L, f"ora_set_window_{s_}").argtypes = [I]
         getattr(L, f"ora_lindman_phase_{s_}").argtypes = [I, P, P, P, I, I, P, P, P, P, D]
     L.ora_set_thermal.argtypes = [I, P, P, C.c_uint32, C.c_uint64, I]
     L.ora_push_cyl_f32.argtypes = [I, P, P, P, P, I, I, C.c_float, I, P, P, P, P, P, P, P, P, D,
@@ -371,14 +372,17 @@ def lindman_phase(g: "Grid", prec, axis, what, e, b, state, dt):
 
 
 def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="boris",
-         iter_tol=1e-3, smooth=None, walls=0, open_fields=None, thermal=None, pmc=0):
+         iter_tol=1e-3, smooth=None, walls=0, open_fields=None, thermal=None, pmc=0,
+         window=False):
     """One full time step; species = list of dicts with ix, x, u, q, rqm.  walls (bit d):
     axis d bounded by conducting walls instead of periodic.  open_fields = (axis, state from
     lindman_state): Lindman open boundaries at both edges of that axis, particles absorbed
     there (left in the arrays with charge and momentum 0).  thermal = dict(mask, uth, ufl, seed,
     step, type: 0 thermal, 1 random dir, 2 waterbag): particles crossing the edges of the axes in mask (walled or open) are re-emitted from
     a thermal bath; step keys the random stream.  pmc (bit d, d walled): perfect magnetic
-    instead of electric conductor walls.
+    instead of electric conductor walls.  window=True: x1 is the axis of a moving window (no
+    guard update along it, particles absorbed below cell 1 -- removed from the species arrays
+    after the step -- and reflected above nx); the window's moves are Window.start_step.
     Returns the per-species energy sums (Boris: time-centred u^2/(gamma+1); exact pusher:
     gamma - 1 of the new momentum; both times q).  fast=True runs the -O3 -ffast-math build
     (timing only)."""
@@ -400,6 +404,7 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
             _p(b), _p(j), ns, _p(np_), ixs, xs, us, qs, _p(rqm), _p(ene), int(nthreads))
     getattr(L, f"ora_set_walls_{prec}")(int(walls))
     getattr(L, f"ora_set_pmc_{prec}")(int(pmc))
+    getattr(L, f"ora_set_window_{prec}")(1 if window else 0)
     if open_fields is not None:
         getattr(L, f"ora_set_open_{prec}")(int(open_fields[0]), _p(open_fields[1]))
     if thermal is not None:
@@ -414,11 +419,105 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     finally:
         getattr(L, f"ora_set_walls_{prec}")(0)
         getattr(L, f"ora_set_pmc_{prec}")(0)
+        getattr(L, f"ora_set_window_{prec}")(0)
         getattr(L, f"ora_set_open_{prec}")(-1, None)
         L.ora_set_thermal(0, None, None, 0, 0, 0)
     if smooth is not None:
         getattr(L, f"ora_set_smooth_{prec}")(None, None)
+    if window:
+        for sp in species:
+            keep = sp["ix"][:, 0] > ORA_GONE // 2
+            if not keep.all():
+                for k in ("ix", "x", "u", "q"):
+                    sp[k] = np.ascontiguousarray(sp[k][keep])
     return ene
+
+
+ORA_GONE = -(1 << 28)
+
+
+class Window:
+    """Moving window along x1 at c (the oracle's restatement):
+
+    * move_boundary_space_global (source/os-space.f90:508-566): every step starts by adding dt
+      to the window motion; once it reaches dx1 the window moves one cell;
+    * a move shifts E and B one cell down along x1, guard cells included, the last x1 plane
+      becoming zero (move_window_vdf, source/vdf/os-vdf.f03:56-205), lowers every particle's
+      x1 cell index by one (move_window_species, source/spec/os-species.f03:171-229) and fills
+      the new last plane of cells with plasma of the injected species (inject_std,
+      source/spec/psource/os-psource-std.f03:759-1120): ppc[d] particles per cell on the
+      OSIRIS lattice, at rest, charge sign(rqm) den / prod(ppc) with den the piecewise-linear
+      profile (prof_x, prof_f; 0 outside) at the particle's global x1 position.
+    Call start_step before every step(..., window=True)."""
+
+    def __init__(self, g: Grid, prec, species_index, ppc, prof_x, prof_f):
+        self.g, self.prec = g, prec
+        self.k = species_index
+        self.ppc = list(ppc) + [1] * (3 - len(ppc))
+        self.prof_x, self.prof_f = list(prof_x), list(prof_f)
+        self.xmoved = 0.0
+        self.moves = 0
+
+    def _den(self, x):
+        px, pf = self.prof_x, self.prof_f
+        if x < px[0] or x > px[-1]:
+            return 0.0
+        for i in range(1, len(px)):
+            if x <= px[i]:
+                w = (x - px[i - 1]) / (px[i] - px[i - 1])
+                return pf[i - 1] + w * (pf[i] - pf[i - 1])
+        return pf[-1]
+
+    def start_step(self, e, b, species, dt):
+        """Advance the window motion; on a move shift the fields and particles and inject.
+        Returns True when the window moved."""
+        self.xmoved += dt
+        if self.xmoved < self.g.dx[0]:
+            return False
+        self.xmoved -= self.g.dx[0]
+        self.moves += 1
+        for f in (e, b):
+            f[..., :-1, :] = f[..., 1:, :].copy()
+            f[..., -1, :] = 0
+        for sp in species:
+            sp["ix"][:, 0] -= 1
+        self._inject(species[self.k])
+        return True
+
+    def _inject(self, sp):
+        g, dim = self.g, self.g.dim
+        dt_ = dtype_of(self.prec)
+        ppc = self.ppc
+        per = int(np.prod(ppc[:dim]))
+        unit = np.float32(1.0) / np.float32(per) if dt_ == np.float32 else 1.0 / per
+        unit = (-1.0 if sp["rqm"] < 0 else 1.0) * float(unit)
+        ny = g.nx[1] if dim > 1 else 1
+        nz = g.nx[2] if dim > 2 else 1
+        ix, x, q = [], [], []
+        for ck in range(nz):
+            for cj in range(ny):
+                for sa in range(ppc[0]):
+                    for sb in range(ppc[1] if dim > 1 else 1):
+                        for sc in range(ppc[2] if dim > 2 else 1):
+                            # lattice offset (2 (s + 1) - 1 - ppc) * (0.5 / ppc), in the
+                            # particles' precision
+                            off = [dt_(2 * (s + 1) - 1 - p) * (dt_(0.5) / dt_(p))
+                                   for s, p in zip((sa, sb, sc), ppc)]
+                            xg = (self.moves + g.nx[0] - 0.5 + float(off[0])) * g.dx[0]
+                            den = self._den(xg)
+                            if dt_ == np.float32:
+                                den = float(np.float32(den))
+                            if not den > 0.0:
+                                continue
+                            ix.append([g.nx[0], 1 + cj, 1 + ck][:dim])
+                            x.append(off[:dim])
+                            q.append(den * unit)
+        if not q:
+            return
+        sp["ix"] = np.ascontiguousarray(np.vstack([sp["ix"], np.array(ix, np.int32)]))
+        sp["x"] = np.ascontiguousarray(np.vstack([sp["x"], np.array(x, dt_)]))
+        sp["u"] = np.ascontiguousarray(np.vstack([sp["u"], np.zeros((len(q), 3), dt_)]))
+        sp["q"] = np.ascontiguousarray(np.concatenate([sp["q"], np.array(q, dt_)]))
 
 
 def max_threads() -> int:

@@ -257,7 +257,12 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
     //  source/spec/os-spec-push.f03:1459-1460)
     const bool fortran_push = c.pusher != OSG_PUSHER_BORIS;
     const double push_dt = (sizeof(T) == 4 && !fortran_push) ? (double)(float)c.dt : c.dt;
-    const int open = s->window ? 1 : 0;   // x1 open while the window moves
+    // moving window: the reference's x1 boundary (p_bc_move_c) updates no guard cells of E,
+    // B or J (update_boundary_emf_bound, source/emf/boundary/os-emf-boundary.f90:779-820, has
+    // no neighbour along x1; the current's boundary type is p_bc_none, source/current/
+    // os-current-define.f03:240-251): the guards keep what the window shift and the Yee
+    // update leave there
+    const int win = s->window ? 1 : 0;
     // conducting walls: their guard cells hold the images set by the last field advance
     const int walls = c.walls;
     // Lindman open boundaries: no periodic update along their axis, the boundary planes come
@@ -269,9 +274,9 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
         open_guards<T>(s->g, (T *)s->e, (T *)s->b, oax, (const T *)s->lind, st);
         launches += 2 * (c.dim - 1) + 1;
     } else {
-        periodic_update<T>(s->g, (T *)s->e, 0, st, open, walls);
-        periodic_update<T>(s->g, (T *)s->b, 0, st, open, walls);
-        launches += 2 * c.dim;
+        periodic_update<T>(s->g, (T *)s->e, 0, st, 0, walls | win);
+        periodic_update<T>(s->g, (T *)s->b, 0, st, 0, walls | win);
+        launches += 2 * (c.dim - __builtin_popcount(walls | win));
     }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[1], st));
     OSG_CUDA(cudaMemsetAsync(s->j, 0, (size_t)s->esz * 3 * s->g.npoints(), st));
@@ -326,8 +331,8 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
         }
     }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[3], st));
-    periodic_update<T>(s->g, (T *)s->j, 1, st, open, skip);
-    launches += c.dim - (oax >= 0 ? 1 : 0);
+    periodic_update<T>(s->g, (T *)s->j, 1, st, 0, skip | win);
+    launches += c.dim - __builtin_popcount(skip | win);
     if (walls) {
         // current deposited beyond a wall comes back as its image (update_boundary_current,
         // source/current/os-current-define.f03:683-725)

@@ -487,10 +487,10 @@ __device__ __forceinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int n
 
 // ------------------------------------------------------------------------------------------
 // 3D deposit.  The CTA's current tile is one shared copy, accumulated exactly as 64-bit fixed
-// point (value x 2^S rounded to an integer; the host picks S so that no tile point can
-// overflow): every add is two native 32-bit integer atomics, the low word and then the high
-// word with the carry of the low one.  The tile sums therefore carry no rounding beyond the
-// one of each added value and do not depend on the order of the adds.
+// point (value x 2^S rounded to an integer): native 32-bit integer atomics on the low word,
+// and on the high word when the low one wraps (FP32 shared-memory atomics are compare-and-swap
+// loops on this GPU).  The tile sums therefore carry no rounding beyond the one of each added
+// value and do not depend on the order of the adds.
 // A warp deposits the segments of up to 32 rows together (its lanes' in-cell segments, or 32
 // queued face crossings): the rows write their values, CH3 at a time, into the warp's row
 // scratch (16 rows per pass); lane l owns columns 2l and 2l + 1 and sums them over each run
@@ -507,26 +507,18 @@ constexpr int SEGQ3_KEEP = 16;   // drain while more than this many wait (a roun
 
 constexpr int scratch_floats3() { return SROWS3 * RS3; }
 
-// exact add of v x scale, rounded to an integer, into the 64-bit fixed-point value (hi:lo).
-// Only 32-bit conversions are used (64-bit ones run on this GPU's slow FP64 pipe): y = v x scale
-// (exact, |y| < 2^62 by the choice of scale) splits as yh 2^32 + r with yh = rint(y / 2^32)
-// and |r| <= 2^31, both exact in float (r holds at most the 24 bits of y below 2^32); the
-// integer (yh, rint(r)) is then the two's complement pair (low word rint(r), high word
-// yh - 1 when rint(r) < 0).
-__device__ __forceinline__ void fx_add(unsigned *lo, unsigned *hi, float v, float scale)
+// Exact add of v x scale, rounded to an integer, into a 64-bit fixed-point value (hi:lo).
+// The host picks the scale so that every single add fits a 32-bit signed integer (a run sum of
+// up to 32 segment values included): the add converts once (fx_lo), adds the low word and
+// returns the high word's change, -1, 0 or +1 (fx_hi_delta): the sign extension of the add
+// plus the carry out of the low word.  It is non-zero only when the low word wraps, so the
+// high-word atomic seldom runs.  Callers issue the low-word adds of several values before
+// looking at their returns, so the round trips overlap.
+__device__ __forceinline__ int fx_lo(float v, float scale) { return __float2int_rn(v * scale); }
+
+__device__ __forceinline__ int fx_hi_delta(int fl, unsigned old)
 {
-    const float y = v * scale;
-    float yh = rintf(y * 2.3283064365386963e-10f);     // y / 2^32
-    float r = fmaf(-yh, 4294967296.0f, y);              // exact
-    if (r >= 2147483648.0f) {                            // keep rint(r) inside int32
-        r -= 4294967296.0f;
-        yh += 1.0f;
-    }
-    const int ri = __float2int_rn(r);
-    const unsigned fl = (unsigned)ri;
-    const unsigned fh = (unsigned)(__float2int_rn(yh) + (ri >> 31));
-    const unsigned old = atomicAdd(lo, fl);
-    atomicAdd(hi, fh + (old + fl < old ? 1u : 0u));
+    return (fl < 0 ? -1 : 0) + (old + (unsigned)fl < old ? 1 : 0);
 }
 
 // B-spline weights at both ends and longitudinal weights (q jn folded in) of one 3D segment
@@ -597,23 +589,6 @@ __device__ __forceinline__ void seg3_chunk(const Seg3W<ORD> &w, float *v)
             }
 }
 
-// values V0 .. V0 + N - 1 of the segment into a scratch row, 16 at a time (only 16 values
-// live in registers)
-template <int ORD, int V0, int N, int S = 0>
-__device__ __forceinline__ void seg3_row(const Seg3W<ORD> &w, float *row)
-{
-    constexpr int M = N - S < 16 ? N - S : 16;
-    static_assert(M % 2 == 0, "rows are written in float pairs");
-    float v[M];
-    seg3_chunk<ORD, V0 + S, M>(w, v);
-#pragma unroll
-    for (int k = 0; k + 4 <= M; k += 4)
-        *reinterpret_cast<float4 *>(row + S + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
-    if constexpr (M % 4 == 2)
-        *reinterpret_cast<float2 *>(row + S + M - 2) = make_float2(v[M - 2], v[M - 1]);
-    if constexpr (S + M < N) seg3_row<ORD, V0, N, S + M>(w, row);
-}
-
 // chunk C of rows_deposit3 (and the chunks after it)
 template <int ORD, int C>
 __device__ __forceinline__ void rows_chunk3(unsigned *Jl, unsigned *Jh, float *scr,
@@ -632,19 +607,26 @@ __device__ __forceinline__ void rows_chunk3(unsigned *Jl, unsigned *Jh, float *s
         o0 = seg_offset<3, ORD>(V0 + c0, jsy, jsz);
         o1 = seg_offset<3, ORD>(V0 + c0 + 1, jsy, jsz);
     }
+    // the chunk's values, computed once by every lane (rows_deposit3 is a function of its own,
+    // so they stay in registers)
+    float v[N];
+    if (has) {
+        seg3_chunk<ORD, V0, N>(w, v);
+    } else {
+#pragma unroll
+        for (int k = 0; k < N; k++) v[k] = 0.f;
+    }
     float2 acc = make_float2(0.f, 0.f);
 #pragma unroll 1
     for (int h = 0; h < 2; h++) {
         __syncwarp();
         if ((lane >> 4) == h) {
             float *row = scr + (lane & 15) * RS3;
-            if (has) {
-                seg3_row<ORD, V0, N>(w, row);
-            } else {
 #pragma unroll
-                for (int k = 0; k + 2 <= N; k += 2)
-                    *reinterpret_cast<float2 *>(row + k) = make_float2(0.f, 0.f);
-            }
+            for (int k = 0; k + 4 <= N; k += 4)
+                *reinterpret_cast<float4 *>(row + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+            if constexpr (N % 4 == 2)
+                *reinterpret_cast<float2 *>(row + N - 2) = make_float2(v[N - 2], v[N - 1]);
         }
         __syncwarp();
         const unsigned eh = ends >> (SROWS3 * h);
@@ -654,8 +636,12 @@ __device__ __forceinline__ void rows_chunk3(unsigned *Jl, unsigned *Jh, float *s
             if ((eh >> rr) & 1u) {
                 const int rb = __shfl_sync(FULL_MASK, b, SROWS3 * h + rr);
                 if (own && rb >= 0) {
-                    fx_add(Jl + rb + o0, Jh + rb + o0, acc.x, scale);
-                    fx_add(Jl + rb + o1, Jh + rb + o1, acc.y, scale);
+                    const int l0 = fx_lo(acc.x, scale), l1 = fx_lo(acc.y, scale);
+                    const unsigned q0 = atomicAdd(Jl + rb + o0, (unsigned)l0);
+                    const unsigned q1 = atomicAdd(Jl + rb + o1, (unsigned)l1);
+                    const int d0 = fx_hi_delta(l0, q0), d1 = fx_hi_delta(l1, q1);
+                    if (d0) atomicAdd(Jh + rb + o0, (unsigned)d0);
+                    if (d1) atomicAdd(Jh + rb + o1, (unsigned)d1);
                 }
                 acc = make_float2(0.f, 0.f);
             }
@@ -685,10 +671,48 @@ __device__ __noinline__ void rows_deposit3(unsigned *Jl, unsigned *Jh, float *sc
     rows_chunk3<ORD, 0>(Jl, Jh, scr, w, has, b, ends, jsy, jsz, scale);
 }
 
-// deposit the top entries of the warp's queue of 3D face crossings (up to 32 at a time)
-// while more than keep wait
+// values V0 .. of one segment added straight into the tile, 16 computed at a time
+template <int ORD, int C>
+__device__ __forceinline__ void lane_chunk3(unsigned *Jl, unsigned *Jh, const Seg3W<ORD> &w,
+                                            int jsy, int jsz, float scale)
+{
+    constexpr int NV = SegVals<3, ORD>::NV;
+    constexpr int V0 = C * 16;
+    constexpr int N = NV - V0 < 16 ? NV - V0 : 16;
+    float v[N];
+    seg3_chunk<ORD, V0, N>(w, v);
+    int fl[N];
+    unsigned old[N];
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        fl[k] = fx_lo(v[k], scale);
+        old[k] = atomicAdd(Jl + seg_offset<3, ORD>(V0 + k, jsy, jsz), (unsigned)fl[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        const int dh = fx_hi_delta(fl[k], old[k]);
+        if (dh) atomicAdd(Jh + seg_offset<3, ORD>(V0 + k, jsy, jsz), (unsigned)dh);
+    }
+    if constexpr (V0 + N < NV) lane_chunk3<ORD, C + 1>(Jl, Jh, w, jsy, jsz, scale);
+}
+
+// One 3D segment per lane (has = false: none), each lane adding its own values straight into
+// the tile: for the face crossings, which seldom share a cell, so that run sums would not pay
 template <int ORD>
-__device__ __forceinline__ void segq_drain3(unsigned *Jl, unsigned *Jh, float *scr, SegRec *sq,
+__device__ __noinline__ void lanes_deposit3(unsigned *Jl, unsigned *Jh, const SegRec r,
+                                            bool has, const float *jn, int jsy, int jsz,
+                                            float scale)
+{
+    if (!has) return;
+    Seg3W<ORD> w;
+    seg3_weights<ORD>(r, jn, w);
+    lane_chunk3<ORD, 0>(Jl + r.base, Jh + r.base, w, jsy, jsz, scale);
+}
+
+// deposit the top entries of the warp's queue of 3D face crossings (up to 32 at a time, one
+// per lane) while more than keep wait
+template <int ORD>
+__device__ __forceinline__ void segq_drain3(unsigned *Jl, unsigned *Jh, SegRec *sq,
                                             int &qn, int keep, const float *jn, int jsy,
                                             int jsz, float scale)
 {
@@ -700,7 +724,7 @@ __device__ __forceinline__ void segq_drain3(unsigned *Jl, unsigned *Jh, float *s
         const bool has = lane < take;
         if (has) r = sq[first + lane];
         qn = first;
-        rows_deposit3<ORD>(Jl, Jh, scr, r, has, jn, jsy, jsz, scale);
+        lanes_deposit3<ORD>(Jl, Jh, r, has, jn, jsy, jsz, scale);
     }
 }
 

@@ -157,19 +157,18 @@ static cudaError_t push_attr(int pusher, int dim, int order, int bytes)
     }
 }
 
-// 3D fixed-point tile current: a tile point receives at most 4 segments per particle of the
-// tile (at most cap slots per species), each value at most 3 |q| jn (weights along the motion
-// <= |q| jn, across it <= 3), and the fold adds at most 8 tiles per global point; the scale
-// 2^S keeps that bound below 2^62.
+// 3D fixed-point tile current: every add must fit a 32-bit signed integer.  A segment value
+// is at most 3 |q| jn (weights along the motion <= |q| jn, across it <= 3) and an add is a run
+// sum of at most 32 of them, so 2^S = 2^31 / (96 qmax jn).  The 64-bit sums cannot overflow
+// for any particle count a GPU holds.
 static int fx_exponent(const TiledState *t)
 {
     double jn = 0.0;
     for (int d = 0; d < t->dim; d++) jn = std::max(jn, t->dx[d] / push_dt(t) / 3.0);
-    double bound = 0.0;
-    for (size_t k = 0; k < t->cap.size() && k < t->qmax.size(); k++)
-        bound += (double)t->cap[k] * t->qmax[k];
-    bound *= 12.0 * 8.0 * jn;
-    int S = bound > 0.0 ? (int)std::floor(62.0 - std::log2(bound)) : 40;
+    double qm = 0.0;
+    for (double v : t->qmax) qm = std::max(qm, v);
+    const double bound = 96.0 * qm * jn;
+    int S = bound > 0.0 ? (int)std::floor(31.0 - std::log2(bound)) : 40;
     return std::max(-100, std::min(S, 100));
 }
 
@@ -668,7 +667,8 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     // the push writes every tile's sorted count and adds arrivals to zeroed counters
     OSG_CUDA(cudaMemsetAsync(t->d_arr[1 - parity], 0, sizeof(int) * MAX_TILED_SPECIES * t->ntiles, st));
     TiledArgs a = tiled_args(t, parity, e, b, j, d_ene, d_status);
-    a.open = (t->window ? 1 : 0) | t->open_fields;
+    a.open = t->open_fields;
+    a.window = t->window ? 1 : 0;
     a.shift_x = t->window && shift ? 1 : 0;
     const size_t sm = t->smem_bytes;
     const unsigned nt = (unsigned)t->ntiles;

@@ -113,11 +113,12 @@ struct TiledArgs {
     // 3D: the tile current is accumulated as 64-bit fixed point, value x fx_scale (a power of
     // two chosen so that no tile point, nor the fold's sum of tiles, can overflow)
     float fx_scale;
-    // bit d: axis d is open (no periodic wrap): particles that leave the box along it are
-    // dropped (absorbed).  Bit 0 with the moving window along x1, or the axis of Lindman
-    // open boundaries.  shift_x = 1 (a step that ends with a window move) stores every
+    // bit d: axis d is not periodic and absorbs particles at both edges (the axis of Lindman
+    // open boundaries).  window = 1: x1 is the moving window's axis (absorbing below,
+    // reflecting above), and shift_x = 1 (a step that ends with a window move) stores every
     // particle one cell lower in x1
     int open;
+    int window;
     int shift_x;
     // bit d: axis d is bounded by conducting walls (particles reflect specularly)
     int walls;
@@ -412,7 +413,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 }
                 // non-periodic axes (a launch-uniform test, so the periodic box pays one branch)
                 bool gone = false;
-                if (a.walls | a.open) {
+                if (a.walls | a.open | a.window) {
 #pragma unroll
                     for (int d = 0; d < DIM; d++) {
                         if ((a.walls >> d) & 1) {
@@ -424,10 +425,24 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                                 xo[d] = -xo[d];
                                 un[d] = -un[d];
                             }
+                        } else if (d == 0 && a.window) {
+                            // moving window along x1: the upper edge reflects specularly
+                            // (p_bc_move_c behaves as p_bc_specular there, source/spec/
+                            // os-spec-boundary.f03:1276, 1293-1310), the lower one absorbs
+                            // (:315); a particle is stored one cell lower when the step ends
+                            // with a window move and leaves when that puts it below cell 1
+                            int cx = cn[0];
+                            if (cx > a.nx[0]) {
+                                cx = a.nx[0];
+                                xo[0] = -xo[0];
+                                un[0] = -un[0];
+                            }
+                            cw[0] = cx - a.shift_x;
+                            gone = gone || cn[0] < 1 || cw[0] < 1;
                         } else if ((a.open >> d) & 1) {
-                            // open axis: a particle outside [1, nx] has left the box or the
-                            // window; its current of this step is already in the segments
-                            cw[d] = cn[d] - (d == 0 ? a.shift_x : 0);
+                            // open axis (Lindman): a particle outside [1, nx] has left the
+                            // box (absorbed); its current of this step is in the segments
+                            cw[d] = cn[d];
                             gone = gone || cw[d] < 1 || cw[d] > a.nx[d];
                         }
                     }
@@ -536,7 +551,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 } else {
                     if (t > 0) {
                         segq_push(sQ, qn, hs, sg[t]);
-                        segq_drain3<ORD>(sJl, sJh, scr, sQ, qn, SEGQ3_KEEP, a.jn, jsy, jsz,
+                        segq_drain3<ORD>(sJl, sJh, sQ, qn, SEGQ3_KEEP, a.jn, jsy, jsz,
                                          a.fx_scale);
                         continue;
                     }
@@ -648,7 +663,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     // ---- the face crossings still queued (the queue carries over from one species to the
     //      next: its entries hold their own charge)
     if constexpr (DIM == 2) segq_drain<ORD>(sJw, sQ, qn, 1, a.jn, scr, cs);
-    else segq_drain3<ORD>(sJl, sJh, scr, sQ, qn, 0, a.jn, jsy, jsz, a.fx_scale);
+    else segq_drain3<ORD>(sJl, sJh, sQ, qn, 0, a.jn, jsy, jsz, a.fx_scale);
     __syncthreads();
     // ---- the tile's energy of every species (the per-warp partials, written before the last
     //      block barrier)
