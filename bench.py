@@ -19,6 +19,7 @@ JSON line keys beyond the base contract:
   fp64_error    normwise difference of E, B, J and the relative difference of the kinetic and
                 field energies between the mixed-precision (tiled FP32) and the plain FP64
                 engine after the same number of steps from the same load
+  run_to_run    normwise difference of E, B, J between two identical runs of the tiled engine
 --impl reference times the CPU oracle port (the reference's CPU path restated; the
 reference's own AVX2 kernels do not build on this Arm host) with all host threads.
 """
@@ -240,6 +241,18 @@ def run_native(args):
     for s in sp:
         sim32.add_species(-1.0, *s)
     sim32.step(n_err)
+    # run-to-run spread of the mixed-precision engine: the same load and steps again (the tile
+    # sums are deterministic; the in-tile particle order, which follows the arrival order of
+    # migrating particles, is not, and the FP32 run sums follow it)
+    sim32b = osg.Simulation(w["nx"], w["dx"], w["dt"], order=w["order"], precision=32,
+                            engine=osg.ENGINE_TILED, capacity=4.0)
+    for s in sp:
+        sim32b.add_species(-1.0, *s)
+    sim32b.step(n_err)
+    spread = {"steps": n_err, "norm": "max|run1 - run2| / max|run2| over the grid"}
+    for name, a, b in zip("EBJ", sim32.fields(), sim32b.fields()):
+        spread[name] = float(np.abs(a.astype(np.float64) - b).max() / np.abs(b).max())
+    sim32b.close()
     fp64_error = {"steps": n_err, "norm": "max|mixed - fp64| / max|fp64| over the grid"}
     f32, f64 = sim32.fields(), sim64.fields()
     for name, a, b in (("E", f32[0], f64[0]), ("B", f32[1], f64[1]), ("J", f32[2], f64[2])):
@@ -280,6 +293,7 @@ def run_native(args):
         "fp64_plain": {"value": v64, "unit": METRIC, "steps": n64,
                        "ratio_mixed_over_fp64": value / world / v64},
         "fp64_error": fp64_error,
+        "run_to_run": spread,
         "gpu_launches": launches,
         "tile_occupancy_max": occupancy,
         "clocks": clk.summary(),

@@ -490,30 +490,20 @@ __device__ __forceinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int n
 // point (value x 2^S rounded to an integer): native 32-bit integer atomics on the low word,
 // and on the high word when the low one wraps (FP32 shared-memory atomics are compare-and-swap
 // loops on this GPU).  The tile sums therefore carry no rounding beyond the one of each added
-// value and do not depend on the order of the adds.
-// A warp deposits the segments of up to 32 rows together (its lanes' in-cell segments, or 32
-// queued face crossings): the rows write their values, CH3 at a time, into the warp's row
-// scratch (16 rows per pass); lane l owns columns 2l and 2l + 1 and sums them over each run
-// of consecutive rows with one stencil origin (the tile is sorted by cell, so a cell's
-// particles sit on neighbouring lanes), adding each run's sum once.  Within one add
-// instruction the lanes hold different values of one segment: their addresses differ.
+// value and do not depend on the order of the adds.  Every lane adds the values of its own
+// segment (lanes_deposit3); the face crossings wait in a per-warp queue so that they are
+// deposited by full warps.
 // ------------------------------------------------------------------------------------------
-constexpr int CH3 = 48;          // values per chunk
-constexpr int RS3 = 52;          // row stride in floats: 16-byte rows of 13 (odd) 16-byte
-                                 // units, so the 16-byte writes of 8 lanes hit distinct banks
-constexpr int SROWS3 = 16;       // rows per scratch pass (the two half warps in turn)
 constexpr int SEGQ3 = 48;        // queued face crossings per warp
 constexpr int SEGQ3_KEEP = 16;   // drain while more than this many wait (a round adds <= 32)
 
-constexpr int scratch_floats3() { return SROWS3 * RS3; }
-
 // Exact add of v x scale, rounded to an integer, into a 64-bit fixed-point value (hi:lo).
-// The host picks the scale so that every single add fits a 32-bit signed integer (a run sum of
-// up to 32 segment values included): the add converts once (fx_lo), adds the low word and
-// returns the high word's change, -1, 0 or +1 (fx_hi_delta): the sign extension of the add
-// plus the carry out of the low word.  It is non-zero only when the low word wraps, so the
-// high-word atomic seldom runs.  Callers issue the low-word adds of several values before
-// looking at their returns, so the round trips overlap.
+// The host picks the scale so that every single add (one segment value) fits a 32-bit signed
+// integer: the add converts once (fx_lo), adds the low word and returns the high word's
+// change, -1, 0 or +1 (fx_hi_delta): the sign extension of the add plus the carry out of the
+// low word.  It is non-zero only when the low word wraps, so the high-word atomic seldom runs.
+// Callers issue the low-word adds of several values before looking at their returns, so the
+// round trips overlap.
 __device__ __forceinline__ int fx_lo(float v, float scale) { return __float2int_rn(v * scale); }
 
 __device__ __forceinline__ int fx_hi_delta(int fl, unsigned old)
@@ -548,165 +538,74 @@ __device__ __forceinline__ float wperp(float s0a, float s1a, float s0b, float s1
     return fmaf(0.5f, t2, t1);
 }
 
-// values V0 .. V0 + N - 1 of a segment, in the seg_offset order
-//   j1 [k3][k2][k1 < ORD], j2 [k3][k2 < ORD][k1], j3 [k3 < ORD][k2][k1]
-template <int ORD, int V0, int N>
-__device__ __forceinline__ void seg3_chunk(const Seg3W<ORD> &w, float *v)
+// v[k] for a runtime index k < N (a chain of selects: the arrays stay in registers)
+template <int N>
+__device__ __forceinline__ float pick(const float (&v)[N], int k)
 {
-    constexpr int NP = ORD + 1, B = ORD * NP * NP;
+    float r = v[0];
 #pragma unroll
-    for (int k3 = 0; k3 < NP; k3++)
-#pragma unroll
-        for (int k2 = 0; k2 < NP; k2++)
-#pragma unroll
-            for (int k1 = 0; k1 < ORD; k1++) {
-                const int n = (k3 * NP + k2) * ORD + k1;
-                if (n >= V0 && n < V0 + N)
-                    v[n - V0] = w.wl[0][k1] * wperp(w.s0[1][k2], w.s1[1][k2], w.s0[2][k3],
-                                                    w.s1[2][k3]);
-            }
-#pragma unroll
-    for (int k3 = 0; k3 < NP; k3++)
-#pragma unroll
-        for (int k2 = 0; k2 < ORD; k2++)
-#pragma unroll
-            for (int k1 = 0; k1 < NP; k1++) {
-                const int n = B + (k3 * ORD + k2) * NP + k1;
-                if (n >= V0 && n < V0 + N)
-                    v[n - V0] = w.wl[1][k2] * wperp(w.s0[0][k1], w.s1[0][k1], w.s0[2][k3],
-                                                    w.s1[2][k3]);
-            }
-#pragma unroll
-    for (int k3 = 0; k3 < ORD; k3++)
-#pragma unroll
-        for (int k2 = 0; k2 < NP; k2++)
-#pragma unroll
-            for (int k1 = 0; k1 < NP; k1++) {
-                const int n = 2 * B + (k3 * NP + k2) * NP + k1;
-                if (n >= V0 && n < V0 + N)
-                    v[n - V0] = w.wl[2][k3] * wperp(w.s0[0][k1], w.s1[0][k1], w.s0[1][k2],
-                                                    w.s1[1][k2]);
-            }
-}
-
-// chunk C of rows_deposit3 (and the chunks after it)
-template <int ORD, int C>
-__device__ __forceinline__ void rows_chunk3(unsigned *Jl, unsigned *Jh, float *scr,
-                                            const Seg3W<ORD> &w, bool has, int b,
-                                            unsigned ends, int jsy, int jsz, float scale)
-{
-    constexpr int NV = SegVals<3, ORD>::NV;
-    constexpr int V0 = C * CH3;
-    constexpr int N = NV - V0 < CH3 ? NV - V0 : CH3;
-    static_assert(N % 2 == 0, "chunks hold whole column pairs");
-    const int lane = (int)(threadIdx.x & 31);
-    const int c0 = 2 * lane;   // the column pair this lane sums
-    const bool own = c0 < N;
-    int o0 = 0, o1 = 0;
-    if (own) {
-        o0 = seg_offset<3, ORD>(V0 + c0, jsy, jsz);
-        o1 = seg_offset<3, ORD>(V0 + c0 + 1, jsy, jsz);
-    }
-    // the chunk's values, computed once by every lane (rows_deposit3 is a function of its own,
-    // so they stay in registers)
-    float v[N];
-    if (has) {
-        seg3_chunk<ORD, V0, N>(w, v);
-    } else {
-#pragma unroll
-        for (int k = 0; k < N; k++) v[k] = 0.f;
-    }
-    float2 acc = make_float2(0.f, 0.f);
-#pragma unroll 1
-    for (int h = 0; h < 2; h++) {
-        __syncwarp();
-        if ((lane >> 4) == h) {
-            float *row = scr + (lane & 15) * RS3;
-#pragma unroll
-            for (int k = 0; k + 4 <= N; k += 4)
-                *reinterpret_cast<float4 *>(row + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
-            if constexpr (N % 4 == 2)
-                *reinterpret_cast<float2 *>(row + N - 2) = make_float2(v[N - 2], v[N - 1]);
-        }
-        __syncwarp();
-        const unsigned eh = ends >> (SROWS3 * h);
-#pragma unroll 4
-        for (int rr = 0; rr < SROWS3; rr++) {
-            if (own) acc = __fadd2_rn(acc, *reinterpret_cast<const float2 *>(scr + rr * RS3 + c0));
-            if ((eh >> rr) & 1u) {
-                const int rb = __shfl_sync(FULL_MASK, b, SROWS3 * h + rr);
-                if (own && rb >= 0) {
-                    const int l0 = fx_lo(acc.x, scale), l1 = fx_lo(acc.y, scale);
-                    const unsigned q0 = atomicAdd(Jl + rb + o0, (unsigned)l0);
-                    const unsigned q1 = atomicAdd(Jl + rb + o1, (unsigned)l1);
-                    const int d0 = fx_hi_delta(l0, q0), d1 = fx_hi_delta(l1, q1);
-                    if (d0) atomicAdd(Jh + rb + o0, (unsigned)d0);
-                    if (d1) atomicAdd(Jh + rb + o1, (unsigned)d1);
-                }
-                acc = make_float2(0.f, 0.f);
-            }
-        }
-    }
-    __syncwarp();
-    if constexpr (V0 + N < NV)
-        rows_chunk3<ORD, C + 1>(Jl, Jh, scr, w, has, b, ends, jsy, jsz, scale);
-}
-
-// Warp-collective deposit of one 3D segment per lane (has = false: none); base = offset of
-// the segment's stencil origin in the current tile.  Runs = maximal groups of consecutive
-// lanes with one base.  Not inlined: the push calls it from several places (the in-cell
-// segments, the queue drains), and one copy of its code keeps the kernel's instruction
-// footprint and register pressure down.
-template <int ORD>
-__device__ __noinline__ void rows_deposit3(unsigned *Jl, unsigned *Jh, float *scr,
-                                           const SegRec r, bool has, const float *jn, int jsy,
-                                           int jsz, float scale)
-{
-    const int lane = (int)(threadIdx.x & 31);
-    const int b = has ? r.base : -1;
-    const int nb = __shfl_down_sync(FULL_MASK, b, 1);
-    const unsigned ends = __ballot_sync(FULL_MASK, lane == 31 || nb != b);
-    Seg3W<ORD> w;
-    if (has) seg3_weights<ORD>(r, jn, w);
-    rows_chunk3<ORD, 0>(Jl, Jh, scr, w, has, b, ends, jsy, jsz, scale);
-}
-
-// values V0 .. of one segment added straight into the tile, 16 computed at a time
-template <int ORD, int C>
-__device__ __forceinline__ void lane_chunk3(unsigned *Jl, unsigned *Jh, const Seg3W<ORD> &w,
-                                            int jsy, int jsz, float scale)
-{
-    constexpr int NV = SegVals<3, ORD>::NV;
-    constexpr int V0 = C * 16;
-    constexpr int N = NV - V0 < 16 ? NV - V0 : 16;
-    float v[N];
-    seg3_chunk<ORD, V0, N>(w, v);
-    int fl[N];
-    unsigned old[N];
-#pragma unroll
-    for (int k = 0; k < N; k++) {
-        fl[k] = fx_lo(v[k], scale);
-        old[k] = atomicAdd(Jl + seg_offset<3, ORD>(V0 + k, jsy, jsz), (unsigned)fl[k]);
-    }
-#pragma unroll
-    for (int k = 0; k < N; k++) {
-        const int dh = fx_hi_delta(fl[k], old[k]);
-        if (dh) atomicAdd(Jh + seg_offset<3, ORD>(V0 + k, jsy, jsz), (unsigned)dh);
-    }
-    if constexpr (V0 + N < NV) lane_chunk3<ORD, C + 1>(Jl, Jh, w, jsy, jsz, scale);
+    for (int j = 1; j < N; j++) r = k == j ? v[j] : r;
+    return r;
 }
 
 // One 3D segment per lane (has = false: none), each lane adding its own values straight into
-// the tile: for the face crossings, which seldom share a cell, so that run sums would not pay
+// the tile.  The values come in 3 (ORD + 1) blocks of ORD (ORD + 1) -- block (c, k) holds
+// component c at plane k: j1 and j2 over z planes, j3 over y planes -- each the outer product
+// of the longitudinal weights of c with a perpendicular weight vector.  The lanes take the
+// blocks in a rotated order (lane l starts at block l mod blocks), so that lanes of one cell
+// add to different addresses in each atomic instruction; the loop over blocks is not
+// unrolled (small code, selects for the block's weights).
 template <int ORD>
 __device__ __noinline__ void lanes_deposit3(unsigned *Jl, unsigned *Jh, const SegRec r,
                                             bool has, const float *jn, int jsy, int jsz,
                                             float scale)
 {
+    constexpr int NP = ORD + 1, NBLK = 3 * NP;
     if (!has) return;
     Seg3W<ORD> w;
     seg3_weights<ORD>(r, jn, w);
-    lane_chunk3<ORD, 0>(Jl + r.base, Jh + r.base, w, jsy, jsz, scale);
+    unsigned *jl = Jl + r.base, *jh = Jh + r.base;
+    const int rot = (int)(threadIdx.x & 31) % NBLK;
+#pragma unroll 1
+    for (int t = 0; t < NBLK; t++) {
+        int blk = t + rot;
+        if (blk >= NBLK) blk -= NBLK;
+        const int c = blk / NP, k = blk - c * NP;
+        // longitudinal weights of component c; perpendicular weights along axis A (y for j1,
+        // x for j2, j3) and, at plane k, along axis B (z for j1, j2; y for j3)
+        float a[ORD], A0[NP], A1[NP];
+#pragma unroll
+        for (int i = 0; i < ORD; i++) a[i] = c == 0 ? w.wl[0][i] : (c == 1 ? w.wl[1][i] : w.wl[2][i]);
+#pragma unroll
+        for (int m = 0; m < NP; m++) {
+            A0[m] = c == 0 ? w.s0[1][m] : w.s0[0][m];
+            A1[m] = c == 0 ? w.s1[1][m] : w.s1[0][m];
+        }
+        const float B0 = c == 2 ? pick(w.s0[1], k) : pick(w.s0[2], k);
+        const float B1 = c == 2 ? pick(w.s1[1], k) : pick(w.s1[2], k);
+        const int si = c == 0 ? 3 : (c == 1 ? jsy : jsz);
+        const int sm = c == 0 ? jsy : 3;
+        const int sk = c == 2 ? jsy : jsz;
+        const int o0 = c + sk * k;
+        int fl[ORD][NP];
+        unsigned old[ORD][NP];
+#pragma unroll
+        for (int m = 0; m < NP; m++) {
+            const float wp = wperp(A0[m], A1[m], B0, B1);
+#pragma unroll
+            for (int i = 0; i < ORD; i++) {
+                fl[i][m] = fx_lo(a[i] * wp, scale);
+                old[i][m] = atomicAdd(jl + o0 + si * i + sm * m, (unsigned)fl[i][m]);
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < NP; m++)
+#pragma unroll
+            for (int i = 0; i < ORD; i++) {
+                const int dh = fx_hi_delta(fl[i][m], old[i][m]);
+                if (dh) atomicAdd(jh + o0 + si * i + sm * m, (unsigned)dh);
+            }
+    }
 }
 
 // deposit the top entries of the warp's queue of 3D face crossings (up to 32 at a time, one

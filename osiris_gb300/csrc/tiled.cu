@@ -158,16 +158,16 @@ static cudaError_t push_attr(int pusher, int dim, int order, int bytes)
 }
 
 // 3D fixed-point tile current: every add must fit a 32-bit signed integer.  A segment value
-// is at most 3 |q| jn (weights along the motion <= |q| jn, across it <= 3) and an add is a run
-// sum of at most 32 of them, so 2^S = 2^31 / (96 qmax jn).  The 64-bit sums cannot overflow
-// for any particle count a GPU holds.
+// is at most 3 |q| jn (weights along the motion <= |q| jn, across it <= 3); with a factor 2 of
+// margin, 2^S = 2^31 / (6 qmax jn).  The 64-bit sums cannot overflow for any particle count a
+// GPU holds.
 static int fx_exponent(const TiledState *t)
 {
     double jn = 0.0;
     for (int d = 0; d < t->dim; d++) jn = std::max(jn, t->dx[d] / push_dt(t) / 3.0);
     double qm = 0.0;
     for (double v : t->qmax) qm = std::max(qm, v);
-    const double bound = 96.0 * qm * jn;
+    const double bound = 6.0 * qm * jn;
     int S = bound > 0.0 ? (int)std::floor(31.0 - std::log2(bound)) : 40;
     return std::max(-100, std::min(S, 100));
 }
@@ -220,9 +220,7 @@ static size_t smem_for(int dim, int order, const int *T, int threads)
     size_t cells = 1;
     for (int d = 0; d < dim; d++) cells *= (size_t)T[d];
     const size_t hist = 2 * cells * sizeof(int);
-    if (dim != 2)
-        return nf * sizeof(float) + warps * scratch_floats3() * sizeof(float) +
-               warps * SEGQ3 * sizeof(SegRec) + hist;
+    if (dim != 2) return nf * sizeof(float) + warps * SEGQ3 * sizeof(SegRec) + hist;
     const int nv = 2 * order * NP + NP * NP;
     const size_t scratch = warps * (size_t)(nv + 1) * SCR_LD * sizeof(float);
     return nf * sizeof(float) + scratch + warps * SEGQ * sizeof(SegRec) + hist;

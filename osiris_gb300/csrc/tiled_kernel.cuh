@@ -209,7 +209,7 @@ __device__ __forceinline__ void discard_dead_slab(const Slabs &in, long slab, in
 // In 2D every warp accumulates into its own copy of the current tile (with a two-sum
 // compensation), so its adds are plain shared read-modify-writes; the copies are summed when
 // the tile is flushed.  In 3D the warps share one current tile, accumulated exactly in 64-bit
-// fixed point by integer atomics (rows_deposit3).
+// fixed point by integer atomics (lanes_deposit3).
 // CTAs of up to 256 threads.  2D linear/quadratic: three resident CTAs per SM (at most 85
 // registers per thread, measured fastest on GB300); 2D quartic: one (it needs ~250 registers
 // without spilling); otherwise two
@@ -261,9 +261,9 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     for (int idx = threadIdx.x; idx < njall + jlo; idx += nthr) sJ[idx] = 0.0f;
     unsigned *sJl = reinterpret_cast<unsigned *>(sJ), *sJh = sJl + jlo;
     // dynamic shared memory after the current tile (16-byte aligned): per-warp value scratch
-    // and queue of face-crossing segments, then two per-cell histograms of the tile sort (one
+    // (2D) and queue of face-crossing segments, then two per-cell histograms of the tile sort (one
     // per species, alternating, so the next one is cleared while the current one is used)
-    constexpr int SCRF = DIM == 2 ? scratch_floats2<ORD>() : scratch_floats3();
+    constexpr int SCRF = DIM == 2 ? scratch_floats2<ORD>() : 0;
     constexpr int QCAP = DIM == 2 ? SEGQ : SEGQ3;
     float *scr = smem + ((6 * ne + njall + jlo + 3) & ~3);
     SegRec *sQ0 = reinterpret_cast<SegRec *>(scr + nwarp * SCRF);
@@ -556,7 +556,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                         continue;
                     }
                     if (!__any_sync(FULL_MASK, hs)) break;
-                    rows_deposit3<ORD>(sJl, sJh, scr, sg[0], hs, a.jn, jsy, jsz, a.fx_scale);
+                    lanes_deposit3<ORD>(sJl, sJh, sg[0], hs, a.jn, jsy, jsz, a.fx_scale);
                 }
             }
         }

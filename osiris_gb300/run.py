@@ -16,7 +16,9 @@ neutralising background):
               {64^2, 128^2, 256^2, 512^2}, ppc from {4, 16, 64}, uth uniform in [0.01, 0.2]
               (MT19937 seed 4), quadratic, dx 0.05, dt 0.035, tile shape and CTA size
               autotuned (--boxes N takes the first N boxes)
-Prints one JSON line per run with the device time per step and the energies.  --dropin (2D
+Prints one JSON line per run with the device time per step and the energies; --fp64-check
+adds the error of a mixed-precision run against the plain FP64 engine (same load, same
+steps).  --dropin (2D
 configurations) times the host-array drop-in flow instead, as an unchanged OSIRIS host drives
 it: per species osg_vadvance_deposit_f32 and the particle wrap, guard updates and Yee on host
 arrays, every copy included.
@@ -197,6 +199,25 @@ def run_batch(args):
     bt.close()
 
 
+def fp64_error(cfg, sim, args):
+    """Error of a mixed-precision run against the FP64 build of the same kernels: the plain FP64
+    engine from the same load, run for the same number of steps; normwise E, B, J differences
+    (max |a - b| / max |b| over the whole grid) and the relative kinetic / field energy
+    differences."""
+    steps = args.warmup + args.steps
+    ref, _ = build_sim(cfg, "plain", 64, None, args.nx)
+    ref.step(steps)
+    out = {"steps": steps}
+    for name, a, b in zip("EBJ", sim.fields(), ref.fields()):
+        out[name] = float(np.abs(a.astype(np.float64) - b).max() / max(np.abs(b).max(), 1e-300))
+    k32, f32 = sim.energy()
+    k64, f64 = ref.energy()
+    out["kinetic"] = float(abs(k32.sum() - k64.sum()) / abs(k64.sum()))
+    out["field"] = float(abs(f32.sum() - f64.sum()) / max(abs(f64.sum()), 1e-300))
+    ref.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="two_stream",
@@ -209,6 +230,9 @@ def main():
     ap.add_argument("--engine", choices=["tiled", "plain"])
     ap.add_argument("--precision", type=int, choices=[32, 64])
     ap.add_argument("--tile", type=int, nargs="+")
+    ap.add_argument("--fp64-check", action="store_true",
+                    help="mixed-precision runs: report the error against the plain FP64 "
+                         "engine after the same steps from the same load")
     ap.add_argument("--dropin", action="store_true",
                     help="2D configurations: time the host-array drop-in flow instead "
                          "(osg_vadvance_deposit_f32 per species, guard updates and Yee on "
@@ -250,11 +274,14 @@ def main():
     sim.step(args.warmup)
     ms = sim.time_steps(args.steps)
     kin, fld = sim.energy()
-    print(json.dumps(dict(config=args.config, particles=npart, steps=args.steps,
-                          ms_per_step=ms / args.steps,
-                          particle_steps_per_s=npart * args.steps / (ms / 1e3),
-                          launches_per_step=sim.launches_per_step(), load_s=t_load,
-                          kinetic=[float(v) for v in kin], field=[float(v) for v in fld])))
+    out = dict(config=args.config, particles=npart, steps=args.steps,
+               ms_per_step=ms / args.steps,
+               particle_steps_per_s=npart * args.steps / (ms / 1e3),
+               launches_per_step=sim.launches_per_step(), load_s=t_load,
+               kinetic=[float(v) for v in kin], field=[float(v) for v in fld])
+    if args.fp64_check and sim.precision == 32:
+        out["fp64_error"] = fp64_error(cfg, sim, args)
+    print(json.dumps(out))
     sim.close()
 
 
