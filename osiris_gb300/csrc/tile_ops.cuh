@@ -486,29 +486,31 @@ __device__ __forceinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int n
 }
 
 // ------------------------------------------------------------------------------------------
-// 3D deposit.  The CTA's current tile is one shared copy, accumulated exactly as 64-bit fixed
-// point (value x 2^S rounded to an integer): native 32-bit integer atomics on the low word,
-// and on the high word when the low one wraps (FP32 shared-memory atomics are compare-and-swap
-// loops on this GPU).  The tile sums therefore carry no rounding beyond the one of each added
-// value and do not depend on the order of the adds.  Every lane adds the values of its own
-// segment (lanes_deposit3); the face crossings wait in a per-warp queue so that they are
-// deposited by full warps.
+// 3D deposit.  The CTA's current tile is one shared copy, accumulated exactly as fixed point
+// (value x 2^S rounded to an integer, v) in two 32-bit words per point: the low word sums the
+// low B bits of every v (v & (2^B - 1), unsigned), the high word the rest (v >> B, signed), so
+// that the point's value is hi 2^B + lo.  Both are plain 32-bit integer adds with no return
+// value (FP32 shared-memory atomics are compare-and-swap loops on this GPU).  The host picks S
+// and B from the most adds a tile point can take in one step, so that neither word can
+// overflow.  The tile sums therefore carry no rounding beyond the one of each added value and
+// do not depend on the order of the adds.  Every lane adds the values of its own segment
+// (lanes_deposit3); the face crossings wait in a per-warp queue so that they are deposited by
+// full warps.
 // ------------------------------------------------------------------------------------------
 constexpr int SEGQ3 = 48;        // queued face crossings per warp
 constexpr int SEGQ3_KEEP = 16;   // drain while more than this many wait (a round adds <= 32)
 
-// Exact add of v x scale, rounded to an integer, into a 64-bit fixed-point value (hi:lo).
-// The host picks the scale so that every single add (one segment value) fits a 32-bit signed
-// integer: the add converts once (fx_lo), adds the low word and returns the high word's
-// change, -1, 0 or +1 (fx_hi_delta): the sign extension of the add plus the carry out of the
-// low word.  It is non-zero only when the low word wraps, so the high-word atomic seldom runs.
-// Callers issue the low-word adds of several values before looking at their returns, so the
-// round trips overlap.
-__device__ __forceinline__ int fx_lo(float v, float scale) { return __float2int_rn(v * scale); }
+// fixed-point format of the 3D tile current: scale = 2^S, shift = B
+struct FxFormat {
+    float scale;
+    int shift;
+};
 
-__device__ __forceinline__ int fx_hi_delta(int fl, unsigned old)
+// add v (a fixed-point value) to the point whose words are lo and hi
+__device__ __forceinline__ void fx_add(unsigned *lo, unsigned *hi, int v, int shift)
 {
-    return (fl < 0 ? -1 : 0) + (old + (unsigned)fl < old ? 1 : 0);
+    atomicAdd(lo, (unsigned)v & ((1u << shift) - 1u));
+    atomicAdd(hi, (unsigned)(v >> shift));
 }
 
 // B-spline weights at both ends and longitudinal weights (q jn folded in) of one 3D segment
@@ -558,12 +560,17 @@ __device__ __forceinline__ float pick(const float (&v)[N], int k)
 template <int ORD>
 __device__ __noinline__ void lanes_deposit3(unsigned *Jl, unsigned *Jh, const SegRec r,
                                             bool has, const float *jn, int jsy, int jsz,
-                                            float scale)
+                                            FxFormat fx)
 {
     constexpr int NP = ORD + 1, NBLK = 3 * NP;
     if (!has) return;
     Seg3W<ORD> w;
     seg3_weights<ORD>(r, jn, w);
+    // the longitudinal weights in fixed-point units (the scale is a power of two: exact)
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int i = 0; i < ORD; i++) w.wl[d][i] *= fx.scale;
     unsigned *jl = Jl + r.base, *jh = Jh + r.base;
     const int rot = (int)(threadIdx.x & 31) % NBLK;
 #pragma unroll 1
@@ -587,24 +594,15 @@ __device__ __noinline__ void lanes_deposit3(unsigned *Jl, unsigned *Jh, const Se
         const int sm = c == 0 ? jsy : 3;
         const int sk = c == 2 ? jsy : jsz;
         const int o0 = c + sk * k;
-        int fl[ORD][NP];
-        unsigned old[ORD][NP];
 #pragma unroll
         for (int m = 0; m < NP; m++) {
             const float wp = wperp(A0[m], A1[m], B0, B1);
 #pragma unroll
             for (int i = 0; i < ORD; i++) {
-                fl[i][m] = fx_lo(a[i] * wp, scale);
-                old[i][m] = atomicAdd(jl + o0 + si * i + sm * m, (unsigned)fl[i][m]);
+                const int o = o0 + si * i + sm * m;
+                fx_add(jl + o, jh + o, __float2int_rn(a[i] * wp), fx.shift);
             }
         }
-#pragma unroll
-        for (int m = 0; m < NP; m++)
-#pragma unroll
-            for (int i = 0; i < ORD; i++) {
-                const int dh = fx_hi_delta(fl[i][m], old[i][m]);
-                if (dh) atomicAdd(jh + o0 + si * i + sm * m, (unsigned)dh);
-            }
     }
 }
 
@@ -613,7 +611,7 @@ __device__ __noinline__ void lanes_deposit3(unsigned *Jl, unsigned *Jh, const Se
 template <int ORD>
 __device__ __forceinline__ void segq_drain3(unsigned *Jl, unsigned *Jh, SegRec *sq,
                                             int &qn, int keep, const float *jn, int jsy,
-                                            int jsz, float scale)
+                                            int jsz, FxFormat fx)
 {
     const int lane = (int)(threadIdx.x & 31);
     while (qn > keep) {
@@ -623,7 +621,7 @@ __device__ __forceinline__ void segq_drain3(unsigned *Jl, unsigned *Jh, SegRec *
         const bool has = lane < take;
         if (has) r = sq[first + lane];
         qn = first;
-        lanes_deposit3<ORD>(Jl, Jh, r, has, jn, jsy, jsz, scale);
+        lanes_deposit3<ORD>(Jl, Jh, r, has, jn, jsy, jsz, fx);
     }
 }
 

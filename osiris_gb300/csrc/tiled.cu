@@ -157,24 +157,35 @@ static cudaError_t push_attr(int pusher, int dim, int order, int bytes)
     }
 }
 
-// 3D fixed-point tile current: every add must fit a 32-bit signed integer.  A segment value
-// is at most 3 |q| jn (weights along the motion <= |q| jn, across it <= 3); with a factor 2 of
-// margin, 2^S = 2^31 / (6 qmax jn).  The 64-bit sums cannot overflow for any particle count a
-// GPU holds.
-static int fx_exponent(const TiledState *t)
+// 3D fixed-point tile current.  A segment value is at most 3 |q| jn (weights along the motion
+// <= |q| jn, across it <= 3); with a factor 2 of margin every value, times 2^S, is below
+// V = 6 qmax jn 2^S in magnitude.  A tile point takes at most N adds per step: every particle
+// of the tile's slabs (at most the sum of the capacities) adds one value per point for each of
+// its at most 4 segments.  The low word sums N values below 2^B: N 2^B <= 2^32.  The high
+// word sums N values of magnitude <= V 2^-B + 1 and must stay below 2^31 - 1:
+// V <= 2^B (2^31 / N - 2).  B is the largest with N 2^B <= 2^32, S the largest with V within
+// both that bound and 2^31 (one value fits a signed 32-bit integer).  For N below 2^17 (slabs
+// of up to 32768 slots in all) 2^S >= 2^28 / (6 qmax jn): each add rounds by at most 2^-28 of
+// the largest value, far below the FP32 rounding of a float sum.
+static FxFormat fx_format(const TiledState *t)
 {
     double jn = 0.0;
     for (int d = 0; d < t->dim; d++) jn = std::max(jn, t->dx[d] / push_dt(t) / 3.0);
     double qm = 0.0;
     for (double v : t->qmax) qm = std::max(qm, v);
+    double n = 0.0;
+    for (long c : t->cap) n += 4.0 * (double)c;
+    n = std::max(n, 1.0);
+    int B = (int)std::floor(32.0 - std::log2(n));
+    while (B > 0 && n * std::ldexp(1.0, B) > 4294967296.0) B--;
+    B = std::max(1, std::min(B, 30));
+    const double vmax = std::min(2147483647.0, std::ldexp(1.0, B) * (2147483648.0 / n - 2.0));
     const double bound = 6.0 * qm * jn;
-    int S = bound > 0.0 ? (int)std::floor(31.0 - std::log2(bound)) : 40;
-    return std::max(-100, std::min(S, 100));
-}
-
-static void fx_scale_for(const TiledState *t, TiledArgs &a)
-{
-    a.fx_scale = std::ldexp(1.0f, fx_exponent(t));
+    int S = bound > 0.0 && vmax > 1.0 ? (int)std::floor(std::log2(vmax / bound)) : 40;
+    FxFormat f;
+    f.scale = std::ldexp(1.0f, std::max(-100, std::min(S, 100)));
+    f.shift = B;
+    return f;
 }
 
 static TiledArgs base_args(const TiledState *t)
@@ -198,7 +209,7 @@ static TiledArgs base_args(const TiledState *t)
     a.tile_lo = t->tile_lo;
     a.discard = t->l2_discard;
     a.walls = t->walls;
-    fx_scale_for(t, a);
+    a.fx = fx_format(t);
     return a;
 }
 
@@ -500,7 +511,9 @@ FoldBox tiled_fold_box(TiledState *t, float *j)
     f.gcl = make_int3(g.gcl[0], g.gcl[1], g.gcl[2]);
     f.ofs = t->order == 1 ? 1 : (t->order == 4 ? 3 : 2);
     f.npts = 3 * g.npoints();
-    f.fx_inv = std::ldexp(1.0f, -fx_exponent(t));
+    const FxFormat fx = fx_format(t);
+    f.fx_inv = 1.0f / fx.scale;
+    f.fx_shift = fx.shift;
     return f;
 }
 
@@ -689,10 +702,10 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     if (nb > 152 * 16) nb = 152 * 16;
     if (t->dim == 2)
         k_tile_fold<2><<<nb, 256, 0, st>>>(f.th, f.tl, j, f.size, f.T, f.ntile, f.je, f.gcl,
-                                            f.ofs, f.npts, f.fx_inv);
+                                            f.ofs, f.npts, f.fx_inv, f.fx_shift);
     else
         k_tile_fold<3><<<nb, 256, 0, st>>>(f.th, f.tl, j, f.size, f.T, f.ntile, f.je, f.gcl,
-                                            f.ofs, f.npts, f.fx_inv);
+                                            f.ofs, f.npts, f.fx_inv, f.fx_shift);
     *launches += 2;
     return OSG_OK;
 }

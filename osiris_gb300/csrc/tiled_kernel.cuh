@@ -57,20 +57,39 @@ __device__ __forceinline__ void load_rec(const float *rec, long p, int *c, float
     }
 }
 
-template <int DIM>
+// STREAM: a record of the output buffer, not read again in this step -- stored with the
+// evict-first policy (.cs), so that it does not push out of L2 the input-slab lines that the
+// sort pass still has to read
+template <int DIM, bool STREAM = false>
 __device__ __forceinline__ void store_rec(float *rec, long p, const int *c, const float *x,
                                           const float *u, float q)
 {
     float4 *r = reinterpret_cast<float4 *>(rec + p * PRec<DIM>::N);
     if constexpr (DIM == 2) {
-        asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(r),
-                     "f"(__int_as_float(c[0])), "f"(__int_as_float(c[1])), "f"(x[0]), "f"(x[1]),
-                     "f"(u[0]), "f"(u[1]), "f"(u[2]), "f"(q)
-                     : "memory");
+        if constexpr (STREAM)
+            asm volatile("st.global.cs.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(r),
+                         "f"(__int_as_float(c[0])), "f"(__int_as_float(c[1])), "f"(x[0]),
+                         "f"(x[1]), "f"(u[0]), "f"(u[1]), "f"(u[2]), "f"(q)
+                         : "memory");
+        else
+            asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(r),
+                         "f"(__int_as_float(c[0])), "f"(__int_as_float(c[1])), "f"(x[0]),
+                         "f"(x[1]), "f"(u[0]), "f"(u[1]), "f"(u[2]), "f"(q)
+                         : "memory");
     } else {
-        r[0] = make_float4(__int_as_float(c[0]), __int_as_float(c[1]), __int_as_float(c[2]), x[0]);
-        r[1] = make_float4(x[1], x[2], u[0], u[1]);
-        r[2] = make_float4(u[2], q, 0.f, 0.f);
+        const float4 r0 = make_float4(__int_as_float(c[0]), __int_as_float(c[1]),
+                                      __int_as_float(c[2]), x[0]);
+        const float4 r1 = make_float4(x[1], x[2], u[0], u[1]);
+        const float4 r2 = make_float4(u[2], q, 0.f, 0.f);
+        if constexpr (STREAM) {
+            __stcs(r, r0);
+            __stcs(r + 1, r1);
+            __stcs(r + 2, r2);
+        } else {
+            r[0] = r0;
+            r[1] = r1;
+            r[2] = r2;
+        }
     }
 }
 
@@ -110,9 +129,10 @@ struct TiledArgs {
     // summed in FP64 in tile order by k_tile_fold
     float *tile_hi;
     float *tile_lo;
-    // 3D: the tile current is accumulated as 64-bit fixed point, value x fx_scale (a power of
-    // two chosen so that no tile point, nor the fold's sum of tiles, can overflow)
-    float fx_scale;
+    // 3D: the tile current is accumulated as fixed point, value x 2^S split into a low word
+    // of B bits and a high word (fx.scale = 2^S, fx.shift = B; chosen so that no tile point,
+    // nor the fold's sum of tiles, can overflow)
+    FxFormat fx;
     // bit d: axis d is not periodic and absorbs particles at both edges (the axis of Lindman
     // open boundaries).  window = 1: x1 is the moving window's axis (absorbing below,
     // reflecting above), and shift_x = 1 (a step that ends with a window move) stores every
@@ -178,7 +198,7 @@ __device__ __forceinline__ void emigrate(const SpeciesDev &sd, long cap, long de
         atomicOr(status, OSG_STATUS_OVERFLOW);
         return;
     }
-    store_rec<DIM>(sd.out.rec, dest * cap + cap - 1 - k, cw, xo, un, q);
+    store_rec<DIM, true>(sd.out.rec, dest * cap + cap - 1 - k, cw, xo, un, q);
 }
 
 // After the sort, a tile's input slab is dead until the next step writes it as its output:
@@ -552,11 +572,11 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                     if (t > 0) {
                         segq_push(sQ, qn, hs, sg[t]);
                         segq_drain3<ORD>(sJl, sJh, sQ, qn, SEGQ3_KEEP, a.jn, jsy, jsz,
-                                         a.fx_scale);
+                                         a.fx);
                         continue;
                     }
                     if (!__any_sync(FULL_MASK, hs)) break;
-                    lanes_deposit3<ORD>(sJl, sJh, sg[0], hs, a.jn, jsy, jsz, a.fx_scale);
+                    lanes_deposit3<ORD>(sJl, sJh, sg[0], hs, a.jn, jsy, jsz, a.fx);
                 }
             }
         }
@@ -652,7 +672,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                     if (DIM > 1) ly = cc1[j] - t0[1];
                     if (DIM > 2) ly += a.T[1] * (cc2[j] - t0[2]);
                     const int oc[3] = {t0[0] + lc - a.T[0] * ly, cc1[j], cc2[j]};
-                    store_rec<DIM>(sd.out.rec, o, oc, cx[j], cu[j], cq[j]);
+                    store_rec<DIM, true>(sd.out.rec, o, oc, cx[j], cu[j], cq[j]);
                 }
             }
         }
@@ -663,7 +683,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     // ---- the face crossings still queued (the queue carries over from one species to the
     //      next: its entries hold their own charge)
     if constexpr (DIM == 2) segq_drain<ORD>(sJw, sQ, qn, 1, a.jn, scr, cs);
-    else segq_drain3<ORD>(sJl, sJh, sQ, qn, 0, a.jn, jsy, jsz, a.fx_scale);
+    else segq_drain3<ORD>(sJl, sJh, sQ, qn, 0, a.jn, jsy, jsz, a.fx);
     __syncthreads();
     // ---- the tile's energy of every species (the per-warp partials, written before the last
     //      block barrier)
@@ -732,12 +752,14 @@ k_push_tiled_batch(const TiledArgs *__restrict__ boxes, const int2 *__restrict__
 // Deterministic current flush: every point of the global current (guard cells included) is
 // the sum of the tile currents whose halo covers it, rounded once to float.  2D: FP64 sum, in
 // increasing tile order, of the float pairs (hi + lo).  3D: exact 64-bit integer sum of the
-// fixed-point tile values (words lo, hi), converted with one rounding and scaled by fx_inv (a
-// power of two) -- no FP64 arithmetic, whose rate is low on this GPU.  A tile with origin cell t0 = tc * T + 1 covers the global positions
+// fixed-point tile values (hi 2^fx_shift + lo), converted with one rounding and scaled by
+// fx_inv (a power of two) -- no FP64 arithmetic, whose rate is low on this GPU.  A tile with
+// origin cell t0 = tc * T + 1 covers the global positions
 // [tc * T - OFS + gcl, tc * T - OFS + gcl + je) along each axis (je = T + ORD + 2 points).
 struct FoldBox {
     const float *th, *tl;   // tile currents (2D: value and compensation; 3D: fixed-point words)
     float fx_inv;           // 3D: 1 / the fixed-point scale
+    int fx_shift;           // 3D: bits of the low word
     float *j;               // global current
     int3 size, T, ntile, je, gcl;
     int ofs;
@@ -749,7 +771,7 @@ __device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
                                                const float *__restrict__ tl,
                                                float *__restrict__ j, int3 size, int3 T,
                                                int3 ntile, int3 je, int3 gcl, int ofs, long npts,
-                                               float fx_inv)
+                                               float fx_inv, int fx_shift)
 {
     OSG_GRID_LOOP(g, npts)
     {
@@ -786,8 +808,8 @@ __device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
                     const int lz = DIM > 2 ? gz - (tz * Ta[2] - ofs + gl[2]) : 0;
                     const long o = tile * (3L * nj) + 3L * (lx + jea[0] * (ly + (long)jea[1] * lz)) + c;
                     if constexpr (DIM == 3) {
-                        fx += (long long)(((unsigned long long)__float_as_uint(tl[o]) << 32) |
-                                          __float_as_uint(th[o]));
+                        fx += (long long)__float_as_int(tl[o]) * (1LL << fx_shift) +
+                              (long long)__float_as_uint(th[o]);
                     } else {
                         v += (double)th[o];
                         if (tl) v += (double)tl[o];
@@ -801,9 +823,9 @@ __device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
 template <int DIM>
 __global__ void k_tile_fold(const float *__restrict__ th, const float *__restrict__ tl,
                             float *__restrict__ j, int3 size, int3 T, int3 ntile, int3 je,
-                            int3 gcl, int ofs, long npts, float fx_inv)
+                            int3 gcl, int ofs, long npts, float fx_inv, int fx_shift)
 {
-    tile_fold_body<DIM>(th, tl, j, size, T, ntile, je, gcl, ofs, npts, fx_inv);
+    tile_fold_body<DIM>(th, tl, j, size, T, ntile, je, gcl, ofs, npts, fx_inv, fx_shift);
 }
 
 // the same for every box of a batch (box = blockIdx.y)
@@ -812,7 +834,7 @@ __global__ void k_batch_fold(const FoldBox *__restrict__ boxes)
 {
     const FoldBox &f = boxes[blockIdx.y];
     tile_fold_body<DIM>(f.th, f.tl, f.j, f.size, f.T, f.ntile, f.je, f.gcl, f.ofs, f.npts,
-                        f.fx_inv);
+                        f.fx_inv, f.fx_shift);
 }
 
 // zero n ints at p for every range of a device table (one launch; defined in tiled.cu)

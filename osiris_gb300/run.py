@@ -281,6 +281,8 @@ def main():
                kinetic=[float(v) for v in kin], field=[float(v) for v in fld])
     if args.fp64_check and sim.precision == 32:
         out["fp64_error"] = fp64_error(cfg, sim, args)
+    # per-phase device ms of 5 more steps, each phase timed alone with CUDA events
+    out["phase_ms"] = sim.profile(5)
     print(json.dumps(out))
     sim.close()
 
