@@ -369,6 +369,16 @@ int osg_sim_gauss_residual(osg_sim *s, double *max_abs, double *l2);
 /* Average device time per launch of each phase over the last profiled steps (ms):
  * [0] push+deposit, [1] current fold, [2] Yee, [3] guard replace, [4] migration/sort. */
 int osg_sim_profile(osg_sim *s, int nsteps, float *ms_phase);
+/* Autotuner; call after the species are added and before the first step (not with the moving
+ * window).  The state is put back after every trial.
+ * TILED: times `steps` steps (after 2 untimed ones) for every candidate tile shape (2D: 8x8,
+ * 16x8, 8x4, 16x16; 3D: 8x8x4, 8x4x4, 4x4x4, 8x8x8; those that divide the box and fit shared
+ * memory) x push CTA size (256, 128), re-bins the particles for the fastest and returns it in
+ * tile[3] and threads.  The tiled engine sorts every step inside its push (n_sort unchanged).
+ * PLAIN: chooses the cell-sort interval n_sort (0 = never) from the measured cost of one sort C
+ * and the growth g of the push time over `steps` unsorted steps: n = sqrt(2 C / g), the
+ * interval with the least time per step; tile and threads are returned as 0. */
+int osg_sim_autotune(osg_sim *s, int steps, int *tile, int *threads, int *n_sort);
 /* Moving window along x1 at the speed of light (TILED engine; call before the first step):
  * every time the window has advanced one cell (the reference's move_boundary_space_global,
  * source/os-space.f90:508-566) the fields shift one cell towards lower x1 with the new plane

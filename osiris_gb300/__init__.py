@@ -127,6 +127,7 @@ def _declare(lb):
     lb.osg_sim_energy.argtypes = [P, P, P]
     lb.osg_sim_gauss_residual.argtypes = [P, C.POINTER(D), C.POINTER(D)]
     lb.osg_sim_profile.argtypes = [P, I, P]
+    lb.osg_sim_autotune.argtypes = [P, I, P, C.POINTER(I), C.POINTER(I)]
     lb.osg_sim_launches_per_step.argtypes = [P]
     lb.osg_sim_time_steps.argtypes = [P, I, C.POINTER(F)]
     lb.osg_sim_tile_occupancy.argtypes = [P, C.POINTER(D)]
@@ -581,6 +582,17 @@ class Simulation:
         n = C.c_long()
         _check(lib().osg_sim_window_moves(self.h, C.byref(n)))
         return n.value
+
+    def autotune(self, steps=4):
+        """Autotuner (osg_sim_autotune): TILED, the fastest tile shape and push CTA size over
+        `steps` timed steps per candidate (the engine is re-binned for it); PLAIN, the cell-sort
+        interval from the measured sort cost and slow-down of unsorted steps.  Call after the
+        species are added, before the first step.  Returns {"tile", "threads", "n_sort"}."""
+        tile = np.zeros(3, np.int32)
+        th, ns = C.c_int(), C.c_int()
+        _check(lib().osg_sim_autotune(self.h, int(steps), _p(tile), C.byref(th), C.byref(ns)))
+        return {"tile": [int(v) for v in tile[:self.dim]], "threads": th.value,
+                "n_sort": ns.value}
 
     def profile(self, n):
         ms = np.zeros(5, np.float32)

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 
 #include <cmath>
 #include <cstdio>
@@ -621,6 +622,29 @@ int osg_sim_destroy(osg_sim *s)
     return OSG_OK;
 }
 
+// plain-engine sort scratch, sized for the largest species
+static int sort_scratch(osg_sim *s)
+{
+    const int dim = s->cfg.dim;
+    size_t n = 1;
+    for (long v : s->np) n = std::max(n, (size_t)v);
+    const size_t need = ((size_t)sizeof(int) * dim + (size_t)s->esz * (dim + 4)) * n;
+    int rc = OSG_OK;
+    if (need > s->sort_buf_bytes) {
+        cudaFree(s->d_sort_buf);
+        s->sort_buf_bytes = 0;
+        s->d_sort_buf = dalloc<char>(need, &rc);
+        if (rc) return rc;
+        s->sort_buf_bytes = need;
+    }
+    if (!s->d_cell_cnt) {
+        const long nc = ncells(s->g);
+        s->d_cell_cnt = dalloc<int>(nc, &rc);
+        if (!rc) s->d_scan_tmp = dalloc<int>((nc + 1023) / 1024 + 1, &rc);
+    }
+    return rc;
+}
+
 int osg_sim_add_species(osg_sim *s, double rqm, long np, const int *ix, const void *x,
                         const void *u, const void *q)
 {
@@ -662,23 +686,11 @@ int osg_sim_add_species(osg_sim *s, double rqm, long np, const int *ix, const vo
             OSG_CUDA(cudaMemcpyAsync(p.q, q, (size_t)s->esz * np, cudaMemcpyHostToDevice, s->st));
         }
         s->plain.push_back(p);
-        // sort scratch sized for the largest species
-        const size_t need = ((size_t)sizeof(int) * dim + (size_t)s->esz * (dim + 4)) * n;
-        if (s->cfg.n_sort > 0 && need > s->sort_buf_bytes) {
-            cudaFree(s->d_sort_buf);
-            s->d_sort_buf = dalloc<char>(need, &rc);
-            if (rc) return rc;
-            s->sort_buf_bytes = need;
-        }
-        if (s->cfg.n_sort > 0 && !s->d_cell_cnt) {
-            const long nc = ncells(s->g);
-            s->d_cell_cnt = dalloc<int>(nc, &rc);
-            if (!rc) s->d_scan_tmp = dalloc<int>((nc + 1023) / 1024 + 1, &rc);
-            if (rc) return rc;
-        }
     }
     s->rqm.push_back(rqm);
     s->np.push_back(np);
+    if (s->cfg.engine == OSG_ENGINE_PLAIN && s->cfg.n_sort > 0 && (rc = sort_scratch(s)))
+        return rc;
     s->graphs_dirty = true;
     OSG_CUDA(cudaStreamSynchronize(s->st));
     return k;
@@ -1109,6 +1121,253 @@ int osg_sim_profile(osg_sim *s, int nsteps, float *ms_phase)
     for (int i = 0; i < 6; i++) cudaEventDestroy(pe.ev[i]);
     if (rc) return rc;
     for (int i = 0; i < 5; i++) ms_phase[i] = acc[i] / nsteps;
+    return check_status(s);
+}
+
+// ------------------------------------------------------------------------ autotuner
+// Device state that trial steps change and the tuner puts back: fields, Lindman planes,
+// thermal-bath step counter (the particles are either copied too, PLAIN, or live in a separate
+// trial TiledState, TILED).
+struct SavedState {
+    std::vector<void *> buf;
+    std::vector<std::pair<void *, size_t>> where;
+    long step_n = 0;
+    int cur = 0;
+    ~SavedState()
+    {
+        for (void *p : buf) cudaFree(p);
+    }
+    int save(void *p, size_t bytes, cudaStream_t st)
+    {
+        if (!p || bytes == 0) return OSG_OK;
+        void *c = nullptr;
+        OSG_CUDA(cudaMalloc(&c, bytes));
+        buf.push_back(c);
+        where.push_back({p, bytes});
+        OSG_CUDA(cudaMemcpyAsync(c, p, bytes, cudaMemcpyDeviceToDevice, st));
+        return OSG_OK;
+    }
+    int restore(osg_sim *s)
+    {
+        for (size_t i = 0; i < buf.size(); i++)
+            OSG_CUDA(cudaMemcpyAsync(where[i].first, buf[i], where[i].second,
+                                     cudaMemcpyDeviceToDevice, s->st));
+        OSG_CUDA(cudaMemsetAsync(s->d_ene, 0, MAX_SPECIES * sizeof(double), s->st));
+        OSG_CUDA(cudaStreamSynchronize(s->st));
+        s->step_n = step_n;
+        s->cur = cur;
+        s->graphs_dirty = true;
+        return OSG_OK;
+    }
+};
+
+static int save_fields(osg_sim *s, SavedState &sv)
+{
+    const size_t gbytes = (size_t)s->esz * 3 * s->g.npoints();
+    int rc;
+    if ((rc = sv.save(s->e, gbytes, s->st)) || (rc = sv.save(s->b, gbytes, s->st)) ||
+        (rc = sv.save(s->j, gbytes, s->st)))
+        return rc;
+    if (s->lind &&
+        (rc = sv.save(s->lind, (size_t)s->esz * lindman_state_size(s->g, s->open_axis), s->st)))
+        return rc;
+    if (s->d_step && (rc = sv.save(s->d_step, sizeof(unsigned long long), s->st))) return rc;
+    sv.step_n = s->step_n;
+    sv.cur = s->cur;
+    return OSG_OK;
+}
+
+// device ms of n steps (graph replays) after w untimed ones
+static int time_trial(osg_sim *s, int w, int n, float *ms)
+{
+    int rc = osg_sim_step_async(s, w);
+    if (rc) return rc;
+    return osg_sim_time_steps(s, n, ms);
+}
+
+// TILED: every candidate tile shape x CTA size runs on a trial copy of the particles
+static int tune_tiled(osg_sim *s, int steps, int *tile, int *threads)
+{
+    const int dim = s->cfg.dim;
+    const int ns = (int)s->np.size();
+    // the particles, once, on the host (the trial states are binned from them)
+    std::vector<std::vector<int>> hix(ns);
+    std::vector<std::vector<float>> hx(ns), hu(ns), hq(ns);
+    std::vector<long> hnp(ns);
+    int rc;
+    for (int k = 0; k < ns; k++) {
+        if ((rc = tiled_count(s->tiled, s->cur, k, &hnp[k], s->st))) return rc;
+        const size_t n = (size_t)std::max(hnp[k], 1L);
+        hix[k].resize(n * dim);
+        hx[k].resize(n * dim);
+        hu[k].resize(n * 3);
+        hq[k].resize(n);
+        if ((rc = tiled_get_species(s->tiled, s->cur, k, hix[k].data(), hx[k].data(),
+                                    hu[k].data(), hq[k].data(), s->st)))
+            return rc;
+    }
+    SavedState sv;
+    if ((rc = save_fields(s, sv))) return rc;
+    std::vector<std::array<int, 3>> tiles;
+    if (dim == 2) tiles = {{8, 8, 1}, {16, 8, 1}, {8, 4, 1}, {16, 16, 1}};
+    else tiles = {{8, 8, 4}, {8, 4, 4}, {4, 4, 4}, {8, 8, 8}};
+    const int thr[2] = {256, 128};
+    TiledState *orig = s->tiled;
+    float best = 1e30f;
+    int bestT[3] = {0, 0, 0}, best_th = 0;
+    for (const auto &T : tiles) {
+        bool fits = true;
+        for (int d = 0; d < dim; d++) fits = fits && T[d] <= s->cfg.nx[d] && s->cfg.nx[d] % T[d] == 0;
+        if (!fits) continue;
+        for (int th : thr) {
+            osg_config c = s->cfg;
+            for (int d = 0; d < 3; d++) c.tile[d] = d < dim ? T[d] : 1;
+            TiledState *tr = nullptr;
+            rc = tiled_create(&tr, c, s->g);
+            if (rc) continue;   // does not fit (shared memory, tile cells)
+            rc = tiled_set_threads(tr, th);
+            for (int k = 0; k < ns && !rc; k++)
+                rc = tiled_add_species(tr, s->rqm[k], hnp[k], hix[k].data(), hx[k].data(),
+                                       hu[k].data(), hq[k].data(), s->st);
+            float ms = 0.0f;
+            if (!rc) {
+                s->tiled = tr;
+                s->cur = 0;
+                s->graphs_dirty = true;
+                rc = time_trial(s, 2, steps, &ms);
+                if (!rc) rc = check_status(s);
+                drop_graphs(s);
+                s->tiled = orig;
+            }
+            tiled_destroy(tr);
+            const int rs = sv.restore(s);
+            if (rs) return rs;
+            if (rc == OSG_ERR_CUDA) return rc;
+            if (rc) continue;
+            if (ms < best) {
+                best = ms;
+                for (int d = 0; d < 3; d++) bestT[d] = d < dim ? T[d] : 1;
+                best_th = th;
+            }
+        }
+    }
+    OSG_CHECK(best_th > 0, OSG_ERR_ARG, "autotuner: no candidate tile shape fits the box");
+    // rebuild the engine with the winner (from the host copy of the particles)
+    bool same = best_th == tiled_threads(orig);
+    for (int d = 0; d < dim; d++) same = same && bestT[d] == s->cfg.tile[d];
+    if (!same) {
+        osg_config c = s->cfg;
+        for (int d = 0; d < 3; d++) c.tile[d] = bestT[d];
+        TiledState *nt = nullptr;
+        if ((rc = tiled_create(&nt, c, s->g))) return rc;
+        rc = tiled_set_threads(nt, best_th);
+        for (int k = 0; k < ns && !rc; k++)
+            rc = tiled_add_species(nt, s->rqm[k], hnp[k], hix[k].data(), hx[k].data(),
+                                   hu[k].data(), hq[k].data(), s->st);
+        if (rc) {
+            tiled_destroy(nt);
+            return rc;
+        }
+        drop_graphs(s);
+        tiled_destroy(orig);
+        s->tiled = nt;
+        s->cur = 0;
+        for (int d = 0; d < 3; d++) s->cfg.tile[d] = bestT[d];
+        s->graphs_dirty = true;
+    }
+    for (int d = 0; d < 3; d++) tile[d] = bestT[d];
+    *threads = best_th;
+    return OSG_OK;
+}
+
+// PLAIN: the cell-sort interval from a cost model.  Unsorted steps get slower as the particles
+// lose their cell order (scattered gathers and current atomics); a sort costs C once.  Sorting
+// every n steps costs (C + g (0 + 1 + ... + (n - 1))) / n per step on top of a sorted step,
+// g = the growth of the push time per unsorted step, minimal at n = sqrt(2 C / g).  The tuner
+// measures g over `steps` unsorted steps from a sorted state (least-squares slope of the push
+// times) and C as the sort phase of one step.
+static int tune_sort(osg_sim *s, int steps, int *n_sort)
+{
+    SavedState sv;
+    int rc = sort_scratch(s);
+    if (rc) return rc;
+    const int dim = s->cfg.dim;
+    for (size_t k = 0; k < s->plain.size(); k++) {
+        const size_t n = (size_t)std::max(s->np[k], 1L);
+        PlainSpecies &p = s->plain[k];
+        // the sort permutes every array, charges included
+        if ((rc = sv.save(p.ix, sizeof(int) * dim * n, s->st)) ||
+            (rc = sv.save(p.x, (size_t)s->esz * dim * n, s->st)) ||
+            (rc = sv.save(p.u, (size_t)s->esz * 3 * n, s->st)) ||
+            (rc = sv.save(p.q, (size_t)s->esz * n, s->st)))
+            return rc;
+    }
+    if ((rc = save_fields(s, sv))) return rc;
+    const int keep = s->cfg.n_sort;
+    PhaseEvents pe;
+    for (int i = 0; i < 6; i++) OSG_CUDA(cudaEventCreate(&pe.ev[i]));
+    std::vector<double> push;
+    float c_sort = 0.0f;
+    // one sorted step first (the measurement starts from cell order), then `steps` unsorted
+    for (int it = 0; it <= steps && !rc; it++) {
+        rc = enqueue_step_any(s, 0, it == 0, false, &pe);
+        if (rc) break;
+        s->step_n++;
+        if (cudaEventSynchronize(pe.ev[5]) != cudaSuccess) {
+            set_error("tuning step failed");
+            rc = OSG_ERR_CUDA;
+            break;
+        }
+        float t = 0.0f;
+        if (it == 0) {
+            cudaEventElapsedTime(&t, pe.ev[2], pe.ev[3]);
+            c_sort = t;
+        } else {
+            cudaEventElapsedTime(&t, pe.ev[1], pe.ev[2]);
+            push.push_back(t);
+        }
+    }
+    for (int i = 0; i < 6; i++) cudaEventDestroy(pe.ev[i]);
+    if (!rc) rc = check_status(s);
+    const int rs = sv.restore(s);
+    s->cfg.n_sort = keep;
+    if (rc) return rc;
+    if (rs) return rs;
+    // least-squares slope of the push time over the unsorted steps
+    const int m = (int)push.size();
+    double sx = 0, sy = 0, sxx = 0, sxy = 0;
+    for (int i = 0; i < m; i++) {
+        sx += i;
+        sy += push[i];
+        sxx += (double)i * i;
+        sxy += i * push[i];
+    }
+    const double den = m * sxx - sx * sx;
+    const double g = den > 0 ? (m * sxy - sx * sy) / den : 0.0;
+    int n = 0;   // never: the push does not slow down measurably
+    if (g > 1e-6 * std::max(sy / std::max(m, 1), 1e-6))
+        n = (int)std::lround(std::sqrt(2.0 * c_sort / g));
+    n = std::max(0, std::min(n, 100000));
+    if (g > 0 && n == 0) n = 1;
+    s->cfg.n_sort = n;
+    s->graphs_dirty = true;
+    *n_sort = n;
+    return OSG_OK;
+}
+
+int osg_sim_autotune(osg_sim *s, int steps, int *tile, int *threads, int *n_sort)
+{
+    OSG_CHECK(s && tile && threads && n_sort && steps >= 2 && steps <= 1000, OSG_ERR_ARG,
+              "bad arguments");
+    OSG_CHECK(!s->np.empty(), OSG_ERR_STATE, "no species");
+    OSG_CHECK(s->step_n == 0, OSG_ERR_STATE, "autotune before the first step");
+    OSG_CHECK(!s->window, OSG_ERR_STATE, "the autotuner does not run with the moving window");
+    for (int d = 0; d < 3; d++) tile[d] = 0;
+    *threads = 0;
+    *n_sort = s->cfg.n_sort;
+    int rc = s->cfg.engine == OSG_ENGINE_TILED ? tune_tiled(s, steps, tile, threads)
+                                               : tune_sort(s, steps, n_sort);
+    if (rc) return rc;
     return check_status(s);
 }
 

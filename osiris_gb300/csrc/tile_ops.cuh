@@ -487,14 +487,15 @@ __device__ __forceinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int n
 
 // ------------------------------------------------------------------------------------------
 // 3D deposit.  The CTA's current tile is one shared copy, accumulated exactly as fixed point
-// (value x 2^S rounded to an integer, v) in two 32-bit words per point: the low word sums the
-// low B bits of every v (v & (2^B - 1), unsigned), the high word the rest (v >> B, signed), so
-// that the point's value is hi 2^B + lo.  Both are plain 32-bit integer adds with no return
-// value (FP32 shared-memory atomics are compare-and-swap loops on this GPU).  The host picks S
-// and B from the most adds a tile point can take in one step, so that neither word can
-// overflow.  The tile sums therefore carry no rounding beyond the one of each added value and
-// do not depend on the order of the adds.  Every lane adds the values of its own segment
-// (lanes_deposit3); the face crossings wait in a per-warp queue so that they are deposited by
+// (value x 2^S rounded to an integer, v) in two 32-bit words per point: the high word sums
+// v >> B (signed), the low word sums v itself, modulo 2^32.  Both are plain 32-bit integer adds
+// with no return value (FP32 shared-memory atomics are compare-and-swap loops on this GPU).  The
+// host picks S and B from the most adds a point can take in one step, N, so that the high word
+// cannot overflow and N 2^B <= 2^32.  The sum of the low B bits of every v, sum - hi 2^B, then
+// lies in [0, 2^32) and equals lo - hi 2^B modulo 2^32: the point's value is
+// hi 2^B + (unsigned)(lo - hi 2^B) (k_tile_fold).  The tile sums therefore carry no rounding
+// beyond the one of each added value and do not depend on the order of the adds.  Every lane
+// adds the values of its own segment (lanes_deposit3); the face crossings wait in a per-warp queue so that they are deposited by
 // full warps.
 // ------------------------------------------------------------------------------------------
 constexpr int SEGQ3 = 48;        // queued face crossings per warp
@@ -509,7 +510,7 @@ struct FxFormat {
 // add v (a fixed-point value) to the point whose words are lo and hi
 __device__ __forceinline__ void fx_add(unsigned *lo, unsigned *hi, int v, int shift)
 {
-    atomicAdd(lo, (unsigned)v & ((1u << shift) - 1u));
+    atomicAdd(lo, (unsigned)v);
     atomicAdd(hi, (unsigned)(v >> shift));
 }
 
@@ -553,10 +554,15 @@ __device__ __forceinline__ float pick(const float (&v)[N], int k)
 // One 3D segment per lane (has = false: none), each lane adding its own values straight into
 // the tile.  The values come in 3 (ORD + 1) blocks of ORD (ORD + 1) -- block (c, k) holds
 // component c at plane k: j1 and j2 over z planes, j3 over y planes -- each the outer product
-// of the longitudinal weights of c with a perpendicular weight vector.  The lanes take the
-// blocks in a rotated order (lane l starts at block l mod blocks), so that lanes of one cell
-// add to different addresses in each atomic instruction; the loop over blocks is not
-// unrolled (small code, selects for the block's weights).
+// of the longitudinal weights of c with a perpendicular weight vector.  Lanes of one cell (up
+// to 8 or so in a cell-sorted tile) must add to different addresses in each atomic
+// instruction:
+// - orders >= 2: the components go in a fixed order (their strides and weights known at
+//   compile time); within a component a lane starts at plane lane mod (ORD + 1) and at
+//   longitudinal index (lane / (ORD + 1)) mod ORD, so lanes of one cell take different
+//   (plane, index) pairs -- (ORD + 1) ORD of them;
+// - linear (two planes, one index): the lanes rotate over all 6 blocks instead.
+// The plane loop is not unrolled (small code; selects pick the plane's weights).
 template <int ORD>
 __device__ __noinline__ void lanes_deposit3(unsigned *Jl, unsigned *Jh, const SegRec r,
                                             bool has, const float *jn, int jsy, int jsz,
@@ -572,35 +578,73 @@ __device__ __noinline__ void lanes_deposit3(unsigned *Jl, unsigned *Jh, const Se
 #pragma unroll
         for (int i = 0; i < ORD; i++) w.wl[d][i] *= fx.scale;
     unsigned *jl = Jl + r.base, *jh = Jh + r.base;
-    const int rot = (int)(threadIdx.x & 31) % NBLK;
-#pragma unroll 1
-    for (int t = 0; t < NBLK; t++) {
-        int blk = t + rot;
-        if (blk >= NBLK) blk -= NBLK;
-        const int c = blk / NP, k = blk - c * NP;
-        // longitudinal weights of component c; perpendicular weights along axis A (y for j1,
-        // x for j2, j3) and, at plane k, along axis B (z for j1, j2; y for j3)
-        float a[ORD], A0[NP], A1[NP];
+    const int lane = (int)(threadIdx.x & 31);
+    if constexpr (ORD >= 2) {
+        const int rk = lane % NP, ri = (lane / NP) % ORD;
 #pragma unroll
-        for (int i = 0; i < ORD; i++) a[i] = c == 0 ? w.wl[0][i] : (c == 1 ? w.wl[1][i] : w.wl[2][i]);
-#pragma unroll
-        for (int m = 0; m < NP; m++) {
-            A0[m] = c == 0 ? w.s0[1][m] : w.s0[0][m];
-            A1[m] = c == 0 ? w.s1[1][m] : w.s1[0][m];
-        }
-        const float B0 = c == 2 ? pick(w.s0[1], k) : pick(w.s0[2], k);
-        const float B1 = c == 2 ? pick(w.s1[1], k) : pick(w.s1[2], k);
-        const int si = c == 0 ? 3 : (c == 1 ? jsy : jsz);
-        const int sm = c == 0 ? jsy : 3;
-        const int sk = c == 2 ? jsy : jsz;
-        const int o0 = c + sk * k;
-#pragma unroll
-        for (int m = 0; m < NP; m++) {
-            const float wp = wperp(A0[m], A1[m], B0, B1);
+        for (int c = 0; c < 3; c++) {
+            // perpendicular axes: A (y for j1, x for j2, j3) and B, the plane axis (z for j1,
+            // j2; y for j3)
+            const int ax = c == 0 ? 1 : 0, bx = c == 2 ? 1 : 2;
+            const int si = c == 0 ? 3 : (c == 1 ? jsy : jsz);
+            const int sm = c == 0 ? jsy : 3;
+            const int sk = c == 2 ? jsy : jsz;
+            float a[ORD];
+            int ao[ORD];
 #pragma unroll
             for (int i = 0; i < ORD; i++) {
-                const int o = o0 + si * i + sm * m;
-                fx_add(jl + o, jh + o, __float2int_rn(a[i] * wp), fx.shift);
+                int ii = i + ri;
+                if (ii >= ORD) ii -= ORD;
+                a[i] = pick(w.wl[c], ii);
+                ao[i] = si * ii;
+            }
+#pragma unroll 1
+            for (int t = 0; t < NP; t++) {
+                int k = t + rk;
+                if (k >= NP) k -= NP;
+                const float B0 = pick(w.s0[bx], k), B1 = pick(w.s1[bx], k);
+                const int o0 = c + sk * k;
+#pragma unroll
+                for (int m = 0; m < NP; m++) {
+                    const float wp = wperp(w.s0[ax][m], w.s1[ax][m], B0, B1);
+#pragma unroll
+                    for (int i = 0; i < ORD; i++) {
+                        const int o = o0 + ao[i] + sm * m;
+                        fx_add(jl + o, jh + o, __float2int_rn(a[i] * wp), fx.shift);
+                    }
+                }
+            }
+        }
+    } else {
+        const int rot = lane % NBLK;
+#pragma unroll 1
+        for (int t = 0; t < NBLK; t++) {
+            int blk = t + rot;
+            if (blk >= NBLK) blk -= NBLK;
+            const int c = blk / NP, k = blk - c * NP;
+            float a[ORD], A0[NP], A1[NP];
+#pragma unroll
+            for (int i = 0; i < ORD; i++)
+                a[i] = c == 0 ? w.wl[0][i] : (c == 1 ? w.wl[1][i] : w.wl[2][i]);
+#pragma unroll
+            for (int m = 0; m < NP; m++) {
+                A0[m] = c == 0 ? w.s0[1][m] : w.s0[0][m];
+                A1[m] = c == 0 ? w.s1[1][m] : w.s1[0][m];
+            }
+            const float B0 = c == 2 ? pick(w.s0[1], k) : pick(w.s0[2], k);
+            const float B1 = c == 2 ? pick(w.s1[1], k) : pick(w.s1[2], k);
+            const int si = c == 0 ? 3 : (c == 1 ? jsy : jsz);
+            const int sm = c == 0 ? jsy : 3;
+            const int sk = c == 2 ? jsy : jsz;
+            const int o0 = c + sk * k;
+#pragma unroll
+            for (int m = 0; m < NP; m++) {
+                const float wp = wperp(A0[m], A1[m], B0, B1);
+#pragma unroll
+                for (int i = 0; i < ORD; i++) {
+                    const int o = o0 + si * i + sm * m;
+                    fx_add(jl + o, jh + o, __float2int_rn(a[i] * wp), fx.shift);
+                }
             }
         }
     }

@@ -161,7 +161,7 @@ static cudaError_t push_attr(int pusher, int dim, int order, int bytes)
 // <= |q| jn, across it <= 3); with a factor 2 of margin every value, times 2^S, is below
 // V = 6 qmax jn 2^S in magnitude.  A tile point takes at most N adds per step: every particle
 // of the tile's slabs (at most the sum of the capacities) adds one value per point for each of
-// its at most 4 segments.  The low word sums N values below 2^B: N 2^B <= 2^32.  The high
+// its at most 4 segments.  The low B bits of N values sum below 2^32: N 2^B <= 2^32.  The high
 // word sums N values of magnitude <= V 2^-B + 1 and must stay below 2^31 - 1:
 // V <= 2^B (2^31 / N - 2).  B is the largest with N 2^B <= 2^32, S the largest with V within
 // both that bound and 2^31 (one value fits a signed 32-bit integer).  For N below 2^17 (slabs
@@ -226,8 +226,12 @@ static size_t smem_for(int dim, int order, const int *T, int threads)
     // 2D: one copy of the current tile per warp, each with its two-sum compensation, then per
     // warp a value scratch and a queue of face-crossing segments; last the cell histogram
     const size_t warps = (size_t)threads / 32;
-    const size_t copies = dim == 2 ? 2 * warps : 2;
-    const size_t nf = (6 * ne + 3 * nj * copies + 3) & ~(size_t)3;
+    size_t jwords = 3 * nj * 2 * warps;
+    if (dim == 3)
+        jwords = 2 * ((size_t)(3 * (T[0] + NP + 1) + j3_pad_y(order)) * (T[1] + NP + 1) +
+                      j3_pad_z(order)) *
+                 (T[2] + NP + 1);
+    const size_t nf = (6 * ne + jwords + 3) & ~(size_t)3;
     size_t cells = 1;
     for (int d = 0; d < dim; d++) cells *= (size_t)T[d];
     const size_t hist = 2 * cells * sizeof(int);

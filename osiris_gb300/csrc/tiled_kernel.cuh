@@ -147,6 +147,12 @@ struct TiledArgs {
     int discard;
 };
 
+// words of padding per row and per plane of the 3D current tile (bank spread of the lanes'
+// fixed-point adds): none -- with the deposit's (plane, index) lane rotation, one or five words
+// per row (and 16 per plane) measured 0-4% slower on configurations 3 and 5
+__host__ __device__ constexpr int j3_pad_y(int) { return 0; }
+__host__ __device__ constexpr int j3_pad_z(int) { return 0; }
+
 static const int MAX_TILED_SPECIES = 16;
 static const int MAX_TILE_CELLS = 1024;   // cells per tile (bins of the per-tile cell sort)
 // the sort key a stayer carries between the two passes: 1 + cell in the tile + rank << bits
@@ -260,7 +266,10 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     }
     const int ne = ee[0] * ee[1] * ee[2], nj = je[0] * je[1] * je[2];
     const int nthr = blockDim.x, nwarp = nthr >> 5, warp = threadIdx.x >> 5;
-    const int njall = 3 * nj * (DIM == 2 ? nwarp : 1);
+    // current tile strides ([z][y][x][3], 3D rows and planes padded)
+    const int jsy = 3 * je[0] + (DIM == 3 ? j3_pad_y(ORD) : 0);
+    const int jsz = jsy * je[1] + (DIM == 3 ? j3_pad_z(ORD) : 0);
+    const int njall = DIM == 2 ? 3 * nj * nwarp : jsz * je[2];
     // 2D: the warp copies of the current tile keep a two-sum compensation at offset jlo;
     // 3D: the low (offset 0) and high (offset jlo) words of the fixed-point tile current
     const int jlo = njall;
@@ -301,7 +310,6 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     __syncthreads();
 
     const int esy = 3 * ee[0], esz = 3 * ee[0] * ee[1];
-    const int jsy = 3 * je[0], jsz = 3 * je[0] * je[1];
     const unsigned lane = threadIdx.x & 31;
     float *sJw = DIM == 2 ? sJ + 3 * nj * warp : sJ;
     ColSlots<ORD> cs;
@@ -712,9 +720,13 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 th[idx] = t;
                 tl[idx] = lo - (t - hi);
             } else {
-                // the fixed-point words as they are (k_tile_fold sums them as integers)
-                th[idx] = __uint_as_float(sJl[idx]);
-                tl[idx] = __uint_as_float(sJh[idx]);
+                // the fixed-point words as they are (k_tile_fold sums them as integers), from
+                // the padded rows
+                const int pnt = idx / 3;
+                const int sp = idx - 3 * pnt + 3 * (pnt % je[0]) + jsy * ((pnt / je[0]) % je[1]) +
+                               jsz * (pnt / (je[0] * je[1]));
+                th[idx] = __uint_as_float(sJl[sp]);
+                tl[idx] = __uint_as_float(sJh[sp]);
             }
         }
     }
@@ -752,9 +764,9 @@ k_push_tiled_batch(const TiledArgs *__restrict__ boxes, const int2 *__restrict__
 // Deterministic current flush: every point of the global current (guard cells included) is
 // the sum of the tile currents whose halo covers it, rounded once to float.  2D: FP64 sum, in
 // increasing tile order, of the float pairs (hi + lo).  3D: exact 64-bit integer sum of the
-// fixed-point tile values (hi 2^fx_shift + lo), converted with one rounding and scaled by
-// fx_inv (a power of two) -- no FP64 arithmetic, whose rate is low on this GPU.  A tile with
-// origin cell t0 = tc * T + 1 covers the global positions
+// fixed-point tile values (from the words hi and lo, see tile_ops.cuh), converted with one
+// rounding and scaled by fx_inv (a power of two) -- no FP64 arithmetic, whose rate is low on
+// this GPU.  A tile with origin cell t0 = tc * T + 1 covers the global positions
 // [tc * T - OFS + gcl, tc * T - OFS + gcl + je) along each axis (je = T + ORD + 2 points).
 struct FoldBox {
     const float *th, *tl;   // tile currents (2D: value and compensation; 3D: fixed-point words)
@@ -808,8 +820,10 @@ __device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
                     const int lz = DIM > 2 ? gz - (tz * Ta[2] - ofs + gl[2]) : 0;
                     const long o = tile * (3L * nj) + 3L * (lx + jea[0] * (ly + (long)jea[1] * lz)) + c;
                     if constexpr (DIM == 3) {
-                        fx += (long long)__float_as_int(tl[o]) * (1LL << fx_shift) +
-                              (long long)__float_as_uint(th[o]);
+                        // hi 2^B + (the low B bits of every add, summed: lo - hi 2^B mod 2^32)
+                        const int hw = __float_as_int(tl[o]);
+                        const unsigned lw = __float_as_uint(th[o]) - ((unsigned)hw << fx_shift);
+                        fx += (long long)hw * (1LL << fx_shift) + (long long)lw;
                     } else {
                         v += (double)th[o];
                         if (tl) v += (double)tl[o];
@@ -954,6 +968,26 @@ int push_batch_launch(int dim, int order, const TiledArgs *boxes, const int2 *wo
                       int *counter, unsigned grid, int threads, size_t smem, cudaStream_t st);
 cudaError_t push_batch_attr(int dim, int order, int bytes);
 
+// Opt a push kernel in to `bytes` of dynamic shared memory (error if that does not fit beside
+// its static shared memory).  The attribute belongs to the kernel, not to a state: it only
+// grows, so that states of different tile shapes or CTA sizes in one process never lower it
+// under one another.  (It is not raised to the device limit up front, which would let the
+// driver size the L1/shared split for the largest launch possible rather than the one made.)
+template <typename K> cudaError_t set_smem_room(K kernel, int bytes)
+{
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    int dev = 0, lim = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) !=
+        cudaSuccess)
+        return e;
+    if (bytes > lim - (int)fa.sharedSizeBytes) return cudaErrorInvalidValue;
+    if (bytes <= fa.maxDynamicSharedSizeBytes) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 #define OSG_DEFINE_PUSH_TILED(P, LAUNCH, ATTR)                                                \
     int LAUNCH(int dim, int order, const TiledArgs &a, unsigned ntiles, int threads,          \
                size_t smem, cudaStream_t st)                                                  \
@@ -987,13 +1021,9 @@ cudaError_t push_batch_attr(int dim, int order, int bytes);
         return OSG_OK;                                                                        \
     }
 #define OSG_PUSH_TILED_ATTR(D, O, P)                                                          \
-    if (dim == D && order == O)                                                               \
-        return cudaFuncSetAttribute(k_push_tiled<D, O, P>,                                    \
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (dim == D && order == O) return set_smem_room(k_push_tiled<D, O, P>, bytes);
 #define OSG_PUSH_BATCH_ATTR(D, O, P)                                                          \
-    if (dim == D && order == O)                                                               \
-        return cudaFuncSetAttribute(k_push_tiled_batch<D, O, P>,                              \
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (dim == D && order == O) return set_smem_room(k_push_tiled_batch<D, O, P>, bytes);
 #define OSG_PUSH_BATCH_LAUNCH(D, O, P)                                                        \
     if (dim == D && order == O) {                                                             \
         k_push_tiled_batch<D, O, P><<<grid, threads, smem, st>>>(boxes, work, nwork, counter); \

@@ -129,13 +129,14 @@ def build_batch(nbox=64, tile=None, threads=0):
     return bt, n
 
 
-def dropin_steps(sp_host, nx, dx, dt, order, steps):
+def dropin_steps(sp_host, nx, dx, dt, order, steps, pinned=True):
     """Drop-in flow on host buffers, as an unchanged OSIRIS host would drive the library: field
     guard replace, per species osg_vadvance_deposit_f32 and the periodic particle boundary,
     current fold and Yee through the host-array C ABI (2D, FP32; every copy inside the timed
     part).  sp_host: per species (ix, x, u, q) host arrays, rqm -1.  Returns particle-steps/s,
     the host-to-device and device-to-host bytes per step (counted from the arrays each call
-    copies) and the number of timed steps."""
+    copies) and the number of timed steps.  pinned=False keeps the particles in ordinary
+    (pageable) host memory, as a Fortran host allocates them."""
     gl, gu = osg.GUARD[order]
     size = [n + gl + gu for n in nx]
     shape = tuple(reversed(size)) + (3,)
@@ -148,7 +149,7 @@ def dropin_steps(sp_host, nx, dx, dt, order, steps):
     for ix, x, u, q in sp_host:
         arrs = []
         for a in (ix, x, u, q):
-            p = osg.pinned_empty(a.shape, a.dtype)
+            p = osg.pinned_empty(a.shape, a.dtype) if pinned else np.empty_like(a)
             p[...] = a
             arrs.append(p)
         pin.append(arrs)
@@ -174,7 +175,7 @@ def dropin_steps(sp_host, nx, dx, dt, order, steps):
     # bytes moved per step (counted from the arrays each call copies)
     h2d = 2 * gbytes + sum(len(p[3]) * 32 + 3 * gbytes for p in pin) + gbytes + 3 * gbytes
     d2h = 2 * gbytes + sum(len(p[3]) * 28 + gbytes + 12 for p in pin) + gbytes + 2 * gbytes
-    for arrs in pin:
+    for arrs in pin if pinned else ():
         for a in arrs:
             osg.pinned_free(a)
     for a in (e, b, j):
@@ -233,6 +234,8 @@ def main():
     ap.add_argument("--fp64-check", action="store_true",
                     help="mixed-precision runs: report the error against the plain FP64 "
                          "engine after the same steps from the same load")
+    ap.add_argument("--pageable", action="store_true",
+                    help="--dropin: particles in pageable host memory instead of pinned")
     ap.add_argument("--dropin", action="store_true",
                     help="2D configurations: time the host-array drop-in flow instead "
                          "(osg_vadvance_deposit_f32 per species, guard updates and Yee on "
@@ -262,8 +265,10 @@ def main():
         r = osg.Rng(cfg["seed"])
         sp = [osg.load_lattice(r, 32, nx, cfg["ppc"], cfg["dx"], -1.0, [s["uth"]] * 3,
                                s["ufl"], cfg["amp"], 1.0) for s in cfg["species"]]
-        rate, h2d, d2h, n = dropin_steps(sp, nx, cfg["dx"], cfg["dt"], cfg["order"], args.steps)
+        rate, h2d, d2h, n = dropin_steps(sp, nx, cfg["dx"], cfg["dt"], cfg["order"], args.steps,
+                                         pinned=not args.pageable)
         print(json.dumps(dict(config=args.config, path="host-array drop-in", nx=nx,
+                              memory="pageable" if args.pageable else "pinned",
                               particles=sum(len(s[3]) for s in sp), steps=n,
                               particle_steps_per_s=rate, h2d_bytes_per_step=h2d,
                               d2h_bytes_per_step=d2h)))
