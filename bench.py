@@ -68,7 +68,7 @@ def peaks():
 # workload, from one ncu capture (one metric pass, --clock-control none) of the current kernel;
 # the command and the figures are in profiles/push_tiled_c2.md.  None when no capture matches
 # the kernel as built.
-PUSH_TRAFFIC_BYTES = 1142254080
+PUSH_TRAFFIC_BYTES = 1115267840
 
 
 class Clocks:

@@ -322,9 +322,10 @@ typedef struct {
                          boundaries (first-order Mur update of the tangential E, the
                          reference's p_bc_lindman) and particles leaving through them are
                          absorbed; not with walls, smoothing or the moving window */
-    int thermal;      /* PLAIN engine: bit d set (axis d walled or open): particles crossing its
-                         edges are re-emitted from a thermal bath (the reference's
-                         p_bc_thermal, thermal_type "thermal") instead of reflected or absorbed */
+    int thermal;      /* bit d set (axis d walled or open): particles crossing its edges are
+                         re-emitted from a thermal bath (the reference's p_bc_thermal) instead
+                         of reflected or absorbed.  Both engines; the random stream is keyed by
+                         the particle's index (PLAIN) or its tile slot (TILED) */
     unsigned int seed;      /* key of the re-emission random stream */
     double uth_bnd[3];      /* the bath's thermal momentum per component */
     double ufl_bnd[3];      /* its fluid momentum (added only when all three are non-zero) */

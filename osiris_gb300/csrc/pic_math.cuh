@@ -722,4 +722,81 @@ inline double pusher_tem(int pusher, double dt, double rqm)
                : 0.5 * dt / rqm;
 }
 
+// Philox4x32-10 (Salmon, Moraes, Dror and Shaw, "Parallel random numbers: as easy as 1, 2, 3",
+// SC11): ten rounds of two 32x32 -> 64-bit multiplies, the key bumped by the Weyl constants
+// between rounds.  A counter-based stream: every re-emission draws from its own counter.
+__device__ __forceinline__ void philox4x32_10(unsigned int c[4], unsigned int k0, unsigned int k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const unsigned int lo0 = 0xD2511F53u * c[0], hi0 = __umulhi(0xD2511F53u, c[0]);
+        const unsigned int lo1 = 0xCD9E8D57u * c[2], hi1 = __umulhi(0xCD9E8D57u, c[2]);
+        const unsigned int n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+// One thermal-bath draw for a particle re-emitted at the lower (lower = true) or upper edge of
+// axis d (thermal_bath, source/spec/os-spec-boundary.f03:972-1067): the momentum un[3] and the
+// uniform number v3 in (0, 1) that places it along d.  One Philox4x32-10 call, counter (the
+// particle's id, its high word, step, d + 4 side) and key (seed, species); the four 32-bit
+// outputs r become (r + 1/2) / 2^32 in double.  thermal_type 0 "thermal": uth_c times a
+// Box-Muller Gaussian for the two tangential components and uth_d times the half-Maxwellian
+// sqrt(-2 ln v) pointing into the box for the normal one; 1 "random dir"; 2 "waterbag".  The
+// fluid momentum ufl is then added relativistically when all three of its components are
+// non-zero.
+template <typename T>
+__device__ __forceinline__ void bath_draw(const T *uth, const T *ufl, int type, int d,
+                                          bool lower, unsigned long long id, unsigned int step,
+                                          unsigned int key0, unsigned int key1, T *un,
+                                          double *v3out)
+{
+    const double inv32 = 2.3283064365386963e-10;   // 2^-32
+    const int code = lower ? 1 : 2;
+    unsigned int r[4] = {(unsigned int)id, (unsigned int)(id >> 32), step,
+                         (unsigned int)(d + 4 * code)};
+    philox4x32_10(r, key0, key1);
+    const double v0 = (r[0] + 0.5) * inv32, v1 = (r[1] + 0.5) * inv32;
+    const double v2 = (r[2] + 0.5) * inv32, v3 = (r[3] + 0.5) * inv32;
+    const T usign = lower ? T(1) : T(-1);
+    if (type == 1) {
+        // "random dir": |uth| along a random direction, u3 = upar |uth| and the other two
+        // on a circle of radius sqrt(1 - upar) |uth| (the reference's expression, :1026-1041)
+        const T ut = sqrt(uth[0] * uth[0] + uth[1] * uth[1] + uth[2] * uth[2]);
+        const T upar = (T)(2.0 * v0 - 1.0);
+        const T uperp = sqrt(T(1) - upar) * ut;
+        const T th = (T)(6.283185307179586 * v1);
+        un[0] = cos(th) * uperp;
+        un[1] = sin(th) * uperp;
+        un[2] = upar * ut;
+        un[d] = usign * fabs(un[d]);
+    } else if (type == 2) {
+        // "waterbag": uniform in [-uth/2, uth/2) per component (:1016-1024)
+        const double w[3] = {v0, v1, v2};
+        for (int c = 0; c < 3; c++) un[c] = uth[c] * (T)(w[c] - 0.5);
+        un[d] = usign * fabs(un[d]);
+    } else {
+        const double rad = sqrt(-2.0 * log(v0)), th = 6.283185307179586 * v1;
+        const double gs[2] = {rad * cos(th), rad * sin(th)};
+        for (int c = 0, k = 0; c < 3; c++)
+            if (c != d) un[c] = uth[c] * (T)gs[k++];
+        un[d] = usign * uth[d] * (T)sqrt(-2.0 * log(v2));
+    }
+    const T f1 = ufl[0], f2 = ufl[1], f3 = ufl[2];
+    if (f1 != T(0) && f2 != T(0) && f3 != T(0)) {
+        const T fa = T(1) / (T(1) + sqrt(T(1) + f1 * f1 + f2 * f2 + f3 * f3));
+        const T gth = sqrt(T(1) + un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);
+        const T fb = gth + fa * (f1 * un[0] + f2 * un[1] + f3 * un[2]);
+        un[0] = un[0] + fb * f1;
+        un[1] = un[1] + fb * f2;
+        un[2] = un[2] + fb * f3;
+    }
+    *v3out = v3;
+}
+
 } // namespace osg

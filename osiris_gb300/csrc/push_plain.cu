@@ -190,25 +190,6 @@ __device__ __forceinline__ int store_position(const PlainPushArgs<T> &a, long p,
     return code << (2 * d);
 }
 
-// Philox4x32-10 (Salmon, Moraes, Dror and Shaw, "Parallel random numbers: as easy as 1, 2, 3",
-// SC11): ten rounds of two 32x32 -> 64-bit multiplies, the key bumped by the Weyl constants
-// between rounds.  A counter-based stream: every re-emission draws from its own counter.
-__device__ __forceinline__ void philox4x32_10(unsigned int c[4], unsigned int k0, unsigned int k1)
-{
-#pragma unroll
-    for (int r = 0; r < 10; r++) {
-        const unsigned int lo0 = 0xD2511F53u * c[0], hi0 = __umulhi(0xD2511F53u, c[0]);
-        const unsigned int lo1 = 0xCD9E8D57u * c[2], hi1 = __umulhi(0xCD9E8D57u, c[2]);
-        const unsigned int n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
-        c[0] = n0;
-        c[1] = lo1;
-        c[2] = n2;
-        c[3] = lo0;
-        k0 += 0x9E3779B9u;
-        k1 += 0xBB67AE85u;
-    }
-}
-
 // Thermal-bath re-emission of particle p after it crossed the edges coded in tb (2 bits per
 // axis: 1 lower, 2 upper), axis by axis (p_bc_thermal, source/spec/os-spec-boundary.f03:
 // 1315-1387, with thermal_bath :972-1067; thermal_type "thermal" below, "random dir" and
@@ -227,52 +208,16 @@ __device__ __forceinline__ void philox4x32_10(unsigned int c[4], unsigned int k0
 template <typename T, int DIM, int ORD>
 __device__ __noinline__ void thermal_reemit(const PlainPushArgs<T> &a, long p, T q, int tb)
 {
-    const double inv32 = 2.3283064365386963e-10;   // 2^-32
     for (int d = 0; d < DIM; d++) {
         const int code = (tb >> (2 * d)) & 3;
         if (!code) continue;
         const bool lower = code == 1;
         a.ix[DIM * p + d] = lower ? 1 : a.thermal[d];
-        unsigned int r[4] = {(unsigned int)p, (unsigned int)((unsigned long long)p >> 32),
-                             (unsigned int)*a.step, (unsigned int)(d + 4 * code)};
-        philox4x32_10(r, a.rng_key[0], a.rng_key[1]);
-        const double v0 = (r[0] + 0.5) * inv32, v1 = (r[1] + 0.5) * inv32;
-        const double v2 = (r[2] + 0.5) * inv32, v3 = (r[3] + 0.5) * inv32;
-        const T usign = lower ? T(1) : T(-1);
         T un[3];
-        if (a.thermal_type == 1) {
-            // "random dir": |uth| along a random direction, u3 = upar |uth| and the other two
-            // on a circle of radius sqrt(1 - upar) |uth| (the reference's expression, :1026-1041)
-            const T ut = sqrt(a.uth_bnd[0] * a.uth_bnd[0] + a.uth_bnd[1] * a.uth_bnd[1] +
-                              a.uth_bnd[2] * a.uth_bnd[2]);
-            const T upar = (T)(2.0 * v0 - 1.0);
-            const T uperp = sqrt(T(1) - upar) * ut;
-            const T th = (T)(6.283185307179586 * v1);
-            un[0] = cos(th) * uperp;
-            un[1] = sin(th) * uperp;
-            un[2] = upar * ut;
-            un[d] = usign * fabs(un[d]);
-        } else if (a.thermal_type == 2) {
-            // "waterbag": uniform in [-uth/2, uth/2) per component (:1016-1024)
-            const double w[3] = {v0, v1, v2};
-            for (int c = 0; c < 3; c++) un[c] = a.uth_bnd[c] * (T)(w[c] - 0.5);
-            un[d] = usign * fabs(un[d]);
-        } else {
-            const double rad = sqrt(-2.0 * log(v0)), th = 6.283185307179586 * v1;
-            const double gs[2] = {rad * cos(th), rad * sin(th)};
-            for (int c = 0, k = 0; c < 3; c++)
-                if (c != d) un[c] = a.uth_bnd[c] * (T)gs[k++];
-            un[d] = usign * a.uth_bnd[d] * (T)sqrt(-2.0 * log(v2));
-        }
-        const T f1 = a.ufl_bnd[0], f2 = a.ufl_bnd[1], f3 = a.ufl_bnd[2];
-        if (f1 != T(0) && f2 != T(0) && f3 != T(0)) {
-            const T fa = T(1) / (T(1) + sqrt(T(1) + f1 * f1 + f2 * f2 + f3 * f3));
-            const T gth = sqrt(T(1) + un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);
-            const T fb = gth + fa * (f1 * un[0] + f2 * un[1] + f3 * un[2]);
-            un[0] = un[0] + fb * f1;
-            un[1] = un[1] + fb * f2;
-            un[2] = un[2] + fb * f3;
-        }
+        double v3;
+        bath_draw<T>(a.uth_bnd, a.ufl_bnd, a.thermal_type, d, lower,
+                     (unsigned long long)p, (unsigned int)*a.step, a.rng_key[0], a.rng_key[1],
+                     un, &v3);
         for (int c = 0; c < 3; c++) a.u[3 * p + c] = un[c];
         const T rg = T(1) / sqrt(T(1) + un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);
         const T xpos = lower ? T(-0.5) : (sizeof(T) == 4 ? T(0.49999997f) : T(0.49999999999999994));

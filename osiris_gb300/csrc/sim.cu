@@ -494,8 +494,9 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               "pmc: a bit mask of walled axes");
     OSG_CHECK(cfg->thermal >= 0 && (cfg->thermal & ~(cfg->walls | cfg->open_fields)) == 0,
               OSG_ERR_ARG, "thermal: a bit mask of walled or open axes");
-    OSG_CHECK(cfg->thermal == 0 || cfg->engine == OSG_ENGINE_PLAIN, OSG_ERR_ARG,
-              "thermal-bath particle boundaries run on the plain engine");
+    OSG_CHECK(cfg->thermal == 0 || cfg->engine == OSG_ENGINE_PLAIN ||
+                  cfg->pusher == OSG_PUSHER_BORIS,
+              OSG_ERR_ARG, "tiled engine: the thermal bath runs with the Boris pusher");
     OSG_CHECK(cfg->thermal_type >= 0 && cfg->thermal_type <= 2, OSG_ERR_ARG,
               "thermal_type: 0 thermal, 1 random dir, 2 waterbag");
     if (cfg->thermal)
@@ -581,6 +582,7 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
             osg_sim_destroy(s);
             return rc;
         }
+        tiled_set_step(s->tiled, s->d_step);
     }
     if (cudaStreamSynchronize(s->st) != cudaSuccess) {
         set_error("initialisation failed");
@@ -1225,6 +1227,7 @@ static int tune_tiled(osg_sim *s, int steps, int *tile, int *threads)
             TiledState *tr = nullptr;
             rc = tiled_create(&tr, c, s->g);
             if (rc) continue;   // does not fit (shared memory, tile cells)
+            tiled_set_step(tr, s->d_step);
             rc = tiled_set_threads(tr, th);
             for (int k = 0; k < ns && !rc; k++)
                 rc = tiled_add_species(tr, s->rqm[k], hnp[k], hix[k].data(), hx[k].data(),
@@ -1260,6 +1263,7 @@ static int tune_tiled(osg_sim *s, int steps, int *tile, int *threads)
         for (int d = 0; d < 3; d++) c.tile[d] = bestT[d];
         TiledState *nt = nullptr;
         if ((rc = tiled_create(&nt, c, s->g))) return rc;
+        tiled_set_step(nt, s->d_step);
         rc = tiled_set_threads(nt, best_th);
         for (int k = 0; k < ns && !rc; k++)
             rc = tiled_add_species(nt, s->rqm[k], hnp[k], hix[k].data(), hx[k].data(),

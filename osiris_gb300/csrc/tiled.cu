@@ -68,6 +68,11 @@ struct TiledState {
     // kernel replay saves and restores device memory and needs the dropped lines defined)
     int l2_discard = 1;
     int walls = 0;   // bit d: conducting walls on axis d
+    // thermal-bath particle boundary (bit d: walled or open axis d re-emits)
+    int thermal = 0, thermal_type = 0;
+    unsigned int seed = 0;
+    float uth_bnd[3] = {0, 0, 0}, ufl_bnd[3] = {0, 0, 0};
+    const unsigned long long *step = nullptr;   // the owner's step counter
     int open_fields = 0;   // bit d: Lindman open boundaries on axis d (particles absorbed)
     int pusher = OSG_PUSHER_BORIS;
     double iter_tol = 1.0e-3;
@@ -173,8 +178,10 @@ static FxFormat fx_format(const TiledState *t)
     for (int d = 0; d < t->dim; d++) jn = std::max(jn, t->dx[d] / push_dt(t) / 3.0);
     double qm = 0.0;
     for (double v : t->qmax) qm = std::max(qm, v);
+    // segments per particle: 4 at most, plus 4 per re-emitting thermal-bath axis
+    const double segs = 4.0 + 4.0 * __builtin_popcount((unsigned)t->thermal);
     double n = 0.0;
-    for (long c : t->cap) n += 4.0 * (double)c;
+    for (long c : t->cap) n += segs * (double)c;
     n = std::max(n, 1.0);
     int B = (int)std::floor(32.0 - std::log2(n));
     while (B > 0 && n * std::ldexp(1.0, B) > 4294967296.0) B--;
@@ -209,6 +216,14 @@ static TiledArgs base_args(const TiledState *t)
     a.tile_lo = t->tile_lo;
     a.discard = t->l2_discard;
     a.walls = t->walls;
+    a.thermal = t->thermal;
+    a.thermal_type = t->thermal_type;
+    a.seed = t->seed;
+    a.step = t->step;
+    for (int d = 0; d < 3; d++) {
+        a.uth_bnd[d] = t->uth_bnd[d];
+        a.ufl_bnd[d] = t->ufl_bnd[d];
+    }
     a.fx = fx_format(t);
     return a;
 }
@@ -250,6 +265,13 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
     t->dt = cfg.dt;
     t->capacity = cfg.capacity > 0 ? cfg.capacity : 3.0;
     t->walls = cfg.walls;
+    t->thermal = cfg.thermal;
+    t->thermal_type = cfg.thermal_type;
+    t->seed = cfg.seed;
+    for (int d = 0; d < 3; d++) {
+        t->uth_bnd[d] = (float)cfg.uth_bnd[d];
+        t->ufl_bnd[d] = (float)cfg.ufl_bnd[d];
+    }
     t->open_fields = cfg.open_fields;
     t->ntiles = 1;
     for (int d = 0; d < 3; d++) {
@@ -555,6 +577,12 @@ void batch_fold(const FoldBox *d_boxes, int nbox, int dim, long max_points, cuda
     const dim3 grid(grid_x(max_points), (unsigned)nbox);
     if (dim == 2) k_batch_fold<2><<<grid, 256, 0, st>>>(d_boxes);
     else k_batch_fold<3><<<grid, 256, 0, st>>>(d_boxes);
+}
+
+int tiled_set_step(TiledState *t, const unsigned long long *step)
+{
+    t->step = step;
+    return OSG_OK;
 }
 
 int tiled_set_threads(TiledState *t, int threads)

@@ -53,5 +53,7 @@ size_t tiled_smem(const TiledState *t);
 int tiled_threads(const TiledState *t);
 // threads per push CTA (multiple of 32, 64..256); call before any step
 int tiled_set_threads(TiledState *t, int threads);
+// the thermal-bath random stream's step counter (device memory of the owner)
+int tiled_set_step(TiledState *t, const unsigned long long *step);
 
 } // namespace osg

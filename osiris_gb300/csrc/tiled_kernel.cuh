@@ -142,6 +142,15 @@ struct TiledArgs {
     int shift_x;
     // bit d: axis d is bounded by conducting walls (particles reflect specularly)
     int walls;
+    // bit d (a walled or open axis): particles crossing its edges are re-emitted from a thermal
+    // bath (tiled_reemit): distribution thermal_type, momenta uth_bnd / ufl_bnd, random stream
+    // keyed by (seed, species) with the step counter at *step
+    int thermal;
+    int thermal_type;
+    unsigned int seed;
+    const unsigned long long *step;
+    float uth_bnd[3];
+    float ufl_bnd[3];
     // 1: drop the dead input-slab lines from L2 after the sort (discard_dead_slab).  0 for
     // multi-pass profiler replay, which saves and restores memory and needs it defined
     int discard;
@@ -234,17 +243,80 @@ __device__ __forceinline__ void discard_dead_slab(const Slabs &in, long slab, in
 // to its new slot, then deposit the segments (round t takes the t-th segment of every lane).
 // In 2D every warp accumulates into its own copy of the current tile (with a two-sum
 // compensation), so its adds are plain shared read-modify-writes; the copies are summed when
-// the tile is flushed.  In 3D the warps share one current tile, accumulated exactly in 64-bit
-// fixed point by integer atomics (lanes_deposit3).
+// the tile is flushed.  In 3D the warps share one current tile, accumulated exactly as fixed
+// point by 32-bit integer atomics (lanes_deposit3).
 // CTAs of up to 256 threads.  2D linear/quadratic: three resident CTAs per SM (at most 85
 // registers per thread, measured fastest on GB300); 2D quartic: one (it needs ~250 registers
 // without spilling); otherwise two
 template <int DIM, int ORD>
 constexpr int push_min_blocks() { return DIM == 2 ? (ORD <= 2 ? 3 : (ORD == 3 ? 2 : 1)) : 2; }
 
+// Thermal-bath re-emission in the tiled engine (p_bc_thermal, source/spec/os-spec-boundary.f03:
+// 1315-1387, thermal_bath :972-1067, rev_current :1392-1440), for a particle whose move
+// crossed the bath edges coded in tb (2 bits per axis: 1 lower, 2 upper), axis by axis as the
+// plain engine's thermal_reemit: the cell along d becomes the edge cell, the momenta come from
+// bath_draw, the offset along d is xpos + u_d / gamma dt/dx_d v (xpos = -1/2 or the float just
+// below 1/2), and the current of the way in, -q from the new position back along
+// -u / gamma dt/dx, goes into the tile: in 2D by FP32 atomics into the warp's copy, in 3D by
+// the exact fixed-point adds.  cn: the cells after the move before any wrap (the path's start
+// cell in the tile's frame); cw receives the cells the particle is stored at.  The random
+// stream is keyed by (seed, species) with the counter (id, step, axis and side); id, the
+// particle's input slot, is unique within a species and step.  Particles of the tiled engine
+// have no fixed index, so the stream is not the plain engine's: the same distributions.
+template <int DIM, int ORD>
+__device__ __noinline__ void tiled_reemit(const TiledArgs &a, int s, long id, int tb,
+                                          const int *t0, const int *cn, int *cw, float *xo,
+                                          float *un, float q, float *sJw, unsigned *sJl,
+                                          unsigned *sJh, int jsy, int jsz)
+{
+    int lc[3] = {0, 0, 0};
+    for (int k = 0; k < DIM; k++) lc[k] = cn[k];
+    for (int d = 0; d < DIM; d++) {
+        const int code = (tb >> (2 * d)) & 3;
+        if (!code) continue;
+        const bool lower = code == 1;
+        cw[d] = lower ? 1 : a.nx[d];
+        lc[d] = cw[d];
+        double v3;
+        bath_draw<float>(a.uth_bnd, a.ufl_bnd, a.thermal_type, d, lower, (unsigned long long)id,
+                         (unsigned int)*a.step, a.seed, (unsigned int)s, un, &v3);
+        const float rg = 1.0f / sqrtf(1.0f + un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);
+        const float xpos = lower ? -0.5f : 0.49999997f;
+        const float vperp = rg * un[d] * a.dtdx[d];
+        xo[d] = xpos + vperp * (float)v3;
+        float xv[3] = {0.f, 0.f, 0.f};
+        int di[3] = {0, 0, 0};
+        for (int k = 0; k < DIM; k++) {
+            xv[k] = xo[k] - un[k] * rg * a.dtdx[k];
+            di[k] = trim(xv[k]);
+        }
+        SegRec sg[DIM == 2 ? 3 : 4];
+        const int ns = make_segments<DIM>(sg, xo, xv, di, un[2] * rg, -q, lc[0] - t0[0] + 1,
+                                          DIM > 1 ? lc[1] - t0[1] + 1 : 0,
+                                          DIM > 2 ? lc[2] - t0[2] + 1 : 0, jsy, jsz);
+        for (int t = 0; t < ns; t++) {
+            if constexpr (DIM == 2) {
+                constexpr int NV = SegVals<2, ORD>::NV;
+                float v[NV];
+                seg_values2_fast<ORD>(seg2_of<ORD>(sg[t]), sg[t].q, a.jn[0], a.jn[1], v);
+                for (int k = 0; k < NV; k++)
+                    atomicAdd(sJw + sg[t].base + seg_offset<2, ORD>(k, jsy, 0), v[k]);
+            } else {
+                lanes_deposit3<ORD>(sJl, sJh, sg[t], true, a.jn, jsy, jsz, a.fx);
+            }
+        }
+    }
+}
+
 // The whole push of one tile by the calling CTA (all threads; contains block barriers; a CTA
 // that pushes several tiles in a row puts a block barrier between the calls).
-template <int DIM, int ORD, int PUSHER>
+// DYN: the warps take the tile's 32-particle chunks from a shared counter (less waiting at the
+// block barrier behind the slowest warp: 1.7% faster on the two-stream workload); otherwise
+// warp w takes chunks w, w + warps, ... (the persistent batch, whose light tiles are one chunk
+// per warp: 2.9% faster there)
+// BATH: the thermal-bath particle boundary is compiled in (a variant of its own: its code in
+// the push loop cost the other kernels 14-43% through register allocation)
+template <int DIM, int ORD, int PUSHER, bool DYN, bool BATH>
 __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
 {
     constexpr int NP = ORD + 1, OFS = Stencil<ORD>::OFS;
@@ -304,9 +376,13 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     __shared__ int sLeaveI[LEAVE_QUEUE][4];      // new cell per axis, destination tile
     __shared__ float sLeaveF[LEAVE_QUEUE][8];    // offsets per axis, momenta, charge
     __shared__ int sNleave;
+    __shared__ int sChunk;   // DYN: next chunk of the current species
     // per-warp energy of every species, summed when the tile is done
     __shared__ float sEne[MAX_TILED_SPECIES][8];
-    if (threadIdx.x == 0) sNleave = 0;
+    if (threadIdx.x == 0) {
+        sNleave = 0;
+        sChunk = 0;
+    }
     __syncthreads();
 
     const int esy = 3 * ee[0], esz = 3 * ee[0] * ee[1];
@@ -442,9 +518,15 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 // non-periodic axes (a launch-uniform test, so the periodic box pays one branch)
                 bool gone = false;
                 if (a.walls | a.open | a.window) {
+                    int tb = 0;   // thermal-bath edges crossed (2 bits per axis)
 #pragma unroll
                     for (int d = 0; d < DIM; d++) {
-                        if ((a.walls >> d) & 1) {
+                        if (BATH && ((a.thermal >> d) & 1)) {
+                            // thermal bath: re-emitted from the edge below
+                            cw[d] = cn[d];
+                            if (cn[d] < 1 || cn[d] > a.nx[d])
+                                tb |= (cn[d] < 1 ? 1 : 2) << (2 * d);
+                        } else if ((a.walls >> d) & 1) {
                             // conducting wall: specular reflection after the deposit of the
                             // unreflected path (p_bc_specular,
                             // source/spec/os-spec-boundary.f03:1293-1310)
@@ -473,6 +555,11 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                             cw[d] = cn[d];
                             gone = gone || cw[d] < 1 || cw[d] > a.nx[d];
                         }
+                    }
+                    if constexpr (BATH) {
+                        if (tb)
+                            tiled_reemit<DIM, ORD>(a, s, p, tb, t0, cn, cw, xo, un, q, sJw,
+                                                   sJl, sJh, jsy, jsz);
                     }
                 }
                 if (gone) {
@@ -540,18 +627,29 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
             return nseg > 0 ? nseg : (has ? 0 : -1);
         };
         // a warp takes 32 consecutive particles of the cell-sorted tile (coalesced; mostly one
-        // cell)
-        const int nit = (n + nthr - 1) / nthr;
-        auto index = [&](int it) { return it * nthr + (int)threadIdx.x; };
-        prefetch(index(0), n);
-        for (int it = 0; it < nit; it++) {
-            const int i = index(it);
+        // cell) at a time
+        const int nck = (n + 31) >> 5;
+        auto next_chunk = [&](int ck) {
+            if constexpr (DYN) {
+                int g = 0;
+                if (lane == 0) g = atomicAdd(&sChunk, 1);
+                return __shfl_sync(FULL_MASK, g, 0);
+            } else {
+                return ck < 0 ? warp : ck + nwarp;
+            }
+        };
+        int ck = next_chunk(-1);
+        if (ck < nck) prefetch(32 * ck + (int)lane, n);
+        while (ck < nck) {
+            const int i = 32 * ck + (int)lane;
+            const int nk = next_chunk(ck);
             SegRec sg[MAXSEG];
             int c[3];
             float xo[3], un[3], q;
             take(c, xo, un, q);
-            if (it + 1 < nit) prefetch(index(it + 1), n);
+            if (nk < nck) prefetch(32 * nk + (int)lane, n);
             const int ns = push_one(i < n, slot(i), c, xo, un, q, sg);
+            if constexpr (BATH) __syncwarp();   // re-emission currents visible to the warp
             // ---- charge-conserving current of the segments into the shared tile: the first
             //      segment (in the particle's own cell, shared by neighbouring lanes of the
             //      cell-sorted tile) is summed per run of lanes with one cell; the others
@@ -587,6 +685,7 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                     lanes_deposit3<ORD>(sJl, sJh, sg[0], hs, a.jn, jsy, jsz, a.fx);
                 }
             }
+            ck = nk;
         }
         // ---- energy: per-warp partial (the tile's sum is taken when the tile is done)
         {
@@ -684,7 +783,10 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
                 }
             }
         }
-        if (threadIdx.x == 0) sNleave = 0;
+        if (threadIdx.x == 0) {
+            sNleave = 0;
+            sChunk = 0;
+        }
         __syncthreads();
         if (a.discard) discard_dead_slab<DIM>(sd.in, slab, nst, nar, cap);
     }
@@ -732,10 +834,57 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     }
 }
 
-template <int DIM, int ORD, int PUSHER>
+// Opt a push kernel in to `bytes` of dynamic shared memory (error if that does not fit beside
+// its static shared memory).  The attribute belongs to the kernel, not to a state: it only
+// grows, so that states of different tile shapes or CTA sizes in one process never lower it
+// under one another.  (It is not raised to the device limit up front, which would let the
+// driver size the L1/shared split for the largest launch possible rather than the one made.)
+template <typename K> cudaError_t set_smem_room(K kernel, int bytes)
+{
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    int dev = 0, lim = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) !=
+        cudaSuccess)
+        return e;
+    if (bytes > lim - (int)fa.sharedSizeBytes) return cudaErrorInvalidValue;
+    if (bytes <= fa.maxDynamicSharedSizeBytes) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+template <int DIM, int ORD, int PUSHER, bool BATH>
 __global__ void __launch_bounds__(256, push_min_blocks<DIM, ORD>()) k_push_tiled(TiledArgs a)
 {
-    push_tile<DIM, ORD, PUSHER>(a, blockIdx.x);
+    push_tile<DIM, ORD, PUSHER, true, BATH>(a, blockIdx.x);
+}
+
+// launch of the single-box push: the thermal-bath variant when the state has a bath (Boris
+// pusher only)
+template <int D, int O, int P>
+int launch_push_tiled(const TiledArgs &a, unsigned ntiles, int threads, size_t smem,
+                      cudaStream_t st)
+{
+    if (a.thermal) {
+        if constexpr (P == OSG_PUSHER_BORIS) {
+            k_push_tiled<D, O, P, true><<<ntiles, threads, smem, st>>>(a);
+            return OSG_OK;
+        } else {
+            set_error("tiled engine: the thermal bath runs with the Boris pusher");
+            return OSG_ERR_ARG;
+        }
+    }
+    k_push_tiled<D, O, P, false><<<ntiles, threads, smem, st>>>(a);
+    return OSG_OK;
+}
+
+template <int D, int O, int P> cudaError_t attr_push_tiled(int bytes)
+{
+    cudaError_t e = set_smem_room(k_push_tiled<D, O, P, false>, bytes);
+    if constexpr (P == OSG_PUSHER_BORIS)
+        if (e == cudaSuccess) e = set_smem_room(k_push_tiled<D, O, P, true>, bytes);
+    return e;
 }
 
 // Persistent push over many independent boxes in one launch: every CTA takes (box, tile)
@@ -756,7 +905,7 @@ k_push_tiled_batch(const TiledArgs *__restrict__ boxes, const int2 *__restrict__
         const int2 w = work[it];
         if (threadIdx.x == 0) sA = boxes[w.x];
         __syncthreads();
-        push_tile<DIM, ORD, PUSHER>(sA, w.y);
+        push_tile<DIM, ORD, PUSHER, false, false>(sA, w.y);
         __syncthreads();
     }
 }
@@ -968,26 +1117,6 @@ int push_batch_launch(int dim, int order, const TiledArgs *boxes, const int2 *wo
                       int *counter, unsigned grid, int threads, size_t smem, cudaStream_t st);
 cudaError_t push_batch_attr(int dim, int order, int bytes);
 
-// Opt a push kernel in to `bytes` of dynamic shared memory (error if that does not fit beside
-// its static shared memory).  The attribute belongs to the kernel, not to a state: it only
-// grows, so that states of different tile shapes or CTA sizes in one process never lower it
-// under one another.  (It is not raised to the device limit up front, which would let the
-// driver size the L1/shared split for the largest launch possible rather than the one made.)
-template <typename K> cudaError_t set_smem_room(K kernel, int bytes)
-{
-    cudaFuncAttributes fa;
-    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
-    if (e != cudaSuccess) return e;
-    int dev = 0, lim = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) !=
-        cudaSuccess)
-        return e;
-    if (bytes > lim - (int)fa.sharedSizeBytes) return cudaErrorInvalidValue;
-    if (bytes <= fa.maxDynamicSharedSizeBytes) return cudaSuccess;
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-}
-
 #define OSG_DEFINE_PUSH_TILED(P, LAUNCH, ATTR)                                                \
     int LAUNCH(int dim, int order, const TiledArgs &a, unsigned ntiles, int threads,          \
                size_t smem, cudaStream_t st)                                                  \
@@ -1016,12 +1145,9 @@ template <typename K> cudaError_t set_smem_room(K kernel, int bytes)
         return cudaErrorInvalidValue;                                                         \
     }
 #define OSG_PUSH_TILED_LAUNCH(D, O, P)                                                        \
-    if (dim == D && order == O) {                                                             \
-        k_push_tiled<D, O, P><<<ntiles, threads, smem, st>>>(a);                              \
-        return OSG_OK;                                                                        \
-    }
+    if (dim == D && order == O) return launch_push_tiled<D, O, P>(a, ntiles, threads, smem, st);
 #define OSG_PUSH_TILED_ATTR(D, O, P)                                                          \
-    if (dim == D && order == O) return set_smem_room(k_push_tiled<D, O, P>, bytes);
+    if (dim == D && order == O) return attr_push_tiled<D, O, P>(bytes);
 #define OSG_PUSH_BATCH_ATTR(D, O, P)                                                          \
     if (dim == D && order == O) return set_smem_room(k_push_tiled_batch<D, O, P>, bytes);
 #define OSG_PUSH_BATCH_LAUNCH(D, O, P)                                                        \

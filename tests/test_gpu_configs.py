@@ -7,7 +7,10 @@ CPU path restated), from the same seeded OSIRIS particle load, after 1 and 10 fu
   uth 0.01, 1e-3 density perturbation, quadratic, seed 2 (16,777,216 particles):
   - the mixed-precision tiled engine (FP32): particles within 1e-5 after 1 step and 5e-5
     after 10, fields as below,
-  - the plain FP64 engine within 1e-12.
+  - the plain FP64 engine within 1e-12;
+* Weibel, 128 x 128 x 128 cells, two species of 2 x 2 x 2 particles per cell counter-streaming
+  at +-0.5 c along z, uth 0.05, cubic, dx 0.1, dt 0.05, seed 3 (33,554,432 particles): the
+  tiled engine (FP32) after 1 and 3 steps, tolerances as for the two-stream box.
 
 Tolerances are normwise (max |a - b| / max |b|) on E, B, J and on each species' positions
 (cell index + offset) and momenta, plus the relative difference of each species' kinetic
@@ -29,10 +32,12 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-THERMAL = dict(nx=[128, 128], ppc=[4, 4], dx=[0.05, 0.05], dt=0.035, seed=1,
-               species=[(0.1, 0.0)], amp=0.0)
-TWO_STREAM = dict(nx=[512, 512], ppc=[8, 4], dx=[0.05, 0.05], dt=0.035, seed=2,
-                  species=[(0.01, 0.2), (0.01, -0.2)], amp=1e-3)
+THERMAL = dict(nx=[128, 128], ppc=[4, 4], dx=[0.05, 0.05], dt=0.035, seed=1, order=2,
+               species=[(0.1, [0.0, 0.0, 0.0])], amp=0.0)
+TWO_STREAM = dict(nx=[512, 512], ppc=[8, 4], dx=[0.05, 0.05], dt=0.035, seed=2, order=2,
+                  species=[(0.01, [0.2, 0.0, 0.0]), (0.01, [-0.2, 0.0, 0.0])], amp=1e-3)
+WEIBEL = dict(nx=[128, 128, 128], ppc=[2, 2, 2], dx=[0.1, 0.1, 0.1], dt=0.05, seed=3, order=3,
+              species=[(0.05, [0.0, 0.0, 0.5]), (0.05, [0.0, 0.0, -0.5])], amp=0.0)
 
 
 @pytest.fixture(scope="module")
@@ -55,8 +60,8 @@ def _load(oracle, cfg, p):
     r = oracle.mt_new(cfg["seed"])
     out = []
     for uth, ufl in cfg["species"]:
-        ix, x, u, q = oracle.load(r, p, 2, cfg["nx"], cfg["ppc"], cfg["dx"], -1.0, [uth] * 3,
-                                  [ufl, 0.0, 0.0], cfg["amp"], 1.0)
+        ix, x, u, q = oracle.load(r, p, len(cfg["nx"]), cfg["nx"], cfg["ppc"], cfg["dx"], -1.0,
+                                  [uth] * 3, ufl, cfg["amp"], 1.0)
         out.append(dict(ix=ix, x=x, u=u, q=q, rqm=-1.0))
     return out
 
@@ -95,11 +100,11 @@ def _run(osg, oracle, cfg, prec, engine, check_steps, tol):
     # FP32: the FP64 oracle beside the FP32 one, for the fields (see the module docstring)
     sp64 = _load(oracle, cfg, "f64") if prec == 32 else None
     eng = osg.ENGINE_TILED if engine == "tiled" else osg.ENGINE_PLAIN
-    sim = osg.Simulation(cfg["nx"], cfg["dx"], cfg["dt"], order=2, precision=prec, engine=eng,
-                         n_sort=0, capacity=4.0 if engine == "tiled" else 0.0)
+    sim = osg.Simulation(cfg["nx"], cfg["dx"], cfg["dt"], order=cfg["order"], precision=prec,
+                         engine=eng, n_sort=0, capacity=4.0 if engine == "tiled" else 0.0)
     for s in sp:
         sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
-    g = oracle.Grid(cfg["nx"], 2, cfg["dx"])
+    g = oracle.Grid(cfg["nx"], cfg["order"], cfg["dx"])
     eo, bo, jo = g.zeros(p), g.zeros(p), g.zeros(p)
     e64, b64, j64 = g.zeros("f64"), g.zeros("f64"), g.zeros("f64")
     nthr = oracle.max_threads()
@@ -157,3 +162,7 @@ def test_two_stream_512_fp64_plain_matches_oracle(osg, oracle):
 
 def test_two_stream_512_fp32_tiled_matches_oracle(osg, oracle):
     _run(osg, oracle, TWO_STREAM, 32, "tiled", (1, 10), {1: 1e-5, 10: 5e-5})
+
+
+def test_weibel_128_fp32_tiled_matches_oracle(osg, oracle):
+    _run(osg, oracle, WEIBEL, 32, "tiled", (1, 3), {1: 1e-5, 3: 5e-5})
