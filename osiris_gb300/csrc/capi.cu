@@ -46,21 +46,33 @@ void set_error(const char *fmt, ...)
 
 // per-thread device staging for the host-array entry points
 static const int SIDE_STREAMS = 3;
-static const int PUSH_CHUNKS = 16;
+static const int MAX_PUSH_CHUNKS = 64;
+
+// chunks of the staged host-array push (above 2 M particles): OSG_DROPIN_CHUNKS, default 16
+static int push_chunks()
+{
+    static int n = 0;
+    if (n == 0) {
+        const char *ev = getenv("OSG_DROPIN_CHUNKS");
+        const int v = ev ? atoi(ev) : 16;
+        n = v < 1 ? 1 : (v > MAX_PUSH_CHUNKS ? MAX_PUSH_CHUNKS : v);
+    }
+    return n;
+}
 
 struct Staging {
     cudaStream_t stream = nullptr;
     // the chunked host-array push: copies in, pushes and copies out each on their own stream
     // (side[0..2]), chunk by chunk, joined by per-chunk events
     cudaStream_t side[SIDE_STREAMS] = {nullptr, nullptr, nullptr};
-    cudaEvent_t ev[2 + 2 * PUSH_CHUNKS] = {nullptr};
+    cudaEvent_t ev[2 + 2 * MAX_PUSH_CHUNKS] = {nullptr};
     void *buf[8] = {nullptr};
     size_t cap[8] = {0};
     ~Staging()
     {
         for (int i = 0; i < 8; i++)
             if (buf[i]) cudaFree(buf[i]);
-        for (int i = 0; i < 2 + 2 * PUSH_CHUNKS; i++)
+        for (int i = 0; i < 2 + 2 * MAX_PUSH_CHUNKS; i++)
             if (ev[i]) cudaEventDestroy(ev[i]);
         for (int i = 0; i < SIDE_STREAMS; i++)
             if (side[i]) cudaStreamDestroy(side[i]);
@@ -71,7 +83,7 @@ struct Staging {
         if (!stream) OSG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         for (int i = 0; i < SIDE_STREAMS; i++)
             if (!side[i]) OSG_CUDA(cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking));
-        for (int i = 0; i < 2 + 2 * PUSH_CHUNKS; i++)
+        for (int i = 0; i < 2 + 2 * MAX_PUSH_CHUNKS; i++)
             if (!ev[i]) OSG_CUDA(cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming));
         return OSG_OK;
     }
@@ -216,7 +228,7 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
         // chunk k + 1, the push of chunk k and the copies out of chunk k - 1 run at once, and
         // neither copy direction waits for the other (per-particle results do not depend on the
         // chunking; the current and energy sums are atomic either way).
-        const long nck = np > (2L << 20) ? PUSH_CHUNKS : 1;
+        const long nck = np > (2L << 20) ? push_chunks() : 1;
         const long chunk = (np + nck - 1) / nck;
         for (long c0 = 0, k = 0; c0 < np; c0 += chunk, k++) {
             const long n = std::min(chunk, np - c0), h = o + c0;
