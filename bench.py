@@ -20,6 +20,11 @@ JSON line keys beyond the base contract:
                 field energies between the mixed-precision (tiled FP32) and the plain FP64
                 engine after the same number of steps from the same load
   run_to_run    normwise difference of E, B, J between two identical runs of the tiled engine
+  other_configs the other benchmark configurations (thermal 128^2 FP64, Weibel 128^3, 64
+                batched boxes, laser wakefield with the moving window), each timed on this
+                GPU with CUDA events (ms per step, particle-steps/s) with its push kernel's
+                algorithmic bytes / CUDA-event time against the measured HBM peak
+                (--no-other-configs skips them)
 --impl reference times the CPU oracle port (the reference's CPU path restated; the
 reference's own AVX2 kernels do not build on this Arm host) with all host threads.
 """
@@ -269,6 +274,7 @@ def run_native(args):
     from oracle import pyoracle as po
     nthr = po.max_threads()
     cpu_v, cpu_sample, _ = cpu_oracle_rate(15.0, nthr)
+    others = None if args.no_other_configs or world > 1 else other_configs(osg, peak)
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
@@ -294,6 +300,7 @@ def run_native(args):
                        "ratio_mixed_over_fp64": value / world / v64},
         "fp64_error": fp64_error,
         "run_to_run": spread,
+        "other_configs": others,
         "gpu_launches": launches,
         "tile_occupancy_max": occupancy,
         "clocks": clk.summary(),
@@ -302,6 +309,55 @@ def run_native(args):
     print(json.dumps(line), flush=True)
     if dist:
         dist[1].destroy_process_group()
+
+
+# algorithmic push bytes: per particle (read + write) and per cell (E, B gathered, J)
+PUSH_BYTES = {("tiled", 2): (60, 36), ("tiled", 3): (76, 36), ("plain64", 2): (104, 72)}
+
+
+def other_configs(osg, peak):
+    """The other benchmark configurations, timed on this GPU: ms per step and particle-steps/s
+    over a few graph steps after a warm-up, the push phase's device time (osg_sim_profile) and
+    its algorithmic bytes per launch against the measured HBM peak."""
+    from osiris_gb300 import run as orun
+    out = {}
+
+    def push_roof(kind, dim, npart, ncell, push_ms):
+        bp, bc = PUSH_BYTES[(kind, dim)]
+        ach = (npart * bp + ncell * bc) / (push_ms * 1e-3) / 1e9
+        return {"push_ms": push_ms, "achieved_gbs": ach, "frac": ach / peak}
+
+    for name, steps, warm in (("thermal", 50, 5), ("weibel", 20, 3)):
+        cfg = orun.CONFIGS[name]
+        sim, npart = orun.build_sim(cfg)
+        sim.step(warm)
+        ms = sim.time_steps(steps)
+        prof = sim.profile(3)
+        ncell = int(np.prod(cfg["nx"]))
+        kind = "plain64" if cfg["precision"] == 64 else "tiled"
+        out[name] = {"cells": cfg["nx"], "particles": npart, "steps": steps,
+                     "ms_per_step": ms / steps, "particle_steps_per_s": npart * steps / (ms / 1e3),
+                     "engine": cfg["engine"], "precision": cfg["precision"],
+                     **push_roof(kind, len(cfg["nx"]), npart, ncell, prof["push"])}
+        sim.close()
+    bt, npart = orun.build_batch()
+    tile, threads = bt.tuning()
+    bt.step(3)
+    ms = bt.time_steps(20)
+    out["batch"] = {"boxes": 64, "particles": npart, "steps": 20, "ms_per_step": ms / 20,
+                    "particle_steps_per_s": npart * 20 / (ms / 1e3), "tile": tile,
+                    "threads": threads}
+    bt.close()
+    sim, n0 = orun.build_lwfa()
+    sim.step(3)
+    ms = sim.time_steps(25)
+    n1 = sim.num_particles(0)
+    out["lwfa"] = {"cells": orun.LWFA["nx"], "particles_start": n0, "particles_end": n1,
+                   "steps": 25, "ms_per_step": ms / 25,
+                   "particle_steps_per_s": n1 * 25 / (ms / 1e3),
+                   "window_moves": sim.window_moves(), "note": "the first steps of the run"}
+    sim.close()
+    return out
 
 
 def run_reference(args):
@@ -334,6 +390,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="skip the timing of the other benchmark configurations")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

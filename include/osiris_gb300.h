@@ -350,8 +350,10 @@ int osg_sim_num_particles(osg_sim *s, int species, long *np);
 /* Copy one species back to host arrays (tile order for the TILED engine). */
 int osg_sim_get_species(osg_sim *s, int species, int *ix, void *x, void *u, void *q);
 /* Advance n full time steps (captured once as a CUDA graph per step shape and replayed).
- * TILED: afterwards, if any tile slab is more than 70% full, all species are re-binned into
- * larger slabs (a host round trip) so the following steps cannot overflow. */
+ * TILED: after every 8 steps, if any tile slab is more than 70% full, all species are re-binned
+ * into larger slabs (a host round trip) so the following steps cannot overflow.
+ * osg_sim_step_async makes no such check: a caller that times long runs with it checks
+ * osg_sim_tile_occupancy between groups of steps. */
 int osg_sim_step(osg_sim *s, int nsteps);
 /* TILED: largest fraction of used particle slots over all tiles and species (0 for PLAIN). */
 int osg_sim_tile_occupancy(osg_sim *s, double *max_frac);

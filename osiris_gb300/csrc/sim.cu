@@ -407,6 +407,9 @@ static int get_graph(osg_sim *s, int parity, int sort, cudaGraphExec_t *out)
     return OSG_OK;
 }
 
+// osg_sim_step checks the tiled engine's slab occupancy after every this many steps
+static const int OCC_CHECK_STEPS = 8;
+
 static bool sort_due(const osg_sim *s, long n)
 {
     return s->cfg.engine == OSG_ENGINE_PLAIN && s->cfg.n_sort > 0 && n > 0 &&
@@ -772,20 +775,27 @@ int osg_sim_sync(osg_sim *s)
 
 int osg_sim_step(osg_sim *s, int nsteps)
 {
-    int rc = osg_sim_step_async(s, nsteps);
-    if (rc) return rc;
-    rc = osg_sim_sync(s);
-    if (rc) return rc;
-    if (s->cfg.engine == OSG_ENGINE_TILED) {
-        // tile slabs filling up (density bunching): re-bin with room to spare before a tile
-        // can overflow; particles move at most one cell per step
-        double m = 0.0;
-        rc = tiled_occupancy(s->tiled, s->cur, &m, s->st);
+    OSG_CHECK(s && nsteps >= 0, OSG_ERR_ARG, "bad arguments");
+    // TILED: the steps go in groups of OCC_CHECK_STEPS; after each group, tile slabs filling
+    // up (density bunching, injected plasma) are re-binned with room to spare before a tile can
+    // overflow (particles move at most one cell per step, so a tile fills a little per step)
+    const int group = s->cfg.engine == OSG_ENGINE_TILED ? OCC_CHECK_STEPS : nsteps;
+    for (int done = 0; done < nsteps;) {
+        const int n = std::min(group, nsteps - done);
+        int rc = osg_sim_step_async(s, n);
         if (rc) return rc;
-        if (m > 0.7) {
-            rc = tiled_regrow(s->tiled, s->cur, s->st);
+        rc = osg_sim_sync(s);
+        if (rc) return rc;
+        done += n;
+        if (s->cfg.engine == OSG_ENGINE_TILED) {
+            double m = 0.0;
+            rc = tiled_occupancy(s->tiled, s->cur, &m, s->st);
             if (rc) return rc;
-            s->graphs_dirty = true;
+            if (m > 0.7) {
+                rc = tiled_regrow(s->tiled, s->cur, s->st);
+                if (rc) return rc;
+                s->graphs_dirty = true;
+            }
         }
     }
     return OSG_OK;

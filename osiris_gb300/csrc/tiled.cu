@@ -78,6 +78,7 @@ struct TiledState {
     double iter_tol = 1.0e-3;
     long nj_tile = 0;    // current points (x3 components) of a tile with its halo
     float *tile_hi = nullptr, *tile_lo = nullptr;
+    int *tile_empty = nullptr;   // per tile: no particles this step (written by the push)
     // moving window along x1 (open x1 boundary, injection into the new cells)
     bool window = false;
     int inj_species = -1;
@@ -214,6 +215,7 @@ static TiledArgs base_args(const TiledState *t)
     a.iter_tol = t->iter_tol;
     a.tile_hi = t->tile_hi;
     a.tile_lo = t->tile_lo;
+    a.tile_empty = t->tile_empty;
     a.discard = t->l2_discard;
     a.walls = t->walls;
     a.thermal = t->thermal;
@@ -348,7 +350,8 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
     t->nj_tile = 3;
     for (int d = 0; d < t->dim; d++) t->nj_tile *= t->T[d] + t->order + 2;
     const size_t tb = sizeof(float) * (size_t)t->nj_tile * t->ntiles;
-    if (cudaMalloc(&t->tile_hi, tb) != cudaSuccess || cudaMalloc(&t->tile_lo, tb) != cudaSuccess) {
+    if (cudaMalloc(&t->tile_hi, tb) != cudaSuccess || cudaMalloc(&t->tile_lo, tb) != cudaSuccess ||
+        cudaMalloc(&t->tile_empty, sizeof(int) * t->ntiles) != cudaSuccess) {
         tiled_destroy(t);
         set_error("tile current allocation of %zu bytes failed", tb);
         return OSG_ERR_NOMEM;
@@ -370,6 +373,7 @@ void tiled_destroy(TiledState *t)
     cudaFree(t->d_compact);
     cudaFree(t->tile_hi);
     cudaFree(t->tile_lo);
+    cudaFree(t->tile_empty);
     cudaFree(t->d_moved);
     delete t;
 }
@@ -529,6 +533,7 @@ FoldBox tiled_fold_box(TiledState *t, float *j)
     FoldBox f;
     f.th = t->tile_hi;
     f.tl = t->tile_lo;
+    f.empty = t->tile_empty;
     f.j = j;
     f.size = make_int3(g.size[0], g.size[1], g.size[2]);
     f.T = make_int3(t->T[0], t->T[1], t->T[2]);
@@ -733,11 +738,11 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     unsigned nb = blocks_for(f.npts, 256);
     if (nb > 152 * 16) nb = 152 * 16;
     if (t->dim == 2)
-        k_tile_fold<2><<<nb, 256, 0, st>>>(f.th, f.tl, j, f.size, f.T, f.ntile, f.je, f.gcl,
-                                            f.ofs, f.npts, f.fx_inv, f.fx_shift);
+        k_tile_fold<2><<<nb, 256, 0, st>>>(f.th, f.tl, f.empty, j, f.size, f.T, f.ntile, f.je,
+                                            f.gcl, f.ofs, f.npts, f.fx_inv, f.fx_shift);
     else
-        k_tile_fold<3><<<nb, 256, 0, st>>>(f.th, f.tl, j, f.size, f.T, f.ntile, f.je, f.gcl,
-                                            f.ofs, f.npts, f.fx_inv, f.fx_shift);
+        k_tile_fold<3><<<nb, 256, 0, st>>>(f.th, f.tl, f.empty, j, f.size, f.T, f.ntile, f.je,
+                                            f.gcl, f.ofs, f.npts, f.fx_inv, f.fx_shift);
     *launches += 2;
     return OSG_OK;
 }
@@ -859,6 +864,11 @@ int tiled_regrow(TiledState *t, int cur, cudaStream_t st)
         if (rc) return rc;
     }
     std::vector<double> rqm = t->rqm;
+    // the new slabs hold 1.5x the old ones at least: re-binning from the current counts alone
+    // (1.25x the fullest tile) would leave a tile that triggered it 80% full
+    if ((int)t->min_cap.size() < ns) t->min_cap.resize(ns, 0);
+    for (int k = 0; k < ns && k < (int)t->cap.size(); k++)
+        t->min_cap[k] = std::max(t->min_cap[k], (long)std::ceil(1.5 * (double)t->cap[k]));
     for (void *p : t->allocs) cudaFree(p);
     t->allocs.clear();
     t->buf[0].clear();

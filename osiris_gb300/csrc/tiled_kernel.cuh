@@ -129,6 +129,9 @@ struct TiledArgs {
     // summed in FP64 in tile order by k_tile_fold
     float *tile_hi;
     float *tile_lo;
+    // per tile: 1 when it held no particle of any species this step (its current buffer is
+    // then not written, and the fold skips it), else 0
+    int *tile_empty;
     // 3D: the tile current is accumulated as fixed point, value x 2^S split into a low word
     // of B bits and a high word (fx.scale = 2^S, fx.shift = B; chosen so that no tile point,
     // nor the fold's sum of tiles, can overflow)
@@ -322,6 +325,26 @@ __device__ __forceinline__ void push_tile(const TiledArgs &a, const long tile)
     constexpr int NP = ORD + 1, OFS = Stencil<ORD>::OFS;
     constexpr int MAXSEG = DIM == 2 ? 3 : 4;
     extern __shared__ float smem[];
+    // a tile without particles (the vacuum of a sparse box) has nothing to push or deposit:
+    // its output counts are 0 and the fold skips its current buffer
+    {
+        __shared__ int sAny;
+        if (threadIdx.x == 0) {
+            int any = 0;
+            for (int s = 0; s < a.nspec; s++) {
+                const SpeciesDev &sd = a.spec[s];
+                any |= sd.in.cnt[tile] | sd.in.arr[tile];
+            }
+            sAny = any;
+            a.tile_empty[tile] = any ? 0 : 1;
+            if (!any)
+                for (int s = 0; s < a.nspec; s++) a.spec[s].out.cnt[tile] = 0;
+        }
+        __syncthreads();
+        const bool empty = sAny == 0;
+        __syncthreads();   // sAny is read by every thread before a next tile of the CTA
+        if (empty) return;
+    }
     int t0[3], tc[3];
     tc[0] = (int)(tile % a.ntile[0]);
     tc[1] = DIM > 1 ? (int)((tile / a.ntile[0]) % a.ntile[1]) : 0;
@@ -919,6 +942,7 @@ k_push_tiled_batch(const TiledArgs *__restrict__ boxes, const int2 *__restrict__
 // [tc * T - OFS + gcl, tc * T - OFS + gcl + je) along each axis (je = T + ORD + 2 points).
 struct FoldBox {
     const float *th, *tl;   // tile currents (2D: value and compensation; 3D: fixed-point words)
+    const int *empty;       // per tile: 1 = no particles this step, buffer not written
     float fx_inv;           // 3D: 1 / the fixed-point scale
     int fx_shift;           // 3D: bits of the low word
     float *j;               // global current
@@ -930,6 +954,7 @@ struct FoldBox {
 template <int DIM>
 __device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
                                                const float *__restrict__ tl,
+                                               const int *__restrict__ empty,
                                                float *__restrict__ j, int3 size, int3 T,
                                                int3 ntile, int3 je, int3 gcl, int ofs, long npts,
                                                float fx_inv, int fx_shift)
@@ -964,6 +989,7 @@ __device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
             for (int ty = lo[1]; ty <= hi[1]; ty++)
                 for (int tx = lo[0]; tx <= hi[0]; tx++) {
                     const long tile = tx + (long)nt[0] * (ty + (long)nt[1] * tz);
+                    if (__ldg(empty + tile)) continue;
                     const int lx = gx - (tx * Ta[0] - ofs + gl[0]);
                     const int ly = DIM > 1 ? gy - (ty * Ta[1] - ofs + gl[1]) : 0;
                     const int lz = DIM > 2 ? gz - (tz * Ta[2] - ofs + gl[2]) : 0;
@@ -985,10 +1011,12 @@ __device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
 
 template <int DIM>
 __global__ void k_tile_fold(const float *__restrict__ th, const float *__restrict__ tl,
-                            float *__restrict__ j, int3 size, int3 T, int3 ntile, int3 je,
-                            int3 gcl, int ofs, long npts, float fx_inv, int fx_shift)
+                            const int *__restrict__ empty, float *__restrict__ j, int3 size,
+                            int3 T, int3 ntile, int3 je, int3 gcl, int ofs, long npts,
+                            float fx_inv, int fx_shift)
 {
-    tile_fold_body<DIM>(th, tl, j, size, T, ntile, je, gcl, ofs, npts, fx_inv, fx_shift);
+    tile_fold_body<DIM>(th, tl, empty, j, size, T, ntile, je, gcl, ofs, npts, fx_inv,
+                        fx_shift);
 }
 
 // the same for every box of a batch (box = blockIdx.y)
@@ -996,8 +1024,8 @@ template <int DIM>
 __global__ void k_batch_fold(const FoldBox *__restrict__ boxes)
 {
     const FoldBox &f = boxes[blockIdx.y];
-    tile_fold_body<DIM>(f.th, f.tl, f.j, f.size, f.T, f.ntile, f.je, f.gcl, f.ofs, f.npts,
-                        f.fx_inv, f.fx_shift);
+    tile_fold_body<DIM>(f.th, f.tl, f.empty, f.j, f.size, f.T, f.ntile, f.je, f.gcl, f.ofs,
+                        f.npts, f.fx_inv, f.fx_shift);
 }
 
 // zero n ints at p for every range of a device table (one launch; defined in tiled.cu)

@@ -256,7 +256,8 @@ def main():
                               particles_end=n1, steps=args.steps, ms_per_step=ms / args.steps,
                               particle_steps_per_s=n1 * args.steps / (ms / 1e3),
                               window_moves=sim.window_moves(), load_s=t_load,
-                              kinetic=[float(v) for v in kin], field=[float(v) for v in fld])))
+                              kinetic=[float(v) for v in kin], field=[float(v) for v in fld],
+                              phase_ms=sim.profile(5))))
         sim.close()
         return
     cfg = CONFIGS[args.config]
