@@ -735,14 +735,14 @@ int tiled_push(TiledState *t, int parity, const float *e, const float *b, float 
     if (rc) return rc;
     // deterministic re-summation of the tile currents into the global current
     const FoldBox f = tiled_fold_box(t, j);
-    unsigned nb = blocks_for(f.npts, 256);
-    if (nb > 152 * 16) nb = 152 * 16;
+    const dim3 grid((unsigned)((3 * f.size.x + 255) / 256), (unsigned)f.size.y,
+                    t->dim == 3 ? (unsigned)f.size.z : 1u);
     if (t->dim == 2)
-        k_tile_fold<2><<<nb, 256, 0, st>>>(f.th, f.tl, f.empty, j, f.size, f.T, f.ntile, f.je,
-                                            f.gcl, f.ofs, f.npts, f.fx_inv, f.fx_shift);
+        k_tile_fold<2><<<grid, 256, 0, st>>>(f.th, f.tl, f.empty, j, f.size, f.T, f.ntile, f.je,
+                                             f.gcl, f.ofs, f.fx_inv, f.fx_shift);
     else
-        k_tile_fold<3><<<nb, 256, 0, st>>>(f.th, f.tl, f.empty, j, f.size, f.T, f.ntile, f.je,
-                                            f.gcl, f.ofs, f.npts, f.fx_inv, f.fx_shift);
+        k_tile_fold<3><<<grid, 256, 0, st>>>(f.th, f.tl, f.empty, j, f.size, f.T, f.ntile, f.je,
+                                             f.gcl, f.ofs, f.fx_inv, f.fx_shift);
     *launches += 2;
     return OSG_OK;
 }

@@ -951,6 +951,63 @@ struct FoldBox {
     long npts;              // 3 x grid points
 };
 
+// x / t for x >= 0, by a shift when t is a power of two (tile shapes always are in practice)
+__device__ __forceinline__ int div_tile(int x, int t)
+{
+    return (t & (t - 1)) == 0 ? x >> (__ffs(t) - 1) : x / t;
+}
+
+// the folded value of component c at grid position (gx, gy, gz)
+template <int DIM>
+__device__ __forceinline__ float tile_fold_point(const float *__restrict__ th,
+                                                 const float *__restrict__ tl,
+                                                 const int *__restrict__ empty, int gx, int gy,
+                                                 int gz, int c, int3 T, int3 ntile, int3 je,
+                                                 int3 gcl, int ofs, float fx_inv, int fx_shift)
+{
+    const int gp[3] = {gx, gy, gz};
+    const int Ta[3] = {T.x, T.y, T.z}, nt[3] = {ntile.x, ntile.y, ntile.z};
+    const int jea[3] = {je.x, je.y, je.z}, gl[3] = {gcl.x, gcl.y, gcl.z};
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        if (d < DIM) {
+            // tiles tc with 0 <= gp - (tc * T - ofs + gl) < je
+            const int r = gp[d] + ofs - gl[d];
+            int a0 = r - jea[d] + 1;
+            a0 = a0 <= 0 ? 0 : div_tile(a0 + Ta[d] - 1, Ta[d]);
+            const int a1 = r < 0 ? -1 : div_tile(r, Ta[d]);
+            lo[d] = a0;
+            hi[d] = a1 < nt[d] - 1 ? a1 : nt[d] - 1;
+        }
+    }
+    const int nj = jea[0] * (DIM > 1 ? jea[1] : 1) * (DIM > 2 ? jea[2] : 1);
+    double v = 0.0;
+    long long fx = 0;
+    for (int tz = lo[2]; tz <= hi[2]; tz++)
+        for (int ty = lo[1]; ty <= hi[1]; ty++)
+            for (int tx = lo[0]; tx <= hi[0]; tx++) {
+                const long tile = tx + (long)nt[0] * (ty + (long)nt[1] * tz);
+                if (__ldg(empty + tile)) continue;
+                const int lx = gx - (tx * Ta[0] - ofs + gl[0]);
+                const int ly = DIM > 1 ? gy - (ty * Ta[1] - ofs + gl[1]) : 0;
+                const int lz = DIM > 2 ? gz - (tz * Ta[2] - ofs + gl[2]) : 0;
+                const long o = tile * (3L * nj) + 3 * (lx + jea[0] * (ly + jea[1] * lz)) + c;
+                if constexpr (DIM == 3) {
+                    // hi 2^B + (the low B bits of every add, summed: lo - hi 2^B mod 2^32)
+                    const int hw = __float_as_int(tl[o]);
+                    const unsigned lw = __float_as_uint(th[o]) - ((unsigned)hw << fx_shift);
+                    fx += (long long)hw * (1LL << fx_shift) + (long long)lw;
+                } else {
+                    v += (double)th[o];
+                    if (tl) v += (double)tl[o];
+                }
+            }
+    if constexpr (DIM == 3) return __ll2float_rn(fx) * fx_inv;
+    else return (float)v;
+}
+
+// every point of a flat grid loop (the batch: small boxes, one launch for all)
 template <int DIM>
 __device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
                                                const float *__restrict__ tl,
@@ -966,57 +1023,27 @@ __device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
         const int gx = (int)(p % size.x);
         const int gy = DIM > 1 ? (int)((p / size.x) % size.y) : 0;
         const int gz = DIM > 2 ? (int)(p / ((long)size.x * size.y)) : 0;
-        const int gp[3] = {gx, gy, gz};
-        const int Ta[3] = {T.x, T.y, T.z}, nt[3] = {ntile.x, ntile.y, ntile.z};
-        const int jea[3] = {je.x, je.y, je.z}, gl[3] = {gcl.x, gcl.y, gcl.z};
-        int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            if (d < DIM) {
-                // tiles tc with 0 <= gp - (tc * T - ofs + gl) < je
-                const int r = gp[d] + ofs - gl[d];
-                int a0 = r - jea[d] + 1;
-                a0 = a0 <= 0 ? 0 : (a0 + Ta[d] - 1) / Ta[d];
-                int a1 = r < 0 ? -1 : r / Ta[d];
-                lo[d] = a0;
-                hi[d] = a1 < nt[d] - 1 ? a1 : nt[d] - 1;
-            }
-        }
-        const int nj = jea[0] * (DIM > 1 ? jea[1] : 1) * (DIM > 2 ? jea[2] : 1);
-        double v = 0.0;
-        long long fx = 0;
-        for (int tz = lo[2]; tz <= hi[2]; tz++)
-            for (int ty = lo[1]; ty <= hi[1]; ty++)
-                for (int tx = lo[0]; tx <= hi[0]; tx++) {
-                    const long tile = tx + (long)nt[0] * (ty + (long)nt[1] * tz);
-                    if (__ldg(empty + tile)) continue;
-                    const int lx = gx - (tx * Ta[0] - ofs + gl[0]);
-                    const int ly = DIM > 1 ? gy - (ty * Ta[1] - ofs + gl[1]) : 0;
-                    const int lz = DIM > 2 ? gz - (tz * Ta[2] - ofs + gl[2]) : 0;
-                    const long o = tile * (3L * nj) + 3L * (lx + jea[0] * (ly + (long)jea[1] * lz)) + c;
-                    if constexpr (DIM == 3) {
-                        // hi 2^B + (the low B bits of every add, summed: lo - hi 2^B mod 2^32)
-                        const int hw = __float_as_int(tl[o]);
-                        const unsigned lw = __float_as_uint(th[o]) - ((unsigned)hw << fx_shift);
-                        fx += (long long)hw * (1LL << fx_shift) + (long long)lw;
-                    } else {
-                        v += (double)th[o];
-                        if (tl) v += (double)tl[o];
-                    }
-                }
-        if constexpr (DIM == 3) j[g] = __ll2float_rn(fx) * fx_inv;
-        else j[g] = (float)v;
+        j[g] = tile_fold_point<DIM>(th, tl, empty, gx, gy, gz, c, T, ntile, je, gcl, ofs,
+                                    fx_inv, fx_shift);
     }
 }
 
+// single box: one grid row (3 components x size.x points) per (blockIdx.y, blockIdx.z) = (y, z),
+// so no thread divides a 64-bit grid index
 template <int DIM>
 __global__ void k_tile_fold(const float *__restrict__ th, const float *__restrict__ tl,
                             const int *__restrict__ empty, float *__restrict__ j, int3 size,
-                            int3 T, int3 ntile, int3 je, int3 gcl, int ofs, long npts,
-                            float fx_inv, int fx_shift)
+                            int3 T, int3 ntile, int3 je, int3 gcl, int ofs, float fx_inv,
+                            int fx_shift)
 {
-    tile_fold_body<DIM>(th, tl, empty, j, size, T, ntile, je, gcl, ofs, npts, fx_inv,
-                        fx_shift);
+    const int gy = DIM > 1 ? (int)blockIdx.y : 0, gz = DIM > 2 ? (int)blockIdx.z : 0;
+    const int row = 3 * size.x;
+    float *jr = j + ((long)gz * size.y + gy) * row;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < row; i += gridDim.x * blockDim.x) {
+        const int gx = i / 3;
+        jr[i] = tile_fold_point<DIM>(th, tl, empty, gx, gy, gz, i - 3 * gx, T, ntile, je, gcl,
+                                     ofs, fx_inv, fx_shift);
+    }
 }
 
 // the same for every box of a batch (box = blockIdx.y)
