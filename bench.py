@@ -23,8 +23,8 @@ JSON line keys beyond the base contract:
   other_configs the other benchmark configurations (thermal 128^2 FP64, Weibel 128^3, 64
                 batched boxes, laser wakefield with the moving window), each timed on this
                 GPU with CUDA events (ms per step, particle-steps/s) with its push kernel's
-                algorithmic bytes / CUDA-event time against the measured HBM peak
-                (--no-other-configs skips them)
+                algorithmic bytes / CUDA-event time against the measured HBM peak, and the
+                single-box autotuner's choice for this workload (--no-other-configs skips them)
 --impl reference times the CPU oracle port (the reference's CPU path restated; the
 reference's own AVX2 kernels do not build on this Arm host) with all host threads.
 """
@@ -340,6 +340,11 @@ def other_configs(osg, peak):
                      "engine": cfg["engine"], "precision": cfg["precision"],
                      **push_roof(kind, len(cfg["nx"]), npart, ncell, prof["push"])}
         sim.close()
+    # the single-box autotuner on the benchmark workload itself (its choice; the timed run
+    # above uses the default 8x8 tiles and 256 threads)
+    sim, npart = orun.build_sim(orun.CONFIGS["two_stream"])
+    out["autotune_two_stream"] = sim.autotune(steps=4)
+    sim.close()
     bt, npart = orun.build_batch()
     tile, threads = bt.tuning()
     bt.step(3)
