@@ -166,3 +166,22 @@ def test_two_stream_512_fp32_tiled_matches_oracle(osg, oracle):
 
 def test_weibel_128_fp32_tiled_matches_oracle(osg, oracle):
     _run(osg, oracle, WEIBEL, 32, "tiled", (1, 3), {1: 1e-5, 3: 5e-5})
+
+
+@pytest.mark.parametrize("cfg,steps", [(TWO_STREAM, 40), (WEIBEL, 10)])
+def test_charge_conservation_at_config_size(osg, oracle, cfg, steps):
+    """Size-independent property at the configurations' own sizes: div E - rho is conserved by
+    the charge-conserving deposit, so its maximum over the grid stays at its value after the
+    load (E = 0 there, so it is max |rho|) -- FP32 tiled engine, to 2e-4 of that value."""
+    sp = _load(oracle, cfg, "f32")
+    sim = osg.Simulation(cfg["nx"], cfg["dx"], cfg["dt"], order=cfg["order"], precision=32,
+                         engine=osg.ENGINE_TILED, capacity=4.0)
+    for s in sp:
+        sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
+    r0, _ = sim.gauss_residual()
+    hist = []
+    for _ in range(4):
+        sim.step(steps // 4)
+        hist.append(sim.gauss_residual()[0])
+    sim.close()
+    assert max(abs(h - r0) for h in hist) <= 2e-4 * r0, (r0, hist)
