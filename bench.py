@@ -172,6 +172,45 @@ def cpu_oracle_rate(target_s, nthreads, steps=None):
     return npart * nstep / el, f"{n}x{n} cells ({npart} particles), {nstep} full steps", el
 
 
+def cpu_config_rate(cfg, prec, nthreads, target_s, steps=2):
+    """CPU oracle (port) particle-steps/s of another configuration (its density, parameters
+    and phases) on a cubic sub-box no larger than the configuration's, sized so the timed part
+    takes about target_s seconds.  Returns (rate, sample description)."""
+    from oracle import pyoracle as po
+    po.build(with_ref=False)
+    dim = len(cfg["nx"])
+    p = "f32" if prec == 32 else "f64"
+
+    def setup(n):
+        nx = [min(n, m) for m in cfg["nx"]]
+        r = po.mt_new(cfg["seed"])
+        sp = []
+        for s in cfg["species"]:
+            ix, x, u, q = po.load(r, p, dim, nx, cfg["ppc"], cfg["dx"], -1.0, [s["uth"]] * 3,
+                                  s["ufl"], cfg["amp"], 1.0)
+            sp.append(dict(ix=ix, x=x, u=u, q=q, rqm=-1.0))
+        g = po.Grid(nx, cfg["order"], cfg["dx"])
+        return nx, g, sp, g.zeros(p), g.zeros(p), g.zeros(p)
+
+    n0 = 16 if dim == 3 else 64
+    nx, g, sp, e, b, j = setup(n0)
+    npart = sum(len(s["q"]) for s in sp)
+    t = time.perf_counter()
+    po.step(g, p, e, b, j, sp, cfg["dt"], nthreads=nthreads, fast=True)
+    per = (time.perf_counter() - t) / npart
+    n = int((target_s / steps / per / (npart / n0 ** dim)) ** (1.0 / dim))
+    n = max(n0, n // 8 * 8)
+    nx, g, sp, e, b, j = setup(n)
+    npart = sum(len(s["q"]) for s in sp)
+    po.step(g, p, e, b, j, sp, cfg["dt"], nthreads=nthreads, fast=True)
+    t = time.perf_counter()
+    for _ in range(steps):
+        po.step(g, p, e, b, j, sp, cfg["dt"], nthreads=nthreads, fast=True)
+    el = time.perf_counter() - t
+    cells = "x".join(str(v) for v in nx)
+    return npart * steps / el, f"{cells} cells ({npart} particles), {steps} full steps"
+
+
 def e2e_host(osg, sp_host, steps):
     """Drop-in flow on host buffers (osiris_gb300.run.dropin_steps), all copies timed."""
     from osiris_gb300.run import dropin_steps
@@ -275,6 +314,17 @@ def run_native(args):
     nthr = po.max_threads()
     cpu_v, cpu_sample, _ = cpu_oracle_rate(15.0, nthr)
     others = None if args.no_other_configs or world > 1 else other_configs(osg, peak)
+    if others is not None:
+        # the CPU baselines the other configurations are reported with: configuration 1 (FP64)
+        # on one thread and on all, configuration 3 (FP32) on all
+        from osiris_gb300 import run as orun
+        cb = {}
+        for key, name, prec, thr in (("thermal_1_thread", "thermal", 64, 1),
+                                     ("thermal_all_threads", "thermal", 64, nthr),
+                                     ("weibel_all_threads", "weibel", 32, nthr)):
+            v, smp = cpu_config_rate(orun.CONFIGS[name], prec, thr, 6.0)
+            cb[key] = {"value": v, "unit": METRIC, "cores": thr, "kind": "port", "sample": smp}
+        others["cpu_baseline"] = cb
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
