@@ -494,8 +494,9 @@ __device__ __forceinline__ void segq_drain(float *sJ, SegRec *sq, int &qn, int n
 // cannot overflow and N 2^B <= 2^32.  The sum of the low B bits of every v, sum - hi 2^B, then
 // lies in [0, 2^32) and equals lo - hi 2^B modulo 2^32: the point's value is
 // hi 2^B + (unsigned)(lo - hi 2^B) (k_tile_fold).  The tile sums therefore carry no rounding
-// beyond the one of each added value and do not depend on the order of the adds.  Every lane
-// adds the values of its own segment (lanes_deposit3); the face crossings wait in a per-warp queue so that they are deposited by
+// beyond the one of each added value (to a multiple of 2^-S, an absolute quantum) and do not
+// depend on the order of the adds.  Every lane adds the values of its own segment
+// (lanes_deposit3); the face crossings wait in a per-warp queue so that they are deposited by
 // full warps.
 // ------------------------------------------------------------------------------------------
 constexpr int SEGQ3 = 48;        // queued face crossings per warp

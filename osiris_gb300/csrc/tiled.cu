@@ -171,8 +171,10 @@ static cudaError_t push_attr(int pusher, int dim, int order, int bytes)
 // word sums N values of magnitude <= V 2^-B + 1 and must stay below 2^31 - 1:
 // V <= 2^B (2^31 / N - 2).  B is the largest with N 2^B <= 2^32, S the largest with V within
 // both that bound and 2^31 (one value fits a signed 32-bit integer).  For N below 2^17 (slabs
-// of up to 32768 slots in all) 2^S >= 2^28 / (6 qmax jn): each add rounds by at most 2^-28 of
-// the largest value, far below the FP32 rounding of a float sum.
+// of up to 32768 slots in all) 2^S >= 2^28 / (6 qmax jn): each add rounds by at most 2^-29 of
+// the largest value a segment can carry, far below the FP32 rounding of a float sum of
+// currents of that order.  The quantum is absolute: currents many orders of magnitude below
+// qmax jn (a cold plasma at rest) are resolved more coarsely than FP32 would.
 static FxFormat fx_format(const TiledState *t)
 {
     double jn = 0.0;
