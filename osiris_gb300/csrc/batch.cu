@@ -87,6 +87,7 @@ struct osg_batch {
     unsigned grid = 0;
     size_t smem = 0;
     long max_side = 0, max_points = 0, max_cnt = 0;
+    int max_row = 0, max_rows = 0;   // the fold's grid: 3 x size[0] values per row, rows
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int launches = 0;
 };
@@ -139,6 +140,7 @@ static int upload_tables(osg_batch *b)
         zero[p].resize(nb);
     }
     b->max_side = b->max_points = b->max_cnt = 0;
+    b->max_row = b->max_rows = 0;
     for (int i = 0; i < nb; i++) {
         BatchBox &bx = b->box[i];
         for (int p = 0; p < 2; p++) {
@@ -149,6 +151,8 @@ static int upload_tables(osg_batch *b)
         fb[i] = make_field_box(bx.g, bx.e, bx.b, bx.j, bx.dx, b->cfg.dt);
         fold[i] = tiled_fold_box(bx.t, bx.j);
         b->max_points = std::max(b->max_points, bx.g.npoints());
+        b->max_row = std::max(b->max_row, 3 * bx.g.size[0]);
+        b->max_rows = std::max(b->max_rows, bx.g.size[1] * (bx.g.dim > 2 ? bx.g.size[2] : 1));
         b->max_cnt = std::max(b->max_cnt, zero[0][i].n);
         for (int d = 0; d < bx.g.dim; d++) {
             long other = 1;
@@ -180,7 +184,7 @@ static int enqueue_step(osg_batch *b, int parity, cudaStream_t st, int *launches
     int rc = push_batch_launch(dim, b->cfg.order, b->d_args[parity], b->d_work, b->nwork,
                                b->d_counter, b->grid, b->threads, b->smem, st);
     if (rc) return rc;
-    batch_fold(b->d_fold, nb, dim, 3 * b->max_points, st);
+    batch_fold(b->d_fold, nb, dim, b->max_row, b->max_rows, st);
     batch_periodic(b->d_fb, nb, dim, 2, 1, b->max_side, st);
     batch_yee(b->d_fb, nb, dim, b->max_points, st);
     n += 2 + dim + 3;

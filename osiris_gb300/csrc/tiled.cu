@@ -579,9 +579,10 @@ void zero_ranges(const IntRange *d_ranges, int nrange, long max_n, cudaStream_t 
     k_zero_ranges<<<dim3(grid_x(max_n), (unsigned)nrange), 256, 0, st>>>(d_ranges);
 }
 
-void batch_fold(const FoldBox *d_boxes, int nbox, int dim, long max_points, cudaStream_t st)
+void batch_fold(const FoldBox *d_boxes, int nbox, int dim, int max_row, int max_rows,
+                cudaStream_t st)
 {
-    const dim3 grid(grid_x(max_points), (unsigned)nbox);
+    const dim3 grid((unsigned)((max_row + 255) / 256), (unsigned)max_rows, (unsigned)nbox);
     if (dim == 2) k_batch_fold<2><<<grid, 256, 0, st>>>(d_boxes);
     else k_batch_fold<3><<<grid, 256, 0, st>>>(d_boxes);
 }

@@ -1007,27 +1007,6 @@ __device__ __forceinline__ float tile_fold_point(const float *__restrict__ th,
     else return (float)v;
 }
 
-// every point of a flat grid loop (the batch: small boxes, one launch for all)
-template <int DIM>
-__device__ __forceinline__ void tile_fold_body(const float *__restrict__ th,
-                                               const float *__restrict__ tl,
-                                               const int *__restrict__ empty,
-                                               float *__restrict__ j, int3 size, int3 T,
-                                               int3 ntile, int3 je, int3 gcl, int ofs, long npts,
-                                               float fx_inv, int fx_shift)
-{
-    OSG_GRID_LOOP(g, npts)
-    {
-        const int c = (int)(g % 3);
-        const long p = g / 3;
-        const int gx = (int)(p % size.x);
-        const int gy = DIM > 1 ? (int)((p / size.x) % size.y) : 0;
-        const int gz = DIM > 2 ? (int)(p / ((long)size.x * size.y)) : 0;
-        j[g] = tile_fold_point<DIM>(th, tl, empty, gx, gy, gz, c, T, ntile, je, gcl, ofs,
-                                    fx_inv, fx_shift);
-    }
-}
-
 // single box: one grid row (3 components x size.x points) per (blockIdx.y, blockIdx.z) = (y, z),
 // so no thread divides a 64-bit grid index
 template <int DIM>
@@ -1046,13 +1025,23 @@ __global__ void k_tile_fold(const float *__restrict__ th, const float *__restric
     }
 }
 
-// the same for every box of a batch (box = blockIdx.y)
+// the same for every box of a batch: box = blockIdx.z, grid row (y, z) = blockIdx.y (rows
+// past the box's last one exit at once)
 template <int DIM>
 __global__ void k_batch_fold(const FoldBox *__restrict__ boxes)
 {
-    const FoldBox &f = boxes[blockIdx.y];
-    tile_fold_body<DIM>(f.th, f.tl, f.empty, f.j, f.size, f.T, f.ntile, f.je, f.gcl, f.ofs,
-                        f.npts, f.fx_inv, f.fx_shift);
+    const FoldBox &f = boxes[blockIdx.z];
+    const int rows = f.size.y * (DIM > 2 ? f.size.z : 1);
+    if ((int)blockIdx.y >= rows) return;
+    const int gy = DIM > 1 ? (int)blockIdx.y % f.size.y : 0;
+    const int gz = DIM > 2 ? (int)blockIdx.y / f.size.y : 0;
+    const int row = 3 * f.size.x;
+    float *jr = f.j + (long)blockIdx.y * row;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < row; i += gridDim.x * blockDim.x) {
+        const int gx = i / 3;
+        jr[i] = tile_fold_point<DIM>(f.th, f.tl, f.empty, gx, gy, gz, i - 3 * gx, f.T, f.ntile,
+                                     f.je, f.gcl, f.ofs, f.fx_inv, f.fx_shift);
+    }
 }
 
 // zero n ints at p for every range of a device table (one launch; defined in tiled.cu)
@@ -1062,7 +1051,8 @@ struct IntRange {
 };
 void zero_ranges(const IntRange *d_ranges, int nrange, long max_n, cudaStream_t st);
 // batched fold of the tile currents of every box (defined in tiled.cu)
-void batch_fold(const FoldBox *d_boxes, int nbox, int dim, long max_points, cudaStream_t st);
+void batch_fold(const FoldBox *d_boxes, int nbox, int dim, int max_row, int max_rows,
+                cudaStream_t st);
 // CTAs of the batched push resident per SM (defined in batch_push.cu)
 int push_batch_occupancy(int dim, int order, int threads, size_t smem);
 
