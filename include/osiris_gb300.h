@@ -335,6 +335,11 @@ typedef struct {
     int pmc;          /* bit d set (d walled): the walls of axis d are perfect magnetic
                          conductors (the reference's p_bc_pmc, "reflecting") instead of
                          electric ones; the current and the particles are treated alike */
+    int emf_smooth_type;  /* the fields the particles see (the reference's e_part/b_part,
+                             smooth_type "stand" of the emf section): copies of E and B after
+                             their guard update, filtered by OSG_SMOOTH_* (all axes); E and B
+                             themselves are not changed.  Periodic boxes. */
+    int emf_smooth_order; /* its order */
 } osg_config;
 
 int osg_sim_create(const osg_config *cfg, osg_sim **out);

@@ -660,4 +660,16 @@ void FN(ora_set_smooth)(const int *ord, const R *coef)
         for (int i = 0; i < 3 * 31; i++) FN(step_smooth_coef)[i] = coef[i];
 }
 
+/* smoothing of the fields the particles see (e_part, b_part: copies of E and B after their
+   guard update, smoothed; update_particle_fld_emf, source/emf/os-emf.f03:1065-1151,
+   smooth_type "stand") applied by the step below (order 0: none) */
+static int FN(step_esmooth_ord)[3] = {0, 0, 0};
+static R FN(step_esmooth_coef)[3 * 31];
+void FN(ora_set_emf_smooth)(const int *ord, const R *coef)
+{
+    for (int d = 0; d < 3; d++) FN(step_esmooth_ord)[d] = ord ? ord[d] : 0;
+    if (coef)
+        for (int i = 0; i < 3 * 31; i++) FN(step_esmooth_coef)[i] = coef[i];
+}
+
 #undef FN

@@ -649,6 +649,18 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
         ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, b, 0, walls | win);                       \
     }                                                                                         \
     memset(j, 0, sizeof(R) * (size_t)gsz);                                                    \
+    /* the fields the particles see: E and B, or their smoothed copies */                      \
+    R *ep = e, *bp = b;                                                                       \
+    if (step_esmooth_ord_##SFXN[0] > 0) {                                                     \
+        ep = (R *)malloc(sizeof(R) * (size_t)gsz);                                            \
+        bp = (R *)malloc(sizeof(R) * (size_t)gsz);                                            \
+        memcpy(ep, e, sizeof(R) * (size_t)gsz);                                               \
+        memcpy(bp, b, sizeof(R) * (size_t)gsz);                                               \
+        ora_smooth_##SFXN(dim, nx, gcl, gcu, ep, step_esmooth_ord_##SFXN,                     \
+                          step_esmooth_coef_##SFXN);                                          \
+        ora_smooth_##SFXN(dim, nx, gcl, gcu, bp, step_esmooth_ord_##SFXN,                     \
+                          step_esmooth_coef_##SFXN);                                          \
+    }                                                                                         \
     int nt = nthreads < 1 ? 1 : nthreads;                                                     \
     R *jt = nt > 1 ? (R *)calloc((size_t)gsz * (nt - 1), sizeof(R)) : 0;                     \
     for (int s = 0; s < nspec; s++) {                                                         \
@@ -660,7 +672,7 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
             int a = t * chunk + 1, bnd = (t + 1) * chunk < np[s] ? (t + 1) * chunk : np[s];    \
             R *jj = t == 0 ? j : jt + (size_t)gsz * (t - 1);                                  \
             if (bnd >= a)                                                                     \
-                ora_push_##SFXN(dim, order, ix[s], x[s], u[s], q[s], a, bnd, rqm[s], e, b,    \
+                ora_push_##SFXN(dim, order, ix[s], x[s], u[s], q[s], a, bnd, rqm[s], ep, bp,  \
                                 emf_size, emf_off, jj, emf_size, emf_off, (double *)dx, dtp,  \
                                 &et[t]);                                                      \
         }                                                                                     \
@@ -680,6 +692,10 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
         for (long i = 0; i < gsz; i++)                                                        \
             for (int t = 1; t < nt; t++) j[i] += jt[(size_t)gsz * (t - 1) + i];                \
         free(jt);                                                                             \
+    }                                                                                         \
+    if (ep != e) {                                                                            \
+        free(ep);                                                                             \
+        free(bp);                                                                             \
     }                                                                                         \
     ora_pusher_##SFXN = 0;                                                                    \
     ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, j, 1, skip);                                  \

@@ -106,6 +106,8 @@ void ora_smooth_f64(int dim, const int *nx, const int *gcl, const int *gcu, doub
                     const int *ord, const double *coef);
 void ora_set_smooth_f32(const int *ord, const float *coef);
 void ora_set_smooth_f64(const int *ord, const double *coef);
+void ora_set_emf_smooth_f32(const int *ord, const float *coef);
+void ora_set_emf_smooth_f64(const int *ord, const double *coef);
 
 void ora_wrap(int dim, const int *nx, int np, int *ix);
 void ora_sort_index(int dim, const int *nx, int np, const int *ix, int *new_idx);

@@ -86,6 +86,7 @@ def _declare(L):
     for s_ in ("f32", "f64"):
         getattr(L, f"ora_smooth_{s_}").argtypes = [I, P, P, P, P, P, P]
         getattr(L, f"ora_set_smooth_{s_}").argtypes = [P, P]
+        getattr(L, f"ora_set_emf_smooth_{s_}").argtypes = [P, P]
         getattr(L, f"ora_walls_{s_}").argtypes = [I, P, P, P, P, I, I, I]
         getattr(L, f"ora_set_walls_{s_}").argtypes = [I]
         getattr(L, f"ora_set_pmc_{s_}").argtypes = [I]
@@ -373,7 +374,7 @@ def lindman_phase(g: "Grid", prec, axis, what, e, b, state, dt):
 
 def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="boris",
          iter_tol=1e-3, smooth=None, walls=0, open_fields=None, thermal=None, pmc=0,
-         window=False):
+         window=False, smooth_emf=None):
     """One full time step; species = list of dicts with ix, x, u, q, rqm.  walls (bit d):
     axis d bounded by conducting walls instead of periodic.  open_fields = (axis, state from
     lindman_state): Lindman open boundaries at both edges of that axis, particles absorbed
@@ -383,6 +384,9 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     instead of electric conductor walls.  window=True: x1 is the axis of a moving window (no
     guard update along it, particles absorbed below cell 1 -- removed from the species arrays
     after the step -- and reflected above nx); the window's moves are Window.start_step.
+    smooth = (type, order) filters the folded current; smooth_emf = (type, order) gives the
+    particles smoothed copies of E and B (the reference's e_part / b_part, smooth_type
+    "stand"), E and B themselves unchanged.
     Returns the per-species energy sums (Boris: time-centred u^2/(gamma+1); exact pusher:
     gamma - 1 of the new momentum; both times q).  fast=True runs the -O3 -ffast-math build
     (timing only)."""
@@ -400,6 +404,10 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     if smooth is not None:
         ordv, coef = _smooth_tables(g.dim, prec, [smooth[0]] * g.dim, [smooth[1]] * g.dim)
         getattr(L, f"ora_set_smooth_{prec}")(_p(ordv), _p(coef))
+    if smooth_emf is not None:
+        eord, ecoef = _smooth_tables(g.dim, prec, [smooth_emf[0]] * g.dim,
+                                     [smooth_emf[1]] * g.dim)
+        getattr(L, f"ora_set_emf_smooth_{prec}")(_p(eord), _p(ecoef))
     args = (g.dim, g.order, _p(nx), _p(gl), _p(gu), _p(_f64(g.dx + [0.0] * 3)), float(dt), _p(e),
             _p(b), _p(j), ns, _p(np_), ixs, xs, us, qs, _p(rqm), _p(ene), int(nthreads))
     getattr(L, f"ora_set_walls_{prec}")(int(walls))
@@ -424,6 +432,8 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
         L.ora_set_thermal(0, None, None, 0, 0, 0)
     if smooth is not None:
         getattr(L, f"ora_set_smooth_{prec}")(None, None)
+    if smooth_emf is not None:
+        getattr(L, f"ora_set_emf_smooth_{prec}")(None, None)
     if window:
         for sp in species:
             keep = sp["ix"][:, 0] > ORA_GONE // 2

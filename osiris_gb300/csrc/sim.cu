@@ -66,6 +66,8 @@ struct osg_sim {
     int open_axis = -1;          // Lindman open boundaries at both edges of this axis
     void *lind = nullptr;        // their state (lindman_state_size reals)
     osg::SmoothSpec smooth;      // current smoothing (order 0 per axis: none)
+    osg::SmoothSpec esmooth;     // smoothing of the fields the particles see (order 0: none)
+    void *e_part = nullptr, *b_part = nullptr;   // those fields, when smoothed
     // graphs: [parity][sort (plain) / window move (tiled)]
     cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     bool graphs_dirty = true;
@@ -279,11 +281,24 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
         periodic_update<T>(s->g, (T *)s->b, 0, st, 0, walls | win);
         launches += 2 * (c.dim - __builtin_popcount(walls | win));
     }
+    // the fields the particles see (update_particle_fld_emf, source/emf/os-emf.f03:1065-1151):
+    // E and B, or their smoothed copies (smooth_type "stand")
+    const void *ep = s->e, *bp = s->b;
+    if (s->esmooth.order[0] > 0) {
+        const size_t gbytes = (size_t)s->esz * 3 * s->g.npoints();
+        OSG_CUDA(cudaMemcpyAsync(s->e_part, s->e, gbytes, cudaMemcpyDeviceToDevice, st));
+        OSG_CUDA(cudaMemcpyAsync(s->b_part, s->b, gbytes, cudaMemcpyDeviceToDevice, st));
+        smooth_field<T>(s->g, s->esmooth, (T *)s->e_part, (T *)s->shift_tmp, st);
+        smooth_field<T>(s->g, s->esmooth, (T *)s->b_part, (T *)s->shift_tmp, st);
+        launches += 2 * c.dim;
+        ep = s->e_part;
+        bp = s->b_part;
+    }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[1], st));
     OSG_CUDA(cudaMemsetAsync(s->j, 0, (size_t)s->esz * 3 * s->g.npoints(), st));
     OSG_CUDA(cudaMemsetAsync(s->d_ene, 0, sizeof(double) * MAX_SPECIES, st));
     if (c.engine == OSG_ENGINE_TILED) {
-        int rc = tiled_push(s->tiled, parity, (const float *)s->e, (const float *)s->b,
+        int rc = tiled_push(s->tiled, parity, (const float *)ep, (const float *)bp,
                             (float *)s->j, s->d_ene, s->d_status, st, &launches, shift ? 1 : 0);
         if (rc) return rc;
     } else {
@@ -292,7 +307,7 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
             PlainSpecies &p = s->plain[k];
             PlainPushArgs<T> a = make_plain_args<T>(
                 c.dim, c.order, p.ix, (T *)p.x, (T *)p.u, (const T *)p.q, s->np[k],
-                (T)s->rqm[k], (const T *)s->e, (const T *)s->b, emf_size, emf_off, (T *)s->j,
+                (T)s->rqm[k], (const T *)ep, (const T *)bp, emf_size, emf_off, (T *)s->j,
                 emf_size, emf_off, c.dx, push_dt, s->d_ene + k, s->d_status);
             for (int d = 0; d < c.dim; d++) {
                 a.wrap[d] = (skip >> d) & 1 ? 0 : c.nx[d];
@@ -485,6 +500,9 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               "the tiled engine is single precision");
     OSG_CHECK(cfg->walls >= 0 && cfg->walls < (1 << cfg->dim), OSG_ERR_ARG,
               "walls: a bit mask of the axes");
+    OSG_CHECK((cfg->walls == 0 && cfg->open_fields == 0) ||
+                  cfg->emf_smooth_type == OSG_SMOOTH_NONE,
+              OSG_ERR_ARG, "smoothing of the particles' fields runs on periodic boxes");
     OSG_CHECK(cfg->walls == 0 || cfg->smooth_type == OSG_SMOOTH_NONE, OSG_ERR_ARG,
               "current smoothing next to conducting walls is not supported");
     OSG_CHECK(cfg->open_fields >= 0 && cfg->open_fields < (1 << cfg->dim) &&
@@ -543,6 +561,25 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
         // the current is used by the E advance), source/current/os-current-define.f03:198-206
         s->gl = std::max(s->gl, n);
         s->gu = std::max(s->gu, n + 1);
+        // the particles' fields: the reference adds the filter's order to the field's guard
+        // cells on both sides (source/emf/os-emf.f03:690-703), so that every point a particle
+        // gathers from is filtered
+        int ne = 0, gli = 0, gui = 0;
+        memset(&s->esmooth, 0, sizeof s->esmooth);
+        if (smooth_coefficients(cfg->emf_smooth_type, cfg->emf_smooth_order, s->esmooth.c[0],
+                                &ne)) {
+            set_error("bad field smoothing type %d / order %d", cfg->emf_smooth_type,
+                      cfg->emf_smooth_order);
+            delete s;
+            return OSG_ERR_ARG;
+        }
+        for (int d = 0; d < cfg->dim; d++) {
+            s->esmooth.order[d] = ne;
+            for (int k = 0; k < 2 * ne + 1; k++) s->esmooth.c[d][k] = s->esmooth.c[0][k];
+        }
+        guard_cells(cfg->order, &gli, &gui);
+        s->gl = std::max(s->gl, gli + ne);
+        s->gu = std::max(s->gu, gui + ne);
     }
     int gcl[3] = {s->gl, s->gl, s->gl}, gcu[3] = {s->gu, s->gu, s->gu};
     s->g = make_grid(cfg->dim, s->cfg.nx, gcl, gcu);
@@ -560,7 +597,12 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
     s->d_ene = rc ? nullptr : dalloc<double>(MAX_SPECIES, &rc);
     s->d_status = rc ? nullptr : dalloc<int>(4, &rc);
     s->d_diag = rc ? nullptr : dalloc<double>(16, &rc);
-    if (!rc && s->smooth.order[0] > 0) s->shift_tmp = dalloc<char>(gbytes, &rc);
+    if (!rc && (s->smooth.order[0] > 0 || s->esmooth.order[0] > 0))
+        s->shift_tmp = dalloc<char>(gbytes, &rc);
+    if (!rc && s->esmooth.order[0] > 0) {
+        s->e_part = dalloc<char>(gbytes, &rc);
+        if (!rc) s->b_part = dalloc<char>(gbytes, &rc);
+    }
     size_t lbytes = 0;
     if (!rc && cfg->thermal) s->d_step = dalloc<unsigned long long>(1, &rc);
     if (!rc && cfg->open_fields) {
@@ -612,6 +654,8 @@ int osg_sim_destroy(osg_sim *s)
     cudaFree(s->b);
     cudaFree(s->j);
     cudaFree(s->shift_tmp);
+    cudaFree(s->e_part);
+    cudaFree(s->b_part);
     cudaFree(s->lind);
     cudaFree(s->d_step);
     cudaFree(s->d_ene);

@@ -14,7 +14,8 @@ STRUCTS = {
     "osg_config": ("Config", ["dim", "order", "precision", "engine", "nx", "dx", "dt", "tile",
                               "n_sort", "capacity", "pusher", "iter_tol", "smooth_type",
                               "smooth_order", "walls", "open_fields", "thermal", "seed",
-                              "uth_bnd", "ufl_bnd", "thermal_type", "pmc"]),
+                              "uth_bnd", "ufl_bnd", "thermal_type", "pmc", "emf_smooth_type",
+                              "emf_smooth_order"]),
     "osg_batch_config": ("BatchConfig", ["dim", "order", "dt", "tile", "threads", "capacity"]),
     "osg_zpulse": ("Zpulse", ["omega0", "a0", "pol", "lon_x0", "lon_duration", "lon_range",
                               "per_w0", "per_focus", "per_center"]),
