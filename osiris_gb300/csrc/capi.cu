@@ -694,9 +694,12 @@ class HostPool {
 int osg_particle_wrap(int dim, const int *nx, long np, int *ix)
 {
     OSG_CHECK(dim >= 1 && dim <= 3 && nx && (np == 0 || ix), OSG_ERR_ARG, "bad arguments");
-    // branch-free per axis so the loop vectorises; large arrays are split over host threads
+    // branch-free per axis so the loop vectorises; large arrays are split over host threads.
+    // Only a few particles cross the box per step: a block of indices is first scanned
+    // (read only) and rewritten only when one of them is out of range, so the unchanged
+    // blocks cost a read and no write-back.
     const int n0 = nx[0], n1 = dim > 1 ? nx[1] : 1, n2 = dim > 2 ? nx[2] : 1;
-    auto wrap_range = [=](long p0, long p1) {
+    auto fix_range = [=](long p0, long p1) {
         int *c = ix + (long)dim * p0;
         const long m = (long)dim * (p1 - p0);
         if (dim == 1) {
@@ -712,6 +715,26 @@ int osg_particle_wrap(int dim, const int *nx, long np, int *ix)
                 c[k + 1] += (c[k + 1] < 1 ? n1 : 0) - (c[k + 1] > n1 ? n1 : 0);
                 c[k + 2] += (c[k + 2] < 1 ? n2 : 0) - (c[k + 2] > n2 ? n2 : 0);
             }
+        }
+    };
+    auto wrap_range = [=](long p0, long p1) {
+        const long blk = 1024;   // particles per scanned block
+        for (long b0 = p0; b0 < p1; b0 += blk) {
+            const long b1 = std::min(p1, b0 + blk);
+            const int *c = ix + (long)dim * b0;
+            const long m = (long)dim * (b1 - b0);
+            int out = 0;
+            if (dim == 1) {
+                for (long k = 0; k < m; k++) out |= (c[k] < 1) | (c[k] > n0);
+            } else if (dim == 2) {
+                for (long k = 0; k < m; k += 2)
+                    out |= (c[k] < 1) | (c[k] > n0) | (c[k + 1] < 1) | (c[k + 1] > n1);
+            } else {
+                for (long k = 0; k < m; k += 3)
+                    out |= (c[k] < 1) | (c[k] > n0) | (c[k + 1] < 1) | (c[k + 1] > n1) |
+                           (c[k + 2] < 1) | (c[k + 2] > n2);
+            }
+            if (out) fix_range(b0, b1);
         }
     };
     if (np < (1L << 20)) {
