@@ -641,9 +641,13 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
     const int walls = step_walls_##SFXN;                                                      \
     const int oax = step_open_##SFXN; /* Lindman axis, -1: none */                            \
     const int win = step_window_##SFXN; /* moving window along x1 */                          \
-    const int skip = walls | (oax >= 0 ? 1 << oax : 0) | win;                                 \
+    const int pax = step_pml_##SFXN; /* PML axis, -1: none */                                 \
+    const int skip = walls | (oax >= 0 ? 1 << oax : 0) | (pax >= 0 ? 1 << pax : 0) | win;     \
     if (oax >= 0) {                                                                           \
         ora_open_guards_##SFXN(dim, nx, gcl, gcu, e, b, oax, step_lind_##SFXN);               \
+    } else if (pax >= 0) {                                                                    \
+        ora_pml_guards_##SFXN(dim, nx, gcl, gcu, e, b, pax, step_pml_nb_##SFXN,               \
+                              step_pml_st_##SFXN);                                            \
     } else {                                                                                  \
         ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, e, 0, walls | win);                       \
         ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, b, 0, walls | win);                       \
@@ -684,6 +688,8 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
                                     step_ufl, step_seed, s, step_count, step_ttype);          \
         if (oax >= 0)                                                                         \
             ora_particle_absorb_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], q[s], oax);         \
+        if (pax >= 0)                                                                         \
+            ora_particle_absorb_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], q[s], pax);         \
         if (win) ora_particle_window_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], q[s]);        \
         ora_particle_bound_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], walls);                  \
     }                                                                                         \
@@ -708,6 +714,9 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
     else if (oax >= 0)                                                                        \
         ora_yee_advance_open_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt, oax,                 \
                                     step_lind_##SFXN);                                        \
+    else if (pax >= 0)                                                                        \
+        ora_yee_advance_pml_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt, pax,                  \
+                                   step_pml_nb_##SFXN, step_pml_st_##SFXN);                   \
     else                                                                                      \
         ora_yee_advance_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt);                           \
     return 0;

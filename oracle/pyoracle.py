@@ -93,6 +93,11 @@ def _declare(L):
         getattr(L, f"ora_set_open_{s_}").argtypes = [I, P]
         getattr(L, f"ora_set_window_{s_}").argtypes = [I]
         getattr(L, f"ora_lindman_phase_{s_}").argtypes = [I, P, P, P, I, I, P, P, P, P, D]
+        getattr(L, f"ora_pml_state_size_{s_}").argtypes = [I, P, P, P, I, I]
+        getattr(L, f"ora_pml_state_size_{s_}").restype = C.c_long
+        getattr(L, f"ora_pml_init_{s_}").argtypes = [I, P, P, P, I, I, P, D, P]
+        getattr(L, f"ora_pml_phase_{s_}").argtypes = [I, P, P, P, I, I, I, P, P, P, P, D]
+        getattr(L, f"ora_set_pml_{s_}").argtypes = [I, I, P]
     L.ora_set_thermal.argtypes = [I, P, P, C.c_uint32, C.c_uint64, I]
     L.ora_push_cyl_f32.argtypes = [I, P, P, P, P, I, I, C.c_float, I, P, P, P, P, P, P, P, P, D,
                                    P]
@@ -372,13 +377,37 @@ def lindman_phase(g: "Grid", prec, axis, what, e, b, state, dt):
                                                  _p(_f64(g.dx + [0.0] * 3)), float(dt))
 
 
+def pml_state(g: "Grid", prec, axis, nb, dt):
+    """State of PML walls of nb cells at both edges of `axis` (2D): zeroed walls and the
+    attenuation tables, kept by the caller between steps."""
+    nx, gl, gu = g.args()
+    L = lib()
+    n = getattr(L, f"ora_pml_state_size_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), int(axis),
+                                                 int(nb))
+    st = np.zeros(n, dtype=dtype_of(prec))
+    getattr(L, f"ora_pml_init_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), int(axis), int(nb),
+                                       _p(_f64(g.dx + [0.0] * 3)), float(dt), _p(st))
+    return st
+
+
+def pml_phase(g: "Grid", prec, axis, nb, what, e, b, state, dt):
+    """One PML phase on `axis`, in place (what 0 the walls' guard update, 1 E walls with the
+    B interfaces, 2 B walls with the E interfaces)."""
+    nx, gl, gu = g.args()
+    getattr(lib(), f"ora_pml_phase_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), int(axis), int(nb),
+                                             int(what), _p(e), _p(b), _p(state),
+                                             _p(_f64(g.dx + [0.0] * 3)), float(dt))
+
+
 def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="boris",
          iter_tol=1e-3, smooth=None, walls=0, open_fields=None, thermal=None, pmc=0,
-         window=False, smooth_emf=None):
+         window=False, smooth_emf=None, pml=None):
     """One full time step; species = list of dicts with ix, x, u, q, rqm.  walls (bit d):
     axis d bounded by conducting walls instead of periodic.  open_fields = (axis, state from
     lindman_state): Lindman open boundaries at both edges of that axis, particles absorbed
-    there (left in the arrays with charge and momentum 0).  thermal = dict(mask, uth, ufl, seed,
+    there (left in the arrays with charge and momentum 0).  pml = (axis, nb, state from
+    pml_state): PML walls of nb cells at both edges of that axis (2D), particles absorbed there
+    the same way.  thermal = dict(mask, uth, ufl, seed,
     step, type: 0 thermal, 1 random dir, 2 waterbag): particles crossing the edges of the axes in mask (walled or open) are re-emitted from
     a thermal bath; step keys the random stream.  pmc (bit d, d walled): perfect magnetic
     instead of electric conductor walls.  window=True: x1 is the axis of a moving window (no
@@ -415,6 +444,8 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     getattr(L, f"ora_set_window_{prec}")(1 if window else 0)
     if open_fields is not None:
         getattr(L, f"ora_set_open_{prec}")(int(open_fields[0]), _p(open_fields[1]))
+    if pml is not None:
+        getattr(L, f"ora_set_pml_{prec}")(int(pml[0]), int(pml[1]), _p(pml[2]))
     if thermal is not None:
         L.ora_set_thermal(int(thermal["mask"]), _p(_f64(thermal["uth"])),
                           _p(_f64(thermal.get("ufl", [0.0] * 3))), int(thermal.get("seed", 0)),
@@ -429,6 +460,7 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
         getattr(L, f"ora_set_pmc_{prec}")(0)
         getattr(L, f"ora_set_window_{prec}")(0)
         getattr(L, f"ora_set_open_{prec}")(-1, None)
+        getattr(L, f"ora_set_pml_{prec}")(-1, 0, None)
         L.ora_set_thermal(0, None, None, 0, 0, 0)
     if smooth is not None:
         getattr(L, f"ora_set_smooth_{prec}")(None, None)

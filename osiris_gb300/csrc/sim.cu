@@ -65,6 +65,9 @@ struct osg_sim {
     unsigned long long *d_step = nullptr;   // step counter of the thermal-bath random stream
     int open_axis = -1;          // Lindman open boundaries at both edges of this axis
     void *lind = nullptr;        // their state (lindman_state_size reals)
+    int pml_axis = -1;           // PML walls at both edges of this axis (2D)
+    int pml_nb = 0;              // their thickness in cells
+    void *pml = nullptr;         // their state (pml_state_size reals)
     osg::SmoothSpec smooth;      // current smoothing (order 0 per axis: none)
     osg::SmoothSpec esmooth;     // smoothing of the fields the particles see (order 0: none)
     void *e_part = nullptr, *b_part = nullptr;   // those fields, when smoothed
@@ -271,10 +274,16 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
     // Lindman open boundaries: no periodic update along their axis, the boundary planes come
     // from their state, the current beyond them is neither folded nor imaged
     const int oax = s->open_axis;
-    const int skip = walls | (oax >= 0 ? 1 << oax : 0);
+    // PML walls: the same, with the boundary points set by the walls' interfaces in the Yee
+    // advance (no restore at the guard update)
+    const int pax = s->pml_axis;
+    const int skip = walls | (oax >= 0 ? 1 << oax : 0) | (pax >= 0 ? 1 << pax : 0);
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[0], st));
     if (oax >= 0) {
         open_guards<T>(s->g, (T *)s->e, (T *)s->b, oax, (const T *)s->lind, st);
+        launches += 2 * (c.dim - 1) + 1;
+    } else if (pax >= 0) {
+        pml_guards<T>(s->g, (T *)s->e, (T *)s->b, pax, s->pml_nb, (T *)s->pml, st);
         launches += 2 * (c.dim - 1) + 1;
     } else {
         periodic_update<T>(s->g, (T *)s->e, 0, st, 0, walls | win);
@@ -312,7 +321,7 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
             for (int d = 0; d < c.dim; d++) {
                 a.wrap[d] = (skip >> d) & 1 ? 0 : c.nx[d];
                 a.reflect[d] = (walls >> d) & 1 ? c.nx[d] : 0;
-                a.absorb[d] = d == oax ? c.nx[d] : 0;
+                a.absorb[d] = (d == oax || d == pax) ? c.nx[d] : 0;
             }
             a.q_absorb = (T *)p.q;
             if (c.thermal) {
@@ -362,8 +371,9 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
     }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[4], st));
     yee_advance<T>(s->g, (T *)s->e, (T *)s->b, (const T *)s->j, c.dx, c.dt, st, walls, c.order,
-                   oax, (T *)s->lind, c.pmc);
-    launches += 3 + (walls ? 6 * __builtin_popcount(walls) : 0) + (oax >= 0 ? 3 : 0);
+                   oax, (T *)s->lind, c.pmc, pax, s->pml_nb, (T *)s->pml);
+    launches += 3 + (walls ? 6 * __builtin_popcount(walls) : 0) + (oax >= 0 ? 3 : 0) +
+                (pax >= 0 ? 4 : 0);
     if (shift) {
         shift_window_x<T>(s->g, (T *)s->e, (T *)s->shift_tmp, st);
         shift_window_x<T>(s->g, (T *)s->b, (T *)s->shift_tmp, st);
@@ -513,6 +523,21 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               OSG_ERR_ARG, "open boundaries combine with neither walls nor smoothing");
     OSG_CHECK(cfg->pmc >= 0 && (cfg->pmc & ~cfg->walls) == 0, OSG_ERR_ARG,
               "pmc: a bit mask of walled axes");
+    OSG_CHECK(cfg->pml >= 0 && cfg->pml < (1 << cfg->dim) && (cfg->pml & (cfg->pml - 1)) == 0,
+              OSG_ERR_ARG, "pml: the bit of one axis (PML walls without corners)");
+    OSG_CHECK(cfg->pml == 0 || cfg->dim == 2, OSG_ERR_ARG, "PML walls are built for 2D boxes");
+    OSG_CHECK(cfg->pml == 0 || (cfg->walls == 0 && cfg->open_fields == 0 &&
+                                cfg->smooth_type == OSG_SMOOTH_NONE &&
+                                cfg->emf_smooth_type == OSG_SMOOTH_NONE && cfg->thermal == 0),
+              OSG_ERR_ARG, "PML walls combine with neither walls, Lindman boundaries, "
+                           "smoothing nor a thermal bath");
+    OSG_CHECK(cfg->pml_cells == 0 || cfg->pml_cells >= 5, OSG_ERR_ARG,
+              "pml_cells: 0 (8) or at least 5");
+    if (cfg->pml) {
+        const int t = 1 - __builtin_ctz(cfg->pml);
+        OSG_CHECK(cfg->nx[t] >= 6, OSG_ERR_ARG,
+                  "PML walls need at least 6 cells along the other axis");
+    }
     OSG_CHECK(cfg->thermal >= 0 && (cfg->thermal & ~(cfg->walls | cfg->open_fields)) == 0,
               OSG_ERR_ARG, "thermal: a bit mask of walled or open axes");
     OSG_CHECK(cfg->thermal == 0 || cfg->engine == OSG_ENGINE_PLAIN ||
@@ -610,6 +635,25 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
         lbytes = (size_t)s->esz * lindman_state_size(s->g, s->open_axis);
         s->lind = dalloc<char>(lbytes, &rc);
     }
+    if (!rc && cfg->pml) {
+        // the walls start at zero (new_wall, source/vdf/os-wall.f90:198-210); the attenuation
+        // tables are computed on the host in double and stored in the field precision
+        s->pml_axis = __builtin_ctz(cfg->pml);
+        s->pml_nb = cfg->pml_cells > 0 ? cfg->pml_cells : 8;
+        const long n = pml_state_size(s->g, s->pml_axis, s->pml_nb);
+        s->pml = dalloc<char>((size_t)s->esz * n, &rc);
+        if (!rc) {
+            std::vector<char> h((size_t)s->esz * n);
+            if (s->esz == 4)
+                pml_init_host<float>(s->g, s->pml_axis, s->pml_nb, cfg->dx, cfg->dt,
+                                     (float *)h.data());
+            else
+                pml_init_host<double>(s->g, s->pml_axis, s->pml_nb, cfg->dx, cfg->dt,
+                                      (double *)h.data());
+            if (cudaMemcpy(s->pml, h.data(), h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+                rc = OSG_ERR_CUDA;
+        }
+    }
     if (rc) {
         osg_sim_destroy(s);
         return rc;
@@ -657,6 +701,7 @@ int osg_sim_destroy(osg_sim *s)
     cudaFree(s->e_part);
     cudaFree(s->b_part);
     cudaFree(s->lind);
+    cudaFree(s->pml);
     cudaFree(s->d_step);
     cudaFree(s->d_ene);
     cudaFree(s->d_status);
@@ -852,8 +897,8 @@ int osg_sim_set_window(osg_sim *s, int species, const int *ppc, int nprof, const
     OSG_CHECK(s->cfg.engine == OSG_ENGINE_TILED, OSG_ERR_ARG,
               "the moving window runs on the tiled engine");
     OSG_CHECK(s->step_n == 0, OSG_ERR_STATE, "set the window before the first step");
-    OSG_CHECK(s->open_axis < 0, OSG_ERR_ARG, "the moving window does not combine with "
-                                             "Lindman open boundaries");
+    OSG_CHECK(s->open_axis < 0 && s->pml_axis < 0, OSG_ERR_ARG,
+              "the moving window does not combine with Lindman or PML boundaries");
     int rc = tiled_set_window(s->tiled, species, ppc, nprof, prof_x, prof_f);
     if (rc) return rc;
     if (!s->shift_tmp) {
@@ -877,8 +922,10 @@ int osg_sim_set_window(osg_sim *s, int species, const int *ppc, int nprof, const
 // run's precision), then long grid points and E(3,points), B(3,points) with guard cells, last,
 // with Lindman open boundaries, their state (lindman_state_size reals; the reference stores
 // its Lindman buffers in the restart file too, restart_write_lindman,
-// source/emf/boundary/os-emf-lindman.f90:135-156).  The current is rebuilt by the next step
-// and is not stored.
+// source/emf/boundary/os-emf-lindman.f90:135-156), with PML walls theirs (pml_state_size
+// reals: the walls, as restart_write_vpml stores its wall objects, source/emf/boundary/
+// os-emf-vpml.f03:205-229, and the attenuation tables).  The current is rebuilt by the next
+// step and is not stored.
 namespace {
 
 struct CkptFile {
@@ -937,6 +984,12 @@ int osg_sim_checkpoint(osg_sim *s, const char *path)
     if (ok && s->lind) {
         std::vector<char> l((size_t)s->esz * lindman_state_size(s->g, s->open_axis));
         OSG_CUDA(cudaMemcpyAsync(l.data(), s->lind, l.size(), cudaMemcpyDeviceToHost, s->st));
+        OSG_CUDA(cudaStreamSynchronize(s->st));
+        ok = put(f, l.data(), l.size());
+    }
+    if (ok && s->pml) {
+        std::vector<char> l((size_t)s->esz * pml_state_size(s->g, s->pml_axis, s->pml_nb));
+        OSG_CUDA(cudaMemcpyAsync(l.data(), s->pml, l.size(), cudaMemcpyDeviceToHost, s->st));
         OSG_CUDA(cudaStreamSynchronize(s->st));
         ok = put(f, l.data(), l.size());
     }
@@ -1003,6 +1056,17 @@ int osg_sim_restore(const char *path, osg_sim **out)
                        cudaSuccess ||
                    cudaStreamSynchronize(s->st) != cudaSuccess) {
             set_error("upload of the Lindman state failed");
+            rc = OSG_ERR_CUDA;
+        }
+    }
+    if (rc == OSG_OK && s->pml) {
+        std::vector<char> l((size_t)esz * pml_state_size(s->g, s->pml_axis, s->pml_nb));
+        if (!get(f, l.data(), l.size())) {
+            rc = OSG_ERR_ARG;
+        } else if (cudaMemcpyAsync(s->pml, l.data(), l.size(), cudaMemcpyHostToDevice, s->st) !=
+                       cudaSuccess ||
+                   cudaStreamSynchronize(s->st) != cudaSuccess) {
+            set_error("upload of the PML state failed");
             rc = OSG_ERR_CUDA;
         }
     }
@@ -1100,7 +1164,7 @@ int osg_sim_energy(osg_sim *s, double *kinetic, double *field)
 int osg_sim_gauss_residual(osg_sim *s, double *max_abs, double *l2)
 {
     OSG_CHECK(s, OSG_ERR_ARG, "null sim");
-    OSG_CHECK(s->cfg.walls == 0 && s->cfg.open_fields == 0, OSG_ERR_STATE,
+    OSG_CHECK(s->cfg.walls == 0 && s->cfg.open_fields == 0 && s->cfg.pml == 0, OSG_ERR_STATE,
               "the Gauss residual is taken on periodic boxes (no walls or open edges)");
     const size_t n = 3 * (size_t)s->g.npoints();
     int rc = OSG_OK;
@@ -1226,6 +1290,10 @@ static int save_fields(osg_sim *s, SavedState &sv)
         return rc;
     if (s->lind &&
         (rc = sv.save(s->lind, (size_t)s->esz * lindman_state_size(s->g, s->open_axis), s->st)))
+        return rc;
+    if (s->pml &&
+        (rc = sv.save(s->pml, (size_t)s->esz * pml_state_size(s->g, s->pml_axis, s->pml_nb),
+                      s->st)))
         return rc;
     if (s->d_step && (rc = sv.save(s->d_step, sizeof(unsigned long long), s->st))) return rc;
     sv.step_n = s->step_n;

@@ -73,7 +73,7 @@ struct TiledState {
     unsigned int seed = 0;
     float uth_bnd[3] = {0, 0, 0}, ufl_bnd[3] = {0, 0, 0};
     const unsigned long long *step = nullptr;   // the owner's step counter
-    int open_fields = 0;   // bit d: Lindman open boundaries on axis d (particles absorbed)
+    int open_fields = 0;   // bit d: Lindman or PML boundaries on axis d (particles absorbed)
     int pusher = OSG_PUSHER_BORIS;
     double iter_tol = 1.0e-3;
     long nj_tile = 0;    // current points (x3 components) of a tile with its halo
@@ -276,7 +276,7 @@ int tiled_create(TiledState **out, const osg_config &cfg, const GridDesc &g)
         t->uth_bnd[d] = (float)cfg.uth_bnd[d];
         t->ufl_bnd[d] = (float)cfg.ufl_bnd[d];
     }
-    t->open_fields = cfg.open_fields;
+    t->open_fields = cfg.open_fields | cfg.pml;   // particles absorbed along either
     t->ntiles = 1;
     for (int d = 0; d < 3; d++) {
         t->nx[d] = d < cfg.dim ? cfg.nx[d] : 1;

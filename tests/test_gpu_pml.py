@@ -1,0 +1,194 @@
+"""GPU parity of PML walls (osg_config.pml, Vay's split-field perfectly matched layer at both
+edges of one axis of a 2D box) against the oracle's step.  The walls advance their E after the
+first B half step and their B after the E step, exchange the boundary points with the box
+through the interfaces, and take their own periodic update along the other axis at the guard
+update; the current is not folded along the PML axis and particles leaving through it are
+absorbed.  Whole field arrays are compared, guard cells included (the interfaces write there).
+
+* plain engine, FP64 1e-12 and FP32 1e-5 / 5e-5 (1 and 10 steps), orders 1-3, either axis;
+* tiled engine (FP32; absorbed particles removed rather than kept with charge 0): fields and
+  the live particles against the oracle, either axis;
+* a vacuum pulse travelling along the PML axis leaves the box with less than 1e-4 of its
+  energy, in both engines;
+* checkpoint / restore keeps the walls: 4 + 4 steps equal 8 steps to 1e-12;
+* configurations the walls are not built for are refused.
+"""
+import numpy as np
+import pytest
+
+from test_gpu_step import _nerr, _setup
+
+pytestmark = pytest.mark.gpu
+
+NB = 8
+
+
+@pytest.fixture(scope="module")
+def osg():
+    import __graft_entry__ as g
+    g.build_native()
+    import osiris_gb300
+    if osiris_gb300.lib().osg_device_count() < 1:
+        pytest.fail("no CUDA device visible")
+    return osiris_gb300
+
+
+def _oracle_run(oracle, g, p, e, b, species, dt, axis, steps, nb=NB):
+    ora = [{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s.items()}
+           for s in species]
+    eo, bo, jo = e.copy(), b.copy(), g.zeros(p)
+    st = oracle.pml_state(g, p, axis, nb, dt)
+    for _ in range(steps):
+        oracle.step(g, p, eo, bo, jo, ora, dt, pml=(axis, nb, st))
+    return eo, bo, jo, ora
+
+
+@pytest.mark.parametrize("axis", [0, 1])
+@pytest.mark.parametrize("order", [1, 2, 3])
+@pytest.mark.parametrize("prec,steps,tol", [(64, 1, 1e-12), (64, 10, 1e-12), (32, 1, 1e-5),
+                                            (32, 10, 5e-5)])
+def test_pml_plain_matches_oracle(osg, oracle, prec, steps, tol, order, axis):
+    nx = [20, 16]
+    p, g, dx, dt, species, e, b = _setup(oracle, prec, 2, order, nx, [2, 2], 11, uth=0.6,
+                                         ufl=0.1)
+    sim = osg.Simulation(nx, dx, dt, order=order, precision=prec, engine=osg.ENGINE_PLAIN,
+                         pml=1 << axis, pml_cells=NB)
+    sim.set_fields(e, b)
+    for s in species:
+        sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
+    sim.step(steps)
+    eg, bg, jg = sim.fields()
+    eo, bo, jo, ora = _oracle_run(oracle, g, p, e, b, species, dt, axis, steps)
+    errs = {"E": _nerr(eg, eo), "B": _nerr(bg, bo), "J": _nerr(jg, jo)}
+    absorbed = 0
+    for k, s in enumerate(ora):
+        ix, x, u, q = sim.species(k)          # the plain engine keeps the particle order
+        errs[f"x{k}"] = _nerr(ix + x, s["ix"] + s["x"])
+        errs[f"u{k}"] = _nerr(u, s["u"])
+        assert np.array_equal(q == 0, s["q"] == 0)
+        absorbed += int((q == 0).sum())
+        assert ix.min() >= 1 and np.all(ix.max(axis=0) <= np.array(nx))
+    sim.close()
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, (bad, errs)
+    if steps > 1:
+        assert absorbed > 0
+
+
+@pytest.mark.parametrize("axis", [0, 1])
+@pytest.mark.parametrize("order", [2, 3])
+@pytest.mark.parametrize("steps,tol", [(1, 1e-5), (10, 5e-5)])
+def test_pml_tiled_matches_oracle(osg, oracle, steps, tol, order, axis):
+    """The tiled engine drops absorbed particles; the oracle keeps them with charge 0."""
+    nx = [32, 24]
+    p, g, dx, dt, species, e, b = _setup(oracle, 32, 2, order, nx, [2, 2], 12, uth=0.6,
+                                         ufl=0.1)
+    sim = osg.Simulation(nx, dx, dt, order=order, precision=32, engine=osg.ENGINE_TILED,
+                         tile=[8, 8], pml=1 << axis, pml_cells=NB)
+    sim.set_fields(e, b)
+    for s in species:
+        sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
+    sim.step(steps)
+    eg, bg, jg = sim.fields()
+    eo, bo, jo, ora = _oracle_run(oracle, g, p, e, b, species, dt, axis, steps)
+    errs = {"E": _nerr(eg, eo), "B": _nerr(bg, bo), "J": _nerr(jg, jo)}
+    for k, s in enumerate(ora):
+        ix, x, u, q = sim.species(k)
+        live = s["q"] != 0
+        assert len(q) == int(live.sum())
+        if steps > 1:
+            assert len(q) < len(s["q"])
+        a = np.argsort(q, kind="stable")
+        o = np.flatnonzero(live)[np.argsort(s["q"][live], kind="stable")]
+        errs[f"x{k}"] = _nerr(ix[a] + x[a], s["ix"][o] + s["x"][o])
+        errs[f"u{k}"] = _nerr(u[a], s["u"][o])
+        assert ix.min() >= 1 and np.all(ix.max(axis=0) <= np.array(nx))
+    sim.close()
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, (bad, errs)
+
+
+@pytest.mark.parametrize("engine,prec", [("plain", 64), ("tiled", 32)])
+@pytest.mark.parametrize("axis", [0, 1])
+def test_vacuum_pulse_leaves_through_the_pml(osg, engine, prec, axis):
+    nl, dx = 128, [0.2, 0.2]
+    nx = [nl, 16] if axis == 0 else [16, nl]
+    dt = 0.9 / np.sqrt(sum(1 / d ** 2 for d in dx))
+    sim = osg.Simulation(nx, dx, dt, order=2, precision=prec,
+                         engine=osg.ENGINE_PLAIN if engine == "plain" else osg.ENGINE_TILED,
+                         tile=([16, 8] if axis == 0 else [8, 16]) if engine == "tiled" else None,
+                         pml=1 << axis)
+    gl, gu = osg.GUARD[2]
+    dtype = np.float32 if prec == 32 else np.float64
+    shape = tuple(reversed([n + gl + gu for n in nx])) + (3,)
+    e, b = np.zeros(shape, dtype), np.zeros(shape, dtype)
+    L = nl * dx[axis]
+    i = np.arange(shape[1 - axis]) - gl
+    prof = lambda x: np.exp(-((x - 0.5 * L) / (0.08 * L)) ** 2)
+    if axis == 0:   # Ey, Bz travelling along +x1
+        e[:, :, 1] = prof(i * dx[0])[None, :]
+        b[:, :, 2] = prof((i + 0.5) * dx[0])[None, :]
+    else:           # Ex, -Bz travelling along +x2
+        e[:, :, 0] = prof(i * dx[1])[:, None]
+        b[:, :, 2] = -prof((i + 0.5) * dx[1])[:, None]
+    sim.set_fields(e, b)
+    empty = np.zeros((0, 2), np.int32), np.zeros((0, 2), dtype), np.zeros((0, 3), dtype), \
+        np.zeros(0, dtype)
+    sim.add_species(-1.0, *empty)
+
+    def energy(fe, fb):
+        sl = (slice(gl, gl + nx[1]), slice(gl, gl + nx[0]))
+        return float((fe[sl].astype(np.float64) ** 2).sum() + (fb[sl].astype(np.float64) ** 2).sum())
+
+    w0 = energy(e, b)
+    sim.step(int(L / dt))
+    e1, b1, _ = sim.fields()
+    assert energy(e1, b1) / w0 < 1e-4
+    sim.close()
+
+
+def test_checkpoint_keeps_the_pml_walls(osg, oracle, tmp_path):
+    nx = [20, 16]
+    p, g, dx, dt, species, e, b = _setup(oracle, 64, 2, 2, nx, [2, 2], 4, uth=0.6, ufl=0.1)
+
+    def fresh():
+        sim = osg.Simulation(nx, dx, dt, order=2, precision=64, engine=osg.ENGINE_PLAIN,
+                             pml=2)
+        sim.set_fields(e, b)
+        for s in species:
+            sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
+        return sim
+
+    ref = fresh()
+    ref.step(8)
+    want = ref.fields()[:2], ref.species(0)
+    ref.close()
+    a = fresh()
+    a.step(4)
+    a.checkpoint(tmp_path / "pml.ckpt")
+    a.close()
+    c = osg.Simulation.restore(tmp_path / "pml.ckpt")
+    assert c.cfg.pml == 2
+    c.step(4)
+    got = c.fields()[:2], c.species(0)
+    c.close()
+    for x, y in zip(got[0], want[0]):
+        assert _nerr(x, y) <= 1e-12
+    (ia, xa, ua, qa), (ib, xb, ub, qb) = got[1], want[1]
+    assert np.array_equal(qa, qb)
+    assert _nerr(ia + xa, ib + xb) <= 1e-12 and _nerr(ua, ub) <= 1e-12
+
+
+@pytest.mark.parametrize("kw", [dict(pml=3), dict(pml=1, walls=2), dict(pml=1, open_fields=2),
+                                dict(pml=1, pml_cells=4), dict(pml=1, smooth_type=2,
+                                                               smooth_order=1)])
+def test_pml_refuses_what_it_is_not_built_for(osg, kw):
+    with pytest.raises(osg.OsirisGB300Error):
+        osg.Simulation([16, 16], [0.1, 0.1], 0.03, order=2, precision=64,
+                       engine=osg.ENGINE_PLAIN, **kw)
+
+
+def test_pml_is_2d(osg):
+    with pytest.raises(osg.OsirisGB300Error):
+        osg.Simulation([8, 8, 8], [0.1] * 3, 0.03, order=2, precision=64,
+                       engine=osg.ENGINE_PLAIN, pml=1)
