@@ -480,317 +480,397 @@ void FN(ora_lindman_phase)(int dim, const int *nx, const int *gcl, const int *gc
         FN(lind_restore)(g, d, e, b, st);
 }
 
-/* PML (Vay's perfectly matched layer, "vpml") at both edges of axis d of a 2D box, restated
- * from source/emf/boundary/os-emf-vpml.f03 for one PML axis (no corners, no diffusion
- * correction, Cartesian).  Each edge holds a wall of nb cells (vpml_bnd_size, default 8,
- * source/emf/boundary/os-emf-boundary.f90:30) along d, range [2 - nb, 1] below and
- * [nx + 1, nx + nb] above (setup_vpml :361-368: two cells of overlap with the grid), over
- * [1 - g1, nt + g2] along the other axis t (g1 = max(gcl_t, 1), g2 = max(gcu_t, 2), new_wall,
- * source/vdf/os-wall.f90:188-195 with corner 2).  A wall point carries four split components
+/* PML (Vay's perfectly matched layer, "vpml") at both edges of the axes in a mask of a 2D box,
+ * restated from source/emf/boundary/os-emf-vpml.f03 (Cartesian, no diffusion correction).
+ * Each PML edge holds a wall of nb cells (vpml_bnd_size, default 8, source/emf/boundary/
+ * os-emf-boundary.f90:30) along its axis a, range [2 - nb, 1] below and [nx + 1, nx + nb]
+ * above (setup_vpml :361-368: two cells of overlap with the box), over [1 - g1, nt + g2] along
+ * the other axis t (new_wall, source/vdf/os-wall.f90:188-195): g1 = max(gcl_t, c - 1),
+ * g2 = max(gcu_t, c) with c = nb for the x1 walls when x2 has PML walls too (they cover the
+ * corners, setup_vpml :382-398), else 2.  A wall point carries four split components
  * (:440-443): 0 X, 1 Y, 2 ZX (the z part driven by x1 derivatives), 3 ZY (by x2 derivatives).
  *
- * State layout (shared with the device engine): wall (side, field) with side 0 lower, 1 upper
- * and field 0 E, 1 B at offset (2 side + field) * W, W = nte * nb * 4 reals, nte = nt + g1 + g2;
- * point (iw, it) component c at 4 ((it - 1 + g1) nb + (iw - range_lo(side))) + c.  Then the
- * attenuation tables at 4 W: table k (0 E lower, 1 E upper, 2 B lower, 3 B upper) entry
- * (coef m = 0..2, cell n = 1..nb) at 4 W + (k * 3 + m) * nb + n - 1.
+ * State layout (shared with the device engine): per PML axis a in increasing order, walls
+ * (side, field), side 0 lower, 1 upper, field 0 E, 1 B, at base_a + (2 side + field) W_a,
+ * W_a = nte_a nb 4 reals, nte_a = nt + g1 + g2; point (iw, it) component c at
+ * 4 ((it - 1 + g1) nb + (iw - lo(side))) + c.  Then the attenuation tables of both axes: axis a,
+ * table k (0 E lower, 1 E upper, 2 B lower, 3 B upper), coefficient m (0..2) of wall cell n
+ * (1..nb) at T + ((4 a + k) 3 + m) nb + n - 1, T the walls' total.
  *
- * Per step: the walls' own periodic update along t at the guard update (update_boundary_vpml
- * :506-524, update_periodic_wall, source/vdf/os-wall-comm.f90:182-344); after the first B half
- * step the E walls advance (update_e_vpml_2d :598-722, after the B interfaces); after the E step
- * the B walls advance (update_b_vpml_2d :1742-1861, after the E interfaces); nothing after the
- * second B half step (source/emf/boundary/os-emf-boundary.f90:931-935, 1071-1074). */
-static int FN(step_pml) = -1, FN(step_pml_nb) = 0;
+ * Per step: the walls' own periodic update along a periodic t at the guard update
+ * (update_boundary_vpml :506-524, update_periodic_wall, source/vdf/os-wall-comm.f90:182-344);
+ * after the first B half step the E walls advance (update_e_vpml_2d :598-722: first the
+ * interfaces of every wall in setup order -- x1 lower, x1 upper, x2 lower, x2 upper -- then the
+ * wall updates); after the E step the B walls likewise (update_b_vpml_2d :1742-1861); nothing
+ * after the second B half step (source/emf/boundary/os-emf-boundary.f90:931-935, 1071-1074). */
+static int FN(step_pml) = 0, FN(step_pml_nb) = 0;
 static R *FN(step_pml_st) = 0;
-void FN(ora_set_pml)(int axis, int nb, R *state)
+void FN(ora_set_pml)(int mask, int nb, R *state)
 {
-    FN(step_pml) = axis;
+    FN(step_pml) = mask;
     FN(step_pml_nb) = nb;
     FN(step_pml_st) = state;
 }
 
 typedef struct {
-    int d, t, nn, nt, nb, g1, g2, nte;
-    long W;
+    int mask, nb, nx[2];
+    int g1[2], g2[2], nte[2];   /* per wall axis a */
+    long W[2], base[2], T;
 } FN(pml_desc);
 
-static FN(pml_desc) FN(pml_make)(const FN(ora_grid) *g, int d, int nb)
+static FN(pml_desc) FN(pml_make)(const FN(ora_grid) *g, int mask, int nb)
 {
     FN(pml_desc) P;
-    P.d = d;
-    P.t = 1 - d;
-    P.nn = g->nx[d];
-    P.nt = g->nx[P.t];
+    P.mask = mask;
     P.nb = nb;
-    P.g1 = g->gcl[P.t] > 1 ? g->gcl[P.t] : 1;
-    P.g2 = g->gcu[P.t] > 2 ? g->gcu[P.t] : 2;
-    P.nte = P.nt + P.g1 + P.g2;
-    P.W = (long)P.nte * nb * 4;
+    long off = 0;
+    for (int a = 0; a < 2; a++) {
+        const int t = 1 - a;
+        P.nx[a] = g->nx[a];
+        const int c = (a == 0 && ((mask >> 1) & 1)) ? nb : 2;
+        P.g1[a] = g->gcl[t] > c - 1 ? g->gcl[t] : c - 1;
+        P.g2[a] = g->gcu[t] > c ? g->gcu[t] : c;
+        P.nte[a] = g->nx[t] + P.g1[a] + P.g2[a];
+        P.W[a] = (long)P.nte[a] * nb * 4;
+        P.base[a] = off;
+        if ((mask >> a) & 1) off += 4 * P.W[a];
+    }
+    P.T = off;
     return P;
 }
 
-long FN(ora_pml_state_size)(int dim, const int *nx, const int *gcl, const int *gcu, int d, int nb)
+long FN(ora_pml_state_size)(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb)
 {
     FN(ora_grid) G;
     FN(grid_init)(&G, dim, nx, gcl, gcu);
-    const FN(pml_desc) P = FN(pml_make)(&G, d, nb);
-    return 4 * P.W + 12L * nb;
+    const FN(pml_desc) P = FN(pml_make)(&G, mask, nb);
+    return P.T + 24L * nb;
 }
 
-static inline int FN(pml_lo)(const FN(pml_desc) *P, int side)
+static inline int FN(pml_lo)(const FN(pml_desc) *P, int a, int side)
 {
-    return side == 0 ? 2 - P->nb : P->nn + 1;
+    return side == 0 ? 2 - P->nb : P->nx[a] + 1;
 }
 
-/* wall (side, field) value of component c at wall-normal iw and transverse it */
-#define PW(side, fld, c, iw, it)                                                               \
-    st[(2 * (side) + (fld)) * P.W +                                                           \
-       4 * ((long)((it) - 1 + P.g1) * P.nb + ((iw) - FN(pml_lo)(&P, side))) + (c)]
-/* the same addressed by (i1, i2) of the box: iw along d, it along t */
-#define PWX(side, fld, c, i1, i2)                                                              \
-    PW(side, fld, c, P.d == 0 ? (i1) : (i2), P.d == 0 ? (i2) : (i1))
-#define PCOEF(k, m, n) st[4 * P.W + ((k) * 3 + (m)) * P.nb + (n) - 1]
+/* component c of wall (a, side, fld) at box coordinates (i1, i2) (iw along a, it along t) */
+#define PWX(a, side, fld, c, i1, i2)                                                           \
+    st[P.base[a] + (2 * (side) + (fld)) * P.W[a] +                                            \
+       4 * ((long)(((a) == 0 ? (i2) : (i1)) - 1 + P.g1[a]) * P.nb +                           \
+            (((a) == 0 ? (i1) : (i2)) - FN(pml_lo)(&P, a, side))) + (c)]
+#define PCOEF(a, k, m, n) st[P.T + ((4 * (a) + (k)) * 3 + (m)) * P.nb + (n) - 1]
 
 /* attenuation tables (setup_att_coeff :3586-3684), computed in double and stored in R:
  * t(x) = exp(s1 (s2 x)^4), s1 = -0.8 (n + 1) / 2 with n = 4, s2 = 1 / (nb - 3); the power is
  * taken as an integer power (the reference's exponent is the real constant 4.0, whose base is
- * negative at the interface point) */
-void FN(ora_pml_init)(int dim, const int *nx, const int *gcl, const int *gcu, int d, int nb,
+ * negative at the interface point of the lower edge).  Tables of both axes are kept. */
+void FN(ora_pml_init)(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
                       const double *dx, double dt, R *st)
 {
     FN(ora_grid) G, *g = &G;
     FN(grid_init)(g, dim, nx, gcl, gcu);
-    const FN(pml_desc) P = FN(pml_make)(g, d, nb);
-    for (long i = 0; i < 4 * P.W + 12L * nb; i++) st[i] = K(0.0);
+    const FN(pml_desc) P = FN(pml_make)(g, mask, nb);
+    for (long i = 0; i < P.T + 24L * nb; i++) st[i] = K(0.0);
     const double s1 = -(0.8 * (4.0 + 1.0)) / 2.0, s2 = 1.0 / (nb - 3);
-    const double dtdx = dt / dx[d], dif = (1.0 - dtdx) / (1.0 + dtdx);
 #define ATT(x) exp(s1 * ((s2 * (x)) * (s2 * (x))) * ((s2 * (x)) * (s2 * (x))))
-    for (int j = 0; j < nb; j++) {
-        /* lower edge: B is the outer point; j = -1/2 is the interface */
-        double tj = ATT(j - 0.5), tj12 = ATT((double)j), tj1 = ATT(j + 0.5);
-        double b1e = dtdx * (1.0 + dif * (1.0 - tj12)), b1b = dtdx * (1.0 + dif * (1.0 - tj1));
-        PCOEF(0, 0, nb - j) = (R)(1.0 - b1e + tj12 * dtdx);
-        PCOEF(0, 1, nb - j) = (R)(tj * b1e);
-        PCOEF(0, 2, nb - j) = (R)dtdx;
-        PCOEF(2, 0, nb - j) = (R)(1.0 - b1b + tj1 * dtdx);
-        PCOEF(2, 1, nb - j) = (R)(tj12 * b1b);
-        PCOEF(2, 2, nb - j) = (R)dtdx;
-        /* upper edge: E is the outer point; j = 0 is the interface */
-        tj = ATT((double)j);
-        tj12 = ATT(j + 0.5);
-        tj1 = ATT(j + 1.0);
-        b1e = dtdx * (1.0 + dif * (1.0 - tj12));
-        b1b = dtdx * (1.0 + dif * (1.0 - tj1));
-        PCOEF(1, 0, j + 1) = (R)(1.0 - b1e + tj12 * dtdx);
-        PCOEF(1, 1, j + 1) = (R)dtdx;
-        PCOEF(1, 2, j + 1) = (R)(tj * b1e);
-        PCOEF(3, 0, j + 1) = (R)(1.0 - b1b + tj1 * dtdx);
-        PCOEF(3, 1, j + 1) = (R)dtdx;
-        PCOEF(3, 2, j + 1) = (R)(tj12 * b1b);
+    for (int a = 0; a < 2; a++) {
+        const double dtdx = dt / dx[a], dif = (1.0 - dtdx) / (1.0 + dtdx);
+        for (int j = 0; j < nb; j++) {
+            /* lower edge: B is the outer point; j = -1/2 is the interface */
+            double tj = ATT(j - 0.5), tj12 = ATT((double)j), tj1 = ATT(j + 0.5);
+            double b1e = dtdx * (1.0 + dif * (1.0 - tj12)), b1b = dtdx * (1.0 + dif * (1.0 - tj1));
+            PCOEF(a, 0, 0, nb - j) = (R)(1.0 - b1e + tj12 * dtdx);
+            PCOEF(a, 0, 1, nb - j) = (R)(tj * b1e);
+            PCOEF(a, 0, 2, nb - j) = (R)dtdx;
+            PCOEF(a, 2, 0, nb - j) = (R)(1.0 - b1b + tj1 * dtdx);
+            PCOEF(a, 2, 1, nb - j) = (R)(tj12 * b1b);
+            PCOEF(a, 2, 2, nb - j) = (R)dtdx;
+            /* upper edge: E is the outer point; j = 0 is the interface */
+            tj = ATT((double)j);
+            tj12 = ATT(j + 0.5);
+            tj1 = ATT(j + 1.0);
+            b1e = dtdx * (1.0 + dif * (1.0 - tj12));
+            b1b = dtdx * (1.0 + dif * (1.0 - tj1));
+            PCOEF(a, 1, 0, j + 1) = (R)(1.0 - b1e + tj12 * dtdx);
+            PCOEF(a, 1, 1, j + 1) = (R)dtdx;
+            PCOEF(a, 1, 2, j + 1) = (R)(tj * b1e);
+            PCOEF(a, 3, 0, j + 1) = (R)(1.0 - b1b + tj1 * dtdx);
+            PCOEF(a, 3, 1, j + 1) = (R)dtdx;
+            PCOEF(a, 3, 2, j + 1) = (R)(tj12 * b1b);
+        }
     }
 #undef ATT
 }
 
-/* interface of both walls with the box for field fld (0 E, 1 B) (update_interface_x1_2d
- * :2880-2993 without the corner contacts, update_interface_x2_2d :3190-3248): the box's point
- * next to the wall's inner end goes into the wall (ZX takes the box's z, ZY 0), and the wall's
- * point one cell further out goes into the box (z = ZX + ZY), for it = 0 .. nt + 2 */
-static void FN(pml_iface)(const FN(ora_grid) *g, const FN(pml_desc) *Pp, R *st, R *f, int fld)
+/* interfaces of the walls of axis a with the box for field fld (0 E, 1 B)
+ * (update_interface_x1_2d :2880-2993, update_interface_x2_2d :3190-3248): the box's point next
+ * to the wall's inner end goes into the wall (ZX takes the box's z, ZY 0), and the wall's point
+ * one cell further out goes into the box (z = ZX + ZY), for it = 0 .. nt + 2; then, for the x1
+ * walls, the contact columns with the x2 walls over the corner rows (:2945-2988) */
+static void FN(pml_iface)(const FN(ora_grid) *g, const FN(pml_desc) *Pp, R *st, R *f, int fld,
+                          int a)
 {
     const FN(pml_desc) P = *Pp;
+    const int t = 1 - a, nt = P.nx[t];
     for (int side = 0; side < 2; side++) {
-        const int lo = FN(pml_lo)(&P, side), hi = lo + P.nb - 1;
+        const int lo = FN(pml_lo)(&P, a, side), hi = lo + P.nb - 1;
         const int to_w = side == 0 ? hi : lo, to_b = side == 0 ? hi - 1 : lo + 1;
-        for (int it = 0; it <= P.nt + 2; it++) {
-            int ic[3] = {1, 1, 1};
-            ic[P.d] = to_w;
-            ic[P.t] = it;
-            for (int c = 0; c < 3; c++) PW(side, fld, c, to_w, it) = f[FN(gidx)(g, c, ic[0], ic[1], 1)];
-            PW(side, fld, 3, to_w, it) = K(0.0);
+        for (int it = 0; it <= nt + 2; it++) {
+            const int w1 = a == 0 ? to_w : it, w2 = a == 0 ? it : to_w;
+            for (int c = 0; c < 3; c++) PWX(a, side, fld, c, w1, w2) = f[FN(gidx)(g, c, w1, w2, 1)];
+            PWX(a, side, fld, 3, w1, w2) = K(0.0);
         }
-        for (int it = 0; it <= P.nt + 2; it++) {
-            int ic[3] = {1, 1, 1};
-            ic[P.d] = to_b;
-            ic[P.t] = it;
-            f[FN(gidx)(g, 0, ic[0], ic[1], 1)] = PW(side, fld, 0, to_b, it);
-            f[FN(gidx)(g, 1, ic[0], ic[1], 1)] = PW(side, fld, 1, to_b, it);
-            f[FN(gidx)(g, 2, ic[0], ic[1], 1)] = PW(side, fld, 2, to_b, it) + PW(side, fld, 3, to_b, it);
+        for (int it = 0; it <= nt + 2; it++) {
+            const int b1 = a == 0 ? to_b : it, b2 = a == 0 ? it : to_b;
+            f[FN(gidx)(g, 0, b1, b2, 1)] = PWX(a, side, fld, 0, b1, b2);
+            f[FN(gidx)(g, 1, b1, b2, 1)] = PWX(a, side, fld, 1, b1, b2);
+            f[FN(gidx)(g, 2, b1, b2, 1)] = PWX(a, side, fld, 2, b1, b2) + PWX(a, side, fld, 3, b1, b2);
+        }
+        if (a == 0 && ((P.mask >> 1) & 1)) {
+            for (int adj = 0; adj < 2; adj++) {
+                /* the x2 wall below (rows 2 - nb .. 0) or above (nx2 + 2 .. nx2 + nb) */
+                const int r0 = adj == 0 ? 2 - P.nb : P.nx[1] + 2;
+                const int r1 = adj == 0 ? 0 : P.nx[1] + P.nb;
+                for (int i2 = r0; i2 <= r1; i2++)
+                    for (int c = 0; c < 4; c++) {
+                        if (side == 0) {
+                            PWX(1, adj, fld, c, 0, i2) = PWX(0, 0, fld, c, 0, i2);
+                            PWX(0, 0, fld, c, 1, i2) = PWX(1, adj, fld, c, 1, i2);
+                        } else {
+                            const int i1 = P.nx[0] + 1;
+                            PWX(0, 1, fld, c, i1, i2) = PWX(1, adj, fld, c, i1, i2);
+                            PWX(1, adj, fld, c, i1 + 1, i2) = PWX(0, 1, fld, c, i1 + 1, i2);
+                        }
+                    }
+            }
         }
     }
 }
 
-/* the E walls (update_e_x1_2d :925-1048, update_e_x2_2d :1369-1456, non-corner branches) */
-static void FN(pml_e)(const FN(pml_desc) *Pp, R *st, const double *dx, double dt)
+/* the E walls of axis a (update_e_x1_2d :925-1048 with its corner branch, update_e_x2_2d
+ * :1369-1456) */
+static void FN(pml_e)(const FN(pml_desc) *Pp, R *st, const double *dx, double dt, int a)
 {
     const FN(pml_desc) P = *Pp;
-    const R dtdx = (R)(dt / dx[P.t]);
+    const int t = 1 - a, nt = P.nx[t];
+    const R dtdx = (R)(dt / dx[t]);
+    const int cor = a == 0 && ((P.mask >> 1) & 1);
     for (int side = 0; side < 2; side++) {
-        const int lo = FN(pml_lo)(&P, side), hi = lo + P.nb - 1;
+        const int lo = FN(pml_lo)(&P, a, side), hi = lo + P.nb - 1;
         const int r0 = lo + 1, r1 = side == 0 ? hi - 1 : hi;
         const int k = side == 0 ? 0 : 1, cofs = side == 0 ? lo - 1 : lo;
-        if (P.d == 0) {
-            for (int i2 = 2 - P.g1; i2 <= P.nt + P.g2; i2++)
+        if (a == 0) {
+            for (int i2 = 2 - P.g1[0]; i2 <= nt + P.g2[0]; i2++) {
+                /* corner rows (x2 walls below or above): damped along x2 as well */
+                int cn = 0, ck = 0;
+                if (cor && i2 <= 0) {
+                    cn = i2 + P.g1[0];
+                    ck = 0;
+                } else if (cor && i2 > nt + 1) {
+                    cn = i2 - nt - 1;
+                    ck = 1;
+                }
                 for (int i1 = r0; i1 <= r1; i1++) {
                     const int ci = i1 - cofs;
-                    const R c1 = PCOEF(k, 0, ci), c2 = PCOEF(k, 1, ci), c3 = PCOEF(k, 2, ci);
-                    PWX(side, 0, 0, i1, i2) = PWX(side, 0, 0, i1, i2) +
-                        dtdx * (PWX(side, 1, 2, i1, i2) + PWX(side, 1, 3, i1, i2) -
-                                PWX(side, 1, 2, i1, i2 - 1) - PWX(side, 1, 3, i1, i2 - 1));
-                    PWX(side, 0, 3, i1, i2) = PWX(side, 0, 3, i1, i2) -
-                        dtdx * (PWX(side, 1, 0, i1, i2) - PWX(side, 1, 0, i1, i2 - 1));
-                    PWX(side, 0, 1, i1, i2) = c1 * PWX(side, 0, 1, i1, i2) -
-                        c2 * (PWX(side, 1, 2, i1, i2) + PWX(side, 1, 3, i1, i2)) +
-                        c3 * (PWX(side, 1, 2, i1 - 1, i2) + PWX(side, 1, 3, i1 - 1, i2));
-                    PWX(side, 0, 2, i1, i2) = c1 * PWX(side, 0, 2, i1, i2) +
-                        c2 * PWX(side, 1, 1, i1, i2) - c3 * PWX(side, 1, 1, i1 - 1, i2);
+                    const R c1 = PCOEF(0, k, 0, ci), c2 = PCOEF(0, k, 1, ci), c3 = PCOEF(0, k, 2, ci);
+                    if (cn) {
+                        const R d1 = PCOEF(1, ck, 0, cn), d2 = PCOEF(1, ck, 1, cn), d3 = PCOEF(1, ck, 2, cn);
+                        PWX(0, side, 0, 0, i1, i2) = d1 * PWX(0, side, 0, 0, i1, i2) +
+                            d2 * (PWX(0, side, 1, 2, i1, i2) + PWX(0, side, 1, 3, i1, i2)) -
+                            d3 * (PWX(0, side, 1, 2, i1, i2 - 1) + PWX(0, side, 1, 3, i1, i2 - 1));
+                        PWX(0, side, 0, 3, i1, i2) = d1 * PWX(0, side, 0, 3, i1, i2) -
+                            d2 * PWX(0, side, 1, 0, i1, i2) + d3 * PWX(0, side, 1, 0, i1, i2 - 1);
+                    } else {
+                        PWX(0, side, 0, 0, i1, i2) = PWX(0, side, 0, 0, i1, i2) +
+                            dtdx * (PWX(0, side, 1, 2, i1, i2) + PWX(0, side, 1, 3, i1, i2) -
+                                    PWX(0, side, 1, 2, i1, i2 - 1) - PWX(0, side, 1, 3, i1, i2 - 1));
+                        PWX(0, side, 0, 3, i1, i2) = PWX(0, side, 0, 3, i1, i2) -
+                            dtdx * (PWX(0, side, 1, 0, i1, i2) - PWX(0, side, 1, 0, i1, i2 - 1));
+                    }
+                    PWX(0, side, 0, 1, i1, i2) = c1 * PWX(0, side, 0, 1, i1, i2) -
+                        c2 * (PWX(0, side, 1, 2, i1, i2) + PWX(0, side, 1, 3, i1, i2)) +
+                        c3 * (PWX(0, side, 1, 2, i1 - 1, i2) + PWX(0, side, 1, 3, i1 - 1, i2));
+                    PWX(0, side, 0, 2, i1, i2) = c1 * PWX(0, side, 0, 2, i1, i2) +
+                        c2 * PWX(0, side, 1, 1, i1, i2) - c3 * PWX(0, side, 1, 1, i1 - 1, i2);
                 }
+            }
         } else {
             /* the wall's lowest row: Y and ZX by the plain Yee update */
-            for (int i1 = 2 - P.g1; i1 <= P.nt + P.g2; i1++) {
+            for (int i1 = 2 - P.g1[1]; i1 <= nt + P.g2[1]; i1++) {
                 const int i2 = lo;
-                PWX(side, 0, 1, i1, i2) = PWX(side, 0, 1, i1, i2) -
-                    dtdx * (PWX(side, 1, 2, i1, i2) + PWX(side, 1, 3, i1, i2) -
-                            PWX(side, 1, 2, i1 - 1, i2) - PWX(side, 1, 3, i1 - 1, i2));
-                PWX(side, 0, 2, i1, i2) = PWX(side, 0, 2, i1, i2) +
-                    dtdx * (PWX(side, 1, 1, i1, i2) - PWX(side, 1, 1, i1 - 1, i2));
+                PWX(1, side, 0, 1, i1, i2) = PWX(1, side, 0, 1, i1, i2) -
+                    dtdx * (PWX(1, side, 1, 2, i1, i2) + PWX(1, side, 1, 3, i1, i2) -
+                            PWX(1, side, 1, 2, i1 - 1, i2) - PWX(1, side, 1, 3, i1 - 1, i2));
+                PWX(1, side, 0, 2, i1, i2) = PWX(1, side, 0, 2, i1, i2) +
+                    dtdx * (PWX(1, side, 1, 1, i1, i2) - PWX(1, side, 1, 1, i1 - 1, i2));
             }
             for (int i2 = r0; i2 <= r1; i2++) {
                 const int ci = i2 - cofs;
-                const R c1 = PCOEF(k, 0, ci), c2 = PCOEF(k, 1, ci), c3 = PCOEF(k, 2, ci);
-                for (int i1 = 2 - P.g1; i1 <= P.nt + P.g2; i1++) {
-                    PWX(side, 0, 0, i1, i2) = c1 * PWX(side, 0, 0, i1, i2) +
-                        c2 * (PWX(side, 1, 2, i1, i2) + PWX(side, 1, 3, i1, i2)) -
-                        c3 * (PWX(side, 1, 2, i1, i2 - 1) + PWX(side, 1, 3, i1, i2 - 1));
-                    PWX(side, 0, 1, i1, i2) = PWX(side, 0, 1, i1, i2) -
-                        dtdx * (PWX(side, 1, 2, i1, i2) + PWX(side, 1, 3, i1, i2) -
-                                PWX(side, 1, 2, i1 - 1, i2) - PWX(side, 1, 3, i1 - 1, i2));
-                    PWX(side, 0, 2, i1, i2) = PWX(side, 0, 2, i1, i2) +
-                        dtdx * (PWX(side, 1, 1, i1, i2) - PWX(side, 1, 1, i1 - 1, i2));
-                    PWX(side, 0, 3, i1, i2) = c1 * PWX(side, 0, 3, i1, i2) -
-                        c2 * PWX(side, 1, 0, i1, i2) + c3 * PWX(side, 1, 0, i1, i2 - 1);
+                const R c1 = PCOEF(1, k, 0, ci), c2 = PCOEF(1, k, 1, ci), c3 = PCOEF(1, k, 2, ci);
+                for (int i1 = 2 - P.g1[1]; i1 <= nt + P.g2[1]; i1++) {
+                    PWX(1, side, 0, 0, i1, i2) = c1 * PWX(1, side, 0, 0, i1, i2) +
+                        c2 * (PWX(1, side, 1, 2, i1, i2) + PWX(1, side, 1, 3, i1, i2)) -
+                        c3 * (PWX(1, side, 1, 2, i1, i2 - 1) + PWX(1, side, 1, 3, i1, i2 - 1));
+                    PWX(1, side, 0, 1, i1, i2) = PWX(1, side, 0, 1, i1, i2) -
+                        dtdx * (PWX(1, side, 1, 2, i1, i2) + PWX(1, side, 1, 3, i1, i2) -
+                                PWX(1, side, 1, 2, i1 - 1, i2) - PWX(1, side, 1, 3, i1 - 1, i2));
+                    PWX(1, side, 0, 2, i1, i2) = PWX(1, side, 0, 2, i1, i2) +
+                        dtdx * (PWX(1, side, 1, 1, i1, i2) - PWX(1, side, 1, 1, i1 - 1, i2));
+                    PWX(1, side, 0, 3, i1, i2) = c1 * PWX(1, side, 0, 3, i1, i2) -
+                        c2 * PWX(1, side, 1, 0, i1, i2) + c3 * PWX(1, side, 1, 0, i1, i2 - 1);
                 }
             }
         }
     }
 }
 
-/* the B walls (update_b_x1_2d :2066-2177, update_b_x2_2d :2512-2579, non-corner branches) */
-static void FN(pml_b)(const FN(pml_desc) *Pp, R *st, const double *dx, double dt)
+/* the B walls of axis a (update_b_x1_2d :2066-2177 with its corner branch, update_b_x2_2d
+ * :2512-2579) */
+static void FN(pml_b)(const FN(pml_desc) *Pp, R *st, const double *dx, double dt, int a)
 {
     const FN(pml_desc) P = *Pp;
-    const R dtdx = (R)(dt / dx[P.t]);
+    const int t = 1 - a, nt = P.nx[t];
+    const R dtdx = (R)(dt / dx[t]);
+    const int cor = a == 0 && ((P.mask >> 1) & 1);
     for (int side = 0; side < 2; side++) {
-        const int lo = FN(pml_lo)(&P, side), hi = lo + P.nb - 1;
+        const int lo = FN(pml_lo)(&P, a, side), hi = lo + P.nb - 1;
         const int r0 = side == 0 ? lo : lo + 1, r1 = hi - 1;
         const int k = side == 0 ? 2 : 3, cofs = side == 0 ? lo - 2 : lo;
-        if (P.d == 0) {
-            for (int i2 = 1 - P.g1; i2 <= P.nt + P.g2 - 1; i2++)
+        if (a == 0) {
+            for (int i2 = 1 - P.g1[0]; i2 <= nt + P.g2[0] - 1; i2++) {
+                int cn = 0, ck = 0;
+                if (cor && i2 <= 0) {
+                    cn = i2 + P.g1[0] + 1;
+                    ck = 2;
+                } else if (cor && i2 > nt + 1) {
+                    cn = i2 - nt - 1;
+                    ck = 3;
+                }
                 for (int i1 = r0; i1 <= r1; i1++) {
                     const int ci = i1 - cofs;
-                    const R c1 = PCOEF(k, 0, ci), c2 = PCOEF(k, 1, ci), c3 = PCOEF(k, 2, ci);
-                    PWX(side, 1, 0, i1, i2) = PWX(side, 1, 0, i1, i2) -
-                        dtdx * (PWX(side, 0, 2, i1, i2 + 1) + PWX(side, 0, 3, i1, i2 + 1) -
-                                PWX(side, 0, 2, i1, i2) - PWX(side, 0, 3, i1, i2));
-                    PWX(side, 1, 3, i1, i2) = PWX(side, 1, 3, i1, i2) +
-                        dtdx * (PWX(side, 0, 0, i1, i2 + 1) - PWX(side, 0, 0, i1, i2));
-                    PWX(side, 1, 1, i1, i2) = c1 * PWX(side, 1, 1, i1, i2) +
-                        c2 * (PWX(side, 0, 2, i1 + 1, i2) + PWX(side, 0, 3, i1 + 1, i2)) -
-                        c3 * (PWX(side, 0, 2, i1, i2) + PWX(side, 0, 3, i1, i2));
-                    PWX(side, 1, 2, i1, i2) = c1 * PWX(side, 1, 2, i1, i2) -
-                        c2 * PWX(side, 0, 1, i1 + 1, i2) + c3 * PWX(side, 0, 1, i1, i2);
+                    const R c1 = PCOEF(0, k, 0, ci), c2 = PCOEF(0, k, 1, ci), c3 = PCOEF(0, k, 2, ci);
+                    if (cn) {
+                        const R d1 = PCOEF(1, ck, 0, cn), d2 = PCOEF(1, ck, 1, cn), d3 = PCOEF(1, ck, 2, cn);
+                        PWX(0, side, 1, 0, i1, i2) = d1 * PWX(0, side, 1, 0, i1, i2) -
+                            d2 * (PWX(0, side, 0, 2, i1, i2 + 1) + PWX(0, side, 0, 3, i1, i2 + 1)) +
+                            d3 * (PWX(0, side, 0, 2, i1, i2) + PWX(0, side, 0, 3, i1, i2));
+                        PWX(0, side, 1, 3, i1, i2) = d1 * PWX(0, side, 1, 3, i1, i2) +
+                            d2 * PWX(0, side, 0, 0, i1, i2 + 1) - d3 * PWX(0, side, 0, 0, i1, i2);
+                    } else {
+                        PWX(0, side, 1, 0, i1, i2) = PWX(0, side, 1, 0, i1, i2) -
+                            dtdx * (PWX(0, side, 0, 2, i1, i2 + 1) + PWX(0, side, 0, 3, i1, i2 + 1) -
+                                    PWX(0, side, 0, 2, i1, i2) - PWX(0, side, 0, 3, i1, i2));
+                        PWX(0, side, 1, 3, i1, i2) = PWX(0, side, 1, 3, i1, i2) +
+                            dtdx * (PWX(0, side, 0, 0, i1, i2 + 1) - PWX(0, side, 0, 0, i1, i2));
+                    }
+                    PWX(0, side, 1, 1, i1, i2) = c1 * PWX(0, side, 1, 1, i1, i2) +
+                        c2 * (PWX(0, side, 0, 2, i1 + 1, i2) + PWX(0, side, 0, 3, i1 + 1, i2)) -
+                        c3 * (PWX(0, side, 0, 2, i1, i2) + PWX(0, side, 0, 3, i1, i2));
+                    PWX(0, side, 1, 2, i1, i2) = c1 * PWX(0, side, 1, 2, i1, i2) -
+                        c2 * PWX(0, side, 0, 1, i1 + 1, i2) + c3 * PWX(0, side, 0, 1, i1, i2);
                 }
+            }
         } else {
             for (int i2 = r0; i2 <= r1; i2++) {
                 const int ci = i2 - cofs;
-                const R c1 = PCOEF(k, 0, ci), c2 = PCOEF(k, 1, ci), c3 = PCOEF(k, 2, ci);
-                for (int i1 = 1 - P.g1; i1 <= P.nt + P.g2 - 1; i1++) {
-                    PWX(side, 1, 0, i1, i2) = c1 * PWX(side, 1, 0, i1, i2) -
-                        c2 * (PWX(side, 0, 2, i1, i2 + 1) + PWX(side, 0, 3, i1, i2 + 1)) +
-                        c3 * (PWX(side, 0, 2, i1, i2) + PWX(side, 0, 3, i1, i2));
-                    PWX(side, 1, 1, i1, i2) = PWX(side, 1, 1, i1, i2) +
-                        dtdx * (PWX(side, 0, 2, i1 + 1, i2) + PWX(side, 0, 3, i1 + 1, i2) -
-                                PWX(side, 0, 2, i1, i2) - PWX(side, 0, 3, i1, i2));
-                    PWX(side, 1, 2, i1, i2) = PWX(side, 1, 2, i1, i2) -
-                        dtdx * (PWX(side, 0, 1, i1 + 1, i2) - PWX(side, 0, 1, i1, i2));
-                    PWX(side, 1, 3, i1, i2) = c1 * PWX(side, 1, 3, i1, i2) +
-                        c2 * PWX(side, 0, 0, i1, i2 + 1) - c3 * PWX(side, 0, 0, i1, i2);
+                const R c1 = PCOEF(1, k, 0, ci), c2 = PCOEF(1, k, 1, ci), c3 = PCOEF(1, k, 2, ci);
+                for (int i1 = 1 - P.g1[1]; i1 <= nt + P.g2[1] - 1; i1++) {
+                    PWX(1, side, 1, 0, i1, i2) = c1 * PWX(1, side, 1, 0, i1, i2) -
+                        c2 * (PWX(1, side, 0, 2, i1, i2 + 1) + PWX(1, side, 0, 3, i1, i2 + 1)) +
+                        c3 * (PWX(1, side, 0, 2, i1, i2) + PWX(1, side, 0, 3, i1, i2));
+                    PWX(1, side, 1, 1, i1, i2) = PWX(1, side, 1, 1, i1, i2) +
+                        dtdx * (PWX(1, side, 0, 2, i1 + 1, i2) + PWX(1, side, 0, 3, i1 + 1, i2) -
+                                PWX(1, side, 0, 2, i1, i2) - PWX(1, side, 0, 3, i1, i2));
+                    PWX(1, side, 1, 2, i1, i2) = PWX(1, side, 1, 2, i1, i2) -
+                        dtdx * (PWX(1, side, 0, 1, i1 + 1, i2) - PWX(1, side, 0, 1, i1, i2));
+                    PWX(1, side, 1, 3, i1, i2) = c1 * PWX(1, side, 1, 3, i1, i2) +
+                        c2 * PWX(1, side, 0, 0, i1, i2 + 1) - c3 * PWX(1, side, 0, 0, i1, i2);
                 }
             }
             /* the wall's highest row: Y and ZX by the plain Yee update */
-            for (int i1 = 1 - P.g1; i1 <= P.nt + P.g2 - 1; i1++) {
+            for (int i1 = 1 - P.g1[1]; i1 <= nt + P.g2[1] - 1; i1++) {
                 const int i2 = hi;
-                PWX(side, 1, 1, i1, i2) = PWX(side, 1, 1, i1, i2) +
-                    dtdx * (PWX(side, 0, 2, i1 + 1, i2) + PWX(side, 0, 3, i1 + 1, i2) -
-                            PWX(side, 0, 2, i1, i2) - PWX(side, 0, 3, i1, i2));
-                PWX(side, 1, 2, i1, i2) = PWX(side, 1, 2, i1, i2) -
-                    dtdx * (PWX(side, 0, 1, i1 + 1, i2) - PWX(side, 0, 1, i1, i2));
+                PWX(1, side, 1, 1, i1, i2) = PWX(1, side, 1, 1, i1, i2) +
+                    dtdx * (PWX(1, side, 0, 2, i1 + 1, i2) + PWX(1, side, 0, 3, i1 + 1, i2) -
+                            PWX(1, side, 0, 2, i1, i2) - PWX(1, side, 0, 3, i1, i2));
+                PWX(1, side, 1, 2, i1, i2) = PWX(1, side, 1, 2, i1, i2) -
+                    dtdx * (PWX(1, side, 0, 1, i1 + 1, i2) - PWX(1, side, 0, 1, i1, i2));
             }
         }
     }
 }
 
-/* the walls' periodic update along t: guard points from the opposite interior points, all
- * four components, over the whole wall-normal range */
+/* the walls' periodic update along t, when t is periodic (no PML walls along it): guard points
+ * from the opposite interior points, all four components, the whole wall-normal range */
 static void FN(pml_wall_guards)(const FN(pml_desc) *Pp, R *st)
 {
     const FN(pml_desc) P = *Pp;
-    for (int side = 0; side < 2; side++) {
-        const int lo = FN(pml_lo)(&P, side);
-        for (int fld = 0; fld < 2; fld++)
-            for (int iw = lo; iw < lo + P.nb; iw++)
-                for (int c = 0; c < 4; c++) {
-                    for (int it = 1 - P.g1; it <= 0; it++)
-                        PW(side, fld, c, iw, it) = PW(side, fld, c, iw, it + P.nt);
-                    for (int it = P.nt + 1; it <= P.nt + P.g2; it++)
-                        PW(side, fld, c, iw, it) = PW(side, fld, c, iw, it - P.nt);
-                }
+    for (int a = 0; a < 2; a++) {
+        const int t = 1 - a, nt = P.nx[t];
+        if (!((P.mask >> a) & 1) || ((P.mask >> t) & 1)) continue;
+        for (int side = 0; side < 2; side++) {
+            const int lo = FN(pml_lo)(&P, a, side);
+            for (int fld = 0; fld < 2; fld++)
+                for (int iw = lo; iw < lo + P.nb; iw++)
+                    for (int c = 0; c < 4; c++) {
+                        for (int it = 1 - P.g1[a]; it <= 0; it++) {
+                            if (a == 0) PWX(0, side, fld, c, iw, it) = PWX(0, side, fld, c, iw, it + nt);
+                            else PWX(1, side, fld, c, it, iw) = PWX(1, side, fld, c, it + nt, iw);
+                        }
+                        for (int it = nt + 1; it <= nt + P.g2[a]; it++) {
+                            if (a == 0) PWX(0, side, fld, c, iw, it) = PWX(0, side, fld, c, iw, it - nt);
+                            else PWX(1, side, fld, c, it, iw) = PWX(1, side, fld, c, it - nt, iw);
+                        }
+                    }
+        }
     }
 }
 
 /* one PML phase (what 0: the walls' guard update, 1: E walls after the first B half step,
- * interfaces with B included, 2: B walls after the E step, interfaces with E included) */
-void FN(ora_pml_phase)(int dim, const int *nx, const int *gcl, const int *gcu, int d, int nb,
+ * interfaces with B first, 2: B walls after the E step, interfaces with E first) */
+void FN(ora_pml_phase)(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
                        int what, R *e, R *b, R *st, const double *dx, double dt)
 {
     FN(ora_grid) G, *g = &G;
     FN(grid_init)(g, dim, nx, gcl, gcu);
-    const FN(pml_desc) P = FN(pml_make)(g, d, nb);
+    const FN(pml_desc) P = FN(pml_make)(g, mask, nb);
     if (what == 0) {
         FN(pml_wall_guards)(&P, st);
-    } else if (what == 1) {
-        FN(pml_iface)(g, &P, st, b, 1);
-        FN(pml_e)(&P, st, dx, dt);
-    } else {
-        FN(pml_iface)(g, &P, st, e, 0);
-        FN(pml_b)(&P, st, dx, dt);
+        return;
+    }
+    for (int a = 0; a < 2; a++)
+        if ((mask >> a) & 1) FN(pml_iface)(g, &P, st, what == 1 ? b : e, what == 1 ? 1 : 0, a);
+    for (int a = 0; a < 2; a++) {
+        if (!((mask >> a) & 1)) continue;
+        if (what == 1) FN(pml_e)(&P, st, dx, dt, a);
+        else FN(pml_b)(&P, st, dx, dt, a);
     }
 }
-#undef PW
 #undef PWX
 #undef PCOEF
 
-/* the Yee advance with PML walls on axis d */
+/* the Yee advance with PML walls on the axes in mask */
 void FN(ora_yee_advance_pml)(int dim, const int *nx, const int *gcl, const int *gcu, R *e, R *b,
-                             const R *j, const double *dx, double dt, int d, int nb, R *st)
+                             const R *j, const double *dx, double dt, int mask, int nb, R *st)
 {
     FN(ora_grid) G, *g = &G;
     FN(grid_init)(g, dim, nx, gcl, gcu);
     FN(dbdt)(g, b, e, dx, dt / 2.0);
-    FN(ora_pml_phase)(dim, nx, gcl, gcu, d, nb, 1, e, b, st, dx, dt);
+    FN(ora_pml_phase)(dim, nx, gcl, gcu, mask, nb, 1, e, b, st, dx, dt);
     FN(dedt)(g, e, b, j, dx, dt);
-    FN(ora_pml_phase)(dim, nx, gcl, gcu, d, nb, 2, e, b, st, dx, dt);
+    FN(ora_pml_phase)(dim, nx, gcl, gcu, mask, nb, 2, e, b, st, dx, dt);
     FN(dbdt)(g, b, e, dx, dt / 2.0);
 }
 
-/* guard update of E and B with PML walls on axis d: the walls' own periodic update, then the
- * box periodic along the other axis only (along d its guard points keep what the interfaces
- * and the Yee steps left there, update_boundary_emf_bound, os-emf-boundary.f90:760-820) */
+/* guard update of E and B with PML walls on the axes in mask: the walls' own periodic update,
+ * then the box periodic along the other axes only (along a PML axis its guard points keep what
+ * the interfaces and the Yee steps left there, update_boundary_emf_bound,
+ * source/emf/boundary/os-emf-boundary.f90:760-820) */
 void FN(ora_pml_guards)(int dim, const int *nx, const int *gcl, const int *gcu, R *e, R *b,
-                        int d, int nb, R *st)
+                        int mask, int nb, R *st)
 {
-    FN(ora_pml_phase)(dim, nx, gcl, gcu, d, nb, 0, e, b, st, 0, 0.0);
-    FN(ora_periodic_skip)(dim, nx, gcl, gcu, e, 0, 1 << d);
-    FN(ora_periodic_skip)(dim, nx, gcl, gcu, b, 0, 1 << d);
+    FN(ora_pml_phase)(dim, nx, gcl, gcu, mask, nb, 0, e, b, st, 0, 0.0);
+    FN(ora_periodic_skip)(dim, nx, gcl, gcu, e, 0, mask);
+    FN(ora_periodic_skip)(dim, nx, gcl, gcu, b, 0, mask);
 }
 
 /* absorbing particle boundary along axis d (p_bc_absorbing: a particle that left the box is

@@ -641,12 +641,12 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
     const int walls = step_walls_##SFXN;                                                      \
     const int oax = step_open_##SFXN; /* Lindman axis, -1: none */                            \
     const int win = step_window_##SFXN; /* moving window along x1 */                          \
-    const int pax = step_pml_##SFXN; /* PML axis, -1: none */                                 \
-    const int skip = walls | (oax >= 0 ? 1 << oax : 0) | (pax >= 0 ? 1 << pax : 0) | win;     \
+    const int pml = step_pml_##SFXN; /* PML axes (bit mask), 0: none */                      \
+    const int skip = walls | (oax >= 0 ? 1 << oax : 0) | pml | win;                           \
     if (oax >= 0) {                                                                           \
         ora_open_guards_##SFXN(dim, nx, gcl, gcu, e, b, oax, step_lind_##SFXN);               \
-    } else if (pax >= 0) {                                                                    \
-        ora_pml_guards_##SFXN(dim, nx, gcl, gcu, e, b, pax, step_pml_nb_##SFXN,               \
+    } else if (pml) {                                                                         \
+        ora_pml_guards_##SFXN(dim, nx, gcl, gcu, e, b, pml, step_pml_nb_##SFXN,               \
                               step_pml_st_##SFXN);                                            \
     } else {                                                                                  \
         ora_periodic_skip_##SFXN(dim, nx, gcl, gcu, e, 0, walls | win);                       \
@@ -688,8 +688,9 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
                                     step_ufl, step_seed, s, step_count, step_ttype);          \
         if (oax >= 0)                                                                         \
             ora_particle_absorb_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], q[s], oax);         \
-        if (pax >= 0)                                                                         \
-            ora_particle_absorb_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], q[s], pax);         \
+        for (int a = 0; a < dim; a++)                                                         \
+            if ((pml >> a) & 1)                                                               \
+                ora_particle_absorb_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], q[s], a);       \
         if (win) ora_particle_window_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], q[s]);        \
         ora_particle_bound_##SFXN(dim, nx, np[s], ix[s], x[s], u[s], walls);                  \
     }                                                                                         \
@@ -714,8 +715,8 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
     else if (oax >= 0)                                                                        \
         ora_yee_advance_open_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt, oax,                 \
                                     step_lind_##SFXN);                                        \
-    else if (pax >= 0)                                                                        \
-        ora_yee_advance_pml_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt, pax,                  \
+    else if (pml)                                                                             \
+        ora_yee_advance_pml_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt, pml,                  \
                                    step_pml_nb_##SFXN, step_pml_st_##SFXN);                   \
     else                                                                                      \
         ora_yee_advance_##SFXN(dim, nx, gcl, gcu, e, b, j, dx, dt);                           \

@@ -87,20 +87,23 @@ void ora_lindman_phase_f64(int dim, const int *nx, const int *gcl, const int *gc
                            double dt);
 void ora_set_open_f32(int axis, float *state);
 void ora_set_open_f64(int axis, double *state);
-/* PML walls at both edges of axis d of a 2D box (nb cells each); the state (walls and
- * attenuation tables) is ora_pml_state_size reals, set up by ora_pml_init */
-long ora_pml_state_size_f32(int dim, const int *nx, const int *gcl, const int *gcu, int d, int nb);
-long ora_pml_state_size_f64(int dim, const int *nx, const int *gcl, const int *gcu, int d, int nb);
-void ora_pml_init_f32(int dim, const int *nx, const int *gcl, const int *gcu, int d, int nb,
+/* PML walls of nb cells at both edges of the axes in mask of a 2D box (corners covered by
+ * the x1 walls); the state (walls and attenuation tables) is ora_pml_state_size reals, set up
+ * by ora_pml_init */
+long ora_pml_state_size_f32(int dim, const int *nx, const int *gcl, const int *gcu, int mask,
+                            int nb);
+long ora_pml_state_size_f64(int dim, const int *nx, const int *gcl, const int *gcu, int mask,
+                            int nb);
+void ora_pml_init_f32(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
                       const double *dx, double dt, float *st);
-void ora_pml_init_f64(int dim, const int *nx, const int *gcl, const int *gcu, int d, int nb,
+void ora_pml_init_f64(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
                       const double *dx, double dt, double *st);
-void ora_pml_phase_f32(int dim, const int *nx, const int *gcl, const int *gcu, int d, int nb,
+void ora_pml_phase_f32(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
                        int what, float *e, float *b, float *st, const double *dx, double dt);
-void ora_pml_phase_f64(int dim, const int *nx, const int *gcl, const int *gcu, int d, int nb,
+void ora_pml_phase_f64(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
                        int what, double *e, double *b, double *st, const double *dx, double dt);
-void ora_set_pml_f32(int axis, int nb, float *state);
-void ora_set_pml_f64(int axis, int nb, double *state);
+void ora_set_pml_f32(int mask, int nb, float *state);
+void ora_set_pml_f64(int mask, int nb, double *state);
 void ora_field_energy_f32(int dim, const int *nx, const int *gcl, const int *gcu,
                           const float *f, const double *dx, double *out);
 void ora_field_energy_f64(int dim, const int *nx, const int *gcl, const int *gcu,

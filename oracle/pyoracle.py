@@ -377,24 +377,24 @@ def lindman_phase(g: "Grid", prec, axis, what, e, b, state, dt):
                                                  _p(_f64(g.dx + [0.0] * 3)), float(dt))
 
 
-def pml_state(g: "Grid", prec, axis, nb, dt):
-    """State of PML walls of nb cells at both edges of `axis` (2D): zeroed walls and the
-    attenuation tables, kept by the caller between steps."""
+def pml_state(g: "Grid", prec, mask, nb, dt):
+    """State of PML walls of nb cells at both edges of the axes in `mask` (2D): zeroed walls
+    and the attenuation tables, kept by the caller between steps."""
     nx, gl, gu = g.args()
     L = lib()
-    n = getattr(L, f"ora_pml_state_size_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), int(axis),
+    n = getattr(L, f"ora_pml_state_size_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), int(mask),
                                                  int(nb))
     st = np.zeros(n, dtype=dtype_of(prec))
-    getattr(L, f"ora_pml_init_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), int(axis), int(nb),
+    getattr(L, f"ora_pml_init_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), int(mask), int(nb),
                                        _p(_f64(g.dx + [0.0] * 3)), float(dt), _p(st))
     return st
 
 
-def pml_phase(g: "Grid", prec, axis, nb, what, e, b, state, dt):
-    """One PML phase on `axis`, in place (what 0 the walls' guard update, 1 E walls with the
-    B interfaces, 2 B walls with the E interfaces)."""
+def pml_phase(g: "Grid", prec, mask, nb, what, e, b, state, dt):
+    """One PML phase for the axes in `mask`, in place (what 0 the walls' guard update, 1 E
+    walls with the B interfaces, 2 B walls with the E interfaces)."""
     nx, gl, gu = g.args()
-    getattr(lib(), f"ora_pml_phase_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), int(axis), int(nb),
+    getattr(lib(), f"ora_pml_phase_{prec}")(g.dim, _p(nx), _p(gl), _p(gu), int(mask), int(nb),
                                              int(what), _p(e), _p(b), _p(state),
                                              _p(_f64(g.dx + [0.0] * 3)), float(dt))
 
@@ -405,9 +405,9 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     """One full time step; species = list of dicts with ix, x, u, q, rqm.  walls (bit d):
     axis d bounded by conducting walls instead of periodic.  open_fields = (axis, state from
     lindman_state): Lindman open boundaries at both edges of that axis, particles absorbed
-    there (left in the arrays with charge and momentum 0).  pml = (axis, nb, state from
-    pml_state): PML walls of nb cells at both edges of that axis (2D), particles absorbed there
-    the same way.  thermal = dict(mask, uth, ufl, seed,
+    there (left in the arrays with charge and momentum 0).  pml = (mask, nb, state from
+    pml_state): PML walls of nb cells at both edges of the axes in mask (2D), particles
+    absorbed there the same way.  thermal = dict(mask, uth, ufl, seed,
     step, type: 0 thermal, 1 random dir, 2 waterbag): particles crossing the edges of the axes in mask (walled or open) are re-emitted from
     a thermal bath; step keys the random stream.  pmc (bit d, d walled): perfect magnetic
     instead of electric conductor walls.  window=True: x1 is the axis of a moving window (no
@@ -460,7 +460,7 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
         getattr(L, f"ora_set_pmc_{prec}")(0)
         getattr(L, f"ora_set_window_{prec}")(0)
         getattr(L, f"ora_set_open_{prec}")(-1, None)
-        getattr(L, f"ora_set_pml_{prec}")(-1, 0, None)
+        getattr(L, f"ora_set_pml_{prec}")(0, 0, None)
         L.ora_set_thermal(0, None, None, 0, 0, 0)
     if smooth is not None:
         getattr(L, f"ora_set_smooth_{prec}")(None, None)

@@ -366,51 +366,57 @@ void lindman_phase(const GridDesc &g, int axis, int what, T *e, T *b, T *lind, c
 
 // ---------------------------------------------------------------------------- PML walls
 // Vay's perfectly matched layer ("vpml", source/emf/boundary/os-emf-vpml.f03) at both edges of
-// one axis d of a 2D box, without corners (a single PML axis) or the diffusion correction.
-// Each edge is a wall of nb cells along d -- range [2 - nb, 1] below, [nx + 1, nx + nb] above
-// (setup_vpml :361-368, two cells of overlap with the box) -- over [1 - g1, nt + g2] along the
-// other axis t (g1 = max(gcl_t, 1), g2 = max(gcu_t, 2): new_wall, source/vdf/os-wall.f90:188-195
-// with corner 2).  A wall point holds four split components: 0 X, 1 Y, 2 ZX (the z part driven
-// by x1 derivatives) and 3 ZY (by x2 derivatives); the box's z is ZX + ZY.
-// State (pml_state_size reals): wall (side, field), side 0 lower / 1 upper, field 0 E / 1 B, at
-// (2 side + field) * W, W = nte * nb * 4 with nte = nt + g1 + g2; point (iw, it) component c at
-// 4 ((it - 1 + g1) nb + iw - lo(side)) + c.  Then the attenuation tables at 4 W: table k (0 E
-// lower, 1 E upper, 2 B lower, 3 B upper), coefficient m (0..2) of wall cell n (1..nb) at
-// 4 W + (3 k + m) nb + n - 1 (setup_att_coeff :3586-3684).
+// the axes in a mask of a 2D box (Cartesian, no diffusion correction).  Each PML edge is a wall
+// of nb cells along its axis a -- range [2 - nb, 1] below, [nx + 1, nx + nb] above (setup_vpml
+// :361-368, two cells of overlap with the box) -- over [1 - g1, nt + g2] along the other axis t
+// (new_wall, source/vdf/os-wall.f90:188-195): g1 = max(gcl_t, c - 1), g2 = max(gcu_t, c), with
+// c = nb for the x1 walls when x2 has PML walls too (they cover the corners, setup_vpml
+// :382-398), else 2.  A wall point holds four split components: 0 X, 1 Y, 2 ZX (the z part
+// driven by x1 derivatives), 3 ZY (by x2 derivatives); the box's z is ZX + ZY.
+// State (pml_state_size reals): per PML axis a in increasing order, walls (side, field), side
+// 0 lower / 1 upper, field 0 E / 1 B, at base_a + (2 side + field) W_a, W_a = nte_a nb 4,
+// nte_a = nt + g1 + g2; point (iw, it) component c at 4 ((it - 1 + g1) nb + iw - lo(side)) + c.
+// Then the attenuation tables of both axes at T (the walls' total): axis a, table k (0 E lower,
+// 1 E upper, 2 B lower, 3 B upper), coefficient m (0..2) of wall cell n (1..nb) at
+// T + ((4 a + k) 3 + m) nb + n - 1 (setup_att_coeff :3586-3684).
 struct PmlDesc {
-    int d, t, nn, nt, nb, g1, g2, nte;
-    long W;
+    int mask, nb, nx[2];
+    int g1[2], g2[2], nte[2];
+    long W[2], base[2], T;
 };
 
-static PmlDesc pml_desc(const GridDesc &g, int d, int nb)
+static PmlDesc pml_desc(const GridDesc &g, int mask, int nb)
 {
     PmlDesc P;
-    P.d = d;
-    P.t = 1 - d;
-    P.nn = g.nx[d];
-    P.nt = g.nx[P.t];
+    P.mask = mask;
     P.nb = nb;
-    P.g1 = g.gcl[P.t] > 1 ? g.gcl[P.t] : 1;
-    P.g2 = g.gcu[P.t] > 2 ? g.gcu[P.t] : 2;
-    P.nte = P.nt + P.g1 + P.g2;
-    P.W = (long)P.nte * nb * 4;
+    long off = 0;
+    for (int a = 0; a < 2; a++) {
+        const int t = 1 - a;
+        P.nx[a] = g.nx[a];
+        const int c = (a == 0 && ((mask >> 1) & 1)) ? nb : 2;
+        P.g1[a] = g.gcl[t] > c - 1 ? g.gcl[t] : c - 1;
+        P.g2[a] = g.gcu[t] > c ? g.gcu[t] : c;
+        P.nte[a] = g.nx[t] + P.g1[a] + P.g2[a];
+        P.W[a] = (long)P.nte[a] * nb * 4;
+        P.base[a] = off;
+        if ((mask >> a) & 1) off += 4 * P.W[a];
+    }
+    P.T = off;
     return P;
 }
 
-long pml_state_size(const GridDesc &g, int axis, int nb)
+long pml_state_size(const GridDesc &g, int mask, int nb)
 {
-    const PmlDesc P = pml_desc(g, axis, nb);
-    return 4 * P.W + 12L * nb;
+    return pml_desc(g, mask, nb).T + 24L * nb;
 }
 
 template <typename T>
-void pml_init_host(const GridDesc &g, int axis, int nb, const double *dx, double dt, T *st)
+void pml_init_host(const GridDesc &g, int mask, int nb, const double *dx, double dt, T *st)
 {
-    const PmlDesc P = pml_desc(g, axis, nb);
-    const long n = 4 * P.W + 12L * nb;
+    const PmlDesc P = pml_desc(g, mask, nb);
+    const long n = P.T + 24L * nb;
     for (long i = 0; i < n; i++) st[i] = T(0);
-    T *cf = st + 4 * P.W;
-    auto at = [&](int k, int m, int c) -> T & { return cf[(3 * k + m) * nb + c - 1]; };
     // t(x) = exp(s1 (s2 x)^4) with s1 = -0.8 (4 + 1) / 2, s2 = 1 / (nb - 3); the fourth power
     // as two squares (the reference's exponent is the real constant 4.0 and its base is
     // negative at the interface point of the lower edge)
@@ -419,117 +425,158 @@ void pml_init_host(const GridDesc &g, int axis, int nb, const double *dx, double
         const double y = s2 * x;
         return exp(s1 * (y * y) * (y * y));
     };
-    const double dtdx = dt / dx[axis], dif = (1.0 - dtdx) / (1.0 + dtdx);
-    for (int j = 0; j < nb; j++) {
-        // lower edge: B is the outer point, j = -1/2 the interface
-        double tj = att(j - 0.5), tj12 = att((double)j), tj1 = att(j + 0.5);
-        double b1e = dtdx * (1.0 + dif * (1.0 - tj12)), b1b = dtdx * (1.0 + dif * (1.0 - tj1));
-        at(0, 0, nb - j) = (T)(1.0 - b1e + tj12 * dtdx);
-        at(0, 1, nb - j) = (T)(tj * b1e);
-        at(0, 2, nb - j) = (T)dtdx;
-        at(2, 0, nb - j) = (T)(1.0 - b1b + tj1 * dtdx);
-        at(2, 1, nb - j) = (T)(tj12 * b1b);
-        at(2, 2, nb - j) = (T)dtdx;
-        // upper edge: E is the outer point, j = 0 the interface
-        tj = att((double)j);
-        tj12 = att(j + 0.5);
-        tj1 = att(j + 1.0);
-        b1e = dtdx * (1.0 + dif * (1.0 - tj12));
-        b1b = dtdx * (1.0 + dif * (1.0 - tj1));
-        at(1, 0, j + 1) = (T)(1.0 - b1e + tj12 * dtdx);
-        at(1, 1, j + 1) = (T)dtdx;
-        at(1, 2, j + 1) = (T)(tj * b1e);
-        at(3, 0, j + 1) = (T)(1.0 - b1b + tj1 * dtdx);
-        at(3, 1, j + 1) = (T)dtdx;
-        at(3, 2, j + 1) = (T)(tj12 * b1b);
+    for (int a = 0; a < 2; a++) {
+        T *cf = st + P.T + 12L * a * nb;
+        auto at = [&](int k, int m, int c) -> T & { return cf[(3 * k + m) * nb + c - 1]; };
+        const double dtdx = dt / dx[a], dif = (1.0 - dtdx) / (1.0 + dtdx);
+        for (int j = 0; j < nb; j++) {
+            // lower edge: B is the outer point, j = -1/2 the interface
+            double tj = att(j - 0.5), tj12 = att((double)j), tj1 = att(j + 0.5);
+            double b1e = dtdx * (1.0 + dif * (1.0 - tj12)), b1b = dtdx * (1.0 + dif * (1.0 - tj1));
+            at(0, 0, nb - j) = (T)(1.0 - b1e + tj12 * dtdx);
+            at(0, 1, nb - j) = (T)(tj * b1e);
+            at(0, 2, nb - j) = (T)dtdx;
+            at(2, 0, nb - j) = (T)(1.0 - b1b + tj1 * dtdx);
+            at(2, 1, nb - j) = (T)(tj12 * b1b);
+            at(2, 2, nb - j) = (T)dtdx;
+            // upper edge: E is the outer point, j = 0 the interface
+            tj = att((double)j);
+            tj12 = att(j + 0.5);
+            tj1 = att(j + 1.0);
+            b1e = dtdx * (1.0 + dif * (1.0 - tj12));
+            b1b = dtdx * (1.0 + dif * (1.0 - tj1));
+            at(1, 0, j + 1) = (T)(1.0 - b1e + tj12 * dtdx);
+            at(1, 1, j + 1) = (T)dtdx;
+            at(1, 2, j + 1) = (T)(tj * b1e);
+            at(3, 0, j + 1) = (T)(1.0 - b1b + tj1 * dtdx);
+            at(3, 1, j + 1) = (T)dtdx;
+            at(3, 2, j + 1) = (T)(tj12 * b1b);
+        }
     }
 }
 
-__device__ __forceinline__ int pml_lo(const PmlDesc &P, int side)
+__device__ __forceinline__ int pml_lo(const PmlDesc &P, int a, int side)
 {
-    return side == 0 ? 2 - P.nb : P.nn + 1;
+    return side == 0 ? 2 - P.nb : P.nx[a] + 1;
 }
 
-// component c of wall (side, fld) at box coordinates (i1, i2) (iw along d, it along t)
+// component c of wall (a, side, fld) at box coordinates (i1, i2) (iw along a, it along t)
 template <typename T>
-__device__ __forceinline__ T &pml_at(const PmlDesc &P, T *st, int side, int fld, int c, int i1,
-                                     int i2)
+__device__ __forceinline__ T &pml_at(const PmlDesc &P, T *st, int a, int side, int fld, int c,
+                                     int i1, int i2)
 {
-    const int iw = P.d == 0 ? i1 : i2, it = P.d == 0 ? i2 : i1;
-    return st[(2 * side + fld) * P.W +
-              4 * ((long)(it - 1 + P.g1) * P.nb + (iw - pml_lo(P, side))) + c];
+    const int iw = a == 0 ? i1 : i2, it = a == 0 ? i2 : i1;
+    return st[P.base[a] + (2 * side + fld) * P.W[a] +
+              4 * ((long)(it - 1 + P.g1[a]) * P.nb + (iw - pml_lo(P, a, side))) + c];
 }
 
 template <typename T>
-__device__ __forceinline__ T pml_coef(const PmlDesc &P, const T *st, int k, int m, int n)
+__device__ __forceinline__ T pml_coef(const PmlDesc &P, const T *st, int a, int k, int m, int n)
 {
-    return st[4 * P.W + (3 * k + m) * P.nb + n - 1];
+    return st[P.T + ((4 * a + k) * 3 + m) * P.nb + n - 1];
 }
 
-// interfaces with the box for field fld (update_interface_x1_2d :2880-2993 without the corner
-// contacts, update_interface_x2_2d :3190-3248): the box point next to the wall's inner end
-// goes into the wall (ZX takes the box's z, ZY 0), the wall point one cell further out goes into
-// the box (z = ZX + ZY); one thread per edge and transverse point 0 .. nt + 2
+// interfaces of the walls of axis a with the box for field fld (update_interface_x1_2d
+// :2880-2943, update_interface_x2_2d :3190-3248): the box point next to the wall's inner end
+// goes into the wall (ZX takes the box's z, ZY 0), the wall point one cell further out goes
+// into the box (z = ZX + ZY); one thread per edge and transverse point 0 .. nt + 2
 template <typename T>
-__global__ void k_pml_iface(GridDesc g, PmlDesc P, T *__restrict__ st, T *__restrict__ f, int fld)
+__global__ void k_pml_iface(GridDesc g, PmlDesc P, T *__restrict__ st, T *__restrict__ f, int fld,
+                            int a)
 {
-    const long n = 2L * (P.nt + 3);
+    const int nt = P.nx[1 - a];
+    const long n = 2L * (nt + 3);
     OSG_GRID_LOOP(m, n)
     {
-        const int side = (int)(m / (P.nt + 3)), it = (int)(m % (P.nt + 3));
-        const int lo = pml_lo(P, side), hi = lo + P.nb - 1;
+        const int side = (int)(m / (nt + 3)), it = (int)(m % (nt + 3));
+        const int lo = pml_lo(P, a, side), hi = lo + P.nb - 1;
         const int to_w = side == 0 ? hi : lo, to_b = side == 0 ? hi - 1 : lo + 1;
-        int ic[3] = {1, 1, 1};
-        ic[P.d] = to_w;
-        ic[P.t] = it;
-        const long pw = pos(g, ic[0], ic[1], ic[2]);
-        const int w1 = P.d == 0 ? to_w : it, w2 = P.d == 0 ? it : to_w;
-        for (int c = 0; c < 3; c++) pml_at(P, st, side, fld, c, w1, w2) = f[pw + c];
-        pml_at(P, st, side, fld, 3, w1, w2) = T(0);
-        ic[P.d] = to_b;
-        const long pb = pos(g, ic[0], ic[1], ic[2]);
-        const int b1 = P.d == 0 ? to_b : it, b2 = P.d == 0 ? it : to_b;
-        f[pb + 0] = pml_at(P, st, side, fld, 0, b1, b2);
-        f[pb + 1] = pml_at(P, st, side, fld, 1, b1, b2);
-        f[pb + 2] = pml_at(P, st, side, fld, 2, b1, b2) + pml_at(P, st, side, fld, 3, b1, b2);
+        const int w1 = a == 0 ? to_w : it, w2 = a == 0 ? it : to_w;
+        const long pw = pos(g, w1, w2, 1);
+        for (int c = 0; c < 3; c++) pml_at(P, st, a, side, fld, c, w1, w2) = f[pw + c];
+        pml_at(P, st, a, side, fld, 3, w1, w2) = T(0);
+        const int b1 = a == 0 ? to_b : it, b2 = a == 0 ? it : to_b;
+        const long pb = pos(g, b1, b2, 1);
+        f[pb + 0] = pml_at(P, st, a, side, fld, 0, b1, b2);
+        f[pb + 1] = pml_at(P, st, a, side, fld, 1, b1, b2);
+        f[pb + 2] = pml_at(P, st, a, side, fld, 2, b1, b2) + pml_at(P, st, a, side, fld, 3, b1, b2);
     }
 }
 
-// the E walls (update_e_x1_2d :925-1048, update_e_x2_2d :1369-1456, non-corner branches): one
-// thread per edge, wall row and transverse point; E reads only B, so the points are independent
+// the x1 walls' contact columns with the x2 walls over the corner rows (update_interface_x1_2d
+// :2945-2988): below, the x2 wall takes the x1 wall's column 0 and gives it column 1; above,
+// the x1 wall takes column nx1 + 1 and gives column nx1 + 2.  One thread per x1 wall, x2 wall,
+// corner row and component
 template <typename T>
-__global__ void k_pml_e(PmlDesc P, T *__restrict__ st, T dtdx)
+__global__ void k_pml_contact(PmlDesc P, T *__restrict__ st, int fld)
 {
-    const long n = 2L * P.nb * P.nte;
+    const int nr = P.nb - 1;   // corner rows per x2 wall: 2 - nb .. 0 and nx2 + 2 .. nx2 + nb
+    const long n = 2L * 2 * nr * 4;
     OSG_GRID_LOOP(m, n)
     {
-        const int side = (int)(m / ((long)P.nb * P.nte));
-        const int rem = (int)(m % ((long)P.nb * P.nte));
-        const int lo = pml_lo(P, side), hi = lo + P.nb - 1;
-        const int iw = lo + rem % P.nb, it = 1 - P.g1 + rem / P.nb;
-        if (it < 2 - P.g1) continue;   // transverse range 2 - g1 .. nt + g2
+        const int c = (int)(m % 4);
+        const int r = (int)((m / 4) % nr), adj = (int)((m / (4 * nr)) % 2), side = (int)(m / (8 * nr));
+        const int i2 = adj == 0 ? 2 - P.nb + r : P.nx[1] + 2 + r;
+        if (side == 0) {
+            pml_at(P, st, 1, adj, fld, c, 0, i2) = pml_at(P, st, 0, 0, fld, c, 0, i2);
+            pml_at(P, st, 0, 0, fld, c, 1, i2) = pml_at(P, st, 1, adj, fld, c, 1, i2);
+        } else {
+            const int i1 = P.nx[0] + 1;
+            pml_at(P, st, 0, 1, fld, c, i1, i2) = pml_at(P, st, 1, adj, fld, c, i1, i2);
+            pml_at(P, st, 1, adj, fld, c, i1 + 1, i2) = pml_at(P, st, 0, 1, fld, c, i1 + 1, i2);
+        }
+    }
+}
+
+// the E walls of axis a (update_e_x1_2d :925-1048 with its corner branch, update_e_x2_2d
+// :1369-1456): one thread per edge, wall row and transverse point; E reads only B, so the
+// points are independent
+template <typename T>
+__global__ void k_pml_e(PmlDesc P, T *__restrict__ st, T dtdx, int a)
+{
+    const int nt = P.nx[1 - a], nte = P.nte[a];
+    const long n = 2L * P.nb * nte;
+    const bool cor = a == 0 && ((P.mask >> 1) & 1);
+    OSG_GRID_LOOP(m, n)
+    {
+        const int side = (int)(m / ((long)P.nb * nte));
+        const int rem = (int)(m % ((long)P.nb * nte));
+        const int lo = pml_lo(P, a, side), hi = lo + P.nb - 1;
+        const int iw = lo + rem % P.nb, it = 1 - P.g1[a] + rem / P.nb;
+        if (it < 2 - P.g1[a]) continue;   // transverse range 2 - g1 .. nt + g2
         const int r0 = lo + 1, r1 = side == 0 ? hi - 1 : hi;
         const int k = side, cofs = side == 0 ? lo - 1 : lo;
-        const bool lowest = P.d == 1 && iw == lo;
+        const bool lowest = a == 1 && iw == lo;
         if (!lowest && (iw < r0 || iw > r1)) continue;
-        const int i1 = P.d == 0 ? iw : it, i2 = P.d == 0 ? it : iw;
-#define WE(c, a, b) pml_at(P, st, side, 0, c, a, b)
-#define WB(c, a, b) pml_at(P, st, side, 1, c, a, b)
-        if (P.d == 0) {
+        const int i1 = a == 0 ? iw : it, i2 = a == 0 ? it : iw;
+#define WE(c, x, y) pml_at(P, st, a, side, 0, c, x, y)
+#define WB(c, x, y) pml_at(P, st, a, side, 1, c, x, y)
+        if (a == 0) {
             const int ci = i1 - cofs;
-            const T c1 = pml_coef(P, st, k, 0, ci), c2 = pml_coef(P, st, k, 1, ci),
-                    c3 = pml_coef(P, st, k, 2, ci);
-            WE(0, i1, i2) = WE(0, i1, i2) + dtdx * (WB(2, i1, i2) + WB(3, i1, i2) -
-                                                    WB(2, i1, i2 - 1) - WB(3, i1, i2 - 1));
-            WE(3, i1, i2) = WE(3, i1, i2) - dtdx * (WB(0, i1, i2) - WB(0, i1, i2 - 1));
+            const T c1 = pml_coef(P, st, 0, k, 0, ci), c2 = pml_coef(P, st, 0, k, 1, ci),
+                    c3 = pml_coef(P, st, 0, k, 2, ci);
+            // corner rows (x2 walls below or above): damped along x2 as well
+            const int cn = !cor ? 0 : (i2 <= 0 ? i2 + P.g1[0] : (i2 > nt + 1 ? i2 - nt - 1 : 0));
+            if (cn) {
+                const int ck = i2 <= 0 ? 0 : 1;
+                const T d1 = pml_coef(P, st, 1, ck, 0, cn), d2 = pml_coef(P, st, 1, ck, 1, cn),
+                        d3 = pml_coef(P, st, 1, ck, 2, cn);
+                WE(0, i1, i2) = d1 * WE(0, i1, i2) + d2 * (WB(2, i1, i2) + WB(3, i1, i2)) -
+                                d3 * (WB(2, i1, i2 - 1) + WB(3, i1, i2 - 1));
+                WE(3, i1, i2) = d1 * WE(3, i1, i2) - d2 * WB(0, i1, i2) + d3 * WB(0, i1, i2 - 1);
+            } else {
+                WE(0, i1, i2) = WE(0, i1, i2) + dtdx * (WB(2, i1, i2) + WB(3, i1, i2) -
+                                                        WB(2, i1, i2 - 1) - WB(3, i1, i2 - 1));
+                WE(3, i1, i2) = WE(3, i1, i2) - dtdx * (WB(0, i1, i2) - WB(0, i1, i2 - 1));
+            }
             WE(1, i1, i2) = c1 * WE(1, i1, i2) - c2 * (WB(2, i1, i2) + WB(3, i1, i2)) +
                             c3 * (WB(2, i1 - 1, i2) + WB(3, i1 - 1, i2));
             WE(2, i1, i2) = c1 * WE(2, i1, i2) + c2 * WB(1, i1, i2) - c3 * WB(1, i1 - 1, i2);
         } else {
             if (!lowest) {
                 const int ci = i2 - cofs;
-                const T c1 = pml_coef(P, st, k, 0, ci), c2 = pml_coef(P, st, k, 1, ci),
-                        c3 = pml_coef(P, st, k, 2, ci);
+                const T c1 = pml_coef(P, st, 1, k, 0, ci), c2 = pml_coef(P, st, 1, k, 1, ci),
+                        c3 = pml_coef(P, st, 1, k, 2, ci);
                 WE(0, i1, i2) = c1 * WE(0, i1, i2) + c2 * (WB(2, i1, i2) + WB(3, i1, i2)) -
                                 c3 * (WB(2, i1, i2 - 1) + WB(3, i1, i2 - 1));
                 WE(3, i1, i2) = c1 * WE(3, i1, i2) - c2 * WB(0, i1, i2) + c3 * WB(0, i1, i2 - 1);
@@ -542,38 +589,51 @@ __global__ void k_pml_e(PmlDesc P, T *__restrict__ st, T dtdx)
     }
 }
 
-// the B walls (update_b_x1_2d :2066-2177, update_b_x2_2d :2512-2579, non-corner branches)
+// the B walls of axis a (update_b_x1_2d :2066-2177 with its corner branch, update_b_x2_2d
+// :2512-2579)
 template <typename T>
-__global__ void k_pml_b(PmlDesc P, T *__restrict__ st, T dtdx)
+__global__ void k_pml_b(PmlDesc P, T *__restrict__ st, T dtdx, int a)
 {
-    const long n = 2L * P.nb * P.nte;
+    const int nt = P.nx[1 - a], nte = P.nte[a];
+    const long n = 2L * P.nb * nte;
+    const bool cor = a == 0 && ((P.mask >> 1) & 1);
     OSG_GRID_LOOP(m, n)
     {
-        const int side = (int)(m / ((long)P.nb * P.nte));
-        const int rem = (int)(m % ((long)P.nb * P.nte));
-        const int lo = pml_lo(P, side), hi = lo + P.nb - 1;
-        const int iw = lo + rem % P.nb, it = 1 - P.g1 + rem / P.nb;
-        if (it > P.nt + P.g2 - 1) continue;   // transverse range 1 - g1 .. nt + g2 - 1
+        const int side = (int)(m / ((long)P.nb * nte));
+        const int rem = (int)(m % ((long)P.nb * nte));
+        const int lo = pml_lo(P, a, side), hi = lo + P.nb - 1;
+        const int iw = lo + rem % P.nb, it = 1 - P.g1[a] + rem / P.nb;
+        if (it > nt + P.g2[a] - 1) continue;   // transverse range 1 - g1 .. nt + g2 - 1
         const int r0 = side == 0 ? lo : lo + 1, r1 = hi - 1;
         const int k = 2 + side, cofs = side == 0 ? lo - 2 : lo;
-        const bool highest = P.d == 1 && iw == hi;
+        const bool highest = a == 1 && iw == hi;
         if (!highest && (iw < r0 || iw > r1)) continue;
-        const int i1 = P.d == 0 ? iw : it, i2 = P.d == 0 ? it : iw;
-        if (P.d == 0) {
+        const int i1 = a == 0 ? iw : it, i2 = a == 0 ? it : iw;
+        if (a == 0) {
             const int ci = i1 - cofs;
-            const T c1 = pml_coef(P, st, k, 0, ci), c2 = pml_coef(P, st, k, 1, ci),
-                    c3 = pml_coef(P, st, k, 2, ci);
-            WB(0, i1, i2) = WB(0, i1, i2) - dtdx * (WE(2, i1, i2 + 1) + WE(3, i1, i2 + 1) -
-                                                    WE(2, i1, i2) - WE(3, i1, i2));
-            WB(3, i1, i2) = WB(3, i1, i2) + dtdx * (WE(0, i1, i2 + 1) - WE(0, i1, i2));
+            const T c1 = pml_coef(P, st, 0, k, 0, ci), c2 = pml_coef(P, st, 0, k, 1, ci),
+                    c3 = pml_coef(P, st, 0, k, 2, ci);
+            const int cn = !cor ? 0 : (i2 <= 0 ? i2 + P.g1[0] + 1 : (i2 > nt + 1 ? i2 - nt - 1 : 0));
+            if (cn) {
+                const int ck = i2 <= 0 ? 2 : 3;
+                const T d1 = pml_coef(P, st, 1, ck, 0, cn), d2 = pml_coef(P, st, 1, ck, 1, cn),
+                        d3 = pml_coef(P, st, 1, ck, 2, cn);
+                WB(0, i1, i2) = d1 * WB(0, i1, i2) - d2 * (WE(2, i1, i2 + 1) + WE(3, i1, i2 + 1)) +
+                                d3 * (WE(2, i1, i2) + WE(3, i1, i2));
+                WB(3, i1, i2) = d1 * WB(3, i1, i2) + d2 * WE(0, i1, i2 + 1) - d3 * WE(0, i1, i2);
+            } else {
+                WB(0, i1, i2) = WB(0, i1, i2) - dtdx * (WE(2, i1, i2 + 1) + WE(3, i1, i2 + 1) -
+                                                        WE(2, i1, i2) - WE(3, i1, i2));
+                WB(3, i1, i2) = WB(3, i1, i2) + dtdx * (WE(0, i1, i2 + 1) - WE(0, i1, i2));
+            }
             WB(1, i1, i2) = c1 * WB(1, i1, i2) + c2 * (WE(2, i1 + 1, i2) + WE(3, i1 + 1, i2)) -
                             c3 * (WE(2, i1, i2) + WE(3, i1, i2));
             WB(2, i1, i2) = c1 * WB(2, i1, i2) - c2 * WE(1, i1 + 1, i2) + c3 * WE(1, i1, i2);
         } else {
             if (!highest) {
                 const int ci = i2 - cofs;
-                const T c1 = pml_coef(P, st, k, 0, ci), c2 = pml_coef(P, st, k, 1, ci),
-                        c3 = pml_coef(P, st, k, 2, ci);
+                const T c1 = pml_coef(P, st, 1, k, 0, ci), c2 = pml_coef(P, st, 1, k, 1, ci),
+                        c3 = pml_coef(P, st, 1, k, 2, ci);
                 WB(0, i1, i2) = c1 * WB(0, i1, i2) - c2 * (WE(2, i1, i2 + 1) + WE(3, i1, i2 + 1)) +
                                 c3 * (WE(2, i1, i2) + WE(3, i1, i2));
                 WB(3, i1, i2) = c1 * WB(3, i1, i2) + c2 * WE(0, i1, i2 + 1) - c3 * WE(0, i1, i2);
@@ -588,12 +648,13 @@ __global__ void k_pml_b(PmlDesc P, T *__restrict__ st, T dtdx)
     }
 }
 
-// the walls' periodic update along t (update_periodic_wall, source/vdf/os-wall-comm.f90:182-344):
-// guard points from the opposite interior points, all components, the whole wall-normal range
+// the walls' periodic update along a periodic t (update_periodic_wall, source/vdf/
+// os-wall-comm.f90:182-344): guard points from the opposite interior points, all components,
+// the whole wall-normal range
 template <typename T>
-__global__ void k_pml_guard(PmlDesc P, T *__restrict__ st)
+__global__ void k_pml_guard(PmlDesc P, T *__restrict__ st, int a)
 {
-    const int ng = P.g1 + P.g2;
+    const int ng = P.g1[a] + P.g2[a], nt = P.nx[1 - a];
     const long n = 4L * P.nb * ng * 4;
     OSG_GRID_LOOP(m, n)
     {
@@ -603,55 +664,69 @@ __global__ void k_pml_guard(PmlDesc P, T *__restrict__ st)
         r /= ng;
         const int iw_ofs = (int)(r % P.nb), wall = (int)(r / P.nb);   // wall = 2 side + fld
         const int side = wall >> 1, fld = wall & 1;
-        const int iw = pml_lo(P, side) + iw_ofs;
-        const int it = gi < P.g1 ? 1 - P.g1 + gi : P.nt + 1 + (gi - P.g1);
-        const int src = gi < P.g1 ? it + P.nt : it - P.nt;
-        const int a1 = P.d == 0 ? iw : it, a2 = P.d == 0 ? it : iw;
-        const int s1 = P.d == 0 ? iw : src, s2 = P.d == 0 ? src : iw;
-        pml_at(P, st, side, fld, c, a1, a2) = pml_at(P, st, side, fld, c, s1, s2);
+        const int iw = pml_lo(P, a, side) + iw_ofs;
+        const int it = gi < P.g1[a] ? 1 - P.g1[a] + gi : nt + 1 + (gi - P.g1[a]);
+        const int src = gi < P.g1[a] ? it + nt : it - nt;
+        const int a1 = a == 0 ? iw : it, a2 = a == 0 ? it : iw;
+        const int s1 = a == 0 ? iw : src, s2 = a == 0 ? src : iw;
+        pml_at(P, st, a, side, fld, c, a1, a2) = pml_at(P, st, a, side, fld, c, s1, s2);
     }
 }
 
 template <typename T>
-void pml_phase(const GridDesc &g, int axis, int nb, int what, T *e, T *b, T *pml,
+void pml_phase(const GridDesc &g, int mask, int nb, int what, T *e, T *b, T *pml,
                const double *dx, double dt, cudaStream_t st)
 {
-    const PmlDesc P = pml_desc(g, axis, nb);
+    const PmlDesc P = pml_desc(g, mask, nb);
     if (what == 0) {
-        const long n = 4L * nb * (P.g1 + P.g2) * 4;
-        k_pml_guard<T><<<blocks_for(n, 256), 256, 0, st>>>(P, pml);
+        for (int a = 0; a < 2; a++) {
+            if (!((mask >> a) & 1) || ((mask >> (1 - a)) & 1)) continue;
+            const long n = 4L * nb * (P.g1[a] + P.g2[a]) * 4;
+            k_pml_guard<T><<<blocks_for(n, 256), 256, 0, st>>>(P, pml, a);
+        }
         return;
     }
-    const T dtdx = (T)(dt / dx[P.t]);
-    k_pml_iface<T><<<blocks_for(2L * (P.nt + 3), 256), 256, 0, st>>>(g, P, pml,
-                                                                        what == 1 ? b : e,
-                                                                        what == 1 ? 1 : 0);
-    const long n = 2L * nb * P.nte;
-    if (what == 1) k_pml_e<T><<<blocks_for(n, 256), 256, 0, st>>>(P, pml, dtdx);
-    else k_pml_b<T><<<blocks_for(n, 256), 256, 0, st>>>(P, pml, dtdx);
+    const int fld = what == 1 ? 1 : 0;
+    T *f = what == 1 ? b : e;
+    // the interfaces of every wall in the reference's order (x1 walls with their corner
+    // contacts, then x2 walls), then the wall updates
+    for (int a = 0; a < 2; a++) {
+        if (!((mask >> a) & 1)) continue;
+        k_pml_iface<T><<<blocks_for(2L * (g.nx[1 - a] + 3), 256), 256, 0, st>>>(g, P, pml, f,
+                                                                                fld, a);
+        if (a == 0 && ((mask >> 1) & 1))
+            k_pml_contact<T><<<blocks_for(16L * (nb - 1), 256), 256, 0, st>>>(P, pml, fld);
+    }
+    for (int a = 0; a < 2; a++) {
+        if (!((mask >> a) & 1)) continue;
+        const T dtdx = (T)(dt / dx[1 - a]);
+        const long n = 2L * nb * P.nte[a];
+        if (what == 1) k_pml_e<T><<<blocks_for(n, 256), 256, 0, st>>>(P, pml, dtdx, a);
+        else k_pml_b<T><<<blocks_for(n, 256), 256, 0, st>>>(P, pml, dtdx, a);
+    }
 }
 
 template <typename T>
-void pml_guards(const GridDesc &g, T *e, T *b, int axis, int nb, T *pml, cudaStream_t st)
+void pml_guards(const GridDesc &g, T *e, T *b, int mask, int nb, T *pml, cudaStream_t st)
 {
-    pml_phase<T>(g, axis, nb, 0, e, b, pml, nullptr, 0.0, st);
-    periodic_update<T>(g, e, 0, st, 0, 1 << axis);
-    periodic_update<T>(g, b, 0, st, 0, 1 << axis);
+    pml_phase<T>(g, mask, nb, 0, e, b, pml, nullptr, 0.0, st);
+    periodic_update<T>(g, e, 0, st, 0, mask);
+    periodic_update<T>(g, b, 0, st, 0, mask);
 }
 
 template <typename T>
 void yee_advance(const GridDesc &g, T *e, T *b, const T *j, const double *dx, double dt,
                  cudaStream_t st, int walls, int order, int open_axis, T *lind, int pmc,
-                 int pml_axis, int pml_nb, T *pml)
+                 int pml_mask, int pml_nb, T *pml)
 {
-    if (pml_axis >= 0 && pml) {
+    if (pml_mask && pml) {
         // PML walls: their E after the first B half step, their B after the E step, nothing
         // after the second B half step (update_boundary_bfld step 1 / update_boundary_efld,
         // source/emf/boundary/os-emf-boundary.f90:931-935, 1071-1074)
         launch_dbdt(g, b, e, dx, dt / 2.0, st);
-        pml_phase<T>(g, pml_axis, pml_nb, 1, e, b, pml, dx, dt, st);
+        pml_phase<T>(g, pml_mask, pml_nb, 1, e, b, pml, dx, dt, st);
         launch_dedt(g, e, b, j, dx, dt, st);
-        pml_phase<T>(g, pml_axis, pml_nb, 2, e, b, pml, dx, dt, st);
+        pml_phase<T>(g, pml_mask, pml_nb, 2, e, b, pml, dx, dt, st);
         launch_dbdt(g, b, e, dx, dt / 2.0, st);
         return;
     }

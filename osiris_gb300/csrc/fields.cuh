@@ -55,25 +55,26 @@ __host__ __device__ inline Box make_box(const GridDesc &g, int lo, int hi_off)
 template <typename T>
 void yee_advance(const GridDesc &g, T *e, T *b, const T *j, const double *dx, double dt,
                  cudaStream_t st, int walls = 0, int order = 2, int open_axis = -1,
-                 T *lind = nullptr, int pmc = 0, int pml_axis = -1, int pml_nb = 0,
+                 T *lind = nullptr, int pmc = 0, int pml_mask = 0, int pml_nb = 0,
                  T *pml = nullptr);
-// PML walls of nb cells at both edges of one axis of a 2D box (Vay's perfectly matched layer,
-// source/emf/boundary/os-emf-vpml.f03; no corners).  The state: four split-field walls (E and
-// B per edge) and the attenuation tables, pml_state_size reals, set up on the host by
-// pml_init_host (zeroed walls, tables from dt and dx).
-long pml_state_size(const GridDesc &g, int axis, int nb);
+// PML walls of nb cells at both edges of the axes in `mask` of a 2D box (Vay's perfectly
+// matched layer, source/emf/boundary/os-emf-vpml.f03; the x1 walls cover the corners when both
+// axes have walls).  The state: four split-field walls per PML axis (E and B per edge) and the
+// attenuation tables, pml_state_size reals, set up on the host by pml_init_host (zeroed walls,
+// tables from dt and dx).
+long pml_state_size(const GridDesc &g, int mask, int nb);
 template <typename T>
-void pml_init_host(const GridDesc &g, int axis, int nb, const double *dx, double dt, T *st);
-// one PML phase: 0 the walls' periodic update along the other axis, 1 the E walls after the
-// first B half step (with the B interfaces), 2 the B walls after the E step (with the E
-// interfaces)
+void pml_init_host(const GridDesc &g, int mask, int nb, const double *dx, double dt, T *st);
+// one PML phase: 0 the walls' periodic update along a periodic other axis, 1 the E walls after
+// the first B half step (interfaces with B first), 2 the B walls after the E step (interfaces
+// with E first)
 template <typename T>
-void pml_phase(const GridDesc &g, int axis, int nb, int what, T *e, T *b, T *pml,
+void pml_phase(const GridDesc &g, int mask, int nb, int what, T *e, T *b, T *pml,
                const double *dx, double dt, cudaStream_t st);
-// guard update of E and B with PML walls on `axis`: the walls' own update, then E and B
-// periodic along the other axis only
+// guard update of E and B with PML walls on the axes in `mask`: the walls' own update, then E
+// and B periodic along the other axes only
 template <typename T>
-void pml_guards(const GridDesc &g, T *e, T *b, int axis, int nb, T *pml, cudaStream_t st);
+void pml_guards(const GridDesc &g, T *e, T *b, int mask, int nb, T *pml, cudaStream_t st);
 // Lindman open boundaries at both edges of one axis (p_bc_lindman,
 // source/emf/boundary/os-emf-lindman.f90).  Their state: 5 buffer planes along the axis
 // (E at 0 and 1, B at 0, E at nx+1 and nx+2), 3 components, per interior point of the other

@@ -65,7 +65,7 @@ struct osg_sim {
     unsigned long long *d_step = nullptr;   // step counter of the thermal-bath random stream
     int open_axis = -1;          // Lindman open boundaries at both edges of this axis
     void *lind = nullptr;        // their state (lindman_state_size reals)
-    int pml_axis = -1;           // PML walls at both edges of this axis (2D)
+    int pml_mask = 0;            // PML walls at both edges of these axes (2D)
     int pml_nb = 0;              // their thickness in cells
     void *pml = nullptr;         // their state (pml_state_size reals)
     osg::SmoothSpec smooth;      // current smoothing (order 0 per axis: none)
@@ -276,15 +276,15 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
     const int oax = s->open_axis;
     // PML walls: the same, with the boundary points set by the walls' interfaces in the Yee
     // advance (no restore at the guard update)
-    const int pax = s->pml_axis;
-    const int skip = walls | (oax >= 0 ? 1 << oax : 0) | (pax >= 0 ? 1 << pax : 0);
+    const int pml = s->pml_mask;
+    const int skip = walls | (oax >= 0 ? 1 << oax : 0) | pml;
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[0], st));
     if (oax >= 0) {
         open_guards<T>(s->g, (T *)s->e, (T *)s->b, oax, (const T *)s->lind, st);
         launches += 2 * (c.dim - 1) + 1;
-    } else if (pax >= 0) {
-        pml_guards<T>(s->g, (T *)s->e, (T *)s->b, pax, s->pml_nb, (T *)s->pml, st);
-        launches += 2 * (c.dim - 1) + 1;
+    } else if (pml) {
+        pml_guards<T>(s->g, (T *)s->e, (T *)s->b, pml, s->pml_nb, (T *)s->pml, st);
+        launches += 2 * (c.dim - __builtin_popcount(pml)) + (pml == 3 ? 0 : 1);
     } else {
         periodic_update<T>(s->g, (T *)s->e, 0, st, 0, walls | win);
         periodic_update<T>(s->g, (T *)s->b, 0, st, 0, walls | win);
@@ -321,7 +321,7 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
             for (int d = 0; d < c.dim; d++) {
                 a.wrap[d] = (skip >> d) & 1 ? 0 : c.nx[d];
                 a.reflect[d] = (walls >> d) & 1 ? c.nx[d] : 0;
-                a.absorb[d] = (d == oax || d == pax) ? c.nx[d] : 0;
+                a.absorb[d] = (d == oax || ((pml >> d) & 1)) ? c.nx[d] : 0;
             }
             a.q_absorb = (T *)p.q;
             if (c.thermal) {
@@ -371,9 +371,9 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
     }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[4], st));
     yee_advance<T>(s->g, (T *)s->e, (T *)s->b, (const T *)s->j, c.dx, c.dt, st, walls, c.order,
-                   oax, (T *)s->lind, c.pmc, pax, s->pml_nb, (T *)s->pml);
+                   oax, (T *)s->lind, c.pmc, pml, s->pml_nb, (T *)s->pml);
     launches += 3 + (walls ? 6 * __builtin_popcount(walls) : 0) + (oax >= 0 ? 3 : 0) +
-                (pax >= 0 ? 4 : 0);
+                (pml ? 2 * (2 * __builtin_popcount(pml) + (pml == 3 ? 1 : 0)) : 0);
     if (shift) {
         shift_window_x<T>(s->g, (T *)s->e, (T *)s->shift_tmp, st);
         shift_window_x<T>(s->g, (T *)s->b, (T *)s->shift_tmp, st);
@@ -523,8 +523,8 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               OSG_ERR_ARG, "open boundaries combine with neither walls nor smoothing");
     OSG_CHECK(cfg->pmc >= 0 && (cfg->pmc & ~cfg->walls) == 0, OSG_ERR_ARG,
               "pmc: a bit mask of walled axes");
-    OSG_CHECK(cfg->pml >= 0 && cfg->pml < (1 << cfg->dim) && (cfg->pml & (cfg->pml - 1)) == 0,
-              OSG_ERR_ARG, "pml: the bit of one axis (PML walls without corners)");
+    OSG_CHECK(cfg->pml >= 0 && cfg->pml < (1 << cfg->dim), OSG_ERR_ARG,
+              "pml: a bit mask of the axes");
     OSG_CHECK(cfg->pml == 0 || cfg->dim == 2, OSG_ERR_ARG, "PML walls are built for 2D boxes");
     OSG_CHECK(cfg->pml == 0 || (cfg->walls == 0 && cfg->open_fields == 0 &&
                                 cfg->smooth_type == OSG_SMOOTH_NONE &&
@@ -533,11 +533,9 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
                            "smoothing nor a thermal bath");
     OSG_CHECK(cfg->pml_cells == 0 || cfg->pml_cells >= 5, OSG_ERR_ARG,
               "pml_cells: 0 (8) or at least 5");
-    if (cfg->pml) {
-        const int t = 1 - __builtin_ctz(cfg->pml);
-        OSG_CHECK(cfg->nx[t] >= 6, OSG_ERR_ARG,
-                  "PML walls need at least 6 cells along the other axis");
-    }
+    if (cfg->pml)
+        for (int d = 0; d < 2; d++)
+            OSG_CHECK(cfg->nx[d] >= 6, OSG_ERR_ARG, "PML walls need at least 6 cells per axis");
     OSG_CHECK(cfg->thermal >= 0 && (cfg->thermal & ~(cfg->walls | cfg->open_fields)) == 0,
               OSG_ERR_ARG, "thermal: a bit mask of walled or open axes");
     OSG_CHECK(cfg->thermal == 0 || cfg->engine == OSG_ENGINE_PLAIN ||
@@ -638,17 +636,17 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
     if (!rc && cfg->pml) {
         // the walls start at zero (new_wall, source/vdf/os-wall.f90:198-210); the attenuation
         // tables are computed on the host in double and stored in the field precision
-        s->pml_axis = __builtin_ctz(cfg->pml);
+        s->pml_mask = cfg->pml;
         s->pml_nb = cfg->pml_cells > 0 ? cfg->pml_cells : 8;
-        const long n = pml_state_size(s->g, s->pml_axis, s->pml_nb);
+        const long n = pml_state_size(s->g, s->pml_mask, s->pml_nb);
         s->pml = dalloc<char>((size_t)s->esz * n, &rc);
         if (!rc) {
             std::vector<char> h((size_t)s->esz * n);
             if (s->esz == 4)
-                pml_init_host<float>(s->g, s->pml_axis, s->pml_nb, cfg->dx, cfg->dt,
+                pml_init_host<float>(s->g, s->pml_mask, s->pml_nb, cfg->dx, cfg->dt,
                                      (float *)h.data());
             else
-                pml_init_host<double>(s->g, s->pml_axis, s->pml_nb, cfg->dx, cfg->dt,
+                pml_init_host<double>(s->g, s->pml_mask, s->pml_nb, cfg->dx, cfg->dt,
                                       (double *)h.data());
             if (cudaMemcpy(s->pml, h.data(), h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
                 rc = OSG_ERR_CUDA;
@@ -897,7 +895,7 @@ int osg_sim_set_window(osg_sim *s, int species, const int *ppc, int nprof, const
     OSG_CHECK(s->cfg.engine == OSG_ENGINE_TILED, OSG_ERR_ARG,
               "the moving window runs on the tiled engine");
     OSG_CHECK(s->step_n == 0, OSG_ERR_STATE, "set the window before the first step");
-    OSG_CHECK(s->open_axis < 0 && s->pml_axis < 0, OSG_ERR_ARG,
+    OSG_CHECK(s->open_axis < 0 && s->pml_mask == 0, OSG_ERR_ARG,
               "the moving window does not combine with Lindman or PML boundaries");
     int rc = tiled_set_window(s->tiled, species, ppc, nprof, prof_x, prof_f);
     if (rc) return rc;
@@ -988,7 +986,7 @@ int osg_sim_checkpoint(osg_sim *s, const char *path)
         ok = put(f, l.data(), l.size());
     }
     if (ok && s->pml) {
-        std::vector<char> l((size_t)s->esz * pml_state_size(s->g, s->pml_axis, s->pml_nb));
+        std::vector<char> l((size_t)s->esz * pml_state_size(s->g, s->pml_mask, s->pml_nb));
         OSG_CUDA(cudaMemcpyAsync(l.data(), s->pml, l.size(), cudaMemcpyDeviceToHost, s->st));
         OSG_CUDA(cudaStreamSynchronize(s->st));
         ok = put(f, l.data(), l.size());
@@ -1060,7 +1058,7 @@ int osg_sim_restore(const char *path, osg_sim **out)
         }
     }
     if (rc == OSG_OK && s->pml) {
-        std::vector<char> l((size_t)esz * pml_state_size(s->g, s->pml_axis, s->pml_nb));
+        std::vector<char> l((size_t)esz * pml_state_size(s->g, s->pml_mask, s->pml_nb));
         if (!get(f, l.data(), l.size())) {
             rc = OSG_ERR_ARG;
         } else if (cudaMemcpyAsync(s->pml, l.data(), l.size(), cudaMemcpyHostToDevice, s->st) !=
@@ -1292,7 +1290,7 @@ static int save_fields(osg_sim *s, SavedState &sv)
         (rc = sv.save(s->lind, (size_t)s->esz * lindman_state_size(s->g, s->open_axis), s->st)))
         return rc;
     if (s->pml &&
-        (rc = sv.save(s->pml, (size_t)s->esz * pml_state_size(s->g, s->pml_axis, s->pml_nb),
+        (rc = sv.save(s->pml, (size_t)s->esz * pml_state_size(s->g, s->pml_mask, s->pml_nb),
                       s->st)))
         return rc;
     if (s->d_step && (rc = sv.save(s->d_step, sizeof(unsigned long long), s->st))) return rc;

@@ -1,15 +1,17 @@
 """GPU parity of PML walls (osg_config.pml, Vay's split-field perfectly matched layer at both
-edges of one axis of a 2D box) against the oracle's step.  The walls advance their E after the
+edges of the axes in a mask of a 2D box; with both axes the x1 walls cover the corners) against
+the oracle's step.  The walls advance their E after the
 first B half step and their B after the E step, exchange the boundary points with the box
 through the interfaces, and take their own periodic update along the other axis at the guard
 update; the current is not folded along the PML axis and particles leaving through it are
 absorbed.  Whole field arrays are compared, guard cells included (the interfaces write there).
 
-* plain engine, FP64 1e-12 and FP32 1e-5 / 5e-5 (1 and 10 steps), orders 1-3, either axis;
+* plain engine, FP64 1e-12 and FP32 1e-5 / 5e-5 (1 and 10 steps), orders 1-3, either axis and
+  both (corners);
 * tiled engine (FP32; absorbed particles removed rather than kept with charge 0): fields and
-  the live particles against the oracle, either axis;
+  the live particles against the oracle, either axis and both;
 * a vacuum pulse travelling along the PML axis leaves the box with less than 1e-4 of its
-  energy, in both engines;
+  energy, in both engines; with both axes, a cylindrical pulse leaves less than 1e-4;
 * checkpoint / restore keeps the walls: 4 + 4 steps equal 8 steps to 1e-12;
 * configurations the walls are not built for are refused.
 """
@@ -33,32 +35,32 @@ def osg():
     return osiris_gb300
 
 
-def _oracle_run(oracle, g, p, e, b, species, dt, axis, steps, nb=NB):
+def _oracle_run(oracle, g, p, e, b, species, dt, mask, steps, nb=NB):
     ora = [{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s.items()}
            for s in species]
     eo, bo, jo = e.copy(), b.copy(), g.zeros(p)
-    st = oracle.pml_state(g, p, axis, nb, dt)
+    st = oracle.pml_state(g, p, mask, nb, dt)
     for _ in range(steps):
-        oracle.step(g, p, eo, bo, jo, ora, dt, pml=(axis, nb, st))
+        oracle.step(g, p, eo, bo, jo, ora, dt, pml=(mask, nb, st))
     return eo, bo, jo, ora
 
 
-@pytest.mark.parametrize("axis", [0, 1])
+@pytest.mark.parametrize("mask", [1, 2, 3])
 @pytest.mark.parametrize("order", [1, 2, 3])
 @pytest.mark.parametrize("prec,steps,tol", [(64, 1, 1e-12), (64, 10, 1e-12), (32, 1, 1e-5),
                                             (32, 10, 5e-5)])
-def test_pml_plain_matches_oracle(osg, oracle, prec, steps, tol, order, axis):
+def test_pml_plain_matches_oracle(osg, oracle, prec, steps, tol, order, mask):
     nx = [20, 16]
     p, g, dx, dt, species, e, b = _setup(oracle, prec, 2, order, nx, [2, 2], 11, uth=0.6,
                                          ufl=0.1)
     sim = osg.Simulation(nx, dx, dt, order=order, precision=prec, engine=osg.ENGINE_PLAIN,
-                         pml=1 << axis, pml_cells=NB)
+                         pml=mask, pml_cells=NB)
     sim.set_fields(e, b)
     for s in species:
         sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
     sim.step(steps)
     eg, bg, jg = sim.fields()
-    eo, bo, jo, ora = _oracle_run(oracle, g, p, e, b, species, dt, axis, steps)
+    eo, bo, jo, ora = _oracle_run(oracle, g, p, e, b, species, dt, mask, steps)
     errs = {"E": _nerr(eg, eo), "B": _nerr(bg, bo), "J": _nerr(jg, jo)}
     absorbed = 0
     for k, s in enumerate(ora):
@@ -75,22 +77,22 @@ def test_pml_plain_matches_oracle(osg, oracle, prec, steps, tol, order, axis):
         assert absorbed > 0
 
 
-@pytest.mark.parametrize("axis", [0, 1])
+@pytest.mark.parametrize("mask", [1, 2, 3])
 @pytest.mark.parametrize("order", [2, 3])
 @pytest.mark.parametrize("steps,tol", [(1, 1e-5), (10, 5e-5)])
-def test_pml_tiled_matches_oracle(osg, oracle, steps, tol, order, axis):
+def test_pml_tiled_matches_oracle(osg, oracle, steps, tol, order, mask):
     """The tiled engine drops absorbed particles; the oracle keeps them with charge 0."""
     nx = [32, 24]
     p, g, dx, dt, species, e, b = _setup(oracle, 32, 2, order, nx, [2, 2], 12, uth=0.6,
                                          ufl=0.1)
     sim = osg.Simulation(nx, dx, dt, order=order, precision=32, engine=osg.ENGINE_TILED,
-                         tile=[8, 8], pml=1 << axis, pml_cells=NB)
+                         tile=[8, 8], pml=mask, pml_cells=NB)
     sim.set_fields(e, b)
     for s in species:
         sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
     sim.step(steps)
     eg, bg, jg = sim.fields()
-    eo, bo, jo, ora = _oracle_run(oracle, g, p, e, b, species, dt, axis, steps)
+    eo, bo, jo, ora = _oracle_run(oracle, g, p, e, b, species, dt, mask, steps)
     errs = {"E": _nerr(eg, eo), "B": _nerr(bg, bo), "J": _nerr(jg, jo)}
     for k, s in enumerate(ora):
         ix, x, u, q = sim.species(k)
@@ -147,13 +149,39 @@ def test_vacuum_pulse_leaves_through_the_pml(osg, engine, prec, axis):
     sim.close()
 
 
+@pytest.mark.parametrize("engine,prec", [("plain", 64), ("tiled", 32)])
+def test_cylindrical_pulse_leaves_through_pml_on_both_axes(osg, engine, prec):
+    nx, dx = [64, 48], [0.2, 0.2]
+    dt = 0.9 / np.sqrt(sum(1 / d ** 2 for d in dx))
+    sim = osg.Simulation(nx, dx, dt, order=2, precision=prec,
+                         engine=osg.ENGINE_PLAIN if engine == "plain" else osg.ENGINE_TILED,
+                         tile=[8, 8] if engine == "tiled" else None, pml=3)
+    gl, gu = osg.GUARD[2]
+    dtype = np.float32 if prec == 32 else np.float64
+    shape = tuple(reversed([n + gl + gu for n in nx])) + (3,)
+    e, b = np.zeros(shape, dtype), np.zeros(shape, dtype)
+    y, x = np.meshgrid(np.arange(shape[0]), np.arange(shape[1]), indexing="ij")
+    e[:, :, 2] = np.exp(-((x - shape[1] / 2) ** 2 + (y - shape[0] / 2) ** 2) / 8.0)
+    sim.set_fields(e, b)
+    empty = np.zeros((0, 2), np.int32), np.zeros((0, 2), dtype), np.zeros((0, 3), dtype), \
+        np.zeros(0, dtype)
+    sim.add_species(-1.0, *empty)
+    sl = (slice(gl, gl + nx[1]), slice(gl, gl + nx[0]))
+    w0 = float((e[sl].astype(np.float64) ** 2).sum())
+    sim.step(int(3 * max(nx) * dx[0] / dt))
+    e1, b1, _ = sim.fields()
+    w1 = float((e1[sl].astype(np.float64) ** 2).sum() + (b1[sl].astype(np.float64) ** 2).sum())
+    assert w1 / w0 < 1e-4
+    sim.close()
+
+
 def test_checkpoint_keeps_the_pml_walls(osg, oracle, tmp_path):
     nx = [20, 16]
     p, g, dx, dt, species, e, b = _setup(oracle, 64, 2, 2, nx, [2, 2], 4, uth=0.6, ufl=0.1)
 
     def fresh():
         sim = osg.Simulation(nx, dx, dt, order=2, precision=64, engine=osg.ENGINE_PLAIN,
-                             pml=2)
+                             pml=3)
         sim.set_fields(e, b)
         for s in species:
             sim.add_species(s["rqm"], s["ix"], s["x"], s["u"], s["q"])
@@ -168,7 +196,7 @@ def test_checkpoint_keeps_the_pml_walls(osg, oracle, tmp_path):
     a.checkpoint(tmp_path / "pml.ckpt")
     a.close()
     c = osg.Simulation.restore(tmp_path / "pml.ckpt")
-    assert c.cfg.pml == 2
+    assert c.cfg.pml == 3
     c.step(4)
     got = c.fields()[:2], c.species(0)
     c.close()
@@ -179,7 +207,7 @@ def test_checkpoint_keeps_the_pml_walls(osg, oracle, tmp_path):
     assert _nerr(ia + xa, ib + xb) <= 1e-12 and _nerr(ua, ub) <= 1e-12
 
 
-@pytest.mark.parametrize("kw", [dict(pml=3), dict(pml=1, walls=2), dict(pml=1, open_fields=2),
+@pytest.mark.parametrize("kw", [dict(pml=4), dict(pml=1, walls=2), dict(pml=1, open_fields=2),
                                 dict(pml=1, pml_cells=4), dict(pml=1, smooth_type=2,
                                                                smooth_order=1)])
 def test_pml_refuses_what_it_is_not_built_for(osg, kw):

@@ -7,7 +7,9 @@ one axis of a 2D box), on the CPU:
   and deep in the wall the damped update tends to the plain Yee update at the interface;
 * a plane pulse travelling along the PML axis, in either direction, leaves the box with less
   than 1e-4 of its energy, while the same box without PML keeps its energy to 1e-5;
-* the state is four split-field walls plus the tables.
+* with PML on both axes (the x1 walls covering the corners) a cylindrical pulse leaves the box
+  with less than 1e-5 of its energy; with one PML axis most of it stays (the other is periodic);
+* the state is four split-field walls per PML axis plus the tables.
 """
 import numpy as np
 import pytest
@@ -17,8 +19,8 @@ from oracle import pyoracle as po
 NB = 8
 
 
-def _tables(st, nb):
-    return st[len(st) - 12 * nb:].reshape(4, 3, nb)
+def _tables(st, nb, axis):
+    return st[len(st) - 24 * nb:].reshape(2, 4, 3, nb)[axis]
 
 
 @pytest.mark.parametrize("axis", [0, 1])
@@ -27,8 +29,8 @@ def test_attenuation_tables(axis):
     dx = [0.1, 0.2]
     dt = 0.04
     g = po.Grid(nx, 2, dx)
-    st = po.pml_state(g, "f64", axis, NB, dt)
-    t = _tables(st, NB)
+    st = po.pml_state(g, "f64", 1 << axis, NB, dt)
+    t = _tables(st, NB, axis)
     dtdx = dt / dx[axis]
     dif = (1 - dtdx) / (1 + dtdx)
     att = lambda x: np.exp(-2.0 * (0.2 * x) ** 4)
@@ -49,7 +51,7 @@ def test_attenuation_tables(axis):
     # next to the interface the damped update is nearly the plain one (1, dtdx, dtdx)
     assert t[1, :, 0] == pytest.approx([1.0, dtdx, dtdx], rel=1e-3)
     # the walls start at zero
-    assert not st[:len(st) - 12 * NB].any()
+    assert not st[:len(st) - 24 * NB].any()
 
 
 def _energy(g, e, b):
@@ -75,9 +77,9 @@ def test_plane_pulse_is_absorbed(axis, sign):
             e[..., 0] = prof[:, None]
             b[..., 2] = -sign * prof_h[:, None]
         w0 = _energy(g, e, b)
-        st = po.pml_state(g, "f64", axis, NB, dt)
+        st = po.pml_state(g, "f64", 1 << axis, NB, dt)
         for _ in range(200):
-            po.step(g, "f64", e, b, j, [], dt, pml=(axis, NB, st) if pml else None)
+            po.step(g, "f64", e, b, j, [], dt, pml=(1 << axis, NB, st) if pml else None)
         res[pml] = _energy(g, e, b) / w0
     assert res[True] < 1e-4, res
     assert abs(res[False] - 1.0) < 1e-5, res
@@ -89,5 +91,22 @@ def test_state_size():
     for axis in (0, 1):
         nt = g.nx[1 - axis]
         nte = nt + max(gl, 1) + max(gu, 2)
-        st = po.pml_state(g, "f32", axis, NB, 0.04)
-        assert st.dtype == np.float32 and len(st) == 4 * nte * NB * 4 + 12 * NB
+        st = po.pml_state(g, "f32", 1 << axis, NB, 0.04)
+        assert st.dtype == np.float32 and len(st) == 4 * nte * NB * 4 + 24 * NB
+
+
+def test_corners_absorb_a_cylindrical_pulse():
+    nx = [48, 40]
+    g = po.Grid(nx, 2, [0.1, 0.1])
+    left = {}
+    for mask in (1, 3):
+        e, b, j = g.zeros("f64"), g.zeros("f64"), g.zeros("f64")
+        st = po.pml_state(g, "f64", mask, NB, 0.05)
+        yy, xx = np.meshgrid(np.arange(g.size[1]), np.arange(g.size[0]), indexing="ij")
+        e[..., 2] = np.exp(-((xx - g.size[0] / 2) ** 2 + (yy - g.size[1] / 2) ** 2) / 8.0)
+        w0 = _energy(g, e, b)
+        for _ in range(400):
+            po.step(g, "f64", e, b, j, [], 0.05, pml=(mask, NB, st))
+        assert np.isfinite(e).all() and np.isfinite(b).all()
+        left[mask] = _energy(g, e, b) / w0
+    assert left[3] < 1e-5 and left[1] > 1e-2, left
