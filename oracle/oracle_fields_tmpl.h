@@ -539,10 +539,162 @@ static FN(pml_desc) FN(pml_make)(const FN(ora_grid) *g, int mask, int nb)
     return P;
 }
 
+/* 3D PML walls at both edges of one axis a (no edges or corners with other PML axes),
+ * restated from update_e_x{1,2,3}_3d (:1172-1704), update_b_x{1,2,3}_3d (:2311-2828) and
+ * update_interface_x{1,2,3}_3d (:2997-3529) without their corner branches.  A wall point holds
+ * six split components (:444-446): 2F + s for field component F with s = 0 the part driven by
+ * the derivative along the lower of the two other axes (XY, YX, ZX) and s = 1 the other (XZ,
+ * YZ, ZY).  Split (F, D) with G the third axis: E_FD += sgn dt/dx_D (B_G(p) - B_G(p - e_D)),
+ * sgn = +1 when D follows F cyclically, -1 otherwise (the curl); B_FD -= sgn dt/dx_D
+ * (E_G(p + e_D) - E_G(p)); B_G / E_G the sum of G's two splits.  Along D = a the update is the
+ * damped one with a's tables.  The wall spans [1 - g1_t, n_t + g2_t] along both other axes t
+ * (g1 = max(gcl_t, 1), g2 = max(gcu_t, 2)).
+ * State layout: wall (side, field) at (2 side + field) W, W = nte_t1 nte_t2 nb 6 (t1 < t2 the
+ * other axes); point (iw, i_t1, i_t2) component c at
+ * 6 (((i_t2 - 1 + g1_t2) nte_t1 + i_t1 - 1 + g1_t1) nb + iw - lo(side)) + c; then the tables of
+ * all three axes at 4 W: axis x, table k, coefficient m, cell n at 4 W + ((4 x + k) 3 + m) nb +
+ * n - 1. */
+typedef struct {
+    int a, t1, t2, nb, n[3], g1[3], g2[3], nte[3];
+    long W;
+} FN(pml3_desc);
+
+static FN(pml3_desc) FN(pml3_make)(const FN(ora_grid) *g, int mask, int nb)
+{
+    FN(pml3_desc) P;
+    P.a = mask == 1 ? 0 : (mask == 2 ? 1 : 2);
+    P.t1 = P.a == 0 ? 1 : 0;
+    P.t2 = P.a == 2 ? 1 : 2;
+    P.nb = nb;
+    for (int d = 0; d < 3; d++) {
+        P.n[d] = g->nx[d];
+        P.g1[d] = g->gcl[d] > 1 ? g->gcl[d] : 1;
+        P.g2[d] = g->gcu[d] > 2 ? g->gcu[d] : 2;
+        P.nte[d] = g->nx[d] + P.g1[d] + P.g2[d];
+    }
+    P.W = (long)P.nte[P.t1] * P.nte[P.t2] * nb * 6;
+    return P;
+}
+
+static inline long FN(pml3_at)(const FN(pml3_desc) *P, int side, int fld, int c, const int *i)
+{
+    const int lo = side == 0 ? 2 - P->nb : P->n[P->a] + 1;
+    return (2 * side + fld) * P->W +
+           6 * ((((long)i[P->t2] - 1 + P->g1[P->t2]) * P->nte[P->t1] + i[P->t1] - 1 +
+                 P->g1[P->t1]) * P->nb + i[P->a] - lo) + c;
+}
+
+#define P3COEF(x, k, m, nn) st[4 * P.W + ((4 * (x) + (k)) * 3 + (m)) * P.nb + (nn) - 1]
+
+static void FN(pml3_iface)(const FN(ora_grid) *g, const FN(pml3_desc) *Pp, R *st, R *f, int fld)
+{
+    const FN(pml3_desc) P = *Pp;
+    for (int side = 0; side < 2; side++) {
+        const int lo = side == 0 ? 2 - P.nb : P.n[P.a] + 1, hi = lo + P.nb - 1;
+        const int to_w = side == 0 ? hi : lo, to_b = side == 0 ? hi - 1 : lo + 1;
+        int i[3];
+        i[P.a] = to_w;
+        for (i[P.t2] = 1; i[P.t2] <= P.n[P.t2] + 1; i[P.t2]++)
+            for (i[P.t1] = 1; i[P.t1] <= P.n[P.t1] + 1; i[P.t1]++)
+                for (int F = 0; F < 3; F++) {
+                    st[FN(pml3_at)(&P, side, fld, 2 * F, i)] = f[FN(gidx)(g, F, i[0], i[1], i[2])];
+                    st[FN(pml3_at)(&P, side, fld, 2 * F + 1, i)] = K(0.0);
+                }
+        i[P.a] = to_b;
+        for (i[P.t2] = 0; i[P.t2] <= P.n[P.t2] + 2; i[P.t2]++)
+            for (i[P.t1] = 0; i[P.t1] <= P.n[P.t1] + 2; i[P.t1]++)
+                for (int F = 0; F < 3; F++)
+                    f[FN(gidx)(g, F, i[0], i[1], i[2])] = st[FN(pml3_at)(&P, side, fld, 2 * F, i)] +
+                                                          st[FN(pml3_at)(&P, side, fld, 2 * F + 1, i)];
+    }
+}
+
+/* one E (fld 0) or B (fld 1) wall update */
+static void FN(pml3_update)(const FN(pml3_desc) *Pp, R *st, const double *dx, double dt, int fld)
+{
+    const FN(pml3_desc) P = *Pp;
+    const int src = 1 - fld;
+    for (int side = 0; side < 2; side++) {
+        const int lo = side == 0 ? 2 - P.nb : P.n[P.a] + 1, hi = lo + P.nb - 1;
+        const int r0 = fld == 0 ? lo + 1 : (side == 0 ? lo : lo + 1);
+        const int r1 = fld == 0 ? (side == 0 ? hi - 1 : hi) : hi - 1;
+        const int k = fld == 0 ? side : 2 + side;
+        const int cofs = side == 0 ? (fld == 0 ? lo - 1 : lo - 2) : lo;
+        const int t0 = fld == 0 ? 2 : 1, te = fld == 0 ? 0 : -1;   /* transverse ranges */
+        int i[3];
+        for (i[P.t2] = t0 - P.g1[P.t2]; i[P.t2] <= P.n[P.t2] + P.g2[P.t2] + te; i[P.t2]++)
+            for (i[P.t1] = t0 - P.g1[P.t1]; i[P.t1] <= P.n[P.t1] + P.g2[P.t1] + te; i[P.t1]++)
+                for (i[P.a] = r0; i[P.a] <= r1; i[P.a]++) {
+                    const int ci = i[P.a] - cofs;
+                    for (int F = 0; F < 3; F++)
+                        for (int s = 0; s < 2; s++) {
+                            const int o1 = F == 0 ? 1 : 0, o2 = F == 2 ? 1 : 2;
+                            const int D = s == 0 ? o1 : o2, G = 3 - F - D;
+                            /* E: +1 when D follows F cyclically; B: the opposite */
+                            const int cyc = D == (F + 1) % 3;
+                            const int sgn = fld == 0 ? (cyc ? 1 : -1) : (cyc ? -1 : 1);
+                            int q[3] = {i[0], i[1], i[2]};
+                            /* E: G at p and p - e_D; B: G at p + e_D and p */
+                            int qa[3] = {i[0], i[1], i[2]}, qb[3] = {i[0], i[1], i[2]};
+                            if (fld == 0) qb[D] -= 1;
+                            else qa[D] += 1;
+                            const R ga = st[FN(pml3_at)(&P, side, src, 2 * G, qa)] +
+                                         st[FN(pml3_at)(&P, side, src, 2 * G + 1, qa)];
+                            R *v = &st[FN(pml3_at)(&P, side, fld, 2 * F + s, q)];
+                            if (D == P.a) {
+                                const R c1 = P3COEF(P.a, k, 0, ci), c2 = P3COEF(P.a, k, 1, ci),
+                                        c3 = P3COEF(P.a, k, 2, ci);
+                                const R gb = st[FN(pml3_at)(&P, side, src, 2 * G, qb)] +
+                                             st[FN(pml3_at)(&P, side, src, 2 * G + 1, qb)];
+                                if (sgn > 0) *v = c1 * *v + c2 * ga - c3 * gb;
+                                else *v = c1 * *v - c2 * ga + c3 * gb;
+                            } else {
+                                const R dtdx = (R)(dt / dx[D]);
+                                const R d = st[FN(pml3_at)(&P, side, src, 2 * G, qa)] +
+                                            st[FN(pml3_at)(&P, side, src, 2 * G + 1, qa)] -
+                                            st[FN(pml3_at)(&P, side, src, 2 * G, qb)] -
+                                            st[FN(pml3_at)(&P, side, src, 2 * G + 1, qb)];
+                                if (sgn > 0) *v = *v + dtdx * d;
+                                else *v = *v - dtdx * d;
+                            }
+                        }
+                }
+    }
+}
+
+/* the walls' periodic update along both other axes (update_periodic_wall; along t1 first, then
+ * t2 over the full extent of t1) */
+static void FN(pml3_wall_guards)(const FN(pml3_desc) *Pp, R *st)
+{
+    const FN(pml3_desc) P = *Pp;
+    for (int side = 0; side < 2; side++) {
+        const int lo = side == 0 ? 2 - P.nb : P.n[P.a] + 1;
+        for (int pass = 0; pass < 2; pass++) {
+            const int t = pass == 0 ? P.t1 : P.t2, o = pass == 0 ? P.t2 : P.t1;
+            for (int fld = 0; fld < 2; fld++) {
+                int i[3], j[3];
+                for (i[P.a] = lo; i[P.a] < lo + P.nb; i[P.a]++)
+                    for (i[o] = 1 - P.g1[o]; i[o] <= P.n[o] + P.g2[o]; i[o]++) {
+                        j[P.a] = i[P.a];
+                        j[o] = i[o];
+                        for (i[t] = 1 - P.g1[t]; i[t] <= P.n[t] + P.g2[t]; i[t]++) {
+                            if (i[t] >= 1 && i[t] <= P.n[t]) continue;
+                            j[t] = i[t] < 1 ? i[t] + P.n[t] : i[t] - P.n[t];
+                            for (int c = 0; c < 6; c++)
+                                st[FN(pml3_at)(&P, side, fld, c, i)] = st[FN(pml3_at)(&P, side, fld, c, j)];
+                        }
+                    }
+            }
+        }
+    }
+}
+#undef P3COEF
+
 long FN(ora_pml_state_size)(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb)
 {
     FN(ora_grid) G;
     FN(grid_init)(&G, dim, nx, gcl, gcu);
+    if (dim == 3) return 4 * FN(pml3_make)(&G, mask, nb).W + 36L * nb;
     const FN(pml_desc) P = FN(pml_make)(&G, mask, nb);
     return P.T + 24L * nb;
 }
@@ -568,11 +720,12 @@ void FN(ora_pml_init)(int dim, const int *nx, const int *gcl, const int *gcu, in
 {
     FN(ora_grid) G, *g = &G;
     FN(grid_init)(g, dim, nx, gcl, gcu);
-    const FN(pml_desc) P = FN(pml_make)(g, mask, nb);
-    for (long i = 0; i < P.T + 24L * nb; i++) st[i] = K(0.0);
+    FN(pml_desc) P = FN(pml_make)(g, mask, nb);
+    if (dim == 3) P.T = 4 * FN(pml3_make)(g, mask, nb).W;   /* the tables follow the walls */
+    for (long i = 0; i < P.T + 12L * dim * nb; i++) st[i] = K(0.0);
     const double s1 = -(0.8 * (4.0 + 1.0)) / 2.0, s2 = 1.0 / (nb - 3);
 #define ATT(x) exp(s1 * ((s2 * (x)) * (s2 * (x))) * ((s2 * (x)) * (s2 * (x))))
-    for (int a = 0; a < 2; a++) {
+    for (int a = 0; a < dim; a++) {
         const double dtdx = dt / dx[a], dif = (1.0 - dtdx) / (1.0 + dtdx);
         for (int j = 0; j < nb; j++) {
             /* lower edge: B is the outer point; j = -1/2 is the interface */
@@ -832,6 +985,16 @@ void FN(ora_pml_phase)(int dim, const int *nx, const int *gcl, const int *gcu, i
 {
     FN(ora_grid) G, *g = &G;
     FN(grid_init)(g, dim, nx, gcl, gcu);
+    if (dim == 3) {
+        const FN(pml3_desc) Q = FN(pml3_make)(g, mask, nb);
+        if (what == 0) {
+            FN(pml3_wall_guards)(&Q, st);
+        } else {
+            FN(pml3_iface)(g, &Q, st, what == 1 ? b : e, what == 1 ? 1 : 0);
+            FN(pml3_update)(&Q, st, dx, dt, what == 1 ? 0 : 1);
+        }
+        return;
+    }
     const FN(pml_desc) P = FN(pml_make)(g, mask, nb);
     if (what == 0) {
         FN(pml_wall_guards)(&P, st);

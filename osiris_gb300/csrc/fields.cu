@@ -406,16 +406,177 @@ static PmlDesc pml_desc(const GridDesc &g, int mask, int nb)
     return P;
 }
 
+// 3D walls at both edges of one axis a (no edges or corners with other PML axes): six split
+// components per point, 2F + s for field component F, s = 0 the part driven by the derivative
+// along the lower of the two other axes (XY, YX, ZX), s = 1 the other (XZ, YZ, ZY)
+// (update_e_x{1,2,3}_3d, update_b_x{1,2,3}_3d, update_interface_x{1,2,3}_3d without their corner
+// branches).  The wall spans [1 - g1_t, n_t + g2_t] along both other axes t (g1 = max(gcl_t, 1),
+// g2 = max(gcu_t, 2)); wall (side, field) at (2 side + field) W, W = nte_t1 nte_t2 nb 6 (t1 < t2),
+// point (iw, i_t1, i_t2) component c at 6 (((i_t2 - 1 + g1_t2) nte_t1 + i_t1 - 1 + g1_t1) nb +
+// iw - lo(side)) + c; the tables of all three axes follow at 4 W.
+struct Pml3Desc {
+    int a, t1, t2, nb, n[3], g1[3], g2[3], nte[3];
+    long W;
+};
+
+static Pml3Desc pml3_desc(const GridDesc &g, int mask, int nb)
+{
+    Pml3Desc P;
+    P.a = mask == 1 ? 0 : (mask == 2 ? 1 : 2);
+    P.t1 = P.a == 0 ? 1 : 0;
+    P.t2 = P.a == 2 ? 1 : 2;
+    P.nb = nb;
+    for (int d = 0; d < 3; d++) {
+        P.n[d] = g.nx[d];
+        P.g1[d] = g.gcl[d] > 1 ? g.gcl[d] : 1;
+        P.g2[d] = g.gcu[d] > 2 ? g.gcu[d] : 2;
+        P.nte[d] = g.nx[d] + P.g1[d] + P.g2[d];
+    }
+    P.W = (long)P.nte[P.t1] * P.nte[P.t2] * nb * 6;
+    return P;
+}
+
+__device__ __forceinline__ long pml3_at(const Pml3Desc &P, int side, int fld, int c, const int *i)
+{
+    const int lo = side == 0 ? 2 - P.nb : P.n[P.a] + 1;
+    return (2 * side + fld) * P.W +
+           6 * ((((long)i[P.t2] - 1 + P.g1[P.t2]) * P.nte[P.t1] + i[P.t1] - 1 + P.g1[P.t1]) *
+                    P.nb + i[P.a] - lo) + c;
+}
+
+// interfaces: the box into the wall over [1, n + 1] of both other axes (first split the box's
+// component, second 0), the wall's sums into the box over [0, n + 2]; one thread per edge and
+// transverse point of the larger range
+template <typename T>
+__global__ void k_pml3_iface(GridDesc g, Pml3Desc P, T *__restrict__ st, T *__restrict__ f, int fld)
+{
+    const int m1 = P.n[P.t1] + 3, m2 = P.n[P.t2] + 3;
+    const long n = 2L * m1 * m2;
+    OSG_GRID_LOOP(m, n)
+    {
+        const int side = (int)(m / ((long)m1 * m2));
+        const int r = (int)(m % ((long)m1 * m2));
+        const int lo = side == 0 ? 2 - P.nb : P.n[P.a] + 1, hi = lo + P.nb - 1;
+        const int to_w = side == 0 ? hi : lo, to_b = side == 0 ? hi - 1 : lo + 1;
+        int i[3];
+        i[P.t1] = r % m1;
+        i[P.t2] = r / m1;
+        if (i[P.t1] >= 1 && i[P.t1] <= P.n[P.t1] + 1 && i[P.t2] >= 1 && i[P.t2] <= P.n[P.t2] + 1) {
+            i[P.a] = to_w;
+            const long pw = pos(g, i[0], i[1], i[2]);
+            for (int F = 0; F < 3; F++) {
+                st[pml3_at(P, side, fld, 2 * F, i)] = f[pw + F];
+                st[pml3_at(P, side, fld, 2 * F + 1, i)] = T(0);
+            }
+        }
+        i[P.a] = to_b;
+        const long pb = pos(g, i[0], i[1], i[2]);
+        for (int F = 0; F < 3; F++)
+            f[pb + F] = st[pml3_at(P, side, fld, 2 * F, i)] + st[pml3_at(P, side, fld, 2 * F + 1, i)];
+    }
+}
+
+// one E (fld 0) or B (fld 1) wall update: split (F, D) with G the third axis,
+// E_FD += sgn dt/dx_D (E: G at p and p - e_D), B_FD -= sgn dt/dx_D (G at p + e_D and p), sgn +1
+// when D follows F cyclically; damped with a's tables along D = a.  E reads only B and B only
+// E: one thread per edge and wall point
+template <typename T>
+__global__ void k_pml3_update(Pml3Desc P, T *__restrict__ st, T dx0, T dx1, T dx2, int fld)
+{
+    const long npl = (long)P.nte[P.t1] * P.nte[P.t2] * P.nb;
+    const long n = 2 * npl;
+    const T dtdx[3] = {dx0, dx1, dx2};
+    const long tab = 4 * P.W;
+    OSG_GRID_LOOP(m, n)
+    {
+        const int side = (int)(m / npl);
+        long r = m % npl;
+        const int lo = side == 0 ? 2 - P.nb : P.n[P.a] + 1, hi = lo + P.nb - 1;
+        int i[3];
+        i[P.a] = lo + (int)(r % P.nb);
+        r /= P.nb;
+        i[P.t1] = 1 - P.g1[P.t1] + (int)(r % P.nte[P.t1]);
+        i[P.t2] = 1 - P.g1[P.t2] + (int)(r / P.nte[P.t1]);
+        const int r0 = fld == 0 ? lo + 1 : (side == 0 ? lo : lo + 1);
+        const int r1 = fld == 0 ? (side == 0 ? hi - 1 : hi) : hi - 1;
+        if (i[P.a] < r0 || i[P.a] > r1) continue;
+        const int t0 = fld == 0 ? 2 : 1, te = fld == 0 ? 0 : -1;
+        if (i[P.t1] < t0 - P.g1[P.t1] || i[P.t1] > P.n[P.t1] + P.g2[P.t1] + te) continue;
+        if (i[P.t2] < t0 - P.g1[P.t2] || i[P.t2] > P.n[P.t2] + P.g2[P.t2] + te) continue;
+        const int k = fld == 0 ? side : 2 + side;
+        const int cofs = side == 0 ? (fld == 0 ? lo - 1 : lo - 2) : lo;
+        const int ci = i[P.a] - cofs;
+        const int src = 1 - fld;
+#pragma unroll
+        for (int F = 0; F < 3; F++)
+#pragma unroll
+            for (int sp = 0; sp < 2; sp++) {
+                const int o1 = F == 0 ? 1 : 0, o2 = F == 2 ? 1 : 2;
+                const int D = sp == 0 ? o1 : o2, G = 3 - F - D;
+                const bool cyc = D == (F + 1) % 3;
+                const int sgn = fld == 0 ? (cyc ? 1 : -1) : (cyc ? -1 : 1);
+                int qa[3] = {i[0], i[1], i[2]}, qb[3] = {i[0], i[1], i[2]};
+                if (fld == 0) qb[D] -= 1;
+                else qa[D] += 1;
+                T &v = st[pml3_at(P, side, fld, 2 * F + sp, i)];
+                const T a0 = st[pml3_at(P, side, src, 2 * G, qa)];
+                const T a1 = st[pml3_at(P, side, src, 2 * G + 1, qa)];
+                const T b0 = st[pml3_at(P, side, src, 2 * G, qb)];
+                const T b1 = st[pml3_at(P, side, src, 2 * G + 1, qb)];
+                if (D == P.a) {
+                    const T *cf = st + tab + (4 * P.a + k) * 3 * P.nb + ci - 1;
+                    const T c1 = cf[0], c2 = cf[P.nb], c3 = cf[2 * P.nb];
+                    const T ga = a0 + a1, gb = b0 + b1;
+                    if (sgn > 0) v = c1 * v + c2 * ga - c3 * gb;
+                    else v = c1 * v - c2 * ga + c3 * gb;
+                } else {
+                    const T d = a0 + a1 - b0 - b1;
+                    if (sgn > 0) v = v + dtdx[D] * d;
+                    else v = v - dtdx[D] * d;
+                }
+            }
+    }
+}
+
+// the walls' periodic update along one other axis t (pass 0: t1 over the wall's extent of t2;
+// pass 1: t2 over the full extent of t1, guards included)
+template <typename T>
+__global__ void k_pml3_guard(Pml3Desc P, T *__restrict__ st, int pass)
+{
+    const int t = pass == 0 ? P.t1 : P.t2, o = pass == 0 ? P.t2 : P.t1;
+    const int ng = P.g1[t] + P.g2[t];
+    const long n = 4L * P.nb * P.nte[o] * ng;
+    OSG_GRID_LOOP(m, n)
+    {
+        long r = m;
+        const int gi = (int)(r % ng);
+        r /= ng;
+        int i[3], j[3];
+        i[o] = 1 - P.g1[o] + (int)(r % P.nte[o]);
+        r /= P.nte[o];
+        const int iw = (int)(r % P.nb), wall = (int)(r / P.nb);
+        const int side = wall >> 1, fld = wall & 1;
+        i[P.a] = (side == 0 ? 2 - P.nb : P.n[P.a] + 1) + iw;
+        i[t] = gi < P.g1[t] ? 1 - P.g1[t] + gi : P.n[t] + 1 + (gi - P.g1[t]);
+        j[P.a] = i[P.a];
+        j[o] = i[o];
+        j[t] = gi < P.g1[t] ? i[t] + P.n[t] : i[t] - P.n[t];
+        for (int c = 0; c < 6; c++) st[pml3_at(P, side, fld, c, i)] = st[pml3_at(P, side, fld, c, j)];
+    }
+}
+
 long pml_state_size(const GridDesc &g, int mask, int nb)
 {
+    if (g.dim == 3) return 4 * pml3_desc(g, mask, nb).W + 36L * nb;
     return pml_desc(g, mask, nb).T + 24L * nb;
 }
 
 template <typename T>
 void pml_init_host(const GridDesc &g, int mask, int nb, const double *dx, double dt, T *st)
 {
-    const PmlDesc P = pml_desc(g, mask, nb);
-    const long n = P.T + 24L * nb;
+    // the tables follow the walls (2D: per PML axis; 3D: the one axis)
+    const long tab = g.dim == 3 ? 4 * pml3_desc(g, mask, nb).W : pml_desc(g, mask, nb).T;
+    const long n = tab + 12L * g.dim * nb;
     for (long i = 0; i < n; i++) st[i] = T(0);
     // t(x) = exp(s1 (s2 x)^4) with s1 = -0.8 (4 + 1) / 2, s2 = 1 / (nb - 3); the fourth power
     // as two squares (the reference's exponent is the real constant 4.0 and its base is
@@ -425,8 +586,8 @@ void pml_init_host(const GridDesc &g, int mask, int nb, const double *dx, double
         const double y = s2 * x;
         return exp(s1 * (y * y) * (y * y));
     };
-    for (int a = 0; a < 2; a++) {
-        T *cf = st + P.T + 12L * a * nb;
+    for (int a = 0; a < g.dim; a++) {
+        T *cf = st + tab + 12L * a * nb;
         auto at = [&](int k, int m, int c) -> T & { return cf[(3 * k + m) * nb + c - 1]; };
         const double dtdx = dt / dx[a], dif = (1.0 - dtdx) / (1.0 + dtdx);
         for (int j = 0; j < nb; j++) {
@@ -677,6 +838,24 @@ template <typename T>
 void pml_phase(const GridDesc &g, int mask, int nb, int what, T *e, T *b, T *pml,
                const double *dx, double dt, cudaStream_t st)
 {
+    if (g.dim == 3) {
+        const Pml3Desc Q = pml3_desc(g, mask, nb);
+        if (what == 0) {
+            for (int pass = 0; pass < 2; pass++) {
+                const int t = pass == 0 ? Q.t1 : Q.t2, o = pass == 0 ? Q.t2 : Q.t1;
+                const long n = 4L * nb * Q.nte[o] * (Q.g1[t] + Q.g2[t]);
+                k_pml3_guard<T><<<blocks_for(n, 256), 256, 0, st>>>(Q, pml, pass);
+            }
+            return;
+        }
+        const long ni = 2L * (Q.n[Q.t1] + 3) * (Q.n[Q.t2] + 3);
+        k_pml3_iface<T><<<blocks_for(ni, 256), 256, 0, st>>>(g, Q, pml, what == 1 ? b : e,
+                                                             what == 1 ? 1 : 0);
+        const long nu = 2L * Q.nte[Q.t1] * Q.nte[Q.t2] * nb;
+        k_pml3_update<T><<<blocks_for(nu, 256), 256, 0, st>>>(
+            Q, pml, (T)(dt / dx[0]), (T)(dt / dx[1]), (T)(dt / dx[2]), what == 1 ? 0 : 1);
+        return;
+    }
     const PmlDesc P = pml_desc(g, mask, nb);
     if (what == 0) {
         for (int a = 0; a < 2; a++) {

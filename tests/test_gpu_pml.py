@@ -12,6 +12,8 @@ absorbed.  Whole field arrays are compared, guard cells included (the interfaces
   the live particles against the oracle, either axis and both;
 * a vacuum pulse travelling along the PML axis leaves the box with less than 1e-4 of its
   energy, in both engines; with both axes, a cylindrical pulse leaves less than 1e-4;
+* 3D, one PML axis: plain FP64 1e-12 and tiled FP32 5e-5 against the oracle after 6 steps,
+  each axis; a plane pulse leaves less than 1e-4 of its energy;
 * checkpoint / restore keeps the walls: 4 + 4 steps equal 8 steps to 1e-12;
 * configurations the walls are not built for are refused.
 """
@@ -216,7 +218,71 @@ def test_pml_refuses_what_it_is_not_built_for(osg, kw):
                        engine=osg.ENGINE_PLAIN, **kw)
 
 
-def test_pml_is_2d(osg):
+def test_pml_3d_one_axis_only(osg):
     with pytest.raises(osg.OsirisGB300Error):
         osg.Simulation([8, 8, 8], [0.1] * 3, 0.03, order=2, precision=64,
-                       engine=osg.ENGINE_PLAIN, pml=1)
+                       engine=osg.ENGINE_PLAIN, pml=3)
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("engine,prec,tol", [("plain", 64, 1e-12), ("tiled", 32, 5e-5)])
+def test_pml_3d_matches_oracle(osg, oracle, engine, prec, tol, axis):
+    nx = [12, 10, 8]
+    p, g, dx, dt, species, e, b = _setup(oracle, prec, 3, 2, nx, [2, 2, 2], 21, uth=0.6,
+                                         ufl=0.1)
+    sim = osg.Simulation(nx, dx, dt, order=2, precision=prec,
+                         engine=osg.ENGINE_PLAIN if engine == "plain" else osg.ENGINE_TILED,
+                         tile=[4, 4, 4] if engine == "tiled" else None, pml=1 << axis)
+    sim.set_fields(e, b)
+    for s_ in species:
+        sim.add_species(s_["rqm"], s_["ix"], s_["x"], s_["u"], s_["q"])
+    steps = 6
+    sim.step(steps)
+    eg, bg, jg = sim.fields()
+    eo, bo, jo, ora = _oracle_run(oracle, g, p, e, b, species, dt, 1 << axis, steps)
+    errs = {"E": _nerr(eg, eo), "B": _nerr(bg, bo), "J": _nerr(jg, jo)}
+    for k, s_ in enumerate(ora):
+        ix, x, u, q = sim.species(k)
+        if engine == "plain":
+            errs[f"x{k}"] = _nerr(ix + x, s_["ix"] + s_["x"])
+            errs[f"u{k}"] = _nerr(u, s_["u"])
+            assert np.array_equal(q == 0, s_["q"] == 0)
+        else:
+            live = s_["q"] != 0
+            assert len(q) == int(live.sum())
+            a = np.argsort(q, kind="stable")
+            o = np.flatnonzero(live)[np.argsort(s_["q"][live], kind="stable")]
+            errs[f"x{k}"] = _nerr(ix[a] + x[a], s_["ix"][o] + s_["x"][o])
+            errs[f"u{k}"] = _nerr(u[a], s_["u"][o])
+    sim.close()
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, (bad, errs)
+
+
+@pytest.mark.parametrize("axis", [0, 2])
+def test_3d_plane_pulse_leaves_through_the_pml(osg, axis):
+    nx = [8, 8, 8]
+    nx[axis] = 96
+    dx = [0.2] * 3
+    dt = 0.9 / np.sqrt(sum(1 / d ** 2 for d in dx))
+    sim = osg.Simulation(nx, dx, dt, order=2, precision=64, engine=osg.ENGINE_PLAIN,
+                         pml=1 << axis)
+    gl, gu = osg.GUARD[2]
+    shape = tuple(reversed([n + gl + gu for n in nx])) + (3,)
+    e, b = np.zeros(shape), np.zeros(shape)
+    L = nx[axis] * dx[axis]
+    i = np.arange(shape[2 - axis]) - gl
+    prof = lambda x: np.exp(-((x - 0.5 * L) / (0.08 * L)) ** 2)
+    shp = [1, 1, 1]
+    shp[2 - axis] = shape[2 - axis]
+    e[..., (axis + 1) % 3] = prof(i * dx[axis]).reshape(shp)
+    b[..., (axis + 2) % 3] = prof((i + 0.5) * dx[axis]).reshape(shp)
+    sim.set_fields(e, b)
+    empty = np.zeros((0, 3), np.int32), np.zeros((0, 3)), np.zeros((0, 3)), np.zeros(0)
+    sim.add_species(-1.0, *empty)
+    sl = (slice(gl, gl + nx[2]), slice(gl, gl + nx[1]), slice(gl, gl + nx[0]))
+    w0 = float((e[sl] ** 2).sum() + (b[sl] ** 2).sum())
+    sim.step(int(L / dt))
+    e1, b1, _ = sim.fields()
+    assert float((e1[sl] ** 2).sum() + (b1[sl] ** 2).sum()) / w0 < 1e-4
+    sim.close()

@@ -9,6 +9,8 @@ one axis of a 2D box), on the CPU:
   than 1e-4 of its energy, while the same box without PML keeps its energy to 1e-5;
 * with PML on both axes (the x1 walls covering the corners) a cylindrical pulse leaves the box
   with less than 1e-5 of its energy; with one PML axis most of it stays (the other is periodic);
+* 3D, one PML axis (six split components per wall point): a plane pulse along that axis, either
+  direction, leaves less than 1e-8 of its energy;
 * the state is four split-field walls per PML axis plus the tables.
 """
 import numpy as np
@@ -110,3 +112,24 @@ def test_corners_absorb_a_cylindrical_pulse():
         assert np.isfinite(e).all() and np.isfinite(b).all()
         left[mask] = _energy(g, e, b) / w0
     assert left[3] < 1e-5 and left[1] > 1e-2, left
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("sign", [1, -1])
+def test_3d_plane_pulse_is_absorbed(axis, sign):
+    nx = [8, 8, 8]
+    nx[axis] = 64
+    g = po.Grid(nx, 2, [0.1, 0.1, 0.1])
+    e, b, j = g.zeros("f64"), g.zeros("f64"), g.zeros("f64")
+    n = g.size[axis]
+    pos = (np.arange(n) - n / 2) * 0.1
+    shp = [1, 1, 1]
+    shp[2 - axis] = n
+    # E along the next axis, B along the one after: E x B points along +axis
+    e[..., (axis + 1) % 3] = np.exp(-(pos / 0.5) ** 2).reshape(shp)
+    b[..., (axis + 2) % 3] = sign * np.exp(-((pos + 0.05) / 0.5) ** 2).reshape(shp)
+    w0 = _energy(g, e, b)
+    st = po.pml_state(g, "f64", 1 << axis, NB, 0.04)
+    for _ in range(200):
+        po.step(g, "f64", e, b, j, [], 0.04, pml=(1 << axis, NB, st))
+    assert _energy(g, e, b) / w0 < 1e-8
