@@ -227,7 +227,7 @@ def test_pml_3d_one_axis_only(osg):
 @pytest.mark.parametrize("axis", [0, 1, 2])
 @pytest.mark.parametrize("engine,prec,tol", [("plain", 64, 1e-12), ("tiled", 32, 5e-5)])
 def test_pml_3d_matches_oracle(osg, oracle, engine, prec, tol, axis):
-    nx = [12, 10, 8]
+    nx = [12, 8, 8]
     p, g, dx, dt, species, e, b = _setup(oracle, prec, 3, 2, nx, [2, 2, 2], 21, uth=0.6,
                                          ufl=0.1)
     sim = osg.Simulation(nx, dx, dt, order=2, precision=prec,
