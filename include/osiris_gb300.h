@@ -340,10 +340,10 @@ typedef struct {
                              their guard update, filtered by OSG_SMOOTH_* (all axes); E and B
                              themselves are not changed.  Periodic boxes. */
     int emf_smooth_order; /* its order */
-    int pml;          /* bit d set (2D; one axis in 3D): both edges of axis d are perfectly
-                         matched layers (Vay's split-field PML, the reference's "vpml" field
-                         boundary) of pml_cells cells each (2D with both axes set: the x1
-                         walls cover the corners), and particles leaving through them are
+    int pml;          /* bit d set (2D, 3D): both edges of axis d are perfectly matched layers
+                         (Vay's split-field PML, the reference's "vpml" field boundary) of
+                         pml_cells cells each (the walls of a lower axis cover the edge regions
+                         of the higher PML axes), and particles leaving through them are
                          absorbed; not with walls, Lindman boundaries, smoothing, a thermal
                          bath or the moving window */
     int pml_cells;    /* PML thickness in cells (0 = the reference default 8; at least 5) */

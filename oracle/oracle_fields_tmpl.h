@@ -539,121 +539,180 @@ static FN(pml_desc) FN(pml_make)(const FN(ora_grid) *g, int mask, int nb)
     return P;
 }
 
-/* 3D PML walls at both edges of one axis a (no edges or corners with other PML axes),
- * restated from update_e_x{1,2,3}_3d (:1172-1704), update_b_x{1,2,3}_3d (:2311-2828) and
- * update_interface_x{1,2,3}_3d (:2997-3529) without their corner branches.  A wall point holds
- * six split components (:444-446): 2F + s for field component F with s = 0 the part driven by
- * the derivative along the lower of the two other axes (XY, YX, ZX) and s = 1 the other (XZ,
- * YZ, ZY).  Split (F, D) with G the third axis: E_FD += sgn dt/dx_D (B_G(p) - B_G(p - e_D)),
- * sgn = +1 when D follows F cyclically, -1 otherwise (the curl); B_FD -= sgn dt/dx_D
- * (E_G(p + e_D) - E_G(p)); B_G / E_G the sum of G's two splits.  Along D = a the update is the
- * damped one with a's tables.  The wall spans [1 - g1_t, n_t + g2_t] along both other axes t
- * (g1 = max(gcl_t, 1), g2 = max(gcu_t, 2)).
- * State layout: wall (side, field) at (2 side + field) W, W = nte_t1 nte_t2 nb 6 (t1 < t2 the
- * other axes); point (iw, i_t1, i_t2) component c at
- * 6 (((i_t2 - 1 + g1_t2) nte_t1 + i_t1 - 1 + g1_t1) nb + iw - lo(side)) + c; then the tables of
- * all three axes at 4 W: axis x, table k, coefficient m, cell n at 4 W + ((4 x + k) 3 + m) nb +
- * n - 1. */
+/* 3D PML walls at both edges of the axes in a mask, restated from update_e_x{1,2,3}_3d
+ * (:1172-1704), update_b_x{1,2,3}_3d (:2311-2828) and update_interface_x{1,2,3}_3d
+ * (:2997-3529).  A wall point holds six split components (:444-446): 2F + s for field component
+ * F with s = 0 the part driven by the derivative along the lower of the two other axes (XY, YX,
+ * ZX) and s = 1 the other (XZ, YZ, ZY).  Split (F, D) with G the third axis:
+ * E_FD += sgn dt/dx_D (B_G(p) - B_G(p - e_D)), sgn = +1 when D follows F cyclically, -1
+ * otherwise (the curl); B_FD -= sgn dt/dx_D (E_G(p + e_D) - E_G(p)); B_G / E_G the sum of G's
+ * two splits.  Along D = a (the wall's axis) the update is the damped one with a's tables; the
+ * walls of a lower axis than a PML axis D extend over D's edge regions (corner priority
+ * x1 > x2 > x3, setup_vpml :382-430), where their D splits are damped with D's tables (the
+ * corner branches).  The wall of axis a spans [1 - g1, n_t + g2] along each other axis t:
+ * g1 = max(gcl_t, c - 1), g2 = max(gcu_t, c), c = nb when t has PML walls and a < t, else 2.
+ * State layout: per PML axis a in increasing order, walls (side, field) at base_a + (2 side +
+ * field) W_a, W_a = nte_a,t1 nte_a,t2 nb 6 (t1 < t2 the other axes); point (iw, i_t1, i_t2)
+ * component c at 6 (((i_t2 - 1 + g1_t2) nte_t1 + i_t1 - 1 + g1_t1) nb + iw - lo(side)) + c;
+ * then the tables of all three axes at T: axis x, table k, coefficient m, cell n at
+ * T + ((4 x + k) 3 + m) nb + n - 1. */
 typedef struct {
-    int a, t1, t2, nb, n[3], g1[3], g2[3], nte[3];
-    long W;
+    int mask, nb, n[3];
+    int g1[3][3], g2[3][3], nte[3][3];   /* [wall axis][other axis] */
+    long W[3], base[3], T;
 } FN(pml3_desc);
 
 static FN(pml3_desc) FN(pml3_make)(const FN(ora_grid) *g, int mask, int nb)
 {
     FN(pml3_desc) P;
-    P.a = mask == 1 ? 0 : (mask == 2 ? 1 : 2);
-    P.t1 = P.a == 0 ? 1 : 0;
-    P.t2 = P.a == 2 ? 1 : 2;
+    P.mask = mask;
     P.nb = nb;
-    for (int d = 0; d < 3; d++) {
-        P.n[d] = g->nx[d];
-        P.g1[d] = g->gcl[d] > 1 ? g->gcl[d] : 1;
-        P.g2[d] = g->gcu[d] > 2 ? g->gcu[d] : 2;
-        P.nte[d] = g->nx[d] + P.g1[d] + P.g2[d];
+    long off = 0;
+    for (int d = 0; d < 3; d++) P.n[d] = g->nx[d];
+    for (int a = 0; a < 3; a++) {
+        long w = (long)nb * 6;
+        for (int t = 0; t < 3; t++) {
+            const int c = (((mask >> t) & 1) && a < t) ? nb : 2;
+            P.g1[a][t] = g->gcl[t] > c - 1 ? g->gcl[t] : c - 1;
+            P.g2[a][t] = g->gcu[t] > c ? g->gcu[t] : c;
+            P.nte[a][t] = g->nx[t] + P.g1[a][t] + P.g2[a][t];
+            if (t != a) w *= P.nte[a][t];
+        }
+        P.W[a] = w;
+        P.base[a] = off;
+        if ((mask >> a) & 1) off += 4 * w;
     }
-    P.W = (long)P.nte[P.t1] * P.nte[P.t2] * nb * 6;
+    P.T = off;
     return P;
 }
 
-static inline long FN(pml3_at)(const FN(pml3_desc) *P, int side, int fld, int c, const int *i)
+static inline long FN(pml3_at)(const FN(pml3_desc) *P, int a, int side, int fld, int c,
+                               const int *i)
 {
-    const int lo = side == 0 ? 2 - P->nb : P->n[P->a] + 1;
-    return (2 * side + fld) * P->W +
-           6 * ((((long)i[P->t2] - 1 + P->g1[P->t2]) * P->nte[P->t1] + i[P->t1] - 1 +
-                 P->g1[P->t1]) * P->nb + i[P->a] - lo) + c;
+    const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+    const int lo = side == 0 ? 2 - P->nb : P->n[a] + 1;
+    return P->base[a] + (2 * side + fld) * P->W[a] +
+           6 * ((((long)i[t2] - 1 + P->g1[a][t2]) * P->nte[a][t1] + i[t1] - 1 + P->g1[a][t1]) *
+                    P->nb + i[a] - lo) + c;
 }
 
-#define P3COEF(x, k, m, nn) st[4 * P.W + ((4 * (x) + (k)) * 3 + (m)) * P.nb + (nn) - 1]
+#define P3COEF(x, k, m, nn) st[P.T + ((4 * (x) + (k)) * 3 + (m)) * P.nb + (nn) - 1]
 
-static void FN(pml3_iface)(const FN(ora_grid) *g, const FN(pml3_desc) *Pp, R *st, R *f, int fld)
+/* the interfaces of the walls of axis a with the box (the box into the first split over
+ * [1, n + 1] of the other axes, the second split 0; the wall's sums into the box over
+ * [0, n + 2]), then their contacts with the walls of the higher PML axes: below, the other wall
+ * takes this wall's plane 0 and gives it plane 1; above, this wall takes plane n_a + 1 and
+ * gives n_a + 2, over the other wall's edge rows along its axis and, along the remaining axis,
+ * [1 - g1, n + g2] of this wall for the x1 walls' x2 contacts, else [1, n + 1] */
+static void FN(pml3_iface)(const FN(ora_grid) *g, const FN(pml3_desc) *Pp, R *st, R *f, int fld,
+                           int a)
 {
     const FN(pml3_desc) P = *Pp;
+    const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
     for (int side = 0; side < 2; side++) {
-        const int lo = side == 0 ? 2 - P.nb : P.n[P.a] + 1, hi = lo + P.nb - 1;
+        const int lo = side == 0 ? 2 - P.nb : P.n[a] + 1, hi = lo + P.nb - 1;
         const int to_w = side == 0 ? hi : lo, to_b = side == 0 ? hi - 1 : lo + 1;
         int i[3];
-        i[P.a] = to_w;
-        for (i[P.t2] = 1; i[P.t2] <= P.n[P.t2] + 1; i[P.t2]++)
-            for (i[P.t1] = 1; i[P.t1] <= P.n[P.t1] + 1; i[P.t1]++)
+        i[a] = to_w;
+        for (i[t2] = 1; i[t2] <= P.n[t2] + 1; i[t2]++)
+            for (i[t1] = 1; i[t1] <= P.n[t1] + 1; i[t1]++)
                 for (int F = 0; F < 3; F++) {
-                    st[FN(pml3_at)(&P, side, fld, 2 * F, i)] = f[FN(gidx)(g, F, i[0], i[1], i[2])];
-                    st[FN(pml3_at)(&P, side, fld, 2 * F + 1, i)] = K(0.0);
+                    st[FN(pml3_at)(&P, a, side, fld, 2 * F, i)] = f[FN(gidx)(g, F, i[0], i[1], i[2])];
+                    st[FN(pml3_at)(&P, a, side, fld, 2 * F + 1, i)] = K(0.0);
                 }
-        i[P.a] = to_b;
-        for (i[P.t2] = 0; i[P.t2] <= P.n[P.t2] + 2; i[P.t2]++)
-            for (i[P.t1] = 0; i[P.t1] <= P.n[P.t1] + 2; i[P.t1]++)
+        i[a] = to_b;
+        for (i[t2] = 0; i[t2] <= P.n[t2] + 2; i[t2]++)
+            for (i[t1] = 0; i[t1] <= P.n[t1] + 2; i[t1]++)
                 for (int F = 0; F < 3; F++)
-                    f[FN(gidx)(g, F, i[0], i[1], i[2])] = st[FN(pml3_at)(&P, side, fld, 2 * F, i)] +
-                                                          st[FN(pml3_at)(&P, side, fld, 2 * F + 1, i)];
+                    f[FN(gidx)(g, F, i[0], i[1], i[2])] = st[FN(pml3_at)(&P, a, side, fld, 2 * F, i)] +
+                                                          st[FN(pml3_at)(&P, a, side, fld, 2 * F + 1, i)];
+        for (int d = a + 1; d < 3; d++) {
+            if (!((P.mask >> d) & 1)) continue;
+            const int o = 3 - a - d;   /* the remaining axis */
+            const int olo = (a == 0 && d == 1) ? 1 - P.g1[a][o] : 1;
+            const int ohi = (a == 0 && d == 1) ? P.n[o] + P.g2[a][o] : P.n[o] + 1;
+            for (int adj = 0; adj < 2; adj++) {
+                const int r0 = adj == 0 ? 2 - P.nb : P.n[d] + 2, r1 = adj == 0 ? 0 : P.n[d] + P.nb;
+                for (i[d] = r0; i[d] <= r1; i[d]++)
+                    for (i[o] = olo; i[o] <= ohi; i[o]++)
+                        for (int c = 0; c < 6; c++) {
+                            if (side == 0) {
+                                i[a] = 0;
+                                st[FN(pml3_at)(&P, d, adj, fld, c, i)] = st[FN(pml3_at)(&P, a, 0, fld, c, i)];
+                                i[a] = 1;
+                                st[FN(pml3_at)(&P, a, 0, fld, c, i)] = st[FN(pml3_at)(&P, d, adj, fld, c, i)];
+                            } else {
+                                i[a] = P.n[a] + 1;
+                                st[FN(pml3_at)(&P, a, 1, fld, c, i)] = st[FN(pml3_at)(&P, d, adj, fld, c, i)];
+                                i[a] = P.n[a] + 2;
+                                st[FN(pml3_at)(&P, d, adj, fld, c, i)] = st[FN(pml3_at)(&P, a, 1, fld, c, i)];
+                            }
+                        }
+            }
+        }
     }
 }
 
-/* one E (fld 0) or B (fld 1) wall update */
-static void FN(pml3_update)(const FN(pml3_desc) *Pp, R *st, const double *dx, double dt, int fld)
+/* one E (fld 0) or B (fld 1) update of the walls of axis a */
+static void FN(pml3_update)(const FN(pml3_desc) *Pp, R *st, const double *dx, double dt, int fld,
+                            int a)
 {
     const FN(pml3_desc) P = *Pp;
+    const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
     const int src = 1 - fld;
     for (int side = 0; side < 2; side++) {
-        const int lo = side == 0 ? 2 - P.nb : P.n[P.a] + 1, hi = lo + P.nb - 1;
+        const int lo = side == 0 ? 2 - P.nb : P.n[a] + 1, hi = lo + P.nb - 1;
         const int r0 = fld == 0 ? lo + 1 : (side == 0 ? lo : lo + 1);
         const int r1 = fld == 0 ? (side == 0 ? hi - 1 : hi) : hi - 1;
         const int k = fld == 0 ? side : 2 + side;
         const int cofs = side == 0 ? (fld == 0 ? lo - 1 : lo - 2) : lo;
         const int t0 = fld == 0 ? 2 : 1, te = fld == 0 ? 0 : -1;   /* transverse ranges */
         int i[3];
-        for (i[P.t2] = t0 - P.g1[P.t2]; i[P.t2] <= P.n[P.t2] + P.g2[P.t2] + te; i[P.t2]++)
-            for (i[P.t1] = t0 - P.g1[P.t1]; i[P.t1] <= P.n[P.t1] + P.g2[P.t1] + te; i[P.t1]++)
-                for (i[P.a] = r0; i[P.a] <= r1; i[P.a]++) {
-                    const int ci = i[P.a] - cofs;
+        for (i[t2] = t0 - P.g1[a][t2]; i[t2] <= P.n[t2] + P.g2[a][t2] + te; i[t2]++)
+            for (i[t1] = t0 - P.g1[a][t1]; i[t1] <= P.n[t1] + P.g2[a][t1] + te; i[t1]++)
+                for (i[a] = r0; i[a] <= r1; i[a]++) {
+                    const int ci = i[a] - cofs;
                     for (int F = 0; F < 3; F++)
-                        for (int s = 0; s < 2; s++) {
+                        for (int sp = 0; sp < 2; sp++) {
                             const int o1 = F == 0 ? 1 : 0, o2 = F == 2 ? 1 : 2;
-                            const int D = s == 0 ? o1 : o2, G = 3 - F - D;
+                            const int D = sp == 0 ? o1 : o2, G = 3 - F - D;
                             /* E: +1 when D follows F cyclically; B: the opposite */
                             const int cyc = D == (F + 1) % 3;
                             const int sgn = fld == 0 ? (cyc ? 1 : -1) : (cyc ? -1 : 1);
-                            int q[3] = {i[0], i[1], i[2]};
-                            /* E: G at p and p - e_D; B: G at p + e_D and p */
                             int qa[3] = {i[0], i[1], i[2]}, qb[3] = {i[0], i[1], i[2]};
                             if (fld == 0) qb[D] -= 1;
                             else qa[D] += 1;
-                            const R ga = st[FN(pml3_at)(&P, side, src, 2 * G, qa)] +
-                                         st[FN(pml3_at)(&P, side, src, 2 * G + 1, qa)];
-                            R *v = &st[FN(pml3_at)(&P, side, fld, 2 * F + s, q)];
-                            if (D == P.a) {
-                                const R c1 = P3COEF(P.a, k, 0, ci), c2 = P3COEF(P.a, k, 1, ci),
-                                        c3 = P3COEF(P.a, k, 2, ci);
-                                const R gb = st[FN(pml3_at)(&P, side, src, 2 * G, qb)] +
-                                             st[FN(pml3_at)(&P, side, src, 2 * G + 1, qb)];
+                            R *v = &st[FN(pml3_at)(&P, a, side, fld, 2 * F + sp, i)];
+                            /* damped along D: the wall's own axis, or an edge region of a higher
+                               PML axis D */
+                            int dk = -1, dn = 0;
+                            if (D == a) {
+                                dk = k;
+                                dn = ci;
+                            } else if (((P.mask >> D) & 1) && a < D) {
+                                if (i[D] <= 0) {
+                                    dk = fld == 0 ? 0 : 2;
+                                    dn = i[D] + P.g1[a][D] + (fld == 0 ? 0 : 1);
+                                } else if (i[D] > P.n[D] + 1) {
+                                    dk = fld == 0 ? 1 : 3;
+                                    dn = i[D] - P.n[D] - 1;
+                                }
+                            }
+                            if (dk >= 0) {
+                                const R c1 = P3COEF(D, dk, 0, dn), c2 = P3COEF(D, dk, 1, dn),
+                                        c3 = P3COEF(D, dk, 2, dn);
+                                const R ga = st[FN(pml3_at)(&P, a, side, src, 2 * G, qa)] +
+                                             st[FN(pml3_at)(&P, a, side, src, 2 * G + 1, qa)];
+                                const R gb = st[FN(pml3_at)(&P, a, side, src, 2 * G, qb)] +
+                                             st[FN(pml3_at)(&P, a, side, src, 2 * G + 1, qb)];
                                 if (sgn > 0) *v = c1 * *v + c2 * ga - c3 * gb;
                                 else *v = c1 * *v - c2 * ga + c3 * gb;
                             } else {
                                 const R dtdx = (R)(dt / dx[D]);
-                                const R d = st[FN(pml3_at)(&P, side, src, 2 * G, qa)] +
-                                            st[FN(pml3_at)(&P, side, src, 2 * G + 1, qa)] -
-                                            st[FN(pml3_at)(&P, side, src, 2 * G, qb)] -
-                                            st[FN(pml3_at)(&P, side, src, 2 * G + 1, qb)];
+                                const R d = st[FN(pml3_at)(&P, a, side, src, 2 * G, qa)] +
+                                            st[FN(pml3_at)(&P, a, side, src, 2 * G + 1, qa)] -
+                                            st[FN(pml3_at)(&P, a, side, src, 2 * G, qb)] -
+                                            st[FN(pml3_at)(&P, a, side, src, 2 * G + 1, qb)];
                                 if (sgn > 0) *v = *v + dtdx * d;
                                 else *v = *v - dtdx * d;
                             }
@@ -662,28 +721,34 @@ static void FN(pml3_update)(const FN(pml3_desc) *Pp, R *st, const double *dx, do
     }
 }
 
-/* the walls' periodic update along both other axes (update_periodic_wall; along t1 first, then
- * t2 over the full extent of t1) */
+/* the walls' periodic update along the periodic other axes (update_periodic_wall; the lower
+ * axis first, then the higher over the full extent of the lower) */
 static void FN(pml3_wall_guards)(const FN(pml3_desc) *Pp, R *st)
 {
     const FN(pml3_desc) P = *Pp;
-    for (int side = 0; side < 2; side++) {
-        const int lo = side == 0 ? 2 - P.nb : P.n[P.a] + 1;
-        for (int pass = 0; pass < 2; pass++) {
-            const int t = pass == 0 ? P.t1 : P.t2, o = pass == 0 ? P.t2 : P.t1;
-            for (int fld = 0; fld < 2; fld++) {
-                int i[3], j[3];
-                for (i[P.a] = lo; i[P.a] < lo + P.nb; i[P.a]++)
-                    for (i[o] = 1 - P.g1[o]; i[o] <= P.n[o] + P.g2[o]; i[o]++) {
-                        j[P.a] = i[P.a];
-                        j[o] = i[o];
-                        for (i[t] = 1 - P.g1[t]; i[t] <= P.n[t] + P.g2[t]; i[t]++) {
-                            if (i[t] >= 1 && i[t] <= P.n[t]) continue;
-                            j[t] = i[t] < 1 ? i[t] + P.n[t] : i[t] - P.n[t];
-                            for (int c = 0; c < 6; c++)
-                                st[FN(pml3_at)(&P, side, fld, c, i)] = st[FN(pml3_at)(&P, side, fld, c, j)];
+    for (int a = 0; a < 3; a++) {
+        if (!((P.mask >> a) & 1)) continue;
+        const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+        for (int side = 0; side < 2; side++) {
+            const int lo = side == 0 ? 2 - P.nb : P.n[a] + 1;
+            for (int pass = 0; pass < 2; pass++) {
+                const int t = pass == 0 ? t1 : t2, o = pass == 0 ? t2 : t1;
+                if ((P.mask >> t) & 1) continue;
+                for (int fld = 0; fld < 2; fld++) {
+                    int i[3], j[3];
+                    for (i[a] = lo; i[a] < lo + P.nb; i[a]++)
+                        for (i[o] = 1 - P.g1[a][o]; i[o] <= P.n[o] + P.g2[a][o]; i[o]++) {
+                            j[a] = i[a];
+                            j[o] = i[o];
+                            for (i[t] = 1 - P.g1[a][t]; i[t] <= P.n[t] + P.g2[a][t]; i[t]++) {
+                                if (i[t] >= 1 && i[t] <= P.n[t]) continue;
+                                j[t] = i[t] < 1 ? i[t] + P.n[t] : i[t] - P.n[t];
+                                for (int c = 0; c < 6; c++)
+                                    st[FN(pml3_at)(&P, a, side, fld, c, i)] =
+                                        st[FN(pml3_at)(&P, a, side, fld, c, j)];
+                            }
                         }
-                    }
+                }
             }
         }
     }
@@ -694,7 +759,7 @@ long FN(ora_pml_state_size)(int dim, const int *nx, const int *gcl, const int *g
 {
     FN(ora_grid) G;
     FN(grid_init)(&G, dim, nx, gcl, gcu);
-    if (dim == 3) return 4 * FN(pml3_make)(&G, mask, nb).W + 36L * nb;
+    if (dim == 3) return FN(pml3_make)(&G, mask, nb).T + 36L * nb;
     const FN(pml_desc) P = FN(pml_make)(&G, mask, nb);
     return P.T + 24L * nb;
 }
@@ -721,7 +786,7 @@ void FN(ora_pml_init)(int dim, const int *nx, const int *gcl, const int *gcu, in
     FN(ora_grid) G, *g = &G;
     FN(grid_init)(g, dim, nx, gcl, gcu);
     FN(pml_desc) P = FN(pml_make)(g, mask, nb);
-    if (dim == 3) P.T = 4 * FN(pml3_make)(g, mask, nb).W;   /* the tables follow the walls */
+    if (dim == 3) P.T = FN(pml3_make)(g, mask, nb).T;   /* the tables follow the walls */
     for (long i = 0; i < P.T + 12L * dim * nb; i++) st[i] = K(0.0);
     const double s1 = -(0.8 * (4.0 + 1.0)) / 2.0, s2 = 1.0 / (nb - 3);
 #define ATT(x) exp(s1 * ((s2 * (x)) * (s2 * (x))) * ((s2 * (x)) * (s2 * (x))))
@@ -989,10 +1054,13 @@ void FN(ora_pml_phase)(int dim, const int *nx, const int *gcl, const int *gcu, i
         const FN(pml3_desc) Q = FN(pml3_make)(g, mask, nb);
         if (what == 0) {
             FN(pml3_wall_guards)(&Q, st);
-        } else {
-            FN(pml3_iface)(g, &Q, st, what == 1 ? b : e, what == 1 ? 1 : 0);
-            FN(pml3_update)(&Q, st, dx, dt, what == 1 ? 0 : 1);
+            return;
         }
+        /* the interfaces of every wall in setup order (x1, x2, x3), then the wall updates */
+        for (int a = 0; a < 3; a++)
+            if ((mask >> a) & 1) FN(pml3_iface)(g, &Q, st, what == 1 ? b : e, what == 1 ? 1 : 0, a);
+        for (int a = 0; a < 3; a++)
+            if ((mask >> a) & 1) FN(pml3_update)(&Q, st, dx, dt, what == 1 ? 0 : 1, a);
         return;
     }
     const FN(pml_desc) P = FN(pml_make)(g, mask, nb);

@@ -406,106 +406,160 @@ static PmlDesc pml_desc(const GridDesc &g, int mask, int nb)
     return P;
 }
 
-// 3D walls at both edges of one axis a (no edges or corners with other PML axes): six split
-// components per point, 2F + s for field component F, s = 0 the part driven by the derivative
-// along the lower of the two other axes (XY, YX, ZX), s = 1 the other (XZ, YZ, ZY)
-// (update_e_x{1,2,3}_3d, update_b_x{1,2,3}_3d, update_interface_x{1,2,3}_3d without their corner
-// branches).  The wall spans [1 - g1_t, n_t + g2_t] along both other axes t (g1 = max(gcl_t, 1),
-// g2 = max(gcu_t, 2)); wall (side, field) at (2 side + field) W, W = nte_t1 nte_t2 nb 6 (t1 < t2),
-// point (iw, i_t1, i_t2) component c at 6 (((i_t2 - 1 + g1_t2) nte_t1 + i_t1 - 1 + g1_t1) nb +
-// iw - lo(side)) + c; the tables of all three axes follow at 4 W.
+// 3D walls at both edges of the axes in a mask: six split components per point, 2F + s for
+// field component F, s = 0 the part driven by the derivative along the lower of the two other
+// axes (XY, YX, ZX), s = 1 the other (XZ, YZ, ZY) (update_e_x{1,2,3}_3d, update_b_x{1,2,3}_3d,
+// update_interface_x{1,2,3}_3d).  The walls of a lower axis than a PML axis D extend over D's
+// edge regions (corner priority x1 > x2 > x3), where their D splits are damped with D's tables.
+// The wall of axis a spans [1 - g1, n_t + g2] along each other axis t: g1 = max(gcl_t, c - 1),
+// g2 = max(gcu_t, c), c = nb when t has PML walls and a < t, else 2.  Per PML axis a in
+// increasing order, wall (side, field) at base_a + (2 side + field) W_a,
+// W_a = nte_a,t1 nte_a,t2 nb 6 (t1 < t2); point (iw, i_t1, i_t2) component c at
+// 6 (((i_t2 - 1 + g1_t2) nte_t1 + i_t1 - 1 + g1_t1) nb + iw - lo(side)) + c; the tables of all
+// three axes follow at T (the walls' total).
 struct Pml3Desc {
-    int a, t1, t2, nb, n[3], g1[3], g2[3], nte[3];
-    long W;
+    int mask, nb, n[3];
+    int g1[3][3], g2[3][3], nte[3][3];   // [wall axis][other axis]
+    long W[3], base[3], T;
 };
 
 static Pml3Desc pml3_desc(const GridDesc &g, int mask, int nb)
 {
     Pml3Desc P;
-    P.a = mask == 1 ? 0 : (mask == 2 ? 1 : 2);
-    P.t1 = P.a == 0 ? 1 : 0;
-    P.t2 = P.a == 2 ? 1 : 2;
+    P.mask = mask;
     P.nb = nb;
-    for (int d = 0; d < 3; d++) {
-        P.n[d] = g.nx[d];
-        P.g1[d] = g.gcl[d] > 1 ? g.gcl[d] : 1;
-        P.g2[d] = g.gcu[d] > 2 ? g.gcu[d] : 2;
-        P.nte[d] = g.nx[d] + P.g1[d] + P.g2[d];
+    long off = 0;
+    for (int d = 0; d < 3; d++) P.n[d] = g.nx[d];
+    for (int a = 0; a < 3; a++) {
+        long w = (long)nb * 6;
+        for (int t = 0; t < 3; t++) {
+            const int c = (((mask >> t) & 1) && a < t) ? nb : 2;
+            P.g1[a][t] = g.gcl[t] > c - 1 ? g.gcl[t] : c - 1;
+            P.g2[a][t] = g.gcu[t] > c ? g.gcu[t] : c;
+            P.nte[a][t] = g.nx[t] + P.g1[a][t] + P.g2[a][t];
+            if (t != a) w *= P.nte[a][t];
+        }
+        P.W[a] = w;
+        P.base[a] = off;
+        if ((mask >> a) & 1) off += 4 * w;
     }
-    P.W = (long)P.nte[P.t1] * P.nte[P.t2] * nb * 6;
+    P.T = off;
     return P;
 }
 
-__device__ __forceinline__ long pml3_at(const Pml3Desc &P, int side, int fld, int c, const int *i)
+__device__ __forceinline__ long pml3_at(const Pml3Desc &P, int a, int side, int fld, int c,
+                                        const int *i)
 {
-    const int lo = side == 0 ? 2 - P.nb : P.n[P.a] + 1;
-    return (2 * side + fld) * P.W +
-           6 * ((((long)i[P.t2] - 1 + P.g1[P.t2]) * P.nte[P.t1] + i[P.t1] - 1 + P.g1[P.t1]) *
-                    P.nb + i[P.a] - lo) + c;
+    const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+    const int lo = side == 0 ? 2 - P.nb : P.n[a] + 1;
+    return P.base[a] + (2 * side + fld) * P.W[a] +
+           6 * ((((long)i[t2] - 1 + P.g1[a][t2]) * P.nte[a][t1] + i[t1] - 1 + P.g1[a][t1]) * P.nb +
+                i[a] - lo) + c;
 }
 
-// interfaces: the box into the wall over [1, n + 1] of both other axes (first split the box's
-// component, second 0), the wall's sums into the box over [0, n + 2]; one thread per edge and
-// transverse point of the larger range
+// interfaces of the walls of axis a: the box into the wall over [1, n + 1] of both other axes
+// (first split the box's component, second 0), the wall's sums into the box over [0, n + 2];
+// one thread per edge and transverse point of the larger range
 template <typename T>
-__global__ void k_pml3_iface(GridDesc g, Pml3Desc P, T *__restrict__ st, T *__restrict__ f, int fld)
+__global__ void k_pml3_iface(GridDesc g, Pml3Desc P, T *__restrict__ st, T *__restrict__ f, int fld,
+                             int a)
 {
-    const int m1 = P.n[P.t1] + 3, m2 = P.n[P.t2] + 3;
+    const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+    const int m1 = P.n[t1] + 3, m2 = P.n[t2] + 3;
     const long n = 2L * m1 * m2;
     OSG_GRID_LOOP(m, n)
     {
         const int side = (int)(m / ((long)m1 * m2));
         const int r = (int)(m % ((long)m1 * m2));
-        const int lo = side == 0 ? 2 - P.nb : P.n[P.a] + 1, hi = lo + P.nb - 1;
+        const int lo = side == 0 ? 2 - P.nb : P.n[a] + 1, hi = lo + P.nb - 1;
         const int to_w = side == 0 ? hi : lo, to_b = side == 0 ? hi - 1 : lo + 1;
         int i[3];
-        i[P.t1] = r % m1;
-        i[P.t2] = r / m1;
-        if (i[P.t1] >= 1 && i[P.t1] <= P.n[P.t1] + 1 && i[P.t2] >= 1 && i[P.t2] <= P.n[P.t2] + 1) {
-            i[P.a] = to_w;
+        i[t1] = r % m1;
+        i[t2] = r / m1;
+        if (i[t1] >= 1 && i[t1] <= P.n[t1] + 1 && i[t2] >= 1 && i[t2] <= P.n[t2] + 1) {
+            i[a] = to_w;
             const long pw = pos(g, i[0], i[1], i[2]);
             for (int F = 0; F < 3; F++) {
-                st[pml3_at(P, side, fld, 2 * F, i)] = f[pw + F];
-                st[pml3_at(P, side, fld, 2 * F + 1, i)] = T(0);
+                st[pml3_at(P, a, side, fld, 2 * F, i)] = f[pw + F];
+                st[pml3_at(P, a, side, fld, 2 * F + 1, i)] = T(0);
             }
         }
-        i[P.a] = to_b;
+        i[a] = to_b;
         const long pb = pos(g, i[0], i[1], i[2]);
         for (int F = 0; F < 3; F++)
-            f[pb + F] = st[pml3_at(P, side, fld, 2 * F, i)] + st[pml3_at(P, side, fld, 2 * F + 1, i)];
+            f[pb + F] = st[pml3_at(P, a, side, fld, 2 * F, i)] +
+                        st[pml3_at(P, a, side, fld, 2 * F + 1, i)];
     }
 }
 
-// one E (fld 0) or B (fld 1) wall update: split (F, D) with G the third axis,
-// E_FD += sgn dt/dx_D (E: G at p and p - e_D), B_FD -= sgn dt/dx_D (G at p + e_D and p), sgn +1
-// when D follows F cyclically; damped with a's tables along D = a.  E reads only B and B only
-// E: one thread per edge and wall point
+// contacts of the walls of axis a with the walls of a higher PML axis d (update_interface_x1_3d
+// :3090-3180, update_interface_x2_3d :3370-3430): below, d's wall takes plane 0 of a's wall and
+// gives it plane 1; above, a's wall takes plane n_a + 1 and gives n_a + 2; over d's edge rows
+// and, along the remaining axis o, [1 - g1, n + g2] of a's wall for the x1 walls' x2 contacts,
+// else [1, n + 1].  One thread per side of a, wall of d, edge row, point along o and component
 template <typename T>
-__global__ void k_pml3_update(Pml3Desc P, T *__restrict__ st, T dx0, T dx1, T dx2, int fld)
+__global__ void k_pml3_contact(Pml3Desc P, T *__restrict__ st, int fld, int a, int d)
 {
-    const long npl = (long)P.nte[P.t1] * P.nte[P.t2] * P.nb;
+    const int o = 3 - a - d;
+    const int olo = (a == 0 && d == 1) ? 1 - P.g1[a][o] : 1;
+    const int ohi = (a == 0 && d == 1) ? P.n[o] + P.g2[a][o] : P.n[o] + 1;
+    const int no = ohi - olo + 1, nr = P.nb - 1;
+    const long n = 4L * nr * no * 6;
+    OSG_GRID_LOOP(m, n)
+    {
+        const int c = (int)(m % 6);
+        long r = m / 6;
+        int i[3];
+        i[o] = olo + (int)(r % no);
+        r /= no;
+        const int row = (int)(r % nr);
+        r /= nr;
+        const int adj = (int)(r % 2), side = (int)(r / 2);
+        i[d] = adj == 0 ? 2 - P.nb + row : P.n[d] + 2 + row;
+        if (side == 0) {
+            i[a] = 0;
+            st[pml3_at(P, d, adj, fld, c, i)] = st[pml3_at(P, a, 0, fld, c, i)];
+            i[a] = 1;
+            st[pml3_at(P, a, 0, fld, c, i)] = st[pml3_at(P, d, adj, fld, c, i)];
+        } else {
+            i[a] = P.n[a] + 1;
+            st[pml3_at(P, a, 1, fld, c, i)] = st[pml3_at(P, d, adj, fld, c, i)];
+            i[a] = P.n[a] + 2;
+            st[pml3_at(P, d, adj, fld, c, i)] = st[pml3_at(P, a, 1, fld, c, i)];
+        }
+    }
+}
+
+// one E (fld 0) or B (fld 1) update of the walls of axis a: split (F, D) with G the third axis,
+// E_FD += sgn dt/dx_D (E: G at p and p - e_D), B_FD -= sgn dt/dx_D (G at p + e_D and p), sgn +1
+// when D follows F cyclically; damped along D = a with a's tables, and in the edge regions of a
+// higher PML axis D with D's.  E reads only B and B only E: one thread per edge and wall point
+template <typename T>
+__global__ void k_pml3_update(Pml3Desc P, T *__restrict__ st, T dx0, T dx1, T dx2, int fld, int a)
+{
+    const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+    const long npl = (long)P.nte[a][t1] * P.nte[a][t2] * P.nb;
     const long n = 2 * npl;
     const T dtdx[3] = {dx0, dx1, dx2};
-    const long tab = 4 * P.W;
     OSG_GRID_LOOP(m, n)
     {
         const int side = (int)(m / npl);
         long r = m % npl;
-        const int lo = side == 0 ? 2 - P.nb : P.n[P.a] + 1, hi = lo + P.nb - 1;
+        const int lo = side == 0 ? 2 - P.nb : P.n[a] + 1, hi = lo + P.nb - 1;
         int i[3];
-        i[P.a] = lo + (int)(r % P.nb);
+        i[a] = lo + (int)(r % P.nb);
         r /= P.nb;
-        i[P.t1] = 1 - P.g1[P.t1] + (int)(r % P.nte[P.t1]);
-        i[P.t2] = 1 - P.g1[P.t2] + (int)(r / P.nte[P.t1]);
+        i[t1] = 1 - P.g1[a][t1] + (int)(r % P.nte[a][t1]);
+        i[t2] = 1 - P.g1[a][t2] + (int)(r / P.nte[a][t1]);
         const int r0 = fld == 0 ? lo + 1 : (side == 0 ? lo : lo + 1);
         const int r1 = fld == 0 ? (side == 0 ? hi - 1 : hi) : hi - 1;
-        if (i[P.a] < r0 || i[P.a] > r1) continue;
+        if (i[a] < r0 || i[a] > r1) continue;
         const int t0 = fld == 0 ? 2 : 1, te = fld == 0 ? 0 : -1;
-        if (i[P.t1] < t0 - P.g1[P.t1] || i[P.t1] > P.n[P.t1] + P.g2[P.t1] + te) continue;
-        if (i[P.t2] < t0 - P.g1[P.t2] || i[P.t2] > P.n[P.t2] + P.g2[P.t2] + te) continue;
+        if (i[t1] < t0 - P.g1[a][t1] || i[t1] > P.n[t1] + P.g2[a][t1] + te) continue;
+        if (i[t2] < t0 - P.g1[a][t2] || i[t2] > P.n[t2] + P.g2[a][t2] + te) continue;
         const int k = fld == 0 ? side : 2 + side;
         const int cofs = side == 0 ? (fld == 0 ? lo - 1 : lo - 2) : lo;
-        const int ci = i[P.a] - cofs;
+        const int ci = i[a] - cofs;
         const int src = 1 - fld;
 #pragma unroll
         for (int F = 0; F < 3; F++)
@@ -518,56 +572,70 @@ __global__ void k_pml3_update(Pml3Desc P, T *__restrict__ st, T dx0, T dx1, T dx
                 int qa[3] = {i[0], i[1], i[2]}, qb[3] = {i[0], i[1], i[2]};
                 if (fld == 0) qb[D] -= 1;
                 else qa[D] += 1;
-                T &v = st[pml3_at(P, side, fld, 2 * F + sp, i)];
-                const T a0 = st[pml3_at(P, side, src, 2 * G, qa)];
-                const T a1 = st[pml3_at(P, side, src, 2 * G + 1, qa)];
-                const T b0 = st[pml3_at(P, side, src, 2 * G, qb)];
-                const T b1 = st[pml3_at(P, side, src, 2 * G + 1, qb)];
-                if (D == P.a) {
-                    const T *cf = st + tab + (4 * P.a + k) * 3 * P.nb + ci - 1;
+                T &v = st[pml3_at(P, a, side, fld, 2 * F + sp, i)];
+                const T a0 = st[pml3_at(P, a, side, src, 2 * G, qa)];
+                const T a1 = st[pml3_at(P, a, side, src, 2 * G + 1, qa)];
+                const T b0 = st[pml3_at(P, a, side, src, 2 * G, qb)];
+                const T b1 = st[pml3_at(P, a, side, src, 2 * G + 1, qb)];
+                int dk = -1, dn = 0;
+                if (D == a) {
+                    dk = k;
+                    dn = ci;
+                } else if (((P.mask >> D) & 1) && a < D) {
+                    if (i[D] <= 0) {
+                        dk = fld == 0 ? 0 : 2;
+                        dn = i[D] + P.g1[a][D] + (fld == 0 ? 0 : 1);
+                    } else if (i[D] > P.n[D] + 1) {
+                        dk = fld == 0 ? 1 : 3;
+                        dn = i[D] - P.n[D] - 1;
+                    }
+                }
+                if (dk >= 0) {
+                    const T *cf = st + P.T + (4 * D + dk) * 3 * P.nb + dn - 1;
                     const T c1 = cf[0], c2 = cf[P.nb], c3 = cf[2 * P.nb];
                     const T ga = a0 + a1, gb = b0 + b1;
                     if (sgn > 0) v = c1 * v + c2 * ga - c3 * gb;
                     else v = c1 * v - c2 * ga + c3 * gb;
                 } else {
-                    const T d = a0 + a1 - b0 - b1;
-                    if (sgn > 0) v = v + dtdx[D] * d;
-                    else v = v - dtdx[D] * d;
+                    const T dd = a0 + a1 - b0 - b1;
+                    if (sgn > 0) v = v + dtdx[D] * dd;
+                    else v = v - dtdx[D] * dd;
                 }
             }
     }
 }
 
-// the walls' periodic update along one other axis t (pass 0: t1 over the wall's extent of t2;
-// pass 1: t2 over the full extent of t1, guards included)
+// the periodic update of the walls of axis a along the periodic other axis t, over the full
+// extent of the remaining axis o (guards included)
 template <typename T>
-__global__ void k_pml3_guard(Pml3Desc P, T *__restrict__ st, int pass)
+__global__ void k_pml3_guard(Pml3Desc P, T *__restrict__ st, int a, int t)
 {
-    const int t = pass == 0 ? P.t1 : P.t2, o = pass == 0 ? P.t2 : P.t1;
-    const int ng = P.g1[t] + P.g2[t];
-    const long n = 4L * P.nb * P.nte[o] * ng;
+    const int o = 3 - a - t;
+    const int ng = P.g1[a][t] + P.g2[a][t];
+    const long n = 4L * P.nb * P.nte[a][o] * ng;
     OSG_GRID_LOOP(m, n)
     {
         long r = m;
         const int gi = (int)(r % ng);
         r /= ng;
         int i[3], j[3];
-        i[o] = 1 - P.g1[o] + (int)(r % P.nte[o]);
-        r /= P.nte[o];
+        i[o] = 1 - P.g1[a][o] + (int)(r % P.nte[a][o]);
+        r /= P.nte[a][o];
         const int iw = (int)(r % P.nb), wall = (int)(r / P.nb);
         const int side = wall >> 1, fld = wall & 1;
-        i[P.a] = (side == 0 ? 2 - P.nb : P.n[P.a] + 1) + iw;
-        i[t] = gi < P.g1[t] ? 1 - P.g1[t] + gi : P.n[t] + 1 + (gi - P.g1[t]);
-        j[P.a] = i[P.a];
+        i[a] = (side == 0 ? 2 - P.nb : P.n[a] + 1) + iw;
+        i[t] = gi < P.g1[a][t] ? 1 - P.g1[a][t] + gi : P.n[t] + 1 + (gi - P.g1[a][t]);
+        j[a] = i[a];
         j[o] = i[o];
-        j[t] = gi < P.g1[t] ? i[t] + P.n[t] : i[t] - P.n[t];
-        for (int c = 0; c < 6; c++) st[pml3_at(P, side, fld, c, i)] = st[pml3_at(P, side, fld, c, j)];
+        j[t] = gi < P.g1[a][t] ? i[t] + P.n[t] : i[t] - P.n[t];
+        for (int c = 0; c < 6; c++)
+            st[pml3_at(P, a, side, fld, c, i)] = st[pml3_at(P, a, side, fld, c, j)];
     }
 }
 
 long pml_state_size(const GridDesc &g, int mask, int nb)
 {
-    if (g.dim == 3) return 4 * pml3_desc(g, mask, nb).W + 36L * nb;
+    if (g.dim == 3) return pml3_desc(g, mask, nb).T + 36L * nb;
     return pml_desc(g, mask, nb).T + 24L * nb;
 }
 
@@ -575,7 +643,7 @@ template <typename T>
 void pml_init_host(const GridDesc &g, int mask, int nb, const double *dx, double dt, T *st)
 {
     // the tables follow the walls (2D: per PML axis; 3D: the one axis)
-    const long tab = g.dim == 3 ? 4 * pml3_desc(g, mask, nb).W : pml_desc(g, mask, nb).T;
+    const long tab = g.dim == 3 ? pml3_desc(g, mask, nb).T : pml_desc(g, mask, nb).T;
     const long n = tab + 12L * g.dim * nb;
     for (long i = 0; i < n; i++) st[i] = T(0);
     // t(x) = exp(s1 (s2 x)^4) with s1 = -0.8 (4 + 1) / 2, s2 = 1 / (nb - 3); the fourth power
@@ -841,19 +909,41 @@ void pml_phase(const GridDesc &g, int mask, int nb, int what, T *e, T *b, T *pml
     if (g.dim == 3) {
         const Pml3Desc Q = pml3_desc(g, mask, nb);
         if (what == 0) {
-            for (int pass = 0; pass < 2; pass++) {
-                const int t = pass == 0 ? Q.t1 : Q.t2, o = pass == 0 ? Q.t2 : Q.t1;
-                const long n = 4L * nb * Q.nte[o] * (Q.g1[t] + Q.g2[t]);
-                k_pml3_guard<T><<<blocks_for(n, 256), 256, 0, st>>>(Q, pml, pass);
+            // the walls' periodic update along their periodic other axes, lower axis first
+            for (int a = 0; a < 3; a++) {
+                if (!((mask >> a) & 1)) continue;
+                for (int t = 0; t < 3; t++) {
+                    if (t == a || ((mask >> t) & 1)) continue;
+                    const long n = 4L * nb * Q.nte[a][3 - a - t] * (Q.g1[a][t] + Q.g2[a][t]);
+                    k_pml3_guard<T><<<blocks_for(n, 256), 256, 0, st>>>(Q, pml, a, t);
+                }
             }
             return;
         }
-        const long ni = 2L * (Q.n[Q.t1] + 3) * (Q.n[Q.t2] + 3);
-        k_pml3_iface<T><<<blocks_for(ni, 256), 256, 0, st>>>(g, Q, pml, what == 1 ? b : e,
-                                                             what == 1 ? 1 : 0);
-        const long nu = 2L * Q.nte[Q.t1] * Q.nte[Q.t2] * nb;
-        k_pml3_update<T><<<blocks_for(nu, 256), 256, 0, st>>>(
-            Q, pml, (T)(dt / dx[0]), (T)(dt / dx[1]), (T)(dt / dx[2]), what == 1 ? 0 : 1);
+        const int fld = what == 1 ? 1 : 0;
+        T *f = what == 1 ? b : e;
+        // the interfaces of every wall in setup order (x1, x2, x3), each with its contacts with
+        // the walls of the higher PML axes, then the wall updates
+        for (int a = 0; a < 3; a++) {
+            if (!((mask >> a) & 1)) continue;
+            const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+            const long ni = 2L * (Q.n[t1] + 3) * (Q.n[t2] + 3);
+            k_pml3_iface<T><<<blocks_for(ni, 256), 256, 0, st>>>(g, Q, pml, f, fld, a);
+            for (int d = a + 1; d < 3; d++) {
+                if (!((mask >> d) & 1)) continue;
+                const int o = 3 - a - d;
+                const int no = (a == 0 && d == 1) ? Q.n[o] + Q.g1[a][o] + Q.g2[a][o] : Q.n[o] + 1;
+                const long nc = 4L * (nb - 1) * no * 6;
+                k_pml3_contact<T><<<blocks_for(nc, 256), 256, 0, st>>>(Q, pml, fld, a, d);
+            }
+        }
+        for (int a = 0; a < 3; a++) {
+            if (!((mask >> a) & 1)) continue;
+            const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+            const long nu = 2L * Q.nte[a][t1] * Q.nte[a][t2] * nb;
+            k_pml3_update<T><<<blocks_for(nu, 256), 256, 0, st>>>(
+                Q, pml, (T)(dt / dx[0]), (T)(dt / dx[1]), (T)(dt / dx[2]), what == 1 ? 0 : 1, a);
+        }
         return;
     }
     const PmlDesc P = pml_desc(g, mask, nb);

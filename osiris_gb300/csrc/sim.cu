@@ -284,8 +284,9 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
         launches += 2 * (c.dim - 1) + 1;
     } else if (pml) {
         pml_guards<T>(s->g, (T *)s->e, (T *)s->b, pml, s->pml_nb, (T *)s->pml, st);
-        launches += 2 * (c.dim - __builtin_popcount(pml)) +
-                    (c.dim == 3 ? 2 : (pml == 3 ? 0 : 1));
+        // one wall guard launch per PML axis and periodic other axis
+        const int np_ = __builtin_popcount(pml);
+        launches += 2 * (c.dim - np_) + np_ * (c.dim - np_);
     } else {
         periodic_update<T>(s->g, (T *)s->e, 0, st, 0, walls | win);
         periodic_update<T>(s->g, (T *)s->b, 0, st, 0, walls | win);
@@ -374,7 +375,11 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
     yee_advance<T>(s->g, (T *)s->e, (T *)s->b, (const T *)s->j, c.dx, c.dt, st, walls, c.order,
                    oax, (T *)s->lind, c.pmc, pml, s->pml_nb, (T *)s->pml);
     launches += 3 + (walls ? 6 * __builtin_popcount(walls) : 0) + (oax >= 0 ? 3 : 0) +
-                (!pml ? 0 : c.dim == 3 ? 4 : 2 * (2 * __builtin_popcount(pml) + (pml == 3 ? 1 : 0)));
+                (!pml ? 0
+                      : 2 * (2 * __builtin_popcount(pml) +
+                             (c.dim == 2 ? (pml == 3) : ((pml & 1) && (pml & 2)) +
+                                                            ((pml & 1) && (pml & 4)) +
+                                                            ((pml & 2) && (pml & 4)))));
     if (shift) {
         shift_window_x<T>(s->g, (T *)s->e, (T *)s->shift_tmp, st);
         shift_window_x<T>(s->g, (T *)s->b, (T *)s->shift_tmp, st);
@@ -526,8 +531,7 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
               "pmc: a bit mask of walled axes");
     OSG_CHECK(cfg->pml >= 0 && cfg->pml < (1 << cfg->dim), OSG_ERR_ARG,
               "pml: a bit mask of the axes");
-    OSG_CHECK(cfg->pml == 0 || cfg->dim == 2 || (cfg->dim == 3 && (cfg->pml & (cfg->pml - 1)) == 0),
-              OSG_ERR_ARG, "PML walls: 2D boxes, or one axis of a 3D box");
+    OSG_CHECK(cfg->pml == 0 || cfg->dim >= 2, OSG_ERR_ARG, "PML walls: 2D and 3D boxes");
     OSG_CHECK(cfg->pml == 0 || (cfg->walls == 0 && cfg->open_fields == 0 &&
                                 cfg->smooth_type == OSG_SMOOTH_NONE &&
                                 cfg->emf_smooth_type == OSG_SMOOTH_NONE && cfg->thermal == 0),

@@ -12,8 +12,10 @@ absorbed.  Whole field arrays are compared, guard cells included (the interfaces
   the live particles against the oracle, either axis and both;
 * a vacuum pulse travelling along the PML axis leaves the box with less than 1e-4 of its
   energy, in both engines; with both axes, a cylindrical pulse leaves less than 1e-4;
-* 3D, one PML axis: plain FP64 1e-12 and tiled FP32 5e-5 against the oracle after 6 steps,
-  each axis; a plane pulse leaves less than 1e-4 of its energy;
+* 3D, any set of PML axes (the walls of a lower axis covering the edge regions of the higher
+  ones): plain FP64 1e-12 and tiled FP32 5e-5 against the oracle after 6 steps; a plane pulse
+  leaves less than 1e-4 of its energy, and with all three axes a divergence-free spherical
+  pulse less than 1e-4;
 * checkpoint / restore keeps the walls: 4 + 4 steps equal 8 steps to 1e-12;
 * configurations the walls are not built for are refused.
 """
@@ -218,28 +220,22 @@ def test_pml_refuses_what_it_is_not_built_for(osg, kw):
                        engine=osg.ENGINE_PLAIN, **kw)
 
 
-def test_pml_3d_one_axis_only(osg):
-    with pytest.raises(osg.OsirisGB300Error):
-        osg.Simulation([8, 8, 8], [0.1] * 3, 0.03, order=2, precision=64,
-                       engine=osg.ENGINE_PLAIN, pml=3)
-
-
-@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("mask", [1, 2, 4, 3, 5, 6, 7])
 @pytest.mark.parametrize("engine,prec,tol", [("plain", 64, 1e-12), ("tiled", 32, 5e-5)])
-def test_pml_3d_matches_oracle(osg, oracle, engine, prec, tol, axis):
+def test_pml_3d_matches_oracle(osg, oracle, engine, prec, tol, mask):
     nx = [12, 8, 8]
     p, g, dx, dt, species, e, b = _setup(oracle, prec, 3, 2, nx, [2, 2, 2], 21, uth=0.6,
                                          ufl=0.1)
     sim = osg.Simulation(nx, dx, dt, order=2, precision=prec,
                          engine=osg.ENGINE_PLAIN if engine == "plain" else osg.ENGINE_TILED,
-                         tile=[4, 4, 4] if engine == "tiled" else None, pml=1 << axis)
+                         tile=[4, 4, 4] if engine == "tiled" else None, pml=mask)
     sim.set_fields(e, b)
     for s_ in species:
         sim.add_species(s_["rqm"], s_["ix"], s_["x"], s_["u"], s_["q"])
     steps = 6
     sim.step(steps)
     eg, bg, jg = sim.fields()
-    eo, bo, jo, ora = _oracle_run(oracle, g, p, e, b, species, dt, 1 << axis, steps)
+    eo, bo, jo, ora = _oracle_run(oracle, g, p, e, b, species, dt, mask, steps)
     errs = {"E": _nerr(eg, eo), "B": _nerr(bg, bo), "J": _nerr(jg, jo)}
     for k, s_ in enumerate(ora):
         ix, x, u, q = sim.species(k)
@@ -257,6 +253,35 @@ def test_pml_3d_matches_oracle(osg, oracle, engine, prec, tol, axis):
     sim.close()
     bad = {k: v for k, v in errs.items() if not v <= tol}
     assert not bad, (bad, errs)
+
+
+@pytest.mark.parametrize("engine,prec", [("plain", 64), ("tiled", 32)])
+def test_3d_spherical_pulse_leaves_through_pml_on_all_axes(osg, engine, prec):
+    nx, dx = [24, 24, 16], [0.1] * 3
+    dt = 0.9 / np.sqrt(sum(1 / d ** 2 for d in dx))
+    sim = osg.Simulation(nx, dx, dt, order=2, precision=prec,
+                         engine=osg.ENGINE_PLAIN if engine == "plain" else osg.ENGINE_TILED,
+                         tile=[8, 8, 8] if engine == "tiled" else None, pml=7)
+    gl, gu = osg.GUARD[2]
+    dtype = np.float32 if prec == 32 else np.float64
+    shape = tuple(reversed([n + gl + gu for n in nx])) + (3,)
+    e, b = np.zeros(shape, dtype), np.zeros(shape, dtype)
+    z, y, x = np.meshgrid(np.arange(shape[0]), np.arange(shape[1]), np.arange(shape[2]),
+                          indexing="ij")
+    az = np.exp(-((x - shape[2] / 2) ** 2 + (y - shape[1] / 2) ** 2 + (z - shape[0] / 2) ** 2) / 6.0)
+    b[:, :-1, :, 0] = (az[:, 1:, :] - az[:, :-1, :]) / dx[1]
+    b[:, :, :-1, 1] = -(az[:, :, 1:] - az[:, :, :-1]) / dx[0]
+    sim.set_fields(e, b)
+    empty = np.zeros((0, 3), np.int32), np.zeros((0, 3), dtype), np.zeros((0, 3), dtype), \
+        np.zeros(0, dtype)
+    sim.add_species(-1.0, *empty)
+    sl = (slice(gl, gl + nx[2]), slice(gl, gl + nx[1]), slice(gl, gl + nx[0]))
+    w0 = float((b[sl].astype(np.float64) ** 2).sum())
+    sim.step(int(3 * max(nx) * dx[0] / dt))
+    e1, b1, _ = sim.fields()
+    w1 = float((e1[sl].astype(np.float64) ** 2).sum() + (b1[sl].astype(np.float64) ** 2).sum())
+    assert w1 / w0 < 1e-4
+    sim.close()
 
 
 @pytest.mark.parametrize("axis", [0, 2])
