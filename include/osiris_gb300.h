@@ -232,6 +232,23 @@ int osg_lindman_f32(int dim, const int *nx, const int *gcl, const int *gcu, int 
                     float *e, float *b, float *state, const double *dx, double dt);
 int osg_lindman_f64(int dim, const int *nx, const int *gcl, const int *gcu, int axis, int what,
                     double *e, double *b, double *state, const double *dx, double dt);
+/* PML walls (Vay's split-field perfectly matched layer, source/emf/boundary/os-emf-vpml.f03) of
+ * nb cells (>= 5) at both edges of the axes in `mask` (2D or 3D; gcl >= 1, gcu >= 2), on HOST
+ * arrays, one phase per call: what 0 in the guard update (the walls' periodic update along their
+ * periodic other axes, update_boundary_vpml :506-524), 1 after the first B half step (the B
+ * interfaces, which write the box's B next to each wall, then the E walls, update_e_vpml_{2,3}d),
+ * 2 after the E step (the E interfaces, which write the box's E, then the B walls,
+ * update_b_vpml_{2,3}d).  `state` holds osg_pml_state_size reals: the split-field walls and the
+ * attenuation tables, set up by osg_pml_init_* (walls zero, tables from dt and dx). */
+long osg_pml_state_size(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb);
+int osg_pml_init_f32(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
+                     const double *dx, double dt, float *state);
+int osg_pml_init_f64(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
+                     const double *dx, double dt, double *state);
+int osg_pml_f32(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb, int what,
+                float *e, float *b, float *state, const double *dx, double dt);
+int osg_pml_f64(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb, int what,
+                double *e, double *b, double *state, const double *dx, double dt);
 int osg_walls_f32(int dim, const int *nx, const int *gcl, const int *gcu, float *f, int kind,
                   int walls, int order);
 int osg_walls_f64(int dim, const int *nx, const int *gcl, const int *gcu, double *f, int kind,

@@ -109,6 +109,8 @@ def _declare(lb):
         getattr(lb, f"osg_periodic_{s}").argtypes = [I, P, P, P, P, I]
         getattr(lb, f"osg_walls_{s}").argtypes = [I, P, P, P, P, I, I, I]
         getattr(lb, f"osg_lindman_{s}").argtypes = [I, P, P, P, I, I, P, P, P, P, D]
+        getattr(lb, f"osg_pml_init_{s}").argtypes = [I, P, P, P, I, I, P, D, P]
+        getattr(lb, f"osg_pml_{s}").argtypes = [I, P, P, P, I, I, I, P, P, P, P, D]
     lb.osg_particle_wrap.argtypes = [I, P, L, P]
     lb.osg_rng_seed.argtypes = [P, I]
     lb.osg_load_lattice.argtypes = [P, I, I, P, P, P, D, P, P, D, D, P, P, P, P]
@@ -312,6 +314,40 @@ def lindman(dim, nx, gcl, gcu, axis, what, e, b, state, dx, dt):
     _check(getattr(lib(), f"osg_lindman_{s}")(dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)),
                                               int(axis), int(what), _p(e), _p(b), _p(state),
                                               _p(_f64(list(dx) + [0.0] * 3)), float(dt)))
+
+
+def pml_state(dim, nx, gcl, gcu, mask, nb, dx, dt, dtype):
+    """State of PML walls of nb cells at both edges of the axes in `mask` on a host grid
+    (osg_pml_init_*): zeroed split-field walls and the attenuation tables."""
+    lb = lib()
+    lb.osg_pml_state_size.argtypes = [I, P, P, P, I, I]
+    lb.osg_pml_state_size.restype = C.c_long
+    n = lb.osg_pml_state_size(dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)), int(mask), int(nb))
+    if n < 0:
+        raise OsirisGB300Error(-1, lb.osg_last_error().decode(errors="replace"))
+    st = np.zeros(n, dtype=dtype)
+    s = "f32" if st.dtype == np.float32 else "f64"
+    _check(getattr(lb, f"osg_pml_init_{s}")(dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)),
+                                            int(mask), int(nb), _p(_f64(list(dx) + [0.0] * 3)),
+                                            float(dt), _p(st)))
+    return st
+
+
+def pml(dim, nx, gcl, gcu, mask, nb, what, e, b, state, dx, dt):
+    """One phase of the PML walls on host arrays (osg_pml_*): what 0 the walls' guard update,
+    1 after the first B half step (B interfaces, E walls), 2 after the E step (E interfaces,
+    B walls); `state` from pml_state is kept by the caller."""
+    s = _prec(state)
+    dt_ = state.dtype
+    for a, n in ((e, "e"), (b, "b")):
+        _need(a, dt_, n)
+    npts = 3 * int(np.prod([int(nx[d]) + int(gcl[d]) + int(gcu[d]) for d in range(dim)]))
+    if e.size != npts or b.size != npts:
+        raise ValueError(f"e and b must hold {npts} reals (3 x the guard-celled grid)")
+    _need(state, dt_, "state")
+    _check(getattr(lib(), f"osg_pml_{s}")(dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)),
+                                          int(mask), int(nb), int(what), _p(e), _p(b), _p(state),
+                                          _p(_f64(list(dx) + [0.0] * 3)), float(dt)))
 
 
 def walls(dim, nx, gcl, gcu, f, kind, mask, order):

@@ -390,6 +390,60 @@ static int lindman_host(int dim, const int *nx, const int *gcl, const int *gcu, 
     return OSG_OK;
 }
 
+static int pml_check(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb)
+{
+    OSG_CHECK(dim >= 2 && dim <= 3 && nx && gcl && gcu && mask > 0 && mask < (1 << dim) &&
+                  nb >= 5,
+              OSG_ERR_ARG, "bad PML arguments (2D/3D, a non-empty axis mask, nb >= 5)");
+    for (int d = 0; d < dim; d++)
+        OSG_CHECK(nx[d] >= 6 && gcl[d] >= 1 && gcu[d] >= 2, OSG_ERR_ARG,
+                  "PML walls need nx >= 6, gcl >= 1 and gcu >= 2 on every axis");
+    return OSG_OK;
+}
+
+template <typename T>
+static int pml_init_h(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
+                      const double *dx, double dt, T *state)
+{
+    int rc = pml_check(dim, nx, gcl, gcu, mask, nb);
+    if (rc) return rc;
+    OSG_CHECK(dx && state && dt > 0, OSG_ERR_ARG, "bad PML arguments");
+    pml_init_host<T>(make_grid(dim, nx, gcl, gcu), mask, nb, dx, dt, state);
+    return OSG_OK;
+}
+
+template <typename T>
+static int pml_host(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
+                    int what, T *e, T *b, T *state, const double *dx, double dt)
+{
+    int rc = pml_check(dim, nx, gcl, gcu, mask, nb);
+    if (rc) return rc;
+    OSG_CHECK(state && what >= 0 && what <= 2 && (what == 0 || (e && b && dx)), OSG_ERR_ARG,
+              "bad PML arguments");
+    GridDesc g = make_grid(dim, nx, gcl, gcu);
+    const long n = g.npoints() * 3, ns = pml_state_size(g, mask, nb);
+    void *d_e = nullptr, *d_b = nullptr, *d_s;
+    if (what > 0) {
+        if ((rc = g_stage.get(4, sizeof(T) * n, &d_e))) return rc;
+        if ((rc = g_stage.get(5, sizeof(T) * n, &d_b))) return rc;
+    }
+    if ((rc = g_stage.get(6, sizeof(T) * ns, &d_s))) return rc;
+    cudaStream_t st = g_stage.stream;
+    if (what > 0) {
+        OSG_CUDA(cudaMemcpyAsync(d_e, e, sizeof(T) * n, cudaMemcpyHostToDevice, st));
+        OSG_CUDA(cudaMemcpyAsync(d_b, b, sizeof(T) * n, cudaMemcpyHostToDevice, st));
+    }
+    OSG_CUDA(cudaMemcpyAsync(d_s, state, sizeof(T) * ns, cudaMemcpyHostToDevice, st));
+    pml_phase<T>(g, mask, nb, what, (T *)d_e, (T *)d_b, (T *)d_s, dx, dt, st);
+    OSG_CUDA(cudaGetLastError());
+    // what 1 writes the box's B next to the walls, what 2 its E
+    if (what == 1) OSG_CUDA(cudaMemcpyAsync(b, d_b, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+    if (what == 2) OSG_CUDA(cudaMemcpyAsync(e, d_e, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+    OSG_CUDA(cudaMemcpyAsync(state, d_s, sizeof(T) * ns, cudaMemcpyDeviceToHost, st));
+    OSG_CUDA(cudaStreamSynchronize(st));
+    return OSG_OK;
+}
+
 template <typename T>
 static int walls_host(int dim, const int *nx, const int *gcl, const int *gcu, T *f, int kind,
                       int walls, int order)
@@ -769,6 +823,36 @@ int osg_smooth_coefficients(int type, int order, double *c, int *n)
     OSG_CHECK(smooth_coefficients(type, order, c, n) == OSG_OK, OSG_ERR_ARG,
               "bad smoothing type %d / order %d", type, order);
     return OSG_OK;
+}
+
+long osg_pml_state_size(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb)
+{
+    if (pml_check(dim, nx, gcl, gcu, mask, nb)) return -1;
+    return pml_state_size(make_grid(dim, nx, gcl, gcu), mask, nb);
+}
+
+int osg_pml_init_f32(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
+                     const double *dx, double dt, float *state)
+{
+    return pml_init_h<float>(dim, nx, gcl, gcu, mask, nb, dx, dt, state);
+}
+
+int osg_pml_init_f64(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
+                     const double *dx, double dt, double *state)
+{
+    return pml_init_h<double>(dim, nx, gcl, gcu, mask, nb, dx, dt, state);
+}
+
+int osg_pml_f32(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb, int what,
+                float *e, float *b, float *state, const double *dx, double dt)
+{
+    return pml_host<float>(dim, nx, gcl, gcu, mask, nb, what, e, b, state, dx, dt);
+}
+
+int osg_pml_f64(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb, int what,
+                double *e, double *b, double *state, const double *dx, double dt)
+{
+    return pml_host<double>(dim, nx, gcl, gcu, mask, nb, what, e, b, state, dx, dt);
 }
 
 int osg_lindman_f32(int dim, const int *nx, const int *gcl, const int *gcu, int axis, int what,

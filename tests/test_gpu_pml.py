@@ -311,3 +311,32 @@ def test_3d_plane_pulse_leaves_through_the_pml(osg, axis):
     e1, b1, _ = sim.fields()
     assert float((e1[sl] ** 2).sum() + (b1[sl] ** 2).sum()) / w0 < 1e-4
     sim.close()
+
+
+@pytest.mark.parametrize("dim,mask", [(2, 1), (2, 2), (2, 3), (3, 1), (3, 4), (3, 5), (3, 7)])
+@pytest.mark.parametrize("what", [0, 1, 2])
+@pytest.mark.parametrize("prec,tol", [(64, 1e-12), (32, 1e-6)])
+def test_host_array_pml_phase_matches_oracle(osg, oracle, dim, mask, what, prec, tol):
+    """One phase of osg_pml_* on host arrays against the oracle's phase, from random fields and
+    random walls (the tables from the initialisation kept)."""
+    nx = [10, 8] if dim == 2 else [8, 6, 7]
+    g = oracle.Grid(nx, 2, [0.1, 0.12, 0.09][:dim])
+    p = "f32" if prec == 32 else "f64"
+    dt = 0.03
+    rng = np.random.default_rng(7 + what + 3 * mask)
+    st0 = oracle.pml_state(g, p, mask, NB, dt)
+    nx_, gl, gu = g.args()
+    st1 = osg.pml_state(dim, nx, gl, gu, mask, NB, g.dx, dt, st0.dtype)
+    assert st1.shape == st0.shape
+    assert _nerr(st1, st0) <= tol          # the same tables (computed in double)
+    nwall = len(st0) - 12 * dim * NB
+    st0[:nwall] = rng.standard_normal(nwall).astype(st0.dtype)
+    st1[...] = st0
+    e = rng.standard_normal(g.shape).astype(st0.dtype)
+    b = rng.standard_normal(g.shape).astype(st0.dtype)
+    eo, bo = e.copy(), b.copy()
+    oracle.pml_phase(g, p, mask, NB, what, eo, bo, st0, dt)
+    osg.pml(dim, nx, gl, gu, mask, NB, what, e, b, st1, g.dx, dt)
+    errs = {"E": _nerr(e, eo), "B": _nerr(b, bo), "state": _nerr(st1, st0)}
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, (bad, errs)
