@@ -361,8 +361,9 @@ typedef struct {
                          (Vay's split-field PML, the reference's "vpml" field boundary) of
                          pml_cells cells each (the walls of a lower axis cover the edge regions
                          of the higher PML axes), and particles leaving through them are
-                         absorbed; not with walls, Lindman boundaries, smoothing, a thermal
-                         bath or the moving window */
+                         absorbed; not with walls, Lindman boundaries, smoothing or a
+                         thermal bath; with the moving window (along x1) on the other axes,
+                         whose walls then move with the fields */
     int pml_cells;    /* PML thickness in cells (0 = the reference default 8; at least 5) */
 } osg_config;
 

@@ -528,7 +528,11 @@ static FN(pml_desc) FN(pml_make)(const FN(ora_grid) *g, int mask, int nb)
         const int t = 1 - a;
         P.nx[a] = g->nx[a];
         const int c = (a == 0 && ((mask >> 1) & 1)) ? nb : 2;
-        P.g1[a] = g->gcl[t] > c - 1 ? g->gcl[t] : c - 1;
+        /* along x1 the lower corner count is one more (the reference's rule for a moving
+           x1, setup_vpml :371-376, kept whether or not the window moves: the extra guard row
+           never reaches the box) */
+        const int cl = t == 0 ? c + 1 : c;
+        P.g1[a] = g->gcl[t] > cl - 1 ? g->gcl[t] : cl - 1;
         P.g2[a] = g->gcu[t] > c ? g->gcu[t] : c;
         P.nte[a] = g->nx[t] + P.g1[a] + P.g2[a];
         P.W[a] = (long)P.nte[a] * nb * 4;
@@ -573,7 +577,8 @@ static FN(pml3_desc) FN(pml3_make)(const FN(ora_grid) *g, int mask, int nb)
         long w = (long)nb * 6;
         for (int t = 0; t < 3; t++) {
             const int c = (((mask >> t) & 1) && a < t) ? nb : 2;
-            P.g1[a][t] = g->gcl[t] > c - 1 ? g->gcl[t] : c - 1;
+            const int cl = t == 0 ? c + 1 : c;   /* as in 2D: one more below along x1 */
+            P.g1[a][t] = g->gcl[t] > cl - 1 ? g->gcl[t] : cl - 1;
             P.g2[a][t] = g->gcu[t] > c ? g->gcu[t] : c;
             P.nte[a][t] = g->nx[t] + P.g1[a][t] + P.g2[a][t];
             if (t != a) w *= P.nte[a][t];
@@ -733,7 +738,7 @@ static void FN(pml3_wall_guards)(const FN(pml3_desc) *Pp, R *st)
             const int lo = side == 0 ? 2 - P.nb : P.n[a] + 1;
             for (int pass = 0; pass < 2; pass++) {
                 const int t = pass == 0 ? t1 : t2, o = pass == 0 ? t2 : t1;
-                if ((P.mask >> t) & 1) continue;
+                if (((P.mask >> t) & 1) || (t == 0 && ((P.mask >> 3) & 1))) continue;
                 for (int fld = 0; fld < 2; fld++) {
                     int i[3], j[3];
                     for (i[a] = lo; i[a] < lo + P.nb; i[a]++)
@@ -1024,7 +1029,8 @@ static void FN(pml_wall_guards)(const FN(pml_desc) *Pp, R *st)
     const FN(pml_desc) P = *Pp;
     for (int a = 0; a < 2; a++) {
         const int t = 1 - a, nt = P.nx[t];
-        if (!((P.mask >> a) & 1) || ((P.mask >> t) & 1)) continue;
+        if (!((P.mask >> a) & 1) || ((P.mask >> t) & 1) || (t == 0 && ((P.mask >> 3) & 1)))
+            continue;
         for (int side = 0; side < 2; side++) {
             const int lo = FN(pml_lo)(&P, a, side);
             for (int fld = 0; fld < 2; fld++)
@@ -1079,6 +1085,43 @@ void FN(ora_pml_phase)(int dim, const int *nx, const int *gcl, const int *gcu, i
 #undef PWX
 #undef PCOEF
 
+/* window move: the walls of the axes other than x1 shift one cell down along x1, all
+ * components, the last x1 plane becoming zero (move_window_vpml :478-494, move_window_wall,
+ * source/vdf/os-wall-comm.f90:57-176) */
+void FN(ora_pml_shift_x)(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
+                         R *st)
+{
+    FN(ora_grid) G, *g = &G;
+    FN(grid_init)(g, dim, nx, gcl, gcu);
+    if (dim == 2) {
+        const FN(pml_desc) P = FN(pml_make)(g, mask, nb);
+        if (!((mask >> 1) & 1)) return;
+        /* x2 walls: point (iw, it) with it along x1, stride 4 nb */
+        for (int w = 0; w < 4; w++) {
+            R *f = st + P.base[1] + w * P.W[1];
+            const long line = 4L * nb, nl = P.nte[1];
+            for (long k = 0; k + 1 < nl; k++)
+                for (long c = 0; c < line; c++) f[k * line + c] = f[(k + 1) * line + c];
+            for (long c = 0; c < line; c++) f[(nl - 1) * line + c] = K(0.0);
+        }
+        return;
+    }
+    const FN(pml3_desc) P = FN(pml3_make)(g, mask, nb);
+    for (int a = 1; a < 3; a++) {
+        if (!((mask >> a) & 1)) continue;
+        /* x1 is the walls' first other axis (t1): stride 6 nb, lines of nte_a,x1 points */
+        const int t2 = a == 2 ? 1 : 2;
+        const long line = 6L * nb, nl = P.nte[a][0];
+        for (int w = 0; w < 4; w++)
+            for (long o = 0; o < P.nte[a][t2]; o++) {
+                R *f = st + P.base[a] + w * P.W[a] + o * nl * line;
+                for (long k = 0; k + 1 < nl; k++)
+                    for (long c = 0; c < line; c++) f[k * line + c] = f[(k + 1) * line + c];
+                for (long c = 0; c < line; c++) f[(nl - 1) * line + c] = K(0.0);
+            }
+    }
+}
+
 /* the Yee advance with PML walls on the axes in mask */
 void FN(ora_yee_advance_pml)(int dim, const int *nx, const int *gcl, const int *gcu, R *e, R *b,
                              const R *j, const double *dx, double dt, int mask, int nb, R *st)
@@ -1099,9 +1142,10 @@ void FN(ora_yee_advance_pml)(int dim, const int *nx, const int *gcl, const int *
 void FN(ora_pml_guards)(int dim, const int *nx, const int *gcl, const int *gcu, R *e, R *b,
                         int mask, int nb, R *st)
 {
+    const int skip = (mask & 7) | ((mask >> 3) & 1);   /* PML axes, and x1 when it moves */
     FN(ora_pml_phase)(dim, nx, gcl, gcu, mask, nb, 0, e, b, st, 0, 0.0);
-    FN(ora_periodic_skip)(dim, nx, gcl, gcu, e, 0, mask);
-    FN(ora_periodic_skip)(dim, nx, gcl, gcu, b, 0, mask);
+    FN(ora_periodic_skip)(dim, nx, gcl, gcu, e, 0, skip);
+    FN(ora_periodic_skip)(dim, nx, gcl, gcu, b, 0, skip);
 }
 
 /* absorbing particle boundary along axis d (p_bc_absorbing: a particle that left the box is

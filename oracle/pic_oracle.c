@@ -642,7 +642,7 @@ void ora_div_f64(int dim, const int *nx, const int *gcl, const int *gcu, const d
     const int oax = step_open_##SFXN; /* Lindman axis, -1: none */                            \
     const int win = step_window_##SFXN; /* moving window along x1 */                          \
     const int pml = step_pml_##SFXN; /* PML axes (bit mask), 0: none */                      \
-    const int skip = walls | (oax >= 0 ? 1 << oax : 0) | pml | win;                           \
+    const int skip = walls | (oax >= 0 ? 1 << oax : 0) | (pml & 7) | win;                     \
     if (oax >= 0) {                                                                           \
         ora_open_guards_##SFXN(dim, nx, gcl, gcu, e, b, oax, step_lind_##SFXN);               \
     } else if (pml) {                                                                         \

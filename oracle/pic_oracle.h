@@ -102,6 +102,10 @@ void ora_pml_phase_f32(int dim, const int *nx, const int *gcl, const int *gcu, i
                        int what, float *e, float *b, float *st, const double *dx, double dt);
 void ora_pml_phase_f64(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
                        int what, double *e, double *b, double *st, const double *dx, double dt);
+void ora_pml_shift_x_f32(int dim, const int *nx, const int *gcl, const int *gcu, int mask,
+                         int nb, float *st);
+void ora_pml_shift_x_f64(int dim, const int *nx, const int *gcl, const int *gcu, int mask,
+                         int nb, double *st);
 void ora_set_pml_f32(int mask, int nb, float *state);
 void ora_set_pml_f64(int mask, int nb, double *state);
 void ora_field_energy_f32(int dim, const int *nx, const int *gcl, const int *gcu,

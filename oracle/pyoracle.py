@@ -98,6 +98,7 @@ def _declare(L):
         getattr(L, f"ora_pml_init_{s_}").argtypes = [I, P, P, P, I, I, P, D, P]
         getattr(L, f"ora_pml_phase_{s_}").argtypes = [I, P, P, P, I, I, I, P, P, P, P, D]
         getattr(L, f"ora_set_pml_{s_}").argtypes = [I, I, P]
+        getattr(L, f"ora_pml_shift_x_{s_}").argtypes = [I, P, P, P, I, I, P]
     L.ora_set_thermal.argtypes = [I, P, P, C.c_uint32, C.c_uint64, I]
     L.ora_push_cyl_f32.argtypes = [I, P, P, P, P, I, I, C.c_float, I, P, P, P, P, P, P, P, P, D,
                                    P]
@@ -406,8 +407,8 @@ def step(g: Grid, prec, e, b, j, species, dt, nthreads=1, fast=False, pusher="bo
     axis d bounded by conducting walls instead of periodic.  open_fields = (axis, state from
     lindman_state): Lindman open boundaries at both edges of that axis, particles absorbed
     there (left in the arrays with charge and momentum 0).  pml = (mask, nb, state from
-    pml_state): PML walls of nb cells at both edges of the axes in mask (2D), particles
-    absorbed there the same way.  thermal = dict(mask, uth, ufl, seed,
+    pml_state): PML walls of nb cells at both edges of the axes in mask (bit 3: x1 is a moving
+    window's axis), particles absorbed there the same way.  thermal = dict(mask, uth, ufl, seed,
     step, type: 0 thermal, 1 random dir, 2 waterbag): particles crossing the edges of the axes in mask (walled or open) are re-emitted from
     a thermal bath; step keys the random stream.  pmc (bit d, d walled): perfect magnetic
     instead of electric conductor walls.  window=True: x1 is the axis of a moving window (no
@@ -510,9 +511,10 @@ class Window:
                 return pf[i - 1] + w * (pf[i] - pf[i - 1])
         return pf[-1]
 
-    def start_step(self, e, b, species, dt):
+    def start_step(self, e, b, species, dt, pml=None):
         """Advance the window motion; on a move shift the fields and particles and inject.
-        Returns True when the window moved."""
+        pml = (mask, nb, state): PML walls of other axes shift with the fields.  Returns True
+        when the window moved."""
         self.xmoved += dt
         if self.xmoved < self.g.dx[0]:
             return False
@@ -521,6 +523,11 @@ class Window:
         for f in (e, b):
             f[..., :-1, :] = f[..., 1:, :].copy()
             f[..., -1, :] = 0
+        if pml is not None:
+            nx, gl, gu = self.g.args()
+            getattr(lib(), f"ora_pml_shift_x_{self.prec}")(self.g.dim, _p(nx), _p(gl), _p(gu),
+                                                            int(pml[0]), int(pml[1]),
+                                                            _p(pml[2]))
         for sp in species:
             sp["ix"][:, 0] -= 1
         self._inject(species[self.k])

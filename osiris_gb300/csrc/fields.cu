@@ -395,7 +395,11 @@ static PmlDesc pml_desc(const GridDesc &g, int mask, int nb)
         const int t = 1 - a;
         P.nx[a] = g.nx[a];
         const int c = (a == 0 && ((mask >> 1) & 1)) ? nb : 2;
-        P.g1[a] = g.gcl[t] > c - 1 ? g.gcl[t] : c - 1;
+        // along x1 the lower corner count is one more (the reference's rule for a moving x1,
+        // setup_vpml :371-376, kept whether or not the window moves: the extra guard row never
+        // reaches the box), so the state's layout does not depend on the window
+        const int cl = t == 0 ? c + 1 : c;
+        P.g1[a] = g.gcl[t] > cl - 1 ? g.gcl[t] : cl - 1;
         P.g2[a] = g.gcu[t] > c ? g.gcu[t] : c;
         P.nte[a] = g.nx[t] + P.g1[a] + P.g2[a];
         P.W[a] = (long)P.nte[a] * nb * 4;
@@ -434,7 +438,8 @@ static Pml3Desc pml3_desc(const GridDesc &g, int mask, int nb)
         long w = (long)nb * 6;
         for (int t = 0; t < 3; t++) {
             const int c = (((mask >> t) & 1) && a < t) ? nb : 2;
-            P.g1[a][t] = g.gcl[t] > c - 1 ? g.gcl[t] : c - 1;
+            const int cl = t == 0 ? c + 1 : c;   // as in 2D: one more below along x1
+            P.g1[a][t] = g.gcl[t] > cl - 1 ? g.gcl[t] : cl - 1;
             P.g2[a][t] = g.gcu[t] > c ? g.gcu[t] : c;
             P.nte[a][t] = g.nx[t] + P.g1[a][t] + P.g2[a][t];
             if (t != a) w *= P.nte[a][t];
@@ -913,7 +918,7 @@ void pml_phase(const GridDesc &g, int mask, int nb, int what, T *e, T *b, T *pml
             for (int a = 0; a < 3; a++) {
                 if (!((mask >> a) & 1)) continue;
                 for (int t = 0; t < 3; t++) {
-                    if (t == a || ((mask >> t) & 1)) continue;
+                    if (t == a || ((mask >> t) & 1) || (t == 0 && ((mask >> 3) & 1))) continue;
                     const long n = 4L * nb * Q.nte[a][3 - a - t] * (Q.g1[a][t] + Q.g2[a][t]);
                     k_pml3_guard<T><<<blocks_for(n, 256), 256, 0, st>>>(Q, pml, a, t);
                 }
@@ -949,7 +954,9 @@ void pml_phase(const GridDesc &g, int mask, int nb, int what, T *e, T *b, T *pml
     const PmlDesc P = pml_desc(g, mask, nb);
     if (what == 0) {
         for (int a = 0; a < 2; a++) {
-            if (!((mask >> a) & 1) || ((mask >> (1 - a)) & 1)) continue;
+            const int t = 1 - a;
+            if (!((mask >> a) & 1) || ((mask >> t) & 1) || (t == 0 && ((mask >> 3) & 1)))
+                continue;
             const long n = 4L * nb * (P.g1[a] + P.g2[a]) * 4;
             k_pml_guard<T><<<blocks_for(n, 256), 256, 0, st>>>(P, pml, a);
         }
@@ -978,9 +985,69 @@ void pml_phase(const GridDesc &g, int mask, int nb, int what, T *e, T *b, T *pml
 template <typename T>
 void pml_guards(const GridDesc &g, T *e, T *b, int mask, int nb, T *pml, cudaStream_t st)
 {
+    const int skip = (mask & 7) | ((mask >> 3) & 1);   // PML axes, and x1 when it moves
     pml_phase<T>(g, mask, nb, 0, e, b, pml, nullptr, 0.0, st);
-    periodic_update<T>(g, e, 0, st, 0, mask);
-    periodic_update<T>(g, b, 0, st, 0, mask);
+    periodic_update<T>(g, e, 0, st, 0, skip);
+    periodic_update<T>(g, b, 0, st, 0, skip);
+}
+
+// window move: the walls of the axes other than x1 shift one cell down along x1, all
+// components, the last x1 plane becoming zero (move_window_vpml :478-494, move_window_wall,
+// source/vdf/os-wall-comm.f90:57-176).  x1 is their first other axis, so a wall is lines of
+// `line` reals (one x1 point) repeated nl times along x1, for each point of the remaining
+// axes; out of place through tmp (at least as long as the largest wall)
+template <typename T>
+__global__ void k_pml_shift_x(const T *__restrict__ in, T *__restrict__ out, long line, long nl,
+                              long n)
+{
+    OSG_GRID_LOOP(p, n)
+    {
+        const long k = (p / line) % nl;
+        out[p] = k + 1 < nl ? in[p + line] : T(0);
+    }
+}
+
+long pml_shift_scratch(const GridDesc &g, int mask, int nb)
+{
+    long w = 0;
+    if (g.dim == 2) {
+        const PmlDesc P = pml_desc(g, mask, nb);
+        if ((mask >> 1) & 1) w = P.W[1];
+    } else {
+        const Pml3Desc P = pml3_desc(g, mask, nb);
+        for (int a = 1; a < 3; a++)
+            if (((mask >> a) & 1) && P.W[a] > w) w = P.W[a];
+    }
+    return w;
+}
+
+template <typename T>
+void pml_shift_x(const GridDesc &g, int mask, int nb, T *pml, T *tmp, cudaStream_t st)
+{
+    for (int a = 1; a < g.dim; a++) {
+        if (!((mask >> a) & 1)) continue;
+        long base, W, line, nl;
+        if (g.dim == 2) {
+            const PmlDesc P = pml_desc(g, mask, nb);
+            base = P.base[1];
+            W = P.W[1];
+            line = 4L * nb;
+            nl = P.nte[1];
+        } else {
+            const Pml3Desc P = pml3_desc(g, mask, nb);
+            base = P.base[a];
+            W = P.W[a];
+            line = 6L * nb;
+            nl = P.nte[a][0];
+        }
+        for (int w = 0; w < 4; w++) {
+            T *f = pml + base + w * W;
+            unsigned blocks = blocks_for(W, 256);
+            if (blocks > 152 * 32) blocks = 152 * 32;
+            k_pml_shift_x<T><<<blocks, 256, 0, st>>>(f, tmp, line, nl, W);
+            cudaMemcpyAsync(f, tmp, sizeof(T) * W, cudaMemcpyDeviceToDevice, st);
+        }
+    }
 }
 
 template <typename T>
@@ -1487,6 +1554,8 @@ template void pml_phase<double>(const GridDesc &, int, int, int, double *, doubl
                                 const double *, double, cudaStream_t);
 template void pml_guards<float>(const GridDesc &, float *, float *, int, int, float *,
                                 cudaStream_t);
+template void pml_shift_x<float>(const GridDesc &, int, int, float *, float *, cudaStream_t);
+template void pml_shift_x<double>(const GridDesc &, int, int, double *, double *, cudaStream_t);
 template void pml_guards<double>(const GridDesc &, double *, double *, int, int, double *,
                                  cudaStream_t);
 template void lindman_phase<float>(const GridDesc &, int, int, float *, float *, float *,

@@ -75,6 +75,13 @@ void pml_phase(const GridDesc &g, int mask, int nb, int what, T *e, T *b, T *pml
 // and B periodic along the other axes only
 template <typename T>
 void pml_guards(const GridDesc &g, T *e, T *b, int mask, int nb, T *pml, cudaStream_t st);
+// (bit 3 of `mask` in pml_phase / pml_guards: x1 is the axis of a moving window, so neither the
+// walls nor the box take a periodic update along it)
+// window move: the PML walls of the axes other than x1 shift one cell down along x1, the last
+// plane zero; tmp holds pml_shift_scratch reals
+long pml_shift_scratch(const GridDesc &g, int mask, int nb);
+template <typename T>
+void pml_shift_x(const GridDesc &g, int mask, int nb, T *pml, T *tmp, cudaStream_t st);
 // Lindman open boundaries at both edges of one axis (p_bc_lindman,
 // source/emf/boundary/os-emf-lindman.f90).  Their state: 5 buffer planes along the axis
 // (E at 0 and 1, B at 0, E at nx+1 and nx+2), 3 components, per interior point of the other

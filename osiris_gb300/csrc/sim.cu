@@ -68,6 +68,7 @@ struct osg_sim {
     int pml_mask = 0;            // PML walls at both edges of these axes (2D)
     int pml_nb = 0;              // their thickness in cells
     void *pml = nullptr;         // their state (pml_state_size reals)
+    void *pml_tmp = nullptr;     // scratch of the walls' shift with the moving window
     osg::SmoothSpec smooth;      // current smoothing (order 0 per axis: none)
     osg::SmoothSpec esmooth;     // smoothing of the fields the particles see (order 0: none)
     void *e_part = nullptr, *b_part = nullptr;   // those fields, when smoothed
@@ -283,7 +284,9 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
         open_guards<T>(s->g, (T *)s->e, (T *)s->b, oax, (const T *)s->lind, st);
         launches += 2 * (c.dim - 1) + 1;
     } else if (pml) {
-        pml_guards<T>(s->g, (T *)s->e, (T *)s->b, pml, s->pml_nb, (T *)s->pml, st);
+        // (bit 3: x1 is the moving window's axis, updated by neither the walls nor the box)
+        pml_guards<T>(s->g, (T *)s->e, (T *)s->b, pml | (win ? 8 : 0), s->pml_nb, (T *)s->pml,
+                      st);
         // one wall guard launch per PML axis and periodic other axis
         const int np_ = __builtin_popcount(pml);
         launches += 2 * (c.dim - np_) + np_ * (c.dim - np_);
@@ -384,6 +387,11 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
         shift_window_x<T>(s->g, (T *)s->e, (T *)s->shift_tmp, st);
         shift_window_x<T>(s->g, (T *)s->b, (T *)s->shift_tmp, st);
         launches += 2;
+        if (s->pml) {
+            // the PML walls of the other axes move with the fields (move_window_vpml)
+            pml_shift_x<T>(s->g, pml, s->pml_nb, (T *)s->pml, (T *)s->pml_tmp, st);
+            launches += 4 * __builtin_popcount(pml & 6);
+        }
         int rc = tiled_window_inject(s->tiled, parity, s->d_status, st, &launches);
         if (rc) return rc;
     }
@@ -706,6 +714,7 @@ int osg_sim_destroy(osg_sim *s)
     cudaFree(s->b_part);
     cudaFree(s->lind);
     cudaFree(s->pml);
+    cudaFree(s->pml_tmp);
     cudaFree(s->d_step);
     cudaFree(s->d_ene);
     cudaFree(s->d_status);
@@ -901,13 +910,17 @@ int osg_sim_set_window(osg_sim *s, int species, const int *ppc, int nprof, const
     OSG_CHECK(s->cfg.engine == OSG_ENGINE_TILED, OSG_ERR_ARG,
               "the moving window runs on the tiled engine");
     OSG_CHECK(s->step_n == 0, OSG_ERR_STATE, "set the window before the first step");
-    OSG_CHECK(s->open_axis < 0 && s->pml_mask == 0, OSG_ERR_ARG,
-              "the moving window does not combine with Lindman or PML boundaries");
+    OSG_CHECK(s->open_axis < 0 && (s->pml_mask & 1) == 0, OSG_ERR_ARG,
+              "the moving window does not combine with Lindman boundaries or PML walls along x1");
     int rc = tiled_set_window(s->tiled, species, ppc, nprof, prof_x, prof_f);
     if (rc) return rc;
     if (!s->shift_tmp) {
         const size_t bytes = (size_t)s->esz * 3 * s->g.npoints();
         OSG_CUDA(cudaMalloc(&s->shift_tmp, bytes));
+    }
+    if (s->pml && !s->pml_tmp) {
+        const size_t bytes = (size_t)s->esz * pml_shift_scratch(s->g, s->pml_mask, s->pml_nb);
+        if (bytes) OSG_CUDA(cudaMalloc(&s->pml_tmp, bytes));
     }
     s->window = true;
     // the reference adds dt to the window motion at the start of step 1 (no move: dt < dx)

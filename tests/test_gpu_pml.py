@@ -340,3 +340,67 @@ def test_host_array_pml_phase_matches_oracle(osg, oracle, dim, mask, what, prec,
     errs = {"E": _nerr(e, eo), "B": _nerr(b, bo), "state": _nerr(st1, st0)}
     bad = {k: v for k, v in errs.items() if not v <= tol}
     assert not bad, (bad, errs)
+
+
+@pytest.mark.parametrize("dim,mask,steps,tol", [(2, 2, 12, 1e-5), (2, 2, 24, 5e-5),
+                                                (3, 6, 10, 5e-5)])
+def test_window_with_transverse_pml_matches_oracle(osg, oracle, dim, mask, steps, tol):
+    """Moving window along x1 with PML walls on the other axes, which shift with the fields on
+    every move (move_window_vpml): tiled engine against the oracle's window and walls.  As in the
+    window's own test, the cell-0 column the reference keeps one push longer and the band its
+    current reaches are left out."""
+    from test_gpu_configs import match_particles
+    nx = [64, 16] if dim == 2 else [32, 8, 8]
+    dx = [0.05] * dim
+    dt = 0.035 if dim == 2 else 0.025
+    edge = 24 if dim == 2 else 12
+    ppc = [2] * dim
+    L = nx[0] * dx[0]
+    prof_x, prof_f = [0.5 * L, 0.8 * L, 1e6], [0.0, 1.0, 1.0]
+    r = oracle.mt_new(7)
+    ix, x, u, q = oracle.load(r, "f32", dim, nx, ppc, dx, -1.0, [0.05] * 3, [0.02, 0.0, 0.0])
+    xg = (ix[:, 0].astype(np.float64) - 0.5 + x[:, 0]) * dx[0]
+    den = np.interp(xg, prof_x, prof_f, left=0.0, right=1.0).astype(np.float32)
+    keep = den > 0
+    sp0 = dict(ix=np.ascontiguousarray(ix[keep]), x=np.ascontiguousarray(x[keep]),
+               u=np.ascontiguousarray(u[keep]), q=np.ascontiguousarray(q[keep] * den[keep]),
+               rqm=-1.0)
+    g = oracle.Grid(nx, 2, dx)
+    rng = np.random.default_rng(3)
+    e0 = (rng.standard_normal(g.shape) * 0.02).astype(np.float32)
+    b0 = (rng.standard_normal(g.shape) * 0.02).astype(np.float32)
+
+    sim = osg.Simulation(nx, dx, dt, order=2, precision=32, engine=osg.ENGINE_TILED,
+                         tile=[8] * dim, pml=mask)
+    sim.set_fields(e0, b0)
+    sim.add_species(-1.0, sp0["ix"], sp0["x"], sp0["u"], sp0["q"])
+    sim.set_window(0, ppc, prof_x, prof_f)
+    sim.step(steps)
+    eg, bg, jg = sim.fields()
+    gix, gx, gu, gq = sim.species(0)
+    moves_gpu = sim.window_moves()
+    sim.close()
+
+    sp = [{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in sp0.items()}]
+    e, b, j = e0.copy(), b0.copy(), g.zeros("f32")
+    st = oracle.pml_state(g, "f32", mask, NB, dt)
+    win = oracle.Window(g, "f32", 0, ppc, prof_x, prof_f)
+    for _ in range(steps):
+        win.start_step(e, b, sp, dt, pml=(mask, NB, st))
+        oracle.step(g, "f32", e, b, j, sp, dt, window=True, pml=(mask | 8, NB, st))
+    win.start_step(e, b, sp, dt, pml=(mask, NB, st))
+    assert win.moves == moves_gpu and moves_gpu > 0
+
+    o = sp[0]
+    live = (o["ix"][:, 0] != 0) & (o["q"] != 0)
+    assert len(gq) == int(live.sum()), (len(gq), int(live.sum()))
+    ref = (o["ix"][live], o["x"][live], o["u"][live])
+    m, _ = match_particles(nx, ref, (gix, gx, gu))
+    gix, gx, gu = gix[m], gx[m], gu[m]
+    far = ref[0][:, 0] >= edge
+    errs = {"x": _nerr((gix + gx)[far], (ref[0] + ref[1])[far]), "u": _nerr(gu[far], ref[2][far])}
+    for name, a, c in (("E", eg, e), ("B", bg, b), ("J", jg, j)):
+        ia, ic = g.interior(a), g.interior(c)
+        errs[name] = _nerr(ia[..., edge - 1:, :], ic[..., edge - 1:, :])
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, (bad, errs)
