@@ -239,7 +239,9 @@ int osg_lindman_f64(int dim, const int *nx, const int *gcl, const int *gcu, int 
  * interfaces, which write the box's B next to each wall, then the E walls, update_e_vpml_{2,3}d),
  * 2 after the E step (the E interfaces, which write the box's E, then the B walls,
  * update_b_vpml_{2,3}d).  `state` holds osg_pml_state_size reals: the split-field walls and the
- * attenuation tables, set up by osg_pml_init_* (walls zero, tables from dt and dx). */
+ * attenuation tables, set up by osg_pml_init_* (walls zero, tables from dt and dx).  Flags above
+ * the axes in `mask` for osg_pml_*: bit 3 x1 moves with a window (no periodic update of the
+ * walls along it), bits 4 and 5 (2D) the diffusion correction of the x1 / x2 walls. */
 long osg_pml_state_size(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb);
 int osg_pml_init_f32(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb,
                      const double *dx, double dt, float *state);
@@ -365,6 +367,9 @@ typedef struct {
                          thermal bath; with the moving window (along x1) on the other axes,
                          whose walls then move with the fields */
     int pml_cells;    /* PML thickness in cells (0 = the reference default 8; at least 5) */
+    int pml_diffuse;  /* bit d set (d a PML axis of a 2D box): its walls take the reference's
+                         diffusion correction (vpml_diffuse: the two parts of B_z exchange 10%
+                         before every E update of the walls) */
 } osg_config;
 
 int osg_sim_create(const osg_config *cfg, osg_sim **out);

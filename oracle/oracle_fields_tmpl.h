@@ -895,6 +895,15 @@ static void FN(pml_e)(const FN(pml_desc) *Pp, R *st, const double *dx, double dt
                 for (int i1 = r0; i1 <= r1; i1++) {
                     const int ci = i1 - cofs;
                     const R c1 = PCOEF(0, k, 0, ci), c2 = PCOEF(0, k, 1, ci), c3 = PCOEF(0, k, 2, ci);
+                    if ((P.mask >> 4) & 1) {
+                        /* correction against noise from particles reaching the wall: the two
+                           parts of B_z exchange 10% (p_difrate) at the point, before its E */
+                        const R bzx = PWX(0, side, 1, 2, i1, i2);
+                        PWX(0, side, 1, 2, i1, i2) = (K(1.0) - K(0.1)) * PWX(0, side, 1, 2, i1, i2) +
+                                                     K(0.1) * PWX(0, side, 1, 3, i1, i2);
+                        PWX(0, side, 1, 3, i1, i2) = (K(1.0) - K(0.1)) * PWX(0, side, 1, 3, i1, i2) +
+                                                     K(0.1) * bzx;
+                    }
                     if (cn) {
                         const R d1 = PCOEF(1, ck, 0, cn), d2 = PCOEF(1, ck, 1, cn), d3 = PCOEF(1, ck, 2, cn);
                         PWX(0, side, 0, 0, i1, i2) = d1 * PWX(0, side, 0, 0, i1, i2) +
@@ -917,6 +926,15 @@ static void FN(pml_e)(const FN(pml_desc) *Pp, R *st, const double *dx, double dt
                 }
             }
         } else {
+            if ((P.mask >> 5) & 1)   /* the diffusion correction over the update range first */
+                for (int i2 = r0; i2 <= r1; i2++)
+                    for (int i1 = 2 - P.g1[1]; i1 <= nt + P.g2[1]; i1++) {
+                        const R bzx = PWX(1, side, 1, 2, i1, i2);
+                        PWX(1, side, 1, 2, i1, i2) = (K(1.0) - K(0.1)) * PWX(1, side, 1, 2, i1, i2) +
+                                                     K(0.1) * PWX(1, side, 1, 3, i1, i2);
+                        PWX(1, side, 1, 3, i1, i2) = (K(1.0) - K(0.1)) * PWX(1, side, 1, 3, i1, i2) +
+                                                     K(0.1) * bzx;
+                    }
             /* the wall's lowest row: Y and ZX by the plain Yee update */
             for (int i1 = 2 - P.g1[1]; i1 <= nt + P.g2[1]; i1++) {
                 const int i2 = lo;

@@ -77,7 +77,8 @@ class Config(C.Structure):
                 ("open_fields", I),
                 ("thermal", I), ("seed", C.c_uint), ("uth_bnd", D * 3), ("ufl_bnd", D * 3),
                 ("thermal_type", I), ("pmc", I), ("emf_smooth_type", I),
-                ("emf_smooth_order", I), ("pml", I), ("pml_cells", I)]
+                ("emf_smooth_order", I), ("pml", I), ("pml_cells", I),
+                ("pml_diffuse", I)]
 
 
 def _declare(lb):
@@ -468,7 +469,7 @@ class Simulation:
                  smooth_type=SMOOTH_NONE, smooth_order=0, walls=0, open_fields=0, thermal=0,
                  uth_bnd=(0.0, 0.0, 0.0), ufl_bnd=(0.0, 0.0, 0.0), seed=0, pmc=0,
                  thermal_type=0, emf_smooth_type=SMOOTH_NONE, emf_smooth_order=0, pml=0,
-                 pml_cells=0):
+                 pml_cells=0, pml_diffuse=0):
         self.dim = len(nx)
         self.nx = list(nx)
         self.order = order
@@ -499,6 +500,7 @@ class Simulation:
         cfg.emf_smooth_order = emf_smooth_order
         cfg.pml = pml
         cfg.pml_cells = pml_cells
+        cfg.pml_diffuse = pml_diffuse
         cfg.seed = seed
         for c in range(3):
             cfg.uth_bnd[c] = uth_bnd[c]

@@ -392,9 +392,11 @@ static int lindman_host(int dim, const int *nx, const int *gcl, const int *gcu, 
 
 static int pml_check(int dim, const int *nx, const int *gcl, const int *gcu, int mask, int nb)
 {
-    OSG_CHECK(dim >= 2 && dim <= 3 && nx && gcl && gcu && mask > 0 && mask < (1 << dim) &&
-                  nb >= 5,
-              OSG_ERR_ARG, "bad PML arguments (2D/3D, a non-empty axis mask, nb >= 5)");
+    const int axes = mask & 7;
+    OSG_CHECK(dim >= 2 && dim <= 3 && nx && gcl && gcu && axes > 0 && axes < (1 << dim) &&
+                  nb >= 5 && (mask & ~63) == 0 && (dim == 2 || (mask >> 4) == 0),
+              OSG_ERR_ARG, "bad PML arguments (2D/3D, a non-empty axis mask and its flags, "
+                           "nb >= 5)");
     for (int d = 0; d < dim; d++)
         OSG_CHECK(nx[d] >= 6 && gcl[d] >= 1 && gcu[d] >= 2, OSG_ERR_ARG,
                   "PML walls need nx >= 6, gcl >= 1 and gcu >= 2 on every axis");

@@ -882,6 +882,32 @@ __global__ void k_pml_b(PmlDesc P, T *__restrict__ st, T dtdx, int a)
     }
 }
 
+// the diffusion correction of the walls of axis a (vpml_diffuse, 2D): over the points of the
+// E update range the two parts of B_z exchange p_difrate = 0.1 (update_e_x1_2d :1001-1006,
+// update_e_x2_2d :1399-1408), before the E walls advance (every point the reference's loop
+// reads after diffusing it is diffused here first; the others are outside the range)
+template <typename T>
+__global__ void k_pml_diffuse(PmlDesc P, T *__restrict__ st, int a)
+{
+    const int nt = P.nx[1 - a], nte = P.nte[a];
+    const long n = 2L * P.nb * nte;
+    OSG_GRID_LOOP(m, n)
+    {
+        const int side = (int)(m / ((long)P.nb * nte));
+        const int rem = (int)(m % ((long)P.nb * nte));
+        const int lo = pml_lo(P, a, side), hi = lo + P.nb - 1;
+        const int iw = lo + rem % P.nb, it = 1 - P.g1[a] + rem / P.nb;
+        if (it < 2 - P.g1[a] || it > nt + P.g2[a]) continue;
+        const int r0 = lo + 1, r1 = side == 0 ? hi - 1 : hi;
+        if (iw < r0 || iw > r1) continue;
+        const int i1 = a == 0 ? iw : it, i2 = a == 0 ? it : iw;
+        T &zx = pml_at(P, st, a, side, 1, 2, i1, i2), &zy = pml_at(P, st, a, side, 1, 3, i1, i2);
+        const T bzx = zx, rm = T(1) - T(0.1);
+        zx = rm * zx + T(0.1) * zy;
+        zy = rm * zy + T(0.1) * bzx;
+    }
+}
+
 // the walls' periodic update along a periodic t (update_periodic_wall, source/vdf/
 // os-wall-comm.f90:182-344): guard points from the opposite interior points, all components,
 // the whole wall-normal range
@@ -977,6 +1003,8 @@ void pml_phase(const GridDesc &g, int mask, int nb, int what, T *e, T *b, T *pml
         if (!((mask >> a) & 1)) continue;
         const T dtdx = (T)(dt / dx[1 - a]);
         const long n = 2L * nb * P.nte[a];
+        if (what == 1 && ((mask >> (4 + a)) & 1))   // bits 4, 5: diffusion on the x1, x2 walls
+            k_pml_diffuse<T><<<blocks_for(n, 256), 256, 0, st>>>(P, pml, a);
         if (what == 1) k_pml_e<T><<<blocks_for(n, 256), 256, 0, st>>>(P, pml, dtdx, a);
         else k_pml_b<T><<<blocks_for(n, 256), 256, 0, st>>>(P, pml, dtdx, a);
     }

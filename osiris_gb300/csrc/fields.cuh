@@ -76,7 +76,8 @@ void pml_phase(const GridDesc &g, int mask, int nb, int what, T *e, T *b, T *pml
 template <typename T>
 void pml_guards(const GridDesc &g, T *e, T *b, int mask, int nb, T *pml, cudaStream_t st);
 // (bit 3 of `mask` in pml_phase / pml_guards: x1 is the axis of a moving window, so neither the
-// walls nor the box take a periodic update along it)
+// walls nor the box take a periodic update along it; bits 4 and 5 in 2D: the x1 / x2 walls take
+// the diffusion correction before their E update)
 // window move: the PML walls of the axes other than x1 shift one cell down along x1, the last
 // plane zero; tmp holds pml_shift_scratch reals
 long pml_shift_scratch(const GridDesc &g, int mask, int nb);

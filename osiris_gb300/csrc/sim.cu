@@ -65,7 +65,8 @@ struct osg_sim {
     unsigned long long *d_step = nullptr;   // step counter of the thermal-bath random stream
     int open_axis = -1;          // Lindman open boundaries at both edges of this axis
     void *lind = nullptr;        // their state (lindman_state_size reals)
-    int pml_mask = 0;            // PML walls at both edges of these axes (2D)
+    int pml_mask = 0;            // PML walls at both edges of these axes
+    int pml_flags = 0;           // bits 4, 5: the x1 / x2 walls' diffusion correction (2D)
     int pml_nb = 0;              // their thickness in cells
     void *pml = nullptr;         // their state (pml_state_size reals)
     void *pml_tmp = nullptr;     // scratch of the walls' shift with the moving window
@@ -376,10 +377,10 @@ static int enqueue_step(osg_sim *s, int parity, bool with_sort, bool shift, Phas
     }
     if (pe) OSG_CUDA(cudaEventRecord(pe->ev[4], st));
     yee_advance<T>(s->g, (T *)s->e, (T *)s->b, (const T *)s->j, c.dx, c.dt, st, walls, c.order,
-                   oax, (T *)s->lind, c.pmc, pml, s->pml_nb, (T *)s->pml);
+                   oax, (T *)s->lind, c.pmc, pml | s->pml_flags, s->pml_nb, (T *)s->pml);
     launches += 3 + (walls ? 6 * __builtin_popcount(walls) : 0) + (oax >= 0 ? 3 : 0) +
                 (!pml ? 0
-                      : 2 * (2 * __builtin_popcount(pml) +
+                      : __builtin_popcount(s->pml_flags) + 2 * (2 * __builtin_popcount(pml) +
                              (c.dim == 2 ? (pml == 3) : ((pml & 1) && (pml & 2)) +
                                                             ((pml & 1) && (pml & 4)) +
                                                             ((pml & 2) && (pml & 4)))));
@@ -547,6 +548,9 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
                            "smoothing nor a thermal bath");
     OSG_CHECK(cfg->pml_cells == 0 || cfg->pml_cells >= 5, OSG_ERR_ARG,
               "pml_cells: 0 (8) or at least 5");
+    OSG_CHECK(cfg->pml_diffuse >= 0 && (cfg->pml_diffuse & ~cfg->pml) == 0 &&
+                  (cfg->pml_diffuse == 0 || cfg->dim == 2),
+              OSG_ERR_ARG, "pml_diffuse: a bit mask of PML axes of a 2D box");
     if (cfg->pml)
         for (int d = 0; d < cfg->dim; d++)
             OSG_CHECK(cfg->nx[d] >= 6, OSG_ERR_ARG, "PML walls need at least 6 cells per axis");
@@ -651,6 +655,7 @@ int osg_sim_create(const osg_config *cfg, osg_sim **out)
         // the walls start at zero (new_wall, source/vdf/os-wall.f90:198-210); the attenuation
         // tables are computed on the host in double and stored in the field precision
         s->pml_mask = cfg->pml;
+        s->pml_flags = (cfg->pml_diffuse & 3) << 4;
         s->pml_nb = cfg->pml_cells > 0 ? cfg->pml_cells : 8;
         const long n = pml_state_size(s->g, s->pml_mask, s->pml_nb);
         s->pml = dalloc<char>((size_t)s->esz * n, &rc);

@@ -15,7 +15,8 @@ STRUCTS = {
                               "n_sort", "capacity", "pusher", "iter_tol", "smooth_type",
                               "smooth_order", "walls", "open_fields", "thermal", "seed",
                               "uth_bnd", "ufl_bnd", "thermal_type", "pmc", "emf_smooth_type",
-                              "emf_smooth_order", "pml", "pml_cells"]),
+                              "emf_smooth_order", "pml", "pml_cells",
+                              "pml_diffuse"]),
     "osg_batch_config": ("BatchConfig", ["dim", "order", "dt", "tile", "threads", "capacity"]),
     "osg_zpulse": ("Zpulse", ["omega0", "a0", "pol", "lon_x0", "lon_duration", "lon_range",
                               "per_w0", "per_focus", "per_center"]),

@@ -404,3 +404,39 @@ def test_window_with_transverse_pml_matches_oracle(osg, oracle, dim, mask, steps
         errs[name] = _nerr(ia[..., edge - 1:, :], ic[..., edge - 1:, :])
     bad = {k: v for k, v in errs.items() if not v <= tol}
     assert not bad, (bad, errs)
+
+
+@pytest.mark.parametrize("mask", [1, 2, 3])
+@pytest.mark.parametrize("engine,prec,tol", [("plain", 64, 1e-12), ("tiled", 32, 5e-5)])
+def test_pml_diffusion_matches_oracle(osg, oracle, engine, prec, tol, mask):
+    """The walls' diffusion correction (pml_diffuse, 2D) against the oracle, 10 steps."""
+    nx = [24, 16]
+    p, g, dx, dt, species, e, b = _setup(oracle, prec, 2, 2, nx, [2, 2], 31, uth=0.6, ufl=0.1)
+    sim = osg.Simulation(nx, dx, dt, order=2, precision=prec,
+                         engine=osg.ENGINE_PLAIN if engine == "plain" else osg.ENGINE_TILED,
+                         tile=[8, 8] if engine == "tiled" else None, pml=mask, pml_diffuse=mask)
+    sim.set_fields(e, b)
+    for s_ in species:
+        sim.add_species(s_["rqm"], s_["ix"], s_["x"], s_["u"], s_["q"])
+    sim.step(10)
+    eg, bg, jg = sim.fields()
+    sim.close()
+    ora = [{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s_.items()}
+           for s_ in species]
+    eo, bo, jo = e.copy(), b.copy(), g.zeros(p)
+    st = oracle.pml_state(g, p, mask, NB, dt)
+    for _ in range(10):
+        oracle.step(g, p, eo, bo, jo, ora, dt, pml=(mask | (mask << 4), NB, st))
+    errs = {"E": _nerr(eg, eo), "B": _nerr(bg, bo), "J": _nerr(jg, jo)}
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, (bad, errs)
+    # without the correction the fields differ
+    sim = osg.Simulation(nx, dx, dt, order=2, precision=prec,
+                         engine=osg.ENGINE_PLAIN if engine == "plain" else osg.ENGINE_TILED,
+                         tile=[8, 8] if engine == "tiled" else None, pml=mask)
+    sim.set_fields(e, b)
+    for s_ in species:
+        sim.add_species(s_["rqm"], s_["ix"], s_["x"], s_["u"], s_["q"])
+    sim.step(10)
+    assert _nerr(sim.fields()[1], bg) > 1e-8
+    sim.close()
