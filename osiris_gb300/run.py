@@ -71,16 +71,17 @@ LWFA = dict(nx=[1024, 128, 128], dx=[0.2, 0.6, 0.6], dt=0.18, order=3, ppc=[2, 1
             x0=130.0)
 
 
-def build_lwfa(nx=None, tile=None):
+def build_lwfa(nx=None, tile=None, pml=False):
     """The laser-wakefield workload: seeded lattice load of the plasma already inside the box
-    (density from the profile), the pulse launched into E/B, the window set."""
+    (density from the profile), the pulse launched into E/B, the window set.  pml=True: PML
+    walls on the transverse axes (moving with the window) instead of periodic ones."""
     c = LWFA
     nx = nx or c["nx"]
     dx = c["dx"]
     ramp_end = c["ramp_start"] + c["ramp_cells"] * dx[0]
     px, pf = [c["ramp_start"], ramp_end, 1e9], [0.0, c["n0"], c["n0"]]
     sim = osg.Simulation(nx, dx, c["dt"], order=c["order"], precision=32,
-                         engine=osg.ENGINE_TILED, tile=tile)
+                         engine=osg.ENGINE_TILED, tile=tile, pml=6 if pml else 0)
     gl, gu = osg.GUARD[c["order"]]
     shape = tuple(reversed([n + gl + gu for n in nx])) + (3,)
     e, b = np.zeros(shape, np.float32), np.zeros(shape, np.float32)
@@ -236,6 +237,8 @@ def main():
                          "engine after the same steps from the same load")
     ap.add_argument("--pageable", action="store_true",
                     help="--dropin: particles in pageable host memory instead of pinned")
+    ap.add_argument("--pml", action="store_true",
+                    help="--config lwfa: PML walls on the transverse axes (moving with the window)")
     ap.add_argument("--dropin", action="store_true",
                     help="2D configurations: time the host-array drop-in flow instead "
                          "(osg_vadvance_deposit_f32 per species, guard updates and Yee on "
@@ -246,7 +249,7 @@ def main():
         return
     if args.config == "lwfa":
         t0 = time.time()
-        sim, n0 = build_lwfa(args.nx, args.tile)
+        sim, n0 = build_lwfa(args.nx, args.tile, pml=args.pml)
         t_load = time.time() - t0
         sim.step(args.warmup)
         ms = sim.time_steps(args.steps)
