@@ -228,8 +228,11 @@ static int push_host(int dim, int order, int *ix, T *x, T *u, T *q, int i0, int 
         // chunk k + 1, the push of chunk k and the copies out of chunk k - 1 run at once, and
         // neither copy direction waits for the other (per-particle results do not depend on the
         // chunking; the current and energy sums are atomic either way).
+        // chunk starts on a multiple of 4096 particles, so that every array's copy starts on a
+        // 16 KB boundary of the (aligned) host array: copies of unaligned ranges measured ~20%
+        // slower over the host link
         const long nck = np > (2L << 20) ? push_chunks() : 1;
-        const long chunk = (np + nck - 1) / nck;
+        const long chunk = nck == 1 ? np : ((np + nck - 1) / nck + 4095) & ~4095L;
         for (long c0 = 0, k = 0; c0 < np; c0 += chunk, k++) {
             const long n = std::min(chunk, np - c0), h = o + c0;
             int *cix = (int *)d_ix + dim * c0;
