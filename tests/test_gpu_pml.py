@@ -221,12 +221,13 @@ def test_pml_refuses_what_it_is_not_built_for(osg, kw):
 
 
 @pytest.mark.parametrize("mask", [1, 2, 4, 3, 5, 6, 7])
+@pytest.mark.parametrize("order", [2, 3])
 @pytest.mark.parametrize("engine,prec,tol", [("plain", 64, 1e-12), ("tiled", 32, 5e-5)])
-def test_pml_3d_matches_oracle(osg, oracle, engine, prec, tol, mask):
+def test_pml_3d_matches_oracle(osg, oracle, engine, prec, tol, order, mask):
     nx = [12, 8, 8]
-    p, g, dx, dt, species, e, b = _setup(oracle, prec, 3, 2, nx, [2, 2, 2], 21, uth=0.6,
+    p, g, dx, dt, species, e, b = _setup(oracle, prec, 3, order, nx, [2, 2, 2], 21, uth=0.6,
                                          ufl=0.1)
-    sim = osg.Simulation(nx, dx, dt, order=2, precision=prec,
+    sim = osg.Simulation(nx, dx, dt, order=order, precision=prec,
                          engine=osg.ENGINE_PLAIN if engine == "plain" else osg.ENGINE_TILED,
                          tile=[4, 4, 4] if engine == "tiled" else None, pml=mask)
     sim.set_fields(e, b)
