@@ -346,7 +346,16 @@ def pml(dim, nx, gcl, gcu, mask, nb, what, e, b, state, dx, dt):
     if e.size != npts or b.size != npts:
         raise ValueError(f"e and b must hold {npts} reals (3 x the guard-celled grid)")
     _need(state, dt_, "state")
-    _check(getattr(lib(), f"osg_pml_{s}")(dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)),
+    lb = lib()
+    lb.osg_pml_state_size.argtypes = [I, P, P, P, I, I]
+    lb.osg_pml_state_size.restype = C.c_long
+    need = lb.osg_pml_state_size(dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)), int(mask) & 7,
+                                 int(nb))
+    if need < 0:
+        raise OsirisGB300Error(-1, lb.osg_last_error().decode(errors="replace"))
+    if state.size < need:
+        raise ValueError(f"state holds {state.size} reals, needs {need}")
+    _check(getattr(lb, f"osg_pml_{s}")(dim, _p(_i32(nx)), _p(_i32(gcl)), _p(_i32(gcu)),
                                           int(mask), int(nb), int(what), _p(e), _p(b), _p(state),
                                           _p(_f64(list(dx) + [0.0] * 3)), float(dt)))
 

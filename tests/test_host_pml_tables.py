@@ -39,3 +39,12 @@ def test_pml_state_refuses_bad_arguments(osg, dim, mask, nb):
     nx, gl, gu = [12] * max(dim, 1), [2] * max(dim, 1), [3] * max(dim, 1)
     with pytest.raises(osg.OsirisGB300Error):
         osg.pml_state(dim, nx, gl, gu, mask, nb, [0.1] * 3, 0.03, np.float64)
+
+
+def test_pml_phase_refuses_a_short_state(osg):
+    nx, gl, gu = [12, 10], [2, 2], [3, 3]
+    st = osg.pml_state(2, nx, gl, gu, 1, 8, [0.1, 0.1], 0.03, np.float64)
+    shape = (10 + 5, 12 + 5, 3)
+    e, b = np.zeros(shape), np.zeros(shape)
+    with pytest.raises(ValueError):
+        osg.pml(2, nx, gl, gu, 1, 8, 1, e, b, st[:-1].copy(), [0.1, 0.1], 0.03)
