@@ -17,6 +17,8 @@ one axis of a 2D box), on the CPU:
   step, which the walls damp only along the other axis: a plane pulse along the PML axis then
   leaves about 2% of its energy for a while, below 1e-3 after 400 steps, the same for either
   axis (without it: 1e-21);
+* a window move shifts every wall of an axis other than x1 one cell down along x1, its last
+  plane zero, and leaves the tables alone;
 * the state is four split-field walls per PML axis plus the tables.
 """
 import numpy as np
@@ -186,3 +188,28 @@ def test_diffusion_correction_keeps_the_absorption(axis):
             left.append(_energy(g, e, b) / w0)
     assert np.isfinite(e).all() and np.isfinite(b).all()
     assert 1e-3 < left[0] < 0.05 and left[1] < 1e-3, left
+
+
+@pytest.mark.parametrize("dim,mask", [(2, 2), (3, 2), (3, 4), (3, 6)])
+def test_window_shift_moves_the_walls_along_x1(dim, mask):
+    """ora_pml_shift_x (a window move): every wall of an axis other than x1 shifts one x1 cell
+    down, its last x1 plane becoming zero (move_window_wall)."""
+    nx = [12, 10] if dim == 2 else [12, 10, 9]
+    g = po.Grid(nx, 2, [0.1] * dim)
+    st = po.pml_state(g, "f64", mask, NB, 0.03)
+    ntab = 12 * dim * NB
+    rng = np.random.default_rng(2)
+    st[:len(st) - ntab] = rng.standard_normal(len(st) - ntab)
+    before = st.copy()
+    nx_, gl, gu = g.args()
+    po.lib().ora_pml_shift_x_f64(dim, po._p(nx_), po._p(gl), po._p(gu), mask, NB, po._p(st))
+    # the walls' x1 extent: nx + max(gcl, 2) + max(gcu, 2) points; a wall is lines of one x1
+    # point (4 nb reals in 2D, 6 nb in 3D) repeated along x1, per point of the remaining axis
+    n1 = nx[0] + max(g.gcl[0], 2) + max(g.gcu[0], 2)
+    line = (4 if dim == 2 else 6) * NB
+    walls = st[:len(st) - ntab]
+    assert np.array_equal(st[len(st) - ntab:], before[len(st) - ntab:])
+    w = walls.reshape(-1, n1, line)
+    b = before[:len(st) - ntab].reshape(-1, n1, line)
+    assert np.array_equal(w[:, :-1], b[:, 1:])
+    assert not w[:, -1].any()
